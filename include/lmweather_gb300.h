@@ -1,0 +1,148 @@
+/* lmweather-gb300: C ABI of the GB300 (sm_103a) shallow-water engine.
+ *
+ * The entry points replace the numerical core that lmweather's wx.* operator surface binds
+ * (lmweather cpp/main.cpp:62-494 calls lmweather::Sphere, cpp/sphere.hpp:27-121, and lmweather::Plane,
+ * cpp/plane.hpp:20-68). Each declaration names the reference member it replaces. Plain pointers and sizes
+ * only; state lives on the GPU, owned by the handle, with one CUDA stream per handle.
+ *
+ * Errors: every function returns LMW_OK (0) or an error class that mirrors the reference's exceptions:
+ * LMW_INVALID_ARGUMENT (std::invalid_argument), LMW_RUNTIME_ERROR (std::runtime_error) or LMW_DEVICE_ERROR
+ * (a CUDA failure). lmw_last_error() returns the calling thread's last message, using the reference's texts.
+ *
+ * Layouts (host buffers, the reference's own): grids are row-major [nlat][nlon], latitudes south to north;
+ * spectra are (T+1)^2 complex values per field at index m*(T+1)+n (n >= m), stored as interleaved
+ * (re, im) doubles; plane h and u are [ny][nx], v is [ny+1][nx] with rows 0 and ny on the walls.
+ */
+#ifndef LMWEATHER_GB300_H
+#define LMWEATHER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { LMW_OK = 0, LMW_INVALID_ARGUMENT = 1, LMW_RUNTIME_ERROR = 2, LMW_DEVICE_ERROR = 3 };
+/* precision modes of the sphere engine */
+enum { LMW_FP64 = 0, LMW_FP32 = 1, LMW_SPLIT_BF16 = 2 };
+/* grid fields for lmw_sphere_grid */
+enum { LMW_GRID_HEIGHT = 0, LMW_GRID_U = 1, LMW_GRID_V = 2, LMW_GRID_VORTICITY = 3 };
+
+typedef struct lmw_sphere lmw_sphere;
+typedef struct lmw_plane lmw_plane;
+
+/* message of the calling thread's last failed call ("" after success) */
+const char *lmw_last_error(void);
+/* "lmweather-gb300 <version>" */
+const char *lmw_version(void);
+/* number of this library's kernel launches issued by the calling thread so far */
+uint64_t lmw_launch_count(void);
+
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (the roofline of the FP64 paths) */
+int lmw_fp64_peak(double *tflops);
+
+/* ---------------------------------------------------------------------------------------- sphere */
+
+/* Sphere::Sphere(int truncation, const SphereParams &) (cpp/sphere.hpp:29, cpp/sphere.cpp:75-103).
+ * Truncation 4..170 as the reference (invalid_argument "truncation must be between 4 and 170"). */
+int lmw_sphere_create(int truncation, double radius, double omega, double gravity, double diffusion, lmw_sphere **out);
+/* Engine options beyond the reference: precision mode (LMW_FP64 .. LMW_SPLIT_BF16), an ensemble of `members`
+ * states sharing the truncation (stepped together), and a truncation cap up to 341. */
+int lmw_sphere_create_ex(int truncation, double radius, double omega, double gravity, double diffusion, int precision,
+                         int members, int max_truncation, lmw_sphere **out);
+int lmw_sphere_destroy(lmw_sphere *s);
+/* Sphere::truncation/nlat/nlon (cpp/sphere.hpp:30-32) and the member count */
+int lmw_sphere_dims(const lmw_sphere *s, int *truncation, int *nlat, int *nlon, int *members);
+/* Sphere::gauss_mu / gauss_weights (cpp/sphere.hpp:93-94): nlat values each */
+int lmw_sphere_gauss(const lmw_sphere *s, double *mu, double *w);
+/* Sphere::time (cpp/sphere.hpp:34) of one member */
+int lmw_sphere_time(const lmw_sphere *s, int member, double *out);
+/* Sphere::set_state_grid (cpp/sphere.hpp:39, cpp/sphere.cpp:217-234); n = nlat*nlon values per grid */
+int lmw_sphere_set_state_grid(lmw_sphere *s, int member, const double *h, const double *u, const double *v, size_t n);
+/* Sphere::set_axis_tilt (cpp/sphere.hpp:40, cpp/sphere.cpp:111-118) */
+int lmw_sphere_set_axis_tilt(lmw_sphere *s, int member, double alpha);
+/* per-member rotation rate (ensembles scale Omega per member); untilted axis */
+int lmw_sphere_set_omega(lmw_sphere *s, int member, double omega);
+/* Sphere::set_diffusion (cpp/sphere.hpp:41) */
+int lmw_sphere_set_diffusion(lmw_sphere *s, double nu4);
+/* Sphere::set_orography_grid (cpp/sphere.hpp:47, cpp/sphere.cpp:105-109) */
+int lmw_sphere_set_orography_grid(lmw_sphere *s, int member, const double *hs, size_t n);
+/* Sphere::add_mode (cpp/sphere.hpp:43, cpp/sphere.cpp:301-311) */
+int lmw_sphere_add_mode(lmw_sphere *s, int member, int n, int m, double amplitude, double mean_depth);
+/* Sphere::perturb (cpp/sphere.hpp:44, cpp/sphere.cpp:313-336) */
+int lmw_sphere_perturb(lmw_sphere *s, int member, double amplitude, uint64_t seed, int max_wave);
+/* Sphere::mark_reference (cpp/sphere.hpp:42, cpp/sphere.cpp:236-239) */
+int lmw_sphere_mark_reference(lmw_sphere *s, int member);
+/* Seeded balanced turbulence (no reference counterpart: the benchmark initialiser): complex-Gaussian vorticity
+ * for 1 <= n <= nforce with an n^-3 kinetic-energy spectrum scaled to max_wind, zero divergence and
+ * h = mean_height + f psi / g, entered through set_state_grid */
+int lmw_sphere_turbulence(lmw_sphere *s, int member, uint64_t seed, double mean_height, double max_wind, int nforce);
+/* spectral state in the reference layout (the private zeta_, delta_, phi_ of cpp/sphere.hpp:111); any pointer may be NULL */
+int lmw_sphere_get_state(lmw_sphere *s, int member, double *zeta, double *delta, double *phi);
+int lmw_sphere_set_state(lmw_sphere *s, int member, const double *zeta, const double *delta, const double *phi, double time);
+/* Sphere::step (cpp/sphere.hpp:67, cpp/sphere.cpp:407-436): one RK4 step of every member */
+int lmw_sphere_step(lmw_sphere *s, double dt);
+/* Sphere::run (cpp/sphere.hpp:68, cpp/sphere.cpp:457-484): equal steps, dt <= 0 picks a stable one, the
+ * reference's stability and finiteness guards every 64 steps (over every member) */
+int lmw_sphere_run(lmw_sphere *s, double seconds, double dt);
+/* Sphere::stable_dt (cpp/sphere.hpp:69, cpp/sphere.cpp:438-447) */
+int lmw_sphere_stable_dt(lmw_sphere *s, int member, double safety, double *out);
+/* Sphere diagnostics (cpp/sphere.cpp:510-590): out[8] = mean_height, kinetic_energy, potential_energy, energy,
+ * potential_enstrophy, max_wind, height_error_l2, height_error_linf */
+int lmw_sphere_diagnostics(lmw_sphere *s, int member, double *out);
+/* Sphere::grid_height/grid_u/grid_v/grid_vorticity (cpp/sphere.hpp:88-91, cpp/sphere.cpp:486-508) */
+int lmw_sphere_grid(lmw_sphere *s, int member, int which, double *out, size_t n);
+/* Sphere::spectrum (cpp/sphere.hpp:63, cpp/sphere.cpp:536-551): T+1 values each */
+int lmw_sphere_spectrum(lmw_sphere *s, int member, double *ke, double *pe);
+
+/* the handle's CUDA stream (a cudaStream_t), for callers that order their own work or events after it */
+int lmw_sphere_stream(const lmw_sphere *s, void **stream);
+/* average device time (ms) per launch of each RK4-stage kernel class over `reps` launches (CUDA events on the
+ * handle's stream): ms[0] Legendre synthesis, ms[1] FFTs + grid products, ms[2] Legendre analysis + RK4 update.
+ * The spectral state is left unchanged. No reference counterpart (measurement hook). */
+int lmw_sphere_kernel_times(lmw_sphere *s, double dt, int reps, double *ms);
+
+/* ---------------------------------------------------------------------------------------- plane */
+
+/* Plane::Plane(const PlaneParams &) (cpp/plane.hpp:22, cpp/plane.cpp:20-25) */
+int lmw_plane_create(int nx, int ny, double lx, double ly, double gravity, double depth, double f0, double beta,
+                     double viscosity, double drag, int linear, lmw_plane **out);
+int lmw_plane_destroy(lmw_plane *p);
+/* Plane::params() setters used by the wx builders (cpp/main.cpp:389-408): gravity, depth, f0, beta,
+ * viscosity, drag, linear */
+int lmw_plane_set_params(lmw_plane *p, double gravity, double depth, double f0, double beta, double viscosity, double drag,
+                         int linear);
+/* Plane::reset (cpp/plane.hpp:40, cpp/plane.cpp:27-32) */
+int lmw_plane_reset(lmw_plane *p);
+/* Plane::set_h_from_grid / set_u_from_grid / set_v_from_grid (cpp/plane.hpp:62-64, cpp/plane.cpp:312-318) */
+int lmw_plane_set_h(lmw_plane *p, const double *h, size_t n);
+int lmw_plane_set_u(lmw_plane *p, const double *u, size_t n);
+int lmw_plane_set_v(lmw_plane *p, const double *v, size_t n);
+/* Plane::h/u/v accessors (cpp/plane.hpp:33-38) for the whole fields; any pointer may be NULL */
+int lmw_plane_get(lmw_plane *p, double *h, double *u, double *v);
+/* Plane::perturb (cpp/plane.hpp:41, cpp/plane.cpp:34-57) */
+int lmw_plane_perturb(lmw_plane *p, double amplitude, uint64_t seed);
+/* Zonal jet in geostrophic balance plus white height noise (no reference counterpart: the benchmark
+ * initialiser): u = u0 sech^2((y - ly/2)/width), h integrated from g dh/dy = -f u, noise of noise_rms */
+int lmw_plane_jet(lmw_plane *p, double u0, double width, double noise_rms, uint64_t seed);
+/* Plane::step (cpp/plane.hpp:42, cpp/plane.cpp:143-158) */
+int lmw_plane_step(lmw_plane *p, double dt);
+/* Plane::run (cpp/plane.hpp:43, cpp/plane.cpp:160-189) */
+int lmw_plane_run(lmw_plane *p, double seconds, double dt);
+/* Plane::stable_dt (cpp/plane.hpp:44, cpp/plane.cpp:131-141) */
+int lmw_plane_stable_dt(lmw_plane *p, double safety, double *out);
+/* Plane::time (cpp/plane.hpp:25) */
+int lmw_plane_time(const lmw_plane *p, double *out);
+/* Plane diagnostics (cpp/plane.cpp:191-243): out[4] = mean_depth, energy, max_speed, pv_anomaly_rms */
+int lmw_plane_diagnostics(lmw_plane *p, double *out);
+/* the handle's CUDA stream (a cudaStream_t) */
+int lmw_plane_stream(const lmw_plane *p, void **stream);
+/* average device time (ms) of one RK4-stage kernel launch over `reps` launches; the state is left unchanged.
+ * No reference counterpart (measurement hook). */
+int lmw_plane_kernel_time(lmw_plane *p, double dt, int reps, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,400 @@
+"""lmweather-gb300: GB300-native (sm_103a) rotating shallow-water time stepping.
+
+Python mirror of lmweather's numerical-core interface (lmweather::Sphere, cpp/sphere.hpp:27-121, and
+lmweather::Plane, cpp/plane.hpp:20-68) over the engine's C ABI (include/lmweather_gb300.h). Method names and
+argument meanings follow the reference; its std::invalid_argument surfaces as ValueError and its
+std::runtime_error as RuntimeError, with the reference's message texts. All state lives on the GPU; there is no
+CPU fallback: without the compiled library (lmweather_gb300/_lib/liblmw_gb300.so) every constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = ["Sphere", "Plane", "DeviceError", "load_library", "library_path", "launch_count", "FP64", "FP32", "SPLIT_BF16"]
+
+FP64, FP32, SPLIT_BF16 = 0, 1, 2
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def library_path() -> str:
+    return os.path.join(_HERE, "_lib", "liblmw_gb300.so")
+
+
+class DeviceError(RuntimeError):
+    """A CUDA failure inside the engine (status LMW_DEVICE_ERROR)."""
+
+
+_D, _I, _P, _SZ, _U64 = C.c_double, C.c_int, C.c_void_p, C.c_size_t, C.c_uint64
+_DP = C.POINTER(C.c_double)
+_PP = C.POINTER(C.c_void_p)
+_IP = C.POINTER(C.c_int)
+
+_SIGS = {
+    "lmw_last_error": (C.c_char_p, []),
+    "lmw_version": (C.c_char_p, []),
+    "lmw_launch_count": (C.c_uint64, []),
+    "lmw_sphere_create": (_I, [_I, _D, _D, _D, _D, _PP]),
+    "lmw_sphere_create_ex": (_I, [_I, _D, _D, _D, _D, _I, _I, _I, _PP]),
+    "lmw_sphere_destroy": (_I, [_P]),
+    "lmw_sphere_dims": (_I, [_P, _IP, _IP, _IP, _IP]),
+    "lmw_sphere_gauss": (_I, [_P, _DP, _DP]),
+    "lmw_sphere_time": (_I, [_P, _I, _DP]),
+    "lmw_sphere_set_state_grid": (_I, [_P, _I, _DP, _DP, _DP, _SZ]),
+    "lmw_sphere_set_axis_tilt": (_I, [_P, _I, _D]),
+    "lmw_sphere_set_omega": (_I, [_P, _I, _D]),
+    "lmw_sphere_set_diffusion": (_I, [_P, _D]),
+    "lmw_sphere_set_orography_grid": (_I, [_P, _I, _DP, _SZ]),
+    "lmw_sphere_add_mode": (_I, [_P, _I, _I, _I, _D, _D]),
+    "lmw_sphere_perturb": (_I, [_P, _I, _D, _U64, _I]),
+    "lmw_sphere_mark_reference": (_I, [_P, _I]),
+    "lmw_sphere_turbulence": (_I, [_P, _I, _U64, _D, _D, _I]),
+    "lmw_sphere_get_state": (_I, [_P, _I, _DP, _DP, _DP]),
+    "lmw_sphere_set_state": (_I, [_P, _I, _DP, _DP, _DP, _D]),
+    "lmw_sphere_step": (_I, [_P, _D]),
+    "lmw_sphere_run": (_I, [_P, _D, _D]),
+    "lmw_sphere_stable_dt": (_I, [_P, _I, _D, _DP]),
+    "lmw_sphere_diagnostics": (_I, [_P, _I, _DP]),
+    "lmw_sphere_grid": (_I, [_P, _I, _I, _DP, _SZ]),
+    "lmw_sphere_spectrum": (_I, [_P, _I, _DP, _DP]),
+    "lmw_plane_create": (_I, [_I, _I, _D, _D, _D, _D, _D, _D, _D, _D, _I, _PP]),
+    "lmw_plane_destroy": (_I, [_P]),
+    "lmw_plane_set_params": (_I, [_P, _D, _D, _D, _D, _D, _D, _I]),
+    "lmw_plane_reset": (_I, [_P]),
+    "lmw_plane_set_h": (_I, [_P, _DP, _SZ]),
+    "lmw_plane_set_u": (_I, [_P, _DP, _SZ]),
+    "lmw_plane_set_v": (_I, [_P, _DP, _SZ]),
+    "lmw_plane_get": (_I, [_P, _DP, _DP, _DP]),
+    "lmw_plane_perturb": (_I, [_P, _D, _U64]),
+    "lmw_plane_jet": (_I, [_P, _D, _D, _D, _U64]),
+    "lmw_plane_step": (_I, [_P, _D]),
+    "lmw_plane_run": (_I, [_P, _D, _D]),
+    "lmw_plane_stable_dt": (_I, [_P, _D, _DP]),
+    "lmw_plane_time": (_I, [_P, _DP]),
+    "lmw_plane_diagnostics": (_I, [_P, _DP]),
+}
+
+
+def load_library() -> C.CDLL:
+    """Load the engine library (built by lmweather_gb300.build). Raises if it is missing: no fallback."""
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"lmweather_gb300 CUDA library not built ({path}); run python -m lmweather_gb300.build")
+        lib = C.CDLL(path)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+def launch_count() -> int:
+    return int(load_library().lmw_launch_count())
+
+
+def _check(code: int) -> None:
+    if code == 0:
+        return
+    msg = load_library().lmw_last_error().decode()
+    if code == 1:
+        raise ValueError(msg)
+    if code == 3:
+        raise DeviceError(msg)
+    raise RuntimeError(msg)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _c128(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+class Sphere:
+    """GPU spectral-transform sphere (cpp/sphere.hpp:27-121). Spectra use the reference layout: (T+1)^2 complex
+    values per field at m*(T+1)+n. `members` > 1 holds an ensemble of states stepped together; per-member calls
+    take `member=`."""
+
+    def __init__(self, truncation: int, radius=6.37122e6, omega=7.292e-5, gravity=9.80616, diffusion=0.0,
+                 precision: int = FP64, members: int = 1, max_truncation: int = 170):
+        self._lib = load_library()
+        h = C.c_void_p()
+        _check(self._lib.lmw_sphere_create_ex(truncation, radius, omega, gravity, diffusion, precision, members,
+                                              max_truncation, C.byref(h)))
+        self._h = h
+        T, nlat, nlon, B = _I(), _I(), _I(), _I()
+        _check(self._lib.lmw_sphere_dims(h, C.byref(T), C.byref(nlat), C.byref(nlon), C.byref(B)))
+        self.T, self.nlat, self.nlon, self.members = T.value, nlat.value, nlon.value, B.value
+        self.radius, self.omega, self.gravity = radius, omega, gravity
+        self.precision = precision
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lmw_sphere_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ geometry
+    def truncation(self) -> int:
+        return self.T
+
+    @property
+    def nspec(self) -> int:
+        return (self.T + 1) ** 2
+
+    @property
+    def ngrid(self) -> int:
+        return self.nlat * self.nlon
+
+    def gauss(self):
+        mu, w = np.zeros(self.nlat), np.zeros(self.nlat)
+        _check(self._lib.lmw_sphere_gauss(self._h, _dp(mu), _dp(w)))
+        return mu, w
+
+    def time(self, member: int = 0) -> float:
+        t = _D()
+        _check(self._lib.lmw_sphere_time(self._h, member, C.byref(t)))
+        return t.value
+
+    # ------------------------------------------------------------ state
+    def set_state_grid(self, h, u, v, member: int = 0):
+        h, u, v = _f64(h), _f64(u), _f64(v)
+        if not (h.size == u.size == v.size):
+            raise ValueError("grid size mismatch")
+        _check(self._lib.lmw_sphere_set_state_grid(self._h, member, _dp(h), _dp(u), _dp(v), h.size))
+        return self
+
+    def set_axis_tilt(self, alpha: float, member: int = 0):
+        _check(self._lib.lmw_sphere_set_axis_tilt(self._h, member, alpha))
+        return self
+
+    def set_omega(self, omega: float, member: int = 0):
+        _check(self._lib.lmw_sphere_set_omega(self._h, member, omega))
+        return self
+
+    def set_diffusion(self, nu4: float):
+        _check(self._lib.lmw_sphere_set_diffusion(self._h, nu4))
+        return self
+
+    def set_orography_grid(self, hs, member: int = 0):
+        hs = _f64(hs)
+        _check(self._lib.lmw_sphere_set_orography_grid(self._h, member, _dp(hs), hs.size))
+        return self
+
+    def add_mode(self, n: int, m: int, amplitude: float, mean_depth: float, member: int = 0):
+        _check(self._lib.lmw_sphere_add_mode(self._h, member, n, m, amplitude, mean_depth))
+        return self
+
+    def perturb(self, amplitude: float, seed: int, max_wave: int, member: int = 0):
+        _check(self._lib.lmw_sphere_perturb(self._h, member, amplitude, seed, max_wave))
+        return self
+
+    def mark_reference(self, member: int = 0):
+        _check(self._lib.lmw_sphere_mark_reference(self._h, member))
+        return self
+
+    def turbulence(self, seed: int, mean_height=8000.0, max_wind=30.0, nforce=21, member: int = 0):
+        _check(self._lib.lmw_sphere_turbulence(self._h, member, seed, mean_height, max_wind, nforce))
+        return self
+
+    def get_state(self, member: int = 0):
+        z, d, f = (np.zeros(self.nspec, np.complex128) for _ in range(3))
+        _check(self._lib.lmw_sphere_get_state(self._h, member, _dp(z.view(np.float64)), _dp(d.view(np.float64)),
+                                              _dp(f.view(np.float64))))
+        return z, d, f
+
+    def set_state(self, zeta, delta, phi, time: float = 0.0, member: int = 0):
+        z, d, f = _c128(zeta), _c128(delta), _c128(phi)
+        if not (z.size == d.size == f.size == self.nspec):
+            raise ValueError("spectral state size mismatch")
+        _check(self._lib.lmw_sphere_set_state(self._h, member, _dp(z.view(np.float64)), _dp(d.view(np.float64)),
+                                              _dp(f.view(np.float64)), time))
+        return self
+
+    # ------------------------------------------------------------ time stepping
+    def step(self, dt: float):
+        _check(self._lib.lmw_sphere_step(self._h, dt))
+        return self
+
+    def run(self, seconds: float, dt: float = 0.0):
+        _check(self._lib.lmw_sphere_run(self._h, seconds, dt))
+        return self
+
+    def stable_dt(self, safety: float = 1.5, member: int = 0) -> float:
+        out = _D()
+        _check(self._lib.lmw_sphere_stable_dt(self._h, member, safety, C.byref(out)))
+        return out.value
+
+    # ------------------------------------------------------------ diagnostics
+    _DIAG = ("mean_height", "kinetic_energy", "potential_energy", "energy", "enstrophy", "max_wind", "error_l2", "error_linf")
+
+    def diagnostics(self, member: int = 0) -> dict:
+        out = np.zeros(8)
+        _check(self._lib.lmw_sphere_diagnostics(self._h, member, _dp(out)))
+        return dict(zip(self._DIAG, out.tolist()))
+
+    def mean_height(self, member: int = 0) -> float:
+        return self.diagnostics(member)["mean_height"]
+
+    def energy(self, member: int = 0) -> float:
+        return self.diagnostics(member)["energy"]
+
+    def kinetic_energy(self, member: int = 0) -> float:
+        return self.diagnostics(member)["kinetic_energy"]
+
+    def potential_energy(self, member: int = 0) -> float:
+        return self.diagnostics(member)["potential_energy"]
+
+    def potential_enstrophy(self, member: int = 0) -> float:
+        return self.diagnostics(member)["enstrophy"]
+
+    def max_wind(self, member: int = 0) -> float:
+        return self.diagnostics(member)["max_wind"]
+
+    def height_error_l2(self, member: int = 0) -> float:
+        return self.diagnostics(member)["error_l2"]
+
+    def height_error_linf(self, member: int = 0) -> float:
+        return self.diagnostics(member)["error_linf"]
+
+    def _grid(self, which: int, member: int) -> np.ndarray:
+        g = np.zeros((self.nlat, self.nlon))
+        _check(self._lib.lmw_sphere_grid(self._h, member, which, _dp(g), g.size))
+        return g
+
+    def grid_height(self, member: int = 0):
+        return self._grid(0, member)
+
+    def grid_u(self, member: int = 0):
+        return self._grid(1, member)
+
+    def grid_v(self, member: int = 0):
+        return self._grid(2, member)
+
+    def grid_vorticity(self, member: int = 0):
+        return self._grid(3, member)
+
+    def spectrum(self, member: int = 0):
+        ke, pe = np.zeros(self.T + 1), np.zeros(self.T + 1)
+        _check(self._lib.lmw_sphere_spectrum(self._h, member, _dp(ke), _dp(pe)))
+        return ke, pe
+
+
+class Plane:
+    """GPU C-grid beta-plane channel (cpp/plane.hpp:20-68)."""
+
+    def __init__(self, nx: int, ny: int, lx: float, ly: float, gravity=9.81, depth=100.0, f0=0.0, beta=0.0,
+                 viscosity=0.0, drag=0.0, linear=False):
+        self._lib = load_library()
+        h = C.c_void_p()
+        _check(self._lib.lmw_plane_create(nx, ny, lx, ly, gravity, depth, f0, beta, viscosity, drag, 1 if linear else 0,
+                                          C.byref(h)))
+        self._h = h
+        self.nx, self.ny, self.lx, self.ly = nx, ny, lx, ly
+        self.params = dict(gravity=gravity, depth=depth, f0=f0, beta=beta, viscosity=viscosity, drag=drag, linear=linear)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lmw_plane_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def dx(self) -> float:
+        return self.lx / self.nx
+
+    def dy(self) -> float:
+        return self.ly / self.ny
+
+    def set_params(self, **kw):
+        self.params.update(kw)
+        p = self.params
+        _check(self._lib.lmw_plane_set_params(self._h, p["gravity"], p["depth"], p["f0"], p["beta"], p["viscosity"],
+                                              p["drag"], 1 if p["linear"] else 0))
+        return self
+
+    def reset(self):
+        _check(self._lib.lmw_plane_reset(self._h))
+        return self
+
+    def set_h_from_grid(self, g):
+        g = _f64(g)
+        _check(self._lib.lmw_plane_set_h(self._h, _dp(g), g.size))
+        return self
+
+    def set_u_from_grid(self, g):
+        g = _f64(g)
+        _check(self._lib.lmw_plane_set_u(self._h, _dp(g), g.size))
+        return self
+
+    def set_v_from_grid(self, g):
+        g = _f64(g)
+        _check(self._lib.lmw_plane_set_v(self._h, _dp(g), g.size))
+        return self
+
+    def get(self):
+        h, u, v = np.zeros((self.ny, self.nx)), np.zeros((self.ny, self.nx)), np.zeros((self.ny + 1, self.nx))
+        _check(self._lib.lmw_plane_get(self._h, _dp(h), _dp(u), _dp(v)))
+        return h, u, v
+
+    def perturb(self, amplitude: float, seed: int):
+        _check(self._lib.lmw_plane_perturb(self._h, amplitude, seed))
+        return self
+
+    def jet(self, u0=20.0, width=1.0e5, noise_rms=0.1, seed=1):
+        _check(self._lib.lmw_plane_jet(self._h, u0, width, noise_rms, seed))
+        return self
+
+    def step(self, dt: float):
+        _check(self._lib.lmw_plane_step(self._h, dt))
+        return self
+
+    def run(self, seconds: float, dt: float = 0.0):
+        _check(self._lib.lmw_plane_run(self._h, seconds, dt))
+        return self
+
+    def stable_dt(self, safety: float = 0.5) -> float:
+        out = _D()
+        _check(self._lib.lmw_plane_stable_dt(self._h, safety, C.byref(out)))
+        return out.value
+
+    def time(self) -> float:
+        out = _D()
+        _check(self._lib.lmw_plane_time(self._h, C.byref(out)))
+        return out.value
+
+    _DIAG = ("mean_depth", "energy", "max_speed", "pv_anomaly_rms")
+
+    def diagnostics(self) -> dict:
+        out = np.zeros(4)
+        _check(self._lib.lmw_plane_diagnostics(self._h, _dp(out)))
+        return dict(zip(self._DIAG, out.tolist()))
+
+    def mean_depth(self) -> float:
+        return self.diagnostics()["mean_depth"]
+
+    def energy(self) -> float:
+        return self.diagnostics()["energy"]
+
+    def max_speed(self) -> float:
+        return self.diagnostics()["max_speed"]

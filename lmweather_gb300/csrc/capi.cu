@@ -1,0 +1,294 @@
+// The C ABI (include/lmweather_gb300.h): exceptions become status codes, the message is kept per thread.
+#include <cstdio>
+#include <exception>
+#include <new>
+#include <string>
+
+#include "../../include/lmweather_gb300.h"
+#include "engine.h"
+#include "sphere_tables.h"
+
+struct lmw_sphere {
+  lmw::SphereEngine *e;
+};
+struct lmw_plane {
+  lmw::PlaneEngine *e;
+};
+
+namespace lmw {
+thread_local uint64_t g_launches = 0;
+
+void cuda_check(cudaError_t e, const char *what, const char *file, int line) {
+  if (e == cudaSuccess) return;
+  char buf[512];
+  std::snprintf(buf, sizeof buf, "CUDA error %s (%s) in %s at %s:%d", cudaGetErrorName(e), cudaGetErrorString(e), what, file, line);
+  throw DeviceError(buf);
+}
+
+std::string fmt_f(double x) {
+  char b[512];
+  std::snprintf(b, sizeof b, "%f", x);
+  return b;
+}
+}  // namespace lmw
+
+namespace {
+thread_local std::string g_err;
+
+template <class F> int guard(F &&fn) {
+  try {
+    fn();
+    g_err.clear();
+    return LMW_OK;
+  } catch (const lmw::DeviceError &e) {
+    g_err = e.what();
+    return LMW_DEVICE_ERROR;
+  } catch (const std::invalid_argument &e) {
+    g_err = e.what();
+    return LMW_INVALID_ARGUMENT;
+  } catch (const std::bad_alloc &) {
+    g_err = "out of host memory";
+    return LMW_RUNTIME_ERROR;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+    return LMW_RUNTIME_ERROR;
+  }
+}
+
+void need(bool ok, const char *msg) {
+  if (!ok) throw lmw::InvalidArgument(msg);
+}
+}  // namespace
+
+extern "C" {
+
+const char *lmw_last_error(void) { return g_err.c_str(); }
+const char *lmw_version(void) { return "lmweather-gb300 0.1.0"; }
+uint64_t lmw_launch_count(void) { return lmw::g_launches; }
+int lmw_fp64_peak(double *tflops) {
+  return guard([&] {
+    need(tflops != nullptr, "output pointer is null");
+    *tflops = lmw::measure_fp64_peak();
+  });
+}
+
+// ------------------------------------------------------------------------------------------------ sphere
+int lmw_sphere_create_ex(int truncation, double radius, double omega, double gravity, double diffusion, int precision, int members,
+                         int max_truncation, lmw_sphere **out) {
+  return guard([&] {
+    need(out != nullptr, "output handle pointer is null");
+    *out = nullptr;
+    lmw::SphereConfig c;
+    c.truncation = truncation;
+    c.radius = radius;
+    c.omega = omega;
+    c.gravity = gravity;
+    c.diffusion = diffusion;
+    c.precision = precision;
+    c.members = members;
+    c.max_truncation = max_truncation;
+    need(max_truncation >= 4 && max_truncation <= 341, "the truncation cap must be between 4 and 341");
+    auto *h = new lmw_sphere{nullptr};
+    try {
+      h->e = new lmw::SphereEngine(c);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int lmw_sphere_create(int truncation, double radius, double omega, double gravity, double diffusion, lmw_sphere **out) {
+  return lmw_sphere_create_ex(truncation, radius, omega, gravity, diffusion, LMW_FP64, 1, 170, out);
+}
+int lmw_sphere_destroy(lmw_sphere *s) {
+  return guard([&] {
+    if (!s) return;
+    delete s->e;
+    delete s;
+  });
+}
+
+#define SPH(...)                                                 \
+  guard([&] {                                                    \
+    need(s != nullptr && s->e != nullptr, "null sphere handle"); \
+    __VA_ARGS__;                                                 \
+  })
+
+int lmw_sphere_dims(const lmw_sphere *s, int *truncation, int *nlat, int *nlon, int *members) {
+  return SPH({
+    if (truncation) *truncation = s->e->N;
+    if (nlat) *nlat = s->e->nlat;
+    if (nlon) *nlon = s->e->nlon;
+    if (members) *members = s->e->B;
+  });
+}
+int lmw_sphere_gauss(const lmw_sphere *s, double *mu, double *w) {
+  return SPH({
+    std::vector<double> x, ww;
+    lmw::gauss_legendre(s->e->nlat, x, ww);
+    if (mu) std::copy(x.begin(), x.end(), mu);
+    if (w) std::copy(ww.begin(), ww.end(), w);
+  });
+}
+int lmw_sphere_time(const lmw_sphere *s, int member, double *out) {
+  return SPH({
+    need(member >= 0 && member < s->e->B, "member index out of range");
+    *out = s->e->t[member];
+  });
+}
+int lmw_sphere_set_state_grid(lmw_sphere *s, int member, const double *h, const double *u, const double *v, size_t n) {
+  return SPH({
+    need(h && u && v, "grid pointer is null");
+    s->e->set_state_grid(h, u, v, n, member);
+  });
+}
+int lmw_sphere_set_axis_tilt(lmw_sphere *s, int member, double alpha) { return SPH(s->e->set_axis_tilt(alpha, member)); }
+int lmw_sphere_set_omega(lmw_sphere *s, int member, double omega) { return SPH(s->e->set_omega(omega, member)); }
+int lmw_sphere_set_diffusion(lmw_sphere *s, double nu4) { return SPH(s->e->set_diffusion(nu4)); }
+int lmw_sphere_set_orography_grid(lmw_sphere *s, int member, const double *hs, size_t n) {
+  return SPH({
+    need(hs != nullptr, "grid pointer is null");
+    s->e->set_orography(hs, n, member);
+  });
+}
+int lmw_sphere_add_mode(lmw_sphere *s, int member, int n, int m, double amplitude, double mean_depth) {
+  return SPH(s->e->add_mode(n, m, amplitude, mean_depth, member));
+}
+int lmw_sphere_perturb(lmw_sphere *s, int member, double amplitude, uint64_t seed, int max_wave) {
+  return SPH(s->e->perturb(amplitude, seed, max_wave, member));
+}
+int lmw_sphere_mark_reference(lmw_sphere *s, int member) { return SPH(s->e->mark_reference(member)); }
+int lmw_sphere_turbulence(lmw_sphere *s, int member, uint64_t seed, double mean_height, double max_wind, int nforce) {
+  return SPH(s->e->turbulence(seed, mean_height, max_wind, nforce, member));
+}
+int lmw_sphere_get_state(lmw_sphere *s, int member, double *zeta, double *delta, double *phi) {
+  return SPH(s->e->get_state(zeta, delta, phi, member));
+}
+int lmw_sphere_set_state(lmw_sphere *s, int member, const double *zeta, const double *delta, const double *phi, double time) {
+  return SPH({
+    need(zeta && delta && phi, "state pointer is null");
+    s->e->set_state(zeta, delta, phi, time, member);
+  });
+}
+int lmw_sphere_step(lmw_sphere *s, double dt) { return SPH(s->e->step(dt)); }
+int lmw_sphere_run(lmw_sphere *s, double seconds, double dt) { return SPH(s->e->run(seconds, dt)); }
+int lmw_sphere_stable_dt(lmw_sphere *s, int member, double safety, double *out) {
+  return SPH({
+    need(member >= 0 && member < s->e->B, "member index out of range");
+    *out = s->e->stable_dt(safety, member);
+  });
+}
+int lmw_sphere_diagnostics(lmw_sphere *s, int member, double *out) { return SPH(s->e->diagnostics(out, member)); }
+int lmw_sphere_grid(lmw_sphere *s, int member, int which, double *out, size_t n) {
+  return SPH({
+    need(n == s->e->ngrid(), "grid size mismatch");
+    s->e->grid(which, out, member);
+  });
+}
+int lmw_sphere_spectrum(lmw_sphere *s, int member, double *ke, double *pe) {
+  return SPH({
+    need(member >= 0 && member < s->e->B, "member index out of range");
+    s->e->spectrum(ke, pe, member);
+  });
+}
+
+int lmw_sphere_stream(const lmw_sphere *s, void **stream) { return SPH(*stream = static_cast<void *>(s->e->stream)); }
+int lmw_sphere_kernel_times(lmw_sphere *s, double dt, int reps, double *ms) {
+  return SPH({
+    need(reps > 0, "reps must be positive");
+    s->e->kernel_times(dt, reps, ms);
+  });
+}
+
+// ------------------------------------------------------------------------------------------------ plane
+int lmw_plane_create(int nx, int ny, double lx, double ly, double gravity, double depth, double f0, double beta, double viscosity,
+                     double drag, int linear, lmw_plane **out) {
+  return guard([&] {
+    need(out != nullptr, "output handle pointer is null");
+    *out = nullptr;
+    lmw::PlaneConfig c;
+    c.nx = nx;
+    c.ny = ny;
+    c.lx = lx;
+    c.ly = ly;
+    c.gravity = gravity;
+    c.depth = depth;
+    c.f0 = f0;
+    c.beta = beta;
+    c.viscosity = viscosity;
+    c.drag = drag;
+    c.linear = linear != 0;
+    auto *h = new lmw_plane{nullptr};
+    try {
+      h->e = new lmw::PlaneEngine(c);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int lmw_plane_destroy(lmw_plane *p) {
+  return guard([&] {
+    if (!p) return;
+    delete p->e;
+    delete p;
+  });
+}
+
+#define PLN(...)                                                \
+  guard([&] {                                                   \
+    need(p != nullptr && p->e != nullptr, "null plane handle"); \
+    __VA_ARGS__;                                                \
+  })
+
+int lmw_plane_set_params(lmw_plane *p, double gravity, double depth, double f0, double beta, double viscosity, double drag, int linear) {
+  return PLN({
+    p->e->p.gravity = gravity;
+    p->e->p.depth = depth;
+    p->e->p.f0 = f0;
+    p->e->p.beta = beta;
+    p->e->p.viscosity = viscosity;
+    p->e->p.drag = drag;
+    p->e->p.linear = linear != 0;
+  });
+}
+int lmw_plane_reset(lmw_plane *p) { return PLN(p->e->reset()); }
+int lmw_plane_set_h(lmw_plane *p, const double *h, size_t n) {
+  return PLN({
+    need(h != nullptr, "grid pointer is null");
+    p->e->set_h(h, n);
+  });
+}
+int lmw_plane_set_u(lmw_plane *p, const double *u, size_t n) {
+  return PLN({
+    need(u != nullptr, "grid pointer is null");
+    p->e->set_u(u, n);
+  });
+}
+int lmw_plane_set_v(lmw_plane *p, const double *v, size_t n) {
+  return PLN({
+    need(v != nullptr, "grid pointer is null");
+    p->e->set_v(v, n);
+  });
+}
+int lmw_plane_get(lmw_plane *p, double *h, double *u, double *v) { return PLN(p->e->get(h, u, v)); }
+int lmw_plane_perturb(lmw_plane *p, double amplitude, uint64_t seed) { return PLN(p->e->perturb(amplitude, seed)); }
+int lmw_plane_jet(lmw_plane *p, double u0, double width, double noise_rms, uint64_t seed) {
+  return PLN(p->e->jet(u0, width, noise_rms, seed));
+}
+int lmw_plane_step(lmw_plane *p, double dt) { return PLN(p->e->step(dt)); }
+int lmw_plane_run(lmw_plane *p, double seconds, double dt) { return PLN(p->e->run(seconds, dt)); }
+int lmw_plane_stable_dt(lmw_plane *p, double safety, double *out) { return PLN(*out = p->e->stable_dt(safety)); }
+int lmw_plane_time(const lmw_plane *p, double *out) { return PLN(*out = p->e->t); }
+int lmw_plane_diagnostics(lmw_plane *p, double *out) { return PLN(p->e->diagnostics(out)); }
+int lmw_plane_stream(const lmw_plane *p, void **stream) { return PLN(*stream = static_cast<void *>(p->e->stream)); }
+int lmw_plane_kernel_time(lmw_plane *p, double dt, int reps, double *ms) {
+  return PLN({
+    need(reps > 0, "reps must be positive");
+    *ms = p->e->kernel_time(dt, reps);
+  });
+}
+
+}  // extern "C"

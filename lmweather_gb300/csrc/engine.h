@@ -1,0 +1,148 @@
+// Engine objects behind the C ABI: device-resident state, one CUDA stream per object.
+#pragma once
+#include "lmw_internal.h"
+
+namespace lmw {
+
+// ------------------------------------------------------------------------------------------------ plane
+// Mirrors lmweather::PlaneParams (cpp/plane.hpp:9-18).
+struct PlaneConfig {
+  int nx = 0, ny = 0;
+  double lx = 0, ly = 0;
+  double gravity = 9.81, depth = 100, f0 = 0, beta = 0, viscosity = 0, drag = 0;
+  bool linear = false;
+};
+
+class PlaneEngine {
+ public:
+  explicit PlaneEngine(const PlaneConfig &c);
+  ~PlaneEngine();
+  PlaneConfig p;
+  double t = 0;
+
+  size_t ncell() const { return static_cast<size_t>(p.nx) * p.ny; }
+  size_t nvpt() const { return static_cast<size_t>(p.nx) * (p.ny + 1); }
+  double dx() const { return p.lx / p.nx; }
+  double dy() const { return p.ly / p.ny; }
+
+  void reset();
+  void set_h(const double *g, size_t n);
+  void set_u(const double *g, size_t n);
+  void set_v(const double *g, size_t n);
+  void get(double *h, double *u, double *v);
+  void perturb(double amplitude, uint64_t seed);
+  void jet(double u0, double width, double noise_rms, uint64_t seed);
+  void step(double dt);
+  void run(double seconds, double dt);
+  double stable_dt(double safety);
+  // mean_depth, energy, max_speed, pv_anomaly_rms
+  void diagnostics(double *out);
+  // device pointers of the state (h, u, v), valid until the engine is destroyed
+  void device_state(double **h, double **u, double **v) {
+    *h = h0.p; *u = u0.p; *v = v0.p;
+  }
+  cudaStream_t stream = nullptr;
+  // enqueue one RK4 step on the engine stream (no synchronisation)
+  void enqueue_step(double dt);
+  // average duration (ms) of one RK4-stage kernel launch over `reps` launches, timed with CUDA events on the
+  // engine stream; the state is left unchanged
+  double kernel_time(double dt, int reps);
+
+ private:
+  DevBuf<double> h0, u0, v0, ha, ua, va, hb, ub, vb, ah, au, av;
+  DevBuf<double> part;
+  DevBuf<Reduce> dred;
+  HostBuf<Reduce> hred;
+  HostBuf<double> stage;
+  int nblk_red = 0;
+  cudaGraphExec_t graph = nullptr;
+  double graph_dt = 0;
+  int graph_steps = 0;
+  void reduce(Reduce &r);
+  void upload(double *dst, const double *src, size_t n);
+  void launch_chunk(double dt, int steps);
+};
+
+// ------------------------------------------------------------------------------------------------ sphere
+// Mirrors lmweather::SphereParams (cpp/sphere.hpp:20-25) plus the engine's precision mode.
+enum Precision { kFP64 = 0, kFP32 = 1, kSplitBF16 = 2 };
+
+struct SphereConfig {
+  int truncation = 42;
+  double radius = 6.37122e6, omega = 7.292e-5, gravity = 9.80616, diffusion = 0;
+  int precision = kFP64;
+  int members = 1;          // ensemble members sharing the truncation (batch dimension)
+  int max_truncation = 341; // the reference caps at 170; the engine allows up to this
+};
+
+struct SphereTables;
+
+class SphereEngine {
+ public:
+  explicit SphereEngine(const SphereConfig &c);
+  ~SphereEngine();
+  SphereConfig p;
+  int N = 0, M = 0, nlat = 0, nlon = 0, nh = 0, ntri = 0, B = 1;
+  std::vector<double> t;  // per member model time
+  cudaStream_t stream = nullptr;
+
+  size_t ngrid() const { return static_cast<size_t>(nlat) * nlon; }
+  size_t nspec_ref() const { return static_cast<size_t>(M) * M; }  // the reference's (T+1)^2 layout
+
+  void set_axis_tilt(double alpha, int member);
+  void set_omega(double omega, int member);
+  void set_diffusion(double nu4) { p.diffusion = nu4; filt_dt = -1; }
+  void set_orography(const double *hs, size_t n, int member);
+  void set_state_grid(const double *h, const double *u, const double *v, size_t n, int member);
+  void set_state(const double *zeta, const double *delta, const double *phi, double time, int member);
+  void get_state(double *zeta, double *delta, double *phi, int member);
+  void add_mode(int n, int m, double amplitude, double mean_depth, int member);
+  void perturb(double amplitude, uint64_t seed, int max_wave, int member);
+  void turbulence(uint64_t seed, double mean_height, double max_wind, int nforce, int member);
+  void mark_reference(int member);
+  void step(double dt);
+  void run(double seconds, double dt);
+  double stable_dt(double safety, int member);
+  // mean_height, kinetic, potential, energy, enstrophy, max_wind, error_l2, error_linf
+  void diagnostics(double *out, int member);
+  // which: 0 height, 1 u, 2 v, 3 vorticity
+  void grid(int which, double *out, int member);
+  void spectrum(double *ke, double *pe, int member);
+  void enqueue_step(double dt);
+  // device pointer of the packed spectral state [member][field][tri] complex128 (FP64 state accumulation)
+  double *device_state() { return x0.p; }
+  uint64_t launches_per_step() const { return launches_step; }
+  // average duration (ms) per launch of each stage kernel class over `reps` launches (CUDA events on the
+  // engine stream): out[0] synthesis, out[1] grid (FFTs + products), out[2] analysis + RK4 update. x0 unchanged.
+  void kernel_times(double dt, int reps, double *out);
+
+ private:
+  SphereTables *tab = nullptr;
+  // state (packed triangle, complex interleaved), stage input, accumulator
+  DevBuf<double> x0, xs, acc;
+  // Fourier coefficients of the synthesised grids, folded analysis inputs
+  DevBuf<double> four, fold;
+  DevBuf<float> four32, fold32;
+  DevBuf<double> fgrid, hsgrid, refgrid, filt, diagrows;
+  DevBuf<double> gridin;
+  DevBuf<Reduce> dred;
+  HostBuf<Reduce> hred;
+  HostBuf<double> hstage;
+  std::vector<double> omega_m;
+  std::vector<char> has_orog;
+  double filt_dt = -1;
+  uint64_t launches_step = 0;
+  cudaGraphExec_t graph = nullptr;
+  double graph_dt = 0;
+  int graph_steps = 0;
+  void upload_filter(double dt);
+  void launch_stage(int stage, double dt);
+  void launch_chunk(double dt, int steps);
+  void synth_grids(int member_first, int count);  // state x0 -> Fourier coefficients of U, V, zeta, phi
+  void reduce_guard(Reduce &r, int member);
+  void analyze_grids_to_state(int member);
+  void to_packed(const double *ref_layout, double *packed);
+  void from_packed(const double *packed, double *ref_layout);
+};
+
+}  // namespace lmw

@@ -1,0 +1,87 @@
+// Internal declarations shared by the engine's translation units (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace lmw {
+
+// The reference's two exception kinds (std::invalid_argument / std::runtime_error) plus device failures.
+struct InvalidArgument : std::invalid_argument {
+  using std::invalid_argument::invalid_argument;
+};
+struct RuntimeError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct DeviceError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+void cuda_check(cudaError_t e, const char *what, const char *file, int line);
+#define LMW_CUDA(call) ::lmw::cuda_check((call), #call, __FILE__, __LINE__)
+#define LMW_LAUNCH_CHECK() ::lmw::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+
+// std::to_string(double) formatting ("%f"), which the reference uses in its run() messages
+std::string fmt_f(double x);
+
+// Device buffer owned by an engine object.
+template <class T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) return;
+    LMW_CUDA(cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(T)));
+    n = count;
+  }
+  void zero(cudaStream_t s) {
+    if (p) LMW_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// Pinned host staging buffer.
+template <class T> struct HostBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  HostBuf() = default;
+  HostBuf(const HostBuf &) = delete;
+  HostBuf &operator=(const HostBuf &) = delete;
+  ~HostBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  void alloc(size_t count) {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return;
+    LMW_CUDA(cudaMallocHost(reinterpret_cast<void **>(&p), count * sizeof(T)));
+    n = count;
+  }
+};
+
+// Counts this library's kernel launches (for the benchmark's launch accounting).
+extern thread_local uint64_t g_launches;
+
+// FP64 FMA throughput of the current device (TFLOP/s), from a dependent-chain DFMA kernel on every SM
+double measure_fp64_peak();
+
+// Device-wide reduction results of one guard/diagnostic pass.
+struct Reduce {
+  double sum[8];
+  double max[4];
+};
+
+}  // namespace lmw

@@ -1,0 +1,527 @@
+// Beta-plane C-grid shallow water on the GPU (FP64), the lmweather Plane model (cpp/plane.cpp).
+//
+// One fused kernel per RK4 stage: a CTA loads a (TY+2) x (TX+2) tile of h, u, v (periodic in x, rows
+// clamped at the walls) into shared memory, forms the Bernoulli function B and the absolute vorticity eta
+// for the tile plus its one-cell halo, evaluates du, dv, dh, and applies the RK4 stage update in the same
+// pass (stage input, accumulator and, at the last stage, the state). Every arithmetic expression follows
+// the reference's order of evaluation and this file is compiled with --fmad=false, so that the result is
+// bitwise identical to cpp/plane.cpp:59-158 built without FMA contraction.
+#include <cmath>
+#include <cstring>
+
+#include "engine.h"
+
+namespace lmw {
+namespace {
+
+constexpr int TX = 32, TY = 8;
+
+struct PlaneDev {
+  int nx, ny, lin;
+  double dxx, dyy, dxx2, dyy2, g, depth, f0, beta, visc, drag, ly;
+};
+
+__device__ __forceinline__ int wrapx(int i, int nx) { return ((i % nx) + nx) % nx; }
+
+// stage 0..3 with coefficients c = 0.5 dt, 0.5 dt, dt, dt/6 (cpp/plane.cpp:143-158)
+__global__ void __launch_bounds__(TX *TY) plane_stage(PlaneDev p, int stage, double c, const double *__restrict__ hi,
+                                                      const double *__restrict__ ui, const double *__restrict__ vi,
+                                                      double *h0, double *u0, double *v0, double *ah, double *au, double *av,
+                                                      double *ho, double *uo, double *vo) {
+  __shared__ double sh[TY + 2][TX + 2], su[TY + 2][TX + 2], sv[TY + 2][TX + 2];
+  __shared__ double sB[TY + 1][TX + 1], sE[TY + 1][TX + 1];
+  const int nx = p.nx, ny = p.ny;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int tid = threadIdx.y * TX + threadIdx.x;
+  // tile load: local (ly, lx) <-> global (j0 - 1 + ly, i0 - 1 + lx), periodic in x
+  for (int e = tid; e < (TY + 2) * (TX + 2); e += TX * TY) {
+    int ly = e / (TX + 2), lx = e % (TX + 2);
+    int jg = j0 - 1 + ly, ig = wrapx(i0 - 1 + lx, nx);
+    double hv = 0, uv = 0, vv = 0;
+    if (jg >= 0 && jg < ny) {
+      size_t o = static_cast<size_t>(jg) * nx + ig;
+      hv = hi[o];
+      uv = ui[o];
+    }
+    if (jg >= 0 && jg <= ny) vv = vi[static_cast<size_t>(jg) * nx + ig];
+    sh[ly][lx] = hv;
+    su[ly][lx] = uv;
+    sv[ly][lx] = vv;
+  }
+  __syncthreads();
+  // Bernoulli B at cells (j0-1+ly, i0-1+lx) and absolute vorticity at corners (j0+ly, i0+lx), cpp/plane.cpp:70-92
+  for (int e = tid; e < (TY + 1) * (TX + 1); e += TX * TY) {
+    int ly = e / (TX + 1), lx = e % (TX + 1);
+    int jb = j0 - 1 + ly;
+    double b = 0;
+    if (jb >= 0 && jb < ny) {
+      double k = 0;
+      if (!p.lin) {
+        double ua = su[ly][lx], ub = su[ly][lx + 1], va = sv[ly][lx], vb = sv[ly + 1][lx];
+        k = 0.5 * (0.5 * (ua * ua + ub * ub) + 0.5 * (va * va + vb * vb));
+      }
+      b = p.g * sh[ly][lx] + k;
+    }
+    sB[ly][lx] = b;
+    int je = j0 + ly;
+    double eta = 0;
+    if (je <= ny) {
+      double f = p.f0 + p.beta * (je * p.dyy - 0.5 * p.ly);
+      double zeta = 0;
+      if (!p.lin) {
+        double dvdx = (sv[ly + 1][lx + 1] - sv[ly + 1][lx]) / p.dxx;
+        double uj = je < ny ? su[ly + 1][lx + 1] : su[ly][lx + 1];
+        double ujm = je > 0 ? su[ly][lx + 1] : su[ly + 1][lx + 1];
+        zeta = dvdx - (uj - ujm) / p.dyy;
+      }
+      eta = f + zeta;
+    }
+    sE[ly][lx] = eta;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = i0 + tx, j = j0 + ty;
+  if (i >= nx || j >= ny) return;
+  const double U = su[ty + 1][tx + 1], V = sv[ty + 1][tx + 1], Hc = sh[ty + 1][tx + 1];
+  // du at the u point (i, j): cpp/plane.cpp:94-105
+  double du;
+  {
+    double q = 0.5 * (sE[ty][tx] + sE[ty + 1][tx]);
+    double vbar = 0.25 * (sv[ty + 1][tx] + sv[ty + 1][tx + 1] + sv[ty + 2][tx] + sv[ty + 2][tx + 1]);
+    double r = q * vbar - (sB[ty + 1][tx + 1] - sB[ty + 1][tx]) / p.dxx - p.drag * U;
+    if (p.visc != 0) {
+      double uy1 = j + 1 < ny ? su[ty + 2][tx + 1] : U, uy0 = j > 0 ? su[ty][tx + 1] : U;
+      r += p.visc * ((su[ty + 1][tx + 2] - 2 * U + su[ty + 1][tx]) / p.dxx2 + (uy1 - 2 * U + uy0) / p.dyy2);
+    }
+    du = r;
+  }
+  // dv at the v point (i, j), interior rows only: cpp/plane.cpp:106-117
+  double dv = 0;
+  if (j >= 1) {
+    double q = 0.5 * (sE[ty][tx] + sE[ty][tx + 1]);
+    double ubar = 0.25 * (su[ty][tx + 1] + su[ty][tx + 2] + su[ty + 1][tx + 1] + su[ty + 1][tx + 2]);
+    double r = -q * ubar - (sB[ty + 1][tx + 1] - sB[ty][tx + 1]) / p.dyy - p.drag * V;
+    if (p.visc != 0) {
+      double vy1 = j + 1 < ny ? sv[ty + 2][tx + 1] : 0.0, vy0 = j - 1 > 0 ? sv[ty][tx + 1] : 0.0;
+      r += p.visc * ((sv[ty + 1][tx + 2] - 2 * V + sv[ty + 1][tx]) / p.dxx2 + (vy1 - 2 * V + vy0) / p.dyy2);
+    }
+    dv = r;
+  }
+  // dh: continuity in flux form, cpp/plane.cpp:119-128
+  double dh;
+  {
+    double hw = p.lin ? p.depth : 0.5 * (sh[ty + 1][tx] + Hc);
+    double fe = (p.lin ? p.depth : 0.5 * (Hc + sh[ty + 1][tx + 2])) * su[ty + 1][tx + 2];
+    double fw = hw * U;
+    double fn = 0, fs = 0;
+    if (j + 1 < ny) fn = (p.lin ? p.depth : 0.5 * (Hc + sh[ty + 2][tx + 1])) * sv[ty + 2][tx + 1];
+    if (j > 0) fs = (p.lin ? p.depth : 0.5 * (sh[ty][tx + 1] + Hc)) * V;
+    dh = -((fe - fw) / p.dxx + (fn - fs) / p.dyy);
+  }
+  const size_t o = static_cast<size_t>(j) * nx + i;
+  // RK4 bookkeeping: cpp/plane.cpp:146-156 (acc = k1 + 2 k2 + 2 k3, state += dt/6 (acc + k4))
+  auto upd = [&](double k, double *x0, double *acc, double *out, size_t idx) {
+    if (stage == 0) {
+      out[idx] = x0[idx] + c * k;
+      acc[idx] = k;
+    } else if (stage < 3) {
+      out[idx] = x0[idx] + c * k;
+      acc[idx] = acc[idx] + 2 * k;
+    } else {
+      x0[idx] = x0[idx] + c * (acc[idx] + k);
+    }
+  };
+  upd(dh, h0, ah, ho, o);
+  upd(du, u0, au, uo, o);
+  upd(dv, v0, av, vo, o);  // rows 0 (wall) .. ny-1; dv = 0 on the wall
+  if (j == ny - 1) upd(0.0, v0, av, vo, o + nx);  // the northern wall row ny
+}
+
+// ---------------------------------------------------------------- reductions (guards and diagnostics)
+// per block: sum h, sum u, sum v, energy sum, pv^2 sum; max speed, max h
+constexpr int RED_THREADS = 256;
+constexpr int RED_SUMS = 5, RED_MAXS = 2;
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(RED_THREADS) plane_reduce(PlaneDev p, const double *__restrict__ h, const double *__restrict__ u,
+                                                            const double *__restrict__ v, double *part) {
+  const int nx = p.nx, ny = p.ny;
+  const size_t ncell = static_cast<size_t>(nx) * ny, nv = static_cast<size_t>(nx) * (ny + 1);
+  double s[RED_SUMS] = {0, 0, 0, 0, 0}, mx[RED_MAXS] = {0, -INFINITY};
+  for (size_t e = blockIdx.x * (size_t)RED_THREADS + threadIdx.x; e < nv; e += (size_t)gridDim.x * RED_THREADS) {
+    s[2] += v[e];
+    if (e >= ncell) continue;
+    int j = static_cast<int>(e / nx), i = static_cast<int>(e % nx);
+    double hh = h[e];
+    s[0] += hh;
+    s[1] += u[e];
+    double uc = 0.5 * (u[e] + u[static_cast<size_t>(j) * nx + (i + 1) % nx]);
+    double vc = 0.5 * (v[e] + v[e + nx]);
+    s[3] += 0.5 * hh * (uc * uc + vc * vc) + 0.5 * p.g * hh * hh;
+    mx[0] = fmax(mx[0], hypot(uc, vc));
+    mx[1] = fmax(mx[1], hh);
+    if (j >= 1) {  // PV anomaly at interior corners, cpp/plane.cpp:228-243
+      int im = (i + nx - 1) % nx;
+      double hav = 0.25 * (h[static_cast<size_t>(j - 1) * nx + im] + h[static_cast<size_t>(j - 1) * nx + i] +
+                           h[static_cast<size_t>(j) * nx + im] + hh);
+      double dvdx = (v[e] - v[static_cast<size_t>(j) * nx + im]) / p.dxx;
+      double z = dvdx - (u[e] - u[e - nx]) / p.dyy;
+      double q = z - p.f0 * (hav - p.depth) / p.depth;
+      s[4] += q * q;
+    }
+  }
+  __shared__ double red[RED_THREADS / 32][RED_SUMS + RED_MAXS];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = 0; k < RED_SUMS; k++) s[k] = warp_sum(s[k]);
+  for (int k = 0; k < RED_MAXS; k++) mx[k] = warp_max(mx[k]);
+  if (lane == 0) {
+    for (int k = 0; k < RED_SUMS; k++) red[wid][k] = s[k];
+    for (int k = 0; k < RED_MAXS; k++) red[wid][RED_SUMS + k] = mx[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < RED_SUMS + RED_MAXS) {
+    int k = threadIdx.x;
+    double a = red[0][k];
+    for (int w = 1; w < RED_THREADS / 32; w++) a = k < RED_SUMS ? a + red[w][k] : fmax(a, red[w][k]);
+    part[static_cast<size_t>(blockIdx.x) * (RED_SUMS + RED_MAXS) + k] = a;
+  }
+}
+
+__global__ void plane_reduce_final(const double *part, int nblk, Reduce *out) {
+  int k = threadIdx.x;
+  if (k >= RED_SUMS + RED_MAXS) return;
+  double a = part[k];
+  for (int b = 1; b < nblk; b++) {
+    double x = part[static_cast<size_t>(b) * (RED_SUMS + RED_MAXS) + k];
+    a = k < RED_SUMS ? a + x : fmax(a, x);
+  }
+  if (k < RED_SUMS) out->sum[k] = a;
+  else out->max[k - RED_SUMS] = a;
+}
+
+PlaneDev make_dev(const PlaneConfig &c) {
+  PlaneDev d;
+  d.nx = c.nx;
+  d.ny = c.ny;
+  d.lin = c.linear ? 1 : 0;
+  d.dxx = c.lx / c.nx;
+  d.dyy = c.ly / c.ny;
+  d.dxx2 = d.dxx * d.dxx;
+  d.dyy2 = d.dyy * d.dyy;
+  d.g = c.gravity;
+  d.depth = c.depth;
+  d.f0 = c.f0;
+  d.beta = c.beta;
+  d.visc = c.viscosity;
+  d.drag = c.drag;
+  d.ly = c.ly;
+  return d;
+}
+
+// splitmix64 and the Irwin-Hall normal of cpp/plane.cpp:12-17,37-41 (host, for the seeded initialisers)
+uint64_t splitmix(uint64_t &x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+double irwin_hall(uint64_t &st) {
+  double s = 0;
+  for (int i = 0; i < 12; i++) s += static_cast<double>(splitmix(st) >> 11) * (1.0 / 9007199254740992.0);
+  return s - 6.0;
+}
+
+}  // namespace
+
+PlaneEngine::PlaneEngine(const PlaneConfig &c) : p(c) {
+  // cpp/plane.cpp:20-25
+  if (c.nx < 4 || c.ny < 4 || c.nx > 4000 || c.ny > 4000 || static_cast<int64_t>(c.nx) * c.ny > 8000000)
+    throw InvalidArgument("grid must be at least 4 x 4 and at most 8 million cells");
+  if (!(c.lx > 0 && c.ly > 0)) throw InvalidArgument("domain sizes must be positive");
+  LMW_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  for (DevBuf<double> *b : {&h0, &u0, &ha, &ua, &hb, &ub, &ah, &au}) b->alloc(ncell());
+  for (DevBuf<double> *b : {&v0, &va, &vb, &av}) b->alloc(nvpt());
+  nblk_red = 2 * 152;
+  part.alloc(static_cast<size_t>(nblk_red) * (RED_SUMS + RED_MAXS));
+  dred.alloc(1);
+  hred.alloc(1);
+  stage.alloc(nvpt());
+  reset();
+}
+
+PlaneEngine::~PlaneEngine() {
+  if (graph) cudaGraphExecDestroy(graph);
+  if (stream) {
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
+}
+
+void PlaneEngine::upload(double *dst, const double *src, size_t n) {
+  for (size_t off = 0; off < n; off += stage.n) {
+    size_t c = std::min(stage.n, n - off);
+    LMW_CUDA(cudaStreamSynchronize(stream));
+    std::memcpy(stage.p, src + off, c * sizeof(double));
+    LMW_CUDA(cudaMemcpyAsync(dst + off, stage.p, c * sizeof(double), cudaMemcpyHostToDevice, stream));
+  }
+  LMW_CUDA(cudaStreamSynchronize(stream));
+}
+
+// cpp/plane.cpp:27-32
+void PlaneEngine::reset() {
+  std::vector<double> hh(ncell(), p.depth);
+  upload(h0.p, hh.data(), ncell());
+  u0.zero(stream);
+  v0.zero(stream);
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  t = 0;
+}
+
+// cpp/plane.cpp:312-318
+void PlaneEngine::set_h(const double *g, size_t n) {
+  if (n != ncell()) throw InvalidArgument("grid size mismatch");
+  upload(h0.p, g, n);
+}
+void PlaneEngine::set_u(const double *g, size_t n) {
+  if (n != ncell()) throw InvalidArgument("grid size mismatch");
+  upload(u0.p, g, n);
+}
+void PlaneEngine::set_v(const double *g, size_t n) {
+  if (n != nvpt()) throw InvalidArgument("grid size mismatch");
+  std::vector<double> vv(g, g + n);
+  for (int i = 0; i < p.nx; i++) {
+    vv[i] = 0;
+    vv[static_cast<size_t>(p.ny) * p.nx + i] = 0;
+  }
+  upload(v0.p, vv.data(), n);
+}
+
+void PlaneEngine::get(double *h, double *u, double *v) {
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  if (h) LMW_CUDA(cudaMemcpy(h, h0.p, ncell() * sizeof(double), cudaMemcpyDeviceToHost));
+  if (u) LMW_CUDA(cudaMemcpy(u, u0.p, ncell() * sizeof(double), cudaMemcpyDeviceToHost));
+  if (v) LMW_CUDA(cudaMemcpy(v, v0.p, nvpt() * sizeof(double), cudaMemcpyDeviceToHost));
+}
+
+// cpp/plane.cpp:34-57: seeded smooth noise. An initialiser, run once on the host in the reference's
+// operation order (bitwise identical), then added to the device height.
+void PlaneEngine::perturb(double amplitude, uint64_t seed) {
+  const int nx = p.nx, ny = p.ny;
+  const size_t N = ncell();
+  uint64_t st = seed * 0x9E3779B97F4A7C15ULL + 777;
+  std::vector<double> n(N), tt(N), h(N);
+  for (auto &x : n) x = irwin_hall(st);
+  for (int pass = 0; pass < 3; pass++) {
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++)
+        tt[static_cast<size_t>(j) * nx + i] = 0.25 * n[static_cast<size_t>(j) * nx + (i + nx - 1) % nx] + 0.5 * n[static_cast<size_t>(j) * nx + i] +
+                                              0.25 * n[static_cast<size_t>(j) * nx + (i + 1) % nx];
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        int jm = std::max(j - 1, 0), jp = std::min(j + 1, ny - 1);
+        n[static_cast<size_t>(j) * nx + i] = 0.25 * tt[static_cast<size_t>(jm) * nx + i] + 0.5 * tt[static_cast<size_t>(j) * nx + i] +
+                                             0.25 * tt[static_cast<size_t>(jp) * nx + i];
+      }
+  }
+  double mean = 0, ms = 0;
+  for (double x : n) mean += x;
+  mean /= n.size();
+  for (double &x : n) {
+    x -= mean;
+    ms += x * x;
+  }
+  double rms = std::sqrt(ms / n.size());
+  double scale = rms > 0 ? amplitude / rms : 0;
+  get(h.data(), nullptr, nullptr);
+  for (size_t i = 0; i < N; i++) h[i] += n[i] * scale;
+  upload(h0.p, h.data(), N);
+}
+
+// Zonal jet in geostrophic balance plus white height noise (this project's benchmark initialiser; the same
+// definition as the oracle's or_plane_jet_grids).
+void PlaneEngine::jet(double u0v, double width, double noise_rms, uint64_t seed) {
+  const int nx = p.nx, ny = p.ny;
+  const double dyy = dy();
+  auto cor = [&](double y) { return p.f0 + p.beta * (y - 0.5 * p.ly); };
+  std::vector<double> prof(ny), hy(ny);
+  for (int j = 0; j < ny; j++) {
+    double y = (j + 0.5) * dyy;
+    double c = std::cosh((y - 0.5 * p.ly) / width);
+    prof[j] = u0v / (c * c);
+  }
+  hy[0] = 0;
+  for (int j = 1; j < ny; j++) {
+    double fa = cor((j - 0.5) * dyy) * prof[j - 1], fb = cor((j + 0.5) * dyy) * prof[j];
+    hy[j] = hy[j - 1] - dyy / p.gravity * 0.5 * (fa + fb);
+  }
+  double mean = 0;
+  for (int j = 0; j < ny; j++) mean += hy[j];
+  mean /= ny;
+  const size_t N = ncell();
+  std::vector<double> noise(N), h(N), u(N);
+  uint64_t st = seed * 0x9E3779B97F4A7C15ULL + 777;
+  for (auto &x : noise) x = irwin_hall(st);
+  double nm = 0, ms = 0;
+  for (double x : noise) nm += x;
+  nm /= N;
+  for (double &x : noise) {
+    x -= nm;
+    ms += x * x;
+  }
+  double rms = std::sqrt(ms / N);
+  double sc = rms > 0 ? noise_rms / rms : 0;
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      size_t k = static_cast<size_t>(j) * nx + i;
+      h[k] = p.depth + (hy[j] - mean) + noise[k] * sc;
+      u[k] = prof[j];
+    }
+  upload(h0.p, h.data(), N);
+  upload(u0.p, u.data(), N);
+  v0.zero(stream);
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  t = 0;
+}
+
+void PlaneEngine::enqueue_step(double dt) {
+  PlaneDev d = make_dev(p);
+  dim3 grid((p.nx + TX - 1) / TX, (p.ny + TY - 1) / TY), block(TX, TY);
+  const double half = 0.5 * dt, c6 = dt / 6;
+  // stage inputs: x0 -> a -> b -> a
+  plane_stage<<<grid, block, 0, stream>>>(d, 0, half, h0.p, u0.p, v0.p, h0.p, u0.p, v0.p, ah.p, au.p, av.p, ha.p, ua.p, va.p);
+  plane_stage<<<grid, block, 0, stream>>>(d, 1, half, ha.p, ua.p, va.p, h0.p, u0.p, v0.p, ah.p, au.p, av.p, hb.p, ub.p, vb.p);
+  plane_stage<<<grid, block, 0, stream>>>(d, 2, dt, hb.p, ub.p, vb.p, h0.p, u0.p, v0.p, ah.p, au.p, av.p, ha.p, ua.p, va.p);
+  plane_stage<<<grid, block, 0, stream>>>(d, 3, c6, ha.p, ua.p, va.p, h0.p, u0.p, v0.p, ah.p, au.p, av.p, nullptr, nullptr, nullptr);
+  LMW_LAUNCH_CHECK();
+  g_launches += 4;
+}
+
+// a chunk of RK4 steps as one CUDA graph (captured once per step size and chunk length)
+void PlaneEngine::launch_chunk(double dt, int steps) {
+  if (steps <= 0) return;
+  if (!graph || graph_dt != dt || graph_steps != steps) {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    cudaGraph_t g;
+    uint64_t before = g_launches;
+    LMW_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < steps; s++) enqueue_step(dt);
+    LMW_CUDA(cudaStreamEndCapture(stream, &g));
+    g_launches = before;
+    LMW_CUDA(cudaGraphInstantiate(&graph, g, 0));
+    cudaGraphDestroy(g);
+    graph_dt = dt;
+    graph_steps = steps;
+  }
+  LMW_CUDA(cudaGraphLaunch(graph, stream));
+  g_launches += 4ull * steps;
+}
+
+double PlaneEngine::kernel_time(double dt, int reps) {
+  PlaneDev d = make_dev(p);
+  dim3 grid((p.nx + TX - 1) / TX, (p.ny + TY - 1) / TY), block(TX, TY);
+  cudaEvent_t e0, e1;
+  LMW_CUDA(cudaEventCreate(&e0));
+  LMW_CUDA(cudaEventCreate(&e1));
+  // stage 1 reads the base state and stage input a, writes stage input b and the accumulator: x0 is untouched
+  plane_stage<<<grid, block, 0, stream>>>(d, 1, 0.5 * dt, ha.p, ua.p, va.p, h0.p, u0.p, v0.p, ah.p, au.p, av.p, hb.p, ub.p, vb.p);
+  LMW_CUDA(cudaEventRecord(e0, stream));
+  for (int r = 0; r < reps; r++)
+    plane_stage<<<grid, block, 0, stream>>>(d, 1, 0.5 * dt, ha.p, ua.p, va.p, h0.p, u0.p, v0.p, ah.p, au.p, av.p, hb.p, ub.p, vb.p);
+  LMW_CUDA(cudaEventRecord(e1, stream));
+  LMW_LAUNCH_CHECK();
+  LMW_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  LMW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  g_launches += reps + 1;
+  return ms / reps;
+}
+
+void PlaneEngine::step(double dt) {
+  enqueue_step(dt);
+  t += dt;
+  LMW_CUDA(cudaStreamSynchronize(stream));
+}
+
+void PlaneEngine::reduce(Reduce &r) {
+  PlaneDev d = make_dev(p);
+  plane_reduce<<<nblk_red, RED_THREADS, 0, stream>>>(d, h0.p, u0.p, v0.p, part.p);
+  plane_reduce_final<<<1, 32, 0, stream>>>(part.p, nblk_red, dred.p);
+  LMW_LAUNCH_CHECK();
+  g_launches += 2;
+  LMW_CUDA(cudaMemcpyAsync(hred.p, dred.p, sizeof(Reduce), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  r = *hred.p;
+}
+
+// cpp/plane.cpp:131-141
+double PlaneEngine::stable_dt(double safety) {
+  double hmax = p.linear ? p.depth : 0, umax = 0;
+  if (!p.linear) {
+    Reduce r;
+    reduce(r);
+    umax = r.max[0];
+    hmax = std::max(hmax, r.max[1]);
+  }
+  if (!(hmax > 0)) throw RuntimeError("the depth must be positive to step the model");
+  double c = std::sqrt(p.gravity * hmax) + umax;
+  double inv = c * std::sqrt(1.0 / (dx() * dx()) + 1.0 / (dy() * dy()));
+  double visc = p.viscosity * (4.0 / (dx() * dx()) + 4.0 / (dy() * dy()));
+  return safety * 2.0 / (inv + visc + std::fabs(p.f0) + std::fabs(p.beta) * p.ly);
+}
+
+// cpp/plane.cpp:160-189
+void PlaneEngine::run(double seconds, double dt) {
+  if (!(seconds >= 0)) throw InvalidArgument("run: seconds must not be negative");
+  if (seconds == 0) return;
+  if (!(dt > 0)) dt = stable_dt(0.5);
+  const double limit = stable_dt(std::sqrt(0.5));
+  if (!(dt <= limit))
+    throw InvalidArgument("run: dt = " + fmt_f(dt) + " s exceeds the RK4 stability limit of about " + fmt_f(limit) +
+                          " s for the present state: use a smaller dt");
+  int64_t n = static_cast<int64_t>(std::ceil(seconds / dt - 1e-9));
+  if (n < 1) n = 1;
+  if (n > 200000000) throw InvalidArgument("run: too many steps; use a larger dt");
+  double hstep = seconds / static_cast<double>(n);
+  int64_t i = 0;
+  while (i < n) {
+    // steps up to and including the next guard point ((i & 63) == 63 or the last step)
+    int64_t next = std::min<int64_t>(n - 1, i | 63);
+    int chunk = static_cast<int>(next - i + 1);
+    if (chunk == 64) launch_chunk(hstep, 64);
+    else for (int s = 0; s < chunk; s++) enqueue_step(hstep);
+    for (int s = 0; s < chunk; s++) t += hstep;
+    i = next + 1;
+    Reduce r;
+    reduce(r);
+    double s = r.sum[0] + r.sum[1] + r.sum[2];
+    if (!std::isfinite(s)) throw RuntimeError("the integration blew up (not finite): use a smaller dt");
+    const double now = stable_dt(std::sqrt(0.5));
+    if (!(hstep <= now))
+      throw RuntimeError("run: dt = " + fmt_f(hstep) + " s exceeds the RK4 stability limit of about " + fmt_f(now) + " s reached at t = " +
+                         fmt_f(t) + " s (the flow accelerated): use a smaller dt");
+  }
+}
+
+// cpp/plane.cpp:191-243: mean_depth, energy, max_speed, pv_anomaly_rms
+void PlaneEngine::diagnostics(double *out) {
+  Reduce r;
+  reduce(r);
+  const double N = static_cast<double>(ncell());
+  out[0] = r.sum[0] / N;
+  out[1] = r.sum[3] / N;
+  out[2] = r.max[0];
+  out[3] = std::sqrt(r.sum[4] / static_cast<double>(static_cast<size_t>(p.nx) * (p.ny - 1)));
+}
+
+}  // namespace lmw

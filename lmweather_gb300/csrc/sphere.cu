@@ -1,0 +1,1084 @@
+// Spectral-transform shallow water on the sphere (the lmweather Sphere model, cpp/sphere.cpp), FP64 path.
+//
+// Per RK4 stage three kernels run on the engine stream:
+//   sph_synth     per zonal wavenumber m (paired with T-m for load balance) and southern latitude jh: the
+//                 six Legendre synthesis sums (psi P, chi P, psi H, chi H, zeta P, Phi P) split by the parity of
+//                 n-m, which gives both mirror latitudes at once (hemispheric fold); writes the Fourier
+//                 coefficients of U, V, zeta, Phi for both latitudes.
+//   sph_grid      per latitude pair: the two latitudes ride in the real and imaginary parts of one complex
+//                 FFT; inverse FFTs of U, V, zeta, Phi, the nonlinear products of cpp/sphere.cpp:348-359 in
+//                 place, forward FFTs of the five products, then the quadrature weights and the fold
+//                 (sum/difference of the mirror latitudes). The grid never leaves shared memory.
+//   sph_analysis  per spectral coefficient (m, n): the seven folded Legendre analysis sums, the tendencies
+//                 of cpp/sphere.cpp:372-389 and the RK4 stage update (cpp/sphere.cpp:416-434) with the del^4
+//                 filter fused into the last stage.
+// Layouts: state x[member][field][tri] complex128, tri(m, n) = packed triangle offset; Fourier
+// coefficients four[member][lat][field][m]; folded analysis inputs fold[member][jh][slot][parity][m].
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+
+#include "engine.h"
+#include "sphere_tables.h"
+
+namespace lmw {
+
+struct SphereTables {
+  HostTables host;
+  DevBuf<double> Ps, Hs, Pa, Ha;  // coefficient-major [tri][jh] (synthesis) and latitude-major [jh][tri] (analysis)
+  DevBuf<double> mu, w, wd, cosl;
+  DevBuf<double2> tw;  // exp(-2 pi i k / nlon), k < nlon/2
+  DevBuf<int> trim, trin, tri;
+};
+
+namespace {
+
+struct SphDev {
+  int N, M, nlat, nlon, nh, ntri, logn;
+  double a, g;
+  const double *Ps, *Hs, *Pa, *Ha, *mu, *w, *wd, *cosl;
+  const double2 *tw;
+  const int *trim, *trin, *tri;
+};
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ __forceinline__ double2 cfma(double2 acc, double2 a, double s) { return make_double2(fma(a.x, s, acc.x), fma(a.y, s, acc.y)); }
+__device__ __forceinline__ double2 conjd(double2 a) { return make_double2(a.x, -a.y); }
+// (i m) z
+__device__ __forceinline__ double2 imul(double2 z, double m) { return make_double2(-m * z.y, m * z.x); }
+
+// ------------------------------------------------------------------------------------------------ synthesis
+constexpr int SYN_THREADS = 64;
+
+// x: [B][3][ntri] (zeta, delta, phi); four: [B][nlat][4][M] (U, V, zeta, Phi)
+__global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, const double2 *__restrict__ x, double2 *__restrict__ four) {
+  const int b = blockIdx.z, pair = blockIdx.y;
+  const int jh = blockIdx.x * SYN_THREADS + threadIdx.x;
+  if (jh >= d.nh) return;
+  const double2 *xz = x + static_cast<size_t>(b) * 3 * d.ntri, *xd = xz + d.ntri, *xf = xd + d.ntri;
+  const int js = jh, jn = d.nlat - 1 - jh;
+  const double aa = -d.a * d.a;
+  for (int pass = 0; pass < 2; pass++) {
+    const int m = pass == 0 ? pair : d.N - pair;
+    if (pass == 1 && m == pair) break;
+    double2 sp[2], sc[2], hp[2], hc[2], zs[2], fs[2];
+    for (int e = 0; e < 2; e++) sp[e] = sc[e] = hp[e] = hc[e] = zs[e] = fs[e] = make_double2(0, 0);
+    const int base = d.tri[m];
+    // n - m even terms accumulate in [0], odd terms in [1] (constant indices after unrolling by two)
+#define LMW_SYN_TERM(PAR, NN)                                                                     \
+  {                                                                                               \
+    const int q = base + (NN) - m;                                                                \
+    const double P = d.Ps[static_cast<size_t>(q) * d.nh + jh], H = d.Hs[static_cast<size_t>(q) * d.nh + jh]; \
+    const double2 z = xz[q], dl = xd[q], f = xf[q];                                               \
+    const double k = (NN) > 0 ? aa / ((NN) * ((NN) + 1.0)) : 0.0;                                 \
+    const double2 psi = cscale(z, k), chi = cscale(dl, k);                                        \
+    sp[PAR] = cfma(sp[PAR], psi, P);                                                              \
+    sc[PAR] = cfma(sc[PAR], chi, P);                                                              \
+    hp[PAR] = cfma(hp[PAR], psi, H);                                                              \
+    hc[PAR] = cfma(hc[PAR], chi, H);                                                              \
+    zs[PAR] = cfma(zs[PAR], z, P);                                                                \
+    fs[PAR] = cfma(fs[PAR], f, P);                                                                \
+  }
+    int n = m;
+    for (; n + 1 <= d.N; n += 2) {
+      LMW_SYN_TERM(0, n)
+      LMW_SYN_TERM(1, n + 1)
+    }
+    if (n <= d.N) LMW_SYN_TERM(0, n)
+#undef LMW_SYN_TERM
+    const double mm = static_cast<double>(m);
+    // southern latitude: even + odd; northern mirror: P sums even - odd, H sums odd - even
+    for (int side = 0; side < 2; side++) {
+      const int j = side == 0 ? js : jn;
+      double2 SP, SC, HP, HC, Z, F;
+      if (side == 0) {
+        SP = cadd(sp[0], sp[1]); SC = cadd(sc[0], sc[1]); HP = cadd(hp[0], hp[1]); HC = cadd(hc[0], hc[1]);
+        Z = cadd(zs[0], zs[1]); F = cadd(fs[0], fs[1]);
+      } else {
+        SP = csub(sp[0], sp[1]); SC = csub(sc[0], sc[1]); HP = csub(hp[1], hp[0]); HC = csub(hc[1], hc[0]);
+        Z = csub(zs[0], zs[1]); F = csub(fs[0], fs[1]);
+      }
+      // cpp/sphere.cpp:200-201: fu = (i m sc - hp)/a, fv = (i m sp + hc)/a
+      double2 fu = csub(imul(SC, mm), HP), fv = cadd(imul(SP, mm), HC);
+      fu = make_double2(fu.x / d.a, fu.y / d.a);
+      fv = make_double2(fv.x / d.a, fv.y / d.a);
+      double2 *o = four + (static_cast<size_t>(b) * d.nlat + j) * 4 * d.M;
+      o[0 * d.M + m] = fu;
+      o[1 * d.M + m] = fv;
+      o[2 * d.M + m] = Z;
+      o[3 * d.M + m] = F;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------ FFTs
+// Radix-2 complex FFTs over `rows` rows of length n in shared memory, all threads of the block cooperating.
+// Inverse: decimation in time from bit-reversed input to natural output. Forward: decimation in frequency
+// from natural input to bit-reversed output. Twiddles exp(-2 pi i k / n) from the table (conjugated for the
+// inverse), computed on the host in FP64.
+__device__ void fft_inverse_dit(double2 *s, int rows, int n, int logn, const double2 *__restrict__ tw) {
+  const int halfn = n >> 1;
+  for (int st = 0; st < logn; st++) {
+    const int half = 1 << st, stride = halfn >> st;
+    for (int e = threadIdx.x; e < rows * halfn; e += blockDim.x) {
+      const int r = e / halfn, bf = e - r * halfn;
+      const int grp = bf >> st, pos = bf & (half - 1);
+      const int i1 = grp * 2 * half + pos, i2 = i1 + half;
+      double2 *row = s + static_cast<size_t>(r) * n;
+      const double2 w = conjd(tw[pos * stride]);
+      const double2 t = cmul(w, row[i2]), u = row[i1];
+      row[i1] = cadd(u, t);
+      row[i2] = csub(u, t);
+    }
+    __syncthreads();
+  }
+}
+__device__ void fft_forward_dif(double2 *s, int rows, int n, int logn, const double2 *__restrict__ tw) {
+  const int halfn = n >> 1;
+  for (int st = logn - 1; st >= 0; st--) {
+    const int half = 1 << st, stride = halfn >> st;
+    for (int e = threadIdx.x; e < rows * halfn; e += blockDim.x) {
+      const int r = e / halfn, bf = e - r * halfn;
+      const int grp = bf >> st, pos = bf & (half - 1);
+      const int i1 = grp * 2 * half + pos, i2 = i1 + half;
+      double2 *row = s + static_cast<size_t>(r) * n;
+      const double2 u = row[i1], v = row[i2];
+      row[i1] = cadd(u, v);
+      row[i2] = cmul(csub(u, v), tw[pos * stride]);
+    }
+    __syncthreads();
+  }
+}
+__device__ __forceinline__ int bitrev(int k, int logn) { return static_cast<int>(__brev(static_cast<unsigned>(k)) >> (32 - logn)); }
+
+// Load the Fourier coefficients of `rows` fields at latitudes js (real part) and jn (imaginary part) into
+// bit-reversed rows: Y[m] = X_s[m] + i X_n[m], Y[n-m] = conj(X_s[m]) + i conj(X_n[m]); Im X[0] is dropped
+// as in cpp/sphere.cpp:132.
+__device__ void load_pair_spectra(double2 *s, int rows, const SphDev &d, const double2 *__restrict__ fs,
+                                  const double2 *__restrict__ fn, int fstride) {
+  const int n = d.nlon;
+  for (int e = threadIdx.x; e < rows * n; e += blockDim.x) s[e] = make_double2(0, 0);
+  __syncthreads();
+  for (int e = threadIdx.x; e < rows * d.M; e += blockDim.x) {
+    const int r = e / d.M, m = e - r * d.M;
+    double2 a = fs[r * fstride + m], c = fn[r * fstride + m];
+    double2 *row = s + static_cast<size_t>(r) * n;
+    if (m == 0) {
+      row[0] = make_double2(a.x, c.x);
+    } else {
+      row[bitrev(m, d.logn)] = make_double2(a.x - c.y, a.y + c.x);
+      row[bitrev(n - m, d.logn)] = make_double2(a.x + c.y, c.x - a.y);
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------------------------------ grid stage
+constexpr int GRID_THREADS = 256;
+constexpr int NSLOT = 5;  // A, B, U Phi, V Phi (times w/((1-mu^2)a)) and the Bernoulli function (times w)
+
+// four: [B][nlat][4][M]; fold: [B][nh][NSLOT][2][M]; fgrid/hsgrid: [B][nlat][nlon]
+__global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, const double2 *__restrict__ four, const double *__restrict__ fgrid,
+                                                         const double *__restrict__ hsgrid, double2 *__restrict__ fold) {
+  extern __shared__ double2 sm[];
+  const int b = blockIdx.y, jh = blockIdx.x;
+  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
+  const double2 *f_s = four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M;
+  const double2 *f_n = four + (static_cast<size_t>(b) * d.nlat + jn) * 4 * d.M;
+  load_pair_spectra(sm, 4, d, f_s, f_n, d.M);
+  fft_inverse_dit(sm, 4, n, d.logn, d.tw);
+  // nonlinear products, cpp/sphere.cpp:348-359 (real part: southern latitude, imaginary part: northern)
+  const double om = 1 - d.mu[js] * d.mu[js];  // the same at the mirror latitude
+  const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
+  const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
+  double2 *rU = sm, *rV = sm + n, *rZ = sm + 2 * n, *rP = sm + 3 * n, *rE = sm + 4 * n;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double2 U = rU[k], V = rV[k], Z = rZ[k], P = rP[k];
+    double2 A, Bv, UP, VP, PE;
+    {
+      double eta = Z.x + fr_s[k];
+      A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
+      PE.x = P.x + d.g * hr_s[k] + (U.x * U.x + V.x * V.x) / (2 * om);
+    }
+    {
+      double eta = Z.y + fr_n[k];
+      A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
+      PE.y = P.y + d.g * hr_n[k] + (U.y * U.y + V.y * V.y) / (2 * om);
+    }
+    rU[k] = A; rV[k] = Bv; rZ[k] = UP; rP[k] = VP; rE[k] = PE;
+  }
+  __syncthreads();
+  fft_forward_dif(sm, NSLOT, n, d.logn, d.tw);
+  // separate the two latitudes, normalise by nlon (cpp/sphere.cpp:128), weight and fold
+  const double inv = 1.0 / n, wd = d.wd[js], wj = d.w[js];
+  double2 *o = fold + (static_cast<size_t>(b) * d.nh + jh) * NSLOT * 2 * d.M;
+  for (int e = threadIdx.x; e < NSLOT * d.M; e += blockDim.x) {
+    const int r = e / d.M, m = e - r * d.M;
+    const double2 *row = sm + static_cast<size_t>(r) * n;
+    const double2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
+    // X_s = (Ym + conj(Y_{n-m}))/2, X_n = -i (Ym - conj(Y_{n-m}))/2
+    double2 Xs = cscale(cadd(Ym, Yc), 0.5 * inv);
+    double2 t = csub(Ym, Yc);
+    double2 Xn = make_double2(0.5 * inv * t.y, -0.5 * inv * t.x);
+    const double wt = r < 4 ? wd : wj;
+    Xs = cscale(Xs, wt);
+    Xn = cscale(Xn, wt);
+    o[(r * 2 + 0) * d.M + m] = cadd(Xs, Xn);
+    o[(r * 2 + 1) * d.M + m] = csub(Xs, Xn);
+  }
+}
+
+// ------------------------------------------------------------------------------------------------ analysis + RK4
+constexpr int ANA_THREADS = 64;
+
+struct StageArgs {
+  int stage;        // 0..3
+  double c;         // 0.5 dt, 0.5 dt, dt, dt/6
+  const double *filt;  // [2][M]: zeta/delta and phi factors by n (last stage)
+};
+
+// x0: state, xs: stage input (written for stages 0-2), acc: RK4 accumulator. All [B][3][ntri].
+__global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, const double2 *__restrict__ fold, StageArgs sa, double2 *x0,
+                                                            double2 *xs, double2 *acc) {
+  const int b = blockIdx.y;
+  const int q = blockIdx.x * ANA_THREADS + threadIdx.x;
+  if (q >= d.ntri) return;
+  const int m = d.trim[q], n = d.trin[q], par = (n - m) & 1;
+  const double2 *fb = fold + static_cast<size_t>(b) * d.nh * NSLOT * 2 * d.M;
+  const int sP = par * d.M + m, sH = (1 - par) * d.M + m;  // parity slot for P and H terms
+  double2 aP = make_double2(0, 0), bH = aP, bP = aP, aH = aP, uP = aP, vH = aP, eP = aP;
+  for (int jh = 0; jh < d.nh; jh++) {
+    const double P = d.Pa[static_cast<size_t>(jh) * d.ntri + q], H = d.Ha[static_cast<size_t>(jh) * d.ntri + q];
+    const double2 *g = fb + static_cast<size_t>(jh) * NSLOT * 2 * d.M;
+    aP = cfma(aP, g[0 * 2 * d.M + sP], P);
+    aH = cfma(aH, g[0 * 2 * d.M + sH], H);
+    bP = cfma(bP, g[1 * 2 * d.M + sP], P);
+    bH = cfma(bH, g[1 * 2 * d.M + sH], H);
+    uP = cfma(uP, g[2 * 2 * d.M + sP], P);
+    vH = cfma(vH, g[3 * 2 * d.M + sH], H);
+    eP = cfma(eP, g[4 * 2 * d.M + sP], P);
+  }
+  const double mm = static_cast<double>(m);
+  // cpp/sphere.cpp:380-383: dz = -D(A,B), dd = D(B,-A) + n(n+1)/a^2 (Phi + E), df = -D(U Phi, V Phi)
+  double2 kz = csub(bH, imul(aP, mm));
+  double2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, n * (n + 1.0) / (d.a * d.a)));
+  double2 kf = csub(vH, imul(uP, mm));
+  if (q == 0) kz = kd = kf = make_double2(0, 0);  // cpp/sphere.cpp:387-389
+  const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
+  const double2 k[3] = {kz, kd, kf};
+  for (int f = 0; f < 3; f++) {
+    const size_t i = base + static_cast<size_t>(f) * d.ntri;
+    if (sa.stage == 0) {
+      acc[i] = k[f];
+      xs[i] = cadd(x0[i], cscale(k[f], sa.c));
+    } else if (sa.stage < 3) {
+      acc[i] = cadd(acc[i], cscale(k[f], 2.0));
+      xs[i] = cadd(x0[i], cscale(k[f], sa.c));
+    } else {
+      // cpp/sphere.cpp:428-434: x += dt/6 (k1 + 2k2 + 2k3 + k4), then the del^4 filter
+      double2 v = cadd(x0[i], cscale(cadd(acc[i], k[f]), sa.c));
+      const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
+      x0[i] = q == 0 ? v : cscale(v, fac);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------ grid analysis
+// set_state_grid on the device (cpp/sphere.cpp:208-234): U = u cos, V = v cos, Phi = g h, forward FFTs,
+// weights and fold into slots (U wd, V wd, Phi w).
+__global__ void __launch_bounds__(GRID_THREADS) sph_grid_in(SphDev d, const double *__restrict__ h, const double *__restrict__ u,
+                                                            const double *__restrict__ v, double2 *__restrict__ fold) {
+  extern __shared__ double2 sm[];
+  const int jh = blockIdx.x, js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
+  const double c = d.cosl[js];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    size_t os = static_cast<size_t>(js) * n + k, on = static_cast<size_t>(jn) * n + k;
+    sm[k] = make_double2(u[os] * c, u[on] * c);
+    sm[n + k] = make_double2(v[os] * c, v[on] * c);
+    sm[2 * n + k] = make_double2(d.g * h[os], d.g * h[on]);
+  }
+  __syncthreads();
+  fft_forward_dif(sm, 3, n, d.logn, d.tw);
+  const double inv = 1.0 / n, wd = d.wd[js], wj = d.w[js];
+  double2 *o = fold + static_cast<size_t>(jh) * 3 * 2 * d.M;
+  for (int e = threadIdx.x; e < 3 * d.M; e += blockDim.x) {
+    const int r = e / d.M, m = e - r * d.M;
+    const double2 *row = sm + static_cast<size_t>(r) * n;
+    const double2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
+    double2 Xs = cscale(cadd(Ym, Yc), 0.5 * inv);
+    double2 t = csub(Ym, Yc);
+    double2 Xn = make_double2(0.5 * inv * t.y, -0.5 * inv * t.x);
+    const double wt = r < 2 ? wd : wj;
+    Xs = cscale(Xs, wt);
+    Xn = cscale(Xn, wt);
+    o[(r * 2 + 0) * d.M + m] = cadd(Xs, Xn);
+    o[(r * 2 + 1) * d.M + m] = csub(Xs, Xn);
+  }
+}
+
+// zeta = D(V, -U), delta = D(U, V) with (0,0) = 0, Phi = analysis(g h): written to the member's state
+__global__ void __launch_bounds__(ANA_THREADS) sph_analysis_in(SphDev d, const double2 *__restrict__ fold, double2 *x) {
+  const int q = blockIdx.x * ANA_THREADS + threadIdx.x;
+  if (q >= d.ntri) return;
+  const int m = d.trim[q], n = d.trin[q], par = (n - m) & 1;
+  const int sP = par * d.M + m, sH = (1 - par) * d.M + m;
+  double2 uP = make_double2(0, 0), uH = uP, vP = uP, vH = uP, pP = uP;
+  for (int jh = 0; jh < d.nh; jh++) {
+    const double P = d.Pa[static_cast<size_t>(jh) * d.ntri + q], H = d.Ha[static_cast<size_t>(jh) * d.ntri + q];
+    const double2 *g = fold + static_cast<size_t>(jh) * 3 * 2 * d.M;
+    uP = cfma(uP, g[0 * 2 * d.M + sP], P);
+    uH = cfma(uH, g[0 * 2 * d.M + sH], H);
+    vP = cfma(vP, g[1 * 2 * d.M + sP], P);
+    vH = cfma(vH, g[1 * 2 * d.M + sH], H);
+    pP = cfma(pP, g[2 * 2 * d.M + sP], P);
+  }
+  const double mm = static_cast<double>(m);
+  double2 z = cadd(imul(vP, mm), uH);   // D(V, -U) = sum wd (i m V P + U H)
+  double2 dl = csub(imul(uP, mm), vH);  // D(U, V) = sum wd (i m U P - V H)
+  if (q == 0) z = dl = make_double2(0, 0);
+  x[q] = z;
+  x[d.ntri + q] = dl;
+  x[2 * static_cast<size_t>(d.ntri) + q] = pP;
+}
+
+// ------------------------------------------------------------------------------------------------ diagnostics
+// Per latitude pair: inverse FFTs of U, V, zeta, Phi; per-row sums of cpp/sphere.cpp:514-590 and maxima.
+// rows: [B][nlat][DIAG_K]: KE row, PE row, enstrophy row, error num row, error den row, max wind, max h,
+// max |h - ref|, max |ref|. Optional grids out: [4][nlat][nlon] (h, u, v, zeta) for member 0 of the call.
+constexpr int DIAG_K = 9;
+
+__device__ __forceinline__ double block_sum(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double s = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += red[i];
+  return s;
+}
+__device__ __forceinline__ double block_max(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double s = -INFINITY;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s = fmax(s, red[i]);
+  return s;
+}
+
+__global__ void __launch_bounds__(GRID_THREADS) sph_diag(SphDev d, const double2 *__restrict__ four, const double *__restrict__ fgrid,
+                                                         const double *__restrict__ hsgrid, const double *__restrict__ refgrid,
+                                                         double *__restrict__ rows, double *__restrict__ grids) {
+  extern __shared__ double2 sm[];
+  __shared__ double red[GRID_THREADS / 32];
+  const int b = blockIdx.y, jh = blockIdx.x;
+  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
+  const double2 *f_s = four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M;
+  const double2 *f_n = four + (static_cast<size_t>(b) * d.nlat + jn) * 4 * d.M;
+  load_pair_spectra(sm, 4, d, f_s, f_n, d.M);
+  fft_inverse_dit(sm, 4, n, d.logn, d.tw);
+  const double c = d.cosl[js];
+  for (int side = 0; side < 2; side++) {
+    const int j = side == 0 ? js : jn;
+    const size_t go = (static_cast<size_t>(b) * d.nlat + j) * n;
+    double acc[5] = {0, 0, 0, 0, 0}, mx[4] = {0, -INFINITY, 0, 0};
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const double2 U = sm[k], V = sm[n + k], Z = sm[2 * n + k], P = sm[3 * n + k];
+      const double Uv = side ? U.y : U.x, Vv = side ? V.y : V.x, Zv = side ? Z.y : Z.x, Pv = side ? P.y : P.x;
+      const double h = Pv / d.g, u = Uv / c, v = Vv / c;
+      const double f = fgrid[go + k], hs = hsgrid[go + k];
+      acc[0] += 0.5 * h * (u * u + v * v);
+      acc[1] += 0.5 * d.g * h * h + d.g * h * hs;
+      acc[2] += 0.5 * (Zv + f) * (Zv + f) / h;
+      const double r = refgrid[go + k] / d.g, dd = h - r;
+      acc[3] += dd * dd;
+      acc[4] += r * r;
+      mx[0] = fmax(mx[0], hypot(u, v));
+      mx[1] = fmax(mx[1], h);
+      mx[2] = fmax(mx[2], fabs(dd));
+      mx[3] = fmax(mx[3], fabs(r));
+      if (grids) {
+        const size_t gi = static_cast<size_t>(j) * n + k, ng = static_cast<size_t>(d.nlat) * n;
+        grids[gi] = h;
+        grids[ng + gi] = u;
+        grids[2 * ng + gi] = v;
+        grids[3 * ng + gi] = Zv;
+      }
+    }
+    double out[DIAG_K];
+    for (int i = 0; i < 5; i++) out[i] = block_sum(acc[i], red);
+    for (int i = 0; i < 4; i++) out[5 + i] = block_max(mx[i], red);
+    if (threadIdx.x == 0)
+      for (int i = 0; i < DIAG_K; i++) rows[(static_cast<size_t>(b) * d.nlat + j) * DIAG_K + i] = out[i];
+  }
+}
+
+// Per member: area means sum_j w_j row_j / nlon (cpp/sphere.cpp:520), error norms, and sum |coefficient|
+// (cpp/sphere.cpp:449-455).
+__global__ void __launch_bounds__(GRID_THREADS) sph_diag_final(SphDev d, const double *__restrict__ rows, const double2 *__restrict__ x,
+                                                               int member0, Reduce *out) {
+  __shared__ double red[GRID_THREADS / 32];
+  const int b = member0 + blockIdx.x;
+  const double2 *xb = x + static_cast<size_t>(b) * 3 * d.ntri;
+  double s = 0;
+  for (int i = threadIdx.x; i < 3 * d.ntri; i += blockDim.x) s += hypot(xb[i].x, xb[i].y);
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) {
+    Reduce r;
+    double ke = 0, pe = 0, en = 0, num = 0, den = 0, wmax = 0, hmax = -INFINITY, dmax = 0, rmax = 0;
+    for (int j = 0; j < d.nlat; j++) {
+      const double *rw = rows + (static_cast<size_t>(b) * d.nlat + j) * DIAG_K;
+      ke += d.w[j] * rw[0] / d.nlon;
+      pe += d.w[j] * rw[1] / d.nlon;
+      en += d.w[j] * rw[2] / d.nlon;
+      num += d.w[j] * rw[3];
+      den += d.w[j] * rw[4];
+      wmax = fmax(wmax, rw[5]);
+      hmax = fmax(hmax, rw[6]);
+      dmax = fmax(dmax, rw[7]);
+      rmax = fmax(rmax, rw[8]);
+    }
+    r.sum[0] = 0.5 * ke;
+    r.sum[1] = 0.5 * pe;
+    r.sum[2] = 0.5 * en;
+    r.sum[3] = num;
+    r.sum[4] = den;
+    r.sum[5] = s;
+    r.sum[6] = r.sum[7] = 0;
+    r.max[0] = wmax;
+    r.max[1] = hmax;
+    r.max[2] = dmax;
+    r.max[3] = rmax;
+    out[blockIdx.x] = r;
+  }
+}
+
+// synthesis of a single field's grid (reference grid for mark_reference): Phi rows of `four` -> grid
+__global__ void __launch_bounds__(GRID_THREADS) sph_phi_grid(SphDev d, const double2 *__restrict__ four, double *__restrict__ out) {
+  extern __shared__ double2 sm[];
+  const int b = blockIdx.y, jh = blockIdx.x;
+  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
+  const double2 *f_s = four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M + 3 * d.M;
+  const double2 *f_n = four + (static_cast<size_t>(b) * d.nlat + jn) * 4 * d.M + 3 * d.M;
+  load_pair_spectra(sm, 1, d, f_s, f_n, d.M);
+  fft_inverse_dit(sm, 1, n, d.logn, d.tw);
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    out[(static_cast<size_t>(b) * d.nlat + js) * n + k] = sm[k].x;
+    out[(static_cast<size_t>(b) * d.nlat + jn) * n + k] = sm[k].y;
+  }
+}
+
+const double kPi = 3.14159265358979323846;
+
+uint64_t splitmix(uint64_t &x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+double irwin_hall(uint64_t &st) {
+  double s = 0;
+  for (int i = 0; i < 12; i++) s += static_cast<double>(splitmix(st) >> 11) * (1.0 / 9007199254740992.0);
+  return s - 6.0;
+}
+
+}  // namespace
+
+// ================================================================================================ engine
+
+static SphDev make_sph(const SphereEngine &e, const SphereTables &t) {
+  SphDev d;
+  d.N = e.N;
+  d.M = e.M;
+  d.nlat = e.nlat;
+  d.nlon = e.nlon;
+  d.nh = e.nh;
+  d.ntri = e.ntri;
+  d.logn = 0;
+  while ((1 << d.logn) < e.nlon) d.logn++;
+  d.a = e.p.radius;
+  d.g = e.p.gravity;
+  d.Ps = t.Ps.p;
+  d.Hs = t.Hs.p;
+  d.Pa = t.Pa.p;
+  d.Ha = t.Ha.p;
+  d.mu = t.mu.p;
+  d.w = t.w.p;
+  d.wd = t.wd.p;
+  d.cosl = t.cosl.p;
+  d.tw = t.tw.p;
+  d.trim = t.trim.p;
+  d.trin = t.trin.p;
+  d.tri = t.tri.p;
+  return d;
+}
+
+SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
+  // cpp/sphere.cpp:75-103
+  if (c.truncation < 4 || c.truncation > c.max_truncation)
+    throw InvalidArgument("truncation must be between 4 and " + std::to_string(c.max_truncation));
+  if (c.members < 1) throw InvalidArgument("an ensemble needs at least one member");
+  if (c.precision != kFP64) throw InvalidArgument("precision mode not available in this build");
+  B = c.members;
+  tab = new SphereTables();
+  HostTables &h = tab->host;
+  h.build(c.truncation);
+  N = h.N;
+  M = h.M;
+  nlat = h.nlat;
+  nlon = h.nlon;
+  nh = h.nh;
+  ntri = h.ntri;
+  t.assign(B, 0.0);
+  omega_m.assign(B, c.omega);
+  has_orog.assign(B, 0);
+  LMW_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  // tables: coefficient-major for synthesis, latitude-major for analysis
+  std::vector<double> Pa(static_cast<size_t>(nh) * ntri), Ha(Pa.size());
+  for (int q = 0; q < ntri; q++)
+    for (int jh = 0; jh < nh; jh++) {
+      Pa[static_cast<size_t>(jh) * ntri + q] = h.P[static_cast<size_t>(q) * nh + jh];
+      Ha[static_cast<size_t>(jh) * ntri + q] = h.H[static_cast<size_t>(q) * nh + jh];
+    }
+  auto up = [&](DevBuf<double> &dst, const std::vector<double> &src) {
+    dst.alloc(src.size());
+    LMW_CUDA(cudaMemcpy(dst.p, src.data(), src.size() * sizeof(double), cudaMemcpyHostToDevice));
+  };
+  up(tab->Ps, h.P);
+  up(tab->Hs, h.H);
+  up(tab->Pa, Pa);
+  up(tab->Ha, Ha);
+  up(tab->mu, h.mu);
+  up(tab->w, h.w);
+  std::vector<double> wd(nlat), cl(nlat);
+  for (int j = 0; j < nlat; j++) {
+    wd[j] = h.w[j] / (1 - h.mu[j] * h.mu[j]) / p.radius;  // cpp/sphere.cpp:371
+    cl[j] = std::sqrt(1 - h.mu[j] * h.mu[j]);
+  }
+  up(tab->wd, wd);
+  up(tab->cosl, cl);
+  std::vector<double2> tw(nlon / 2);
+  for (int k = 0; k < nlon / 2; k++) {
+    double ang = -2 * kPi * k / nlon;
+    tw[k] = make_double2(std::cos(ang), std::sin(ang));
+  }
+  tab->tw.alloc(tw.size());
+  LMW_CUDA(cudaMemcpy(tab->tw.p, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  std::vector<int> tm(ntri), tn(ntri);
+  for (int m = 0; m <= N; m++)
+    for (int n = m; n <= N; n++) {
+      tm[h.tri[m] + n - m] = m;
+      tn[h.tri[m] + n - m] = n;
+    }
+  auto upi = [&](DevBuf<int> &dst, const std::vector<int> &src) {
+    dst.alloc(src.size());
+    LMW_CUDA(cudaMemcpy(dst.p, src.data(), src.size() * sizeof(int), cudaMemcpyHostToDevice));
+  };
+  upi(tab->trim, tm);
+  upi(tab->trin, tn);
+  upi(tab->tri, h.tri);
+  const size_t nst = static_cast<size_t>(B) * 3 * ntri * 2;
+  x0.alloc(nst);
+  xs.alloc(nst);
+  acc.alloc(nst);
+  four.alloc(static_cast<size_t>(B) * nlat * 4 * M * 2);
+  fold.alloc(static_cast<size_t>(B) * nh * NSLOT * 2 * M * 2);
+  fgrid.alloc(static_cast<size_t>(B) * ngrid());
+  hsgrid.alloc(static_cast<size_t>(B) * ngrid());
+  refgrid.alloc(static_cast<size_t>(B) * ngrid());
+  filt.alloc(2 * M);
+  diagrows.alloc(static_cast<size_t>(B) * nlat * DIAG_K);
+  gridin.alloc(4 * ngrid());
+  dred.alloc(B);
+  hred.alloc(B);
+  hstage.alloc(std::max<size_t>(4 * ngrid(), static_cast<size_t>(3) * 2 * nspec_ref()));
+  x0.zero(stream);
+  hsgrid.zero(stream);
+  refgrid.zero(stream);
+  const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
+  LMW_CUDA(cudaFuncSetAttribute(sph_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  LMW_CUDA(cudaFuncSetAttribute(sph_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  LMW_CUDA(cudaFuncSetAttribute(sph_grid_in, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  for (int b = 0; b < B; b++) set_axis_tilt(0, b);
+  LMW_CUDA(cudaStreamSynchronize(stream));
+}
+
+SphereEngine::~SphereEngine() {
+  if (graph) cudaGraphExecDestroy(graph);
+  if (stream) {
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
+  delete tab;
+}
+
+static void check_member(const SphereEngine &e, int member) {
+  if (member < 0 || member >= e.B) throw InvalidArgument("member index out of range");
+}
+
+// cpp/sphere.cpp:111-118 (with the member's own rotation rate)
+void SphereEngine::set_axis_tilt(double alpha, int member) {
+  check_member(*this, member);
+  const HostTables &h = tab->host;
+  std::vector<double> f(ngrid());
+  for (int j = 0; j < nlat; j++)
+    for (int k = 0; k < nlon; k++) {
+      double lam = 2 * kPi * k / nlon, c = std::sqrt(1 - h.mu[j] * h.mu[j]);
+      f[static_cast<size_t>(j) * nlon + k] = 2 * omega_m[member] * (-std::cos(lam) * c * std::sin(alpha) + h.mu[j] * std::cos(alpha));
+    }
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  LMW_CUDA(cudaMemcpy(fgrid.p + static_cast<size_t>(member) * ngrid(), f.data(), ngrid() * sizeof(double), cudaMemcpyHostToDevice));
+}
+
+void SphereEngine::set_omega(double omega, int member) {
+  check_member(*this, member);
+  omega_m[member] = omega;
+  set_axis_tilt(0, member);
+}
+
+// cpp/sphere.cpp:105-109
+void SphereEngine::set_orography(const double *hs, size_t n, int member) {
+  check_member(*this, member);
+  if (n != ngrid()) throw InvalidArgument("grid size mismatch");
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  LMW_CUDA(cudaMemcpy(hsgrid.p + static_cast<size_t>(member) * ngrid(), hs, n * sizeof(double), cudaMemcpyHostToDevice));
+  has_orog[member] = 1;
+}
+
+void SphereEngine::synth_grids(int member_first, int count) {
+  SphDev d = make_sph(*this, *tab);
+  const size_t st = static_cast<size_t>(member_first) * 3 * ntri;
+  const size_t fo = static_cast<size_t>(member_first) * nlat * 4 * M;
+  dim3 g((nh + SYN_THREADS - 1) / SYN_THREADS, N / 2 + 1, count);
+  sph_synth<<<g, SYN_THREADS, 0, stream>>>(d, reinterpret_cast<const double2 *>(x0.p) + st, reinterpret_cast<double2 *>(four.p) + fo);
+  LMW_LAUNCH_CHECK();
+  g_launches += 1;
+}
+
+// cpp/sphere.cpp:236-239: remember the current height grid
+void SphereEngine::mark_reference(int member) {
+  check_member(*this, member);
+  SphDev d = make_sph(*this, *tab);
+  synth_grids(member, 1);
+  const size_t smem = static_cast<size_t>(nlon) * sizeof(double2);
+  sph_phi_grid<<<dim3(nh, 1), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p) + static_cast<size_t>(member) * nlat * 4 * M,
+                                                        refgrid.p + static_cast<size_t>(member) * ngrid());
+  LMW_LAUNCH_CHECK();
+  g_launches += 1;
+  LMW_CUDA(cudaStreamSynchronize(stream));
+}
+
+void SphereEngine::analyze_grids_to_state(int member) {
+  SphDev d = make_sph(*this, *tab);
+  const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
+  const size_t ng = ngrid();
+  sph_grid_in<<<nh, GRID_THREADS, smem, stream>>>(d, gridin.p, gridin.p + ng, gridin.p + 2 * ng, reinterpret_cast<double2 *>(fold.p));
+  sph_analysis_in<<<(ntri + ANA_THREADS - 1) / ANA_THREADS, ANA_THREADS, 0, stream>>>(
+      d, reinterpret_cast<const double2 *>(fold.p), reinterpret_cast<double2 *>(x0.p) + static_cast<size_t>(member) * 3 * ntri);
+  LMW_LAUNCH_CHECK();
+  g_launches += 2;
+}
+
+// cpp/sphere.cpp:217-234
+void SphereEngine::set_state_grid(const double *h, const double *u, const double *v, size_t n, int member) {
+  check_member(*this, member);
+  if (n != ngrid()) throw InvalidArgument("grid size mismatch");
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  std::memcpy(hstage.p, h, n * sizeof(double));
+  std::memcpy(hstage.p + n, u, n * sizeof(double));
+  std::memcpy(hstage.p + 2 * n, v, n * sizeof(double));
+  LMW_CUDA(cudaMemcpyAsync(gridin.p, hstage.p, 3 * n * sizeof(double), cudaMemcpyHostToDevice, stream));
+  // grid_in expects (h, u, v) in this order
+  analyze_grids_to_state(member);
+  t[member] = 0;
+  mark_reference(member);
+}
+
+void SphereEngine::to_packed(const double *ref, double *packed) {
+  for (int m = 0; m <= N; m++)
+    for (int n = m; n <= N; n++) {
+      size_t q = static_cast<size_t>(tab->host.tri[m] + n - m), r = static_cast<size_t>(m) * M + n;
+      packed[2 * q] = ref[2 * r];
+      packed[2 * q + 1] = ref[2 * r + 1];
+    }
+}
+void SphereEngine::from_packed(const double *packed, double *ref) {
+  std::memset(ref, 0, nspec_ref() * 2 * sizeof(double));
+  for (int m = 0; m <= N; m++)
+    for (int n = m; n <= N; n++) {
+      size_t q = static_cast<size_t>(tab->host.tri[m] + n - m), r = static_cast<size_t>(m) * M + n;
+      ref[2 * r] = packed[2 * q];
+      ref[2 * r + 1] = packed[2 * q + 1];
+    }
+}
+
+void SphereEngine::set_state(const double *zeta, const double *delta, const double *phi, double time, int member) {
+  check_member(*this, member);
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  const size_t pk = static_cast<size_t>(ntri) * 2;
+  to_packed(zeta, hstage.p);
+  to_packed(delta, hstage.p + pk);
+  to_packed(phi, hstage.p + 2 * pk);
+  LMW_CUDA(cudaMemcpyAsync(x0.p + static_cast<size_t>(member) * 3 * pk, hstage.p, 3 * pk * sizeof(double), cudaMemcpyHostToDevice, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  t[member] = time;
+}
+
+void SphereEngine::get_state(double *zeta, double *delta, double *phi, int member) {
+  check_member(*this, member);
+  const size_t pk = static_cast<size_t>(ntri) * 2;
+  LMW_CUDA(cudaMemcpyAsync(hstage.p, x0.p + static_cast<size_t>(member) * 3 * pk, 3 * pk * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  if (zeta) from_packed(hstage.p, zeta);
+  if (delta) from_packed(hstage.p + pk, delta);
+  if (phi) from_packed(hstage.p + 2 * pk, phi);
+}
+
+// cpp/sphere.cpp:301-311
+void SphereEngine::add_mode(int n, int m, double amplitude, double mean_depth, int member) {
+  check_member(*this, member);
+  if (m < 0 || n < std::max(m, 1) || n > N) throw InvalidArgument("mode (n, m) needs 0 <= m <= n <= truncation and n >= 1");
+  std::vector<double> z(2 * nspec_ref(), 0.0), ph(2 * nspec_ref(), 0.0);
+  ph[0] = p.gravity * mean_depth * std::sqrt(2.0);
+  ph[2 * (static_cast<size_t>(m) * M + n)] += p.gravity * amplitude * (m == 0 ? 1.0 : 0.5);
+  set_state(z.data(), z.data(), ph.data(), 0.0, member);
+  mark_reference(member);
+}
+
+// cpp/sphere.cpp:313-336. The seeded coefficients and their grid rms are formed on the host in the reference's
+// order; the scaled increment is added to the device state.
+void SphereEngine::perturb(double amplitude, uint64_t seed, int max_wave, int member) {
+  check_member(*this, member);
+  if (max_wave < 1 || max_wave > N) throw InvalidArgument("max_wave must be between 1 and the truncation");
+  uint64_t st = seed * 0x9E3779B97F4A7C15ULL + 12345;
+  std::vector<cplx> add(nspec_ref(), 0);
+  for (int m = 0; m <= max_wave; m++)
+    for (int n = std::max(m, 1); n <= max_wave; n++) {
+      double re = irwin_hall(st), im = m == 0 ? 0.0 : irwin_hall(st);
+      add[static_cast<size_t>(m) * M + n] = cplx(re, im);
+    }
+  std::vector<double> g;
+  tab->host.synthesize(add, g);
+  const std::vector<double> &w = tab->host.w;
+  double ms = 0, wsum = 0;
+  for (int j = 0; j < nlat; j++)
+    for (int k = 0; k < nlon; k++) {
+      double x = g[static_cast<size_t>(j) * nlon + k];
+      ms += w[j] * x * x;
+      wsum += w[j];
+    }
+  double rms = std::sqrt(ms / wsum);
+  double scale = rms > 0 ? amplitude / rms * p.gravity : 0;
+  std::vector<double> z(2 * nspec_ref()), d(2 * nspec_ref()), ph(2 * nspec_ref());
+  get_state(z.data(), d.data(), ph.data(), member);
+  cplx *phc = reinterpret_cast<cplx *>(ph.data());
+  for (size_t i = 0; i < nspec_ref(); i++) phc[i] += add[i] * scale;
+  set_state(z.data(), d.data(), ph.data(), 0.0, member);
+  mark_reference(member);
+}
+
+// Seeded balanced turbulence (this project's benchmark initialiser; the same definition as the oracle's
+// or_sphere_turbulence_grids): complex-Gaussian vorticity for 1 <= n <= nforce with a kinetic-energy spectrum
+// proportional to n^-3 and the largest grid wind equal to max_wind, zero divergence, h = mean + f psi / g.
+void SphereEngine::turbulence(uint64_t seed, double mean_height, double max_wind, int nforce, int member) {
+  check_member(*this, member);
+  const HostTables &h = tab->host;
+  const double a = p.radius, a2 = a * a;
+  std::vector<cplx> z(nspec_ref(), 0), zero(nspec_ref(), 0), psi(nspec_ref(), 0);
+  uint64_t st = seed * 0x9E3779B97F4A7C15ULL + 424242;
+  nforce = std::min(nforce, N);
+  for (int n = 1; n <= nforce; n++) {
+    for (int m = 0; m <= n; m++) {
+      double re = irwin_hall(st), im = m == 0 ? 0.0 : irwin_hall(st);
+      z[static_cast<size_t>(m) * M + n] = cplx(re, im);
+    }
+    double e = 0;
+    for (int m = 0; m <= n; m++) {
+      cplx c = z[static_cast<size_t>(m) * M + n];
+      e += 0.25 * (m == 0 ? 1.0 : 2.0) * a2 * (c.real() * c.real() + c.imag() * c.imag()) / (n * (n + 1.0));
+    }
+    double target = 1.0 / (static_cast<double>(n) * n * n);
+    double sc = e > 0 ? std::sqrt(target / e) : 0.0;
+    for (int m = 0; m <= n; m++) z[static_cast<size_t>(m) * M + n] *= sc;
+  }
+  std::vector<double> U, V;
+  h.winds(z, zero, a, U, V);
+  double wmax = 0;
+  for (int j = 0; j < nlat; j++) {
+    double c = std::sqrt(1 - h.mu[j] * h.mu[j]);
+    for (int k = 0; k < nlon; k++) {
+      size_t i = static_cast<size_t>(j) * nlon + k;
+      double sp = std::sqrt(U[i] * U[i] + V[i] * V[i]) / c;
+      wmax = wmax < sp ? sp : wmax;
+    }
+  }
+  double gsc = wmax > 0 ? max_wind / wmax : 0.0;
+  for (auto &c : z) c *= gsc;
+  h.winds(z, zero, a, U, V);
+  std::vector<double> hh, uu(ngrid()), vv(ngrid());
+  for (int j = 0; j < nlat; j++) {
+    double c = std::sqrt(1 - h.mu[j] * h.mu[j]);
+    for (int k = 0; k < nlon; k++) {
+      size_t i = static_cast<size_t>(j) * nlon + k;
+      uu[i] = U[i] / c;
+      vv[i] = V[i] / c;
+    }
+  }
+  for (int m = 0; m <= N; m++)
+    for (int n = std::max(m, 1); n <= N; n++) psi[static_cast<size_t>(m) * M + n] = z[static_cast<size_t>(m) * M + n] * (-a2 / (n * (n + 1.0)));
+  h.synthesize(psi, hh);
+  for (int j = 0; j < nlat; j++) {
+    double f = 2 * omega_m[member] * h.mu[j];
+    for (int k = 0; k < nlon; k++) {
+      size_t i = static_cast<size_t>(j) * nlon + k;
+      hh[i] = mean_height + f * hh[i] / p.gravity;
+    }
+  }
+  set_state_grid(hh.data(), uu.data(), vv.data(), ngrid(), member);
+}
+
+// del^4 filter factors for this step size (cpp/sphere.cpp:392-405), by total wavenumber n
+void SphereEngine::upload_filter(double dt) {
+  if (filt_dt == dt) return;
+  std::vector<double> f(2 * M, 1.0);
+  if (p.diffusion > 0) {
+    const double a2 = p.radius * p.radius;
+    for (int n = 1; n <= N; n++) {
+      double l = n * (n + 1.0);
+      double kv = (l - 2) / a2, kp = l / a2;
+      f[n] = std::exp(-p.diffusion * kv * kv * dt);
+      f[M + n] = std::exp(-p.diffusion * kp * kp * dt);
+    }
+  }
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  LMW_CUDA(cudaMemcpy(filt.p, f.data(), 2 * M * sizeof(double), cudaMemcpyHostToDevice));
+  filt_dt = dt;
+}
+
+void SphereEngine::launch_stage(int stage, double dt) {
+  SphDev d = make_sph(*this, *tab);
+  const double2 *in = reinterpret_cast<const double2 *>(stage == 0 ? x0.p : xs.p);
+  dim3 gs((nh + SYN_THREADS - 1) / SYN_THREADS, N / 2 + 1, B);
+  sph_synth<<<gs, SYN_THREADS, 0, stream>>>(d, in, reinterpret_cast<double2 *>(four.p));
+  const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
+  sph_grid<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), fgrid.p, hsgrid.p,
+                                                        reinterpret_cast<double2 *>(fold.p));
+  StageArgs sa;
+  sa.stage = stage;
+  sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
+  sa.filt = filt.p;
+  sph_analysis<<<dim3((ntri + ANA_THREADS - 1) / ANA_THREADS, B), ANA_THREADS, 0, stream>>>(
+      d, reinterpret_cast<const double2 *>(fold.p), sa, reinterpret_cast<double2 *>(x0.p), reinterpret_cast<double2 *>(xs.p),
+      reinterpret_cast<double2 *>(acc.p));
+  LMW_LAUNCH_CHECK();
+  g_launches += 3;
+}
+
+void SphereEngine::kernel_times(double dt, int reps, double *out) {
+  upload_filter(dt);
+  SphDev d = make_sph(*this, *tab);
+  const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
+  dim3 gs((nh + SYN_THREADS - 1) / SYN_THREADS, N / 2 + 1, B);
+  StageArgs sa;
+  sa.stage = 1;
+  sa.c = 0.5 * dt;
+  sa.filt = filt.p;
+  auto syn = [&] { sph_synth<<<gs, SYN_THREADS, 0, stream>>>(d, reinterpret_cast<const double2 *>(x0.p), reinterpret_cast<double2 *>(four.p)); };
+  auto grd = [&] {
+    sph_grid<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), fgrid.p, hsgrid.p,
+                                                          reinterpret_cast<double2 *>(fold.p));
+  };
+  auto ana = [&] {
+    sph_analysis<<<dim3((ntri + ANA_THREADS - 1) / ANA_THREADS, B), ANA_THREADS, 0, stream>>>(
+        d, reinterpret_cast<const double2 *>(fold.p), sa, reinterpret_cast<double2 *>(x0.p), reinterpret_cast<double2 *>(xs.p),
+        reinterpret_cast<double2 *>(acc.p));
+  };
+  cudaEvent_t e0, e1;
+  LMW_CUDA(cudaEventCreate(&e0));
+  LMW_CUDA(cudaEventCreate(&e1));
+  int k = 0;
+  for (auto fn : {std::function<void()>(syn), std::function<void()>(grd), std::function<void()>(ana)}) {
+    fn();  // warm
+    LMW_CUDA(cudaEventRecord(e0, stream));
+    for (int r = 0; r < reps; r++) fn();
+    LMW_CUDA(cudaEventRecord(e1, stream));
+    LMW_LAUNCH_CHECK();
+    LMW_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    LMW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    out[k++] = ms / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  g_launches += 3ull * (reps + 1);
+}
+
+void SphereEngine::enqueue_step(double dt) {
+  upload_filter(dt);
+  for (int s = 0; s < 4; s++) launch_stage(s, dt);
+  launches_step = 12;
+}
+
+void SphereEngine::launch_chunk(double dt, int steps) {
+  if (steps <= 0) return;
+  upload_filter(dt);
+  if (!graph || graph_dt != dt || graph_steps != steps) {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    cudaGraph_t g;
+    uint64_t before = g_launches;
+    LMW_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < steps; s++)
+      for (int k = 0; k < 4; k++) launch_stage(k, dt);
+    LMW_CUDA(cudaStreamEndCapture(stream, &g));
+    g_launches = before;
+    LMW_CUDA(cudaGraphInstantiate(&graph, g, 0));
+    cudaGraphDestroy(g);
+    graph_dt = dt;
+    graph_steps = steps;
+  }
+  LMW_CUDA(cudaGraphLaunch(graph, stream));
+  g_launches += 12ull * steps;
+}
+
+void SphereEngine::step(double dt) {
+  enqueue_step(dt);
+  for (int b = 0; b < B; b++) t[b] += dt;
+  LMW_CUDA(cudaStreamSynchronize(stream));
+}
+
+void SphereEngine::reduce_guard(Reduce &r, int member) {
+  SphDev d = make_sph(*this, *tab);
+  synth_grids(member, 1);
+  const size_t smem = 4 * static_cast<size_t>(nlon) * sizeof(double2);
+  const size_t go = static_cast<size_t>(member) * ngrid();
+  sph_diag<<<dim3(nh, 1), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p) + static_cast<size_t>(member) * nlat * 4 * M,
+                                                        fgrid.p + go, hsgrid.p + go, refgrid.p + go, diagrows.p, nullptr);
+  sph_diag_final<<<1, GRID_THREADS, 0, stream>>>(d, diagrows.p, reinterpret_cast<const double2 *>(x0.p) + static_cast<size_t>(member) * 3 * ntri,
+                                                0, dred.p);
+  LMW_LAUNCH_CHECK();
+  g_launches += 2;
+  LMW_CUDA(cudaMemcpyAsync(hred.p, dred.p, sizeof(Reduce), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  r = hred.p[0];
+}
+
+// cpp/sphere.cpp:438-447
+double SphereEngine::stable_dt(double safety, int member) {
+  Reduce r;
+  reduce_guard(r, member);
+  double hmax = std::max(0.0, r.max[1]), wmax = r.max[0];
+  if (!(hmax > 0)) throw RuntimeError("the height field must be positive to step the model");
+  double omega = (N / p.radius) * (std::sqrt(p.gravity * hmax) + wmax) + 2 * omega_m[member];
+  if (!(omega > 0)) return 1e9;
+  return safety / omega;
+}
+
+// cpp/sphere.cpp:457-484; every member steps with the same dt, the guards check each member
+void SphereEngine::run(double seconds, double dt) {
+  if (!(seconds >= 0)) throw InvalidArgument("run: seconds must not be negative");
+  if (seconds == 0) return;
+  if (!(dt > 0)) {
+    dt = 1e300;
+    for (int b = 0; b < B; b++) dt = std::min(dt, stable_dt(1.5, b));
+  }
+  double limit = 1e300;
+  for (int b = 0; b < B; b++) limit = std::min(limit, stable_dt(2.0 * std::sqrt(2.0), b));
+  if (!(dt <= limit))
+    throw InvalidArgument("run: dt = " + fmt_f(dt) + " s exceeds the RK4 stability limit of about " + fmt_f(limit) +
+                          " s for the present state: use a smaller dt");
+  int64_t n = static_cast<int64_t>(std::ceil(seconds / dt - 1e-9));
+  if (n < 1) n = 1;
+  if (n > 50000000) throw InvalidArgument("run: more than 5e7 steps; use a larger dt");
+  double h = seconds / static_cast<double>(n);
+  upload_filter(h);
+  int64_t i = 0;
+  while (i < n) {
+    int64_t next = std::min<int64_t>(n - 1, i | 63);
+    int chunk = static_cast<int>(next - i + 1);
+    if (chunk == 64) launch_chunk(h, 64);
+    else for (int s = 0; s < chunk; s++) enqueue_step(h);
+    for (int s = 0; s < chunk; s++)
+      for (int b = 0; b < B; b++) t[b] += h;
+    i = next + 1;
+    if ((next & 63) == 63) {
+      for (int b = 0; b < B; b++) {
+        Reduce r;
+        reduce_guard(r, b);
+        if (!std::isfinite(r.sum[5])) throw RuntimeError("the integration blew up (not finite): use a smaller dt");
+        double hmax = std::max(0.0, r.max[1]);
+        if (!(hmax > 0)) throw RuntimeError("the height field must be positive to step the model");
+        double omega = (N / p.radius) * (std::sqrt(p.gravity * hmax) + r.max[0]) + 2 * omega_m[b];
+        double now = omega > 0 ? 2.0 * std::sqrt(2.0) / omega : 1e9;
+        if (!(h <= now))
+          throw RuntimeError("run: dt = " + fmt_f(h) + " s exceeds the RK4 stability limit of about " + fmt_f(now) + " s reached at t = " +
+                             fmt_f(t[b]) + " s (the flow accelerated): use a smaller dt");
+      }
+    }
+  }
+  for (int b = 0; b < B; b++) {
+    Reduce r;
+    reduce_guard(r, b);
+    if (!std::isfinite(r.sum[5])) throw RuntimeError("the integration blew up (not finite): use a smaller dt");
+  }
+}
+
+// cpp/sphere.cpp:510-590
+void SphereEngine::diagnostics(double *out, int member) {
+  check_member(*this, member);
+  Reduce r;
+  reduce_guard(r, member);
+  const size_t pk = static_cast<size_t>(ntri) * 2;
+  double phi00[2];
+  LMW_CUDA(cudaMemcpy(phi00, x0.p + static_cast<size_t>(member) * 3 * pk + 2 * pk, sizeof(phi00), cudaMemcpyDeviceToHost));
+  out[0] = phi00[0] / std::sqrt(2.0) / p.gravity;
+  out[1] = r.sum[0];
+  out[2] = r.sum[1];
+  out[3] = r.sum[0] + r.sum[1];
+  out[4] = r.sum[2];
+  out[5] = r.max[0];
+  out[6] = std::sqrt(r.sum[3] / r.sum[4]);
+  out[7] = r.max[2] / r.max[3];
+}
+
+void SphereEngine::grid(int which, double *out, int member) {
+  check_member(*this, member);
+  if (which < 0 || which > 3) throw InvalidArgument("grid field must be 0 (height), 1 (u), 2 (v) or 3 (vorticity)");
+  SphDev d = make_sph(*this, *tab);
+  synth_grids(member, 1);
+  const size_t smem = 4 * static_cast<size_t>(nlon) * sizeof(double2);
+  const size_t go = static_cast<size_t>(member) * ngrid();
+  sph_diag<<<dim3(nh, 1), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p) + static_cast<size_t>(member) * nlat * 4 * M,
+                                                        fgrid.p + go, hsgrid.p + go, refgrid.p + go, diagrows.p, gridin.p);
+  LMW_LAUNCH_CHECK();
+  g_launches += 1;
+  LMW_CUDA(cudaMemcpyAsync(out, gridin.p + static_cast<size_t>(which) * ngrid(), ngrid() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+}
+
+// cpp/sphere.cpp:536-551 (from the spectral state)
+void SphereEngine::spectrum(double *ke, double *pe, int member) {
+  std::vector<double> z(2 * nspec_ref()), dd(2 * nspec_ref()), ph(2 * nspec_ref());
+  get_state(z.data(), dd.data(), ph.data(), member);
+  for (int n = 0; n <= N; n++) ke[n] = pe[n] = 0;
+  const double a2 = p.radius * p.radius, g2 = p.gravity * p.gravity;
+  for (int m = 0; m <= N; m++) {
+    double cm = m == 0 ? 1.0 : 2.0;
+    for (int n = std::max(m, 1); n <= N; n++) {
+      size_t q = 2 * (static_cast<size_t>(m) * M + n);
+      double nz = z[q] * z[q] + z[q + 1] * z[q + 1], nd = dd[q] * dd[q] + dd[q + 1] * dd[q + 1], np = ph[q] * ph[q] + ph[q + 1] * ph[q + 1];
+      ke[n] += 0.25 * cm * a2 * (nz + nd) / (n * (n + 1.0));
+      pe[n] += 0.25 * cm * p.gravity * np / g2;
+    }
+  }
+}
+
+}  // namespace lmw

@@ -1,0 +1,108 @@
+"""GPU parity of the C-grid plane (cpp/plane.cpp) through the C ABI: bitwise identical to the reference's
+outputs (golden fixtures made by the reference itself, and the oracle at the full 1024 x 512 size)."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle_lib import OraclePlane
+
+pytestmark = pytest.mark.gpu
+
+
+def test_plane_jet_200_steps_bitwise(engine):
+    g = golden("plane_small.npz")
+    p = engine.Plane(64, 32, 3.2e5, 1.6e5, f0=1e-4, beta=1.6e-11, gravity=9.81, depth=100.0)
+    p.set_h_from_grid(g["h0"]).set_u_from_grid(g["u0"]).set_v_from_grid(g["v0"])
+    for _ in range(int(g["steps"])):
+        p.step(float(g["dt"]))
+    h, u, v = p.get()
+    assert np.array_equal(h, g["h"]) and np.array_equal(u, g["u"]) and np.array_equal(v, g["v"])
+    assert p.time() == pytest.approx(200 * 60.0)
+
+
+def test_plane_linear_viscous_drag_run_bitwise(engine):
+    g = golden("plane_small.npz")
+    p = engine.Plane(48, 24, 2.4e5, 1.2e5, f0=5e-5, beta=2e-11, gravity=9.81, depth=50.0, viscosity=200.0, drag=1e-5,
+                     linear=True)
+    p.perturb(0.5, 9)
+    h, u, v = p.get()
+    assert np.array_equal(h, g["lin_h0"])
+    p.run(7200.0, 0.0)  # automatic dt from stable_dt, guards every 64 steps
+    h, u, v = p.get()
+    assert np.array_equal(h, g["lin_h"]) and np.array_equal(u, g["lin_u"]) and np.array_equal(v, g["lin_v"])
+    assert p.time() == pytest.approx(float(g["lin_time"]), rel=1e-15)
+
+
+def test_plane_nonlinear_viscous_run_bitwise(engine):
+    g = golden("plane_small.npz")
+    p = engine.Plane(40, 20, 2.0e5, 1.0e5, f0=1e-4, beta=0.0, gravity=9.81, depth=80.0, viscosity=50.0, drag=2e-6)
+    p.perturb(1.0, 4)
+    p.run(3600.0, 20.0)
+    h, u, v = p.get()
+    assert np.array_equal(h, g["visc_h"]) and np.array_equal(u, g["visc_u"]) and np.array_equal(v, g["visc_v"])
+    d = p.diagnostics()
+    for k, ref in zip(("mean_depth", "energy", "max_speed", "pv_anomaly_rms"), g["visc_diag"]):
+        assert d[k] == pytest.approx(ref, rel=1e-13, abs=1e-300), k
+
+
+def test_plane_config1_full_size_bitwise_against_oracle(engine):
+    # 1024 x 512 cells, dx = dy = 5 km, f0 = 1e-4, beta = 1.6e-11, H = 100 m, jet 20 sech^2(y/100 km) + 0.1 m noise
+    nx, ny, L = 1024, 512, 5000.0
+    kw = dict(f0=1e-4, beta=1.6e-11, gravity=9.81, depth=100.0)
+    o = OraclePlane(nx, ny, nx * L, ny * L, **kw)
+    h0, u0 = o.jet_grids(u0=20.0, width=1.0e5, noise_rms=0.1, seed=1)
+    p = engine.Plane(nx, ny, nx * L, ny * L, **kw)
+    p.jet(20.0, 1.0e5, 0.1, 1)
+    h, u, v = p.get()
+    assert np.array_equal(h, h0) and np.array_equal(u, u0) and not v.any()
+    o.set(h0, u0, np.zeros((ny + 1, nx)))
+    for _ in range(6):
+        o.step(60.0)
+        p.step(60.0)
+    for a, b in zip(p.get(), o.get()):
+        assert np.array_equal(a, b)
+    d, od = p.diagnostics(), o.diagnostics()
+    assert d["mean_depth"] == pytest.approx(od["mean_depth"], rel=1e-14)
+    assert d["energy"] == pytest.approx(od["energy"], rel=1e-13)
+
+
+def test_plane_run_guards_and_messages(engine):
+    p = engine.Plane(64, 32, 3.2e5, 1.6e5, f0=1e-4, depth=100.0)
+    p.perturb(0.2, 1)
+    limit = p.stable_dt(math.sqrt(0.5))
+    with pytest.raises(ValueError, match="exceeds the RK4 stability limit of about"):
+        p.run(3600.0, 2 * limit)
+    with pytest.raises(ValueError, match="seconds must not be negative"):
+        p.run(-5.0, 1.0)
+    m0 = p.mean_depth()
+    p.run(0.0, 1.0)
+    p.run(1800.0, 0.0)
+    assert abs(p.mean_depth() - m0) <= 1e-12 * m0
+    with pytest.raises(ValueError, match="grid size mismatch"):
+        p.set_h_from_grid(np.zeros(5))
+
+
+def test_plane_gravity_wave_known_answer(engine):
+    # tests/core.cpp:102-110: a standing wave is inverted after half a period
+    nx, ny, lx, ly, H = 100, 8, 1.0e6, 2.0e4, 100.0
+    p = engine.Plane(nx, ny, lx, ly, depth=H, linear=True)
+    k, c = 2 * math.pi / lx, math.sqrt(9.81 * H)
+    xc = (np.arange(nx) + 0.5) * lx / nx
+    p.set_h_from_grid(np.tile(H + np.cos(k * xc), (ny, 1)))
+    p.run(math.pi / (c * k), 0.0)
+    h, _, _ = p.get()
+    assert abs((h[ny // 2, 0] - H) + math.cos(k * xc[0])) <= 2e-3
+    assert abs(p.mean_depth() - H) <= 1e-10
+
+
+def test_plane_deterministic(engine):
+    runs = []
+    for _ in range(2):
+        p = engine.Plane(96, 48, 4.8e5, 2.4e5, f0=1e-4, beta=1e-11)
+        p.perturb(0.5, 12)
+        p.run(3000.0, 30.0)
+        runs.append(p.get())
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
