@@ -64,7 +64,8 @@ def test_plane_config1_full_size_bitwise_against_oracle(engine):
     for a, b in zip(p.get(), o.get()):
         assert np.array_equal(a, b)
     d, od = p.diagnostics(), o.diagnostics()
-    assert d["mean_depth"] == pytest.approx(od["mean_depth"], rel=1e-14)
+    # the oracle sums 524288 depths in sequence (3e-14 relative rounding); the device sums in a tree
+    assert d["mean_depth"] == pytest.approx(od["mean_depth"], rel=1e-13)
     assert d["energy"] == pytest.approx(od["energy"], rel=1e-13)
 
 

@@ -1,7 +1,11 @@
 """GPU parity of the spectral-transform sphere (cpp/sphere.cpp), FP64 path, through the C ABI.
 
-Bar: every spectral field within 1e-12 norm-relative (max |difference| / max |reference|) of the reference's own
-run, and mass, energy and enstrophy within 1e-12 relative. The floor: the reference against itself, built with
+Bar: every spectral field within 1e-12 norm-relative of the reference's own run, and mass, energy and enstrophy
+within 1e-12 relative. Norm-relative means max |difference| / max |reference| with the field's natural scale as
+the denominator: Phi against Phi, and vorticity and divergence (both derivatives of the wind, in s^-1) against
+the larger of max |zeta| and max |delta|. Where the flow is non-divergent (balanced initial states, Williamson
+test case 2) the divergence is pure round-off (1e-22 against a vorticity of 1e-5) and no run reproduces another's
+round-off. The floor: the reference against itself, built with
 and without FMA contraction, differs by 2e-13 norm-relative in delta after 480 T42 steps (same seeded state),
 while single small coefficients can differ by 7e-8 relative; per-coefficient agreement is reported, not
 required to 1e-12."""
@@ -20,9 +24,15 @@ def normrel(a, b):
     return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
 
 
+def state_errors(got, ref):
+    wind = max(np.abs(ref[0]).max(), np.abs(ref[1]).max())
+    return {"zeta": np.abs(got[0] - ref[0]).max() / wind, "delta": np.abs(got[1] - ref[1]).max() / wind,
+            "phi": normrel(got[2], ref[2])}
+
+
 def assert_state(got, ref, tol=TOL):
-    for name, a, b in zip(("zeta", "delta", "phi"), got, ref):
-        assert normrel(a, b) <= tol, (name, normrel(a, b))
+    for name, err in state_errors(got, ref).items():
+        assert err <= tol, (name, err)
 
 
 def test_t21_turbulence_48_steps_against_reference_run(engine):
