@@ -27,7 +27,7 @@ namespace lmw {
 struct SphereTables {
   HostTables host;
   DevBuf<double> Ps, Hs, Pa, Ha;  // coefficient-major [tri][jh] (synthesis) and latitude-major [jh][tri] (analysis)
-  DevBuf<double> mu, w, wd, cosl;
+  DevBuf<double> mu, w, wd, cosl, r2om, kfac, lapl;
   DevBuf<double2> tw;  // exp(-2 pi i k / nlon), k < nlon/2
   DevBuf<int> trim, trin, tri;
 };
@@ -37,7 +37,7 @@ namespace {
 struct SphDev {
   int N, M, nlat, nlon, nh, ntri, logn;
   double a, g;
-  const double *Ps, *Hs, *Pa, *Ha, *mu, *w, *wd, *cosl;
+  const double *Ps, *Hs, *Pa, *Ha, *mu, *w, *wd, *cosl, *r2om, *kfac, *lapl;
   const double2 *tw;
   const int *trim, *trin, *tri;
 };
@@ -52,67 +52,76 @@ __device__ __forceinline__ double2 conjd(double2 a) { return make_double2(a.x, -
 __device__ __forceinline__ double2 imul(double2 z, double m) { return make_double2(-m * z.y, m * z.x); }
 
 // ------------------------------------------------------------------------------------------------ synthesis
-constexpr int SYN_THREADS = 64;
+// Block: SYN_CHUNKS warps for one wavenumber m and 32 southern latitudes (lane = latitude). Warp c sums the terms
+// n = m + c, m + c + SYN_CHUNKS, ... (one parity of n - m per warp), so the n-sum runs in SYN_CHUNKS pieces at
+// once; the pieces meet in shared memory. Reading the coefficient-major table is coalesced across the lanes.
+constexpr int SYN_CHUNKS = 8, SYN_THREADS = 32 * SYN_CHUNKS, SYN_Q = 12;
 
 // x: [B][3][ntri] (zeta, delta, phi); four: [B][nlat][4][M] (U, V, zeta, Phi)
 __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, const double2 *__restrict__ x, double2 *__restrict__ four) {
-  const int b = blockIdx.z, pair = blockIdx.y;
-  const int jh = blockIdx.x * SYN_THREADS + threadIdx.x;
-  if (jh >= d.nh) return;
+  __shared__ double part[SYN_CHUNKS][SYN_Q][33];
+  const int b = blockIdx.z, m = blockIdx.y;
+  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
+  const int jh = blockIdx.x * 32 + lane;
+  const bool live = jh < d.nh;
   const double2 *xz = x + static_cast<size_t>(b) * 3 * d.ntri, *xd = xz + d.ntri, *xf = xd + d.ntri;
-  const int js = jh, jn = d.nlat - 1 - jh;
-  const double aa = -d.a * d.a;
-  for (int pass = 0; pass < 2; pass++) {
-    const int m = pass == 0 ? pair : d.N - pair;
-    if (pass == 1 && m == pair) break;
-    double2 sp[2], sc[2], hp[2], hc[2], zs[2], fs[2];
-    for (int e = 0; e < 2; e++) sp[e] = sc[e] = hp[e] = hc[e] = zs[e] = fs[e] = make_double2(0, 0);
-    const int base = d.tri[m];
-    // n - m even terms accumulate in [0], odd terms in [1] (constant indices after unrolling by two)
-#define LMW_SYN_TERM(PAR, NN)                                                                     \
-  {                                                                                               \
-    const int q = base + (NN) - m;                                                                \
-    const double P = d.Ps[static_cast<size_t>(q) * d.nh + jh], H = d.Hs[static_cast<size_t>(q) * d.nh + jh]; \
-    const double2 z = xz[q], dl = xd[q], f = xf[q];                                               \
-    const double k = (NN) > 0 ? aa / ((NN) * ((NN) + 1.0)) : 0.0;                                 \
-    const double2 psi = cscale(z, k), chi = cscale(dl, k);                                        \
-    sp[PAR] = cfma(sp[PAR], psi, P);                                                              \
-    sc[PAR] = cfma(sc[PAR], chi, P);                                                              \
-    hp[PAR] = cfma(hp[PAR], psi, H);                                                              \
-    hc[PAR] = cfma(hc[PAR], chi, H);                                                              \
-    zs[PAR] = cfma(zs[PAR], z, P);                                                                \
-    fs[PAR] = cfma(fs[PAR], f, P);                                                                \
-  }
-    int n = m;
-    for (; n + 1 <= d.N; n += 2) {
-      LMW_SYN_TERM(0, n)
-      LMW_SYN_TERM(1, n + 1)
-    }
-    if (n <= d.N) LMW_SYN_TERM(0, n)
-#undef LMW_SYN_TERM
-    const double mm = static_cast<double>(m);
-    // southern latitude: even + odd; northern mirror: P sums even - odd, H sums odd - even
-    for (int side = 0; side < 2; side++) {
-      const int j = side == 0 ? js : jn;
-      double2 SP, SC, HP, HC, Z, F;
-      if (side == 0) {
-        SP = cadd(sp[0], sp[1]); SC = cadd(sc[0], sc[1]); HP = cadd(hp[0], hp[1]); HC = cadd(hc[0], hc[1]);
-        Z = cadd(zs[0], zs[1]); F = cadd(fs[0], fs[1]);
-      } else {
-        SP = csub(sp[0], sp[1]); SC = csub(sc[0], sc[1]); HP = csub(hp[1], hp[0]); HC = csub(hc[1], hc[0]);
-        Z = csub(zs[0], zs[1]); F = csub(fs[0], fs[1]);
-      }
-      // cpp/sphere.cpp:200-201: fu = (i m sc - hp)/a, fv = (i m sp + hc)/a
-      double2 fu = csub(imul(SC, mm), HP), fv = cadd(imul(SP, mm), HC);
-      fu = make_double2(fu.x / d.a, fu.y / d.a);
-      fv = make_double2(fv.x / d.a, fv.y / d.a);
-      double2 *o = four + (static_cast<size_t>(b) * d.nlat + j) * 4 * d.M;
-      o[0 * d.M + m] = fu;
-      o[1 * d.M + m] = fv;
-      o[2 * d.M + m] = Z;
-      o[3 * d.M + m] = F;
+  double2 sp = make_double2(0, 0), sc = sp, hp = sp, hc = sp, zs = sp, fs = sp;
+  const int base = d.tri[m];
+  if (live) {
+#pragma unroll 2
+    for (int n = m + c; n <= d.N; n += SYN_CHUNKS) {
+      const int q = base + n - m;
+      const double P = d.Ps[static_cast<size_t>(q) * d.nh + jh], H = d.Hs[static_cast<size_t>(q) * d.nh + jh];
+      const double2 z = xz[q], dl = xd[q], f = xf[q];
+      const double k = d.kfac[n];  // psi = -a^2/(n(n+1)) zeta, cpp/sphere.cpp:185-190
+      const double2 psi = cscale(z, k), chi = cscale(dl, k);
+      sp = cfma(sp, psi, P);
+      sc = cfma(sc, chi, P);
+      hp = cfma(hp, psi, H);
+      hc = cfma(hc, chi, H);
+      zs = cfma(zs, z, P);
+      fs = cfma(fs, f, P);
     }
   }
+  const double v[SYN_Q] = {sp.x, sp.y, sc.x, sc.y, hp.x, hp.y, hc.x, hc.y, zs.x, zs.y, fs.x, fs.y};
+#pragma unroll
+  for (int i = 0; i < SYN_Q; i++) part[c][i][lane] = v[i];
+  __syncthreads();
+  if (threadIdx.x >= 64) return;
+  const int side = threadIdx.x >> 5;  // 0: southern latitude (table latitude), 1: its northern mirror
+  if (!live) return;
+  // even (n - m) pieces are the chunks with even c, odd pieces the chunks with odd c
+  double e[SYN_Q], o[SYN_Q];
+#pragma unroll
+  for (int i = 0; i < SYN_Q; i++) {
+    double se = 0, so = 0;
+#pragma unroll
+    for (int k = 0; k < SYN_CHUNKS; k += 2) {
+      se += part[k][i][lane];
+      so += part[k + 1][i][lane];
+    }
+    e[i] = se;
+    o[i] = so;
+  }
+  // southern latitude: even + odd; northern mirror: P sums even - odd, H sums odd - even
+  double r[SYN_Q];
+#pragma unroll
+  for (int i = 0; i < SYN_Q; i++) {
+    const bool hsum = i >= 4 && i < 8;
+    r[i] = side == 0 ? e[i] + o[i] : (hsum ? o[i] - e[i] : e[i] - o[i]);
+  }
+  const double mm = static_cast<double>(m);
+  const double2 SP = make_double2(r[0], r[1]), SC = make_double2(r[2], r[3]), HP = make_double2(r[4], r[5]), HC = make_double2(r[6], r[7]);
+  // cpp/sphere.cpp:200-201: fu = (i m sc - hp)/a, fv = (i m sp + hc)/a
+  double2 fu = csub(imul(SC, mm), HP), fv = cadd(imul(SP, mm), HC);
+  fu = make_double2(fu.x / d.a, fu.y / d.a);
+  fv = make_double2(fv.x / d.a, fv.y / d.a);
+  const int j = side == 0 ? jh : d.nlat - 1 - jh;
+  double2 *out = four + (static_cast<size_t>(b) * d.nlat + j) * 4 * d.M;
+  out[0 * d.M + m] = fu;
+  out[1 * d.M + m] = fv;
+  out[2 * d.M + m] = make_double2(r[8], r[9]);
+  out[3 * d.M + m] = make_double2(r[10], r[11]);
 }
 
 // ------------------------------------------------------------------------------------------------ FFTs
@@ -192,7 +201,7 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, const double2
   load_pair_spectra(sm, 4, d, f_s, f_n, d.M);
   fft_inverse_dit(sm, 4, n, d.logn, d.tw);
   // nonlinear products, cpp/sphere.cpp:348-359 (real part: southern latitude, imaginary part: northern)
-  const double om = 1 - d.mu[js] * d.mu[js];  // the same at the mirror latitude
+  const double r2om = d.r2om[js];  // 1 / (2 (1 - mu^2)), the same at the mirror latitude
   const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
   const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
   double2 *rU = sm, *rV = sm + n, *rZ = sm + 2 * n, *rP = sm + 3 * n, *rE = sm + 4 * n;
@@ -202,12 +211,12 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, const double2
     {
       double eta = Z.x + fr_s[k];
       A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
-      PE.x = P.x + d.g * hr_s[k] + (U.x * U.x + V.x * V.x) / (2 * om);
+      PE.x = P.x + d.g * hr_s[k] + (U.x * U.x + V.x * V.x) * r2om;
     }
     {
       double eta = Z.y + fr_n[k];
       A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
-      PE.y = P.y + d.g * hr_n[k] + (U.y * U.y + V.y * V.y) / (2 * om);
+      PE.y = P.y + d.g * hr_n[k] + (U.y * U.y + V.y * V.y) * r2om;
     }
     rU[k] = A; rV[k] = Bv; rZ[k] = UP; rP[k] = VP; rE[k] = PE;
   }
@@ -233,7 +242,10 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, const double2
 }
 
 // ------------------------------------------------------------------------------------------------ analysis + RK4
-constexpr int ANA_THREADS = 64;
+// Block: ANA_CHUNKS warps for 32 spectral coefficients (lane = coefficient, coalesced latitude-major tables).
+// Warp c sums the latitude pairs jh = c, c + ANA_CHUNKS, ...; the pieces meet in shared memory and warp 0 forms
+// the tendencies and applies the RK4 stage update.
+constexpr int ANA_CHUNKS = 8, ANA_THREADS = 32 * ANA_CHUNKS, ANA_Q = 14;
 
 struct StageArgs {
   int stage;        // 0..3
@@ -244,32 +256,53 @@ struct StageArgs {
 // x0: state, xs: stage input (written for stages 0-2), acc: RK4 accumulator. All [B][3][ntri].
 __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, const double2 *__restrict__ fold, StageArgs sa, double2 *x0,
                                                             double2 *xs, double2 *acc) {
+  __shared__ double part[ANA_CHUNKS][ANA_Q][33];
   const int b = blockIdx.y;
-  const int q = blockIdx.x * ANA_THREADS + threadIdx.x;
-  if (q >= d.ntri) return;
-  const int m = d.trim[q], n = d.trin[q], par = (n - m) & 1;
+  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
+  const int q = blockIdx.x * 32 + lane;
+  const bool live = q < d.ntri;
+  const int m = live ? d.trim[q] : 0, n = live ? d.trin[q] : 0, par = (n - m) & 1;
   const double2 *fb = fold + static_cast<size_t>(b) * d.nh * NSLOT * 2 * d.M;
   const int sP = par * d.M + m, sH = (1 - par) * d.M + m;  // parity slot for P and H terms
   double2 aP = make_double2(0, 0), bH = aP, bP = aP, aH = aP, uP = aP, vH = aP, eP = aP;
-  for (int jh = 0; jh < d.nh; jh++) {
-    const double P = d.Pa[static_cast<size_t>(jh) * d.ntri + q], H = d.Ha[static_cast<size_t>(jh) * d.ntri + q];
-    const double2 *g = fb + static_cast<size_t>(jh) * NSLOT * 2 * d.M;
-    aP = cfma(aP, g[0 * 2 * d.M + sP], P);
-    aH = cfma(aH, g[0 * 2 * d.M + sH], H);
-    bP = cfma(bP, g[1 * 2 * d.M + sP], P);
-    bH = cfma(bH, g[1 * 2 * d.M + sH], H);
-    uP = cfma(uP, g[2 * 2 * d.M + sP], P);
-    vH = cfma(vH, g[3 * 2 * d.M + sH], H);
-    eP = cfma(eP, g[4 * 2 * d.M + sP], P);
+  if (live) {
+#pragma unroll 2
+    for (int jh = c; jh < d.nh; jh += ANA_CHUNKS) {
+      const double P = d.Pa[static_cast<size_t>(jh) * d.ntri + q], H = d.Ha[static_cast<size_t>(jh) * d.ntri + q];
+      const double2 *g = fb + static_cast<size_t>(jh) * NSLOT * 2 * d.M;
+      aP = cfma(aP, g[0 * 2 * d.M + sP], P);
+      aH = cfma(aH, g[0 * 2 * d.M + sH], H);
+      bP = cfma(bP, g[1 * 2 * d.M + sP], P);
+      bH = cfma(bH, g[1 * 2 * d.M + sH], H);
+      uP = cfma(uP, g[2 * 2 * d.M + sP], P);
+      vH = cfma(vH, g[3 * 2 * d.M + sH], H);
+      eP = cfma(eP, g[4 * 2 * d.M + sP], P);
+    }
   }
+  const double v[ANA_Q] = {aP.x, aP.y, aH.x, aH.y, bP.x, bP.y, bH.x, bH.y, uP.x, uP.y, vH.x, vH.y, eP.x, eP.y};
+#pragma unroll
+  for (int i = 0; i < ANA_Q; i++) part[c][i][lane] = v[i];
+  __syncthreads();
+  if (c != 0 || !live) return;
+  double t[ANA_Q];
+#pragma unroll
+  for (int i = 0; i < ANA_Q; i++) {
+    double acc_i = 0;
+#pragma unroll
+    for (int k = 0; k < ANA_CHUNKS; k++) acc_i += part[k][i][lane];
+    t[i] = acc_i;
+  }
+  aP = make_double2(t[0], t[1]); aH = make_double2(t[2], t[3]); bP = make_double2(t[4], t[5]); bH = make_double2(t[6], t[7]);
+  uP = make_double2(t[8], t[9]); vH = make_double2(t[10], t[11]); eP = make_double2(t[12], t[13]);
   const double mm = static_cast<double>(m);
   // cpp/sphere.cpp:380-383: dz = -D(A,B), dd = D(B,-A) + n(n+1)/a^2 (Phi + E), df = -D(U Phi, V Phi)
   double2 kz = csub(bH, imul(aP, mm));
-  double2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, n * (n + 1.0) / (d.a * d.a)));
+  double2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, d.lapl[n]));
   double2 kf = csub(vH, imul(uP, mm));
   if (q == 0) kz = kd = kf = make_double2(0, 0);  // cpp/sphere.cpp:387-389
   const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
   const double2 k[3] = {kz, kd, kf};
+#pragma unroll
   for (int f = 0; f < 3; f++) {
     const size_t i = base + static_cast<size_t>(f) * d.ntri;
     if (sa.stage == 0) {
@@ -280,9 +313,9 @@ __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, const doub
       xs[i] = cadd(x0[i], cscale(k[f], sa.c));
     } else {
       // cpp/sphere.cpp:428-434: x += dt/6 (k1 + 2k2 + 2k3 + k4), then the del^4 filter
-      double2 v = cadd(x0[i], cscale(cadd(acc[i], k[f]), sa.c));
+      double2 val = cadd(x0[i], cscale(cadd(acc[i], k[f]), sa.c));
       const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
-      x0[i] = q == 0 ? v : cscale(v, fac);
+      x0[i] = q == 0 ? val : cscale(val, fac);
     }
   }
 }
@@ -514,6 +547,9 @@ static SphDev make_sph(const SphereEngine &e, const SphereTables &t) {
   d.w = t.w.p;
   d.wd = t.wd.p;
   d.cosl = t.cosl.p;
+  d.r2om = t.r2om.p;
+  d.kfac = t.kfac.p;
+  d.lapl = t.lapl.p;
   d.tw = t.tw.p;
   d.trim = t.trim.p;
   d.trin = t.trin.p;
@@ -565,6 +601,15 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   }
   up(tab->wd, wd);
   up(tab->cosl, cl);
+  std::vector<double> r2(nlat), kf(M, 0.0), lp(M, 0.0);
+  for (int j = 0; j < nlat; j++) r2[j] = 1.0 / (2 * (1 - h.mu[j] * h.mu[j]));
+  for (int n = 1; n <= N; n++) {
+    kf[n] = -p.radius * p.radius / (n * (n + 1.0));            // cpp/sphere.cpp:187
+    lp[n] = n * (n + 1.0) / (p.radius * p.radius);             // cpp/sphere.cpp:382
+  }
+  up(tab->r2om, r2);
+  up(tab->kfac, kf);
+  up(tab->lapl, lp);
   std::vector<double2> tw(nlon / 2);
   for (int k = 0; k < nlon / 2; k++) {
     double ang = -2 * kPi * k / nlon;
@@ -657,7 +702,7 @@ void SphereEngine::synth_grids(int member_first, int count) {
   SphDev d = make_sph(*this, *tab);
   const size_t st = static_cast<size_t>(member_first) * 3 * ntri;
   const size_t fo = static_cast<size_t>(member_first) * nlat * 4 * M;
-  dim3 g((nh + SYN_THREADS - 1) / SYN_THREADS, N / 2 + 1, count);
+  dim3 g((nh + 31) / 32, M, count);
   sph_synth<<<g, SYN_THREADS, 0, stream>>>(d, reinterpret_cast<const double2 *>(x0.p) + st, reinterpret_cast<double2 *>(four.p) + fo);
   LMW_LAUNCH_CHECK();
   g_launches += 1;
@@ -866,7 +911,7 @@ void SphereEngine::upload_filter(double dt) {
 void SphereEngine::launch_stage(int stage, double dt) {
   SphDev d = make_sph(*this, *tab);
   const double2 *in = reinterpret_cast<const double2 *>(stage == 0 ? x0.p : xs.p);
-  dim3 gs((nh + SYN_THREADS - 1) / SYN_THREADS, N / 2 + 1, B);
+  dim3 gs((nh + 31) / 32, M, B);
   sph_synth<<<gs, SYN_THREADS, 0, stream>>>(d, in, reinterpret_cast<double2 *>(four.p));
   const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
   sph_grid<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), fgrid.p, hsgrid.p,
@@ -875,7 +920,7 @@ void SphereEngine::launch_stage(int stage, double dt) {
   sa.stage = stage;
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
   sa.filt = filt.p;
-  sph_analysis<<<dim3((ntri + ANA_THREADS - 1) / ANA_THREADS, B), ANA_THREADS, 0, stream>>>(
+  sph_analysis<<<dim3((ntri + 31) / 32, B), ANA_THREADS, 0, stream>>>(
       d, reinterpret_cast<const double2 *>(fold.p), sa, reinterpret_cast<double2 *>(x0.p), reinterpret_cast<double2 *>(xs.p),
       reinterpret_cast<double2 *>(acc.p));
   LMW_LAUNCH_CHECK();
@@ -886,7 +931,7 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
   upload_filter(dt);
   SphDev d = make_sph(*this, *tab);
   const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
-  dim3 gs((nh + SYN_THREADS - 1) / SYN_THREADS, N / 2 + 1, B);
+  dim3 gs((nh + 31) / 32, M, B);
   StageArgs sa;
   sa.stage = 1;
   sa.c = 0.5 * dt;
@@ -897,7 +942,7 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
                                                           reinterpret_cast<double2 *>(fold.p));
   };
   auto ana = [&] {
-    sph_analysis<<<dim3((ntri + ANA_THREADS - 1) / ANA_THREADS, B), ANA_THREADS, 0, stream>>>(
+    sph_analysis<<<dim3((ntri + 31) / 32, B), ANA_THREADS, 0, stream>>>(
         d, reinterpret_cast<const double2 *>(fold.p), sa, reinterpret_cast<double2 *>(x0.p), reinterpret_cast<double2 *>(xs.p),
         reinterpret_cast<double2 *>(acc.p));
   };

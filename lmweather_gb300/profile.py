@@ -1,0 +1,50 @@
+"""Run one named workload for a fixed number of RK4 steps: the command that profiler captures wrap.
+
+    python -m lmweather_gb300.profile --case t42 --steps 4
+    ncu --metrics gpu__time_duration.sum --clock-control none --csv python -m lmweather_gb300.profile --case t42 --steps 4
+
+Cases: t42 (config-0 sphere, FP64), t170 (sphere T170, dt 450 s), plane (1024 x 512 beta-plane jet, dt 60 s).
+One untimed warm-up step runs first.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+A = 6.37122e6
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default="t42", choices=["t42", "t85", "t170", "t341", "plane"])
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--precision", type=int, default=0)
+    args = ap.parse_args()
+    import lmweather_gb300 as lw
+    from lmweather_gb300 import build
+
+    build.build()
+    t0 = time.perf_counter()
+    if args.case == "plane":
+        p = lw.Plane(1024, 512, 1024 * 5000.0, 512 * 5000.0, f0=1e-4, beta=1.6e-11, gravity=9.81, depth=100.0)
+        p.jet(20.0, 1.0e5, 0.1, 1)
+        p.step(60.0)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            p.step(60.0)
+        print(f"plane 1024x512: {args.steps} steps in {time.perf_counter() - t0:.4f} s")
+        return 0
+    T, dt = {"t42": (42, 900.0), "t85": (85, 450.0), "t170": (170, 450.0), "t341": (341, 225.0)}[args.case]
+    nu = A ** 4 / (86400.0 * (T * (T + 1)) ** 2)
+    s = lw.Sphere(T, diffusion=nu, precision=args.precision, max_truncation=max(T, 170))
+    s.turbulence(1, 8000.0, 30.0, T // 2)
+    s.step(dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.step(dt)
+    print(f"sphere T{T}: {args.steps} steps in {time.perf_counter() - t0:.4f} s")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
