@@ -138,6 +138,27 @@ int lmw_plane_time(const lmw_plane *p, double *out);
 int lmw_plane_diagnostics(lmw_plane *p, double *out);
 /* the handle's CUDA stream (a cudaStream_t) */
 int lmw_plane_stream(const lmw_plane *p, void **stream);
+
+/* Allocation-free RK4 stepping of the plane, for callers that cannot allocate device memory: code that runs
+ * inside a fixed memory budget taken up front, a real-time loop where cudaMalloc would stall on device-wide
+ * synchronisation, or a host that hands out device memory only from its own pool. No counterpart in the
+ * reference (whose Plane::step, cpp/plane.cpp:143-158, allocates its stage vectors on the host heap).
+ *
+ * h, u (nx*ny doubles) and v (nx*(ny+1) doubles) are caller-owned DEVICE pointers in the layouts above; they
+ * are advanced in place by `steps` RK4 steps of size dt with the same kernels, and the same bits, as
+ * lmw_plane_step. The parameters mean what they mean in lmw_plane_create. The call only enqueues work on
+ * `stream` (a cudaStream_t; NULL is the default stream) and returns; the fields are ready when the stream
+ * reaches that point. It calls no cudaMalloc, cudaFree or other allocating routine: the stage inputs and the
+ * accumulator live in one fixed device array that every GPU loading this library reserves until the process
+ * exits (about 19 MB). Grids above 262144 cells (nx*ny) are rejected with LMW_INVALID_ARGUMENT.
+ *
+ * The first call on a device looks up that array's device address (once per device, with that device
+ * current); make that first call before any stream capture. Every call shares the array and it keeps the last
+ * call's contents (each step overwrites what it reads, so nothing needs clearing): calls whose work overlaps on
+ * the GPU, on different streams or different threads, race on it and must be serialised by the caller. */
+int lmw_plane_step_noalloc(int nx, int ny, double lx, double ly, double gravity, double depth, double f0, double beta,
+                           double viscosity, double drag, int linear, double *h, double *u, double *v, double dt, int steps,
+                           void *stream);
 /* average device time (ms) of one RK4-stage kernel launch over `reps` launches; the state is left unchanged.
  * No reference counterpart (measurement hook). */
 int lmw_plane_kernel_time(lmw_plane *p, double dt, int reps, double *ms);

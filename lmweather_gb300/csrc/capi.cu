@@ -283,6 +283,25 @@ int lmw_plane_run(lmw_plane *p, double seconds, double dt) { return PLN(p->e->ru
 int lmw_plane_stable_dt(lmw_plane *p, double safety, double *out) { return PLN(*out = p->e->stable_dt(safety)); }
 int lmw_plane_time(const lmw_plane *p, double *out) { return PLN(*out = p->e->t); }
 int lmw_plane_diagnostics(lmw_plane *p, double *out) { return PLN(p->e->diagnostics(out)); }
+int lmw_plane_step_noalloc(int nx, int ny, double lx, double ly, double gravity, double depth, double f0, double beta,
+                           double viscosity, double drag, int linear, double *h, double *u, double *v, double dt, int steps,
+                           void *stream) {
+  return guard([&] {
+    lmw::PlaneConfig c;
+    c.nx = nx;
+    c.ny = ny;
+    c.lx = lx;
+    c.ly = ly;
+    c.gravity = gravity;
+    c.depth = depth;
+    c.f0 = f0;
+    c.beta = beta;
+    c.viscosity = viscosity;
+    c.drag = drag;
+    c.linear = linear != 0;
+    lmw::plane_step_noalloc(c, h, u, v, dt, steps, static_cast<cudaStream_t>(stream));
+  });
+}
 int lmw_plane_stream(const lmw_plane *p, void **stream) { return PLN(*stream = static_cast<void *>(p->e->stream)); }
 int lmw_plane_kernel_time(lmw_plane *p, double dt, int reps, double *ms) {
   return PLN({

@@ -63,6 +63,9 @@ class PlaneEngine {
   void launch_chunk(double dt, int steps);
 };
 
+// RK4 steps of caller-owned device fields with the scratch in a fixed device array (no allocation)
+void plane_step_noalloc(const PlaneConfig &c, double *h, double *u, double *v, double dt, int steps, cudaStream_t stream);
+
 // ------------------------------------------------------------------------------------------------ sphere
 // Mirrors lmweather::SphereParams (cpp/sphere.hpp:20-25) plus the engine's precision mode.
 enum Precision { kFP64 = 0, kFP32 = 1, kSplitBF16 = 2 };

@@ -8,6 +8,7 @@
 // bitwise identical to cpp/plane.cpp:59-158 built without FMA contraction.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "engine.h"
 
@@ -239,7 +240,62 @@ double irwin_hall(uint64_t &st) {
   return s - 6.0;
 }
 
+// Scratch of lmw_plane_step_noalloc: the two RK4 stage inputs and the accumulator (three fields each), in
+// device memory reserved when the library is loaded, so that the entry point never allocates. Each field slot
+// holds kNoAllocFieldCap doubles: up to kNoAllocMaxCells cells for h and u, plus one row (nx <= 4000) for v.
+constexpr size_t kNoAllocMaxCells = 262144;
+constexpr size_t kNoAllocFieldCap = kNoAllocMaxCells + 4096;
+static __device__ __align__(256) double g_noalloc_scratch[9 * kNoAllocFieldCap];
+
 }  // namespace
+
+// Device address of g_noalloc_scratch on the current device. In host code the symbol's name is only a host-side
+// stand-in, never a device address; the address is looked up once per device (with that device current) and
+// cached. The first call on a device does this look-up.
+static double *noalloc_scratch() {
+  static std::mutex mu;
+  static double *addr[64] = {nullptr};
+  int dev = 0;
+  LMW_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) throw InvalidArgument("lmw_plane_step_noalloc: device ordinal out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    LMW_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    addr[dev] = static_cast<double *>(p);
+  }
+  return addr[dev];
+}
+
+void plane_step_noalloc(const PlaneConfig &c, double *h, double *u, double *v, double dt, int steps, cudaStream_t stream) {
+  if (c.nx < 4 || c.ny < 4 || c.nx > 4000 || c.ny > 4000 || static_cast<int64_t>(c.nx) * c.ny > 8000000)
+    throw InvalidArgument("grid must be at least 4 x 4 and at most 8 million cells");
+  if (!(c.lx > 0 && c.ly > 0)) throw InvalidArgument("domain sizes must be positive");
+  const size_t cells = static_cast<size_t>(c.nx) * c.ny;
+  if (cells > kNoAllocMaxCells)
+    throw InvalidArgument("lmw_plane_step_noalloc: the grid has " + std::to_string(cells) + " cells; this entry point's fixed scratch holds at most " +
+                          std::to_string(kNoAllocMaxCells) + " cells (use lmw_plane_create for larger grids)");
+  if (!h || !u || !v) throw InvalidArgument("lmw_plane_step_noalloc: field pointer is null");
+  if (steps < 0) throw InvalidArgument("lmw_plane_step_noalloc: steps must not be negative");
+  if (!std::isfinite(dt)) throw InvalidArgument("lmw_plane_step_noalloc: dt must be finite");
+  double *sc = noalloc_scratch();
+  double *ha = sc, *ua = sc + kNoAllocFieldCap, *va = sc + 2 * kNoAllocFieldCap;
+  double *hb = sc + 3 * kNoAllocFieldCap, *ub = sc + 4 * kNoAllocFieldCap, *vb = sc + 5 * kNoAllocFieldCap;
+  double *ah = sc + 6 * kNoAllocFieldCap, *au = sc + 7 * kNoAllocFieldCap, *av = sc + 8 * kNoAllocFieldCap;
+  // every stage-0 launch writes all of a and the accumulator before any later stage reads them: nothing in the
+  // scratch has to start at zero
+  PlaneDev d = make_dev(c);
+  dim3 grid((c.nx + TX - 1) / TX, (c.ny + TY - 1) / TY), block(TX, TY);
+  const double half = 0.5 * dt, c6 = dt / 6;
+  for (int s = 0; s < steps; s++) {
+    plane_stage<<<grid, block, 0, stream>>>(d, 0, half, h, u, v, h, u, v, ah, au, av, ha, ua, va);
+    plane_stage<<<grid, block, 0, stream>>>(d, 1, half, ha, ua, va, h, u, v, ah, au, av, hb, ub, vb);
+    plane_stage<<<grid, block, 0, stream>>>(d, 2, dt, hb, ub, vb, h, u, v, ah, au, av, ha, ua, va);
+    plane_stage<<<grid, block, 0, stream>>>(d, 3, c6, ha, ua, va, h, u, v, ah, au, av, nullptr, nullptr, nullptr);
+    LMW_LAUNCH_CHECK();
+    g_launches += 4;
+  }
+}
 
 PlaneEngine::PlaneEngine(const PlaneConfig &c) : p(c) {
   // cpp/plane.cpp:20-25
