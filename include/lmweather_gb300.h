@@ -39,6 +39,13 @@ const char *lmw_version(void);
 /* number of this library's kernel launches issued by the calling thread so far */
 uint64_t lmw_launch_count(void);
 
+/* The engine's split-BF16 tensor-core GEMM (tcgen05, FP32 accumulation in tensor memory) on one problem from
+ * host arrays: D (128 x N) = A (128 x K) * B (N x K)^T with A and B split on the device into `terms` = 1 (BF16),
+ * 3 (hi/lo) or 6 (hi/mid/lo) BF16 products. N and K multiples of 16, N <= 256. `layout` selects the shared-memory
+ * descriptor stride convention (0, the engine's). kernel_status receives the kernel's error code (0: every wait
+ * on the tensor cores completed). Validation hook; no reference counterpart. */
+int lmw_tc_gemm_selftest(const float *A, const float *B, float *D, int N, int K, int terms, int layout, int *kernel_status);
+
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (the roofline of the FP64 paths) */
 int lmw_fp64_peak(double *tflops);
 

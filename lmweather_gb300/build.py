@@ -28,6 +28,7 @@ UNITS = [
     ("sphere32.cu", []),
     ("capi.cu", []),
     ("peak.cu", []),
+    ("tc_gemm.cu", []),
     ("sphere_tables.cpp", []),
 ]
 

@@ -7,6 +7,7 @@
 #include "../../include/lmweather_gb300.h"
 #include "engine.h"
 #include "sphere_tables.h"
+#include "tc_gemm.h"
 
 struct lmw_sphere {
   lmw::SphereEngine *e;
@@ -65,6 +66,12 @@ extern "C" {
 const char *lmw_last_error(void) { return g_err.c_str(); }
 const char *lmw_version(void) { return "lmweather-gb300 0.1.0"; }
 uint64_t lmw_launch_count(void) { return lmw::g_launches; }
+int lmw_tc_gemm_selftest(const float *A, const float *B, float *D, int N, int K, int terms, int layout, int *kernel_status) {
+  return guard([&] {
+    need(A && B && D && kernel_status, "pointer is null");
+    *kernel_status = lmw::tc_gemm_selftest(A, B, D, N, K, terms, layout);
+  });
+}
 int lmw_fp64_peak(double *tflops) {
   return guard([&] {
     need(tflops != nullptr, "output pointer is null");

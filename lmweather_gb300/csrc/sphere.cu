@@ -28,7 +28,10 @@ struct SphereTables {
   HostTables host;
   DevBuf<double> Ps, Hs, Pa, Ha;  // coefficient-major [tri][jh] (synthesis) and latitude-major [jh][tri] (analysis)
   DevBuf<double> mu, w, wd, cosl, r2om, kfac, lapl;
-  DevBuf<double2> tw;  // exp(-2 pi i k / nlon), k < nlon/2
+  DevBuf<double2> tw;
+  // FP32 copies for the reduced-precision stage kernels
+  DevBuf<float> Ps32, Hs32, Pa32, Ha32, w32, wd32, r2om32, kfac32, lapl32;
+  DevBuf<float2> tw32;  // exp(-2 pi i k / nlon), k < nlon/2
   DevBuf<int> trim, trin, tri;
 };
 
@@ -40,6 +43,24 @@ struct SphDev {
   const double *Ps, *Hs, *Pa, *Ha, *mu, *w, *wd, *cosl, *r2om, *kfac, *lapl;
   const double2 *tw;
   const int *trim, *trin, *tri;
+};
+
+template <class R> struct V2;
+template <> struct V2<double> { using type = double2; };
+template <> struct V2<float> { using type = float2; };
+__device__ __forceinline__ double2 mk2(double x, double y) { return make_double2(x, y); }
+__device__ __forceinline__ float2 mk2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cfma(float2 acc, float2 a, float s) { return make_float2(fmaf(a.x, s, acc.x), fmaf(a.y, s, acc.y)); }
+__device__ __forceinline__ float2 conjd(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 imul(float2 z, float m) { return make_float2(-m * z.y, m * z.x); }
+// Legendre tables, weights and twiddles in the compute precision of a stage kernel
+template <class R> struct SphTab {
+  const R *Ps, *Hs, *Pa, *Ha, *w, *wd, *r2om, *kfac, *lapl;
+  const typename V2<R>::type *tw;
 };
 
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
@@ -58,23 +79,27 @@ __device__ __forceinline__ double2 imul(double2 z, double m) { return make_doubl
 constexpr int SYN_CHUNKS = 8, SYN_THREADS = 32 * SYN_CHUNKS, SYN_Q = 12;
 
 // x: [B][3][ntri] (zeta, delta, phi); four: [B][nlat][4][M] (U, V, zeta, Phi)
-__global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, const double2 *__restrict__ x, double2 *__restrict__ four) {
-  __shared__ double part[SYN_CHUNKS][SYN_Q][33];
+template <class R>
+__global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, SphTab<R> t, const double2 *__restrict__ x,
+                                                         typename V2<R>::type *__restrict__ four) {
+  using C2 = typename V2<R>::type;
+  __shared__ R part[SYN_CHUNKS][SYN_Q][33];
   const int b = blockIdx.z, m = blockIdx.y;
   const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
   const int jh = blockIdx.x * 32 + lane;
   const bool live = jh < d.nh;
   const double2 *xz = x + static_cast<size_t>(b) * 3 * d.ntri, *xd = xz + d.ntri, *xf = xd + d.ntri;
-  double2 sp = make_double2(0, 0), sc = sp, hp = sp, hc = sp, zs = sp, fs = sp;
+  C2 sp = mk2(R(0), R(0)), sc = sp, hp = sp, hc = sp, zs = sp, fs = sp;
   const int base = d.tri[m];
   if (live) {
 #pragma unroll 2
     for (int n = m + c; n <= d.N; n += SYN_CHUNKS) {
       const int q = base + n - m;
-      const double P = d.Ps[static_cast<size_t>(q) * d.nh + jh], H = d.Hs[static_cast<size_t>(q) * d.nh + jh];
-      const double2 z = xz[q], dl = xd[q], f = xf[q];
-      const double k = d.kfac[n];  // psi = -a^2/(n(n+1)) zeta, cpp/sphere.cpp:185-190
-      const double2 psi = cscale(z, k), chi = cscale(dl, k);
+      const R P = t.Ps[static_cast<size_t>(q) * d.nh + jh], H = t.Hs[static_cast<size_t>(q) * d.nh + jh];
+      const double2 zd = xz[q], dd = xd[q], fd = xf[q];
+      const C2 z = mk2(R(zd.x), R(zd.y)), dl = mk2(R(dd.x), R(dd.y)), f = mk2(R(fd.x), R(fd.y));
+      const R k = t.kfac[n];  // psi = -a^2/(n(n+1)) zeta, cpp/sphere.cpp:185-190
+      const C2 psi = cscale(z, k), chi = cscale(dl, k);
       sp = cfma(sp, psi, P);
       sc = cfma(sc, chi, P);
       hp = cfma(hp, psi, H);
@@ -83,7 +108,7 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, const double2
       fs = cfma(fs, f, P);
     }
   }
-  const double v[SYN_Q] = {sp.x, sp.y, sc.x, sc.y, hp.x, hp.y, hc.x, hc.y, zs.x, zs.y, fs.x, fs.y};
+  const R v[SYN_Q] = {sp.x, sp.y, sc.x, sc.y, hp.x, hp.y, hc.x, hc.y, zs.x, zs.y, fs.x, fs.y};
 #pragma unroll
   for (int i = 0; i < SYN_Q; i++) part[c][i][lane] = v[i];
   __syncthreads();
@@ -91,10 +116,10 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, const double2
   const int side = threadIdx.x >> 5;  // 0: southern latitude (table latitude), 1: its northern mirror
   if (!live) return;
   // even (n - m) pieces are the chunks with even c, odd pieces the chunks with odd c
-  double e[SYN_Q], o[SYN_Q];
+  R e[SYN_Q], o[SYN_Q];
 #pragma unroll
   for (int i = 0; i < SYN_Q; i++) {
-    double se = 0, so = 0;
+    R se = 0, so = 0;
 #pragma unroll
     for (int k = 0; k < SYN_CHUNKS; k += 2) {
       se += part[k][i][lane];
@@ -104,24 +129,29 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, const double2
     o[i] = so;
   }
   // southern latitude: even + odd; northern mirror: P sums even - odd, H sums odd - even
-  double r[SYN_Q];
+  R r[SYN_Q];
 #pragma unroll
   for (int i = 0; i < SYN_Q; i++) {
     const bool hsum = i >= 4 && i < 8;
     r[i] = side == 0 ? e[i] + o[i] : (hsum ? o[i] - e[i] : e[i] - o[i]);
   }
-  const double mm = static_cast<double>(m);
-  const double2 SP = make_double2(r[0], r[1]), SC = make_double2(r[2], r[3]), HP = make_double2(r[4], r[5]), HC = make_double2(r[6], r[7]);
+  const R mm = static_cast<R>(m), ia = static_cast<R>(1.0 / d.a);
+  const C2 SP = mk2(r[0], r[1]), SC = mk2(r[2], r[3]), HP = mk2(r[4], r[5]), HC = mk2(r[6], r[7]);
   // cpp/sphere.cpp:200-201: fu = (i m sc - hp)/a, fv = (i m sp + hc)/a
-  double2 fu = csub(imul(SC, mm), HP), fv = cadd(imul(SP, mm), HC);
-  fu = make_double2(fu.x / d.a, fu.y / d.a);
-  fv = make_double2(fv.x / d.a, fv.y / d.a);
+  C2 fu = csub(imul(SC, mm), HP), fv = cadd(imul(SP, mm), HC);
+  if (sizeof(R) == 8) {
+    fu = mk2(R(fu.x / d.a), R(fu.y / d.a));
+    fv = mk2(R(fv.x / d.a), R(fv.y / d.a));
+  } else {
+    fu = cscale(fu, ia);
+    fv = cscale(fv, ia);
+  }
   const int j = side == 0 ? jh : d.nlat - 1 - jh;
-  double2 *out = four + (static_cast<size_t>(b) * d.nlat + j) * 4 * d.M;
+  C2 *out = four + (static_cast<size_t>(b) * d.nlat + j) * 4 * d.M;
   out[0 * d.M + m] = fu;
   out[1 * d.M + m] = fv;
-  out[2 * d.M + m] = make_double2(r[8], r[9]);
-  out[3 * d.M + m] = make_double2(r[10], r[11]);
+  out[2 * d.M + m] = mk2(r[8], r[9]);
+  out[3 * d.M + m] = mk2(r[10], r[11]);
 }
 
 // ------------------------------------------------------------------------------------------------ FFTs
@@ -129,7 +159,7 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, const double2
 // Inverse: decimation in time from bit-reversed input to natural output. Forward: decimation in frequency
 // from natural input to bit-reversed output. Twiddles exp(-2 pi i k / n) from the table (conjugated for the
 // inverse), computed on the host in FP64.
-__device__ void fft_inverse_dit(double2 *s, int rows, int n, int logn, const double2 *__restrict__ tw) {
+template <class C2> __device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw) {
   const int halfn = n >> 1;
   for (int st = 0; st < logn; st++) {
     const int half = 1 << st, stride = halfn >> st;
@@ -137,16 +167,16 @@ __device__ void fft_inverse_dit(double2 *s, int rows, int n, int logn, const dou
       const int r = e / halfn, bf = e - r * halfn;
       const int grp = bf >> st, pos = bf & (half - 1);
       const int i1 = grp * 2 * half + pos, i2 = i1 + half;
-      double2 *row = s + static_cast<size_t>(r) * n;
-      const double2 w = conjd(tw[pos * stride]);
-      const double2 t = cmul(w, row[i2]), u = row[i1];
+      C2 *row = s + static_cast<size_t>(r) * n;
+      const C2 w = conjd(tw[pos * stride]);
+      const C2 t = cmul(w, row[i2]), u = row[i1];
       row[i1] = cadd(u, t);
       row[i2] = csub(u, t);
     }
     __syncthreads();
   }
 }
-__device__ void fft_forward_dif(double2 *s, int rows, int n, int logn, const double2 *__restrict__ tw) {
+template <class C2> __device__ void fft_forward_dif(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw) {
   const int halfn = n >> 1;
   for (int st = logn - 1; st >= 0; st--) {
     const int half = 1 << st, stride = halfn >> st;
@@ -154,8 +184,8 @@ __device__ void fft_forward_dif(double2 *s, int rows, int n, int logn, const dou
       const int r = e / halfn, bf = e - r * halfn;
       const int grp = bf >> st, pos = bf & (half - 1);
       const int i1 = grp * 2 * half + pos, i2 = i1 + half;
-      double2 *row = s + static_cast<size_t>(r) * n;
-      const double2 u = row[i1], v = row[i2];
+      C2 *row = s + static_cast<size_t>(r) * n;
+      const C2 u = row[i1], v = row[i2];
       row[i1] = cadd(u, v);
       row[i2] = cmul(csub(u, v), tw[pos * stride]);
     }
@@ -167,20 +197,20 @@ __device__ __forceinline__ int bitrev(int k, int logn) { return static_cast<int>
 // Load the Fourier coefficients of `rows` fields at latitudes js (real part) and jn (imaginary part) into
 // bit-reversed rows: Y[m] = X_s[m] + i X_n[m], Y[n-m] = conj(X_s[m]) + i conj(X_n[m]); Im X[0] is dropped
 // as in cpp/sphere.cpp:132.
-__device__ void load_pair_spectra(double2 *s, int rows, const SphDev &d, const double2 *__restrict__ fs,
-                                  const double2 *__restrict__ fn, int fstride) {
+template <class C2>
+__device__ void load_pair_spectra(C2 *s, int rows, const SphDev &d, const C2 *__restrict__ fs, const C2 *__restrict__ fn, int fstride) {
   const int n = d.nlon;
-  for (int e = threadIdx.x; e < rows * n; e += blockDim.x) s[e] = make_double2(0, 0);
+  for (int e = threadIdx.x; e < rows * n; e += blockDim.x) s[e] = mk2(decltype(C2::x)(0), decltype(C2::x)(0));
   __syncthreads();
   for (int e = threadIdx.x; e < rows * d.M; e += blockDim.x) {
     const int r = e / d.M, m = e - r * d.M;
-    double2 a = fs[r * fstride + m], c = fn[r * fstride + m];
-    double2 *row = s + static_cast<size_t>(r) * n;
+    C2 a = fs[r * fstride + m], c = fn[r * fstride + m];
+    C2 *row = s + static_cast<size_t>(r) * n;
     if (m == 0) {
-      row[0] = make_double2(a.x, c.x);
+      row[0] = mk2(a.x, c.x);
     } else {
-      row[bitrev(m, d.logn)] = make_double2(a.x - c.y, a.y + c.x);
-      row[bitrev(n - m, d.logn)] = make_double2(a.x + c.y, c.x - a.y);
+      row[bitrev(m, d.logn)] = mk2(a.x - c.y, a.y + c.x);
+      row[bitrev(n - m, d.logn)] = mk2(a.x + c.y, c.x - a.y);
     }
   }
   __syncthreads();
@@ -191,49 +221,54 @@ constexpr int GRID_THREADS = 256;
 constexpr int NSLOT = 5;  // A, B, U Phi, V Phi (times w/((1-mu^2)a)) and the Bernoulli function (times w)
 
 // four: [B][nlat][4][M]; fold: [B][nh][NSLOT][2][M]; fgrid/hsgrid: [B][nlat][nlon]
-__global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, const double2 *__restrict__ four, const double *__restrict__ fgrid,
-                                                         const double *__restrict__ hsgrid, double2 *__restrict__ fold) {
-  extern __shared__ double2 sm[];
+template <class R>
+__global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, SphTab<R> t, const typename V2<R>::type *__restrict__ four,
+                                                         const double *__restrict__ fgrid, const double *__restrict__ hsgrid,
+                                                         typename V2<R>::type *__restrict__ fold) {
+  using C2 = typename V2<R>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C2 *sm = reinterpret_cast<C2 *>(smraw);
   const int b = blockIdx.y, jh = blockIdx.x;
   const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
-  const double2 *f_s = four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M;
-  const double2 *f_n = four + (static_cast<size_t>(b) * d.nlat + jn) * 4 * d.M;
+  const C2 *f_s = four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M;
+  const C2 *f_n = four + (static_cast<size_t>(b) * d.nlat + jn) * 4 * d.M;
   load_pair_spectra(sm, 4, d, f_s, f_n, d.M);
-  fft_inverse_dit(sm, 4, n, d.logn, d.tw);
+  fft_inverse_dit(sm, 4, n, d.logn, t.tw);
   // nonlinear products, cpp/sphere.cpp:348-359 (real part: southern latitude, imaginary part: northern)
-  const double r2om = d.r2om[js];  // 1 / (2 (1 - mu^2)), the same at the mirror latitude
+  const R r2om = t.r2om[js], g = static_cast<R>(d.g);  // 1 / (2 (1 - mu^2)), the same at the mirror latitude
   const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
   const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
-  double2 *rU = sm, *rV = sm + n, *rZ = sm + 2 * n, *rP = sm + 3 * n, *rE = sm + 4 * n;
+  C2 *rU = sm, *rV = sm + n, *rZ = sm + 2 * n, *rP = sm + 3 * n, *rE = sm + 4 * n;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const double2 U = rU[k], V = rV[k], Z = rZ[k], P = rP[k];
-    double2 A, Bv, UP, VP, PE;
+    const C2 U = rU[k], V = rV[k], Z = rZ[k], P = rP[k];
+    C2 A, Bv, UP, VP, PE;
     {
-      double eta = Z.x + fr_s[k];
+      R eta = Z.x + static_cast<R>(fr_s[k]);
       A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
-      PE.x = P.x + d.g * hr_s[k] + (U.x * U.x + V.x * V.x) * r2om;
+      PE.x = P.x + g * static_cast<R>(hr_s[k]) + (U.x * U.x + V.x * V.x) * r2om;
     }
     {
-      double eta = Z.y + fr_n[k];
+      R eta = Z.y + static_cast<R>(fr_n[k]);
       A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
-      PE.y = P.y + d.g * hr_n[k] + (U.y * U.y + V.y * V.y) * r2om;
+      PE.y = P.y + g * static_cast<R>(hr_n[k]) + (U.y * U.y + V.y * V.y) * r2om;
     }
     rU[k] = A; rV[k] = Bv; rZ[k] = UP; rP[k] = VP; rE[k] = PE;
   }
   __syncthreads();
-  fft_forward_dif(sm, NSLOT, n, d.logn, d.tw);
+  fft_forward_dif(sm, NSLOT, n, d.logn, t.tw);
   // separate the two latitudes, normalise by nlon (cpp/sphere.cpp:128), weight and fold
-  const double inv = 1.0 / n, wd = d.wd[js], wj = d.w[js];
-  double2 *o = fold + (static_cast<size_t>(b) * d.nh + jh) * NSLOT * 2 * d.M;
+  const R inv = R(1) / n, wd = t.wd[js], wj = t.w[js];
+  C2 *o = fold + (static_cast<size_t>(b) * d.nh + jh) * NSLOT * 2 * d.M;
   for (int e = threadIdx.x; e < NSLOT * d.M; e += blockDim.x) {
     const int r = e / d.M, m = e - r * d.M;
-    const double2 *row = sm + static_cast<size_t>(r) * n;
-    const double2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
+    const C2 *row = sm + static_cast<size_t>(r) * n;
+    const C2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
     // X_s = (Ym + conj(Y_{n-m}))/2, X_n = -i (Ym - conj(Y_{n-m}))/2
-    double2 Xs = cscale(cadd(Ym, Yc), 0.5 * inv);
-    double2 t = csub(Ym, Yc);
-    double2 Xn = make_double2(0.5 * inv * t.y, -0.5 * inv * t.x);
-    const double wt = r < 4 ? wd : wj;
+    const R hinv = R(0.5) * inv;
+    C2 Xs = cscale(cadd(Ym, Yc), hinv);
+    C2 tt = csub(Ym, Yc);
+    C2 Xn = mk2(hinv * tt.y, -hinv * tt.x);
+    const R wt = r < 4 ? wd : wj;
     Xs = cscale(Xs, wt);
     Xn = cscale(Xn, wt);
     o[(r * 2 + 0) * d.M + m] = cadd(Xs, Xn);
@@ -254,22 +289,24 @@ struct StageArgs {
 };
 
 // x0: state, xs: stage input (written for stages 0-2), acc: RK4 accumulator. All [B][3][ntri].
-__global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, const double2 *__restrict__ fold, StageArgs sa, double2 *x0,
-                                                            double2 *xs, double2 *acc) {
-  __shared__ double part[ANA_CHUNKS][ANA_Q][33];
+template <class R>
+__global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, SphTab<R> t, const typename V2<R>::type *__restrict__ fold,
+                                                            StageArgs sa, double2 *x0, double2 *xs, double2 *acc) {
+  using C2 = typename V2<R>::type;
+  __shared__ R part[ANA_CHUNKS][ANA_Q][33];
   const int b = blockIdx.y;
   const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
   const int q = blockIdx.x * 32 + lane;
   const bool live = q < d.ntri;
   const int m = live ? d.trim[q] : 0, n = live ? d.trin[q] : 0, par = (n - m) & 1;
-  const double2 *fb = fold + static_cast<size_t>(b) * d.nh * NSLOT * 2 * d.M;
+  const C2 *fb = fold + static_cast<size_t>(b) * d.nh * NSLOT * 2 * d.M;
   const int sP = par * d.M + m, sH = (1 - par) * d.M + m;  // parity slot for P and H terms
-  double2 aP = make_double2(0, 0), bH = aP, bP = aP, aH = aP, uP = aP, vH = aP, eP = aP;
+  C2 aP = mk2(R(0), R(0)), bH = aP, bP = aP, aH = aP, uP = aP, vH = aP, eP = aP;
   if (live) {
 #pragma unroll 2
     for (int jh = c; jh < d.nh; jh += ANA_CHUNKS) {
-      const double P = d.Pa[static_cast<size_t>(jh) * d.ntri + q], H = d.Ha[static_cast<size_t>(jh) * d.ntri + q];
-      const double2 *g = fb + static_cast<size_t>(jh) * NSLOT * 2 * d.M;
+      const R P = t.Pa[static_cast<size_t>(jh) * d.ntri + q], H = t.Ha[static_cast<size_t>(jh) * d.ntri + q];
+      const C2 *g = fb + static_cast<size_t>(jh) * NSLOT * 2 * d.M;
       aP = cfma(aP, g[0 * 2 * d.M + sP], P);
       aH = cfma(aH, g[0 * 2 * d.M + sH], H);
       bP = cfma(bP, g[1 * 2 * d.M + sP], P);
@@ -279,29 +316,30 @@ __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, const doub
       eP = cfma(eP, g[4 * 2 * d.M + sP], P);
     }
   }
-  const double v[ANA_Q] = {aP.x, aP.y, aH.x, aH.y, bP.x, bP.y, bH.x, bH.y, uP.x, uP.y, vH.x, vH.y, eP.x, eP.y};
+  const R v[ANA_Q] = {aP.x, aP.y, aH.x, aH.y, bP.x, bP.y, bH.x, bH.y, uP.x, uP.y, vH.x, vH.y, eP.x, eP.y};
 #pragma unroll
   for (int i = 0; i < ANA_Q; i++) part[c][i][lane] = v[i];
   __syncthreads();
   if (c != 0 || !live) return;
-  double t[ANA_Q];
+  R tsum[ANA_Q];
 #pragma unroll
   for (int i = 0; i < ANA_Q; i++) {
-    double acc_i = 0;
+    R acc_i = 0;
 #pragma unroll
     for (int k = 0; k < ANA_CHUNKS; k++) acc_i += part[k][i][lane];
-    t[i] = acc_i;
+    tsum[i] = acc_i;
   }
-  aP = make_double2(t[0], t[1]); aH = make_double2(t[2], t[3]); bP = make_double2(t[4], t[5]); bH = make_double2(t[6], t[7]);
-  uP = make_double2(t[8], t[9]); vH = make_double2(t[10], t[11]); eP = make_double2(t[12], t[13]);
-  const double mm = static_cast<double>(m);
+  aP = mk2(tsum[0], tsum[1]); aH = mk2(tsum[2], tsum[3]); bP = mk2(tsum[4], tsum[5]); bH = mk2(tsum[6], tsum[7]);
+  uP = mk2(tsum[8], tsum[9]); vH = mk2(tsum[10], tsum[11]); eP = mk2(tsum[12], tsum[13]);
+  const R mm = static_cast<R>(m);
   // cpp/sphere.cpp:380-383: dz = -D(A,B), dd = D(B,-A) + n(n+1)/a^2 (Phi + E), df = -D(U Phi, V Phi)
-  double2 kz = csub(bH, imul(aP, mm));
-  double2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, d.lapl[n]));
-  double2 kf = csub(vH, imul(uP, mm));
-  if (q == 0) kz = kd = kf = make_double2(0, 0);  // cpp/sphere.cpp:387-389
+  C2 kz = csub(bH, imul(aP, mm));
+  C2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
+  C2 kf = csub(vH, imul(uP, mm));
+  if (q == 0) kz = kd = kf = mk2(R(0), R(0));  // cpp/sphere.cpp:387-389
   const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
-  const double2 k[3] = {kz, kd, kf};
+  // the RK4 state accumulates in FP64 whatever the precision of the tendencies
+  const double2 k[3] = {make_double2(kz.x, kz.y), make_double2(kd.x, kd.y), make_double2(kf.x, kf.y)};
 #pragma unroll
   for (int f = 0; f < 3; f++) {
     const size_t i = base + static_cast<size_t>(f) * d.ntri;
@@ -557,12 +595,19 @@ static SphDev make_sph(const SphereEngine &e, const SphereTables &t) {
   return d;
 }
 
+static SphTab<double> tab64(const SphereTables &t) {
+  return SphTab<double>{t.Ps.p, t.Hs.p, t.Pa.p, t.Ha.p, t.w.p, t.wd.p, t.r2om.p, t.kfac.p, t.lapl.p, t.tw.p};
+}
+static SphTab<float> tab32(const SphereTables &t) {
+  return SphTab<float>{t.Ps32.p, t.Hs32.p, t.Pa32.p, t.Ha32.p, t.w32.p, t.wd32.p, t.r2om32.p, t.kfac32.p, t.lapl32.p, t.tw32.p};
+}
+
 SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   // cpp/sphere.cpp:75-103
   if (c.truncation < 4 || c.truncation > c.max_truncation)
     throw InvalidArgument("truncation must be between 4 and " + std::to_string(c.max_truncation));
   if (c.members < 1) throw InvalidArgument("an ensemble needs at least one member");
-  if (c.precision != kFP64) throw InvalidArgument("precision mode not available in this build");
+  if (c.precision != kFP64 && c.precision != kFP32) throw InvalidArgument("precision mode not available in this build");
   B = c.members;
   tab = new SphereTables();
   HostTables &h = tab->host;
@@ -617,6 +662,26 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   }
   tab->tw.alloc(tw.size());
   LMW_CUDA(cudaMemcpy(tab->tw.p, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  if (p.precision != kFP64) {
+    auto up32 = [&](DevBuf<float> &dst, const std::vector<double> &src) {
+      std::vector<float> f(src.begin(), src.end());
+      dst.alloc(f.size());
+      LMW_CUDA(cudaMemcpy(dst.p, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    };
+    up32(tab->Ps32, h.P);
+    up32(tab->Hs32, h.H);
+    up32(tab->Pa32, Pa);
+    up32(tab->Ha32, Ha);
+    up32(tab->w32, h.w);
+    up32(tab->wd32, wd);
+    up32(tab->r2om32, r2);
+    up32(tab->kfac32, kf);
+    up32(tab->lapl32, lp);
+    std::vector<float2> t32(tw.size());
+    for (size_t k = 0; k < tw.size(); k++) t32[k] = make_float2(static_cast<float>(tw[k].x), static_cast<float>(tw[k].y));
+    tab->tw32.alloc(t32.size());
+    LMW_CUDA(cudaMemcpy(tab->tw32.p, t32.data(), t32.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  }
   std::vector<int> tm(ntri), tn(ntri);
   for (int m = 0; m <= N; m++)
     for (int n = m; n <= N; n++) {
@@ -636,6 +701,10 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   acc.alloc(nst);
   four.alloc(static_cast<size_t>(B) * nlat * 4 * M * 2);
   fold.alloc(static_cast<size_t>(B) * nh * NSLOT * 2 * M * 2);
+  if (p.precision != kFP64) {
+    four32.alloc(static_cast<size_t>(B) * nlat * 4 * M * 2);
+    fold32.alloc(static_cast<size_t>(B) * nh * NSLOT * 2 * M * 2);
+  }
   fgrid.alloc(static_cast<size_t>(B) * ngrid());
   hsgrid.alloc(static_cast<size_t>(B) * ngrid());
   refgrid.alloc(static_cast<size_t>(B) * ngrid());
@@ -649,7 +718,8 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   hsgrid.zero(stream);
   refgrid.zero(stream);
   const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
-  LMW_CUDA(cudaFuncSetAttribute(sph_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  LMW_CUDA(cudaFuncSetAttribute(sph_grid<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  LMW_CUDA(cudaFuncSetAttribute(sph_grid<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   LMW_CUDA(cudaFuncSetAttribute(sph_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   LMW_CUDA(cudaFuncSetAttribute(sph_grid_in, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   for (int b = 0; b < B; b++) set_axis_tilt(0, b);
@@ -703,7 +773,8 @@ void SphereEngine::synth_grids(int member_first, int count) {
   const size_t st = static_cast<size_t>(member_first) * 3 * ntri;
   const size_t fo = static_cast<size_t>(member_first) * nlat * 4 * M;
   dim3 g((nh + 31) / 32, M, count);
-  sph_synth<<<g, SYN_THREADS, 0, stream>>>(d, reinterpret_cast<const double2 *>(x0.p) + st, reinterpret_cast<double2 *>(four.p) + fo);
+  sph_synth<double><<<g, SYN_THREADS, 0, stream>>>(d, tab64(*tab), reinterpret_cast<const double2 *>(x0.p) + st,
+                                                   reinterpret_cast<double2 *>(four.p) + fo);
   LMW_LAUNCH_CHECK();
   g_launches += 1;
 }
@@ -908,21 +979,32 @@ void SphereEngine::upload_filter(double dt) {
   filt_dt = dt;
 }
 
-void SphereEngine::launch_stage(int stage, double dt) {
-  SphDev d = make_sph(*this, *tab);
-  const double2 *in = reinterpret_cast<const double2 *>(stage == 0 ? x0.p : xs.p);
-  dim3 gs((nh + 31) / 32, M, B);
-  sph_synth<<<gs, SYN_THREADS, 0, stream>>>(d, in, reinterpret_cast<double2 *>(four.p));
-  const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
-  sph_grid<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), fgrid.p, hsgrid.p,
-                                                        reinterpret_cast<double2 *>(fold.p));
+// One RK4 stage in the engine's precision: FP64 tables and buffers, or FP32 (tendencies in FP32, the state in FP64)
+template <class R>
+static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage, double dt, const double *filt, const double2 *in,
+                          typename V2<R>::type *four, typename V2<R>::type *fold, double2 *x0, double2 *xs, double2 *acc,
+                          const double *fgrid, const double *hsgrid, cudaStream_t stream, int which = -1) {
+  const size_t smem = 5 * static_cast<size_t>(d.nlon) * sizeof(typename V2<R>::type);
   StageArgs sa;
   sa.stage = stage;
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
-  sa.filt = filt.p;
-  sph_analysis<<<dim3((ntri + 31) / 32, B), ANA_THREADS, 0, stream>>>(
-      d, reinterpret_cast<const double2 *>(fold.p), sa, reinterpret_cast<double2 *>(x0.p), reinterpret_cast<double2 *>(xs.p),
-      reinterpret_cast<double2 *>(acc.p));
+  sa.filt = filt;
+  if (which < 0 || which == 0) sph_synth<R><<<dim3((d.nh + 31) / 32, d.M, B), SYN_THREADS, 0, stream>>>(d, t, in, four);
+  if (which < 0 || which == 1) sph_grid<R><<<dim3(d.nh, B), GRID_THREADS, smem, stream>>>(d, t, four, fgrid, hsgrid, fold);
+  if (which < 0 || which == 2)
+    sph_analysis<R><<<dim3((d.ntri + 31) / 32, B), ANA_THREADS, 0, stream>>>(d, t, fold, sa, x0, xs, acc);
+}
+
+void SphereEngine::launch_stage(int stage, double dt) {
+  SphDev d = make_sph(*this, *tab);
+  const double2 *in = reinterpret_cast<const double2 *>(stage == 0 ? x0.p : xs.p);
+  double2 *X0 = reinterpret_cast<double2 *>(x0.p), *XS = reinterpret_cast<double2 *>(xs.p), *AC = reinterpret_cast<double2 *>(acc.p);
+  if (p.precision == kFP64)
+    stage_kernels<double>(d, tab64(*tab), B, stage, dt, filt.p, in, reinterpret_cast<double2 *>(four.p), reinterpret_cast<double2 *>(fold.p),
+                          X0, XS, AC, fgrid.p, hsgrid.p, stream);
+  else
+    stage_kernels<float>(d, tab32(*tab), B, stage, dt, filt.p, in, reinterpret_cast<float2 *>(four32.p), reinterpret_cast<float2 *>(fold32.p),
+                         X0, XS, AC, fgrid.p, hsgrid.p, stream);
   LMW_LAUNCH_CHECK();
   g_launches += 3;
 }
@@ -930,36 +1012,29 @@ void SphereEngine::launch_stage(int stage, double dt) {
 void SphereEngine::kernel_times(double dt, int reps, double *out) {
   upload_filter(dt);
   SphDev d = make_sph(*this, *tab);
-  const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
-  dim3 gs((nh + 31) / 32, M, B);
-  StageArgs sa;
-  sa.stage = 1;
-  sa.c = 0.5 * dt;
-  sa.filt = filt.p;
-  auto syn = [&] { sph_synth<<<gs, SYN_THREADS, 0, stream>>>(d, reinterpret_cast<const double2 *>(x0.p), reinterpret_cast<double2 *>(four.p)); };
-  auto grd = [&] {
-    sph_grid<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), fgrid.p, hsgrid.p,
-                                                          reinterpret_cast<double2 *>(fold.p));
-  };
-  auto ana = [&] {
-    sph_analysis<<<dim3((ntri + 31) / 32, B), ANA_THREADS, 0, stream>>>(
-        d, reinterpret_cast<const double2 *>(fold.p), sa, reinterpret_cast<double2 *>(x0.p), reinterpret_cast<double2 *>(xs.p),
-        reinterpret_cast<double2 *>(acc.p));
+  double2 *X0 = reinterpret_cast<double2 *>(x0.p), *XS = reinterpret_cast<double2 *>(xs.p), *AC = reinterpret_cast<double2 *>(acc.p);
+  // stage 1 reads x0 and writes the stage input and the accumulator: x0 is unchanged
+  auto one = [&](int which) {
+    if (p.precision == kFP64)
+      stage_kernels<double>(d, tab64(*tab), B, 1, dt, filt.p, X0, reinterpret_cast<double2 *>(four.p), reinterpret_cast<double2 *>(fold.p), X0,
+                            XS, AC, fgrid.p, hsgrid.p, stream, which);
+    else
+      stage_kernels<float>(d, tab32(*tab), B, 1, dt, filt.p, X0, reinterpret_cast<float2 *>(four32.p), reinterpret_cast<float2 *>(fold32.p),
+                           X0, XS, AC, fgrid.p, hsgrid.p, stream, which);
   };
   cudaEvent_t e0, e1;
   LMW_CUDA(cudaEventCreate(&e0));
   LMW_CUDA(cudaEventCreate(&e1));
-  int k = 0;
-  for (auto fn : {std::function<void()>(syn), std::function<void()>(grd), std::function<void()>(ana)}) {
-    fn();  // warm
+  for (int k = 0; k < 3; k++) {
+    one(k);  // warm
     LMW_CUDA(cudaEventRecord(e0, stream));
-    for (int r = 0; r < reps; r++) fn();
+    for (int r = 0; r < reps; r++) one(k);
     LMW_CUDA(cudaEventRecord(e1, stream));
     LMW_LAUNCH_CHECK();
     LMW_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
     LMW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    out[k++] = ms / reps;
+    out[k] = ms / reps;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -221,3 +221,26 @@ def test_t341_lifts_the_reference_cap(engine):
     o.step(225.0)
     s.step(225.0)
     assert_state_floor(s.get_state(), o.get_state())
+
+
+def height_l2_error(a, b):
+    return np.sqrt(((a - b) ** 2).mean()) / np.sqrt((b ** 2).mean())
+
+
+@pytest.mark.parametrize("T,dt,steps", [(42, 900.0, 96), (170, 450.0, 16)])
+def test_fp32_path_against_fp64(engine, T, dt, steps):
+    # FP32 Legendre sums, FFTs and products; FP64 state accumulation: the height stays within 1e-6 (relative L2)
+    nu = 6.37122e6 ** 4 / (86400.0 * (T * (T + 1)) ** 2)
+    runs = {}
+    for prec in (engine.FP64, engine.FP32):
+        s = engine.Sphere(T, diffusion=nu, precision=prec)
+        s.turbulence(4, 8000.0, 30.0, T // 2)
+        for _ in range(steps):
+            s.step(dt)
+        runs[prec] = (s.grid_height(), s.diagnostics())
+    err = height_l2_error(runs[engine.FP32][0], runs[engine.FP64][0])
+    print(f"T{T} FP32 vs FP64 after {steps} steps: height relative L2 {err:.3e}")
+    assert err < 1e-6
+    d32, d64 = runs[engine.FP32][1], runs[engine.FP64][1]
+    assert d32["mean_height"] == pytest.approx(d64["mean_height"], rel=1e-12)
+    assert d32["energy"] == pytest.approx(d64["energy"], rel=1e-6)
