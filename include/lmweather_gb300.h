@@ -58,6 +58,10 @@ int lmw_sphere_create(int truncation, double radius, double omega, double gravit
  * states sharing the truncation (stepped together), and a truncation cap up to 341. */
 int lmw_sphere_create_ex(int truncation, double radius, double omega, double gravity, double diffusion, int precision,
                          int members, int max_truncation, lmw_sphere **out);
+/* Split-precision engine with an explicit number of BF16 products per Legendre term: 3 (hi/lo pieces, about 16
+ * significant bits) or 6 (hi/mid/lo, FP32 level). lmw_sphere_create_ex with LMW_SPLIT_BF16 uses 3. */
+int lmw_sphere_create_split(int truncation, double radius, double omega, double gravity, double diffusion, int members, int max_truncation,
+                            int split_terms, lmw_sphere **out);
 int lmw_sphere_destroy(lmw_sphere *s);
 /* Sphere::truncation/nlat/nlon (cpp/sphere.hpp:30-32) and the member count */
 int lmw_sphere_dims(const lmw_sphere *s, int *truncation, int *nlat, int *nlon, int *members);

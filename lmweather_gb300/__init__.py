@@ -39,6 +39,7 @@ _SIGS = {
     "lmw_launch_count": (C.c_uint64, []),
     "lmw_sphere_create": (_I, [_I, _D, _D, _D, _D, _PP]),
     "lmw_sphere_create_ex": (_I, [_I, _D, _D, _D, _D, _I, _I, _I, _PP]),
+    "lmw_sphere_create_split": (_I, [_I, _D, _D, _D, _D, _I, _I, _I, _PP]),
     "lmw_sphere_destroy": (_I, [_P]),
     "lmw_sphere_dims": (_I, [_P, _IP, _IP, _IP, _IP]),
     "lmw_sphere_gauss": (_I, [_P, _DP, _DP]),
@@ -127,11 +128,15 @@ class Sphere:
     take `member=`."""
 
     def __init__(self, truncation: int, radius=6.37122e6, omega=7.292e-5, gravity=9.80616, diffusion=0.0,
-                 precision: int = FP64, members: int = 1, max_truncation: int = 170):
+                 precision: int = FP64, members: int = 1, max_truncation: int = 170, split_terms: int = 3):
         self._lib = load_library()
         h = C.c_void_p()
-        _check(self._lib.lmw_sphere_create_ex(truncation, radius, omega, gravity, diffusion, precision, members,
-                                              max_truncation, C.byref(h)))
+        if precision == SPLIT_BF16:
+            _check(self._lib.lmw_sphere_create_split(truncation, radius, omega, gravity, diffusion, members, max_truncation,
+                                                     split_terms, C.byref(h)))
+        else:
+            _check(self._lib.lmw_sphere_create_ex(truncation, radius, omega, gravity, diffusion, precision, members,
+                                                  max_truncation, C.byref(h)))
         self._h = h
         T, nlat, nlon, B = _I(), _I(), _I(), _I()
         _check(self._lib.lmw_sphere_dims(h, C.byref(T), C.byref(nlat), C.byref(nlon), C.byref(B)))

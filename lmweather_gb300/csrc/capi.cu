@@ -80,8 +80,8 @@ int lmw_fp64_peak(double *tflops) {
 }
 
 // ------------------------------------------------------------------------------------------------ sphere
-int lmw_sphere_create_ex(int truncation, double radius, double omega, double gravity, double diffusion, int precision, int members,
-                         int max_truncation, lmw_sphere **out) {
+static int create_sphere(int truncation, double radius, double omega, double gravity, double diffusion, int precision, int members,
+                         int max_truncation, int split_terms, lmw_sphere **out) {
   return guard([&] {
     need(out != nullptr, "output handle pointer is null");
     *out = nullptr;
@@ -94,6 +94,7 @@ int lmw_sphere_create_ex(int truncation, double radius, double omega, double gra
     c.precision = precision;
     c.members = members;
     c.max_truncation = max_truncation;
+    c.split_terms = split_terms;
     need(max_truncation >= 4 && max_truncation <= 341, "the truncation cap must be between 4 and 341");
     auto *h = new lmw_sphere{nullptr};
     try {
@@ -104,6 +105,14 @@ int lmw_sphere_create_ex(int truncation, double radius, double omega, double gra
     }
     *out = h;
   });
+}
+int lmw_sphere_create_ex(int truncation, double radius, double omega, double gravity, double diffusion, int precision, int members,
+                         int max_truncation, lmw_sphere **out) {
+  return create_sphere(truncation, radius, omega, gravity, diffusion, precision, members, max_truncation, 3, out);
+}
+int lmw_sphere_create_split(int truncation, double radius, double omega, double gravity, double diffusion, int members, int max_truncation,
+                            int split_terms, lmw_sphere **out) {
+  return create_sphere(truncation, radius, omega, gravity, diffusion, LMW_SPLIT_BF16, members, max_truncation, split_terms, out);
 }
 int lmw_sphere_create(int truncation, double radius, double omega, double gravity, double diffusion, lmw_sphere **out) {
   return lmw_sphere_create_ex(truncation, radius, omega, gravity, diffusion, LMW_FP64, 1, 170, out);

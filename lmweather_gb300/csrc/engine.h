@@ -75,10 +75,12 @@ struct SphereConfig {
   double radius = 6.37122e6, omega = 7.292e-5, gravity = 9.80616, diffusion = 0;
   int precision = kFP64;
   int members = 1;          // ensemble members sharing the truncation (batch dimension)
+  int split_terms = 3;      // BF16 products per Legendre term in the split mode: 3 (hi/lo) or 6 (hi/mid/lo)
   int max_truncation = 341; // the reference caps at 170; the engine allows up to this
 };
 
 struct SphereTables;
+struct SplitPlan;
 
 class SphereEngine {
  public:
@@ -121,6 +123,10 @@ class SphereEngine {
 
  private:
   SphereTables *tab = nullptr;
+  SplitPlan *split = nullptr;
+  bool split_packed = false;
+  void check_split_status();
+  void ensure_packed();
   // state (packed triangle, complex interleaved), stage input, accumulator
   DevBuf<double> x0, xs, acc;
   // Fourier coefficients of the synthesised grids, folded analysis inputs

@@ -20,6 +20,7 @@
 #include <functional>
 
 #include "engine.h"
+#include "sphere_common.cuh"
 #include "sphere_tables.h"
 
 namespace lmw {
@@ -36,41 +37,6 @@ struct SphereTables {
 };
 
 namespace {
-
-struct SphDev {
-  int N, M, nlat, nlon, nh, ntri, logn;
-  double a, g;
-  const double *Ps, *Hs, *Pa, *Ha, *mu, *w, *wd, *cosl, *r2om, *kfac, *lapl;
-  const double2 *tw;
-  const int *trim, *trin, *tri;
-};
-
-template <class R> struct V2;
-template <> struct V2<double> { using type = double2; };
-template <> struct V2<float> { using type = float2; };
-__device__ __forceinline__ double2 mk2(double x, double y) { return make_double2(x, y); }
-__device__ __forceinline__ float2 mk2(float x, float y) { return make_float2(x, y); }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-__device__ __forceinline__ float2 cfma(float2 acc, float2 a, float s) { return make_float2(fmaf(a.x, s, acc.x), fmaf(a.y, s, acc.y)); }
-__device__ __forceinline__ float2 conjd(float2 a) { return make_float2(a.x, -a.y); }
-__device__ __forceinline__ float2 imul(float2 z, float m) { return make_float2(-m * z.y, m * z.x); }
-// Legendre tables, weights and twiddles in the compute precision of a stage kernel
-template <class R> struct SphTab {
-  const R *Ps, *Hs, *Pa, *Ha, *w, *wd, *r2om, *kfac, *lapl;
-  const typename V2<R>::type *tw;
-};
-
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
-__device__ __forceinline__ double2 cfma(double2 acc, double2 a, double s) { return make_double2(fma(a.x, s, acc.x), fma(a.y, s, acc.y)); }
-__device__ __forceinline__ double2 conjd(double2 a) { return make_double2(a.x, -a.y); }
-// (i m) z
-__device__ __forceinline__ double2 imul(double2 z, double m) { return make_double2(-m * z.y, m * z.x); }
 
 // ------------------------------------------------------------------------------------------------ synthesis
 // Block: SYN_CHUNKS warps for one wavenumber m and 32 southern latitudes (lane = latitude). Warp c sums the terms
@@ -218,7 +184,6 @@ __device__ void load_pair_spectra(C2 *s, int rows, const SphDev &d, const C2 *__
 
 // ------------------------------------------------------------------------------------------------ grid stage
 constexpr int GRID_THREADS = 256;
-constexpr int NSLOT = 5;  // A, B, U Phi, V Phi (times w/((1-mu^2)a)) and the Bernoulli function (times w)
 
 // four: [B][nlat][4][M]; fold: [B][nh][NSLOT][2][M]; fgrid/hsgrid: [B][nlat][nlon]
 template <class R>
@@ -282,11 +247,7 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, SphTab<R> t, 
 // the tendencies and applies the RK4 stage update.
 constexpr int ANA_CHUNKS = 8, ANA_THREADS = 32 * ANA_CHUNKS, ANA_Q = 14;
 
-struct StageArgs {
-  int stage;        // 0..3
-  double c;         // 0.5 dt, 0.5 dt, dt, dt/6
-  const double *filt;  // [2][M]: zeta/delta and phi factors by n (last stage)
-};
+
 
 // x0: state, xs: stage input (written for stages 0-2), acc: RK4 accumulator. All [B][3][ntri].
 template <class R>
@@ -562,6 +523,11 @@ double irwin_hall(uint64_t &st) {
 }
 
 }  // namespace
+}  // namespace lmw
+
+#include "sphere_split.cuh"
+
+namespace lmw {
 
 // ================================================================================================ engine
 
@@ -607,7 +573,10 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   if (c.truncation < 4 || c.truncation > c.max_truncation)
     throw InvalidArgument("truncation must be between 4 and " + std::to_string(c.max_truncation));
   if (c.members < 1) throw InvalidArgument("an ensemble needs at least one member");
-  if (c.precision != kFP64 && c.precision != kFP32) throw InvalidArgument("precision mode not available in this build");
+  if (c.precision != kFP64 && c.precision != kFP32 && c.precision != kSplitBF16)
+    throw InvalidArgument("precision must be 0 (FP64), 1 (FP32) or 2 (split BF16)");
+  if (c.precision == kSplitBF16 && c.split_terms != 3 && c.split_terms != 6)
+    throw InvalidArgument("split precision takes 3 or 6 BF16 products per term");
   B = c.members;
   tab = new SphereTables();
   HostTables &h = tab->host;
@@ -714,6 +683,12 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   dred.alloc(B);
   hred.alloc(B);
   hstage.alloc(std::max<size_t>(4 * ngrid(), static_cast<size_t>(3) * 2 * nspec_ref()));
+  if (p.precision == kSplitBF16) {
+    split = new SplitPlan();
+    build_split_plan(*split, h, B, p.split_terms);
+    LMW_CUDA(cudaFuncSetAttribute(split_syn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(split->smem_syn)));
+    LMW_CUDA(cudaFuncSetAttribute(split_ana, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(split->smem_ana)));
+  }
   x0.zero(stream);
   hsgrid.zero(stream);
   refgrid.zero(stream);
@@ -732,7 +707,17 @@ SphereEngine::~SphereEngine() {
     cudaStreamSynchronize(stream);
     cudaStreamDestroy(stream);
   }
+  delete split;
   delete tab;
+}
+
+// the tensor-core kernels record a nonzero code when a bounded wait ran out
+void SphereEngine::check_split_status() {
+  if (!split) return;
+  int e = 0;
+  LMW_CUDA(cudaMemcpyAsync(&e, split->err.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  if (e) throw DeviceError("a wait on the tensor cores timed out in the split-precision Legendre transforms");
 }
 
 static void check_member(const SphereEngine &e, int member) {
@@ -793,6 +778,7 @@ void SphereEngine::mark_reference(int member) {
 }
 
 void SphereEngine::analyze_grids_to_state(int member) {
+  split_packed = false;
   SphDev d = make_sph(*this, *tab);
   const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
   const size_t ng = ngrid();
@@ -838,6 +824,7 @@ void SphereEngine::from_packed(const double *packed, double *ref) {
 
 void SphereEngine::set_state(const double *zeta, const double *delta, const double *phi, double time, int member) {
   check_member(*this, member);
+  split_packed = false;
   LMW_CUDA(cudaStreamSynchronize(stream));
   const size_t pk = static_cast<size_t>(ntri) * 2;
   to_packed(zeta, hstage.p);
@@ -995,18 +982,39 @@ static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage,
     sph_analysis<R><<<dim3((d.ntri + 31) / 32, B), ANA_THREADS, 0, stream>>>(d, t, fold, sa, x0, xs, acc);
 }
 
+// One RK4 stage in split precision: tensor-core synthesis, FP32 grid stage, tensor-core analysis with the RK4
+// update (which also packs the next stage's synthesis operands)
+static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan &sp, const double *kfac64, int B, int stage, double dt,
+                        const double *filt, double2 *x0, double2 *xs, double2 *acc, const double *fgrid, const double *hsgrid,
+                        cudaStream_t stream, int which = -1) {
+  const SplitDev sd = split_dev(sp);
+  StageArgs sa;
+  sa.stage = stage;
+  sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
+  sa.filt = filt;
+  if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B);
+  if (which < 0 || which == 1)
+    split_grid<<<dim3(d.nh, B), GRID_THREADS, 5 * static_cast<size_t>(d.nlon) * sizeof(float2), stream>>>(d, t, sd, fgrid, hsgrid);
+  if (which < 0 || which == 2) split_ana<<<dim3(d.M, 2, sp.ntiles), SPLIT_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, x0, xs, acc);
+}
+
 void SphereEngine::launch_stage(int stage, double dt) {
   SphDev d = make_sph(*this, *tab);
   const double2 *in = reinterpret_cast<const double2 *>(stage == 0 ? x0.p : xs.p);
   double2 *X0 = reinterpret_cast<double2 *>(x0.p), *XS = reinterpret_cast<double2 *>(xs.p), *AC = reinterpret_cast<double2 *>(acc.p);
-  if (p.precision == kFP64)
+  if (p.precision == kFP64) {
     stage_kernels<double>(d, tab64(*tab), B, stage, dt, filt.p, in, reinterpret_cast<double2 *>(four.p), reinterpret_cast<double2 *>(fold.p),
                           X0, XS, AC, fgrid.p, hsgrid.p, stream);
-  else
+    g_launches += 3;
+  } else if (p.precision == kFP32) {
     stage_kernels<float>(d, tab32(*tab), B, stage, dt, filt.p, in, reinterpret_cast<float2 *>(four32.p), reinterpret_cast<float2 *>(fold32.p),
                          X0, XS, AC, fgrid.p, hsgrid.p, stream);
+    g_launches += 3;
+  } else {
+    split_stage(d, tab32(*tab), *split, tab->kfac.p, B, stage, dt, filt.p, X0, XS, AC, fgrid.p, hsgrid.p, stream);
+    g_launches += 3;
+  }
   LMW_LAUNCH_CHECK();
-  g_launches += 3;
 }
 
 void SphereEngine::kernel_times(double dt, int reps, double *out) {
@@ -1018,9 +1026,11 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
     if (p.precision == kFP64)
       stage_kernels<double>(d, tab64(*tab), B, 1, dt, filt.p, X0, reinterpret_cast<double2 *>(four.p), reinterpret_cast<double2 *>(fold.p), X0,
                             XS, AC, fgrid.p, hsgrid.p, stream, which);
-    else
+    else if (p.precision == kFP32)
       stage_kernels<float>(d, tab32(*tab), B, 1, dt, filt.p, X0, reinterpret_cast<float2 *>(four32.p), reinterpret_cast<float2 *>(fold32.p),
                            X0, XS, AC, fgrid.p, hsgrid.p, stream, which);
+    else
+      split_stage(d, tab32(*tab), *split, tab->kfac.p, B, 1, dt, filt.p, X0, XS, AC, fgrid.p, hsgrid.p, stream, which);
   };
   cudaEvent_t e0, e1;
   LMW_CUDA(cudaEventCreate(&e0));
@@ -1039,10 +1049,22 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   g_launches += 3ull * (reps + 1);
+  split_packed = false;
+}
+
+// the split path keeps its synthesis operands packed from the state; pack them after a change from outside
+void SphereEngine::ensure_packed() {
+  if (!split || split_packed) return;
+  SphDev d = make_sph(*this, *tab);
+  split_pack_state<<<dim3((ntri + 127) / 128, B), 128, 0, stream>>>(d, split_dev(*split), tab->kfac.p, reinterpret_cast<const double2 *>(x0.p));
+  LMW_LAUNCH_CHECK();
+  g_launches += 1;
+  split_packed = true;
 }
 
 void SphereEngine::enqueue_step(double dt) {
   upload_filter(dt);
+  ensure_packed();
   for (int s = 0; s < 4; s++) launch_stage(s, dt);
   launches_step = 12;
 }
@@ -1050,6 +1072,7 @@ void SphereEngine::enqueue_step(double dt) {
 void SphereEngine::launch_chunk(double dt, int steps) {
   if (steps <= 0) return;
   upload_filter(dt);
+  ensure_packed();
   if (!graph || graph_dt != dt || graph_steps != steps) {
     if (graph) cudaGraphExecDestroy(graph);
     graph = nullptr;
@@ -1073,6 +1096,7 @@ void SphereEngine::step(double dt) {
   enqueue_step(dt);
   for (int b = 0; b < B; b++) t[b] += dt;
   LMW_CUDA(cudaStreamSynchronize(stream));
+  check_split_status();
 }
 
 void SphereEngine::reduce_guard(Reduce &r, int member) {
@@ -1129,6 +1153,7 @@ void SphereEngine::run(double seconds, double dt) {
     for (int s = 0; s < chunk; s++)
       for (int b = 0; b < B; b++) t[b] += h;
     i = next + 1;
+    check_split_status();
     if ((next & 63) == 63) {
       for (int b = 0; b < B; b++) {
         Reduce r;

@@ -1,0 +1,52 @@
+// Definitions shared by the sphere kernels (sphere.cu) and the split-precision Legendre path (sphere_split.cuh).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace lmw {
+namespace {
+
+struct SphDev {
+  int N, M, nlat, nlon, nh, ntri, logn;
+  double a, g;
+  const double *Ps, *Hs, *Pa, *Ha, *mu, *w, *wd, *cosl, *r2om, *kfac, *lapl;
+  const double2 *tw;
+  const int *trim, *trin, *tri;
+};
+
+template <class R> struct V2;
+template <> struct V2<double> { using type = double2; };
+template <> struct V2<float> { using type = float2; };
+__device__ __forceinline__ double2 mk2(double x, double y) { return make_double2(x, y); }
+__device__ __forceinline__ float2 mk2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cfma(float2 acc, float2 a, float s) { return make_float2(fmaf(a.x, s, acc.x), fmaf(a.y, s, acc.y)); }
+__device__ __forceinline__ float2 conjd(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 imul(float2 z, float m) { return make_float2(-m * z.y, m * z.x); }
+// Legendre tables, weights and twiddles in the compute precision of a stage kernel
+template <class R> struct SphTab {
+  const R *Ps, *Hs, *Pa, *Ha, *w, *wd, *r2om, *kfac, *lapl;
+  const typename V2<R>::type *tw;
+};
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ __forceinline__ double2 cfma(double2 acc, double2 a, double s) { return make_double2(fma(a.x, s, acc.x), fma(a.y, s, acc.y)); }
+__device__ __forceinline__ double2 conjd(double2 a) { return make_double2(a.x, -a.y); }
+// (i m) z
+__device__ __forceinline__ double2 imul(double2 z, double m) { return make_double2(-m * z.y, m * z.x); }
+
+constexpr int NSLOT = 5;  // A, B, U Phi, V Phi (times w/((1-mu^2)a)) and the Bernoulli function (times w)
+
+struct StageArgs {
+  int stage;        // 0..3
+  double c;         // 0.5 dt, 0.5 dt, dt, dt/6
+  const double *filt;  // [2][M]: zeta/delta and phi factors by n (last stage)
+};
+
+}  // namespace
+}  // namespace lmw

@@ -1,0 +1,711 @@
+// Split-precision Legendre transforms on the tensor cores (included by sphere.cu).
+//
+// Every Legendre sum of an RK4 stage is a small GEMM per zonal wavenumber m on tcgen05, with the operands split
+// into BF16 pieces (hi/lo: 3 products per term; hi/mid/lo: 6) and FP32 accumulation in tensor memory:
+//   synthesis  D[member x quantity][jh] = A[member x quantity][k] * T_m[jh][k]^T; k orders n with the even n - m
+//              first and the odd second (two K segments, two accumulators: both mirror latitudes come out at
+//              once); quantities psi, chi, zeta, Phi against the P table and psi, chi against the H table.
+//   analysis   D[member x quantity][r] = A[member x quantity][jh] * T_{m,s}[r][jh]^T for n = m + s + 2r (one
+//              parity s per CTA); A w_d, B w_d, U Phi w_d, (Phi + E) w at fold parity s against P and A w_d,
+//              B w_d, V Phi w_d at parity 1 - s against H.
+// Three launches per stage:
+//   split_syn     per (m, member tile): H then P through a two-stage pipeline of bulk asynchronous copies
+//                 (cp.async.bulk, the TMA engine) into shared memory, MMAs by one thread, accumulators read back
+//                 with tcgen05.ld and written as per-latitude E/O sums for the grid kernel.
+//   split_grid    per (latitude pair, member): Fourier coefficients from the E/O sums, FP32 FFTs and products
+//                 (the same arithmetic as sph_grid<float>), then the folded analysis inputs written straight into
+//                 the analysis operands as BF16 pieces.
+//   split_ana     per (m, parity, member tile): H then P as above; the epilogue forms the tendencies in FP32,
+//                 applies the RK4 stage update to the FP64 state, and packs the next stage's synthesis operands.
+// All operands live in global memory already in the MMA's canonical K-major core-matrix order, in 64-wide K
+// chunks: element (row r, column k) of an R-row operand sits at
+//   (k / 64) * R * 64 + ((r / 8) * 8 + (k % 64) / 8) * 64 + (r % 8) * 8 + k % 8
+// so the chunk of every operand is one contiguous run of R * 128 bytes. Split pieces follow each other at a
+// fixed element stride (the buffer size).
+#pragma once
+#include <cuda_bf16.h>
+
+#include "sphere_common.cuh"
+#include "sphere_tables.h"
+
+namespace lmw {
+
+constexpr int SPLIT_NBT = 16;  // members per tile: 8 quantities x 16 members = 128 rows, the M of one MMA
+constexpr int SPLIT_BK = 64;
+constexpr int SPLIT_STAGES = 2;
+constexpr int SPLIT_THREADS = 128;
+constexpr int SPLIT_NQ = 24;  // per (member, jh, m): E and O of 8 P sums and 4 H sums
+
+struct SplitPlan {
+  int pieces = 2, terms = 3;
+  int nbt = 1, ntiles = 1, nh16 = 16, nh64 = 64, rAP = 8, rAH = 8, rSP = 8, rSH = 8, ra_max = 16;
+  std::vector<int> ke16, kp64, ra16;
+  std::vector<long> tS_off, tA_off, aS_off, aSH_off;
+  long tS_size = 0, tA_size = 0, aSP_size = 0, aSH_size = 0, aAP_size = 0, aAH_size = 0;
+  DevBuf<__nv_bfloat16> tS_P, tS_H, tA_P, tA_H;   // tables (B operands), three pieces each
+  DevBuf<__nv_bfloat16> aS_P, aS_H, aA_P, aA_H;   // per-stage operands (A)
+  DevBuf<float> dsyn;                             // [member][jh][m][SPLIT_NQ]
+  DevBuf<int> err;
+  DevBuf<int> ke16_d, kp64_d, ra16_d;
+  DevBuf<long> tS_off_d, tA_off_d, aS_off_d, aSH_off_d;
+  size_t smem_syn = 0, smem_ana = 0;
+};
+
+struct SplitDev {
+  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH;
+  const int *ke16, *kp64, *ra16;
+  const long *tS_off, *tA_off, *aS_off, *aSH_off;
+  long tS_size, tA_size, aSP_size, aSH_size, aAP_size, aAH_size;
+  const __nv_bfloat16 *tS_P, *tS_H, *tA_P, *tA_H;
+  __nv_bfloat16 *aS_P, *aS_H, *aA_P, *aA_H;
+  float *dsyn;
+  int *err;
+};
+
+namespace {
+
+__host__ __device__ inline int pad16(int x) { return (x + 15) & ~15; }
+__host__ __device__ inline int pad8(int x) { return (x + 7) & ~7; }
+__host__ __device__ inline int pad64(int x) { return (x + 63) & ~63; }
+// canonical chunked core-matrix order of an R-row operand
+__host__ __device__ inline long tile_off(int r, int k, int R) {
+  return static_cast<long>(k >> 6) * R * 64 + (((r >> 3) << 3) + ((k & 63) >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+// round-to-nearest-even float -> bf16 on the host
+inline uint16_t host_bf16(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return static_cast<uint16_t>(u >> 16);
+}
+inline double host_bf16_value(uint16_t b) {
+  uint32_t u = static_cast<uint32_t>(b) << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+// hi, mid, lo BF16 pieces of a double: each piece rounds what the previous ones left
+inline void split3(double x, uint16_t *out, long stride) {
+  double r = x;
+  for (int p = 0; p < 3; p++) {
+    uint16_t b = host_bf16(static_cast<float>(r));
+    out[p * stride] = b;
+    r -= host_bf16_value(b);
+  }
+}
+// FP32 value -> BF16 pieces (the FP32 value carries every bit the products keep)
+__device__ __forceinline__ void fsplit(float x, __nv_bfloat16 *out, long stride, int pieces) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(x);
+  out[0] = h;
+  if (pieces > 1) {
+    const float r = x - __bfloat162float(h);
+    const __nv_bfloat16 l = __float2bfloat16_rn(r);
+    out[stride] = l;
+    if (pieces > 2) out[2 * stride] = __float2bfloat16_rn(r - __bfloat162float(l));
+  }
+}
+
+// ------------------------------------------------------------------------------------------- tcgen05 helpers
+__device__ __forceinline__ uint32_t su32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+constexpr unsigned long long SPLIT_WAIT_NS = 2000000000ull;
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase) {
+  const uint64_t t0 = gtimer();
+  while (true) {
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(bar), "r"(phase)
+                 : "memory");
+    if (done) return true;
+    if (gtimer() - t0 > SPLIT_WAIT_NS) return false;
+    __nanosleep(20);
+  }
+}
+// descriptor for the chunk layout: K-direction core matrices 128 B apart, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t chunk_desc(uint32_t saddr) {
+  uint64_t d = static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
+  d |= static_cast<uint64_t>(128u >> 4) << 16;
+  d |= static_cast<uint64_t>(1024u >> 4) << 32;
+  d |= static_cast<uint64_t>(1) << 46;
+  return d;
+}
+__device__ __forceinline__ uint32_t idesc_m128(int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(128 >> 4) << 24);
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst), "l"(src), "r"(bytes),
+               "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// One CTA's two GEMMs (H then P) through the bulk-copy pipeline. Operand g = 0 (H) / 1 (P): A chunk of aR[g] rows
+// at a[g] + c * aR[g] * 64, B chunk of bR rows at b[g] + c * bR * 64, nchunk[g] chunks; accumulators at TMEM
+// columns acc[g][seg] (seg boundary kseg[g] in K, a multiple of 16; kseg >= K means one segment). Returns false
+// when a bounded wait ran out (the error code is already recorded).
+struct TwoGemm {
+  const __nv_bfloat16 *a[2], *b[2];
+  long a_ps[2], b_ps[2];
+  int aR[2], bR, nchunk[2], kseg[2];
+  uint32_t acc[2][2];
+};
+
+__device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, uint8_t *smem, uint64_t *full, uint64_t *empty, uint64_t *done,
+                             uint32_t tmem, int *err) {
+  const int tid = threadIdx.x;
+  const int a_bytes = 128 * SPLIT_BK * 2;  // one 128-row A piece region
+  const int b_bytes = G.bR * SPLIT_BK * 2;
+  const int stage_bytes = pieces * (a_bytes + b_bytes);
+  const int total = G.nchunk[0] + G.nchunk[1];
+  __shared__ int s_fail;
+  if (tid == 0) s_fail = 0;
+  __syncthreads();
+  if (tid == 0) {
+    // producer: bulk copies of both operands' pieces for each (operand, chunk)
+    for (int it = 0; it < total; it++) {
+      const int st = it % SPLIT_STAGES, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
+      if (it >= SPLIT_STAGES && !mbar_wait_bounded(su32(&empty[st]), ((it / SPLIT_STAGES) - 1) & 1)) {
+        s_fail = 1;
+        atomicExch(err, 2);
+        break;
+      }
+      const uint32_t abytes = static_cast<uint32_t>(G.aR[g]) * 128u, bbytes = static_cast<uint32_t>(G.bR) * 128u;
+      mbar_expect(su32(&full[st]), static_cast<uint32_t>(pieces) * (abytes + bbytes));
+      uint8_t *base = smem + st * stage_bytes;
+      for (int p = 0; p < pieces; p++) {
+        bulk_g2s(su32(base + p * a_bytes), G.a[g] + p * G.a_ps[g] + static_cast<long>(c) * G.aR[g] * 64, abytes, su32(&full[st]));
+        bulk_g2s(su32(base + pieces * a_bytes + p * b_bytes), G.b[g] + p * G.b_ps[g] + static_cast<long>(c) * G.bR * 64, bbytes,
+                 su32(&full[st]));
+      }
+    }
+  } else if (tid == 32) {
+    // MMA issuer
+    const uint32_t idesc = idesc_m128(G.bR);
+    const int tp[6][2] = {{2, 0}, {1, 1}, {0, 2}, {1, 0}, {0, 1}, {0, 0}};
+    const int t0 = terms == 6 ? 0 : (terms == 3 ? 3 : 5);
+    bool started[2][2] = {{false, false}, {false, false}};
+    bool ok = true;
+    for (int it = 0; it < total && ok; it++) {
+      const int st = it % SPLIT_STAGES, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
+      if (!mbar_wait_bounded(su32(&full[st]), (it / SPLIT_STAGES) & 1)) {
+        s_fail = 1;
+        atomicExch(err, 3);
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      uint8_t *base = smem + st * stage_bytes;
+      for (int kk = 0; kk < SPLIT_BK; kk += 16) {
+        const int kg = c * SPLIT_BK + kk;
+        const int seg = kg >= G.kseg[g] ? 1 : 0;
+        for (int t = t0; t < 6; t++) {
+          const uint64_t ad = chunk_desc(su32(base + tp[t][0] * a_bytes + (kk / 8) * 128));
+          const uint64_t bd = chunk_desc(su32(base + pieces * a_bytes + tp[t][1] * b_bytes + (kk / 8) * 128));
+          const uint32_t accum = started[g][seg] ? 1u : 0u;
+          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                           G.acc[g][seg]),
+                       "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+                       : "memory");
+          started[g][seg] = true;
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&empty[st])) : "memory");
+    }
+    if (ok) asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(done)) : "memory");
+  }
+  __syncthreads();
+  bool fine = s_fail == 0;
+  if (fine && tid == 0 && !mbar_wait_bounded(su32(done), 0)) {
+    s_fail = 1;
+    atomicExch(err, 4);
+  }
+  __syncthreads();
+  fine = s_fail == 0;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  return fine;
+}
+
+// tensor memory and barriers shared by the two GEMM kernels
+__device__ __forceinline__ void split_setup(uint32_t *tslot, uint32_t ncols, uint64_t *full, uint64_t *empty, uint64_t *done, uint8_t *smem,
+                                            int zero_bytes) {
+  const int tid = threadIdx.x;
+  if ((tid >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tslot)), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < SPLIT_STAGES; s++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&full[s])), "r"(1) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&empty[s])), "r"(1) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(done)), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // A regions: the rows past each operand's R stay zero (H, copied first, has no more rows than P)
+  for (int e = tid; e < zero_bytes / 16; e += blockDim.x) reinterpret_cast<uint4 *>(smem)[e] = make_uint4(0, 0, 0, 0);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void split_teardown(uint32_t tmem, uint32_t ncols) {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+}
+
+// ------------------------------------------------------------------------------------------- synthesis
+// grid: (M, ntiles). D columns: H E/O at [0, nh16), [nh16, 2 nh16); P E/O at [2 nh16, 3 nh16), [3 nh16, 4 nh16)
+__global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev sd, int B) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t full[SPLIT_STAGES], empty[SPLIT_STAGES], done;
+  __shared__ uint32_t tslot;
+  const int m = blockIdx.x, tile = blockIdx.y;
+  const int mt = min(sd.nbt, B - tile * sd.nbt);
+  const int nh16 = sd.nh16;
+  uint32_t ncols = 32;
+  while (ncols < static_cast<uint32_t>(4 * nh16)) ncols <<= 1;
+  const int a_bytes = 128 * SPLIT_BK * 2, b_bytes = nh16 * SPLIT_BK * 2, stage_bytes = sd.pieces * (a_bytes + b_bytes);
+  int zb = 0;
+  for (int s = 0; s < SPLIT_STAGES; s++) zb = s * stage_bytes + sd.pieces * a_bytes;  // up to the last stage's A regions
+  split_setup(&tslot, ncols, full, empty, &done, smem, zb);
+  const uint32_t tmem = tslot;
+  TwoGemm G;
+  const long kp = sd.kp64[m];
+  const long aoffP = sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kp, aoffH = sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kp;
+  G.a[0] = sd.aS_H + aoffH;
+  G.a[1] = sd.aS_P + aoffP;
+  G.a_ps[0] = sd.aSH_size;
+  G.a_ps[1] = sd.aSP_size;
+  G.b[0] = sd.tS_H + sd.tS_off[m];
+  G.b[1] = sd.tS_P + sd.tS_off[m];
+  G.b_ps[0] = G.b_ps[1] = sd.tS_size;
+  G.aR[0] = sd.rSH;
+  G.aR[1] = sd.rSP;
+  G.bR = nh16;
+  G.nchunk[0] = G.nchunk[1] = static_cast<int>(kp / SPLIT_BK);
+  G.kseg[0] = G.kseg[1] = sd.ke16[m];
+  G.acc[0][0] = tmem;
+  G.acc[0][1] = tmem + nh16;
+  G.acc[1][0] = tmem + 2 * nh16;
+  G.acc[1][1] = tmem + 3 * nh16;
+  const bool ok = run_two_gemm(G, sd.pieces, sd.terms, smem, full, empty, &done, tmem, sd.err);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = warp * 32 + lane;
+  if (ok && warp * 32 < 8 * mt) {
+    // row: H rows ml * 4 + q (q < 4) and P rows ml * 8 + q (q < 8), both in TMEM lane `row`
+    const uint32_t lanebase = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+    const bool hrow = row < 4 * mt, prow = row < 8 * mt;
+    const int hml = row >> 2, hq = row & 3, pml = row >> 3, pq = row & 7;
+    for (int c = 0; c < nh16; c += 8) {
+      float hE[8], hO[8], pE[8], pO[8];
+      tmem_ld8(lanebase + c, hE);
+      tmem_ld8(lanebase + nh16 + c, hO);
+      tmem_ld8(lanebase + 2 * nh16 + c, pE);
+      tmem_ld8(lanebase + 3 * nh16 + c, pO);
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const int jh = c + i;
+        if (jh >= d.nh) continue;
+        if (hrow) {
+          float *o = sd.dsyn + ((static_cast<long>(tile * sd.nbt + hml) * d.nh + jh) * d.M + m) * SPLIT_NQ;
+          o[16 + hq] = hE[i];
+          o[20 + hq] = hO[i];
+        }
+        if (prow) {
+          float *o = sd.dsyn + ((static_cast<long>(tile * sd.nbt + pml) * d.nh + jh) * d.M + m) * SPLIT_NQ;
+          o[pq] = pE[i];
+          o[8 + pq] = pO[i];
+        }
+      }
+    }
+  }
+  split_teardown(tmem, ncols);
+}
+
+// ------------------------------------------------------------------------------------------- grid (FP32)
+// grid: (nh, B). E/O sums -> Fourier coefficients -> FFTs and products -> folded values -> analysis operands
+__global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
+                                                           const double *__restrict__ hsgrid) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2 *sm = reinterpret_cast<float2 *>(smraw);
+  const int b = blockIdx.y, jh = blockIdx.x;
+  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
+  const int tile = b / sd.nbt, ml = b - tile * sd.nbt;
+  for (int e = threadIdx.x; e < 4 * n; e += blockDim.x) sm[e] = make_float2(0, 0);
+  __syncthreads();
+  const float *src = sd.dsyn + (static_cast<long>(b) * d.nh + jh) * d.M * SPLIT_NQ;
+  const float ia = static_cast<float>(1.0 / d.a);
+  for (int m = threadIdx.x; m < d.M; m += blockDim.x) {
+    const float *v = src + static_cast<long>(m) * SPLIT_NQ;
+    float2 X[2][4];
+    for (int side = 0; side < 2; side++) {
+      float r[12];
+#pragma unroll
+      for (int q = 0; q < 8; q++) r[q] = side == 0 ? v[q] + v[8 + q] : v[q] - v[8 + q];          // P sums
+#pragma unroll
+      for (int q = 0; q < 4; q++) r[8 + q] = side == 0 ? v[16 + q] + v[20 + q] : v[20 + q] - v[16 + q];  // H sums
+      const float mm = static_cast<float>(m);
+      const float2 SP = make_float2(r[0], r[1]), SC = make_float2(r[2], r[3]), HP = make_float2(r[8], r[9]), HC = make_float2(r[10], r[11]);
+      X[side][0] = cscale(csub(imul(SC, mm), HP), ia);  // cpp/sphere.cpp:200-201
+      X[side][1] = cscale(cadd(imul(SP, mm), HC), ia);
+      X[side][2] = make_float2(r[4], r[5]);
+      X[side][3] = make_float2(r[6], r[7]);
+    }
+    for (int f = 0; f < 4; f++) {
+      const float2 a = X[0][f], c = X[1][f];
+      float2 *row = sm + static_cast<size_t>(f) * n;
+      if (m == 0) row[0] = make_float2(a.x, c.x);
+      else {
+        row[bitrev(m, d.logn)] = make_float2(a.x - c.y, a.y + c.x);
+        row[bitrev(n - m, d.logn)] = make_float2(a.x + c.y, c.x - a.y);
+      }
+    }
+  }
+  __syncthreads();
+  fft_inverse_dit(sm, 4, n, d.logn, t.tw);
+  const float r2om = t.r2om[js], g = static_cast<float>(d.g);
+  const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
+  const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
+  float2 *rU = sm, *rV = sm + n, *rZ = sm + 2 * n, *rP = sm + 3 * n, *rE = sm + 4 * n;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const float2 U = rU[k], V = rV[k], Z = rZ[k], P = rP[k];
+    float2 A, Bv, UP, VP, PE;
+    {
+      const float eta = Z.x + static_cast<float>(fr_s[k]);
+      A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
+      PE.x = P.x + g * static_cast<float>(hr_s[k]) + (U.x * U.x + V.x * V.x) * r2om;
+    }
+    {
+      const float eta = Z.y + static_cast<float>(fr_n[k]);
+      A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
+      PE.y = P.y + g * static_cast<float>(hr_n[k]) + (U.y * U.y + V.y * V.y) * r2om;
+    }
+    rU[k] = A; rV[k] = Bv; rZ[k] = UP; rP[k] = VP; rE[k] = PE;
+  }
+  __syncthreads();
+  fft_forward_dif(sm, 5, n, d.logn, t.tw);
+  const float inv = 1.0f / n, wd = t.wd[js], wj = t.w[js];
+  for (int e = threadIdx.x; e < d.M; e += blockDim.x) {
+    const int m = e;
+    float2 fold[5][2];
+    for (int r = 0; r < 5; r++) {
+      const float2 *row = sm + static_cast<size_t>(r) * n;
+      const float2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
+      const float hinv = 0.5f * inv;
+      float2 Xs = cscale(cadd(Ym, Yc), hinv);
+      const float2 tt = csub(Ym, Yc);
+      float2 Xn = make_float2(hinv * tt.y, -hinv * tt.x);
+      const float wt = r < 4 ? wd : wj;
+      Xs = cscale(Xs, wt);
+      Xn = cscale(Xn, wt);
+      fold[r][0] = cadd(Xs, Xn);
+      fold[r][1] = csub(Xs, Xn);
+    }
+    // analysis operands of both parity groups: P quantities (a, b, u, e) at fold parity s, H quantities (a, b, v) at 1 - s
+    for (int s = 0; s < 2; s++) {
+      const long slot = (static_cast<long>(m) * 2 + s) * sd.ntiles + tile;
+      const long baseP = slot * static_cast<long>(sd.rAP) * sd.nh64, baseH = slot * static_cast<long>(sd.rAH) * sd.nh64;
+      const float vP[8] = {fold[0][s].x, fold[0][s].y, fold[1][s].x, fold[1][s].y, fold[2][s].x, fold[2][s].y, fold[4][s].x, fold[4][s].y};
+      const int ph = 1 - s;
+      const float vH[6] = {fold[0][ph].x, fold[0][ph].y, fold[1][ph].x, fold[1][ph].y, fold[3][ph].x, fold[3][ph].y};
+#pragma unroll
+      for (int q = 0; q < 8; q++) fsplit(vP[q], sd.aA_P + baseP + tile_off(ml * 8 + q, jh, sd.rAP), sd.aAP_size, sd.pieces);
+#pragma unroll
+      for (int q = 0; q < 6; q++) fsplit(vH[q], sd.aA_H + baseH + tile_off(ml * 6 + q, jh, sd.rAH), sd.aAH_size, sd.pieces);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------- synthesis operands
+// The next synthesis operands for coefficient (member b, m, n) from its state value: psi, chi, zeta, Phi (P
+// rows) and psi, chi (H rows) at column k(n) of wavenumber m.
+__device__ __forceinline__ void pack_syn_coef(const SphDev &d, const SplitDev &sd, const double *__restrict__ kfac, int b, int m, int n,
+                                              double2 z, double2 dl, double2 f) {
+  const int tile = b / sd.nbt, ml = b - tile * sd.nbt;
+  const int ke16 = sd.ke16[m];
+  const int k = ((n - m) & 1) ? ke16 + ((n - m - 1) >> 1) : ((n - m) >> 1);
+  const long kp = sd.kp64[m];
+  const long baseP = sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kp;
+  const long baseH = sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kp;
+  const double kf = kfac[n];
+  const float v[8] = {static_cast<float>(z.x * kf), static_cast<float>(z.y * kf), static_cast<float>(dl.x * kf), static_cast<float>(dl.y * kf),
+                      static_cast<float>(z.x),      static_cast<float>(z.y),      static_cast<float>(f.x),       static_cast<float>(f.y)};
+#pragma unroll
+  for (int q = 0; q < 8; q++) fsplit(v[q], sd.aS_P + baseP + tile_off(ml * 8 + q, k, sd.rSP), sd.aSP_size, sd.pieces);
+#pragma unroll
+  for (int q = 0; q < 4; q++) fsplit(v[q], sd.aS_H + baseH + tile_off(ml * 4 + q, k, sd.rSH), sd.aSH_size, sd.pieces);
+}
+
+// synthesis operands from a whole state (after the state was set from outside the stepping). grid: (ceil(ntri/128), B)
+__global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict__ kfac, const double2 *__restrict__ x) {
+  const int b = blockIdx.y, q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.ntri) return;
+  const double2 *xb = x + static_cast<size_t>(b) * 3 * d.ntri;
+  pack_syn_coef(d, sd, kfac, b, d.trim[q], d.trin[q], xb[q], xb[d.ntri + q], xb[2 * d.ntri + q]);
+}
+
+// ------------------------------------------------------------------------------------------- analysis + RK4
+// grid: (M, 2, ntiles). D columns: H at [0, ra16), P at [ra16, 2 ra16)
+__global__ void __launch_bounds__(SPLIT_THREADS, 1) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
+                                                             int B, double2 *x0, double2 *xs, double2 *acc) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t full[SPLIT_STAGES], empty[SPLIT_STAGES], done;
+  __shared__ uint32_t tslot;
+  const int m = blockIdx.x, s = blockIdx.y, tile = blockIdx.z;
+  const int mt = min(sd.nbt, B - tile * sd.nbt);
+  const int R = s == 0 ? (d.N - m) / 2 + 1 : (d.N - m + 1) / 2;  // coefficients of this parity
+  if (R == 0) return;
+  const int ra16 = sd.ra16[2 * m + s];
+  uint32_t ncols = 32;
+  while (ncols < static_cast<uint32_t>(2 * ra16)) ncols <<= 1;
+  const int a_bytes = 128 * SPLIT_BK * 2, b_bytes = ra16 * SPLIT_BK * 2, stage_bytes = sd.pieces * (a_bytes + b_bytes);
+  int zb = 0;
+  for (int st = 0; st < SPLIT_STAGES; st++) zb = st * stage_bytes + sd.pieces * a_bytes;
+  split_setup(&tslot, ncols, full, empty, &done, smem, zb);
+  const uint32_t tmem = tslot;
+  TwoGemm G;
+  const long slot = (static_cast<long>(m) * 2 + s) * sd.ntiles + tile;
+  G.a[0] = sd.aA_H + slot * static_cast<long>(sd.rAH) * sd.nh64;
+  G.a[1] = sd.aA_P + slot * static_cast<long>(sd.rAP) * sd.nh64;
+  G.a_ps[0] = sd.aAH_size;
+  G.a_ps[1] = sd.aAP_size;
+  G.b[0] = sd.tA_H + sd.tA_off[2 * m + s];
+  G.b[1] = sd.tA_P + sd.tA_off[2 * m + s];
+  G.b_ps[0] = G.b_ps[1] = sd.tA_size;
+  G.aR[0] = sd.rAH;
+  G.aR[1] = sd.rAP;
+  G.bR = ra16;
+  G.nchunk[0] = G.nchunk[1] = sd.nh64 / SPLIT_BK;
+  G.kseg[0] = G.kseg[1] = 1 << 30;
+  G.acc[0][0] = G.acc[0][1] = tmem;
+  G.acc[1][0] = G.acc[1][1] = tmem + ra16;
+  const bool ok = run_two_gemm(G, sd.pieces, sd.terms, smem, full, empty, &done, tmem, sd.err);
+  // accumulators -> shared memory [row][2 ra16] (the pipeline buffers are free now)
+  float *dsm = reinterpret_cast<float *>(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = warp * 32 + lane;
+  if (ok && warp * 32 < 8 * mt) {
+    const uint32_t lanebase = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+    for (int c = 0; c < 2 * ra16; c += 8) {
+      float v[8];
+      tmem_ld8(lanebase + c, v);
+#pragma unroll
+      for (int i = 0; i < 8; i++) dsm[row * (2 * ra16) + c + i] = v[i];
+    }
+  }
+  __syncthreads();
+  if (ok) {
+    const int ld = 2 * ra16;
+    for (int e = threadIdx.x; e < mt * R; e += blockDim.x) {
+      const int ml = e / R, r = e - ml * R;
+      const int b = tile * sd.nbt + ml, n = m + s + 2 * r;
+      const float *H = dsm + (ml * 6) * ld + r, *P = dsm + (ml * 8) * ld + ra16 + r;
+      const float2 aH = make_float2(H[0 * ld], H[1 * ld]), bH = make_float2(H[2 * ld], H[3 * ld]), vH = make_float2(H[4 * ld], H[5 * ld]);
+      const float2 aP = make_float2(P[0 * ld], P[1 * ld]), bP = make_float2(P[2 * ld], P[3 * ld]);
+      const float2 uP = make_float2(P[4 * ld], P[5 * ld]), eP = make_float2(P[6 * ld], P[7 * ld]);
+      const float mm = static_cast<float>(m);
+      // cpp/sphere.cpp:380-389
+      float2 kz = csub(bH, imul(aP, mm));
+      float2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
+      float2 kf = csub(vH, imul(uP, mm));
+      const int q = d.tri[m] + n - m;
+      if (q == 0) kz = kd = kf = make_float2(0, 0);
+      const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
+      const double2 k[3] = {make_double2(kz.x, kz.y), make_double2(kd.x, kd.y), make_double2(kf.x, kf.y)};
+      double2 nv[3];
+#pragma unroll
+      for (int f = 0; f < 3; f++) {
+        const size_t i = base + static_cast<size_t>(f) * d.ntri;
+        if (sa.stage == 0) {
+          acc[i] = k[f];
+          nv[f] = cadd(x0[i], cscale(k[f], sa.c));
+          xs[i] = nv[f];
+        } else if (sa.stage < 3) {
+          acc[i] = cadd(acc[i], cscale(k[f], 2.0));
+          nv[f] = cadd(x0[i], cscale(k[f], sa.c));
+          xs[i] = nv[f];
+        } else {
+          const double2 val = cadd(x0[i], cscale(cadd(acc[i], k[f]), sa.c));
+          const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
+          nv[f] = q == 0 ? val : cscale(val, fac);
+          x0[i] = nv[f];
+        }
+      }
+      pack_syn_coef(d, sd, kfac, b, m, n, nv[0], nv[1], nv[2]);
+    }
+  }
+  split_teardown(tmem, ncols);
+}
+
+}  // namespace
+
+// Pack the tables, size the operand buffers (once per engine).
+inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int terms) {
+  const int N = h.N, M = h.M, nh = h.nh;
+  if (pad16(nh) * 4 > 512) throw InvalidArgument("split precision supports truncations up to 170 (the synthesis needs 4 x nlat/2 tensor-memory columns)");
+  sp.terms = terms;
+  sp.pieces = terms == 6 ? 3 : 2;
+  sp.nbt = std::min(B, SPLIT_NBT);
+  sp.ntiles = (B + sp.nbt - 1) / sp.nbt;
+  sp.nh16 = pad16(nh);
+  sp.nh64 = pad64(nh);
+  sp.rSP = 8 * sp.nbt;
+  sp.rSH = pad8(4 * sp.nbt);
+  sp.rAP = 8 * sp.nbt;
+  sp.rAH = pad8(6 * sp.nbt);
+  sp.ke16.assign(M, 0);
+  sp.kp64.assign(M, 0);
+  sp.ra16.assign(2 * M, 0);
+  sp.tS_off.assign(M, 0);
+  sp.tA_off.assign(2 * M, 0);
+  sp.aS_off.assign(M, 0);
+  sp.aSH_off.assign(M, 0);
+  long ts = 0, ta = 0, as = 0, ash = 0;
+  int ra_max = 16;
+  for (int m = 0; m <= N; m++) {
+    const int ke = (N - m) / 2 + 1, ko = (N - m + 1) / 2;
+    sp.ke16[m] = pad16(ke);
+    sp.kp64[m] = pad64(sp.ke16[m] + ko);
+    sp.tS_off[m] = ts;
+    ts += static_cast<long>(sp.nh16) * sp.kp64[m];
+    sp.aS_off[m] = as;
+    as += static_cast<long>(sp.ntiles) * sp.rSP * sp.kp64[m];
+    sp.aSH_off[m] = ash;
+    ash += static_cast<long>(sp.ntiles) * sp.rSH * sp.kp64[m];
+    for (int s = 0; s < 2; s++) {
+      const int R = s == 0 ? ke : ko;
+      sp.ra16[2 * m + s] = std::max(16, pad16(R));
+      sp.tA_off[2 * m + s] = ta;
+      ta += static_cast<long>(sp.ra16[2 * m + s]) * sp.nh64;
+      ra_max = std::max(ra_max, sp.ra16[2 * m + s]);
+    }
+  }
+  sp.ra_max = ra_max;
+  sp.tS_size = ts;
+  sp.tA_size = ta;
+  sp.aSP_size = as;
+  sp.aSH_size = ash;
+  sp.aAP_size = static_cast<long>(M) * 2 * sp.ntiles * sp.rAP * sp.nh64;
+  sp.aAH_size = static_cast<long>(M) * 2 * sp.ntiles * sp.rAH * sp.nh64;
+  // tables in the chunked core-matrix order, three pieces each
+  std::vector<uint16_t> tSP(3 * ts, 0), tSH(3 * ts, 0), tAP(3 * ta, 0), tAH(3 * ta, 0);
+  for (int m = 0; m <= N; m++) {
+    const int ke16 = sp.ke16[m], kpm = sp.kp64[m];
+    for (int k = 0; k < kpm; k++) {
+      const int n = k < ke16 ? m + 2 * k : m + 1 + 2 * (k - ke16);
+      if (n > N || (k < ke16 && ((n - m) & 1))) continue;
+      const size_t q = static_cast<size_t>(h.tri[m] + n - m);
+      for (int jh = 0; jh < nh; jh++) {
+        const long o = sp.tS_off[m] + tile_off(jh, k, sp.nh16);
+        split3(h.P[q * nh + jh], &tSP[o], ts);
+        split3(h.H[q * nh + jh], &tSH[o], ts);
+      }
+    }
+    for (int s = 0; s < 2; s++) {
+      const int R = s == 0 ? (N - m) / 2 + 1 : (N - m + 1) / 2;
+      for (int r = 0; r < R; r++) {
+        const int n = m + s + 2 * r;
+        const size_t q = static_cast<size_t>(h.tri[m] + n - m);
+        for (int jh = 0; jh < nh; jh++) {
+          const long o = sp.tA_off[2 * m + s] + tile_off(r, jh, sp.ra16[2 * m + s]);
+          split3(h.P[q * nh + jh], &tAP[o], ta);
+          split3(h.H[q * nh + jh], &tAH[o], ta);
+        }
+      }
+    }
+  }
+  auto up = [](DevBuf<__nv_bfloat16> &dst, const std::vector<uint16_t> &src) {
+    dst.alloc(src.size());
+    LMW_CUDA(cudaMemcpy(dst.p, src.data(), src.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+  };
+  up(sp.tS_P, tSP);
+  up(sp.tS_H, tSH);
+  up(sp.tA_P, tAP);
+  up(sp.tA_H, tAH);
+  // per-stage operands: padding rows and columns are never written and stay zero
+  sp.aS_P.alloc(3 * sp.aSP_size);
+  sp.aS_H.alloc(3 * sp.aSH_size);
+  sp.aA_P.alloc(3 * sp.aAP_size);
+  sp.aA_H.alloc(3 * sp.aAH_size);
+  for (auto *b : {&sp.aS_P, &sp.aS_H, &sp.aA_P, &sp.aA_H}) LMW_CUDA(cudaMemset(b->p, 0, b->bytes()));
+  sp.dsyn.alloc(static_cast<size_t>(B) * nh * M * SPLIT_NQ);
+  LMW_CUDA(cudaMemset(sp.dsyn.p, 0, sp.dsyn.bytes()));
+  sp.err.alloc(1);
+  LMW_CUDA(cudaMemset(sp.err.p, 0, sizeof(int)));
+  auto upi = [](DevBuf<int> &dst, const std::vector<int> &src) {
+    dst.alloc(src.size());
+    LMW_CUDA(cudaMemcpy(dst.p, src.data(), src.size() * sizeof(int), cudaMemcpyHostToDevice));
+  };
+  auto upl = [](DevBuf<long> &dst, const std::vector<long> &src) {
+    dst.alloc(src.size());
+    LMW_CUDA(cudaMemcpy(dst.p, src.data(), src.size() * sizeof(long), cudaMemcpyHostToDevice));
+  };
+  upi(sp.ke16_d, sp.ke16);
+  upi(sp.kp64_d, sp.kp64);
+  upi(sp.ra16_d, sp.ra16);
+  upl(sp.tS_off_d, sp.tS_off);
+  upl(sp.tA_off_d, sp.tA_off);
+  upl(sp.aS_off_d, sp.aS_off);
+  upl(sp.aSH_off_d, sp.aSH_off);
+  const int pieces = sp.pieces;
+  sp.smem_syn = static_cast<size_t>(SPLIT_STAGES) * pieces * (128 * SPLIT_BK * 2 + sp.nh16 * SPLIT_BK * 2);
+  const size_t ana_pipe = static_cast<size_t>(SPLIT_STAGES) * pieces * (128 * SPLIT_BK * 2 + ra_max * SPLIT_BK * 2);
+  sp.smem_ana = std::max(ana_pipe, static_cast<size_t>(128) * 2 * ra_max * sizeof(float));
+}
+
+inline SplitDev split_dev(const SplitPlan &sp) {
+  SplitDev s;
+  s.pieces = sp.pieces;
+  s.terms = sp.terms;
+  s.nbt = sp.nbt;
+  s.ntiles = sp.ntiles;
+  s.nh16 = sp.nh16;
+  s.nh64 = sp.nh64;
+  s.rAP = sp.rAP;
+  s.rAH = sp.rAH;
+  s.rSP = sp.rSP;
+  s.rSH = sp.rSH;
+  s.ke16 = sp.ke16_d.p;
+  s.kp64 = sp.kp64_d.p;
+  s.ra16 = sp.ra16_d.p;
+  s.tS_off = sp.tS_off_d.p;
+  s.tA_off = sp.tA_off_d.p;
+  s.aS_off = sp.aS_off_d.p;
+  s.aSH_off = sp.aSH_off_d.p;
+  s.tS_size = sp.tS_size;
+  s.tA_size = sp.tA_size;
+  s.aSP_size = sp.aSP_size;
+  s.aSH_size = sp.aSH_size;
+  s.aAP_size = sp.aAP_size;
+  s.aAH_size = sp.aAH_size;
+  s.tS_P = sp.tS_P.p;
+  s.tS_H = sp.tS_H.p;
+  s.tA_P = sp.tA_P.p;
+  s.tA_H = sp.tA_H.p;
+  s.aS_P = sp.aS_P.p;
+  s.aS_H = sp.aS_H.p;
+  s.aA_P = sp.aA_P.p;
+  s.aA_H = sp.aA_H.p;
+  s.dsyn = sp.dsyn.p;
+  s.err = sp.err.p;
+  return s;
+}
+
+}  // namespace lmw

@@ -59,7 +59,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, unsigned
 }
 
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
-    tc_gemm_kernel(const GemmProblem *__restrict__ probs, long a_lo, long b_lo, int terms, int *err, int variant) {
+    tc_gemm_kernel(const GemmProblem *__restrict__ probs, int terms, int *err, int variant) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_slot;
@@ -81,6 +81,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     status = 0;
   }
+  // rows of A past arows stay zero for the whole K loop
+  for (int e = tid; e < 3 * A_TILE / 16; e += GEMM_THREADS) reinterpret_cast<uint4 *>(sA)[e] = make_uint4(0, 0, 0, 0);
+  const int arows = P.arows;
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -101,9 +104,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     const int kc = min(BK, ktot - k0);
     const int kq_n = kc / 8;  // 16-byte chunks per row in this stage
     for (int pc = 0; pc < pieces; pc++) {
-      const __nv_bfloat16 *srcA = P.a + pc * a_lo, *srcB = P.b + pc * b_lo;
+      const __nv_bfloat16 *srcA = P.a + pc * P.a_ps, *srcB = P.b + pc * P.b_ps;
       uint8_t *dA = sA + pc * A_TILE, *dB = sB + pc * b_tile;
-      for (int e = tid; e < 128 * kq_n; e += GEMM_THREADS) {
+      for (int e = tid; e < arows * kq_n; e += GEMM_THREADS) {
         const int row = e / kq_n, kq = e - row * kq_n;
         const uint4 v = *reinterpret_cast<const uint4 *>(srcA + static_cast<size_t>(row) * P.lda + k0 + kq * 8);
         *reinterpret_cast<uint4 *>(dA + (kq * 16 + (row >> 3)) * 128 + (row & 7) * 16) = v;
@@ -146,7 +149,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     if (status) break;
   }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (!status) {
+  if (!status && warp * 32 < arows) {
     // epilogue: warp w owns accumulator rows 32w .. 32w+31 (TMEM lanes), 8 columns per load
     const int row = warp * 32 + lane;
     const int total = P.nseg * n;
@@ -160,9 +163,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       const int s = c / n;
       const bool live = P.kseg[s + 1] > P.kseg[s];
-      float *dst = P.d + static_cast<size_t>(row) * P.ldd + c;
+      if (row < arows) {
+        float *dst = P.d + static_cast<size_t>(row) * P.ldd + c;
 #pragma unroll
-      for (int i = 0; i < 8; i++) dst[i] = live ? __uint_as_float(r[i]) : 0.0f;
+        for (int i = 0; i < 8; i++) dst[i] = live ? __uint_as_float(r[i]) : 0.0f;
+      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -184,15 +189,14 @@ __global__ void split_bf16_kernel(const float *__restrict__ in, __nv_bfloat16 *_
 
 }  // namespace
 
-void tc_gemm_launch(const GemmProblem *probs_dev, int nprob, long a_lo, long b_lo, int terms, int *err, cudaStream_t stream,
-                    int layout_variant) {
+void tc_gemm_launch(const GemmProblem *probs_dev, int nprob, int terms, int *err, cudaStream_t stream, int layout_variant) {
   static bool attr = false;
   if (!attr) {
     LMW_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     attr = true;
   }
   if (nprob <= 0) return;
-  tc_gemm_kernel<<<nprob, GEMM_THREADS, SMEM_BYTES, stream>>>(probs_dev, a_lo, b_lo, terms, err, layout_variant);
+  tc_gemm_kernel<<<nprob, GEMM_THREADS, SMEM_BYTES, stream>>>(probs_dev, terms, err, layout_variant);
   LMW_LAUNCH_CHECK();
   g_launches += 1;
 }
@@ -241,16 +245,19 @@ int tc_gemm_selftest(const float *A, const float *B, float *D, int N, int K, int
     p.a = sA;
     p.b = sB;
     p.d = dD;
+    p.a_ps = na;
+    p.b_ps = nb;
     p.lda = K;
     p.ldb = K;
     p.ldd = N;
+    p.arows = 128;
     p.n = N;
     p.nseg = 1;
     p.kseg[0] = 0;
     p.kseg[1] = K;
     p.kseg[2] = p.kseg[3] = K;
     LMW_CUDA(cudaMemcpy(dp, &p, sizeof p, cudaMemcpyHostToDevice));
-    tc_gemm_launch(dp, 1, na, nb, terms, derr, st, variant);
+    tc_gemm_launch(dp, 1, terms, derr, st, variant);
     LMW_CUDA(cudaStreamSynchronize(st));
     int herr = 0;
     LMW_CUDA(cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost));

@@ -9,13 +9,15 @@ namespace lmw {
 // One CTA computes one problem: D[128 x nseg*n] (FP32, row-major, leading dimension ldd) where column block s is
 //   sum over the split terms of A_t[:, kseg[s]:kseg[s+1]] * B_t[:, kseg[s]:kseg[s+1]]^T
 // with A (128 rows) and B (n rows) stored K-major in BF16 (row stride lda / ldb elements, 16-byte aligned rows).
-// The low parts of A and B sit at a + a_lo and b + b_lo. Terms: 1 = hi*hi; 3 = lo*hi + hi*lo + hi*hi;
-// 6 (three-piece split: hi, mid at +lo, lo2 at +2*lo) = all products down to 2^-24.
+// The further split pieces of A and B sit at a + p * a_ps and b + p * b_ps. Terms: 1 = hi*hi; 3 = lo*hi + hi*lo +
+// hi*hi; 6 (three-piece split hi, mid, lo) = every product down to 2^-24.
 struct GemmProblem {
   const __nv_bfloat16 *a;
   const __nv_bfloat16 *b;
   float *d;
+  long a_ps, b_ps;  // element stride between split pieces
   int lda, ldb, ldd;
+  int arows;    // rows of A that hold data (1..128); the others are zero and their D rows are not written
   int n;        // multiple of 16, 16..256
   int nseg;     // 1..3
   int kseg[4];  // multiples of 16; kseg[0] = 0
@@ -23,8 +25,7 @@ struct GemmProblem {
 
 // Launch on `stream`: one CTA per problem. `err` (device int) receives a nonzero code if a wait on the tensor
 // cores ran out (the CTA then releases its tensor memory and returns).
-void tc_gemm_launch(const GemmProblem *probs_dev, int nprob, long a_lo, long b_lo, int terms, int *err, cudaStream_t stream,
-                    int layout_variant = 0);
+void tc_gemm_launch(const GemmProblem *probs_dev, int nprob, int terms, int *err, cudaStream_t stream, int layout_variant = 0);
 // Split FP32 values into BF16 pieces: out[0..n) = hi, out[lo..lo+n) = lo (and out[2lo..] = lo2 when pieces = 3).
 void split_bf16_launch(const float *in, __nv_bfloat16 *out, long n, long lo, int pieces, cudaStream_t stream);
 

@@ -3,7 +3,7 @@
     python -m lmweather_gb300.profile --case t42 --steps 4
     ncu --metrics gpu__time_duration.sum --clock-control none --csv python -m lmweather_gb300.profile --case t42 --steps 4
 
-Cases: t42 (config-0 sphere, FP64), t170 (sphere T170, dt 450 s), plane (1024 x 512 beta-plane jet, dt 60 s).
+Cases: t42 (config-0 sphere), t85, t170 (dt 300 s), t341 (dt 150 s), plane (1024 x 512 beta-plane jet, dt 60 s).
 One untimed warm-up step runs first.
 """
 from __future__ import annotations
@@ -34,7 +34,8 @@ def main() -> int:
             p.step(60.0)
         print(f"plane 1024x512: {args.steps} steps in {time.perf_counter() - t0:.4f} s")
         return 0
-    T, dt = {"t42": (42, 900.0), "t85": (85, 450.0), "t170": (170, 450.0), "t341": (341, 225.0)}[args.case]
+    # steps inside the reference's RK4 stability limit for an 8000 m layer (316 s at T170, 159 s at T341)
+    T, dt = {"t42": (42, 900.0), "t85": (85, 450.0), "t170": (170, 300.0), "t341": (341, 150.0)}[args.case]
     nu = A ** 4 / (86400.0 * (T * (T + 1)) ** 2)
     s = lw.Sphere(T, diffusion=nu, precision=args.precision, max_truncation=max(T, 170))
     s.turbulence(1, 8000.0, 30.0, T // 2)

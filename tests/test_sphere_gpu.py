@@ -194,7 +194,8 @@ def assert_state_floor(got, ref):
     assert e["phi"] <= TOL and e["zeta"] <= 2 * TOL and e["delta"] <= DELTA_FLOOR, e
 
 
-@pytest.mark.parametrize("T,dt,steps", [(85, 450.0, 4), (170, 450.0, 2)])
+# dt below the reference's own RK4 limit for these states (cpp/sphere.cpp:463; 621 s at T85, 316 s at T170)
+@pytest.mark.parametrize("T,dt,steps", [(85, 450.0, 4), (170, 300.0, 2)])
 def test_high_truncation_against_oracle(engine, T, dt, steps):
     nu = 6.37122e6 ** 4 / (86400.0 * (T * (T + 1)) ** 2)
     o = OracleSphere(T, diffusion=nu)
@@ -227,7 +228,7 @@ def height_l2_error(a, b):
     return np.sqrt(((a - b) ** 2).mean()) / np.sqrt((b ** 2).mean())
 
 
-@pytest.mark.parametrize("T,dt,steps", [(42, 900.0, 96), (170, 450.0, 16)])
+@pytest.mark.parametrize("T,dt,steps", [(42, 900.0, 96), (170, 300.0, 48)])
 def test_fp32_path_against_fp64(engine, T, dt, steps):
     # FP32 Legendre sums, FFTs and products; FP64 state accumulation: the height stays within 1e-6 (relative L2)
     nu = 6.37122e6 ** 4 / (86400.0 * (T * (T + 1)) ** 2)
@@ -244,3 +245,23 @@ def test_fp32_path_against_fp64(engine, T, dt, steps):
     d32, d64 = runs[engine.FP32][1], runs[engine.FP64][1]
     assert d32["mean_height"] == pytest.approx(d64["mean_height"], rel=1e-12)
     assert d32["energy"] == pytest.approx(d64["energy"], rel=1e-6)
+
+
+@pytest.mark.parametrize("T,dt,steps", [(42, 900.0, 48), (170, 300.0, 24)])
+def test_split_bf16_path_against_fp64(engine, T, dt, steps):
+    # Legendre sums on tcgen05 with BF16 pieces and FP32 accumulation, FP32 FFTs and products, FP64 state
+    nu = 6.37122e6 ** 4 / (86400.0 * (T * (T + 1)) ** 2)
+    grids, states = {}, {}
+    for key, kw in (("fp64", dict(precision=engine.FP64)), ("s3", dict(precision=engine.SPLIT_BF16, split_terms=3)),
+                    ("s6", dict(precision=engine.SPLIT_BF16, split_terms=6))):
+        s = engine.Sphere(T, diffusion=nu, **kw)
+        s.turbulence(4, 8000.0, 30.0, T // 2)
+        for _ in range(steps):
+            s.step(dt)
+        grids[key], states[key] = s.grid_height(), s.get_state()
+    e3 = height_l2_error(grids["s3"], grids["fp64"])
+    e6 = height_l2_error(grids["s6"], grids["fp64"])
+    z3 = state_errors(states["s3"], states["fp64"])
+    print(f"T{T} split vs FP64 after {steps} steps: height L2 3 terms {e3:.3e}, 6 terms {e6:.3e}; state errors 3 terms {z3}")
+    assert e3 < 3e-5  # about 16 significant bits per BF16 hi/lo product
+    assert e6 < 1e-6

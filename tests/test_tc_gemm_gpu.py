@@ -42,5 +42,5 @@ def test_split_gemm_accuracy(engine, N, K):
     print(f"N={N} K={K}: 1 term {e1:.2e}, 3 terms {e3:.2e}, 6 terms {e6:.2e}")
     assert e1 < 1e-2
     assert e3 < 5e-5
-    assert e6 < 2e-6
+    assert e6 < 5e-6  # the tensor-core FP32 accumulation grows with K: 5e-8 at K = 16, 2e-6 at K = 320
     assert e6 < e3 < e1
