@@ -985,17 +985,19 @@ static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage,
 // One RK4 stage in split precision: tensor-core synthesis, FP32 grid stage, tensor-core analysis with the RK4
 // update (which also packs the next stage's synthesis operands)
 static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan &sp, const double *kfac64, int B, int stage, double dt,
-                        const double *filt, double2 *x0, double2 *xs, double2 *acc, const double *fgrid, const double *hsgrid,
+                        const double *filt, float2 *fold, double2 *x0, double2 *xs, double2 *acc, const double *fgrid, const double *hsgrid,
                         cudaStream_t stream, int which = -1) {
-  const SplitDev sd = split_dev(sp);
+  SplitDev sd = split_dev(sp);
+  sd.fold = fold;
   StageArgs sa;
   sa.stage = stage;
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
   sa.filt = filt;
-  if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B);
+  if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
   if (which < 0 || which == 1)
     split_grid<<<dim3(d.nh, B), GRID_THREADS, 5 * static_cast<size_t>(d.nlon) * sizeof(float2), stream>>>(d, t, sd, fgrid, hsgrid);
-  if (which < 0 || which == 2) split_ana<<<dim3(d.M, 2, sp.ntiles), SPLIT_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, x0, xs, acc);
+  if (which < 0 || which == 2)
+    split_ana<<<dim3(d.M, 2, sp.ntiles), SPLIT_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
 }
 
 void SphereEngine::launch_stage(int stage, double dt) {
@@ -1011,7 +1013,8 @@ void SphereEngine::launch_stage(int stage, double dt) {
                          X0, XS, AC, fgrid.p, hsgrid.p, stream);
     g_launches += 3;
   } else {
-    split_stage(d, tab32(*tab), *split, tab->kfac.p, B, stage, dt, filt.p, X0, XS, AC, fgrid.p, hsgrid.p, stream);
+    split_stage(d, tab32(*tab), *split, tab->kfac.p, B, stage, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, AC, fgrid.p,
+                hsgrid.p, stream);
     g_launches += 3;
   }
   LMW_LAUNCH_CHECK();
@@ -1030,7 +1033,8 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
       stage_kernels<float>(d, tab32(*tab), B, 1, dt, filt.p, X0, reinterpret_cast<float2 *>(four32.p), reinterpret_cast<float2 *>(fold32.p),
                            X0, XS, AC, fgrid.p, hsgrid.p, stream, which);
     else
-      split_stage(d, tab32(*tab), *split, tab->kfac.p, B, 1, dt, filt.p, X0, XS, AC, fgrid.p, hsgrid.p, stream, which);
+      split_stage(d, tab32(*tab), *split, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, AC, fgrid.p,
+                  hsgrid.p, stream, which);
   };
   cudaEvent_t e0, e1;
   LMW_CUDA(cudaEventCreate(&e0));

@@ -32,7 +32,8 @@ namespace lmw {
 
 constexpr int SPLIT_NBT = 16;  // members per tile: 8 quantities x 16 members = 128 rows, the M of one MMA
 constexpr int SPLIT_BK = 64;
-constexpr int SPLIT_STAGES = 2;
+constexpr int SPLIT_MAX_STAGES = 4;
+constexpr int SPLIT_MARGIN = 16384;  // an M = 128 MMA reads 16 KB past an A base: every A base keeps 16 KB of allocation
 constexpr int SPLIT_THREADS = 128;
 constexpr int SPLIT_NQ = 24;  // per (member, jh, m): E and O of 8 P sums and 4 H sums
 
@@ -49,6 +50,7 @@ struct SplitPlan {
   DevBuf<int> ke16_d, kp64_d, ra16_d;
   DevBuf<long> tS_off_d, tA_off_d, aS_off_d, aSH_off_d;
   size_t smem_syn = 0, smem_ana = 0;
+  int ns_syn = 2, ns_ana = 2;  // pipeline stages
 };
 
 struct SplitDev {
@@ -59,6 +61,7 @@ struct SplitDev {
   const __nv_bfloat16 *tS_P, *tS_H, *tA_P, *tA_H;
   __nv_bfloat16 *aS_P, *aS_H, *aA_P, *aA_H;
   float *dsyn;
+  float2 *fold;  // [member][jh][slot][parity][m], as the FP32 grid kernel writes it
   int *err;
 };
 
@@ -157,21 +160,42 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
   for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// One CTA's two GEMMs (H then P) through the bulk-copy pipeline. Operand g = 0 (H) / 1 (P): A chunk of aR[g] rows
-// at a[g] + c * aR[g] * 64, B chunk of bR rows at b[g] + c * bR * 64, nchunk[g] chunks; accumulators at TMEM
-// columns acc[g][seg] (seg boundary kseg[g] in K, a multiple of 16; kseg >= K means one segment). Returns false
-// when a bounded wait ran out (the error code is already recorded).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,"
+      "%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]),
+        "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// One CTA's two GEMMs (H then P). Operand g = 0 (H) / 1 (P): nchunk[g] K chunks of 64. A is either streamed
+// with B (a[g] != nullptr: chunk c of aR[g] rows at a[g] + c * aR[g] * 64, pieces a_ps[g] apart) or resident in
+// shared memory (a_res[g]: chunk c, piece p at a_res[g] + (p * nchunk[g] + c) * aR[g] * 128 bytes). B chunk c of
+// bR rows at b[g] + c * bR * 64. Accumulators at TMEM columns acc[g][seg], the second segment starting at K =
+// kseg[g]. Only the first aR[g] accumulator rows are meaningful: an M = 128 MMA also reads whatever lies in the
+// 16 KB after an A base, and the rows it makes from that are never read. Returns false when a bounded wait ran
+// out (the error code is already recorded).
 struct TwoGemm {
   const __nv_bfloat16 *a[2], *b[2];
   long a_ps[2], b_ps[2];
-  int aR[2], bR, nchunk[2], kseg[2];
+  uint32_t a_res[2];
+  int aR[2], aRmax, bR, nchunk[2], kseg[2];
   uint32_t acc[2][2];
 };
 
-__device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, uint8_t *smem, uint64_t *full, uint64_t *empty, uint64_t *done,
-                             uint32_t tmem, int *err) {
+__device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, uint8_t *pipe, uint64_t *full, uint64_t *empty, uint64_t *done,
+                             int *err) {
   const int tid = threadIdx.x;
-  const int a_bytes = 128 * SPLIT_BK * 2;  // one 128-row A piece region
+  const bool astream = G.a[0] != nullptr;
+  const int a_bytes = astream ? G.aRmax * SPLIT_BK * 2 : 0;
   const int b_bytes = G.bR * SPLIT_BK * 2;
   const int stage_bytes = pieces * (a_bytes + b_bytes);
   const int total = G.nchunk[0] + G.nchunk[1];
@@ -179,19 +203,20 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, uint8_t *s
   if (tid == 0) s_fail = 0;
   __syncthreads();
   if (tid == 0) {
-    // producer: bulk copies of both operands' pieces for each (operand, chunk)
+    // producer: bulk copies of each (operand, chunk)
     for (int it = 0; it < total; it++) {
-      const int st = it % SPLIT_STAGES, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
-      if (it >= SPLIT_STAGES && !mbar_wait_bounded(su32(&empty[st]), ((it / SPLIT_STAGES) - 1) & 1)) {
+      const int st = it % ns, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
+      if (it >= ns && !mbar_wait_bounded(su32(&empty[st]), ((it / ns) - 1) & 1)) {
         s_fail = 1;
         atomicExch(err, 2);
         break;
       }
-      const uint32_t abytes = static_cast<uint32_t>(G.aR[g]) * 128u, bbytes = static_cast<uint32_t>(G.bR) * 128u;
+      const uint32_t abytes = astream ? static_cast<uint32_t>(G.aR[g]) * 128u : 0u, bbytes = static_cast<uint32_t>(G.bR) * 128u;
       mbar_expect(su32(&full[st]), static_cast<uint32_t>(pieces) * (abytes + bbytes));
-      uint8_t *base = smem + st * stage_bytes;
+      uint8_t *base = pipe + st * stage_bytes;
       for (int p = 0; p < pieces; p++) {
-        bulk_g2s(su32(base + p * a_bytes), G.a[g] + p * G.a_ps[g] + static_cast<long>(c) * G.aR[g] * 64, abytes, su32(&full[st]));
+        if (astream)
+          bulk_g2s(su32(base + p * a_bytes), G.a[g] + p * G.a_ps[g] + static_cast<long>(c) * G.aR[g] * 64, abytes, su32(&full[st]));
         bulk_g2s(su32(base + pieces * a_bytes + p * b_bytes), G.b[g] + p * G.b_ps[g] + static_cast<long>(c) * G.bR * 64, bbytes,
                  su32(&full[st]));
       }
@@ -204,21 +229,24 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, uint8_t *s
     bool started[2][2] = {{false, false}, {false, false}};
     bool ok = true;
     for (int it = 0; it < total && ok; it++) {
-      const int st = it % SPLIT_STAGES, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
-      if (!mbar_wait_bounded(su32(&full[st]), (it / SPLIT_STAGES) & 1)) {
+      const int st = it % ns, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
+      if (!mbar_wait_bounded(su32(&full[st]), (it / ns) & 1)) {
         s_fail = 1;
         atomicExch(err, 3);
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      uint8_t *base = smem + st * stage_bytes;
+      uint8_t *base = pipe + st * stage_bytes;
       for (int kk = 0; kk < SPLIT_BK; kk += 16) {
         const int kg = c * SPLIT_BK + kk;
         const int seg = kg >= G.kseg[g] ? 1 : 0;
         for (int t = t0; t < 6; t++) {
-          const uint64_t ad = chunk_desc(su32(base + tp[t][0] * a_bytes + (kk / 8) * 128));
-          const uint64_t bd = chunk_desc(su32(base + pieces * a_bytes + tp[t][1] * b_bytes + (kk / 8) * 128));
+          const int pa = tp[t][0], pb = tp[t][1];
+          const uint32_t abase = astream ? su32(base + pa * a_bytes)
+                                         : G.a_res[g] + static_cast<uint32_t>((pa * G.nchunk[g] + c) * G.aR[g] * 128);
+          const uint64_t ad = chunk_desc(abase + (kk / 8) * 128);
+          const uint64_t bd = chunk_desc(su32(base + pieces * a_bytes + pb * b_bytes + (kk / 8) * 128));
           const uint32_t accum = started[g][seg] ? 1u : 0u;
           asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
                            G.acc[g][seg]),
@@ -232,36 +260,30 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, uint8_t *s
     if (ok) asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(done)) : "memory");
   }
   __syncthreads();
-  bool fine = s_fail == 0;
-  if (fine && tid == 0 && !mbar_wait_bounded(su32(done), 0)) {
+  if (s_fail == 0 && tid == 0 && !mbar_wait_bounded(su32(done), 0)) {
     s_fail = 1;
     atomicExch(err, 4);
   }
   __syncthreads();
-  fine = s_fail == 0;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  return fine;
+  return s_fail == 0;
 }
 
 // tensor memory and barriers shared by the two GEMM kernels
-__device__ __forceinline__ void split_setup(uint32_t *tslot, uint32_t ncols, uint64_t *full, uint64_t *empty, uint64_t *done, uint8_t *smem,
-                                            int zero_bytes) {
+__device__ __forceinline__ void split_setup(uint32_t *tslot, uint32_t ncols, uint64_t *full, uint64_t *empty, uint64_t *done, int ns) {
   const int tid = threadIdx.x;
   if ((tid >> 5) == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tslot)), "r"(ncols) : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    for (int s = 0; s < SPLIT_STAGES; s++) {
+    for (int s = 0; s < ns; s++) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&full[s])), "r"(1) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&empty[s])), "r"(1) : "memory");
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(done)), "r"(1) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // A regions: the rows past each operand's R stay zero (H, copied first, has no more rows than P)
-  for (int e = tid; e < zero_bytes / 16; e += blockDim.x) reinterpret_cast<uint4 *>(smem)[e] = make_uint4(0, 0, 0, 0);
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -274,19 +296,16 @@ __device__ __forceinline__ void split_teardown(uint32_t tmem, uint32_t ncols) {
 
 // ------------------------------------------------------------------------------------------- synthesis
 // grid: (M, ntiles). D columns: H E/O at [0, nh16), [nh16, 2 nh16); P E/O at [2 nh16, 3 nh16), [3 nh16, 4 nh16)
-__global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev sd, int B) {
+__global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev sd, int B, int ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t full[SPLIT_STAGES], empty[SPLIT_STAGES], done;
+  __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
   const int m = blockIdx.x, tile = blockIdx.y;
   const int mt = min(sd.nbt, B - tile * sd.nbt);
   const int nh16 = sd.nh16;
   uint32_t ncols = 32;
   while (ncols < static_cast<uint32_t>(4 * nh16)) ncols <<= 1;
-  const int a_bytes = 128 * SPLIT_BK * 2, b_bytes = nh16 * SPLIT_BK * 2, stage_bytes = sd.pieces * (a_bytes + b_bytes);
-  int zb = 0;
-  for (int s = 0; s < SPLIT_STAGES; s++) zb = s * stage_bytes + sd.pieces * a_bytes;  // up to the last stage's A regions
-  split_setup(&tslot, ncols, full, empty, &done, smem, zb);
+  split_setup(&tslot, ncols, full, empty, &done, ns);
   const uint32_t tmem = tslot;
   TwoGemm G;
   const long kp = sd.kp64[m];
@@ -295,11 +314,13 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
   G.a[1] = sd.aS_P + aoffP;
   G.a_ps[0] = sd.aSH_size;
   G.a_ps[1] = sd.aSP_size;
+  G.a_res[0] = G.a_res[1] = 0;
   G.b[0] = sd.tS_H + sd.tS_off[m];
   G.b[1] = sd.tS_P + sd.tS_off[m];
   G.b_ps[0] = G.b_ps[1] = sd.tS_size;
   G.aR[0] = sd.rSH;
   G.aR[1] = sd.rSP;
+  G.aRmax = sd.rSP;
   G.bR = nh16;
   G.nchunk[0] = G.nchunk[1] = static_cast<int>(kp / SPLIT_BK);
   G.kseg[0] = G.kseg[1] = sd.ke16[m];
@@ -307,34 +328,41 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
   G.acc[0][1] = tmem + nh16;
   G.acc[1][0] = tmem + 2 * nh16;
   G.acc[1][1] = tmem + 3 * nh16;
-  const bool ok = run_two_gemm(G, sd.pieces, sd.terms, smem, full, empty, &done, tmem, sd.err);
+  const bool ok = run_two_gemm(G, sd.pieces, sd.terms, ns, smem, full, empty, &done, sd.err);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = warp * 32 + lane;
-  if (ok && warp * 32 < 8 * mt) {
-    // row: H rows ml * 4 + q (q < 4) and P rows ml * 8 + q (q < 8), both in TMEM lane `row`
-    const uint32_t lanebase = tmem + (static_cast<uint32_t>(warp * 32) << 16);
-    const bool hrow = row < 4 * mt, prow = row < 8 * mt;
-    const int hml = row >> 2, hq = row & 3, pml = row >> 3, pq = row & 7;
-    for (int c = 0; c < nh16; c += 8) {
-      float hE[8], hO[8], pE[8], pO[8];
-      tmem_ld8(lanebase + c, hE);
-      tmem_ld8(lanebase + nh16 + c, hO);
-      tmem_ld8(lanebase + 2 * nh16 + c, pE);
-      tmem_ld8(lanebase + 3 * nh16 + c, pO);
-#pragma unroll
-      for (int i = 0; i < 8; i++) {
-        const int jh = c + i;
-        if (jh >= d.nh) continue;
-        if (hrow) {
-          float *o = sd.dsyn + ((static_cast<long>(tile * sd.nbt + hml) * d.nh + jh) * d.M + m) * SPLIT_NQ;
-          o[16 + hq] = hE[i];
-          o[20 + hq] = hO[i];
+  // accumulator columns in blocks of 32 (TMEM -> shared memory by the warps that own live rows, then coalesced
+  // stores by every thread): block cb covers jh in [32 cb, 32 cb + 32) of the four accumulators H E, H O, P E, P O
+  float *tile_s = reinterpret_cast<float *>(smem);  // [4][8 mt][33]
+  const int rows = 8 * mt;
+  for (int cb = 0; ok && cb < nh16; cb += 32) {
+    const int wcols = min(32, nh16 - cb);
+    __syncthreads();
+    if (warp * 32 < rows) {
+      const uint32_t lanebase = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+      for (int a4 = 0; a4 < 4; a4++) {
+        float v[32];
+        if (wcols == 32) tmem_ld32(lanebase + a4 * nh16 + cb, v);
+        else {
+          tmem_ld8(lanebase + a4 * nh16 + cb, v);
+          tmem_ld8(lanebase + a4 * nh16 + cb + 8, v + 8);
         }
-        if (prow) {
-          float *o = sd.dsyn + ((static_cast<long>(tile * sd.nbt + pml) * d.nh + jh) * d.M + m) * SPLIT_NQ;
-          o[pq] = pE[i];
-          o[8 + pq] = pO[i];
+        if (row < rows) {
+#pragma unroll
+          for (int i = 0; i < 32; i++)
+            if (i < wcols) tile_s[(a4 * rows + row) * 33 + i] = v[i];
         }
       }
+    }
+    __syncthreads();
+    // dsyn[member][jh][m][slot]: slot q (P E), 8 + q (P O) for q < 8; 16 + q (H E), 20 + q (H O) for q < 4
+    for (int e = threadIdx.x; e < mt * wcols * SPLIT_NQ; e += blockDim.x) {
+      const int slot = e % SPLIT_NQ, rest = e / SPLIT_NQ, i = rest % wcols, ml = rest / wcols;
+      const int jh = cb + i;
+      if (jh >= d.nh) continue;
+      float v;
+      if (slot < 16) v = tile_s[(((slot < 8) ? 2 : 3) * rows + ml * 8 + (slot & 7)) * 33 + i];
+      else v = tile_s[(((slot < 20) ? 0 : 1) * rows + ml * 4 + ((slot - 16) & 3)) * 33 + i];
+      sd.dsyn[((static_cast<long>(tile * sd.nbt + ml) * d.nh + jh) * d.M + m) * SPLIT_NQ + slot] = v;
     }
   }
   split_teardown(tmem, ncols);
@@ -348,7 +376,6 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
   float2 *sm = reinterpret_cast<float2 *>(smraw);
   const int b = blockIdx.y, jh = blockIdx.x;
   const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
-  const int tile = b / sd.nbt, ml = b - tile * sd.nbt;
   for (int e = threadIdx.x; e < 4 * n; e += blockDim.x) sm[e] = make_float2(0, 0);
   __syncthreads();
   const float *src = sd.dsyn + (static_cast<long>(b) * d.nh + jh) * d.M * SPLIT_NQ;
@@ -419,17 +446,11 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
       fold[r][0] = cadd(Xs, Xn);
       fold[r][1] = csub(Xs, Xn);
     }
-    // analysis operands of both parity groups: P quantities (a, b, u, e) at fold parity s, H quantities (a, b, v) at 1 - s
-    for (int s = 0; s < 2; s++) {
-      const long slot = (static_cast<long>(m) * 2 + s) * sd.ntiles + tile;
-      const long baseP = slot * static_cast<long>(sd.rAP) * sd.nh64, baseH = slot * static_cast<long>(sd.rAH) * sd.nh64;
-      const float vP[8] = {fold[0][s].x, fold[0][s].y, fold[1][s].x, fold[1][s].y, fold[2][s].x, fold[2][s].y, fold[4][s].x, fold[4][s].y};
-      const int ph = 1 - s;
-      const float vH[6] = {fold[0][ph].x, fold[0][ph].y, fold[1][ph].x, fold[1][ph].y, fold[3][ph].x, fold[3][ph].y};
+    float2 *o = sd.fold + (static_cast<size_t>(b) * d.nh + jh) * 5 * 2 * d.M;
 #pragma unroll
-      for (int q = 0; q < 8; q++) fsplit(vP[q], sd.aA_P + baseP + tile_off(ml * 8 + q, jh, sd.rAP), sd.aAP_size, sd.pieces);
-#pragma unroll
-      for (int q = 0; q < 6; q++) fsplit(vH[q], sd.aA_H + baseH + tile_off(ml * 6 + q, jh, sd.rAH), sd.aAH_size, sd.pieces);
+    for (int r = 0; r < 5; r++) {
+      o[(r * 2 + 0) * d.M + m] = fold[r][0];
+      o[(r * 2 + 1) * d.M + m] = fold[r][1];
     }
   }
 }
@@ -465,9 +486,9 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict
 // ------------------------------------------------------------------------------------------- analysis + RK4
 // grid: (M, 2, ntiles). D columns: H at [0, ra16), P at [ra16, 2 ra16)
 __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
-                                                             int B, double2 *x0, double2 *xs, double2 *acc) {
+                                                             int B, int ns, double2 *x0, double2 *xs, double2 *acc) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t full[SPLIT_STAGES], empty[SPLIT_STAGES], done;
+  __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
   const int m = blockIdx.x, s = blockIdx.y, tile = blockIdx.z;
   const int mt = min(sd.nbt, B - tile * sd.nbt);
@@ -476,38 +497,84 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_ana(SphDev d, SplitDev
   const int ra16 = sd.ra16[2 * m + s];
   uint32_t ncols = 32;
   while (ncols < static_cast<uint32_t>(2 * ra16)) ncols <<= 1;
-  const int a_bytes = 128 * SPLIT_BK * 2, b_bytes = ra16 * SPLIT_BK * 2, stage_bytes = sd.pieces * (a_bytes + b_bytes);
-  int zb = 0;
-  for (int st = 0; st < SPLIT_STAGES; st++) zb = st * stage_bytes + sd.pieces * a_bytes;
-  split_setup(&tslot, ncols, full, empty, &done, smem, zb);
+  const int nchunk = sd.nh64 / SPLIT_BK;
+  // resident A operands: H (rAH rows) then P (rAP rows), every chunk and piece, in the chunk layout
+  const int aH_bytes = sd.pieces * nchunk * sd.rAH * 128, aP_bytes = sd.pieces * nchunk * sd.rAP * 128;
+  uint8_t *aH = smem, *aP = smem + aH_bytes, *pipe = smem + aH_bytes + aP_bytes;
+  {
+    // gather the folded grid values of this (m, s), one latitude per thread: P quantities a, b, u, e at parity s
+    // and H quantities a, b, v at parity 1 - s
+    const int ph = 1 - s;
+    const long pstrideP = static_cast<long>(nchunk) * sd.rAP * 64, pstrideH = static_cast<long>(nchunk) * sd.rAH * 64;
+    for (int e = threadIdx.x; e < mt * sd.nh64; e += blockDim.x) {
+      const int jh = e % sd.nh64, ml = e / sd.nh64;
+      float2 zp[4] = {}, zh[3] = {};
+      if (jh < d.nh) {
+        const float2 *g = sd.fold + (static_cast<size_t>(tile * sd.nbt + ml) * d.nh + jh) * 5 * 2 * d.M;
+        zp[0] = g[(0 * 2 + s) * d.M + m];
+        zp[1] = g[(1 * 2 + s) * d.M + m];
+        zp[2] = g[(2 * 2 + s) * d.M + m];
+        zp[3] = g[(4 * 2 + s) * d.M + m];
+        zh[0] = g[(0 * 2 + ph) * d.M + m];
+        zh[1] = g[(1 * 2 + ph) * d.M + m];
+        zh[2] = g[(3 * 2 + ph) * d.M + m];
+      }
+      const int c = jh >> 6, kin = jh & 63;
+      __nv_bfloat16 *dP = reinterpret_cast<__nv_bfloat16 *>(aP) + static_cast<long>(c) * sd.rAP * 64;
+      __nv_bfloat16 *dH = reinterpret_cast<__nv_bfloat16 *>(aH) + static_cast<long>(c) * sd.rAH * 64;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        fsplit(zp[q].x, dP + tile_off(ml * 8 + 2 * q, kin, sd.rAP), pstrideP, sd.pieces);
+        fsplit(zp[q].y, dP + tile_off(ml * 8 + 2 * q + 1, kin, sd.rAP), pstrideP, sd.pieces);
+      }
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        fsplit(zh[q].x, dH + tile_off(ml * 6 + 2 * q, kin, sd.rAH), pstrideH, sd.pieces);
+        fsplit(zh[q].y, dH + tile_off(ml * 6 + 2 * q + 1, kin, sd.rAH), pstrideH, sd.pieces);
+      }
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  split_setup(&tslot, ncols, full, empty, &done, ns);
   const uint32_t tmem = tslot;
   TwoGemm G;
-  const long slot = (static_cast<long>(m) * 2 + s) * sd.ntiles + tile;
-  G.a[0] = sd.aA_H + slot * static_cast<long>(sd.rAH) * sd.nh64;
-  G.a[1] = sd.aA_P + slot * static_cast<long>(sd.rAP) * sd.nh64;
-  G.a_ps[0] = sd.aAH_size;
-  G.a_ps[1] = sd.aAP_size;
+  G.a[0] = G.a[1] = nullptr;
+  G.a_ps[0] = G.a_ps[1] = 0;
+  G.a_res[0] = su32(aH);
+  G.a_res[1] = su32(aP);
   G.b[0] = sd.tA_H + sd.tA_off[2 * m + s];
   G.b[1] = sd.tA_P + sd.tA_off[2 * m + s];
   G.b_ps[0] = G.b_ps[1] = sd.tA_size;
   G.aR[0] = sd.rAH;
   G.aR[1] = sd.rAP;
+  G.aRmax = sd.rAP;
   G.bR = ra16;
-  G.nchunk[0] = G.nchunk[1] = sd.nh64 / SPLIT_BK;
+  G.nchunk[0] = G.nchunk[1] = nchunk;
   G.kseg[0] = G.kseg[1] = 1 << 30;
   G.acc[0][0] = G.acc[0][1] = tmem;
   G.acc[1][0] = G.acc[1][1] = tmem + ra16;
-  const bool ok = run_two_gemm(G, sd.pieces, sd.terms, smem, full, empty, &done, tmem, sd.err);
+  const bool ok = run_two_gemm(G, sd.pieces, sd.terms, ns, pipe, full, empty, &done, sd.err);
   // accumulators -> shared memory [row][2 ra16] (the pipeline buffers are free now)
   float *dsm = reinterpret_cast<float *>(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = warp * 32 + lane;
   if (ok && warp * 32 < 8 * mt) {
     const uint32_t lanebase = tmem + (static_cast<uint32_t>(warp * 32) << 16);
-    for (int c = 0; c < 2 * ra16; c += 8) {
+    int c = 0;
+    for (; c + 32 <= 2 * ra16; c += 32) {
+      float v[32];
+      tmem_ld32(lanebase + c, v);
+      if (row < 8 * mt) {
+#pragma unroll
+        for (int i = 0; i < 32; i++) dsm[row * (2 * ra16) + c + i] = v[i];
+      }
+    }
+    for (; c < 2 * ra16; c += 8) {
       float v[8];
       tmem_ld8(lanebase + c, v);
+      if (row < 8 * mt) {
 #pragma unroll
-      for (int i = 0; i < 8; i++) dsm[row * (2 * ra16) + c + i] = v[i];
+        for (int i = 0; i < 8; i++) dsm[row * (2 * ra16) + c + i] = v[i];
+      }
     }
   }
   __syncthreads();
@@ -665,9 +732,22 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   upl(sp.aS_off_d, sp.aS_off);
   upl(sp.aSH_off_d, sp.aSH_off);
   const int pieces = sp.pieces;
-  sp.smem_syn = static_cast<size_t>(SPLIT_STAGES) * pieces * (128 * SPLIT_BK * 2 + sp.nh16 * SPLIT_BK * 2);
-  const size_t ana_pipe = static_cast<size_t>(SPLIT_STAGES) * pieces * (128 * SPLIT_BK * 2 + ra_max * SPLIT_BK * 2);
-  sp.smem_ana = std::max(ana_pipe, static_cast<size_t>(128) * 2 * ra_max * sizeof(float));
+  const size_t budget = 220 * 1024;
+  const size_t syn_stage = static_cast<size_t>(pieces) * (sp.rSP + sp.nh16) * SPLIT_BK * 2;
+  sp.ns_syn = static_cast<int>(std::min<size_t>(SPLIT_MAX_STAGES, (budget - SPLIT_MARGIN) / syn_stage));
+  if (sp.ns_syn < 2) throw InvalidArgument("split precision: the synthesis pipeline does not fit in shared memory");
+  sp.smem_syn = sp.ns_syn * syn_stage + SPLIT_MARGIN;
+  const size_t nchunk = sp.nh64 / SPLIT_BK;
+  const size_t ana_res = static_cast<size_t>(pieces) * nchunk * (sp.rAH + sp.rAP) * 128;
+  const size_t ana_stage = static_cast<size_t>(pieces) * ra_max * SPLIT_BK * 2;
+  // two analysis CTAs per SM when a 3-stage pipeline fits in half of the shared memory
+  const size_t half = 110 * 1024;
+  if (ana_res + 3 * ana_stage + SPLIT_MARGIN <= half && static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float) <= half)
+    sp.ns_ana = 3;
+  else
+    sp.ns_ana = static_cast<int>(std::min<size_t>(SPLIT_MAX_STAGES, (budget - SPLIT_MARGIN - ana_res) / ana_stage));
+  if (sp.ns_ana < 2) throw InvalidArgument("split precision: the analysis pipeline does not fit in shared memory");
+  sp.smem_ana = std::max(ana_res + sp.ns_ana * ana_stage + SPLIT_MARGIN, static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float));
 }
 
 inline SplitDev split_dev(const SplitPlan &sp) {
@@ -704,6 +784,7 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.aA_P = sp.aA_P.p;
   s.aA_H = sp.aA_H.p;
   s.dsyn = sp.dsyn.p;
+  s.fold = nullptr;
   s.err = sp.err.p;
   return s;
 }
