@@ -174,6 +174,27 @@ int lmw_plane_step_noalloc(int nx, int ny, double lx, double ly, double gravity,
  * No reference counterpart (measurement hook). */
 int lmw_plane_kernel_time(lmw_plane *p, double dt, int reps, double *ms);
 
+/* ---------------------------------------------------------------------------------------- ensemble */
+
+typedef struct lmw_ensemble lmw_ensemble;
+/* An ensemble of spheres with mixed truncations (no single reference counterpart: each member is a
+ * Sphere(T, SphereParams) of cpp/sphere.hpp:29 initialised by lmw_sphere_turbulence with nforce = T/2 and del^4
+ * diffusion with a 1-day e-folding at n = T). Members of one truncation are stepped together as one batch;
+ * precision and split_terms as in lmw_sphere_create_split. Arrays have `count` entries. */
+int lmw_ensemble_create(int count, const int *truncation, const uint64_t *seed, const double *mean_height, const double *omega, double radius,
+                        double gravity, double max_wind, int precision, int split_terms, lmw_ensemble **out);
+int lmw_ensemble_destroy(lmw_ensemble *e);
+/* Sphere::run(seconds, 0) for every member (cpp/sphere.cpp:457-484): each truncation group at its own stable step
+ * (stable_dt(1.5), the smallest over the group), the guards every 64 steps over every member. */
+int lmw_ensemble_run(lmw_ensemble *e, double seconds);
+/* per truncation group: truncation, member count, and the step size and step count of the last run */
+int lmw_ensemble_groups(lmw_ensemble *e, int *ngroups, int *truncations, int *counts, double *last_dt, int64_t *last_steps);
+/* one member's spectral state (reference layout of its truncation), diagnostics (as lmw_sphere_diagnostics) and grids */
+int lmw_ensemble_member_state(lmw_ensemble *e, int member, double *zeta, double *delta, double *phi);
+int lmw_ensemble_member_set_state(lmw_ensemble *e, int member, const double *zeta, const double *delta, const double *phi);
+int lmw_ensemble_member_diagnostics(lmw_ensemble *e, int member, double *out);
+int lmw_ensemble_member_grid(lmw_ensemble *e, int member, int which, double *out, size_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,7 +13,7 @@ import os
 
 import numpy as np
 
-__all__ = ["Sphere", "Plane", "DeviceError", "load_library", "library_path", "launch_count", "FP64", "FP32", "SPLIT_BF16"]
+__all__ = ["Sphere", "Plane", "Ensemble", "DeviceError", "load_library", "library_path", "launch_count", "FP64", "FP32", "SPLIT_BF16"]
 
 FP64, FP32, SPLIT_BF16 = 0, 1, 2
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -76,6 +76,14 @@ _SIGS = {
     "lmw_plane_stable_dt": (_I, [_P, _D, _DP]),
     "lmw_plane_time": (_I, [_P, _DP]),
     "lmw_plane_diagnostics": (_I, [_P, _DP]),
+    "lmw_ensemble_create": (_I, [_I, _IP, C.POINTER(C.c_uint64), _DP, _DP, _D, _D, _D, _I, _I, _PP]),
+    "lmw_ensemble_destroy": (_I, [_P]),
+    "lmw_ensemble_run": (_I, [_P, _D]),
+    "lmw_ensemble_groups": (_I, [_P, _IP, _IP, _IP, _DP, C.POINTER(C.c_int64)]),
+    "lmw_ensemble_member_state": (_I, [_P, _I, _DP, _DP, _DP]),
+    "lmw_ensemble_member_set_state": (_I, [_P, _I, _DP, _DP, _DP]),
+    "lmw_ensemble_member_diagnostics": (_I, [_P, _I, _DP]),
+    "lmw_ensemble_member_grid": (_I, [_P, _I, _I, _DP, _SZ]),
 }
 
 
@@ -403,3 +411,59 @@ class Plane:
 
     def max_speed(self) -> float:
         return self.diagnostics()["max_speed"]
+
+
+class Ensemble:
+    """Spheres with mixed truncations stepped together on the GPU (members of one truncation form one batch).
+    Member i: truncation[i], seed[i] (balanced turbulence, nforce = T/2), mean_height[i], omega[i]."""
+
+    def __init__(self, truncation, seed, mean_height, omega, radius=6.37122e6, gravity=9.80616, max_wind=30.0,
+                 precision: int = FP64, split_terms: int = 3):
+        self._lib = load_library()
+        n = len(truncation)
+        tr = np.ascontiguousarray(truncation, np.int32)
+        sd = np.ascontiguousarray(seed, np.uint64)
+        mh = np.ascontiguousarray(mean_height, np.float64)
+        om = np.ascontiguousarray(omega, np.float64)
+        h = C.c_void_p()
+        _check(self._lib.lmw_ensemble_create(n, tr.ctypes.data_as(_IP), sd.ctypes.data_as(C.POINTER(C.c_uint64)), _dp(mh), _dp(om),
+                                             radius, gravity, max_wind, precision, split_terms, C.byref(h)))
+        self._h = h
+        self.truncation = tr.copy()
+        self.count = n
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lmw_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, seconds: float):
+        _check(self._lib.lmw_ensemble_run(self._h, seconds))
+        return self
+
+    def groups(self):
+        ng = _I()
+        _check(self._lib.lmw_ensemble_groups(self._h, C.byref(ng), None, None, None, None))
+        G = ng.value
+        tr, cnt = np.zeros(G, np.int32), np.zeros(G, np.int32)
+        dt, st = np.zeros(G), np.zeros(G, np.int64)
+        _check(self._lib.lmw_ensemble_groups(self._h, C.byref(ng), tr.ctypes.data_as(_IP), cnt.ctypes.data_as(_IP), _dp(dt),
+                                             st.ctypes.data_as(C.POINTER(C.c_int64))))
+        return [dict(truncation=int(tr[g]), members=int(cnt[g]), dt=float(dt[g]), steps=int(st[g])) for g in range(G)]
+
+    def member_state(self, i: int):
+        T = int(self.truncation[i])
+        z, d, f = (np.zeros((T + 1) ** 2, np.complex128) for _ in range(3))
+        _check(self._lib.lmw_ensemble_member_state(self._h, i, _dp(z.view(np.float64)), _dp(d.view(np.float64)), _dp(f.view(np.float64))))
+        return z, d, f
+
+    def member_diagnostics(self, i: int) -> dict:
+        out = np.zeros(8)
+        _check(self._lib.lmw_ensemble_member_diagnostics(self._h, i, _dp(out)))
+        return dict(zip(Sphere._DIAG, out.tolist()))

@@ -25,6 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = [
     ("plane.cu", ["--fmad=false"]),
     ("sphere.cu", []),
+    ("ensemble.cu", []),
     ("sphere32.cu", []),
     ("capi.cu", []),
     ("peak.cu", []),

@@ -15,6 +15,9 @@ struct lmw_sphere {
 struct lmw_plane {
   lmw::PlaneEngine *e;
 };
+struct lmw_ensemble {
+  lmw::EnsembleEngine *e;
+};
 
 namespace lmw {
 thread_local uint64_t g_launches = 0;
@@ -323,6 +326,84 @@ int lmw_plane_kernel_time(lmw_plane *p, double dt, int reps, double *ms) {
   return PLN({
     need(reps > 0, "reps must be positive");
     *ms = p->e->kernel_time(dt, reps);
+  });
+}
+
+// ------------------------------------------------------------------------------------------------ ensemble
+int lmw_ensemble_create(int count, const int *truncation, const uint64_t *seed, const double *mean_height, const double *omega, double radius,
+                        double gravity, double max_wind, int precision, int split_terms, lmw_ensemble **out) {
+  return guard([&] {
+    need(out != nullptr, "output handle pointer is null");
+    *out = nullptr;
+    need(count > 0 && truncation && seed && mean_height && omega, "member arrays are missing");
+    std::vector<lmw::MemberSpec> specs(count);
+    for (int i = 0; i < count; i++) {
+      specs[i].truncation = truncation[i];
+      specs[i].seed = seed[i];
+      specs[i].mean_height = mean_height[i];
+      specs[i].omega = omega[i];
+    }
+    auto *h = new lmw_ensemble{nullptr};
+    try {
+      h->e = new lmw::EnsembleEngine(specs, radius, gravity, max_wind, precision, split_terms);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int lmw_ensemble_destroy(lmw_ensemble *e) {
+  return guard([&] {
+    if (!e) return;
+    delete e->e;
+    delete e;
+  });
+}
+#define ENS(...)                                                   \
+  guard([&] {                                                      \
+    need(e != nullptr && e->e != nullptr, "null ensemble handle"); \
+    __VA_ARGS__;                                                   \
+  })
+int lmw_ensemble_run(lmw_ensemble *e, double seconds) { return ENS(e->e->run(seconds)); }
+int lmw_ensemble_groups(lmw_ensemble *e, int *ngroups, int *truncations, int *counts, double *last_dt, int64_t *last_steps) {
+  return ENS({
+    const int G = static_cast<int>(e->e->groups.size());
+    if (ngroups) *ngroups = G;
+    for (int g = 0; g < G; g++) {
+      if (truncations) truncations[g] = e->e->truncations[g];
+      if (counts) counts[g] = e->e->groups[g]->B;
+      if (last_dt) last_dt[g] = e->e->last_dt[g];
+      if (last_steps) last_steps[g] = e->e->last_steps[g];
+    }
+  });
+}
+int lmw_ensemble_member_state(lmw_ensemble *e, int member, double *zeta, double *delta, double *phi) {
+  return ENS({
+    int k = 0;
+    e->e->engine_of(member, &k).get_state(zeta, delta, phi, k);
+  });
+}
+int lmw_ensemble_member_set_state(lmw_ensemble *e, int member, const double *zeta, const double *delta, const double *phi) {
+  return ENS({
+    need(zeta && delta && phi, "state pointer is null");
+    int k = 0;
+    lmw::SphereEngine &s = e->e->engine_of(member, &k);
+    s.set_state(zeta, delta, phi, s.t[k], k);
+  });
+}
+int lmw_ensemble_member_diagnostics(lmw_ensemble *e, int member, double *out) {
+  return ENS({
+    int k = 0;
+    e->e->engine_of(member, &k).diagnostics(out, k);
+  });
+}
+int lmw_ensemble_member_grid(lmw_ensemble *e, int member, int which, double *out, size_t n) {
+  return ENS({
+    int k = 0;
+    lmw::SphereEngine &s = e->e->engine_of(member, &k);
+    need(n == s.ngrid(), "grid size mismatch");
+    s.grid(which, out, k);
   });
 }
 

@@ -1,5 +1,7 @@
 // Engine objects behind the C ABI: device-resident state, one CUDA stream per object.
 #pragma once
+#include <memory>
+
 #include "lmw_internal.h"
 
 namespace lmw {
@@ -108,6 +110,16 @@ class SphereEngine {
   void step(double dt);
   void run(double seconds, double dt);
   double stable_dt(double safety, int member);
+  double stable_dt_all(double safety);
+  // a run split into guard-sized chunks, so that several engines can interleave their work on their streams
+  struct RunPlan {
+    int64_t n = 0, i = 0;
+    double h = 0;
+    bool guard_due = false;
+  };
+  RunPlan plan_run(double seconds, double dt);
+  bool advance(RunPlan &rp);
+  void guard(RunPlan &rp);
   // mean_height, kinetic, potential, energy, enstrophy, max_wind, error_l2, error_linf
   void diagnostics(double *out, int member);
   // which: 0 height, 1 u, 2 v, 3 vorticity
@@ -149,9 +161,36 @@ class SphereEngine {
   void launch_chunk(double dt, int steps);
   void synth_grids(int member_first, int count);  // state x0 -> Fourier coefficients of U, V, zeta, phi
   void reduce_guard(Reduce &r, int member);
+  void reduce_guard_all();
+  double limit_from(const Reduce &r, int b, double safety) const;
   void analyze_grids_to_state(int member);
   void to_packed(const double *ref_layout, double *packed);
   void from_packed(const double *packed, double *ref_layout);
+};
+
+// ------------------------------------------------------------------------------------------------ ensemble
+struct MemberSpec {
+  int truncation = 42;
+  uint64_t seed = 1;
+  double mean_height = 8000.0;
+  double omega = 7.292e-5;
+};
+
+class EnsembleEngine {
+ public:
+  EnsembleEngine(const std::vector<MemberSpec> &specs, double radius, double gravity, double max_wind, int precision, int split_terms);
+  std::vector<MemberSpec> members;
+  std::vector<std::unique_ptr<SphereEngine>> groups;
+  std::vector<int> truncations, group_of, index_in_group;
+  std::vector<double> last_dt;
+  std::vector<int64_t> last_steps;
+  void run(double seconds);
+  void check_member(int i) const;
+  SphereEngine &engine_of(int i, int *k) {
+    check_member(i);
+    *k = index_in_group[i];
+    return *groups[group_of[i]];
+  }
 };
 
 }  // namespace lmw

@@ -1119,6 +1119,37 @@ void SphereEngine::reduce_guard(Reduce &r, int member) {
   r = hred.p[0];
 }
 
+// guard reductions of every member in one pass (FP64 synthesis and grid reductions), read back once
+void SphereEngine::reduce_guard_all() {
+  SphDev d = make_sph(*this, *tab);
+  synth_grids(0, B);
+  const size_t smem = 4 * static_cast<size_t>(nlon) * sizeof(double2);
+  sph_diag<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), fgrid.p, hsgrid.p, refgrid.p, diagrows.p,
+                                                        nullptr);
+  sph_diag_final<<<B, GRID_THREADS, 0, stream>>>(d, diagrows.p, reinterpret_cast<const double2 *>(x0.p), 0, dred.p);
+  LMW_LAUNCH_CHECK();
+  g_launches += 2;
+  LMW_CUDA(cudaMemcpyAsync(hred.p, dred.p, B * sizeof(Reduce), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+}
+
+// RK4 limit of member b from its guard reduction (cpp/sphere.cpp:438-447)
+double SphereEngine::limit_from(const Reduce &r, int b, double safety) const {
+  double hmax = std::max(0.0, r.max[1]);
+  if (!(hmax > 0)) throw RuntimeError("the height field must be positive to step the model");
+  double omega = (N / p.radius) * (std::sqrt(p.gravity * hmax) + r.max[0]) + 2 * omega_m[b];
+  if (!(omega > 0)) return 1e9;
+  return safety / omega;
+}
+
+// the smallest stable step over the members
+double SphereEngine::stable_dt_all(double safety) {
+  reduce_guard_all();
+  double dt = 1e300;
+  for (int b = 0; b < B; b++) dt = std::min(dt, limit_from(hred.p[b], b, safety));
+  return dt;
+}
+
 // cpp/sphere.cpp:438-447
 double SphereEngine::stable_dt(double safety, int member) {
   Reduce r;
@@ -1130,54 +1161,62 @@ double SphereEngine::stable_dt(double safety, int member) {
   return safety / omega;
 }
 
-// cpp/sphere.cpp:457-484; every member steps with the same dt, the guards check each member
-void SphereEngine::run(double seconds, double dt) {
+// cpp/sphere.cpp:457-466: equal steps, the stability pre-check over every member
+SphereEngine::RunPlan SphereEngine::plan_run(double seconds, double dt) {
+  RunPlan rp;
   if (!(seconds >= 0)) throw InvalidArgument("run: seconds must not be negative");
-  if (seconds == 0) return;
-  if (!(dt > 0)) {
-    dt = 1e300;
-    for (int b = 0; b < B; b++) dt = std::min(dt, stable_dt(1.5, b));
-  }
-  double limit = 1e300;
-  for (int b = 0; b < B; b++) limit = std::min(limit, stable_dt(2.0 * std::sqrt(2.0), b));
+  if (seconds == 0) return rp;
+  if (!(dt > 0)) dt = stable_dt_all(1.5);
+  const double limit = stable_dt_all(2.0 * std::sqrt(2.0));
   if (!(dt <= limit))
     throw InvalidArgument("run: dt = " + fmt_f(dt) + " s exceeds the RK4 stability limit of about " + fmt_f(limit) +
                           " s for the present state: use a smaller dt");
   int64_t n = static_cast<int64_t>(std::ceil(seconds / dt - 1e-9));
   if (n < 1) n = 1;
   if (n > 50000000) throw InvalidArgument("run: more than 5e7 steps; use a larger dt");
-  double h = seconds / static_cast<double>(n);
-  upload_filter(h);
-  int64_t i = 0;
-  while (i < n) {
-    int64_t next = std::min<int64_t>(n - 1, i | 63);
-    int chunk = static_cast<int>(next - i + 1);
-    if (chunk == 64) launch_chunk(h, 64);
-    else for (int s = 0; s < chunk; s++) enqueue_step(h);
-    for (int s = 0; s < chunk; s++)
-      for (int b = 0; b < B; b++) t[b] += h;
-    i = next + 1;
-    check_split_status();
-    if ((next & 63) == 63) {
-      for (int b = 0; b < B; b++) {
-        Reduce r;
-        reduce_guard(r, b);
-        if (!std::isfinite(r.sum[5])) throw RuntimeError("the integration blew up (not finite): use a smaller dt");
-        double hmax = std::max(0.0, r.max[1]);
-        if (!(hmax > 0)) throw RuntimeError("the height field must be positive to step the model");
-        double omega = (N / p.radius) * (std::sqrt(p.gravity * hmax) + r.max[0]) + 2 * omega_m[b];
-        double now = omega > 0 ? 2.0 * std::sqrt(2.0) / omega : 1e9;
-        if (!(h <= now))
-          throw RuntimeError("run: dt = " + fmt_f(h) + " s exceeds the RK4 stability limit of about " + fmt_f(now) + " s reached at t = " +
-                             fmt_f(t[b]) + " s (the flow accelerated): use a smaller dt");
-      }
+  rp.n = n;
+  rp.h = seconds / static_cast<double>(n);
+  upload_filter(rp.h);
+  return rp;
+}
+
+// enqueue the steps up to the next guard point (no synchronisation); true when a guard check is due
+bool SphereEngine::advance(RunPlan &rp) {
+  if (rp.i >= rp.n) return false;
+  int64_t next = std::min<int64_t>(rp.n - 1, rp.i | 63);
+  int chunk = static_cast<int>(next - rp.i + 1);
+  if (chunk == 64) launch_chunk(rp.h, 64);
+  else for (int s = 0; s < chunk; s++) enqueue_step(rp.h);
+  for (int s = 0; s < chunk; s++)
+    for (int b = 0; b < B; b++) t[b] += rp.h;
+  rp.i = next + 1;
+  rp.guard_due = (next & 63) == 63;
+  return true;
+}
+
+// cpp/sphere.cpp:473-483: every 64 steps the finiteness check and the stability re-check, and a final
+// finiteness check, over every member
+void SphereEngine::guard(RunPlan &rp) {
+  const bool last = rp.i >= rp.n;
+  if (!rp.guard_due && !last) return;
+  check_split_status();
+  reduce_guard_all();
+  for (int b = 0; b < B; b++) {
+    const Reduce &r = hred.p[b];
+    if (!std::isfinite(r.sum[5])) throw RuntimeError("the integration blew up (not finite): use a smaller dt");
+    if (rp.guard_due) {
+      const double now = limit_from(r, b, 2.0 * std::sqrt(2.0));
+      if (!(rp.h <= now))
+        throw RuntimeError("run: dt = " + fmt_f(rp.h) + " s exceeds the RK4 stability limit of about " + fmt_f(now) + " s reached at t = " +
+                           fmt_f(t[b]) + " s (the flow accelerated): use a smaller dt");
     }
   }
-  for (int b = 0; b < B; b++) {
-    Reduce r;
-    reduce_guard(r, b);
-    if (!std::isfinite(r.sum[5])) throw RuntimeError("the integration blew up (not finite): use a smaller dt");
-  }
+  rp.guard_due = false;
+}
+
+void SphereEngine::run(double seconds, double dt) {
+  RunPlan rp = plan_run(seconds, dt);
+  while (advance(rp)) guard(rp);
 }
 
 // cpp/sphere.cpp:510-590
