@@ -890,7 +890,8 @@ void SphereEngine::perturb(double amplitude, uint64_t seed, int max_wave, int me
 
 // Seeded balanced turbulence (this project's benchmark initialiser; the same definition as the oracle's
 // or_sphere_turbulence_grids): complex-Gaussian vorticity for 1 <= n <= nforce with a kinetic-energy spectrum
-// proportional to n^-3 and the largest grid wind equal to max_wind, zero divergence, h = mean + f psi / g.
+// proportional to n^-3 and the largest grid wind equal to max_wind, zero divergence, h = mean + f psi / g less
+// the area mean of f psi / g.
 void SphereEngine::turbulence(uint64_t seed, double mean_height, double max_wind, int nforce, int member) {
   check_member(*this, member);
   const HostTables &h = tab->host;
@@ -942,9 +943,18 @@ void SphereEngine::turbulence(uint64_t seed, double mean_height, double max_wind
     double f = 2 * omega_m[member] * h.mu[j];
     for (int k = 0; k < nlon; k++) {
       size_t i = static_cast<size_t>(j) * nlon + k;
-      hh[i] = mean_height + f * hh[i] / p.gravity;
+      hh[i] = f * hh[i] / p.gravity;
     }
   }
+  // remove the Gaussian-quadrature area mean of the balanced part: the mean height is mean_height
+  double sum = 0;
+  for (int j = 0; j < nlat; j++) {
+    double row = 0;
+    for (int k = 0; k < nlon; k++) row += hh[static_cast<size_t>(j) * nlon + k];
+    sum += h.w[j] * row / nlon;
+  }
+  const double hmean = 0.5 * sum;
+  for (auto &x : hh) x = mean_height + (x - hmean);
   set_state_grid(hh.data(), uu.data(), vv.data(), ngrid(), member);
 }
 

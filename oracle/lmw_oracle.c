@@ -764,7 +764,8 @@ void or_sphere_analyze_divergence(const or_sphere *s, const double *A, const dou
  * (Irwin-Hall normals from splitmix64, imaginary part 0 at m = 0), rescaled per degree n so that the
  * kinetic-energy spectrum (the reference's formula, cpp/sphere.cpp:547) goes as n^-3, then globally so that
  * the largest grid wind equals max_wind. Divergence is zero. Height is mean_height + f psi / g with
- * f = 2 Omega mu (linear balance). The grids feed set_state_grid. */
+ * f = 2 Omega mu (linear balance), less the area mean of f psi / g so that the mean height is mean_height. The
+ * grids feed set_state_grid. */
 void or_sphere_turbulence_grids(const or_sphere *s, uint64_t seed, double mean_height, double max_wind, int nforce,
                                 double *h, double *u, double *v) {
   const double a = s->radius, a2 = a * a;
@@ -815,9 +816,19 @@ void or_sphere_turbulence_grids(const or_sphere *s, uint64_t seed, double mean_h
     double f = 2 * s->omega * s->mu[j];
     for (int k = 0; k < s->nlon; k++) {
       size_t i = (size_t)j * s->nlon + k;
-      h[i] = mean_height + f * h[i] / s->gravity;
+      h[i] = f * h[i] / s->gravity;
     }
   }
+  /* remove the area mean of the balanced part (Gaussian quadrature, as the reference's area means) so that the
+     mean height is mean_height */
+  double sum = 0;
+  for (int j = 0; j < s->nlat; j++) {
+    double row = 0;
+    for (int k = 0; k < s->nlon; k++) row += h[(size_t)j * s->nlon + k];
+    sum += s->w[j] * row / s->nlon;
+  }
+  const double hmean = 0.5 * sum;
+  for (size_t i = 0; i < ng; i++) h[i] = mean_height + (h[i] - hmean);
   free(z); free(zero); free(psi); free(U); free(V);
 }
 

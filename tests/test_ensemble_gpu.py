@@ -28,7 +28,7 @@ def test_ensemble_members_match_single_runs(engine):
         for a, b in zip(ens.member_state(i), s.get_state()):
             scale = np.abs(b).max()
             assert np.abs(a - b).max() <= 1e-13 * scale
-        assert ens.member_diagnostics(i)["mean_height"] == pytest.approx(heights[i], rel=1e-12)
+        assert ens.member_diagnostics(i)["mean_height"] == pytest.approx(heights[i], rel=1e-12)  # the recipe's mean
 
 
 def test_ensemble_split_precision_close_to_fp64(engine):
