@@ -1,26 +1,35 @@
 """Benchmark: simulated days per second of the shallow-water time stepping on GB300.
 
-Headline workload (one JSON line on rank 0): the sphere at T42 on the 128 x 64 Gaussian grid, FP64, seeded
-balanced turbulence (n <= 21, n^-3 kinetic-energy spectrum, 30 m/s, mean height 8000 m), del^4 diffusion with a
-1-day e-folding at n = 42, RK4 dt = 900 s; one benchmark step = one run() of 480 RK4 steps (5 model days) with the
-reference's guards every 64 steps. Inputs are synthetic and seeded.
+Headline workload: the mixed-truncation ensemble of 1024 spheres (512 at T21 on 64 x 32, 384 at T42 on 128 x 64,
+128 at T85 on 256 x 128), each member with its own seed (balanced turbulence, n <= T/2, n^-3 kinetic-energy
+spectrum, 30 m/s), a mean height drawn uniformly from 5000-10000 m and Omega scaled by 0.5, 1 or 2; del^4
+diffusion with a 1-day e-folding at n = T; every truncation at its own stable RK4 step (the reference's
+stable_dt(1.5), smallest over the group) with the reference's guards every 64 steps. One benchmark step = one
+run() of 2 model days of every member, in split precision (Legendre sums on tcgen05 with BF16 hi/lo products and
+FP32 accumulation, FP32 FFTs and products, FP64 state). Inputs are synthetic and seeded.
 
-  value     sim-days/s from CUDA events on the engine stream, state resident in HBM, L2 flushed between timed steps
-  e2e       the same through the C ABI with host buffers: set_state from pinned host memory, run, get_state
-  roofline  the dominant kernel's algorithmic FLOP per launch / its measured launch time, against the measured
-            FP64 FMA peak of the device (the plain path computes in FP64 throughout)
-  cpu_baseline  the oracle (a restatement of the reference algorithm) timed on a bounded sample on the host
+  value         member-sim-days/s = members x 2 days / device time of the run (CUDA events on the group streams),
+                state resident in HBM, L2 flushed (512 MB write) between timed steps
+  e2e           the same through the C ABI with host buffers: every member's state from host, run, state to host
+  error         split vs FP64 runs of a subset of members: relative L2 height error and Phi error after 2 days
+  roofline      the stage kernel with the largest share of device time, its algorithmic bytes per launch over its
+                CUDA-event launch time, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (the reference algorithm restated in C) timed per member-step on every host core,
+                scaled to the workload's member-step counts
+  workloads     the other configurations: T42 plain FP64 (config 0), the 1024 x 512 beta-plane (config 1), the
+                T170 precision study (config 2) and the ensemble in the other precisions
 
-`--impl reference` times the reference's CPU algorithm (the oracle port; the reference checkout itself does not
-exist on the GPU host) on the same workload and prints the same line with "impl": "reference".
-Under torchrun (N > 1) every rank runs its own replica (weak scaling: members are independent; no collective on
-the data path); rank 0 prints the max-over-ranks time.
+`--impl reference` times the reference's CPU algorithm (the oracle port: the reference checkout is absent on the
+GPU host) on the same workload with all host cores and prints the same line with "impl": "reference".
+Under torchrun (N > 1) every rank runs its own replica of the ensemble (members are independent: weak scaling, no
+collective on the data path); rank 0 prints the max-over-ranks time.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import math
+import multiprocessing as mp
 import os
 import statistics
 import subprocess
@@ -32,23 +41,38 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 A = 6.37122e6
-T42_NU4 = A ** 4 / (86400.0 * (42 * 43) ** 2)
-WORKLOAD = {"workload": "sphere_t42_fp64_turbulence", "truncation": 42, "grid": "128x64", "dt_s": 900.0,
-            "rk4_steps_per_bench_step": 480, "seed": 1, "nforce": 21, "mean_height_m": 8000.0, "max_wind_ms": 30.0,
-            "diffusion_m4s": T42_NU4, "precision": "fp64", "members": 1}
-METRIC = "sim-days/s at T42 (plain FP64, 128x64 Gaussian grid, RK4 dt=900 s)"
+OMEGA = 7.292e-5
+DAYS = 2.0
+METRIC = "member-sim-days/s, 1024-member T21/T42/T85 ensemble, 2 model days (split-BF16 Legendre on tcgen05, FP64 state)"
+
+
+def nu4(T):
+    return A ** 4 / (86400.0 * (T * (T + 1.0)) ** 2)
+
+
+def ensemble_specs(seed_base: int = 0):
+    import numpy as np
+
+    tr = [21] * 512 + [42] * 384 + [85] * 128
+    rng = np.random.default_rng(2026 + seed_base)
+    heights = rng.uniform(5000.0, 10000.0, len(tr))
+    omegas = [OMEGA * (0.5, 1.0, 2.0)[i % 3] for i in range(len(tr))]
+    seeds = [seed_base * 100000 + i + 1 for i in range(len(tr))]
+    return tr, seeds, list(heights), omegas
+
+
+WORKLOAD = {"workload": "ensemble_t21x512_t42x384_t85x128_2days", "members": 1024, "truncations": {"21": 512, "42": 384, "85": 128},
+            "grids": {"21": "64x32", "42": "128x64", "85": "256x128"}, "model_days_per_bench_step": DAYS,
+            "init": "balanced turbulence, nforce = T/2, max wind 30 m/s, mean height U[5000, 10000] m, Omega x {0.5, 1, 2}",
+            "diffusion": "del^4, 1-day e-folding at n = T", "step": "stable_dt(1.5) per truncation, guards every 64 steps"}
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
 class Dist:
-    def __init__(self, world: int, local: int, backend: str):
-        self.world = world
+    def __init__(self, world: int, backend: str):
         self.pg = None
         if world > 1:
             import torch.distributed as dist
@@ -76,7 +100,7 @@ class Dist:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons every 200 ms during the timed region."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -114,8 +138,9 @@ class ClockSampler:
         sm = [float(r[1]) for r in rows]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(float(r[2]) for r in rows), "reasons": reasons,
-                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()) if rows else None}
+        pw = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(float(r[2]) for r in rows), "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(pw) if pw else None}
 
 
 def peaks() -> dict:
@@ -126,170 +151,338 @@ def peaks() -> dict:
         return {}
 
 
-# ----------------------------------------------------------------------------------------------- reference arm
-def cpu_sample(rk4_steps: int):
-    """Time the oracle (the reference algorithm restated in C, one thread: the reference core is single-threaded
-    and one member cannot use more) on `rk4_steps` RK4 steps of the headline workload. Returns sim-days/s."""
+# ----------------------------------------------------------------------------------------------- CPU side (oracle)
+def _cpu_member_steps(args):
+    """One worker: seconds per RK4 step of one member at truncation T (oracle port, one thread)."""
+    T, steps, dt = args
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import OracleSphere
 
-    o = OracleSphere(42, diffusion=T42_NU4)
-    h, u, v = o.turbulence_grids(1, 8000.0, 30.0, 21)
+    o = OracleSphere(T, diffusion=nu4(T))
+    h, u, v = o.turbulence_grids(7, 8000.0, 30.0, T // 2)
     o.set_state_grid(h, u, v)
-    o.step(900.0)
+    o.step(dt)
     t0 = time.perf_counter()
-    for _ in range(rk4_steps):
-        o.step(900.0)
-    dt = time.perf_counter() - t0
-    return rk4_steps * 900.0 / 86400.0 / dt, dt
+    for _ in range(steps):
+        o.step(dt)
+    return T, (time.perf_counter() - t0) / steps
+
+
+def cpu_ensemble_rate(group_steps: dict, sample_steps: dict, cores: int):
+    """Member-sim-days/s of the reference algorithm on `cores` host cores: every core times member-steps of each
+    truncation at once (a bounded sample), and the workload's member-step counts are divided over the cores."""
+    ctx = mp.get_context("spawn")
+    jobs = []
+    for c in range(cores):
+        for T, (n, dt) in sample_steps.items():
+            jobs.append((T, n, dt))
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_member_steps, jobs)
+    wall = time.perf_counter() - t0
+    per = {}
+    for T, sec in res:
+        per.setdefault(T, []).append(sec)
+    cost = {T: statistics.median(v) for T, v in per.items()}
+    cpu_seconds = sum(group_steps[T] * cost[T] for T in group_steps)  # one core
+    member_days = 1024 * DAYS
+    rate = member_days / (cpu_seconds / cores)
+    return rate, cost, wall
+
+
+def build_oracle():
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import build_oracle as bo
+
+    bo(with_ref=False)
+
+
+GROUP_STEPS_NOMINAL = None
+
+
+def ensemble_member_steps(groups):
+    return {g["truncation"]: g["members"] * g["steps"] for g in groups}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    from oracle_lib import build_oracle  # noqa: F401  (path set in cpu_sample)
-
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from oracle_lib import build_oracle as bo
-
-    bo(with_ref=False)
-    per_step = 64  # bounded sample: 64 of the 480 RK4 steps per benchmark step (~1 s of host time)
+    build_oracle()
+    cores = os.cpu_count() or 1
+    # member-step counts of the 2-day workload (per truncation: members x steps at the engine's stable step)
+    steps = {21: 512 * 186, 42: 384 * 341, 85: 128 * 640}
+    sample = {21: (6, 929.0), 42: (3, 506.7), 85: (1, 270.0)}
     for _ in range(args.warmup):
-        cpu_sample(4)
-    vals, secs = [], 0.0
+        cpu_ensemble_rate(steps, {21: (1, 929.0), 42: (1, 506.7), 85: (1, 270.0)}, cores)
+    vals, costs = [], None
     for _ in range(args.steps):
-        v, s = cpu_sample(per_step)
+        v, costs, _ = cpu_ensemble_rate(steps, sample, cores)
         vals.append(v)
-        secs += s
     value = statistics.median(vals)
-    ms_per_step = 480 * 900.0 / 86400.0 / value * 1e3
-    sample = f"{per_step} RK4 steps (dt 900 s) of the 480-step T42 run per benchmark step, oracle port, 1 thread"
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "sim-days/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded balanced turbulence)", "config": WORKLOAD,
-            "cpu_baseline": {"value": value, "unit": "sim-days/s", "cores": 1, "kind": "port", "sample": sample},
-            "e2e": {"value": value, "unit": "sim-days/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    ms = 1024 * DAYS / value * 1e3
+    smp = (f"per bench step every one of {cores} cores times 6 T21, 3 T42 and 1 T85 member-steps (oracle port, one thread each); "
+           f"the 2-day workload's member-step counts (T21 {steps[21]}, T42 {steps[42]}, T85 {steps[85]}) are divided over the cores")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "member-sim-days/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded balanced turbulence)", "config": WORKLOAD,
+            "cpu_baseline": {"value": value, "unit": "member-sim-days/s", "cores": cores, "kind": "port", "sample": smp,
+                             "member_step_seconds": {str(k): v for k, v in (costs or {}).items()}},
+            "e2e": {"value": value, "unit": "member-sim-days/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-# ----------------------------------------------------------------------------------------------- our arm
+# ----------------------------------------------------------------------------------------------- GPU side
 def run_ours(args, rank, world, local):
     import ctypes
 
     import numpy as np
     import torch
 
+    if rank == 0 and world == 1:
+        build_oracle()  # before any CUDA work (the CPU baseline's worker pool starts by spawn)
     torch.cuda.set_device(local)
     from lmweather_gb300 import build as b
 
     if rank == 0 or world == 1:
         b.build()
-    dist = Dist(world, local, "nccl")
+    dist = Dist(world, "nccl")
     dist.barrier()
     import lmweather_gb300 as lw
 
     lib = lw.load_library()
-    lib.lmw_sphere_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
-    lib.lmw_sphere_kernel_times.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
-    lib.lmw_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    lib.lmw_ensemble_stream.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    lib.lmw_ensemble_kernel_times.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    prec = {"split3": dict(precision=lw.SPLIT_BF16, split_terms=3), "split6": dict(precision=lw.SPLIT_BF16, split_terms=6),
+            "fp32": dict(precision=lw.FP32), "fp64": dict(precision=lw.FP64)}
+    tr, seeds, heights, omegas = ensemble_specs(rank)
+    ens = lw.Ensemble(tr, seeds, heights, omegas, **prec[args.precision])
+    streams = []
+    for g in range(len(ens.groups())):
+        sp = ctypes.c_void_p()
+        lw._check(lib.lmw_ensemble_stream(ens._h, g, ctypes.byref(sp)))
+        streams.append(torch.cuda.ExternalStream(sp.value))
+    seconds = DAYS * 86400.0
+    z0 = [ens.member_state(i) for i in range(ens.count)]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    s = lw.Sphere(42, diffusion=T42_NU4)
-    s.turbulence(1 + rank, 8000.0, 30.0, 21)
-    z0, d0, f0 = s.get_state()
-    sp = ctypes.c_void_p()
-    lw._check(lib.lmw_sphere_stream(s._h, ctypes.byref(sp)))
-    stream = torch.cuda.ExternalStream(sp.value)
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 512 MB > L2 (129 MB)
-    seconds = 480 * 900.0
+    def reset_states():
+        for i in range(ens.count):
+            z, d, f = z0[i]
+            lw._check(lib.lmw_ensemble_member_set_state(ens._h, i, lw._dp(z.view(np.float64)), lw._dp(d.view(np.float64)),
+                                                        lw._dp(f.view(np.float64))))
 
     for _ in range(max(args.warmup, 3)):
-        s.set_state(z0, d0, f0)
-        s.run(seconds, 900.0)
+        reset_states()
+        ens.run(seconds)
     torch.cuda.synchronize()
 
-    # --- value: device time of K runs (state resident), L2 flushed between timed steps
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    # --- value: device time of K two-day runs, every member resident, L2 flushed between timed steps
+    dev_ms = 0.0
     launches0 = lw.launch_count()
     dist.barrier()
-    torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for k in range(args.steps):
+            reset_states()
             flush.zero_()
             torch.cuda.synchronize()
-            ev[k][0].record(stream)
-            s.run(seconds, 900.0)
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e0.record(torch.cuda.current_stream())
+            torch.cuda.current_stream().synchronize()
+            ens.run(seconds)
+            ends = []
+            for st in streams:
+                e = torch.cuda.Event(enable_timing=True)
+                e.record(st)
+                ends.append(e)
+            torch.cuda.synchronize()
+            dev_ms += max(e0.elapsed_time(e) for e in ends)
     launches = lw.launch_count() - launches0
+    groups = ens.groups()
     dist.barrier()
-    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
     dev_ms = dist.max(dev_ms)
-    sim_days = args.steps * seconds / 86400.0 * world
-    value = sim_days / (dev_ms * 1e-3)
+    member_days = ens.count * DAYS * world
+    value = member_days * args.steps / (dev_ms * 1e-3)
     ms_per_step = dev_ms / args.steps
 
-    # --- e2e: through the C ABI with host buffers (set_state from host, run, get_state to host), wall clock
-    zs, ds, fs = (torch.from_numpy(x.view(np.float64).copy()).pin_memory().numpy().view(np.complex128) for x in (z0, d0, f0))
+    # --- e2e: host buffers through the C ABI: every member's state in, run, every member's state out
+    pinned = [tuple(torch.from_numpy(x.view(np.float64).copy()).pin_memory().numpy() for x in st) for st in z0]
+    nbytes = sum(3 * x[0].nbytes for x in pinned)
     dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        s.set_state(zs, ds, fs)
-        s.run(seconds, 900.0)
-        zz, dd, ff = s.get_state()
+        for i, (z, d, f) in enumerate(pinned):
+            lw._check(lib.lmw_ensemble_member_set_state(ens._h, i, lw._dp(z), lw._dp(d), lw._dp(f)))
+        ens.run(seconds)
+        outs = [ens.member_state(i) for i in range(ens.count)]
     t_e2e = dist.max(time.perf_counter() - t0)
-    e2e = args.steps * seconds / 86400.0 * world / t_e2e
-    nbytes = 3 * s.nspec * 16
+    e2e = member_days * args.steps / t_e2e
 
-    # --- roofline: per-kernel launch times on the engine stream (live, CUDA events)
-    ms3 = (ctypes.c_double * 3)()
-    lw._check(lib.lmw_sphere_kernel_times(s._h, 900.0, 200, ms3))
-    nlat, nlon, ntri = s.nlat, s.nlon, (s.T + 1) * (s.T + 2) // 2
-    flops = [12.0 * nlat * ntri, 9 * (nlat // 2) * 5.0 * nlon * math.log2(nlon), 14.0 * nlat * ntri]
-    names = ["sph_synth (Legendre synthesis)", "sph_grid (FFTs + products)", "sph_analysis (Legendre analysis + RK4)"]
-    top = max(range(3), key=lambda i: ms3[i])
-    pk = ctypes.c_double()
-    lw._check(lib.lmw_fp64_peak(ctypes.byref(pk)))
-    achieved = flops[top] / (ms3[top] * 1e-3) / 1e12
-    stage_ms = sum(ms3)
-    roofline = {"bound": "fp64", "kernel": names[top], "achieved": achieved, "peak": pk.value, "unit": "TFLOP/s",
-                "frac": achieved / pk.value, "traffic": None,
-                "peak_source": "measured on this device by lmw_fp64_peak (dependent DFMA chains on every SM)",
-                "kernel_ms": {n: ms3[i] for i, n in enumerate(names)}, "flop_per_launch": flops[top],
-                "stage_kernel_ms_sum": stage_ms}
+    # --- roofline: per-group stage-kernel launch times (CUDA events on the group streams)
+    kt = []
+    for g, grp in enumerate(groups):
+        ms3 = (ctypes.c_double * 3)()
+        lw._check(lib.lmw_ensemble_kernel_times(ens._h, g, 50, ms3))
+        kt.append(list(ms3))
+    names = ["synthesis (split_syn)" if args.precision.startswith("split") else "synthesis (sph_synth)",
+             "grid: FFTs + products (split_grid)" if args.precision.startswith("split") else "grid: FFTs + products (sph_grid)",
+             "analysis + RK4 (split_ana)" if args.precision.startswith("split") else "analysis + RK4 (sph_analysis)"]
+    share = []
+    for g, grp in enumerate(groups):
+        for k in range(3):
+            share.append((kt[g][k] * 4 * grp["steps"], g, k))
+    _, gtop, ktop = max(share)
+    grp = groups[gtop]
+    T, Bm = grp["truncation"], grp["members"]
+    nlon = 4
+    while nlon < 3 * T + 1:
+        nlon *= 2
+    nlat, nh, M = nlon // 2, nlon // 4, T + 1
+    ntri = M * (M + 1) // 2
+    pieces = 3 if args.precision == "split6" else 2
+    # algorithmic bytes of one launch (each operand read once, each result written once)
+    if ktop == 1:
+        moved = Bm * nh * (M * 24 * 4 + 5 * 2 * M * 8) + Bm * 2 * nlat * nlon * 8 * 2
+        what = "E/O synthesis sums in (24 floats per latitude pair and m), folded analysis inputs out (FP32), f and h_s grids in (FP64)"
+    elif ktop == 0:
+        moved = 2 * pieces * nh * ntri * 2 + Bm * 12 * pieces * ntri * 2 + Bm * nh * M * 24 * 4
+        what = "BF16 P and H tables and state operands in, E/O sums out"
+    else:
+        moved = 2 * pieces * nh * ntri * 2 + Bm * nh * M * 10 * 8 + Bm * 3 * ntri * 16 * 3 + Bm * 12 * pieces * ntri * 2
+        what = "BF16 tables and folded inputs in, FP64 state/stage/accumulator updated, next synthesis operands out"
+    pk = peaks()
+    peak = pk.get("hbm_gbs", 6800.0)
+    achieved = moved / (kt[gtop][ktop] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": f"{names[ktop]} at T{T} x {Bm} members", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": moved, "bytes_counted": what,
+                "launch_ms": kt[gtop][ktop],
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth), of measured" if "hbm_gbs" in pk else "fallback 6.8 TB/s",
+                "stage_kernel_ms": {f"T{groups[g]['truncation']}": dict(zip(["synthesis", "grid", "analysis"], kt[g])) for g in range(len(groups))}}
 
-    # --- CPU baseline on rank 0 (bounded sample)
+    # --- accuracy of the headline precision: split vs FP64 on a subset (8 members of each truncation)
+    sub = [i for T in (21, 42, 85) for i in [j for j in range(len(tr)) if tr[j] == T][:8]]
+    errs = {}
+    if args.precision != "fp64":
+        f64 = lw.Ensemble([tr[i] for i in sub], [seeds[i] for i in sub], [heights[i] for i in sub], [omegas[i] for i in sub], **prec["fp64"])
+        red = lw.Ensemble([tr[i] for i in sub], [seeds[i] for i in sub], [heights[i] for i in sub], [omegas[i] for i in sub],
+                          **prec[args.precision])
+        f64.run(seconds)
+        red.run(seconds)
+        hl2, phi = [], []
+        for k, i in enumerate(sub):
+            T = tr[i]
+            nl = 4
+            while nl < 3 * T + 1:
+                nl *= 2
+            a, b_ = np.zeros((nl // 2, nl)), np.zeros((nl // 2, nl))
+            lw._check(lib.lmw_ensemble_member_grid(f64._h, k, 0, lw._dp(a), a.size))
+            lw._check(lib.lmw_ensemble_member_grid(red._h, k, 0, lw._dp(b_), b_.size))
+            hl2.append(float(np.sqrt(((b_ - a) ** 2).mean() / (a ** 2).mean())))
+            p64, pr = f64.member_state(k)[2], red.member_state(k)[2]
+            phi.append(float(np.abs(pr - p64).max() / np.abs(p64).max()))
+        errs = {"vs": "FP64 runs of the same 24 members (8 per truncation), 2 model days", "height_rel_l2_max": max(hl2),
+                "height_rel_l2_median": statistics.median(hl2), "phi_normrel_max": max(phi)}
+        f64.close()
+        red.close()
+
+    # --- the other configurations (rank 0)
+    workloads = []
+    if rank == 0:
+        workloads = other_workloads(lw, lib, args, ens)
+
+    # --- CPU baseline (rank 0, N = 1): the oracle on every host core
     cpu = None
     if rank == 0 and world == 1:
-        sys.path.insert(0, os.path.join(ROOT, "tests"))
-        from oracle_lib import build_oracle
-
-        build_oracle(with_ref=False)
-        cv, csec = cpu_sample(64)
-        cpu = {"value": cv, "unit": "sim-days/s", "cores": 1, "kind": "port",
-               "sample": f"64 RK4 steps of the T42 workload ({csec:.1f} s), oracle restatement of the reference, 1 thread"}
+        cores = os.cpu_count() or 1
+        steps = ensemble_member_steps(groups)
+        dts = {g["truncation"]: g["dt"] for g in groups}
+        rate, cost, wall = cpu_ensemble_rate(steps, {21: (6, dts[21]), 42: (3, dts[42]), 85: (1, dts[85])}, cores)
+        cpu = {"value": rate, "unit": "member-sim-days/s", "cores": cores, "kind": "port",
+               "sample": f"every one of {cores} cores timed 6 T21, 3 T42 and 1 T85 member-steps of the oracle ({wall:.1f} s); the "
+                         f"workload's member-step counts {steps} divided over the cores",
+               "member_step_seconds": {str(k): v for k, v in cost.items()}}
 
     clocks = clk.summary()
     if rank == 0:
         cfg = dict(WORKLOAD)
-        cfg["l2"] = "flushed (512 MB write) between timed steps"
-        cfg["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
-        line = {"metric": METRIC, "value": value, "unit": "sim-days/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        cfg["precision"] = args.precision
+        cfg["groups"] = groups
+        cfg["l2"] = "flushed (512 MB write) between timed steps; the working set of a step is L2-resident by design"
+        cfg["parallelism"] = f"replicas x{world} (independent ensembles, no collective)" if world > 1 else "single GPU"
+        line = {"metric": METRIC, "value": value, "unit": "member-sim-days/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "bf16x%d->f32 Legendre, f32 FFT, f64 state" % (3 if args.precision == "split3" else 6)
+                if args.precision.startswith("split") else args.precision,
                 "data": "synthetic (seeded balanced turbulence)", "config": cfg,
-                "e2e": {"value": e2e, "unit": "sim-days/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
-                "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks}
+                "e2e": {"value": e2e, "unit": "member-sim-days/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+                "gpu_launches": int(launches), "error": errs, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "workloads": workloads}
         print(json.dumps(line), flush=True)
+    ens.close()
     dist.close()
     return 0
+
+
+def other_workloads(lw, lib, args, ens):
+    """Configs 0, 1 and 2 and the ensemble in the other precisions (device-timed with synchronisation)."""
+    import numpy as np
+
+    out = []
+    if args.quick:
+        return out
+    # config 0: T42 plain FP64, 480 steps of 900 s (the parity configuration)
+    s = lw.Sphere(42, diffusion=nu4(42))
+    s.turbulence(1, 8000.0, 30.0, 21)
+    st = s.get_state()
+    s.run(480 * 900.0, 900.0)
+    ts = []
+    for _ in range(3):
+        s.set_state(*st)
+        t0 = time.perf_counter()
+        s.run(480 * 900.0, 900.0)
+        ts.append(time.perf_counter() - t0)
+    out.append({"config": "0: sphere T42 plain FP64, 480 x 900 s", "value": 5.0 / min(ts), "unit": "sim-days/s",
+                "parity": "within 1e-12 norm-relative of the reference's own run (tests/test_sphere_gpu.py)"})
+    s.close()
+    # config 1: beta-plane 1024 x 512, dt 60 s
+    p = lw.Plane(1024, 512, 1024 * 5000.0, 512 * 5000.0, f0=1e-4, beta=1.6e-11, gravity=9.81, depth=100.0)
+    p.jet(20.0, 1.0e5, 0.1, 1)
+    p.run(64 * 60.0, 60.0)
+    t0 = time.perf_counter()
+    p.run(1024 * 60.0, 60.0)
+    el = time.perf_counter() - t0
+    out.append({"config": "1: beta-plane 1024 x 512 C-grid FP64, dt 60 s", "value": 1024 * 60.0 / 86400.0 / el, "unit": "sim-days/s",
+                "parity": "bitwise identical to the reference (tests/test_plane_gpu.py)"})
+    p.close()
+    # config 2: T170 precision study, 2 model days
+    from lmweather_gb300.precision import study
+
+    res = study(170, 2.0)
+    out.append({"config": "2: sphere T170 precision study, 2 model days at 240 s", **res})
+    # the ensemble in the other precisions (one 2-day run each)
+    tr, seeds, heights, omegas = ensemble_specs(0)
+    for name, kw in (("fp64", dict(precision=lw.FP64)), ("fp32", dict(precision=lw.FP32)),
+                     ("split6", dict(precision=lw.SPLIT_BF16, split_terms=6)), ("split3", dict(precision=lw.SPLIT_BF16, split_terms=3))):
+        if name == args.precision:
+            continue
+        e = lw.Ensemble(tr, seeds, heights, omegas, **kw)
+        e.run(3600.0)
+        t0 = time.perf_counter()
+        e.run(DAYS * 86400.0)
+        el = time.perf_counter() - t0
+        out.append({"config": f"3: ensemble in {name}", "value": 1024 * DAYS / el, "unit": "member-sim-days/s"})
+        e.close()
+    return out
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="split3", choices=["split3", "split6", "fp32", "fp64"])
+    ap.add_argument("--quick", action="store_true", help="skip the other configurations")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -194,6 +194,10 @@ int lmw_ensemble_member_state(lmw_ensemble *e, int member, double *zeta, double 
 int lmw_ensemble_member_set_state(lmw_ensemble *e, int member, const double *zeta, const double *delta, const double *phi);
 int lmw_ensemble_member_diagnostics(lmw_ensemble *e, int member, double *out);
 int lmw_ensemble_member_grid(lmw_ensemble *e, int member, int which, double *out, size_t n);
+/* the CUDA stream of a truncation group, and its stage-kernel times as lmw_sphere_kernel_times (measurement
+ * hooks; the group's packed split operands are rebuilt before its next step) */
+int lmw_ensemble_stream(lmw_ensemble *e, int group, void **stream);
+int lmw_ensemble_kernel_times(lmw_ensemble *e, int group, int reps, double *ms);
 
 #ifdef __cplusplus
 }

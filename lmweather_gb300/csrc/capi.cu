@@ -398,6 +398,21 @@ int lmw_ensemble_member_diagnostics(lmw_ensemble *e, int member, double *out) {
     e->e->engine_of(member, &k).diagnostics(out, k);
   });
 }
+int lmw_ensemble_stream(lmw_ensemble *e, int group, void **stream) {
+  return ENS({
+    need(group >= 0 && group < static_cast<int>(e->e->groups.size()), "group index out of range");
+    *stream = static_cast<void *>(e->e->groups[group]->stream);
+  });
+}
+int lmw_ensemble_kernel_times(lmw_ensemble *e, int group, int reps, double *ms) {
+  return ENS({
+    need(group >= 0 && group < static_cast<int>(e->e->groups.size()), "group index out of range");
+    need(reps > 0, "reps must be positive");
+    lmw::SphereEngine &g = *e->e->groups[group];
+    const double dt = e->e->last_dt[group] > 0 ? e->e->last_dt[group] : 300.0;
+    g.kernel_times(dt, reps, ms);
+  });
+}
 int lmw_ensemble_member_grid(lmw_ensemble *e, int member, int which, double *out, size_t n) {
   return ENS({
     int k = 0;

@@ -561,6 +561,25 @@ static SphDev make_sph(const SphereEngine &e, const SphereTables &t) {
   return d;
 }
 
+// The dynamic shared-memory limit is a property of each kernel function, shared by every engine of the
+// process: raise it once to the device's opt-in maximum (engines of different truncations need different sizes).
+static void allow_max_shared_memory() {
+  static int done_for_device = -1;
+  int dev = 0, optin = 0;
+  LMW_CUDA(cudaGetDevice(&dev));
+  if (done_for_device == dev) return;
+  LMW_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const int dyn = optin - 2048;  // the kernels' static shared memory stays below 2 KB
+  LMW_CUDA(cudaFuncSetAttribute(sph_grid<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(sph_grid<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(sph_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(sph_grid_in, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_syn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_ana, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  done_for_device = dev;
+}
+
 static SphTab<double> tab64(const SphereTables &t) {
   return SphTab<double>{t.Ps.p, t.Hs.p, t.Pa.p, t.Ha.p, t.w.p, t.wd.p, t.r2om.p, t.kfac.p, t.lapl.p, t.tw.p};
 }
@@ -686,17 +705,12 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   if (p.precision == kSplitBF16) {
     split = new SplitPlan();
     build_split_plan(*split, h, B, p.split_terms);
-    LMW_CUDA(cudaFuncSetAttribute(split_syn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(split->smem_syn)));
-    LMW_CUDA(cudaFuncSetAttribute(split_ana, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(split->smem_ana)));
+
   }
   x0.zero(stream);
   hsgrid.zero(stream);
   refgrid.zero(stream);
-  const size_t smem = 5 * static_cast<size_t>(nlon) * sizeof(double2);
-  LMW_CUDA(cudaFuncSetAttribute(sph_grid<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  LMW_CUDA(cudaFuncSetAttribute(sph_grid<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  LMW_CUDA(cudaFuncSetAttribute(sph_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  LMW_CUDA(cudaFuncSetAttribute(sph_grid_in, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  allow_max_shared_memory();
   for (int b = 0; b < B; b++) set_axis_tilt(0, b);
   LMW_CUDA(cudaStreamSynchronize(stream));
 }

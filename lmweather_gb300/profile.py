@@ -34,8 +34,8 @@ def main() -> int:
             p.step(60.0)
         print(f"plane 1024x512: {args.steps} steps in {time.perf_counter() - t0:.4f} s")
         return 0
-    # steps inside the reference's RK4 stability limit for an 8000 m layer (316 s at T170, 159 s at T341)
-    T, dt = {"t42": (42, 900.0), "t85": (85, 450.0), "t170": (170, 300.0), "t341": (341, 150.0)}[args.case]
+    # steps inside the reference's RK4 stability limit for an 8000 m layer (316 s at T170 falling below 300 s on day 2; 159 s at T341)
+    T, dt = {"t42": (42, 900.0), "t85": (85, 450.0), "t170": (170, 240.0), "t341": (341, 150.0)}[args.case]
     nu = A ** 4 / (86400.0 * (T * (T + 1)) ** 2)
     s = lw.Sphere(T, diffusion=nu, precision=args.precision, max_truncation=max(T, 170))
     s.turbulence(1, 8000.0, 30.0, T // 2)
