@@ -3,8 +3,9 @@
     python -m lmweather_gb300.profile --case t42 --steps 4
     ncu --metrics gpu__time_duration.sum --clock-control none --csv python -m lmweather_gb300.profile --case t42 --steps 4
 
-Cases: t42 (config-0 sphere), t85, t170 (dt 300 s), t341 (dt 150 s), plane (1024 x 512 beta-plane jet, dt 60 s).
-One untimed warm-up step runs first.
+Cases: t42 (config-0 sphere), t85, t170 (dt 240 s), t341 (dt 150 s), plane (1024 x 512 beta-plane jet, dt 60 s),
+ens (an ensemble of --members spheres at --truncation, the groups of the benchmark ensemble). One untimed warm-up
+step runs first.
 """
 from __future__ import annotations
 
@@ -16,7 +17,10 @@ A = 6.37122e6
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="t42", choices=["t42", "t85", "t170", "t341", "plane"])
+    ap.add_argument("--case", default="t42", choices=["t42", "t85", "t170", "t341", "plane", "ens"])
+    ap.add_argument("--truncation", type=int, default=85)
+    ap.add_argument("--members", type=int, default=128)
+    ap.add_argument("--split-terms", type=int, default=3)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--precision", type=int, default=0)
     args = ap.parse_args()
@@ -34,10 +38,23 @@ def main() -> int:
             p.step(60.0)
         print(f"plane 1024x512: {args.steps} steps in {time.perf_counter() - t0:.4f} s")
         return 0
+    if args.case == "ens":
+        T, B = args.truncation, args.members
+        nu = A ** 4 / (86400.0 * (T * (T + 1)) ** 2)
+        s = lw.Sphere(T, diffusion=nu, precision=args.precision, members=B, split_terms=args.split_terms)
+        for b in range(B):
+            s.turbulence(b + 1, 5000.0 + 5000.0 * b / B, 30.0, T // 2, member=b)
+        dt = 0.9 * min(s.stable_dt(1.5, member=b) for b in range(B))
+        s.step(dt)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.step(dt)
+        print(f"ensemble T{T} x {B}: {args.steps} steps in {time.perf_counter() - t0:.4f} s")
+        return 0
     # steps inside the reference's RK4 stability limit for an 8000 m layer (316 s at T170 falling below 300 s on day 2; 159 s at T341)
     T, dt = {"t42": (42, 900.0), "t85": (85, 450.0), "t170": (170, 240.0), "t341": (341, 150.0)}[args.case]
     nu = A ** 4 / (86400.0 * (T * (T + 1)) ** 2)
-    s = lw.Sphere(T, diffusion=nu, precision=args.precision, max_truncation=max(T, 170))
+    s = lw.Sphere(T, diffusion=nu, precision=args.precision, max_truncation=max(T, 170), split_terms=args.split_terms)
     s.turbulence(1, 8000.0, 30.0, T // 2)
     s.step(dt)
     t0 = time.perf_counter()
