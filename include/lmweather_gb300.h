@@ -199,6 +199,74 @@ int lmw_ensemble_member_grid(lmw_ensemble *e, int member, int which, double *out
 int lmw_ensemble_stream(lmw_ensemble *e, int group, void **stream);
 int lmw_ensemble_kernel_times(lmw_ensemble *e, int group, int reps, double *ms);
 
+/* ---------------------------------------------------------------------------------------- learned surrogate */
+/* No counterpart in the reference (it has no learned component). A residual MLP advances the packed spectral
+ * state of a sphere by one window; plain RK4 (Sphere::run, cpp/sphere.cpp:457-484) generates its training data,
+ * checks it and takes members over. Every GEMM of training and inference runs on tcgen05 with BF16 operands and
+ * FP32 accumulation; weights are kept in FP32 for Adam. */
+
+typedef struct lmw_mlp lmw_mlp;
+/* four layers in_dim -> hidden -> hidden -> hidden -> out_dim, GELU after the first three; hidden and max_batch
+ * multiples of 128; weights ~ N(0, 1/fan_in) (the last layer scaled by last_layer_scale), biases zero */
+int lmw_mlp_create(int in_dim, int hidden, int out_dim, int max_batch, uint64_t seed, double last_layer_scale, lmw_mlp **out);
+int lmw_mlp_destroy(lmw_mlp *m);
+/* host row-major W [nout][nin] (logical sizes) and b [nout] of layer 0..3 */
+int lmw_mlp_set_layer(lmw_mlp *m, int layer, const float *w, const float *b);
+int lmw_mlp_get_layer(lmw_mlp *m, int layer, float *w, float *b);
+/* y [batch][out_dim] = net(x [batch][in_dim]); batch a multiple of 128 */
+int lmw_mlp_forward(lmw_mlp *m, const float *x, int batch, float *y);
+/* forward, loss = 1/(2 batch) sum_f mask_f (y - target)^2 and the gradients of every layer; mask [out_dim] holds
+ * per-output weights (0 masks an output; null: all 1) */
+int lmw_mlp_backward(lmw_mlp *m, const float *x, const float *target, const float *mask, int batch, double *loss);
+int lmw_mlp_get_grad(lmw_mlp *m, int layer, float *gw, float *gb);
+/* one Adam step from the last gradients */
+int lmw_mlp_adam(lmw_mlp *m, double lr, double beta1, double beta2, double eps);
+/* device time (ms) of one training step (forward, backward, Adam) and of one forward pass at this batch; the
+ * weights move (by a 1e-12 learning rate) */
+int lmw_mlp_time(lmw_mlp *m, int batch, int reps, double *train_ms, double *forward_ms);
+/* C [M][N] = bf16(A [M][K]) bf16(B [N][K])^T on the tensor cores (host buffers; M, N multiples of 128, K of 64) */
+int lmw_gemm_bf16(const float *a, const float *b, int M, int N, int K, float *c);
+
+typedef struct lmw_surrogate lmw_surrogate;
+/* surrogate of a sphere of this truncation over windows of window_seconds, trained on RK4 runs with step dt;
+ * hidden width as lmw_mlp_create; del^4 diffusion with a 1-day e-folding at n = T, as in the training runs */
+int lmw_surrogate_create(int truncation, int hidden, uint64_t seed, double window_seconds, double dt, double radius, double omega, double gravity,
+                         lmw_surrogate **out);
+int lmw_surrogate_destroy(lmw_surrogate *s);
+/* dims[0] = features (6 (T+1)(T+2)/2), dims[1] = padded features, dims[2] = hidden */
+int lmw_surrogate_dims(lmw_surrogate *s, int *dims);
+/* training data: `trajectories` members (seeds seed0 + i, balanced turbulence with nforce = T/2 and 30 m/s, mean
+ * heights uniform in [hmin, hmax] from seed0) each run for `windows` windows by RK4 in `precision`; snapshots kept
+ * on the device. seconds = wall time. */
+int lmw_surrogate_generate(lmw_surrogate *s, int trajectories, int windows, uint64_t seed0, double hmin, double hmax, int precision,
+                           double *seconds);
+/* Adam with a cosine learning rate from lr to lr_min over `epochs` epochs of the training trajectories (the last
+ * val_fraction of the trajectories are held out). loss_mode 0: mean square of the per-n normalised increments;
+ * 1: energy norm of the increment error (kinetic energy of the vorticity and divergence errors plus available
+ * potential energy of the Phi errors). stats: [0] final training loss per step, [1] validation
+ * per-window height error mean, [2] median, [3] 90th percentile, [4] max, [5] persistence error mean, [6] the
+ * untrained network's error mean, [7] seconds, [8] optimiser steps */
+int lmw_surrogate_fit(lmw_surrogate *s, int epochs, int batch, double lr, double lr_min, double val_fraction, uint64_t shuffle_seed,
+                      int loss_mode, double *stats);
+/* per-window relative L2 height errors of the network and of persistence on stored pairs [first, first + count) */
+int lmw_surrogate_evaluate(lmw_surrogate *s, int first, int count, double *err, double *persistence);
+/* one window of the network on host states [count][features] (packed spectral order of lmw_sphere_get_state's
+ * packed layout: field, then m, then n, real and imaginary parts), in place */
+int lmw_surrogate_advance(lmw_surrogate *s, int count, double *states);
+/* hybrid rollout of `members` held-out members over `windows` windows; RK4 (check_precision) recomputes every
+ * check_every-th window and takes members over whose relative L2 height error exceeds threshold. out[16]:
+ * [0] hybrid s, [1] network s, [2] check s, [3] takeover s, [4] members taken over, [5] checks, [6] median
+ * window error, [7] max, [8] fraction over threshold, [9] plain FP64 RK4 s for ref_windows windows, [10]
+ * ref_windows, [11] hybrid member-sim-days/s, [12] plain RK4 member-sim-days/s, [13] network-only
+ * member-sim-days/s, [14] mean window error, [15] 90th percentile. window_err (optional): [check][member],
+ * -1 where the member was already taken over. final_states (optional): [member][features] after the last window.
+ * Member j starts from balanced turbulence with seed seed0 + j and a mean height drawn from a 64-bit Mersenne
+ * Twister seeded with seed0 (uniform in [hmin, hmax]). */
+int lmw_surrogate_rollout(lmw_surrogate *s, int members, uint64_t seed0, double hmin, double hmax, int windows, int check_every, double threshold,
+                          int check_precision, int ref_windows, double *out, double *window_err, double *final_states);
+/* device time (ms) of one training step and of one forward pass of the surrogate's network */
+int lmw_surrogate_time(lmw_surrogate *s, int batch, int reps, double *train_ms, double *forward_ms);
+
 #ifdef __cplusplus
 }
 #endif

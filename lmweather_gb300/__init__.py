@@ -13,7 +13,7 @@ import os
 
 import numpy as np
 
-__all__ = ["Sphere", "Plane", "Ensemble", "DeviceError", "load_library", "library_path", "launch_count", "FP64", "FP32", "SPLIT_BF16"]
+__all__ = ["Sphere", "Plane", "Ensemble", "Mlp", "Surrogate", "gemm_bf16", "DeviceError", "load_library", "library_path", "launch_count", "FP64", "FP32", "SPLIT_BF16"]
 
 FP64, FP32, SPLIT_BF16 = 0, 1, 2
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -32,6 +32,7 @@ _D, _I, _P, _SZ, _U64 = C.c_double, C.c_int, C.c_void_p, C.c_size_t, C.c_uint64
 _DP = C.POINTER(C.c_double)
 _PP = C.POINTER(C.c_void_p)
 _IP = C.POINTER(C.c_int)
+_FP = C.POINTER(C.c_float)
 
 _SIGS = {
     "lmw_last_error": (C.c_char_p, []),
@@ -84,6 +85,25 @@ _SIGS = {
     "lmw_ensemble_member_set_state": (_I, [_P, _I, _DP, _DP, _DP]),
     "lmw_ensemble_member_diagnostics": (_I, [_P, _I, _DP]),
     "lmw_ensemble_member_grid": (_I, [_P, _I, _I, _DP, _SZ]),
+    "lmw_mlp_create": (_I, [_I, _I, _I, _I, _U64, _D, _PP]),
+    "lmw_mlp_destroy": (_I, [_P]),
+    "lmw_mlp_set_layer": (_I, [_P, _I, _FP, _FP]),
+    "lmw_mlp_get_layer": (_I, [_P, _I, _FP, _FP]),
+    "lmw_mlp_forward": (_I, [_P, _FP, _I, _FP]),
+    "lmw_mlp_backward": (_I, [_P, _FP, _FP, _FP, _I, _DP]),
+    "lmw_mlp_get_grad": (_I, [_P, _I, _FP, _FP]),
+    "lmw_mlp_adam": (_I, [_P, _D, _D, _D, _D]),
+    "lmw_mlp_time": (_I, [_P, _I, _I, _DP, _DP]),
+    "lmw_gemm_bf16": (_I, [_FP, _FP, _I, _I, _I, _FP]),
+    "lmw_surrogate_create": (_I, [_I, _I, _U64, _D, _D, _D, _D, _D, _PP]),
+    "lmw_surrogate_destroy": (_I, [_P]),
+    "lmw_surrogate_dims": (_I, [_P, _IP]),
+    "lmw_surrogate_generate": (_I, [_P, _I, _I, _U64, _D, _D, _I, _DP]),
+    "lmw_surrogate_fit": (_I, [_P, _I, _I, _D, _D, _D, _U64, _I, _DP]),
+    "lmw_surrogate_evaluate": (_I, [_P, _I, _I, _DP, _DP]),
+    "lmw_surrogate_advance": (_I, [_P, _I, _DP]),
+    "lmw_surrogate_rollout": (_I, [_P, _I, _U64, _D, _D, _I, _I, _D, _I, _I, _DP, _DP, _DP]),
+    "lmw_surrogate_time": (_I, [_P, _I, _I, _DP, _DP]),
 }
 
 
@@ -467,3 +487,159 @@ class Ensemble:
         out = np.zeros(8)
         _check(self._lib.lmw_ensemble_member_diagnostics(self._h, i, _dp(out)))
         return dict(zip(Sphere._DIAG, out.tolist()))
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fp(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(_FP)
+
+
+def gemm_bf16(a, b) -> np.ndarray:
+    """C = bf16(A) bf16(B)^T on the tensor cores (FP32 accumulation); A [M][K], B [N][K]."""
+    a, b = _f32(a), _f32(b)
+    M, K = a.shape
+    N = b.shape[0]
+    c = np.zeros((M, N), np.float32)
+    _check(load_library().lmw_gemm_bf16(_fp(a), _fp(b), M, N, K, _fp(c)))
+    return c
+
+
+class Mlp:
+    """Four-layer GELU MLP (in -> hidden -> hidden -> hidden -> out) trained with the engine's own tcgen05 BF16
+    kernels. No counterpart in the reference."""
+
+    def __init__(self, in_dim: int, hidden: int, out_dim: int, max_batch: int = 128, seed: int = 1, last_layer_scale: float = 1.0):
+        self._lib = load_library()
+        h = C.c_void_p()
+        _check(self._lib.lmw_mlp_create(in_dim, hidden, out_dim, max_batch, seed, last_layer_scale, C.byref(h)))
+        self._h = h
+        self.dims = (in_dim, hidden, out_dim)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lmw_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _shape(self, layer):
+        i, h, o = self.dims
+        return (h if layer < 3 else o), (i if layer == 0 else h)
+
+    def set_layer(self, layer: int, w, b):
+        w, b = _f32(w), _f32(b)
+        assert w.shape == self._shape(layer)
+        _check(self._lib.lmw_mlp_set_layer(self._h, layer, _fp(w), _fp(b)))
+
+    def get_layer(self, layer: int):
+        no, ni = self._shape(layer)
+        w, b = np.zeros((no, ni), np.float32), np.zeros(no, np.float32)
+        _check(self._lib.lmw_mlp_get_layer(self._h, layer, _fp(w), _fp(b)))
+        return w, b
+
+    def forward(self, x) -> np.ndarray:
+        x = _f32(x)
+        y = np.zeros((x.shape[0], self.dims[2]), np.float32)
+        _check(self._lib.lmw_mlp_forward(self._h, _fp(x), x.shape[0], _fp(y)))
+        return y
+
+    def backward(self, x, target, mask=None) -> float:
+        x, t = _f32(x), _f32(target)
+        m = None if mask is None else _f32(mask)
+        loss = _D()
+        _check(self._lib.lmw_mlp_backward(self._h, _fp(x), _fp(t), _fp(m), x.shape[0], C.byref(loss)))
+        return loss.value
+
+    def grad(self, layer: int):
+        no, ni = self._shape(layer)
+        gw, gb = np.zeros((no, ni), np.float32), np.zeros(no, np.float32)
+        _check(self._lib.lmw_mlp_get_grad(self._h, layer, _fp(gw), _fp(gb)))
+        return gw, gb
+
+    def adam(self, lr=3e-4, beta1=0.9, beta2=0.999, eps=1e-8):
+        _check(self._lib.lmw_mlp_adam(self._h, lr, beta1, beta2, eps))
+
+    def time(self, batch: int, reps: int = 10):
+        tr, fw = _D(), _D()
+        _check(self._lib.lmw_mlp_time(self._h, batch, reps, C.byref(tr), C.byref(fw)))
+        return tr.value, fw.value
+
+
+class Surrogate:
+    """Learned surrogate of the sphere: a residual MLP advancing the packed spectral state by one window, trained
+    on RK4 trajectories, checked and taken over by RK4 in hybrid rollouts. No counterpart in the reference."""
+
+    FIT = ("train_loss", "val_err_mean", "val_err_median", "val_err_p90", "val_err_max", "val_persist_mean", "val_untrained_mean",
+           "seconds", "steps")
+    ROLLOUT = ("hybrid_s", "network_s", "check_s", "takeover_s", "taken_over", "checks", "err_median", "err_max", "frac_over",
+               "rk4_s", "rk4_windows", "hybrid_rate", "rk4_rate", "network_rate", "err_mean", "err_p90")
+
+    def __init__(self, truncation: int = 42, hidden: int = 4096, seed: int = 1, window: float = 21600.0, dt: float = 900.0,
+                 radius=6.37122e6, omega=7.292e-5, gravity=9.80616):
+        self._lib = load_library()
+        h = C.c_void_p()
+        _check(self._lib.lmw_surrogate_create(truncation, hidden, seed, window, dt, radius, omega, gravity, C.byref(h)))
+        self._h = h
+        d = np.zeros(3, np.int32)
+        _check(self._lib.lmw_surrogate_dims(self._h, d.ctypes.data_as(_IP)))
+        self.features, self.padded, self.hidden = (int(v) for v in d)
+        self.truncation = truncation
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.lmw_surrogate_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def generate(self, trajectories: int, windows: int, seed0: int = 1, hmin=5000.0, hmax=10000.0, precision: int = FP64) -> float:
+        sec = _D()
+        _check(self._lib.lmw_surrogate_generate(self._h, trajectories, windows, seed0, hmin, hmax, precision, C.byref(sec)))
+        return sec.value
+
+    def fit(self, epochs: int, batch: int = 512, lr=3e-4, lr_min=3e-5, val_fraction=0.1, seed: int = 1, loss: str = "energy") -> dict:
+        st = np.zeros(9)
+        mode = {"normalised": 0, "energy": 1}[loss]
+        _check(self._lib.lmw_surrogate_fit(self._h, epochs, batch, lr, lr_min, val_fraction, seed, mode, _dp(st)))
+        return dict(zip(self.FIT, st.tolist()))
+
+    def evaluate(self, first: int, count: int):
+        e, p = np.zeros(count), np.zeros(count)
+        _check(self._lib.lmw_surrogate_evaluate(self._h, first, count, _dp(e), _dp(p)))
+        return e, p
+
+    def advance(self, states) -> np.ndarray:
+        st = np.array(states, dtype=np.float64, order="C", copy=True)
+        _check(self._lib.lmw_surrogate_advance(self._h, st.shape[0], _dp(st)))
+        return st
+
+    def rollout(self, members: int, seed0: int, windows: int, check_every: int = 4, threshold: float = 1e-3, check_precision: int = FP64,
+                ref_windows: int = 4, hmin=5000.0, hmax=10000.0, with_errors: bool = False, with_states: bool = False) -> dict:
+        out = np.zeros(16)
+        nchk = windows // check_every
+        we = np.zeros(max(1, nchk) * members) if with_errors else None
+        fs = np.zeros((members, self.features)) if with_states else None
+        _check(self._lib.lmw_surrogate_rollout(self._h, members, seed0, hmin, hmax, windows, check_every, threshold, check_precision,
+                                               ref_windows, _dp(out), None if we is None else _dp(we), None if fs is None else _dp(fs)))
+        r = dict(zip(self.ROLLOUT, out.tolist()))
+        if we is not None:
+            r["window_errors"] = we[: nchk * members].reshape(nchk, members)
+        if fs is not None:
+            r["final_states"] = fs
+        return r
+
+    def time(self, batch: int = 512, reps: int = 10):
+        tr, fw = _D(), _D()
+        _check(self._lib.lmw_surrogate_time(self._h, batch, reps, C.byref(tr), C.byref(fw)))
+        return tr.value, fw.value

@@ -30,6 +30,7 @@ UNITS = [
     ("capi.cu", []),
     ("peak.cu", []),
     ("tc_gemm.cu", []),
+    ("surrogate.cu", []),
     ("sphere_tables.cpp", []),
 ]
 

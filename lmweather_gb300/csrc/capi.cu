@@ -7,6 +7,7 @@
 #include "../../include/lmweather_gb300.h"
 #include "engine.h"
 #include "sphere_tables.h"
+#include "surrogate.h"
 #include "tc_gemm.h"
 
 struct lmw_sphere {
@@ -17,6 +18,12 @@ struct lmw_plane {
 };
 struct lmw_ensemble {
   lmw::EnsembleEngine *e;
+};
+struct lmw_mlp {
+  lmw::Mlp *m;
+};
+struct lmw_surrogate {
+  lmw::Surrogate *s;
 };
 
 namespace lmw {
@@ -420,6 +427,161 @@ int lmw_ensemble_member_grid(lmw_ensemble *e, int member, int which, double *out
     need(n == s.ngrid(), "grid size mismatch");
     s.grid(which, out, k);
   });
+}
+
+
+// ------------------------------------------------------------------------------------------------ surrogate
+int lmw_mlp_create(int in_dim, int hidden, int out_dim, int max_batch, uint64_t seed, double last_layer_scale, lmw_mlp **out) {
+  return guard([&] {
+    need(out != nullptr, "null output pointer");
+    *out = nullptr;
+    auto *h = new lmw_mlp{nullptr};
+    try {
+      h->m = new lmw::Mlp(in_dim, hidden, out_dim, max_batch, seed, last_layer_scale);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int lmw_mlp_destroy(lmw_mlp *m) {
+  return guard([&] {
+    if (!m) return;
+    delete m->m;
+    delete m;
+  });
+}
+#define MLP(m, ...)                                           \
+  guard([&] {                                                 \
+    need((m) != nullptr && (m)->m != nullptr, "null network"); \
+    __VA_ARGS__;                                              \
+  })
+int lmw_mlp_set_layer(lmw_mlp *m, int layer, const float *w, const float *b) {
+  return MLP(m, need(w != nullptr, "null weights"); m->m->set_layer(layer, w, b));
+}
+int lmw_mlp_get_layer(lmw_mlp *m, int layer, float *w, float *b) {
+  return MLP(m, need(w != nullptr, "null weights"); m->m->get_layer(layer, w, b));
+}
+int lmw_mlp_forward(lmw_mlp *m, const float *x, int batch, float *y) {
+  return MLP(m, need(x != nullptr && y != nullptr, "null buffer"); m->m->upload_input(x, batch); m->m->forward(batch); m->m->check_status();
+             m->m->download_output(y, batch));
+}
+int lmw_mlp_backward(lmw_mlp *m, const float *x, const float *target, const float *mask, int batch, double *loss) {
+  return MLP(m, need(x != nullptr && target != nullptr, "null buffer"); m->m->upload_input(x, batch); m->m->upload_target(target, mask, batch);
+             m->m->take_loss(); m->m->forward(batch); m->m->backward(batch); const double l = m->m->take_loss(); if (loss) *loss = l);
+}
+int lmw_mlp_get_grad(lmw_mlp *m, int layer, float *gw, float *gb) {
+  return MLP(m, need(gw != nullptr, "null gradient buffer"); m->m->get_grad(layer, gw, gb));
+}
+int lmw_mlp_adam(lmw_mlp *m, double lr, double beta1, double beta2, double eps) {
+  return MLP(m, m->m->adam(lr, beta1, beta2, eps); m->m->check_status());
+}
+int lmw_mlp_time(lmw_mlp *m, int batch, int reps, double *train_ms, double *forward_ms) {
+  return MLP(m, need(reps > 0, "reps must be positive"); const double a = m->m->time_train_step(batch, reps);
+             const double f = m->m->time_forward(batch, reps); if (train_ms) *train_ms = a; if (forward_ms) *forward_ms = f);
+}
+int lmw_gemm_bf16(const float *a, const float *b, int M, int N, int K, float *c) {
+  return guard([&] {
+    need(a != nullptr && b != nullptr && c != nullptr, "null buffer");
+    need(M > 0 && N > 0 && K > 0 && M % 128 == 0 && N % 128 == 0 && K % 64 == 0, "M, N must be multiples of 128 and K of 64");
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) throw lmw::DeviceError("no CUDA device");
+    cudaStream_t s;
+    LMW_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    lmw::DevBuf<__nv_bfloat16> A, B;
+    lmw::DevBuf<float> C;
+    lmw::DevBuf<int> err;
+    A.alloc(static_cast<size_t>(M) * K);
+    B.alloc(static_cast<size_t>(N) * K);
+    C.alloc(static_cast<size_t>(M) * N);
+    err.alloc(1);
+    err.zero(s);
+    lmw::to_blocked(a, M, K, M, K, A.p, s);
+    lmw::to_blocked(b, N, K, N, K, B.p, s);
+    lmw::mlp_gemm_f32(A.p, B.p, M, N, K, C.p, N, nullptr, err.p, s);
+    int e = 0;
+    LMW_CUDA(cudaMemcpyAsync(c, C.p, C.bytes(), cudaMemcpyDeviceToHost, s));
+    LMW_CUDA(cudaMemcpyAsync(&e, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LMW_CUDA(cudaStreamSynchronize(s));
+    cudaStreamDestroy(s);
+    if (e) throw lmw::RuntimeError("the tensor-core GEMM timed out waiting on its pipeline");
+  });
+}
+
+int lmw_surrogate_create(int truncation, int hidden, uint64_t seed, double window_seconds, double dt, double radius, double omega, double gravity,
+                         lmw_surrogate **out) {
+  return guard([&] {
+    need(out != nullptr, "null output pointer");
+    *out = nullptr;
+    auto *h = new lmw_surrogate{nullptr};
+    try {
+      h->s = new lmw::Surrogate(truncation, hidden, seed, window_seconds, dt, radius, omega, gravity);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int lmw_surrogate_destroy(lmw_surrogate *s) {
+  return guard([&] {
+    if (!s) return;
+    delete s->s;
+    delete s;
+  });
+}
+#define SUR(s, ...)                                             \
+  guard([&] {                                                   \
+    need((s) != nullptr && (s)->s != nullptr, "null surrogate"); \
+    __VA_ARGS__;                                                \
+  })
+int lmw_surrogate_dims(lmw_surrogate *s, int *dims) {
+  return SUR(s, need(dims != nullptr, "null buffer"); dims[0] = s->s->nfeat; dims[1] = s->s->net->dim[0]; dims[2] = s->s->net->hidden);
+}
+int lmw_surrogate_generate(lmw_surrogate *s, int trajectories, int windows, uint64_t seed0, double hmin, double hmax, int precision,
+                           double *seconds) {
+  return SUR(s, need(precision >= 0 && precision <= 2, "precision must be 0 (FP64), 1 (FP32) or 2 (split BF16)");
+             s->s->generate(trajectories, windows, seed0, hmin, hmax, precision, 1024); if (seconds) *seconds = s->s->gen_seconds);
+}
+int lmw_surrogate_fit(lmw_surrogate *s, int epochs, int batch, double lr, double lr_min, double val_fraction, uint64_t shuffle_seed,
+                      int loss_mode, double *stats) {
+  return SUR(s, need(loss_mode == 0 || loss_mode == 1, "loss mode must be 0 or 1");
+             if (s->s->loss_mode != loss_mode) s->s->have_norm = false; s->s->loss_mode = loss_mode;
+             const lmw::SurrogateStats st = s->s->fit(epochs, batch, lr, lr_min, val_fraction, shuffle_seed); if (stats) {
+    stats[0] = st.train_loss;
+    stats[1] = st.val_err_mean;
+    stats[2] = st.val_err_median;
+    stats[3] = st.val_err_p90;
+    stats[4] = st.val_err_max;
+    stats[5] = st.val_persist_mean;
+    stats[6] = st.val_untrained_mean;
+    stats[7] = st.seconds;
+    stats[8] = st.steps;
+  });
+}
+int lmw_surrogate_evaluate(lmw_surrogate *s, int first, int count, double *err, double *persistence) {
+  return SUR(s, need(err != nullptr && persistence != nullptr, "null buffer"); need(count > 0, "count must be positive"); std::vector<double> e, p;
+             s->s->evaluate(first, first + count, e, p); std::copy(e.begin(), e.end(), err); std::copy(p.begin(), p.end(), persistence));
+}
+int lmw_surrogate_advance(lmw_surrogate *s, int count, double *states) {
+  return SUR(s, need(states != nullptr, "null buffer"); need(count > 0, "count must be positive"); lmw::DevBuf<double> d;
+             const size_t n = static_cast<size_t>(count) * s->s->nfeat; d.alloc(n);
+             LMW_CUDA(cudaMemcpyAsync(d.p, states, n * sizeof(double), cudaMemcpyHostToDevice, s->s->stream));
+             s->s->advance_states(d.p, count, nullptr);
+             LMW_CUDA(cudaMemcpyAsync(states, d.p, n * sizeof(double), cudaMemcpyDeviceToHost, s->s->stream));
+             LMW_CUDA(cudaStreamSynchronize(s->s->stream)); s->s->net->check_status());
+}
+int lmw_surrogate_rollout(lmw_surrogate *s, int members, uint64_t seed0, double hmin, double hmax, int windows, int check_every, double threshold,
+                          int check_precision, int ref_windows, double *out, double *window_err, double *final_states) {
+  return SUR(s, need(out != nullptr, "null buffer"); need(check_precision >= 0 && check_precision <= 2, "check precision must be 0, 1 or 2");
+             s->s->rollout(members, seed0, hmin, hmax, windows, check_every, threshold, check_precision, ref_windows, out, window_err,
+                           final_states));
+}
+int lmw_surrogate_time(lmw_surrogate *s, int batch, int reps, double *train_ms, double *forward_ms) {
+  return SUR(s, need(reps > 0, "reps must be positive"); need(s->s->ntraj > 0, "no training data yet");
+             const double a = s->s->net->time_train_step(batch, reps); const double f = s->s->net->time_forward(batch, reps);
+             if (train_ms) *train_ms = a; if (forward_ms) *forward_ms = f);
 }
 
 }  // extern "C"

@@ -128,6 +128,8 @@ class SphereEngine {
   void enqueue_step(double dt);
   // device pointer of the packed spectral state [member][field][tri] complex128 (FP64 state accumulation)
   double *device_state() { return x0.p; }
+  // to be called after the state was written through device_state() (repacks the split operands)
+  void state_written() { split_packed = false; }
   uint64_t launches_per_step() const { return launches_step; }
   // average duration (ms) per launch of each stage kernel class over `reps` launches (CUDA events on the
   // engine stream): out[0] synthesis, out[1] grid (FFTs + products), out[2] analysis + RK4 update. x0 unchanged.
@@ -153,9 +155,13 @@ class SphereEngine {
   std::vector<char> has_orog;
   double filt_dt = -1;
   uint64_t launches_step = 0;
-  cudaGraphExec_t graph = nullptr;
-  double graph_dt = 0;
-  int graph_steps = 0;
+  // captured step chunks, keyed by (dt, steps); the guard-sized chunk and a run's remainder chunk both stay
+  struct ChunkGraph {
+    double dt;
+    int steps;
+    cudaGraphExec_t exec;
+  };
+  std::vector<ChunkGraph> graphs;
   void upload_filter(double dt);
   void launch_stage(int stage, double dt);
   void launch_chunk(double dt, int steps);

@@ -716,7 +716,7 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
 }
 
 SphereEngine::~SphereEngine() {
-  if (graph) cudaGraphExecDestroy(graph);
+  for (const ChunkGraph &cg : graphs) cudaGraphExecDestroy(cg.exec);
   if (stream) {
     cudaStreamSynchronize(stream);
     cudaStreamDestroy(stream);
@@ -1101,9 +1101,14 @@ void SphereEngine::launch_chunk(double dt, int steps) {
   if (steps <= 0) return;
   upload_filter(dt);
   ensure_packed();
-  if (!graph || graph_dt != dt || graph_steps != steps) {
-    if (graph) cudaGraphExecDestroy(graph);
-    graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  for (const ChunkGraph &cg : graphs)
+    if (cg.dt == dt && cg.steps == steps) exec = cg.exec;
+  if (!exec) {
+    if (graphs.size() >= 4) {
+      cudaGraphExecDestroy(graphs.front().exec);
+      graphs.erase(graphs.begin());
+    }
     cudaGraph_t g;
     uint64_t before = g_launches;
     LMW_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -1111,12 +1116,11 @@ void SphereEngine::launch_chunk(double dt, int steps) {
       for (int k = 0; k < 4; k++) launch_stage(k, dt);
     LMW_CUDA(cudaStreamEndCapture(stream, &g));
     g_launches = before;
-    LMW_CUDA(cudaGraphInstantiate(&graph, g, 0));
+    LMW_CUDA(cudaGraphInstantiate(&exec, g, 0));
     cudaGraphDestroy(g);
-    graph_dt = dt;
-    graph_steps = steps;
+    graphs.push_back({dt, steps, exec});
   }
-  LMW_CUDA(cudaGraphLaunch(graph, stream));
+  LMW_CUDA(cudaGraphLaunch(exec, stream));
   g_launches += 12ull * steps;
 }
 
@@ -1209,7 +1213,7 @@ bool SphereEngine::advance(RunPlan &rp) {
   if (rp.i >= rp.n) return false;
   int64_t next = std::min<int64_t>(rp.n - 1, rp.i | 63);
   int chunk = static_cast<int>(next - rp.i + 1);
-  if (chunk == 64) launch_chunk(rp.h, 64);
+  if (chunk >= 4) launch_chunk(rp.h, chunk);
   else for (int s = 0; s < chunk; s++) enqueue_step(rp.h);
   for (int s = 0; s < chunk; s++)
     for (int b = 0; b < B; b++) t[b] += rp.h;
