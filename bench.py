@@ -459,6 +459,8 @@ def other_workloads(lw, lib, args, ens):
 
     res = study(170, 2.0)
     out.append({"config": "2: sphere T170 precision study, 2 model days at 240 s", **res})
+    # config 4: the learned surrogate at T42 (bounded: see surrogate_workload)
+    out.append(surrogate_workload(lw))
     # the ensemble in the other precisions (one 2-day run each)
     tr, seeds, heights, omegas = ensemble_specs(0)
     for name, kw in (("fp64", dict(precision=lw.FP64)), ("fp32", dict(precision=lw.FP32)),
@@ -473,6 +475,36 @@ def other_workloads(lw, lib, args, ens):
         out.append({"config": f"3: ensemble in {name}", "value": 1024 * DAYS / el, "unit": "member-sim-days/s"})
         e.close()
     return out
+
+
+def surrogate_workload(lw, trajectories=1024, windows=80, epochs=60, members=1024, rollout_windows=16):
+    """Config 4 within the benchmark's time: the T42 residual MLP (5676 -> 4096 x 3 -> 5676, GELU, BF16 on tcgen05)
+    trained on `trajectories` x `windows` solver pairs (split-precision RK4 data, FP64 state; 6-hour windows of
+    900 s steps, mean height 8000 m), then a hybrid rollout of `members` held-out members over `rollout_windows`
+    windows with FP64 RK4 checking every 4th window and taking over above 1e-3. The full configuration (204,800
+    pairs, 100 epochs, 80 rollout windows) is python -m lmweather_gb300.surrogate_study."""
+    t0 = time.perf_counter()
+    sur = lw.Surrogate(42, hidden=4096, seed=1)
+    gen_s = sur.generate(trajectories, windows, seed0=1_000_000, hmin=8000.0, hmax=8000.0, precision=lw.SPLIT_BF16)
+    fit = sur.fit(epochs, batch=512, lr=3e-4, lr_min=3e-5, val_fraction=0.1, seed=1, loss="energy")
+    train_ms, fwd_ms = sur.time(512, 10)
+    _, fwd1024 = sur.time(1024, 10)
+    r = sur.rollout(members, seed0=9_000_001, windows=rollout_windows, check_every=4, threshold=1e-3, check_precision=lw.FP64,
+                    ref_windows=4, hmin=8000.0, hmax=8000.0)
+    sur.close()
+    fl = 2 * (5676 * 4096 * 2 + 4096 * 4096 * 2)
+    return {"config": "4: learned surrogate T42, 6-hour windows (bounded training)",
+            "unit": "member-sim-days/s",
+            "network_only": members * 0.25 / (fwd1024 * 1e-3), "hybrid": r["hybrid_rate"], "plain_rk4_fp64": r["rk4_rate"],
+            "speedup_network_vs_rk4": members * 0.25 / (fwd1024 * 1e-3) / r["rk4_rate"],
+            "speedup_hybrid_vs_rk4": r["hybrid_rate"] / r["rk4_rate"],
+            "window_height_error": {"validation_mean": fit["val_err_mean"], "validation_p90": fit["val_err_p90"],
+                                    "persistence_mean": fit["val_persist_mean"], "untrained_mean": fit["val_untrained_mean"],
+                                    "rollout_checks_median": r["err_median"], "rollout_checks_max": r["err_max"]},
+            "taken_over": r["taken_over"], "threshold": 1e-3, "members": members, "rollout_windows": rollout_windows,
+            "pairs": trajectories * windows, "epochs": epochs, "generate_s": gen_s, "train_s": fit["seconds"],
+            "train_step_ms_batch512": train_ms, "forward_ms_batch1024": fwd1024,
+            "forward_tflops_batch1024": fl * 1024 / (fwd1024 * 1e-3) / 1e12, "wall_s": time.perf_counter() - t0}
 
 
 def main():

@@ -264,6 +264,14 @@ int lmw_surrogate_advance(lmw_surrogate *s, int count, double *states);
  * Twister seeded with seed0 (uniform in [hmin, hmax]). */
 int lmw_surrogate_rollout(lmw_surrogate *s, int members, uint64_t seed0, double hmin, double hmax, int windows, int check_every, double threshold,
                           int check_precision, int ref_windows, double *out, double *window_err, double *final_states);
+/* a fresh network (weights from seed) and optimiser; the training data stay */
+int lmw_surrogate_reset(lmw_surrogate *s, uint64_t seed);
+/* adaptive gradient clipping of training: the global gradient norm is held to at most ratio times its running
+ * mean (default 2; 0 switches clipping off) */
+int lmw_surrogate_set_clip(lmw_surrogate *s, double ratio);
+/* per epoch of the last fit: mean training loss and mean global gradient norm per step (count = epochs; at most
+ * max values written) */
+int lmw_surrogate_history(lmw_surrogate *s, int max, double *loss, double *grad_norm, int *count);
 /* device time (ms) of one training step and of one forward pass of the surrogate's network */
 int lmw_surrogate_time(lmw_surrogate *s, int batch, int reps, double *train_ms, double *forward_ms);
 

@@ -104,6 +104,9 @@ _SIGS = {
     "lmw_surrogate_advance": (_I, [_P, _I, _DP]),
     "lmw_surrogate_rollout": (_I, [_P, _I, _U64, _D, _D, _I, _I, _D, _I, _I, _DP, _DP, _DP]),
     "lmw_surrogate_time": (_I, [_P, _I, _I, _DP, _DP]),
+    "lmw_surrogate_reset": (_I, [_P, _U64]),
+    "lmw_surrogate_set_clip": (_I, [_P, _D]),
+    "lmw_surrogate_history": (_I, [_P, _I, _DP, _DP, _IP]),
 }
 
 
@@ -613,6 +616,19 @@ class Surrogate:
         mode = {"normalised": 0, "energy": 1}[loss]
         _check(self._lib.lmw_surrogate_fit(self._h, epochs, batch, lr, lr_min, val_fraction, seed, mode, _dp(st)))
         return dict(zip(self.FIT, st.tolist()))
+
+    def reset(self, seed: int):
+        _check(self._lib.lmw_surrogate_reset(self._h, seed))
+
+    def set_clip(self, ratio: float):
+        _check(self._lib.lmw_surrogate_set_clip(self._h, ratio))
+
+    def history(self):
+        n = _I()
+        _check(self._lib.lmw_surrogate_history(self._h, 0, None, None, C.byref(n)))
+        loss, gn = np.zeros(max(1, n.value)), np.zeros(max(1, n.value))
+        _check(self._lib.lmw_surrogate_history(self._h, n.value, _dp(loss), _dp(gn), C.byref(n)))
+        return loss[: n.value], gn[: n.value]
 
     def evaluate(self, first: int, count: int):
         e, p = np.zeros(count), np.zeros(count)

@@ -585,3 +585,17 @@ int lmw_surrogate_time(lmw_surrogate *s, int batch, int reps, double *train_ms, 
 }
 
 }  // extern "C"
+
+extern "C" {
+int lmw_surrogate_reset(lmw_surrogate *s, uint64_t seed) { return SUR(s, s->s->reset(seed)); }
+int lmw_surrogate_set_clip(lmw_surrogate *s, double ratio) {
+  return SUR(s, need(ratio >= 0, "the clipping ratio must not be negative"); s->s->clip_ratio = ratio);
+}
+int lmw_surrogate_history(lmw_surrogate *s, int max, double *loss, double *grad_norm, int *count) {
+  return SUR(s, need(count != nullptr, "null buffer"); const int n = static_cast<int>(s->s->hist_loss.size()); *count = n;
+             for (int i = 0; i < n && i < max; i++) {
+               if (loss) loss[i] = s->s->hist_loss[i];
+               if (grad_norm) grad_norm[i] = s->s->hist_gnorm[i];
+             });
+}
+}  // extern "C"

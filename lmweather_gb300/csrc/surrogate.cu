@@ -227,13 +227,20 @@ void transpose(const bf16 *in, bf16 *out, int R, int C, cudaStream_t s) {
   g_launches += 1;
 }
 
-// bias gradient: column sums of a blocked [rows][N] gradient
-__global__ void colsum_blocked(const bf16 *__restrict__ gsrc, float *__restrict__ out, int rows, int N) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
+// bias gradient: row sums of the transposed gradient (blocked [N][batch]), one warp per row reading 16-byte
+// chunks; a fixed reduction order (deterministic)
+__global__ void rowsum_blocked(const bf16 *__restrict__ gt, float *__restrict__ out, int N, int batch) {
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (row >= N) return;
   float s = 0.0f;
-  for (int b = 0; b < rows; b++) s += __bfloat162float(gsrc[boff(b, n, N)]);
-  out[n] = s;
+  for (int k8 = lane * 8; k8 < batch; k8 += 256) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(gt + boff(row, k8, batch));
+    const bf16 *p = reinterpret_cast<const bf16 *>(&v);
+#pragma unroll
+    for (int j = 0; j < 8; j++) s += __bfloat162float(p[j]);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[row] = s;
 }
 
 // loss 1/(2 batch) sum_f w_f (y - t)^2 with per-output weights w (0 masks an output) and its gradient
@@ -272,6 +279,7 @@ struct AdamArgs {
   int nout, nin;
   float lr, b1, b2, eps, c1, c2;
   int update;
+  const float *scale;  // gradient scale from the clipping kernel (null: 1)
 };
 
 // Adam on a 64 x 64 tile of W [nout][nin] (FP32 row-major), then the BF16 blocked copies W [nout][nin] and
@@ -284,7 +292,7 @@ __global__ void adam_tile(AdamArgs a) {
     const long i = static_cast<long>(n0 + rr) * a.nin + k0 + cc;
     float w = a.w[i];
     if (a.update) {
-      const float g = a.g[i];
+      const float g = a.g[i] * (a.scale ? *a.scale : 1.0f);
       const float m = a.b1 * a.m[i] + (1.0f - a.b1) * g;
       const float v = a.b2 * a.v[i] + (1.0f - a.b2) * g * g;
       w -= a.lr * (m * a.c1) / (sqrtf(v * a.c2) + a.eps);
@@ -308,15 +316,46 @@ __global__ void adam_tile(AdamArgs a) {
   }
 }
 
-__global__ void adam_vec(float *w, float *m, float *v, const float *g, int n, float lr, float b1, float b2, float eps, float c1, float c2) {
+__global__ void adam_vec(float *w, float *m, float *v, const float *g, int n, float lr, float b1, float b2, float eps, float c1, float c2,
+                         const float *scale) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float gi = g[i];
+  const float gi = g[i] * (scale ? *scale : 1.0f);
   const float mi = b1 * m[i] + (1.0f - b1) * gi;
   const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
   w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
   m[i] = mi;
   v[i] = vi;
+}
+
+// sum of squares of n values into *acc (double)
+__global__ void sumsq(const float *__restrict__ x, long n, double *acc) {
+  double s = 0;
+  for (long i = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; i < n; i += static_cast<long>(gridDim.x) * blockDim.x) {
+    const double v = x[i];
+    s += v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); w++) t += red[w];
+    atomicAdd(acc, t);
+  }
+}
+
+// adaptive clipping: the global gradient norm is held to at most `ratio` times its running mean (the first
+// steps set the mean); clip[0] = scale for this step, clip[1] = running mean, clip[2] += this step's norm
+__global__ void clip_scale(const double *gnorm2, float *scale, double *clip, float ratio) {
+  const double norm = sqrt(*gnorm2);
+  double mean = clip[1];
+  if (!(mean > 0)) mean = norm;
+  const double cap = ratio * mean;
+  scale[0] = norm > cap && norm > 0 ? static_cast<float>(cap / norm) : 1.0f;
+  clip[1] = 0.99 * mean + 0.01 * (norm < cap ? norm : cap);
+  clip[2] += norm;
 }
 
 __device__ __forceinline__ uint64_t splitmix(uint64_t x) {
@@ -428,6 +467,10 @@ Mlp::Mlp(int in_dim, int hidden_, int out_dim, int max_batch_, uint64_t seed, do
   }
   loss_acc.alloc(1);
   loss_acc.zero(stream);
+  gnorm2.alloc(1);
+  gscale.alloc(1);
+  clip.alloc(3);
+  clip.zero(stream);
   err.alloc(1);
   err.zero(stream);
   LMW_CUDA(cudaStreamSynchronize(stream));
@@ -442,7 +485,7 @@ Mlp::~Mlp() {
 
 void Mlp::publish(int l) {
   Layer &Ly = L[l];
-  AdamArgs a{Ly.w.p, Ly.m.p, Ly.v.p, Ly.gw.p, Ly.wb.p, Ly.wt.p, Ly.nout, Ly.nin, 0, 0, 0, 0, 0, 0, 0};
+  AdamArgs a{Ly.w.p, Ly.m.p, Ly.v.p, Ly.gw.p, Ly.wb.p, Ly.wt.p, Ly.nout, Ly.nin, 0, 0, 0, 0, 0, 0, 0, nullptr};
   adam_tile<<<dim3(Ly.nin / 64, Ly.nout / 64), 256, 0, stream>>>(a);
   LMW_LAUNCH_CHECK();
   g_launches += 1;
@@ -571,7 +614,7 @@ void Mlp::backward(int batch) {
     gw.ldc = win;
     gw.err = err.p;
     gemm(gw, stream);
-    colsum_blocked<<<(wcur + 255) / 256, 256, 0, stream>>>(gcur, L[l].gb.p, batch, wcur);
+    rowsum_blocked<<<(wcur + 7) / 8, 256, 0, stream>>>(tgrad.p, L[l].gb.p, wcur, batch);
     LMW_LAUNCH_CHECK();
     g_launches += 1;
     if (l == 0) break;
@@ -592,20 +635,45 @@ void Mlp::backward(int batch) {
   }
 }
 
-void Mlp::adam(double lr, double beta1, double beta2, double eps) {
+void Mlp::adam(double lr, double beta1, double beta2, double eps, double clip_ratio) {
   adam_t += 1;
   const float c1 = static_cast<float>(1.0 / (1.0 - std::pow(beta1, adam_t))), c2 = static_cast<float>(1.0 / (1.0 - std::pow(beta2, adam_t)));
+  const float *scale = nullptr;
+  if (clip_ratio > 0) {
+    LMW_CUDA(cudaMemsetAsync(gnorm2.p, 0, sizeof(double), stream));
+    for (int l = 0; l < NL; l++) {
+      const long nw = static_cast<long>(L[l].nin) * L[l].nout;
+      sumsq<<<grid_for(nw, 256), 256, 0, stream>>>(L[l].gw.p, nw, gnorm2.p);
+      LMW_LAUNCH_CHECK();
+      sumsq<<<grid_for(L[l].nout, 256), 256, 0, stream>>>(L[l].gb.p, L[l].nout, gnorm2.p);
+      LMW_LAUNCH_CHECK();
+    }
+    clip_scale<<<1, 1, 0, stream>>>(gnorm2.p, gscale.p, clip.p, static_cast<float>(clip_ratio));
+    LMW_LAUNCH_CHECK();
+    g_launches += 2 * NL + 1;
+    scale = gscale.p;
+  }
   for (int l = 0; l < NL; l++) {
     Layer &Ly = L[l];
     AdamArgs a{Ly.w.p, Ly.m.p, Ly.v.p, Ly.gw.p, Ly.wb.p, Ly.wt.p, Ly.nout, Ly.nin, static_cast<float>(lr), static_cast<float>(beta1), static_cast<float>(beta2),
-               static_cast<float>(eps), c1, c2, 1};
+               static_cast<float>(eps), c1, c2, 1, scale};
     adam_tile<<<dim3(Ly.nin / 64, Ly.nout / 64), 256, 0, stream>>>(a);
     LMW_LAUNCH_CHECK();
     adam_vec<<<(Ly.nout + 255) / 256, 256, 0, stream>>>(Ly.b.p, Ly.mb.p, Ly.vb.p, Ly.gb.p, Ly.nout, static_cast<float>(lr), static_cast<float>(beta1),
-                                                       static_cast<float>(beta2), static_cast<float>(eps), c1, c2);
+                                                       static_cast<float>(beta2), static_cast<float>(eps), c1, c2, scale);
     LMW_LAUNCH_CHECK();
     g_launches += 2;
   }
+}
+
+double Mlp::take_grad_norm_sum() {
+  double v[3] = {0, 0, 0};
+  LMW_CUDA(cudaMemcpyAsync(v, clip.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  const double zero = 0;
+  LMW_CUDA(cudaMemcpyAsync(clip.p + 2, &zero, sizeof(double), cudaMemcpyHostToDevice, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  return v[2];
 }
 
 void Mlp::check_status() {
@@ -639,7 +707,7 @@ double Mlp::time_train_step(int batch, int reps) {
   for (int r = 0; r < reps; r++) {
     forward(batch);
     backward(batch);
-    adam(1e-12, 0.9, 0.999, 1e-8);
+    adam(1e-12, 0.9, 0.999, 1e-8, 2.0);
   }
   LMW_CUDA(cudaEventRecord(e1, stream));
   LMW_CUDA(cudaEventSynchronize(e1));
@@ -817,15 +885,17 @@ __global__ void apply_increment(double *__restrict__ st, int count, int nfeat, i
   }
 }
 
-// relative L2 height error between two FP64 state sets, per member
-__global__ void state_errors(const double *__restrict__ a, const double *__restrict__ r, int nfeat, const float *__restrict__ cw, double *__restrict__ err) {
+// relative L2 height error between member amap[b] of a (b without a map) and member b of r
+__global__ void state_errors(const double *__restrict__ a, const int *__restrict__ amap, const double *__restrict__ r, int nfeat,
+                             const float *__restrict__ cw, double *__restrict__ err) {
   __shared__ double red[32];
   const int b = blockIdx.x;
+  const long ra = amap ? amap[b] : b;
   double num = 0, den = 0;
   for (int f = threadIdx.x; f < nfeat; f += blockDim.x) {
     const double c = cw[f];
     if (c == 0.0) continue;
-    const double x = a[static_cast<long>(b) * nfeat + f], t = r[static_cast<long>(b) * nfeat + f];
+    const double x = a[ra * nfeat + f], t = r[static_cast<long>(b) * nfeat + f];
     num += c * (x - t) * (x - t);
     den += c * t * t;
   }
@@ -858,7 +928,7 @@ double seconds_since(std::chrono::steady_clock::time_point t0) {
 
 }  // namespace
 
-Surrogate::Surrogate(int truncation, int hidden, uint64_t seed, double window_seconds, double dt_, double radius, double omega, double gravity)
+Surrogate::Surrogate(int truncation, int hidden_, uint64_t seed, double window_seconds, double dt_, double radius, double omega, double gravity)
     : T(truncation), window(window_seconds), dt(dt_) {
   if (truncation < 4 || truncation > 170) throw InvalidArgument("truncation must be between 4 and 170");
   if (!(window_seconds > 0) || !(dt_ > 0)) throw InvalidArgument("the window and the step must be positive");
@@ -872,6 +942,7 @@ Surrogate::Surrogate(int truncation, int hidden, uint64_t seed, double window_se
   cfg.diffusion = std::pow(radius, 4) / (86400.0 * std::pow(T * (T + 1.0), 2));
   cfg.precision = kFP64;
   cfg.max_truncation = 170;
+  hidden = hidden_;
   net = std::make_unique<Mlp>(nfeat, hidden, nfeat, 1024, seed, 0.1);
   stream = net->stream;
   const int dp = net->dim[0];
@@ -891,6 +962,15 @@ Surrogate::Surrogate(int truncation, int hidden, uint64_t seed, double window_se
 }
 
 Surrogate::~Surrogate() = default;
+
+void Surrogate::reset(uint64_t seed) {
+  net.reset();
+  net = std::make_unique<Mlp>(nfeat, hidden, nfeat, 1024, seed, 0.1);
+  stream = net->stream;
+  have_norm = false;
+  hist_loss.clear();
+  hist_gnorm.clear();
+}
 
 void Surrogate::generate(int trajectories, int windows, uint64_t seed0, double hmin, double hmax, int precision, int batch_members) {
   if (trajectories < 2 || windows < 1) throw InvalidArgument("need at least two trajectories and one window");
@@ -1065,6 +1145,10 @@ SurrogateStats Surrogate::fit(int epochs, int batch, double lr, double lr_min, d
   st.val_persist_mean = std::accumulate(p.begin(), p.end(), 0.0) / p.size();
   const int spe = ntrain / batch;
   const long total = static_cast<long>(epochs) * spe;
+  // linear warm-up of the learning rate over the first 5 % of the steps (at most 1000)
+  const long warmup = std::max<long>(1, std::min<long>(1000, total / 20));
+  hist_loss.clear();
+  hist_gnorm.clear();
   DevBuf<int> order;
   order.alloc(ntrain);
   std::vector<int> ids(ntrain);
@@ -1078,16 +1162,20 @@ SurrogateStats Surrogate::fit(int epochs, int batch, double lr, double lr_min, d
     std::shuffle(ids.begin(), ids.end(), rng);
     LMW_CUDA(cudaMemcpyAsync(order.p, ids.data(), ntrain * sizeof(int), cudaMemcpyHostToDevice, stream));
     for (int s = 0; s < spe; s++, step++) {
-      const double lr_t = lr_min + 0.5 * (lr - lr_min) * (1.0 + std::cos(M_PI * static_cast<double>(step) / static_cast<double>(std::max<long>(1, total))));
+      const double warm = std::min(1.0, static_cast<double>(step + 1) / static_cast<double>(warmup));
+      const double lr_t =
+          warm * (lr_min + 0.5 * (lr - lr_min) * (1.0 + std::cos(M_PI * static_cast<double>(step) / static_cast<double>(std::max<long>(1, total)))));
       gather_pairs<<<batch, 256, 0, stream>>>(snaps.p, order.p + static_cast<long>(s) * batch, nwin, dp, nfeat, mu.p, sig.p, sigd.p, outmask.p, net->x0.p,
                                               net->target.p);
       LMW_LAUNCH_CHECK();
       net->forward(batch);
       net->backward(batch);
-      net->adam(lr_t, 0.9, 0.999, 1e-8);
+      net->adam(lr_t, 0.9, 0.999, 1e-8, clip_ratio);
     }
-    // the mean loss per step of this epoch (synchronises once per epoch)
+    // the mean loss and gradient norm per step of this epoch (synchronises once per epoch)
     last_loss = net->take_loss() / spe;
+    hist_loss.push_back(last_loss);
+    hist_gnorm.push_back(net->take_grad_norm_sum() / spe);
     // keep the host's copy of the order alive until the stream has consumed it
     LMW_CUDA(cudaStreamSynchronize(stream));
   }
@@ -1148,9 +1236,20 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
   rs_mode.alloc(members);
   rs_mode.zero(stream);
   LMW_CUDA(cudaMemcpyAsync(rs_state.p, init.device_state(), nst * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-  SphereConfig cc = c;
-  cc.precision = check_precision;
-  SphereEngine check(cc);
+  // the network's members are checked by one batched RK4 engine of exactly their count (rebuilt when
+  // takeovers change the count)
+  std::vector<int> netids(members);
+  std::iota(netids.begin(), netids.end(), 0);
+  DevBuf<int> netids_d;
+  std::unique_ptr<SphereEngine> check;
+  auto make_check = [&](int k) {
+    SphereConfig cc = c;
+    cc.members = k;
+    cc.precision = check_precision;
+    check = std::make_unique<SphereEngine>(cc);
+    netids_d.alloc(k);
+    LMW_CUDA(cudaMemcpyAsync(netids_d.p, netids.data(), k * sizeof(int), cudaMemcpyHostToDevice, check->stream));
+  };
   struct Group {
     std::unique_ptr<SphereEngine> e;
     DevBuf<int> ids;
@@ -1165,11 +1264,19 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
   cudaEvent_t e0, e1;
   LMW_CUDA(cudaEventCreate(&e0));
   LMW_CUDA(cudaEventCreate(&e1));
+  // one window of plain RK4 at the training step, or at the engine's own stable step where a state the network
+  // produced has become too fast for it (the reference's stable_dt(1.5), cpp/sphere.cpp:438-447)
+  const double rk4_limit = 2.0 * std::sqrt(2.0);
+  auto rk4_window = [&](SphereEngine &e) {
+    const double use = dt <= e.stable_dt_all(rk4_limit) ? dt : 0.0;
+    e.run(window, use);
+  };
   // warm the check engine's graphs and the network (not timed)
   LMW_CUDA(cudaStreamSynchronize(stream));
-  LMW_CUDA(cudaMemcpyAsync(check.device_state(), rs_state.p, nst * sizeof(double), cudaMemcpyDeviceToDevice, check.stream));
-  check.state_written();
-  check.run(window, dt);
+  make_check(members);
+  copy_members_launch(rs_state.p, netids_d.p, check->device_state(), nullptr, members, nfeat, check->stream);
+  check->state_written();
+  check->run(window, dt);
   net->forward(std::min(net->max_batch, (members + 127) / 128 * 128));
   LMW_CUDA(cudaDeviceSynchronize());
   double t_net = 0, t_check = 0, t_take = 0;
@@ -1179,11 +1286,11 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
     const bool is_check = (w % check_every) == check_every - 1;
     if (is_check) LMW_CUDA(cudaMemcpyAsync(rs_start.p, rs_state.p, nst * sizeof(double), cudaMemcpyDeviceToDevice, stream));
     LMW_CUDA(cudaEventRecord(e0, stream));
-    advance_states(rs_state.p, members, rs_mode.p);
+    if (!netids.empty()) advance_states(rs_state.p, members, rs_mode.p);
     LMW_CUDA(cudaEventRecord(e1, stream));
     if (!groups.empty()) {
       const auto tg = std::chrono::steady_clock::now();
-      for (auto &g : groups) g->e->run(window, dt);
+      for (auto &g : groups) rk4_window(*g->e);
       for (auto &g : groups) {
         LMW_CUDA(cudaStreamSynchronize(g->e->stream));
         copy_members_launch(g->e->device_state(), nullptr, rs_state.p, g->ids.p, g->n, nfeat, stream);
@@ -1196,46 +1303,60 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
     LMW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     t_net += ms * 1e-3;
     if (!is_check) continue;
-    const auto tc0 = std::chrono::steady_clock::now();
-    LMW_CUDA(cudaStreamSynchronize(stream));
-    LMW_CUDA(cudaMemcpyAsync(check.device_state(), rs_start.p, nst * sizeof(double), cudaMemcpyDeviceToDevice, check.stream));
-    check.state_written();
-    check.run(window, dt);
-    state_errors<<<members, 256, 0, check.stream>>>(rs_state.p, check.device_state(), nfeat, cw.p, merr.p);
-    LMW_LAUNCH_CHECK();
-    LMW_CUDA(cudaMemcpyAsync(herr.data(), merr.p, members * sizeof(double), cudaMemcpyDeviceToHost, check.stream));
-    LMW_CUDA(cudaStreamSynchronize(check.stream));
-    std::vector<int> fresh;
-    for (int b = 0; b < members; b++) {
-      double ev = -1.0;
-      if (!mode[b]) {
-        ev = herr[b];
-        checked.push_back(ev);
-        if (!(ev <= threshold)) {
-          over++;
-          fresh.push_back(b);
-          mode[b] = 1;
-        }
-      }
-      if (window_err) window_err[static_cast<size_t>(nchecks) * members + b] = ev;
-    }
+    if (window_err)
+      for (int b = 0; b < members; b++) window_err[static_cast<size_t>(nchecks) * members + b] = -1.0;
     nchecks++;
+    if (netids.empty()) continue;
+    const auto tc0 = std::chrono::steady_clock::now();
+    const int k = static_cast<int>(netids.size());
+    if (check->B != k) make_check(k);
+    LMW_CUDA(cudaStreamSynchronize(stream));
+    copy_members_launch(rs_start.p, netids_d.p, check->device_state(), nullptr, k, nfeat, check->stream);
+    check->state_written();
+    rk4_window(*check);
+    state_errors<<<k, 256, 0, check->stream>>>(rs_state.p, netids_d.p, check->device_state(), nfeat, cw.p, merr.p);
+    LMW_LAUNCH_CHECK();
+    LMW_CUDA(cudaMemcpyAsync(herr.data(), merr.p, k * sizeof(double), cudaMemcpyDeviceToHost, check->stream));
+    LMW_CUDA(cudaStreamSynchronize(check->stream));
+    std::vector<int> fresh, rows, keep;
+    for (int i = 0; i < k; i++) {
+      const int b = netids[i];
+      const double ev = herr[i];
+      checked.push_back(ev);
+      if (window_err) window_err[static_cast<size_t>(nchecks - 1) * members + b] = ev;
+      if (!(ev <= threshold)) {
+        over++;
+        fresh.push_back(b);
+        rows.push_back(i);
+        mode[b] = 1;
+      } else {
+        keep.push_back(b);
+      }
+    }
     if (!fresh.empty()) {
       auto g = std::make_unique<Group>();
       g->n = static_cast<int>(fresh.size());
       g->ids.alloc(g->n);
-      LMW_CUDA(cudaMemcpyAsync(g->ids.p, fresh.data(), g->n * sizeof(int), cudaMemcpyHostToDevice, check.stream));
+      DevBuf<int> rows_d;
+      rows_d.alloc(g->n);
+      LMW_CUDA(cudaMemcpyAsync(g->ids.p, fresh.data(), g->n * sizeof(int), cudaMemcpyHostToDevice, check->stream));
+      LMW_CUDA(cudaMemcpyAsync(rows_d.p, rows.data(), g->n * sizeof(int), cudaMemcpyHostToDevice, check->stream));
       SphereConfig gc = cfg;
       gc.members = g->n;
       gc.precision = kFP64;
       g->e = std::make_unique<SphereEngine>(gc);
-      copy_members_launch(check.device_state(), g->ids.p, g->e->device_state(), nullptr, g->n, nfeat, check.stream);
-      copy_members_launch(check.device_state(), g->ids.p, rs_state.p, g->ids.p, g->n, nfeat, check.stream);
-      LMW_CUDA(cudaStreamSynchronize(check.stream));
+      copy_members_launch(check->device_state(), rows_d.p, g->e->device_state(), nullptr, g->n, nfeat, check->stream);
+      copy_members_launch(check->device_state(), rows_d.p, rs_state.p, g->ids.p, g->n, nfeat, check->stream);
+      LMW_CUDA(cudaStreamSynchronize(check->stream));
       g->e->state_written();
       taken += g->n;
       groups.push_back(std::move(g));
       LMW_CUDA(cudaMemcpyAsync(rs_mode.p, mode.data(), members * sizeof(int), cudaMemcpyHostToDevice, stream));
+      netids = keep;
+      if (!netids.empty()) {
+        LMW_CUDA(cudaStreamSynchronize(check->stream));
+        make_check(static_cast<int>(netids.size()));
+      }
     }
     t_check += seconds_since(tc0);
   }

@@ -40,7 +40,8 @@ class Mlp {
   DevBuf<__nv_bfloat16> dy, dz[2];       // output gradient [batch][dim4], hidden gradients [batch][h]
   DevBuf<float> y;                       // output, row-major [batch][dim4]
   DevBuf<float> target, mask;            // row-major [batch][dim4]; per output feature 1 or 0
-  DevBuf<double> loss_acc;
+  DevBuf<double> loss_acc, gnorm2, clip;
+  DevBuf<float> gscale;
   DevBuf<int> err;
 
   // host row-major weights of the logical size [nout][nin] and biases [nout]
@@ -54,7 +55,9 @@ class Mlp {
 
   void forward(int batch);                 // x0 -> y
   void backward(int batch);                // y, target, mask -> gradients; loss accumulated into loss_acc
-  void adam(double lr, double beta1, double beta2, double eps);
+  // clip_ratio > 0: the global gradient norm is clipped to clip_ratio times its running mean (on the device)
+  void adam(double lr, double beta1, double beta2, double eps, double clip_ratio = 0.0);
+  double take_grad_norm_sum();             // synchronises; the summed gradient norms since the last call
   double take_loss();                      // synchronises; returns and clears the accumulated loss
   void check_status();
   // average duration (ms) of one forward + backward + Adam step at this batch (CUDA events on the stream)
@@ -81,8 +84,10 @@ class Surrogate {
  public:
   Surrogate(int truncation, int hidden, uint64_t seed, double window_seconds, double dt, double radius, double omega, double gravity);
   ~Surrogate();
-  int T = 42, ntri = 0, nfeat = 0;
+  int T = 42, ntri = 0, nfeat = 0, hidden = 4096;
   double window = 21600.0, dt = 900.0;
+  double clip_ratio = 2.0;  // adaptive gradient clipping of training (0: off)
+  std::vector<double> hist_loss, hist_gnorm;  // per epoch of the last fit: mean loss and gradient norm per step
   SphereConfig cfg;
   std::unique_ptr<Mlp> net;
   cudaStream_t stream = nullptr;
@@ -99,6 +104,7 @@ class Surrogate {
   // (kinetic energy of the vorticity/divergence errors plus available potential energy of the Phi errors)
   int loss_mode = 1;
 
+  void reset(uint64_t seed);  // a fresh network and optimiser (the data stay)
   void generate(int trajectories, int windows, uint64_t seed0, double hmin, double hmax, int precision, int batch_members);
   void normalise(int ntrain_trajectories);
   SurrogateStats fit(int epochs, int batch, double lr, double lr_min, double val_fraction, uint64_t shuffle_seed);

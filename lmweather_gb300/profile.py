@@ -17,7 +17,8 @@ A = 6.37122e6
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="t42", choices=["t42", "t85", "t170", "t341", "plane", "ens"])
+    ap.add_argument("--case", default="t42", choices=["t42", "t85", "t170", "t341", "plane", "ens", "mlp"])
+    ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--truncation", type=int, default=85)
     ap.add_argument("--members", type=int, default=128)
     ap.add_argument("--split-terms", type=int, default=3)
@@ -37,6 +38,21 @@ def main() -> int:
         for _ in range(args.steps):
             p.step(60.0)
         print(f"plane 1024x512: {args.steps} steps in {time.perf_counter() - t0:.4f} s")
+        return 0
+    if args.case == "mlp":
+        # the surrogate's network at its T42 size: training steps (forward, backward, Adam) on a random batch
+        import numpy as np
+
+        rng = np.random.default_rng(1)
+        net = lw.Mlp(5676, 4096, 5676, max_batch=args.batch, seed=1, last_layer_scale=0.1)
+        x = rng.standard_normal((args.batch, 5676)).astype(np.float32)
+        t = 0.1 * rng.standard_normal((args.batch, 5676)).astype(np.float32)
+        net.backward(x, t)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            net.backward(x, t)
+            net.adam(1e-4)
+        print(f"mlp 5676-4096x3-5676 batch {args.batch}: {args.steps} training steps in {time.perf_counter() - t0:.4f} s")
         return 0
     if args.case == "ens":
         T, B = args.truncation, args.members
