@@ -1019,7 +1019,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   sa.filt = filt;
   if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
   if (which < 0 || which == 1)
-    split_grid<<<dim3(d.nh, B), GRID_THREADS, 5 * static_cast<size_t>(d.nlon) * sizeof(float2), stream>>>(d, t, sd, fgrid, hsgrid);
+    split_grid<<<dim3(d.nh / sp.jb, B), GRID_THREADS, 5 * static_cast<size_t>(sp.jb) * d.nlon * sizeof(float2), stream>>>(d, t, sd, fgrid, hsgrid);
   if (which < 0 || which == 2)
     split_ana<<<dim3(d.M, 2, sp.ntiles), SPLIT_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
 }

@@ -9,12 +9,12 @@
 //              parity s per CTA); A w_d, B w_d, U Phi w_d, (Phi + E) w at fold parity s against P and A w_d,
 //              B w_d, V Phi w_d at parity 1 - s against H.
 // Three launches per stage:
-//   split_syn     per (m, member tile): H then P through a two-stage pipeline of bulk asynchronous copies
-//                 (cp.async.bulk, the TMA engine) into shared memory, MMAs by one thread, accumulators read back
-//                 with tcgen05.ld and written as per-latitude E/O sums for the grid kernel.
-//   split_grid    per (latitude pair, member): Fourier coefficients from the E/O sums, FP32 FFTs and products
-//                 (the same arithmetic as sph_grid<float>), then the folded analysis inputs written straight into
-//                 the analysis operands as BF16 pieces.
+//   split_syn     per (m, member tile): H then P through a pipeline of bulk asynchronous copies (cp.async.bulk,
+//                 the TMA engine) into shared memory, MMAs by one thread, accumulators read back with tcgen05.ld
+//                 and combined into the Fourier coefficients of U, V, zeta and Phi at both mirror latitudes.
+//   split_grid    per (block of latitude pairs, member): FP32 FFTs and products (the same arithmetic as
+//                 sph_grid<float>), then the folded analysis inputs, stored m-major so that the analysis reads
+//                 them with unit stride.
 //   split_ana     per (m, parity, member tile): H then P as above; the epilogue forms the tendencies in FP32,
 //                 applies the RK4 stage update to the FP64 state, and packs the next stage's synthesis operands.
 // All operands live in global memory already in the MMA's canonical K-major core-matrix order, in 64-wide K
@@ -35,7 +35,10 @@ constexpr int SPLIT_BK = 64;
 constexpr int SPLIT_MAX_STAGES = 4;
 constexpr int SPLIT_MARGIN = 16384;  // an M = 128 MMA reads 16 KB past an A base: every A base keeps 16 KB of allocation
 constexpr int SPLIT_THREADS = 128;
-constexpr int SPLIT_NQ = 24;  // per (member, jh, m): E and O of 8 P sums and 4 H sums
+constexpr int SPLIT_NQ = 16;  // per (member, jh, m): U, V, zeta, Phi Fourier coefficients at the southern and northern latitude
+constexpr int SPLIT_JB_MAX = 4;  // latitude pairs per grid CTA
+// dynamic shared memory per CTA when two CTAs share an SM (228 KB per SM, 1 KB reserved per CTA, static barriers)
+constexpr size_t SPLIT_HALF_SM = 115456;
 
 struct SplitPlan {
   int pieces = 2, terms = 3;
@@ -51,17 +54,18 @@ struct SplitPlan {
   DevBuf<long> tS_off_d, tA_off_d, aS_off_d, aSH_off_d;
   size_t smem_syn = 0, smem_ana = 0;
   int ns_syn = 2, ns_ana = 2;  // pipeline stages
+  int jb = 1;                 // latitude pairs per grid CTA
 };
 
 struct SplitDev {
-  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH;
+  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb;
   const int *ke16, *kp64, *ra16;
   const long *tS_off, *tA_off, *aS_off, *aSH_off;
   long tS_size, tA_size, aSP_size, aSH_size, aAP_size, aAH_size;
   const __nv_bfloat16 *tS_P, *tS_H, *tA_P, *tA_H;
   __nv_bfloat16 *aS_P, *aS_H, *aA_P, *aA_H;
-  float *dsyn;
-  float2 *fold;  // [member][jh][slot][parity][m], as the FP32 grid kernel writes it
+  float *dsyn;   // [member][jh][m][16]: U, V, zeta, Phi at the southern then the northern latitude (complex)
+  float2 *fold;  // [m][slot][parity][member][jh]: folded analysis inputs
   int *err;
 };
 
@@ -354,51 +358,54 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
       }
     }
     __syncthreads();
-    // dsyn[member][jh][m][slot]: slot q (P E), 8 + q (P O) for q < 8; 16 + q (H E), 20 + q (H O) for q < 4
-    for (int e = threadIdx.x; e < mt * wcols * SPLIT_NQ; e += blockDim.x) {
-      const int slot = e % SPLIT_NQ, rest = e / SPLIT_NQ, i = rest % wcols, ml = rest / wcols;
-      const int jh = cb + i;
-      if (jh >= d.nh) continue;
-      float v;
-      if (slot < 16) v = tile_s[(((slot < 8) ? 2 : 3) * rows + ml * 8 + (slot & 7)) * 33 + i];
-      else v = tile_s[(((slot < 20) ? 0 : 1) * rows + ml * 4 + ((slot - 16) & 3)) * 33 + i];
-      sd.dsyn[((static_cast<long>(tile * sd.nbt + ml) * d.nh + jh) * d.M + m) * SPLIT_NQ + slot] = v;
+    // Fourier coefficients of both mirror latitudes: P sums south E + O, north E - O; H sums (opposite parity)
+    // south E + O, north O - E; U = (i m chi P - psi H) / a, V = (i m psi P + chi H) / a (cpp/sphere.cpp:200-201)
+    const float mm = static_cast<float>(m), ia = static_cast<float>(1.0 / d.a);
+    for (int e = threadIdx.x; e < mt * 32; e += blockDim.x) {
+      const int i = e & 31, ml = e >> 5, jh = cb + i;
+      if (i >= wcols || jh >= d.nh) continue;
+      const float *PE = tile_s + (2 * rows + ml * 8) * 33 + i, *PO = tile_s + (3 * rows + ml * 8) * 33 + i;
+      const float *HE = tile_s + (0 * rows + ml * 4) * 33 + i, *HO = tile_s + (1 * rows + ml * 4) * 33 + i;
+      float4 *dst = reinterpret_cast<float4 *>(sd.dsyn + ((static_cast<long>(tile * sd.nbt + ml) * d.nh + jh) * d.M + m) * SPLIT_NQ);
+#pragma unroll
+      for (int side = 0; side < 2; side++) {
+        float pv[8], hv[4];
+#pragma unroll
+        for (int q = 0; q < 8; q++) pv[q] = side == 0 ? PE[q * 33] + PO[q * 33] : PE[q * 33] - PO[q * 33];
+#pragma unroll
+        for (int q = 0; q < 4; q++) hv[q] = side == 0 ? HE[q * 33] + HO[q * 33] : HO[q * 33] - HE[q * 33];
+        const float2 U = cscale(csub(imul(make_float2(pv[2], pv[3]), mm), make_float2(hv[0], hv[1])), ia);
+        const float2 V = cscale(cadd(imul(make_float2(pv[0], pv[1]), mm), make_float2(hv[2], hv[3])), ia);
+        dst[2 * side] = make_float4(U.x, U.y, V.x, V.y);
+        dst[2 * side + 1] = make_float4(pv[4], pv[5], pv[6], pv[7]);
+      }
     }
   }
   split_teardown(tmem, ncols);
 }
 
 // ------------------------------------------------------------------------------------------- grid (FP32)
-// grid: (nh, B). E/O sums -> Fourier coefficients -> FFTs and products -> folded values -> analysis operands
+// grid: (nh / jb, B). Fourier records of jb latitude pairs -> FFTs and products -> folded values, written to
+// fold[m][slot][parity][member][jh] (jb consecutive latitudes per store)
 __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
                                                            const double *__restrict__ hsgrid) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  float2 *sm = reinterpret_cast<float2 *>(smraw);
-  const int b = blockIdx.y, jh = blockIdx.x;
-  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
-  for (int e = threadIdx.x; e < 4 * n; e += blockDim.x) sm[e] = make_float2(0, 0);
+  float2 *sm = reinterpret_cast<float2 *>(smraw);  // rows f * jb + p: U, V, zeta, Phi and the fifth product of pair p
+  const int JB = sd.jb, B = gridDim.y;
+  const int b = blockIdx.y, jh0 = blockIdx.x * JB;
+  const int n = d.nlon, M = d.M;
+  for (int e = threadIdx.x; e < 4 * JB * n; e += blockDim.x) sm[e] = make_float2(0, 0);
   __syncthreads();
-  const float *src = sd.dsyn + (static_cast<long>(b) * d.nh + jh) * d.M * SPLIT_NQ;
-  const float ia = static_cast<float>(1.0 / d.a);
-  for (int m = threadIdx.x; m < d.M; m += blockDim.x) {
-    const float *v = src + static_cast<long>(m) * SPLIT_NQ;
-    float2 X[2][4];
-    for (int side = 0; side < 2; side++) {
-      float r[12];
+  for (int e = threadIdx.x; e < JB * M; e += blockDim.x) {
+    const int pr = e / M, m = e - pr * M;
+    const float4 *rec = reinterpret_cast<const float4 *>(sd.dsyn + ((static_cast<long>(b) * d.nh + jh0 + pr) * M + m) * SPLIT_NQ);
+    const float4 s0 = rec[0], s1 = rec[1], n0 = rec[2], n1 = rec[3];
+    const float2 A[4] = {make_float2(s0.x, s0.y), make_float2(s0.z, s0.w), make_float2(s1.x, s1.y), make_float2(s1.z, s1.w)};
+    const float2 C[4] = {make_float2(n0.x, n0.y), make_float2(n0.z, n0.w), make_float2(n1.x, n1.y), make_float2(n1.z, n1.w)};
 #pragma unroll
-      for (int q = 0; q < 8; q++) r[q] = side == 0 ? v[q] + v[8 + q] : v[q] - v[8 + q];          // P sums
-#pragma unroll
-      for (int q = 0; q < 4; q++) r[8 + q] = side == 0 ? v[16 + q] + v[20 + q] : v[20 + q] - v[16 + q];  // H sums
-      const float mm = static_cast<float>(m);
-      const float2 SP = make_float2(r[0], r[1]), SC = make_float2(r[2], r[3]), HP = make_float2(r[8], r[9]), HC = make_float2(r[10], r[11]);
-      X[side][0] = cscale(csub(imul(SC, mm), HP), ia);  // cpp/sphere.cpp:200-201
-      X[side][1] = cscale(cadd(imul(SP, mm), HC), ia);
-      X[side][2] = make_float2(r[4], r[5]);
-      X[side][3] = make_float2(r[6], r[7]);
-    }
     for (int f = 0; f < 4; f++) {
-      const float2 a = X[0][f], c = X[1][f];
-      float2 *row = sm + static_cast<size_t>(f) * n;
+      const float2 a = A[f], c = C[f];
+      float2 *row = sm + static_cast<size_t>(f * JB + pr) * n;
       if (m == 0) row[0] = make_float2(a.x, c.x);
       else {
         row[bitrev(m, d.logn)] = make_float2(a.x - c.y, a.y + c.x);
@@ -407,12 +414,17 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
     }
   }
   __syncthreads();
-  fft_inverse_dit(sm, 4, n, d.logn, t.tw);
-  const float r2om = t.r2om[js], g = static_cast<float>(d.g);
-  const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
-  const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
-  float2 *rU = sm, *rV = sm + n, *rZ = sm + 2 * n, *rP = sm + 3 * n, *rE = sm + 4 * n;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+  fft_inverse_dit(sm, 4 * JB, n, d.logn, t.tw);
+  const float g = static_cast<float>(d.g);
+  for (int e = threadIdx.x; e < JB * n; e += blockDim.x) {
+    const int pr = e >> d.logn, k = e & (n - 1);
+    const int js = jh0 + pr, jn = d.nlat - 1 - js;
+    const float r2om = t.r2om[js];
+    const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
+    const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
+    float2 *rU = sm + static_cast<size_t>(0 * JB + pr) * n, *rV = sm + static_cast<size_t>(1 * JB + pr) * n;
+    float2 *rZ = sm + static_cast<size_t>(2 * JB + pr) * n, *rP = sm + static_cast<size_t>(3 * JB + pr) * n;
+    float2 *rE = sm + static_cast<size_t>(4 * JB + pr) * n;
     const float2 U = rU[k], V = rV[k], Z = rZ[k], P = rP[k];
     float2 A, Bv, UP, VP, PE;
     {
@@ -428,29 +440,42 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
     rU[k] = A; rV[k] = Bv; rZ[k] = UP; rP[k] = VP; rE[k] = PE;
   }
   __syncthreads();
-  fft_forward_dif(sm, 5, n, d.logn, t.tw);
-  const float inv = 1.0f / n, wd = t.wd[js], wj = t.w[js];
-  for (int e = threadIdx.x; e < d.M; e += blockDim.x) {
-    const int m = e;
-    float2 fold[5][2];
-    for (int r = 0; r < 5; r++) {
-      const float2 *row = sm + static_cast<size_t>(r) * n;
-      const float2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
-      const float hinv = 0.5f * inv;
-      float2 Xs = cscale(cadd(Ym, Yc), hinv);
-      const float2 tt = csub(Ym, Yc);
-      float2 Xn = make_float2(hinv * tt.y, -hinv * tt.x);
-      const float wt = r < 4 ? wd : wj;
-      Xs = cscale(Xs, wt);
-      Xn = cscale(Xn, wt);
-      fold[r][0] = cadd(Xs, Xn);
-      fold[r][1] = csub(Xs, Xn);
-    }
-    float2 *o = sd.fold + (static_cast<size_t>(b) * d.nh + jh) * 5 * 2 * d.M;
+  fft_forward_dif(sm, 5 * JB, n, d.logn, t.tw);
+  const float inv = 1.0f / n, hinv = 0.5f * inv;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
 #pragma unroll
     for (int r = 0; r < 5; r++) {
-      o[(r * 2 + 0) * d.M + m] = fold[r][0];
-      o[(r * 2 + 1) * d.M + m] = fold[r][1];
+      float2 f0[SPLIT_JB_MAX], f1[SPLIT_JB_MAX];
+#pragma unroll
+      for (int pr = 0; pr < SPLIT_JB_MAX; pr++) {
+        if (pr >= JB) break;
+        const int js = jh0 + pr;
+        const float2 *row = sm + static_cast<size_t>(r * JB + pr) * n;
+        const float2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
+        float2 Xs = cscale(cadd(Ym, Yc), hinv);
+        const float2 tt = csub(Ym, Yc);
+        float2 Xn = make_float2(hinv * tt.y, -hinv * tt.x);
+        const float wt = r < 4 ? t.wd[js] : t.w[js];
+        Xs = cscale(Xs, wt);
+        Xn = cscale(Xn, wt);
+        f0[pr] = cadd(Xs, Xn);
+        f1[pr] = csub(Xs, Xn);
+      }
+      float2 *o0 = sd.fold + ((static_cast<long>(m) * 10 + r * 2 + 0) * B + b) * d.nh + jh0;
+      float2 *o1 = sd.fold + ((static_cast<long>(m) * 10 + r * 2 + 1) * B + b) * d.nh + jh0;
+      if (JB == 4) {
+        reinterpret_cast<float4 *>(o0)[0] = make_float4(f0[0].x, f0[0].y, f0[1].x, f0[1].y);
+        reinterpret_cast<float4 *>(o0)[1] = make_float4(f0[2].x, f0[2].y, f0[3].x, f0[3].y);
+        reinterpret_cast<float4 *>(o1)[0] = make_float4(f1[0].x, f1[0].y, f1[1].x, f1[1].y);
+        reinterpret_cast<float4 *>(o1)[1] = make_float4(f1[2].x, f1[2].y, f1[3].x, f1[3].y);
+      } else {
+#pragma unroll
+        for (int pr = 0; pr < SPLIT_JB_MAX; pr++) {
+          if (pr >= JB) break;
+          o0[pr] = f0[pr];
+          o1[pr] = f1[pr];
+        }
+      }
     }
   }
 }
@@ -506,18 +531,20 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_ana(SphDev d, SplitDev
     // and H quantities a, b, v at parity 1 - s
     const int ph = 1 - s;
     const long pstrideP = static_cast<long>(nchunk) * sd.rAP * 64, pstrideH = static_cast<long>(nchunk) * sd.rAH * 64;
+    const long sstride = static_cast<long>(B) * d.nh;  // between slots/parities of fold[m][slot][parity][member][jh]
+    const float2 *gm = sd.fold + static_cast<long>(m) * 10 * sstride + static_cast<long>(tile * sd.nbt) * d.nh;
     for (int e = threadIdx.x; e < mt * sd.nh64; e += blockDim.x) {
       const int jh = e % sd.nh64, ml = e / sd.nh64;
       float2 zp[4] = {}, zh[3] = {};
       if (jh < d.nh) {
-        const float2 *g = sd.fold + (static_cast<size_t>(tile * sd.nbt + ml) * d.nh + jh) * 5 * 2 * d.M;
-        zp[0] = g[(0 * 2 + s) * d.M + m];
-        zp[1] = g[(1 * 2 + s) * d.M + m];
-        zp[2] = g[(2 * 2 + s) * d.M + m];
-        zp[3] = g[(4 * 2 + s) * d.M + m];
-        zh[0] = g[(0 * 2 + ph) * d.M + m];
-        zh[1] = g[(1 * 2 + ph) * d.M + m];
-        zh[2] = g[(3 * 2 + ph) * d.M + m];
+        const float2 *g = gm + static_cast<long>(ml) * d.nh + jh;
+        zp[0] = g[(0 * 2 + s) * sstride];
+        zp[1] = g[(1 * 2 + s) * sstride];
+        zp[2] = g[(2 * 2 + s) * sstride];
+        zp[3] = g[(4 * 2 + s) * sstride];
+        zh[0] = g[(0 * 2 + ph) * sstride];
+        zh[1] = g[(1 * 2 + ph) * sstride];
+        zh[2] = g[(3 * 2 + ph) * sstride];
       }
       const int c = jh >> 6, kin = jh & 63;
       __nv_bfloat16 *dP = reinterpret_cast<__nv_bfloat16 *>(aP) + static_cast<long>(c) * sd.rAP * 64;
@@ -734,14 +761,28 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   const int pieces = sp.pieces;
   const size_t budget = 220 * 1024;
   const size_t syn_stage = static_cast<size_t>(pieces) * (sp.rSP + sp.nh16) * SPLIT_BK * 2;
-  sp.ns_syn = static_cast<int>(std::min<size_t>(SPLIT_MAX_STAGES, (budget - SPLIT_MARGIN) / syn_stage));
-  if (sp.ns_syn < 2) throw InvalidArgument("split precision: the synthesis pipeline does not fit in shared memory");
-  sp.smem_syn = sp.ns_syn * syn_stage + SPLIT_MARGIN;
+  // the pipeline never needs more stages than a CTA has chunks (two GEMMs of kp64 / 64 chunks); two CTAs per SM
+  // when two stages fit in half of the shared memory
+  int max_chunks = 0;
+  for (int m = 0; m <= N; m++) max_chunks = std::max(max_chunks, 2 * static_cast<int>(sp.kp64[m] / SPLIT_BK));
+  const size_t half_budget = SPLIT_HALF_SM;
+  if (2 * syn_stage + SPLIT_MARGIN <= half_budget) sp.ns_syn = static_cast<int>(std::min<size_t>(std::min(SPLIT_MAX_STAGES, max_chunks), (half_budget - SPLIT_MARGIN) / syn_stage));
+  else sp.ns_syn = static_cast<int>(std::min<size_t>(std::min(SPLIT_MAX_STAGES, max_chunks), (budget - SPLIT_MARGIN) / syn_stage));
+  sp.ns_syn = std::max(sp.ns_syn, 2);
+  if (sp.ns_syn * syn_stage + SPLIT_MARGIN > budget) throw InvalidArgument("split precision: the synthesis pipeline does not fit in shared memory");
+  sp.smem_syn = std::max(sp.ns_syn * syn_stage + SPLIT_MARGIN, static_cast<size_t>(4 * 8 * sp.nbt * 33 * sizeof(float)));
+  // latitude pairs per grid CTA: four when that still gives two CTAs per SM
+  sp.jb = 1;
+  for (int jb = SPLIT_JB_MAX; jb > 1; jb /= 2)
+    if (nh % jb == 0 && static_cast<long>(nh / jb) * B >= 2 * 152) {
+      sp.jb = jb;
+      break;
+    }
   const size_t nchunk = sp.nh64 / SPLIT_BK;
   const size_t ana_res = static_cast<size_t>(pieces) * nchunk * (sp.rAH + sp.rAP) * 128;
   const size_t ana_stage = static_cast<size_t>(pieces) * ra_max * SPLIT_BK * 2;
   // two analysis CTAs per SM when a 3-stage pipeline fits in half of the shared memory
-  const size_t half = 110 * 1024;
+  const size_t half = SPLIT_HALF_SM;
   if (ana_res + 3 * ana_stage + SPLIT_MARGIN <= half && static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float) <= half)
     sp.ns_ana = 3;
   else
@@ -762,6 +803,7 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.rAH = sp.rAH;
   s.rSP = sp.rSP;
   s.rSH = sp.rSH;
+  s.jb = sp.jb;
   s.ke16 = sp.ke16_d.p;
   s.kp64 = sp.kp64_d.p;
   s.ra16 = sp.ra16_d.p;
