@@ -125,37 +125,89 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, SphTab<R> t, 
 // Inverse: decimation in time from bit-reversed input to natural output. Forward: decimation in frequency
 // from natural input to bit-reversed output. Twiddles exp(-2 pi i k / n) from the table (conjugated for the
 // inverse), computed on the host in FP64.
-template <class C2> __device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw) {
-  const int halfn = n >> 1;
-  for (int st = 0; st < logn; st++) {
-    const int half = 1 << st, stride = halfn >> st;
-    for (int e = threadIdx.x; e < rows * halfn; e += blockDim.x) {
-      const int r = e / halfn, bf = e - r * halfn;
-      const int grp = bf >> st, pos = bf & (half - 1);
-      const int i1 = grp * 2 * half + pos, i2 = i1 + half;
-      C2 *row = s + static_cast<size_t>(r) * n;
-      const C2 w = conjd(tw[pos * stride]);
-      const C2 t = cmul(w, row[i2]), u = row[i1];
-      row[i1] = cadd(u, t);
-      row[i2] = csub(u, t);
+// Radix-2 FFT stages fused in groups of up to three: a thread loads the 2^F elements that F consecutive stages
+// combine (indices i0 + j 2^st), applies the F stages' butterflies in registers and stores them back, so each
+// group costs one pass through shared memory and one barrier instead of F. The butterflies, their order and
+// the twiddle factors are those of the plain radix-2 transform, so the results are bit for bit the same.
+// Rows may be padded (PAD): element i of a row sits at i + i / 8 and rows are n + n / 8 long, which spreads the
+// strided accesses of the first stage groups over the shared-memory banks.
+template <bool PAD> __device__ __forceinline__ int fft_at(int i) { return PAD ? i + (i >> 3) : i; }
+template <bool PAD> __host__ __device__ __forceinline__ int fft_row(int n) { return PAD ? n + (n >> 3) : n; }
+
+template <class C2, int F, bool PAD>
+__device__ __forceinline__ void dit_group(C2 *s, int rows, int n, int logn, int st, const C2 *__restrict__ tw) {
+  constexpr int E = 1 << F;
+  const int halfn = n >> 1, lo = (1 << st) - 1;
+  for (int e = threadIdx.x; e < (rows << (logn - F)); e += blockDim.x) {
+    const int r = e >> (logn - F), q = e & ((1 << (logn - F)) - 1);
+    const int i0 = ((q >> st) << (st + F)) + (q & lo);
+    C2 *row = s + static_cast<size_t>(r) * fft_row<PAD>(n);
+    C2 x[E];
+#pragma unroll
+    for (int j = 0; j < E; j++) x[j] = row[fft_at<PAD>(i0 + (j << st))];
+#pragma unroll
+    for (int f = 0; f < F; f++) {
+      const int h = 1 << f, stride = halfn >> (st + f);
+#pragma unroll
+      for (int j = 0; j < E; j++) {
+        if (j & h) continue;
+        const C2 w = conjd(tw[((q & lo) + ((j & (h - 1)) << st)) * stride]);
+        const C2 t = cmul(w, x[j + h]), u = x[j];
+        x[j] = cadd(u, t);
+        x[j + h] = csub(u, t);
+      }
     }
-    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < E; j++) row[fft_at<PAD>(i0 + (j << st))] = x[j];
   }
 }
-template <class C2> __device__ void fft_forward_dif(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw) {
-  const int halfn = n >> 1;
-  for (int st = logn - 1; st >= 0; st--) {
-    const int half = 1 << st, stride = halfn >> st;
-    for (int e = threadIdx.x; e < rows * halfn; e += blockDim.x) {
-      const int r = e / halfn, bf = e - r * halfn;
-      const int grp = bf >> st, pos = bf & (half - 1);
-      const int i1 = grp * 2 * half + pos, i2 = i1 + half;
-      C2 *row = s + static_cast<size_t>(r) * n;
-      const C2 u = row[i1], v = row[i2];
-      row[i1] = cadd(u, v);
-      row[i2] = cmul(csub(u, v), tw[pos * stride]);
+template <class C2, int F, bool PAD>
+__device__ __forceinline__ void dif_group(C2 *s, int rows, int n, int logn, int st, const C2 *__restrict__ tw) {
+  constexpr int E = 1 << F;
+  const int halfn = n >> 1, lo = (1 << st) - 1;
+  for (int e = threadIdx.x; e < (rows << (logn - F)); e += blockDim.x) {
+    const int r = e >> (logn - F), q = e & ((1 << (logn - F)) - 1);
+    const int i0 = ((q >> st) << (st + F)) + (q & lo);
+    C2 *row = s + static_cast<size_t>(r) * fft_row<PAD>(n);
+    C2 x[E];
+#pragma unroll
+    for (int j = 0; j < E; j++) x[j] = row[fft_at<PAD>(i0 + (j << st))];
+#pragma unroll
+    for (int f = F - 1; f >= 0; f--) {
+      const int h = 1 << f, stride = halfn >> (st + f);
+#pragma unroll
+      for (int j = 0; j < E; j++) {
+        if (j & h) continue;
+        const C2 u = x[j], v = x[j + h];
+        x[j] = cadd(u, v);
+        x[j + h] = cmul(csub(u, v), tw[((q & lo) + ((j & (h - 1)) << st)) * stride]);
+      }
     }
+#pragma unroll
+    for (int j = 0; j < E; j++) row[fft_at<PAD>(i0 + (j << st))] = x[j];
+  }
+}
+// inverse transform (decimation in time) of `rows` rows in bit-reversed order, in place
+template <class C2, bool PAD = false> __device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw) {
+  for (int st = 0; st < logn;) {
+    const int F = logn - st >= 3 ? 3 : logn - st;
+    if (F == 3) dit_group<C2, 3, PAD>(s, rows, n, logn, st, tw);
+    else if (F == 2) dit_group<C2, 2, PAD>(s, rows, n, logn, st, tw);
+    else dit_group<C2, 1, PAD>(s, rows, n, logn, st, tw);
     __syncthreads();
+    st += F;
+  }
+}
+// forward transform (decimation in frequency) of `rows` rows in natural order, output bit-reversed, in place
+template <class C2, bool PAD = false> __device__ void fft_forward_dif(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw) {
+  for (int hi = logn; hi > 0;) {
+    const int F = hi >= 3 ? 3 : hi;
+    const int st = hi - F;
+    if (F == 3) dif_group<C2, 3, PAD>(s, rows, n, logn, st, tw);
+    else if (F == 2) dif_group<C2, 2, PAD>(s, rows, n, logn, st, tw);
+    else dif_group<C2, 1, PAD>(s, rows, n, logn, st, tw);
+    __syncthreads();
+    hi = st;
   }
 }
 __device__ __forceinline__ int bitrev(int k, int logn) { return static_cast<int>(__brev(static_cast<unsigned>(k)) >> (32 - logn)); }
@@ -1019,7 +1071,8 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   sa.filt = filt;
   if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
   if (which < 0 || which == 1)
-    split_grid<<<dim3(d.nh / sp.jb, B), GRID_THREADS, 5 * static_cast<size_t>(sp.jb) * d.nlon * sizeof(float2), stream>>>(d, t, sd, fgrid, hsgrid);
+    split_grid<<<dim3(d.nh / sp.jb, B), GRID_THREADS, 5 * static_cast<size_t>(sp.jb) * fft_row<true>(d.nlon) * sizeof(float2), stream>>>(d, t, sd, fgrid,
+                                                                                                                               hsgrid);
   if (which < 0 || which == 2)
     split_ana<<<dim3(d.M, 2, sp.ntiles), SPLIT_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
 }

@@ -393,8 +393,8 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
   float2 *sm = reinterpret_cast<float2 *>(smraw);  // rows f * jb + p: U, V, zeta, Phi and the fifth product of pair p
   const int JB = sd.jb, B = gridDim.y;
   const int b = blockIdx.y, jh0 = blockIdx.x * JB;
-  const int n = d.nlon, M = d.M;
-  for (int e = threadIdx.x; e < 4 * JB * n; e += blockDim.x) sm[e] = make_float2(0, 0);
+  const int n = d.nlon, M = d.M, rl = fft_row<true>(n);  // padded rows: element i at fft_at<true>(i)
+  for (int e = threadIdx.x; e < 4 * JB * rl; e += blockDim.x) sm[e] = make_float2(0, 0);
   __syncthreads();
   for (int e = threadIdx.x; e < JB * M; e += blockDim.x) {
     const int pr = e / M, m = e - pr * M;
@@ -405,16 +405,16 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
 #pragma unroll
     for (int f = 0; f < 4; f++) {
       const float2 a = A[f], c = C[f];
-      float2 *row = sm + static_cast<size_t>(f * JB + pr) * n;
+      float2 *row = sm + static_cast<size_t>(f * JB + pr) * rl;
       if (m == 0) row[0] = make_float2(a.x, c.x);
       else {
-        row[bitrev(m, d.logn)] = make_float2(a.x - c.y, a.y + c.x);
-        row[bitrev(n - m, d.logn)] = make_float2(a.x + c.y, c.x - a.y);
+        row[fft_at<true>(bitrev(m, d.logn))] = make_float2(a.x - c.y, a.y + c.x);
+        row[fft_at<true>(bitrev(n - m, d.logn))] = make_float2(a.x + c.y, c.x - a.y);
       }
     }
   }
   __syncthreads();
-  fft_inverse_dit(sm, 4 * JB, n, d.logn, t.tw);
+  fft_inverse_dit<float2, true>(sm, 4 * JB, n, d.logn, t.tw);
   const float g = static_cast<float>(d.g);
   for (int e = threadIdx.x; e < JB * n; e += blockDim.x) {
     const int pr = e >> d.logn, k = e & (n - 1);
@@ -422,10 +422,11 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
     const float r2om = t.r2om[js];
     const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
     const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
-    float2 *rU = sm + static_cast<size_t>(0 * JB + pr) * n, *rV = sm + static_cast<size_t>(1 * JB + pr) * n;
-    float2 *rZ = sm + static_cast<size_t>(2 * JB + pr) * n, *rP = sm + static_cast<size_t>(3 * JB + pr) * n;
-    float2 *rE = sm + static_cast<size_t>(4 * JB + pr) * n;
-    const float2 U = rU[k], V = rV[k], Z = rZ[k], P = rP[k];
+    float2 *rU = sm + static_cast<size_t>(0 * JB + pr) * rl, *rV = sm + static_cast<size_t>(1 * JB + pr) * rl;
+    float2 *rZ = sm + static_cast<size_t>(2 * JB + pr) * rl, *rP = sm + static_cast<size_t>(3 * JB + pr) * rl;
+    float2 *rE = sm + static_cast<size_t>(4 * JB + pr) * rl;
+    const int kp = fft_at<true>(k);
+    const float2 U = rU[kp], V = rV[kp], Z = rZ[kp], P = rP[kp];
     float2 A, Bv, UP, VP, PE;
     {
       const float eta = Z.x + static_cast<float>(fr_s[k]);
@@ -437,10 +438,10 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
       A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
       PE.y = P.y + g * static_cast<float>(hr_n[k]) + (U.y * U.y + V.y * V.y) * r2om;
     }
-    rU[k] = A; rV[k] = Bv; rZ[k] = UP; rP[k] = VP; rE[k] = PE;
+    rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
   __syncthreads();
-  fft_forward_dif(sm, 5 * JB, n, d.logn, t.tw);
+  fft_forward_dif<float2, true>(sm, 5 * JB, n, d.logn, t.tw);
   const float inv = 1.0f / n, hinv = 0.5f * inv;
   for (int m = threadIdx.x; m < M; m += blockDim.x) {
 #pragma unroll
@@ -450,8 +451,8 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
       for (int pr = 0; pr < SPLIT_JB_MAX; pr++) {
         if (pr >= JB) break;
         const int js = jh0 + pr;
-        const float2 *row = sm + static_cast<size_t>(r * JB + pr) * n;
-        const float2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
+        const float2 *row = sm + static_cast<size_t>(r * JB + pr) * rl;
+        const float2 Ym = row[fft_at<true>(bitrev(m, d.logn))], Yc = conjd(row[fft_at<true>(bitrev((n - m) & (n - 1), d.logn))]);
         float2 Xs = cscale(cadd(Ym, Yc), hinv);
         const float2 tt = csub(Ym, Yc);
         float2 Xn = make_float2(hinv * tt.y, -hinv * tt.x);
