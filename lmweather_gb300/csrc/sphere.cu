@@ -1074,7 +1074,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
     split_grid<<<dim3(d.nh / sp.jb, B), GRID_THREADS, 5 * static_cast<size_t>(sp.jb) * fft_row<true>(d.nlon) * sizeof(float2), stream>>>(d, t, sd, fgrid,
                                                                                                                                hsgrid);
   if (which < 0 || which == 2)
-    split_ana<<<dim3(d.M, 2, sp.ntiles), SPLIT_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
+    split_ana<<<dim3(d.M, 2, sp.ntiles), SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
 }
 
 void SphereEngine::launch_stage(int stage, double dt) {

@@ -35,6 +35,7 @@ constexpr int SPLIT_BK = 64;
 constexpr int SPLIT_MAX_STAGES = 4;
 constexpr int SPLIT_MARGIN = 16384;  // an M = 128 MMA reads 16 KB past an A base: every A base keeps 16 KB of allocation
 constexpr int SPLIT_THREADS = 128;
+constexpr int SPLIT_ANA_THREADS = 256;  // analysis: 8 warps for the gather and the RK4 epilogue, warps 0-3 read TMEM
 constexpr int SPLIT_NQ = 16;  // per (member, jh, m): U, V, zeta, Phi Fourier coefficients at the southern and northern latitude
 constexpr int SPLIT_JB_MAX = 4;  // latitude pairs per grid CTA
 // dynamic shared memory per CTA when two CTAs share an SM (228 KB per SM, 1 KB reserved per CTA, static barriers)
@@ -511,7 +512,7 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict
 
 // ------------------------------------------------------------------------------------------- analysis + RK4
 // grid: (M, 2, ntiles). D columns: H at [0, ra16), P at [ra16, 2 ra16)
-__global__ void __launch_bounds__(SPLIT_THREADS, 1) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
+__global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
                                                              int B, int ns, double2 *x0, double2 *xs, double2 *acc) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
@@ -528,37 +529,49 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_ana(SphDev d, SplitDev
   const int aH_bytes = sd.pieces * nchunk * sd.rAH * 128, aP_bytes = sd.pieces * nchunk * sd.rAP * 128;
   uint8_t *aH = smem, *aP = smem + aH_bytes, *pipe = smem + aH_bytes + aP_bytes;
   {
-    // gather the folded grid values of this (m, s), one latitude per thread: P quantities a, b, u, e at parity s
-    // and H quantities a, b, v at parity 1 - s
+    // gather the folded grid values of this (m, s) into the resident A operands: P quantities a, b, u, e at
+    // parity s and H quantities a, b, v at parity 1 - s. One work item = (member, quantity, 8 latitudes): eight
+    // consecutive float2 loads, then one 16-byte store per (real/imaginary row, piece) into the chunk layout.
     const int ph = 1 - s;
     const long pstrideP = static_cast<long>(nchunk) * sd.rAP * 64, pstrideH = static_cast<long>(nchunk) * sd.rAH * 64;
     const long sstride = static_cast<long>(B) * d.nh;  // between slots/parities of fold[m][slot][parity][member][jh]
     const float2 *gm = sd.fold + static_cast<long>(m) * 10 * sstride + static_cast<long>(tile * sd.nbt) * d.nh;
-    for (int e = threadIdx.x; e < mt * sd.nh64; e += blockDim.x) {
-      const int jh = e % sd.nh64, ml = e / sd.nh64;
-      float2 zp[4] = {}, zh[3] = {};
-      if (jh < d.nh) {
-        const float2 *g = gm + static_cast<long>(ml) * d.nh + jh;
-        zp[0] = g[(0 * 2 + s) * sstride];
-        zp[1] = g[(1 * 2 + s) * sstride];
-        zp[2] = g[(2 * 2 + s) * sstride];
-        zp[3] = g[(4 * 2 + s) * sstride];
-        zh[0] = g[(0 * 2 + ph) * sstride];
-        zh[1] = g[(1 * 2 + ph) * sstride];
-        zh[2] = g[(3 * 2 + ph) * sstride];
-      }
-      const int c = jh >> 6, kin = jh & 63;
-      __nv_bfloat16 *dP = reinterpret_cast<__nv_bfloat16 *>(aP) + static_cast<long>(c) * sd.rAP * 64;
-      __nv_bfloat16 *dH = reinterpret_cast<__nv_bfloat16 *>(aH) + static_cast<long>(c) * sd.rAH * 64;
+    const int nkb = sd.nh64 >> 3;
+    for (int e = threadIdx.x; e < mt * 7 * nkb; e += blockDim.x) {
+      const int kb = e % nkb, rest = e / nkb, qi = rest % 7, ml = rest / 7;
+      // qi 0..3: P slots 0, 1, 2, 4 at parity s; 4..6: H slots 0, 1, 3 at parity 1 - s
+      const int slot = qi < 3 ? qi : (qi == 3 ? 4 : (qi == 6 ? 3 : qi - 4));
+      const int par = qi < 4 ? s : ph;
+      const int j0 = kb * 8;
+      float2 v[8];
+      const float2 *g = gm + static_cast<long>(slot * 2 + par) * sstride + static_cast<long>(ml) * d.nh + j0;
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        fsplit(zp[q].x, dP + tile_off(ml * 8 + 2 * q, kin, sd.rAP), pstrideP, sd.pieces);
-        fsplit(zp[q].y, dP + tile_off(ml * 8 + 2 * q + 1, kin, sd.rAP), pstrideP, sd.pieces);
-      }
+      for (int j = 0; j < 8; j++) v[j] = j0 + j < d.nh ? g[j] : make_float2(0.0f, 0.0f);
+      const int c = j0 >> 6, kin = j0 & 63;
+      const bool isP = qi < 4;
+      const int R = isP ? sd.rAP : sd.rAH;
+      const int row = isP ? ml * 8 + 2 * qi : ml * 6 + 2 * (qi - 4);
+      __nv_bfloat16 *base = reinterpret_cast<__nv_bfloat16 *>(isP ? aP : aH) + static_cast<long>(c) * R * 64;
+      const long pstride = isP ? pstrideP : pstrideH;
 #pragma unroll
-      for (int q = 0; q < 3; q++) {
-        fsplit(zh[q].x, dH + tile_off(ml * 6 + 2 * q, kin, sd.rAH), pstrideH, sd.pieces);
-        fsplit(zh[q].y, dH + tile_off(ml * 6 + 2 * q + 1, kin, sd.rAH), pstrideH, sd.pieces);
+      for (int ri = 0; ri < 2; ri++) {
+        uint4 k0, k1, k2;
+        __nv_bfloat16 *b0 = reinterpret_cast<__nv_bfloat16 *>(&k0), *b1 = reinterpret_cast<__nv_bfloat16 *>(&k1),
+                      *b2 = reinterpret_cast<__nv_bfloat16 *>(&k2);
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const float x = ri == 0 ? v[j].x : v[j].y;
+          const __nv_bfloat16 h = __float2bfloat16_rn(x);
+          const float r1 = x - __bfloat162float(h);
+          const __nv_bfloat16 l = __float2bfloat16_rn(r1);
+          b0[j] = h;
+          b1[j] = l;
+          b2[j] = __float2bfloat16_rn(r1 - __bfloat162float(l));
+        }
+        __nv_bfloat16 *dst = base + tile_off(row + ri, kin, R);
+        *reinterpret_cast<uint4 *>(dst) = k0;
+        if (sd.pieces > 1) *reinterpret_cast<uint4 *>(dst + pstride) = k1;
+        if (sd.pieces > 2) *reinterpret_cast<uint4 *>(dst + 2 * pstride) = k2;
       }
     }
   }
