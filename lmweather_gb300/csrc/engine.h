@@ -130,6 +130,8 @@ class SphereEngine {
   double *device_state() { return x0.p; }
   // to be called after the state was written through device_state() (repacks the split operands)
   void state_written() { split_packed = false; }
+  DevBuf<int> gflag;   // per member: bit 0 tilted Coriolis grid, bit 1 orography
+  DevBuf<double> om2;  // per member: 2 Omega
   uint64_t launches_per_step() const { return launches_step; }
   // average duration (ms) per launch of each stage kernel class over `reps` launches (CUDA events on the
   // engine stream): out[0] synthesis, out[1] grid (FFTs + products), out[2] analysis + RK4 update. x0 unchanged.
@@ -147,6 +149,8 @@ class SphereEngine {
   DevBuf<double> four, fold;
   DevBuf<float> four32, fold32;
   DevBuf<double> fgrid, hsgrid, refgrid, filt, diagrows;
+  std::vector<int> gflag_h;
+  void upload_member_flags(int member);
   DevBuf<double> gridin;
   DevBuf<Reduce> dred;
   HostBuf<Reduce> hred;

@@ -215,20 +215,20 @@ __device__ __forceinline__ int bitrev(int k, int logn) { return static_cast<int>
 // Load the Fourier coefficients of `rows` fields at latitudes js (real part) and jn (imaginary part) into
 // bit-reversed rows: Y[m] = X_s[m] + i X_n[m], Y[n-m] = conj(X_s[m]) + i conj(X_n[m]); Im X[0] is dropped
 // as in cpp/sphere.cpp:132.
-template <class C2>
+template <class C2, bool PAD = false>
 __device__ void load_pair_spectra(C2 *s, int rows, const SphDev &d, const C2 *__restrict__ fs, const C2 *__restrict__ fn, int fstride) {
-  const int n = d.nlon;
-  for (int e = threadIdx.x; e < rows * n; e += blockDim.x) s[e] = mk2(decltype(C2::x)(0), decltype(C2::x)(0));
+  const int n = d.nlon, rl = fft_row<PAD>(n);
+  for (int e = threadIdx.x; e < rows * rl; e += blockDim.x) s[e] = mk2(decltype(C2::x)(0), decltype(C2::x)(0));
   __syncthreads();
   for (int e = threadIdx.x; e < rows * d.M; e += blockDim.x) {
     const int r = e / d.M, m = e - r * d.M;
     C2 a = fs[r * fstride + m], c = fn[r * fstride + m];
-    C2 *row = s + static_cast<size_t>(r) * n;
+    C2 *row = s + static_cast<size_t>(r) * rl;
     if (m == 0) {
       row[0] = mk2(a.x, c.x);
     } else {
-      row[bitrev(m, d.logn)] = mk2(a.x - c.y, a.y + c.x);
-      row[bitrev(n - m, d.logn)] = mk2(a.x + c.y, c.x - a.y);
+      row[fft_at<PAD>(bitrev(m, d.logn))] = mk2(a.x - c.y, a.y + c.x);
+      row[fft_at<PAD>(bitrev(n - m, d.logn))] = mk2(a.x + c.y, c.x - a.y);
     }
   }
   __syncthreads();
@@ -246,40 +246,43 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, SphTab<R> t, 
   extern __shared__ __align__(16) unsigned char smraw[];
   C2 *sm = reinterpret_cast<C2 *>(smraw);
   const int b = blockIdx.y, jh = blockIdx.x;
-  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
+  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon, rl = fft_row<true>(n);  // padded rows
   const C2 *f_s = four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M;
   const C2 *f_n = four + (static_cast<size_t>(b) * d.nlat + jn) * 4 * d.M;
-  load_pair_spectra(sm, 4, d, f_s, f_n, d.M);
-  fft_inverse_dit(sm, 4, n, d.logn, t.tw);
+  load_pair_spectra<C2, true>(sm, 4, d, f_s, f_n, d.M);
+  fft_inverse_dit<C2, true>(sm, 4, n, d.logn, t.tw);
   // nonlinear products, cpp/sphere.cpp:348-359 (real part: southern latitude, imaginary part: northern)
   const R r2om = t.r2om[js], g = static_cast<R>(d.g);  // 1 / (2 (1 - mu^2)), the same at the mirror latitude
   const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
   const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
-  C2 *rU = sm, *rV = sm + n, *rZ = sm + 2 * n, *rP = sm + 3 * n, *rE = sm + 4 * n;
+  const int gf = d.gflag[b];
+  const double f0s = d.om2[b] * d.mu[js], f0n = d.om2[b] * d.mu[jn];
+  C2 *rU = sm, *rV = sm + rl, *rZ = sm + 2 * rl, *rP = sm + 3 * rl, *rE = sm + 4 * rl;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const C2 U = rU[k], V = rV[k], Z = rZ[k], P = rP[k];
+    const int kp = fft_at<true>(k);
+    const C2 U = rU[kp], V = rV[kp], Z = rZ[kp], P = rP[kp];
     C2 A, Bv, UP, VP, PE;
     {
-      R eta = Z.x + static_cast<R>(fr_s[k]);
+      R eta = Z.x + static_cast<R>((gf & 1) ? fr_s[k] : f0s);
       A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
-      PE.x = P.x + g * static_cast<R>(hr_s[k]) + (U.x * U.x + V.x * V.x) * r2om;
+      PE.x = P.x + g * static_cast<R>((gf & 2) ? hr_s[k] : 0.0) + (U.x * U.x + V.x * V.x) * r2om;
     }
     {
-      R eta = Z.y + static_cast<R>(fr_n[k]);
+      R eta = Z.y + static_cast<R>((gf & 1) ? fr_n[k] : f0n);
       A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
-      PE.y = P.y + g * static_cast<R>(hr_n[k]) + (U.y * U.y + V.y * V.y) * r2om;
+      PE.y = P.y + g * static_cast<R>((gf & 2) ? hr_n[k] : 0.0) + (U.y * U.y + V.y * V.y) * r2om;
     }
-    rU[k] = A; rV[k] = Bv; rZ[k] = UP; rP[k] = VP; rE[k] = PE;
+    rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
   __syncthreads();
-  fft_forward_dif(sm, NSLOT, n, d.logn, t.tw);
+  fft_forward_dif<C2, true>(sm, NSLOT, n, d.logn, t.tw);
   // separate the two latitudes, normalise by nlon (cpp/sphere.cpp:128), weight and fold
   const R inv = R(1) / n, wd = t.wd[js], wj = t.w[js];
   C2 *o = fold + (static_cast<size_t>(b) * d.nh + jh) * NSLOT * 2 * d.M;
   for (int e = threadIdx.x; e < NSLOT * d.M; e += blockDim.x) {
     const int r = e / d.M, m = e - r * d.M;
-    const C2 *row = sm + static_cast<size_t>(r) * n;
-    const C2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
+    const C2 *row = sm + static_cast<size_t>(r) * rl;
+    const C2 Ym = row[fft_at<true>(bitrev(m, d.logn))], Yc = conjd(row[fft_at<true>(bitrev((n - m) & (n - 1), d.logn))]);
     // X_s = (Ym + conj(Y_{n-m}))/2, X_n = -i (Ym - conj(Y_{n-m}))/2
     const R hinv = R(0.5) * inv;
     C2 Xs = cscale(cadd(Ym, Yc), hinv);
@@ -609,6 +612,8 @@ static SphDev make_sph(const SphereEngine &e, const SphereTables &t) {
   d.tw = t.tw.p;
   d.trim = t.trim.p;
   d.trin = t.trin.p;
+  d.gflag = e.gflag.p;
+  d.om2 = e.om2.p;
   d.tri = t.tri.p;
   return d;
 }
@@ -753,6 +758,11 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   gridin.alloc(4 * ngrid());
   dred.alloc(B);
   hred.alloc(B);
+  gflag.alloc(B);
+  om2.alloc(B);
+  gflag.zero(stream);
+  om2.zero(stream);
+  gflag_h.assign(B, 0);
   hstage.alloc(std::max<size_t>(4 * ngrid(), static_cast<size_t>(3) * 2 * nspec_ref()));
   if (p.precision == kSplitBF16) {
     split = new SplitPlan();
@@ -791,8 +801,18 @@ static void check_member(const SphereEngine &e, int member) {
 }
 
 // cpp/sphere.cpp:111-118 (with the member's own rotation rate)
+void SphereEngine::upload_member_flags(int member) {
+  const double o2 = 2 * omega_m[member];
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  LMW_CUDA(cudaMemcpy(gflag.p + member, &gflag_h[member], sizeof(int), cudaMemcpyHostToDevice));
+  LMW_CUDA(cudaMemcpy(om2.p + member, &o2, sizeof(double), cudaMemcpyHostToDevice));
+}
+
 void SphereEngine::set_axis_tilt(double alpha, int member) {
   check_member(*this, member);
+  // an untilted grid is f = (2 Omega) mu exactly (the tilt terms are signed zeros): the grid kernels compute it
+  gflag_h[member] = (gflag_h[member] & ~1) | (alpha != 0.0 ? 1 : 0);
+  upload_member_flags(member);
   const HostTables &h = tab->host;
   std::vector<double> f(ngrid());
   for (int j = 0; j < nlat; j++)
@@ -817,6 +837,8 @@ void SphereEngine::set_orography(const double *hs, size_t n, int member) {
   LMW_CUDA(cudaStreamSynchronize(stream));
   LMW_CUDA(cudaMemcpy(hsgrid.p + static_cast<size_t>(member) * ngrid(), hs, n * sizeof(double), cudaMemcpyHostToDevice));
   has_orog[member] = 1;
+  gflag_h[member] |= 2;
+  upload_member_flags(member);
 }
 
 void SphereEngine::synth_grids(int member_first, int count) {
@@ -1047,7 +1069,7 @@ template <class R>
 static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage, double dt, const double *filt, const double2 *in,
                           typename V2<R>::type *four, typename V2<R>::type *fold, double2 *x0, double2 *xs, double2 *acc,
                           const double *fgrid, const double *hsgrid, cudaStream_t stream, int which = -1) {
-  const size_t smem = 5 * static_cast<size_t>(d.nlon) * sizeof(typename V2<R>::type);
+  const size_t smem = 5 * static_cast<size_t>(fft_row<true>(d.nlon)) * sizeof(typename V2<R>::type);  // padded FFT rows
   StageArgs sa;
   sa.stage = stage;
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);

@@ -11,6 +11,9 @@ struct SphDev {
   const double *Ps, *Hs, *Pa, *Ha, *mu, *w, *wd, *cosl, *r2om, *kfac, *lapl;
   const double2 *tw;
   const int *trim, *trin, *tri;
+  // per member: bit 0 = the Coriolis grid is tilted (read fgrid, else f = om2 mu), bit 1 = orography (read hsgrid)
+  const int *gflag;
+  const double *om2;  // 2 Omega per member
 };
 
 template <class R> struct V2;

@@ -423,6 +423,7 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
     const float r2om = t.r2om[js];
     const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
     const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
+    const int gf = d.gflag[b];
     float2 *rU = sm + static_cast<size_t>(0 * JB + pr) * rl, *rV = sm + static_cast<size_t>(1 * JB + pr) * rl;
     float2 *rZ = sm + static_cast<size_t>(2 * JB + pr) * rl, *rP = sm + static_cast<size_t>(3 * JB + pr) * rl;
     float2 *rE = sm + static_cast<size_t>(4 * JB + pr) * rl;
@@ -430,14 +431,14 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
     const float2 U = rU[kp], V = rV[kp], Z = rZ[kp], P = rP[kp];
     float2 A, Bv, UP, VP, PE;
     {
-      const float eta = Z.x + static_cast<float>(fr_s[k]);
+      const float eta = Z.x + static_cast<float>((gf & 1) ? fr_s[k] : d.om2[b] * d.mu[js]);
       A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
-      PE.x = P.x + g * static_cast<float>(hr_s[k]) + (U.x * U.x + V.x * V.x) * r2om;
+      PE.x = P.x + g * static_cast<float>((gf & 2) ? hr_s[k] : 0.0) + (U.x * U.x + V.x * V.x) * r2om;
     }
     {
-      const float eta = Z.y + static_cast<float>(fr_n[k]);
+      const float eta = Z.y + static_cast<float>((gf & 1) ? fr_n[k] : d.om2[b] * d.mu[jn]);
       A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
-      PE.y = P.y + g * static_cast<float>(hr_n[k]) + (U.y * U.y + V.y * V.y) * r2om;
+      PE.y = P.y + g * static_cast<float>((gf & 2) ? hr_n[k] : 0.0) + (U.y * U.y + V.y * V.y) * r2om;
     }
     rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
