@@ -299,6 +299,9 @@ def run_ours(args, rank, world, local):
             dev_ms += max(e0.elapsed_time(e) for e in ends)
     launches = lw.launch_count() - launches0
     groups = ens.groups()
+    if args.precision.startswith("split"):
+        for g, grp in enumerate(groups):
+            grp["autotuned_plan"] = ens.split_plan(g)
     dist.barrier()
     dev_ms = dist.max(dev_ms)
     member_days = ens.count * DAYS * world

@@ -85,6 +85,8 @@ _SIGS = {
     "lmw_ensemble_member_set_state": (_I, [_P, _I, _DP, _DP, _DP]),
     "lmw_ensemble_member_diagnostics": (_I, [_P, _I, _DP]),
     "lmw_ensemble_member_grid": (_I, [_P, _I, _I, _DP, _SZ]),
+    "lmw_sphere_split_plan": (_I, [_P, _IP]),
+    "lmw_ensemble_split_plan": (_I, [_P, _I, _IP]),
     "lmw_mlp_create": (_I, [_I, _I, _I, _I, _U64, _D, _PP]),
     "lmw_mlp_destroy": (_I, [_P]),
     "lmw_mlp_set_layer": (_I, [_P, _I, _FP, _FP]),
@@ -248,6 +250,12 @@ class Sphere:
     def turbulence(self, seed: int, mean_height=8000.0, max_wind=30.0, nforce=21, member: int = 0):
         _check(self._lib.lmw_sphere_turbulence(self._h, member, seed, mean_height, max_wind, nforce))
         return self
+
+    def split_plan(self) -> dict:
+        """The autotuned launch plan of the split path (zeros in the other precisions)."""
+        out = np.zeros(4, np.int32)
+        _check(self._lib.lmw_sphere_split_plan(self._h, out.ctypes.data_as(_IP)))
+        return dict(zip(("lat_pairs_per_grid_cta", "fft_stages_per_pass", "synthesis_stages", "analysis_stages"), out.tolist()))
 
     def get_state(self, member: int = 0):
         z, d, f = (np.zeros(self.nspec, np.complex128) for _ in range(3))
@@ -479,6 +487,12 @@ class Ensemble:
         _check(self._lib.lmw_ensemble_groups(self._h, C.byref(ng), tr.ctypes.data_as(_IP), cnt.ctypes.data_as(_IP), _dp(dt),
                                              st.ctypes.data_as(C.POINTER(C.c_int64))))
         return [dict(truncation=int(tr[g]), members=int(cnt[g]), dt=float(dt[g]), steps=int(st[g])) for g in range(G)]
+
+    def split_plan(self, group: int) -> dict:
+        """The autotuned launch plan of a truncation group's split path."""
+        out = np.zeros(4, np.int32)
+        _check(self._lib.lmw_ensemble_split_plan(self._h, group, out.ctypes.data_as(_IP)))
+        return dict(zip(("lat_pairs_per_grid_cta", "fft_stages_per_pass", "synthesis_stages", "analysis_stages"), out.tolist()))
 
     def member_state(self, i: int):
         T = int(self.truncation[i])

@@ -587,6 +587,21 @@ int lmw_surrogate_time(lmw_surrogate *s, int batch, int reps, double *train_ms, 
 }  // extern "C"
 
 extern "C" {
+int lmw_sphere_split_plan(lmw_sphere *s, int *out) {
+  return guard([&] {
+    need(s != nullptr && s->e != nullptr, "null sphere handle");
+    need(out != nullptr, "null buffer");
+    s->e->split_plan(out);
+  });
+}
+int lmw_ensemble_split_plan(lmw_ensemble *e, int group, int *out) {
+  return guard([&] {
+    need(e != nullptr && e->e != nullptr, "null ensemble handle");
+    need(out != nullptr, "null buffer");
+    need(group >= 0 && group < static_cast<int>(e->e->groups.size()), "group index out of range");
+    e->e->groups[group]->split_plan(out);
+  });
+}
 int lmw_surrogate_reset(lmw_surrogate *s, uint64_t seed) { return SUR(s, s->s->reset(seed)); }
 int lmw_surrogate_set_clip(lmw_surrogate *s, double ratio) {
   return SUR(s, need(ratio >= 0, "the clipping ratio must not be negative"); s->s->clip_ratio = ratio);

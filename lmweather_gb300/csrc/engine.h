@@ -136,6 +136,9 @@ class SphereEngine {
   // average duration (ms) per launch of each stage kernel class over `reps` launches (CUDA events on the
   // engine stream): out[0] synthesis, out[1] grid (FFTs + products), out[2] analysis + RK4 update. x0 unchanged.
   void kernel_times(double dt, int reps, double *out);
+  // the split path's measured launch plan: latitude pairs per grid CTA, FFT stages per pass, synthesis and
+  // analysis pipeline stages (zeros without the split path)
+  void split_plan(int *out) const;
 
  private:
   SphereTables *tab = nullptr;
@@ -143,6 +146,7 @@ class SphereEngine {
   bool split_packed = false;
   void check_split_status();
   void ensure_packed();
+  void autotune_split();
   // state (packed triangle, complex interleaved), stage input, accumulator
   DevBuf<double> x0, xs, acc;
   // Fourier coefficients of the synthesised grids, folded analysis inputs

@@ -188,9 +188,11 @@ __device__ __forceinline__ void dif_group(C2 *s, int rows, int n, int logn, int 
   }
 }
 // inverse transform (decimation in time) of `rows` rows in bit-reversed order, in place
-template <class C2, bool PAD = false> __device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw) {
+// fmax: stages per group (1..3)
+template <class C2, bool PAD = false>
+__device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw, int fmax = 3) {
   for (int st = 0; st < logn;) {
-    const int F = logn - st >= 3 ? 3 : logn - st;
+    const int F = logn - st >= fmax ? fmax : logn - st;
     if (F == 3) dit_group<C2, 3, PAD>(s, rows, n, logn, st, tw);
     else if (F == 2) dit_group<C2, 2, PAD>(s, rows, n, logn, st, tw);
     else dit_group<C2, 1, PAD>(s, rows, n, logn, st, tw);
@@ -199,9 +201,10 @@ template <class C2, bool PAD = false> __device__ void fft_inverse_dit(C2 *s, int
   }
 }
 // forward transform (decimation in frequency) of `rows` rows in natural order, output bit-reversed, in place
-template <class C2, bool PAD = false> __device__ void fft_forward_dif(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw) {
+template <class C2, bool PAD = false>
+__device__ void fft_forward_dif(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw, int fmax = 3) {
   for (int hi = logn; hi > 0;) {
-    const int F = hi >= 3 ? 3 : hi;
+    const int F = hi >= fmax ? fmax : hi;
     const int st = hi - F;
     if (F == 3) dif_group<C2, 3, PAD>(s, rows, n, logn, st, tw);
     else if (F == 2) dif_group<C2, 2, PAD>(s, rows, n, logn, st, tw);
@@ -775,6 +778,7 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   allow_max_shared_memory();
   for (int b = 0; b < B; b++) set_axis_tilt(0, b);
   LMW_CUDA(cudaStreamSynchronize(stream));
+  autotune_split();
 }
 
 SphereEngine::~SphereEngine() {
@@ -1153,6 +1157,102 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
   cudaEventDestroy(e1);
   g_launches += 3ull * (reps + 1);
   split_packed = false;
+}
+
+// Measured choice of the split path's launch plan: latitude pairs per grid CTA (4, 2, 1), FFT stages fused per
+// shared-memory pass (3 or 2), and the pipeline depth of the synthesis and analysis kernels (2-4 stages where
+// they fit). Each kernel is timed alone for every candidate (CUDA events on the engine stream, stage 1 on the
+// present state, which leaves the state unchanged); the arithmetic does not depend on the choice.
+void SphereEngine::autotune_split() {
+  if (!split) return;
+  SplitPlan &sp = *split;
+  const double dt = 60.0;
+  upload_filter(dt);
+  SphDev d = make_sph(*this, *tab);
+  double2 *X0 = reinterpret_cast<double2 *>(x0.p), *XS = reinterpret_cast<double2 *>(xs.p), *AC = reinterpret_cast<double2 *>(acc.p);
+  cudaEvent_t e0, e1;
+  LMW_CUDA(cudaEventCreate(&e0));
+  LMW_CUDA(cudaEventCreate(&e1));
+  auto timed = [&](int which) {
+    auto one = [&] {
+      split_stage(d, tab32(*tab), sp, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, AC, fgrid.p, hsgrid.p, stream,
+                  which);
+    };
+    one();
+    LMW_CUDA(cudaEventRecord(e0, stream));
+    for (int r = 0; r < 3; r++) one();
+    LMW_CUDA(cudaEventRecord(e1, stream));
+    LMW_LAUNCH_CHECK();
+    LMW_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    LMW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    g_launches += 4;
+    return static_cast<double>(ms);
+  };
+  ensure_packed();
+  // grid kernel
+  {
+    int bj = sp.jb, bf = sp.fgrp;
+    double best = 1e30;
+    for (int jb = SPLIT_JB_MAX; jb >= 1; jb /= 2) {
+      if (nh % jb) continue;
+      for (int fg = 3; fg >= 2; fg--) {
+        sp.jb = jb;
+        sp.fgrp = fg;
+        const double t = timed(1);
+        if (t < best) {
+          best = t;
+          bj = jb;
+          bf = fg;
+        }
+      }
+    }
+    sp.jb = bj;
+    sp.fgrp = bf;
+  }
+  // synthesis and analysis pipeline depth
+  {
+    const int ns0 = sp.ns_syn, na0 = sp.ns_ana;
+    int bs = ns0, ba = na0;
+    double best_s = 1e30, best_a = 1e30;
+    for (int ns = 2; ns <= SPLIT_MAX_STAGES; ns++) {
+      const size_t bytes = std::max(ns * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
+      if (bytes > sp.budget_bytes) continue;
+      sp.ns_syn = ns;
+      sp.smem_syn = bytes;
+      const double t = timed(0);
+      if (t < best_s) {
+        best_s = t;
+        bs = ns;
+      }
+    }
+    for (int ns = 2; ns <= SPLIT_MAX_STAGES; ns++) {
+      const size_t bytes = std::max(sp.ana_res_bytes + ns * sp.ana_stage_bytes + SPLIT_MARGIN, sp.ana_min_bytes);
+      if (bytes > sp.budget_bytes) continue;
+      sp.ns_ana = ns;
+      sp.smem_ana = bytes;
+      const double t = timed(2);
+      if (t < best_a) {
+        best_a = t;
+        ba = ns;
+      }
+    }
+    sp.ns_syn = bs;
+    sp.smem_syn = std::max(bs * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
+    sp.ns_ana = ba;
+    sp.smem_ana = std::max(sp.ana_res_bytes + ba * sp.ana_stage_bytes + SPLIT_MARGIN, sp.ana_min_bytes);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  check_split_status();
+  split_packed = false;
+}
+
+void SphereEngine::split_plan(int *out) const {
+  out[0] = split ? split->jb : 0;
+  out[1] = split ? split->fgrp : 0;
+  out[2] = split ? split->ns_syn : 0;
+  out[3] = split ? split->ns_ana : 0;
 }
 
 // the split path keeps its synthesis operands packed from the state; pack them after a change from outside

@@ -56,10 +56,12 @@ struct SplitPlan {
   size_t smem_syn = 0, smem_ana = 0;
   int ns_syn = 2, ns_ana = 2;  // pipeline stages
   int jb = 1;                 // latitude pairs per grid CTA
+  int fgrp = 3;               // FFT stages per shared-memory pass
+  size_t syn_stage_bytes = 0, syn_min_bytes = 0, ana_res_bytes = 0, ana_stage_bytes = 0, ana_min_bytes = 0, budget_bytes = 0;
 };
 
 struct SplitDev {
-  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb;
+  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb, fgrp;
   const int *ke16, *kp64, *ra16;
   const long *tS_off, *tA_off, *aS_off, *aSH_off;
   long tS_size, tA_size, aSP_size, aSH_size, aAP_size, aAH_size;
@@ -415,7 +417,7 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
     }
   }
   __syncthreads();
-  fft_inverse_dit<float2, true>(sm, 4 * JB, n, d.logn, t.tw);
+  fft_inverse_dit<float2, true>(sm, 4 * JB, n, d.logn, t.tw, sd.fgrp);
   const float g = static_cast<float>(d.g);
   for (int e = threadIdx.x; e < JB * n; e += blockDim.x) {
     const int pr = e >> d.logn, k = e & (n - 1);
@@ -443,7 +445,7 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
     rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
   __syncthreads();
-  fft_forward_dif<float2, true>(sm, 5 * JB, n, d.logn, t.tw);
+  fft_forward_dif<float2, true>(sm, 5 * JB, n, d.logn, t.tw, sd.fgrp);
   const float inv = 1.0f / n, hinv = 0.5f * inv;
   for (int m = threadIdx.x; m < M; m += blockDim.x) {
 #pragma unroll
@@ -804,6 +806,12 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
     sp.ns_ana = static_cast<int>(std::min<size_t>(SPLIT_MAX_STAGES, (budget - SPLIT_MARGIN - ana_res) / ana_stage));
   if (sp.ns_ana < 2) throw InvalidArgument("split precision: the analysis pipeline does not fit in shared memory");
   sp.smem_ana = std::max(ana_res + sp.ns_ana * ana_stage + SPLIT_MARGIN, static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float));
+  sp.syn_stage_bytes = syn_stage;
+  sp.syn_min_bytes = static_cast<size_t>(4 * 8 * sp.nbt * 33 * sizeof(float));
+  sp.ana_res_bytes = ana_res;
+  sp.ana_stage_bytes = ana_stage;
+  sp.ana_min_bytes = static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float);
+  sp.budget_bytes = budget;
 }
 
 inline SplitDev split_dev(const SplitPlan &sp) {
@@ -819,6 +827,7 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.rSP = sp.rSP;
   s.rSH = sp.rSH;
   s.jb = sp.jb;
+  s.fgrp = sp.fgrp;
   s.ke16 = sp.ke16_d.p;
   s.kp64 = sp.kp64_d.p;
   s.ra16 = sp.ra16_d.p;
