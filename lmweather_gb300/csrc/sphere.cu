@@ -1173,75 +1173,81 @@ void SphereEngine::autotune_split() {
   cudaEvent_t e0, e1;
   LMW_CUDA(cudaEventCreate(&e0));
   LMW_CUDA(cudaEventCreate(&e1));
+  auto launch = [&](int which) {
+    split_stage(d, tab32(*tab), sp, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, AC, fgrid.p, hsgrid.p, stream,
+                which);
+    g_launches += 1;
+  };
   auto timed = [&](int which) {
-    auto one = [&] {
-      split_stage(d, tab32(*tab), sp, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, AC, fgrid.p, hsgrid.p, stream,
-                  which);
-    };
-    one();
+    launch(which);
     LMW_CUDA(cudaEventRecord(e0, stream));
-    for (int r = 0; r < 3; r++) one();
+    for (int r = 0; r < 5; r++) launch(which);
     LMW_CUDA(cudaEventRecord(e1, stream));
     LMW_LAUNCH_CHECK();
     LMW_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
     LMW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    g_launches += 4;
     return static_cast<double>(ms);
   };
   ensure_packed();
-  // grid kernel
-  {
-    int bj = sp.jb, bf = sp.fgrp;
-    double best = 1e30;
-    for (int jb = SPLIT_JB_MAX; jb >= 1; jb /= 2) {
-      if (nh % jb) continue;
-      for (int fg = 3; fg >= 2; fg--) {
-        sp.jb = jb;
-        sp.fgrp = fg;
-        const double t = timed(1);
-        if (t < best) {
-          best = t;
-          bj = jb;
-          bf = fg;
-        }
-      }
-    }
-    sp.jb = bj;
-    sp.fgrp = bf;
+  // warm the device (clocks) on the default plan before any measurement
+  for (int r = 0; r < 10; r++)
+    for (int k = 0; k < 3; k++) launch(k);
+  struct Cand {
+    int which, jb, fg, ns;
+    size_t bytes;
+    double best;
+  };
+  std::vector<Cand> cands;
+  for (int jb = SPLIT_JB_MAX; jb >= 1; jb /= 2)
+    if (nh % jb == 0)
+      for (int fg = 3; fg >= 2; fg--) cands.push_back({1, jb, fg, 0, 0, 1e30});
+  for (int ns = 2; ns <= SPLIT_MAX_STAGES; ns++) {
+    const size_t bs = std::max(ns * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
+    if (bs <= sp.budget_bytes) cands.push_back({0, 0, 0, ns, bs, 1e30});
+    const size_t ba = std::max(sp.ana_res_bytes + ns * sp.ana_stage_bytes + SPLIT_MARGIN, sp.ana_min_bytes);
+    if (ba <= sp.budget_bytes) cands.push_back({2, 0, 0, ns, ba, 1e30});
   }
-  // synthesis and analysis pipeline depth
-  {
-    const int ns0 = sp.ns_syn, na0 = sp.ns_ana;
-    int bs = ns0, ba = na0;
-    double best_s = 1e30, best_a = 1e30;
-    for (int ns = 2; ns <= SPLIT_MAX_STAGES; ns++) {
-      const size_t bytes = std::max(ns * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
-      if (bytes > sp.budget_bytes) continue;
-      sp.ns_syn = ns;
-      sp.smem_syn = bytes;
-      const double t = timed(0);
-      if (t < best_s) {
-        best_s = t;
-        bs = ns;
-      }
+  const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana;
+  const size_t sms0 = sp.smem_syn, sma0 = sp.smem_ana;
+  auto apply = [&](const Cand &c) {
+    sp.jb = jb0;
+    sp.fgrp = fg0;
+    sp.ns_syn = nss0;
+    sp.smem_syn = sms0;
+    sp.ns_ana = nsa0;
+    sp.smem_ana = sma0;
+    if (c.which == 1) {
+      sp.jb = c.jb;
+      sp.fgrp = c.fg;
+    } else if (c.which == 0) {
+      sp.ns_syn = c.ns;
+      sp.smem_syn = c.bytes;
+    } else {
+      sp.ns_ana = c.ns;
+      sp.smem_ana = c.bytes;
     }
-    for (int ns = 2; ns <= SPLIT_MAX_STAGES; ns++) {
-      const size_t bytes = std::max(sp.ana_res_bytes + ns * sp.ana_stage_bytes + SPLIT_MARGIN, sp.ana_min_bytes);
-      if (bytes > sp.budget_bytes) continue;
-      sp.ns_ana = ns;
-      sp.smem_ana = bytes;
-      const double t = timed(2);
-      if (t < best_a) {
-        best_a = t;
-        ba = ns;
-      }
+  };
+  // two rounds in opposite orders; each candidate keeps its faster round
+  for (int round = 0; round < 2; round++)
+    for (size_t i = 0; i < cands.size(); i++) {
+      Cand &c = cands[round == 0 ? i : cands.size() - 1 - i];
+      apply(c);
+      c.best = std::min(c.best, timed(c.which));
     }
-    sp.ns_syn = bs;
-    sp.smem_syn = std::max(bs * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
-    sp.ns_ana = ba;
-    sp.smem_ana = std::max(sp.ana_res_bytes + ba * sp.ana_stage_bytes + SPLIT_MARGIN, sp.ana_min_bytes);
-  }
+  auto pick = [&](int which) -> const Cand * {
+    const Cand *b = nullptr;
+    for (const Cand &c : cands)
+      if (c.which == which && (!b || c.best < b->best)) b = &c;
+    return b;
+  };
+  const Cand *bg = pick(1), *bs = pick(0), *ba = pick(2);
+  sp.jb = bg ? bg->jb : jb0;
+  sp.fgrp = bg ? bg->fg : fg0;
+  sp.ns_syn = bs ? bs->ns : nss0;
+  sp.smem_syn = bs ? bs->bytes : sms0;
+  sp.ns_ana = ba ? ba->ns : nsa0;
+  sp.smem_ana = ba ? ba->bytes : sma0;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   check_split_status();

@@ -579,6 +579,18 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
     }
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  // while two threads run the GEMM pipeline, the others ask L2 for the FP64 state lines the epilogue will read
+  if (threadIdx.x >= 64) {
+    for (int e = threadIdx.x - 64; e < mt * R; e += blockDim.x - 64) {
+      const int ml = e / R, r = e - ml * R;
+      const size_t base = static_cast<size_t>(tile * sd.nbt + ml) * 3 * d.ntri + d.tri[m] + s + 2 * r;
+#pragma unroll
+      for (int f = 0; f < 3; f++) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(x0 + base + static_cast<size_t>(f) * d.ntri));
+        if (sa.stage > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(acc + base + static_cast<size_t>(f) * d.ntri));
+      }
+    }
+  }
   split_setup(&tslot, ncols, full, empty, &done, ns);
   const uint32_t tmem = tslot;
   TwoGemm G;
