@@ -79,6 +79,20 @@ int lmw_sphere_set_omega(lmw_sphere *s, int member, double omega);
 int lmw_sphere_set_diffusion(lmw_sphere *s, double nu4);
 /* Sphere::set_orography_grid (cpp/sphere.hpp:47, cpp/sphere.cpp:105-109) */
 int lmw_sphere_set_orography_grid(lmw_sphere *s, int member, const double *hs, size_t n);
+/* Sphere::set_tracer_grid (cpp/sphere.cpp:264-270): a passive tracer q from its grid (nlat*nlon, analysed as
+ * analyze_scalar does); the grid's synthesis becomes the reference of the tracer errors. FP64 precision only. The
+ * tracer is advected with the flow, dq = A(q delta) - D(U q, V q) (cpp/sphere.cpp:250-263), filtered like Phi. */
+int lmw_sphere_set_tracer_grid(lmw_sphere *s, int member, const double *q, size_t n);
+/* Sphere::set_advect_only (cpp/sphere.hpp:45): the flow is frozen (its tendencies are zero, the filter still
+ * applies) and only the tracer moves; run() then needs a tracer ("advect_only: set a tracer first") */
+int lmw_sphere_set_advect_only(lmw_sphere *s, int on);
+/* the tracer's spectrum in the reference layout ((T+1)^2 complex), its grid (Sphere::grid_tracer,
+ * cpp/sphere.cpp:283) and diagnostics: out[0] tracer_mean, out[1] tracer_mass (area mean of h q), out[2] l2 and
+ * out[3] linf error against the grid it was set from (cpp/sphere.cpp:271-284, 571-590) */
+int lmw_sphere_tracer_state(lmw_sphere *s, int member, double *q);
+int lmw_sphere_set_tracer_state(lmw_sphere *s, int member, const double *q);
+int lmw_sphere_tracer_grid(lmw_sphere *s, int member, double *out, size_t n);
+int lmw_sphere_tracer_diagnostics(lmw_sphere *s, int member, double *out);
 /* Sphere::add_mode (cpp/sphere.hpp:43, cpp/sphere.cpp:301-311) */
 int lmw_sphere_add_mode(lmw_sphere *s, int member, int n, int m, double amplitude, double mean_depth);
 /* Sphere::perturb (cpp/sphere.hpp:44, cpp/sphere.cpp:313-336) */

@@ -86,6 +86,12 @@ _SIGS = {
     "lmw_ensemble_member_diagnostics": (_I, [_P, _I, _DP]),
     "lmw_ensemble_member_grid": (_I, [_P, _I, _I, _DP, _SZ]),
     "lmw_sphere_split_plan": (_I, [_P, _IP]),
+    "lmw_sphere_set_tracer_grid": (_I, [_P, _I, _DP, _SZ]),
+    "lmw_sphere_set_advect_only": (_I, [_P, _I]),
+    "lmw_sphere_tracer_state": (_I, [_P, _I, _DP]),
+    "lmw_sphere_set_tracer_state": (_I, [_P, _I, _DP]),
+    "lmw_sphere_tracer_grid": (_I, [_P, _I, _DP, _SZ]),
+    "lmw_sphere_tracer_diagnostics": (_I, [_P, _I, _DP]),
     "lmw_ensemble_split_plan": (_I, [_P, _I, _IP]),
     "lmw_mlp_create": (_I, [_I, _I, _I, _I, _U64, _D, _PP]),
     "lmw_mlp_destroy": (_I, [_P]),
@@ -250,6 +256,31 @@ class Sphere:
     def turbulence(self, seed: int, mean_height=8000.0, max_wind=30.0, nforce=21, member: int = 0):
         _check(self._lib.lmw_sphere_turbulence(self._h, member, seed, mean_height, max_wind, nforce))
         return self
+
+    # ---- passive tracer (cpp/sphere.cpp:250-300), FP64 precision
+    def set_tracer_grid(self, q, member: int = 0):
+        q = _f64(q)
+        _check(self._lib.lmw_sphere_set_tracer_grid(self._h, member, _dp(q), q.size))
+        return self
+
+    def set_advect_only(self, on: bool = True):
+        _check(self._lib.lmw_sphere_set_advect_only(self._h, 1 if on else 0))
+        return self
+
+    def tracer_state(self, member: int = 0):
+        q = np.zeros(self.nspec, np.complex128)
+        _check(self._lib.lmw_sphere_tracer_state(self._h, member, _dp(q.view(np.float64))))
+        return q
+
+    def grid_tracer(self, member: int = 0):
+        out = np.zeros((self.nlat, self.nlon))
+        _check(self._lib.lmw_sphere_tracer_grid(self._h, member, _dp(out), out.size))
+        return out
+
+    def tracer_diagnostics(self, member: int = 0) -> dict:
+        out = np.zeros(4)
+        _check(self._lib.lmw_sphere_tracer_diagnostics(self._h, member, _dp(out)))
+        return dict(zip(("tracer_mean", "tracer_mass", "tracer_error_l2", "tracer_error_linf"), out.tolist()))
 
     def split_plan(self) -> dict:
         """The autotuned launch plan of the split path (zeros in the other precisions)."""

@@ -178,6 +178,38 @@ int lmw_sphere_set_orography_grid(lmw_sphere *s, int member, const double *hs, s
     s->e->set_orography(hs, n, member);
   });
 }
+int lmw_sphere_set_tracer_grid(lmw_sphere *s, int member, const double *q, size_t n) {
+  return SPH({
+    need(q != nullptr, "grid pointer is null");
+    s->e->set_tracer_grid(q, n, member);
+  });
+}
+int lmw_sphere_set_advect_only(lmw_sphere *s, int on) { return SPH(s->e->set_advect_only(on != 0)); }
+int lmw_sphere_tracer_state(lmw_sphere *s, int member, double *q) {
+  return SPH({
+    need(q != nullptr, "null buffer");
+    s->e->tracer_state(q, member);
+  });
+}
+int lmw_sphere_set_tracer_state(lmw_sphere *s, int member, const double *q) {
+  return SPH({
+    need(q != nullptr, "null buffer");
+    s->e->set_tracer_state(q, member);
+  });
+}
+int lmw_sphere_tracer_grid(lmw_sphere *s, int member, double *out, size_t n) {
+  return SPH({
+    need(out != nullptr, "null buffer");
+    if (n != s->e->ngrid()) throw lmw::InvalidArgument("grid size mismatch");
+    s->e->tracer_grid(out, member);
+  });
+}
+int lmw_sphere_tracer_diagnostics(lmw_sphere *s, int member, double *out) {
+  return SPH({
+    need(out != nullptr, "null buffer");
+    s->e->tracer_diagnostics(out, member);
+  });
+}
 int lmw_sphere_add_mode(lmw_sphere *s, int member, int n, int m, double amplitude, double mean_depth) {
   return SPH(s->e->add_mode(n, m, amplitude, mean_depth, member));
 }

@@ -126,6 +126,16 @@ class SphereEngine {
   void grid(int which, double *out, int member);
   void spectrum(double *ke, double *pe, int member);
   void enqueue_step(double dt);
+  // passive tracer q (cpp/sphere.cpp:250-263, 264-300), FP64 precision only: set from a grid per member, advected
+  // by the flow (or by a frozen flow in advect-only mode), filtered like Phi
+  bool has_tracer = false, advect_only = false;
+  void set_tracer_grid(const double *q, size_t n, int member);
+  void set_advect_only(bool on);
+  void tracer_grid(double *out, int member);
+  void tracer_state(double *q_ref_layout, int member);
+  void set_tracer_state(const double *q_ref_layout, int member);
+  // mean, mass (area mean of h q) and l2 / linf errors against the grid the tracer was set from
+  void tracer_diagnostics(double *out, int member);
   // device pointer of the packed spectral state [member][field][tri] complex128 (FP64 state accumulation)
   double *device_state() { return x0.p; }
   // to be called after the state was written through device_state() (repacks the split operands)
@@ -153,6 +163,9 @@ class SphereEngine {
   DevBuf<double> four, fold;
   DevBuf<float> four32, fold32;
   DevBuf<double> fgrid, hsgrid, refgrid, filt, diagrows;
+  DevBuf<double> tq0, tqs, tqacc, fourq, foldq, refq, tgrid;  // tracer state, stage input, accumulator; transforms
+  void ensure_tracer();
+  void tracer_stage(int stage, double dt, int part);
   std::vector<int> gflag_h;
   void upload_member_flags(int member);
   DevBuf<double> gridin;
@@ -170,6 +183,7 @@ class SphereEngine {
     cudaGraphExec_t exec;
   };
   std::vector<ChunkGraph> graphs;
+  void graphs_clear();
   void upload_filter(double dt);
   void launch_stage(int stage, double dt);
   void launch_chunk(double dt, int steps);

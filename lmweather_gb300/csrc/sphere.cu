@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, SphTab<R> 
   C2 kz = csub(bH, imul(aP, mm));
   C2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
   C2 kf = csub(vH, imul(uP, mm));
-  if (q == 0) kz = kd = kf = mk2(R(0), R(0));  // cpp/sphere.cpp:387-389
+  if (q == 0 || sa.zero) kz = kd = kf = mk2(R(0), R(0));  // cpp/sphere.cpp:387-389
   const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
   // the RK4 state accumulates in FP64 whatever the precision of the tendencies
   const double2 k[3] = {make_double2(kz.x, kz.y), make_double2(kd.x, kd.y), make_double2(kf.x, kf.y)};
@@ -584,6 +584,7 @@ double irwin_hall(uint64_t &st) {
 }  // namespace lmw
 
 #include "sphere_split.cuh"
+#include "sphere_tracer.cuh"
 
 namespace lmw {
 
@@ -1072,12 +1073,13 @@ void SphereEngine::upload_filter(double dt) {
 template <class R>
 static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage, double dt, const double *filt, const double2 *in,
                           typename V2<R>::type *four, typename V2<R>::type *fold, double2 *x0, double2 *xs, double2 *acc,
-                          const double *fgrid, const double *hsgrid, cudaStream_t stream, int which = -1) {
+                          const double *fgrid, const double *hsgrid, cudaStream_t stream, int which = -1, int zero = 0) {
   const size_t smem = 5 * static_cast<size_t>(fft_row<true>(d.nlon)) * sizeof(typename V2<R>::type);  // padded FFT rows
   StageArgs sa;
   sa.stage = stage;
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
   sa.filt = filt;
+  sa.zero = zero;
   if (which < 0 || which == 0) sph_synth<R><<<dim3((d.nh + 31) / 32, d.M, B), SYN_THREADS, 0, stream>>>(d, t, in, four);
   if (which < 0 || which == 1) sph_grid<R><<<dim3(d.nh, B), GRID_THREADS, smem, stream>>>(d, t, four, fgrid, hsgrid, fold);
   if (which < 0 || which == 2)
@@ -1107,7 +1109,16 @@ void SphereEngine::launch_stage(int stage, double dt) {
   SphDev d = make_sph(*this, *tab);
   const double2 *in = reinterpret_cast<const double2 *>(stage == 0 ? x0.p : xs.p);
   double2 *X0 = reinterpret_cast<double2 *>(x0.p), *XS = reinterpret_cast<double2 *>(xs.p), *AC = reinterpret_cast<double2 *>(acc.p);
-  if (p.precision == kFP64) {
+  if (p.precision == kFP64 && has_tracer) {
+    // the tracer's kernels read the flow's stage input and its synthesised winds before the flow's analysis
+    // overwrites the stage input
+    for (int k = 0; k < 3; k++) {
+      stage_kernels<double>(d, tab64(*tab), B, stage, dt, filt.p, in, reinterpret_cast<double2 *>(four.p), reinterpret_cast<double2 *>(fold.p),
+                            X0, XS, AC, fgrid.p, hsgrid.p, stream, k, advect_only ? 1 : 0);
+      tracer_stage(stage, dt, k);
+    }
+    g_launches += 6;
+  } else if (p.precision == kFP64) {
     stage_kernels<double>(d, tab64(*tab), B, stage, dt, filt.p, in, reinterpret_cast<double2 *>(four.p), reinterpret_cast<double2 *>(fold.p),
                           X0, XS, AC, fgrid.p, hsgrid.p, stream);
     g_launches += 3;
@@ -1121,6 +1132,153 @@ void SphereEngine::launch_stage(int stage, double dt) {
     g_launches += 3;
   }
   LMW_LAUNCH_CHECK();
+}
+
+// ------------------------------------------------------------------------------------------------ tracer
+void SphereEngine::ensure_tracer() {
+  if (p.precision != kFP64) throw InvalidArgument("the tracer is supported in FP64 precision only");
+  if (tq0.p) return;
+  const size_t nq = static_cast<size_t>(B) * ntri * 2;
+  tq0.alloc(nq);
+  tqs.alloc(nq);
+  tqacc.alloc(nq);
+  fourq.alloc(static_cast<size_t>(B) * nlat * 2 * M * 2);
+  foldq.alloc(static_cast<size_t>(B) * nh * TRC_SLOT * 2 * M * 2);
+  refq.alloc(static_cast<size_t>(B) * ngrid());
+  tgrid.alloc(static_cast<size_t>(B) * ngrid());
+  for (auto *b : {&tq0, &tqs, &tqacc, &fourq, &foldq, &refq, &tgrid}) b->zero(stream);
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  graphs_clear();
+}
+
+// part 0: q and delta synthesis, 1: grid products, 2: analysis and RK4 update of q
+void SphereEngine::tracer_stage(int stage, double dt, int part) {
+  SphDev d = make_sph(*this, *tab);
+  const double2 *in = reinterpret_cast<const double2 *>(stage == 0 ? x0.p : xs.p);
+  const double2 *qin = reinterpret_cast<const double2 *>(stage == 0 ? tq0.p : tqs.p);
+  if (part == 0) {
+    trc_synth<<<dim3((nh + 31) / 32, M, B), SYN_THREADS, 0, stream>>>(d, tab64(*tab), in, qin, reinterpret_cast<double2 *>(fourq.p));
+  } else if (part == 1) {
+    const size_t smem = 4 * static_cast<size_t>(fft_row<true>(nlon)) * sizeof(double2);
+    trc_grid<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, tab64(*tab), reinterpret_cast<const double2 *>(four.p),
+                                                          reinterpret_cast<const double2 *>(fourq.p), reinterpret_cast<double2 *>(foldq.p));
+  } else {
+    StageArgs sa;
+    sa.stage = stage;
+    sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
+    sa.filt = filt.p;
+    trc_analysis<<<dim3((ntri + 31) / 32, B), ANA_THREADS, 0, stream>>>(d, tab64(*tab), reinterpret_cast<const double2 *>(foldq.p), sa,
+                                                                        reinterpret_cast<double2 *>(tq0.p), reinterpret_cast<double2 *>(tqs.p),
+                                                                        reinterpret_cast<double2 *>(tqacc.p));
+  }
+  LMW_LAUNCH_CHECK();
+}
+
+// cpp/sphere.cpp:264-270: q from its grid (analysis), and the grid it was set from as the reference of the
+// tracer errors (its synthesis)
+void SphereEngine::set_tracer_grid(const double *qg, size_t n, int member) {
+  check_member(*this, member);
+  if (n != ngrid()) throw InvalidArgument("grid size mismatch");
+  ensure_tracer();
+  const HostTables &h = tab->host;
+  // analyze_scalar, cpp/sphere.cpp:138-149: spec_nm = sum_j w_j F_m(j) P_nm(j), F_m = FFT(row) / nlon
+  std::vector<cplx> spec(nspec_ref(), cplx(0, 0)), row(nlon);
+  for (int j = 0; j < nlat; j++) {
+    for (int k = 0; k < nlon; k++) row[k] = cplx(qg[static_cast<size_t>(j) * nlon + k], 0.0);
+    fft_host(row, -1);
+    for (int m = 0; m <= N; m++) {
+      const cplx fm = row[m] / static_cast<double>(nlon);
+      const cplx f = fm * h.w[j];
+      for (int nn = m; nn <= N; nn++) spec[static_cast<size_t>(m) * M + nn] += f * h.Pj(j, m, nn);
+    }
+  }
+  set_tracer_state(reinterpret_cast<const double *>(spec.data()), member);
+  std::vector<double> ref(ngrid());
+  h.synthesize(spec, ref);
+  LMW_CUDA(cudaMemcpy(refq.p + static_cast<size_t>(member) * ngrid(), ref.data(), ngrid() * sizeof(double), cudaMemcpyHostToDevice));
+}
+
+void SphereEngine::set_tracer_state(const double *qr, int member) {
+  check_member(*this, member);
+  ensure_tracer();
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  to_packed(qr, hstage.p);
+  LMW_CUDA(cudaMemcpy(tq0.p + static_cast<size_t>(member) * ntri * 2, hstage.p, static_cast<size_t>(ntri) * 2 * sizeof(double),
+                      cudaMemcpyHostToDevice));
+  if (!has_tracer) {
+    has_tracer = true;
+    graphs_clear();
+  }
+}
+
+void SphereEngine::set_advect_only(bool on) {
+  if (advect_only != on) graphs_clear();
+  advect_only = on;
+}
+
+void SphereEngine::tracer_state(double *qr, int member) {
+  check_member(*this, member);
+  if (!has_tracer) {
+    std::memset(qr, 0, nspec_ref() * 2 * sizeof(double));
+    return;
+  }
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  LMW_CUDA(cudaMemcpy(hstage.p, tq0.p + static_cast<size_t>(member) * ntri * 2, static_cast<size_t>(ntri) * 2 * sizeof(double),
+                      cudaMemcpyDeviceToHost));
+  from_packed(hstage.p, qr);
+}
+
+void SphereEngine::tracer_grid(double *out, int member) {
+  check_member(*this, member);
+  if (!has_tracer) {
+    std::memset(out, 0, ngrid() * sizeof(double));
+    return;
+  }
+  SphDev d = make_sph(*this, *tab);
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  const size_t fo = static_cast<size_t>(member) * nlat * 2 * M;
+  trc_synth<<<dim3((nh + 31) / 32, M, 1), SYN_THREADS, 0, stream>>>(d, tab64(*tab), reinterpret_cast<const double2 *>(x0.p) + static_cast<size_t>(member) * 3 * ntri,
+                                                                  reinterpret_cast<const double2 *>(tq0.p) + static_cast<size_t>(member) * ntri,
+                                                                  reinterpret_cast<double2 *>(fourq.p) + fo);
+  trc_to_grid<<<dim3(nh, 1), GRID_THREADS, static_cast<size_t>(nlon) * sizeof(double2), stream>>>(
+      d, reinterpret_cast<const double2 *>(fourq.p) + fo, tgrid.p + static_cast<size_t>(member) * ngrid());
+  LMW_LAUNCH_CHECK();
+  g_launches += 2;
+  LMW_CUDA(cudaMemcpyAsync(out, tgrid.p + static_cast<size_t>(member) * ngrid(), ngrid() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+}
+
+// cpp/sphere.cpp:271-284 and 571-590: out[0] mean, out[1] mass = area mean of h q, out[2] l2, out[3] linf error
+// against the grid the tracer was set from
+void SphereEngine::tracer_diagnostics(double *out, int member) {
+  check_member(*this, member);
+  std::vector<double> q(ngrid()), hgt(ngrid()), ref(ngrid(), 0.0);
+  tracer_grid(q.data(), member);
+  grid(0, hgt.data(), member);
+  if (has_tracer)
+    LMW_CUDA(cudaMemcpy(ref.data(), refq.p + static_cast<size_t>(member) * ngrid(), ngrid() * sizeof(double), cudaMemcpyDeviceToHost));
+  double q00[2] = {0, 0};
+  if (has_tracer)
+    LMW_CUDA(cudaMemcpy(q00, tq0.p + static_cast<size_t>(member) * ntri * 2, sizeof(q00), cudaMemcpyDeviceToHost));
+  const HostTables &h = tab->host;
+  double sum = 0, num = 0, den = 0, mn = 0, mr = 0;
+  for (int j = 0; j < nlat; j++) {
+    double rowsum = 0;
+    for (int k = 0; k < nlon; k++) {
+      const size_t i = static_cast<size_t>(j) * nlon + k;
+      rowsum += hgt[i] * q[i];
+      const double dd = q[i] - ref[i];
+      num += h.w[j] * dd * dd;
+      den += h.w[j] * ref[i] * ref[i];
+      mn = std::max(mn, std::fabs(dd));
+      mr = std::max(mr, std::fabs(ref[i]));
+    }
+    sum += h.w[j] * rowsum / nlon;
+  }
+  out[0] = q00[0] / std::sqrt(2.0);
+  out[1] = 0.5 * sum;
+  out[2] = den > 0 ? std::sqrt(num / den) : 0.0;
+  out[3] = mr > 0 ? mn / mr : 0.0;
 }
 
 void SphereEngine::kernel_times(double dt, int reps, double *out) {
@@ -1278,6 +1436,11 @@ void SphereEngine::enqueue_step(double dt) {
   launches_step = 12;
 }
 
+void SphereEngine::graphs_clear() {
+  for (const ChunkGraph &cg : graphs) cudaGraphExecDestroy(cg.exec);
+  graphs.clear();
+}
+
 void SphereEngine::launch_chunk(double dt, int steps) {
   if (steps <= 0) return;
   upload_filter(dt);
@@ -1336,6 +1499,7 @@ void SphereEngine::reduce_guard_all() {
   sph_diag<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), fgrid.p, hsgrid.p, refgrid.p, diagrows.p,
                                                         nullptr);
   sph_diag_final<<<B, GRID_THREADS, 0, stream>>>(d, diagrows.p, reinterpret_cast<const double2 *>(x0.p), 0, dred.p);
+  if (has_tracer) trc_abs_sum<<<B, GRID_THREADS, 0, stream>>>(d, reinterpret_cast<const double2 *>(tq0.p), dred.p);
   LMW_LAUNCH_CHECK();
   g_launches += 2;
   LMW_CUDA(cudaMemcpyAsync(hred.p, dred.p, B * sizeof(Reduce), cudaMemcpyDeviceToHost, stream));
@@ -1346,7 +1510,8 @@ void SphereEngine::reduce_guard_all() {
 double SphereEngine::limit_from(const Reduce &r, int b, double safety) const {
   double hmax = std::max(0.0, r.max[1]);
   if (!(hmax > 0)) throw RuntimeError("the height field must be positive to step the model");
-  double omega = (N / p.radius) * (std::sqrt(p.gravity * hmax) + r.max[0]) + 2 * omega_m[b];
+  // cpp/sphere.cpp:438-447; advect-only: the frozen flow's advection alone
+  double omega = advect_only ? (N / p.radius) * r.max[0] : (N / p.radius) * (std::sqrt(p.gravity * hmax) + r.max[0]) + 2 * omega_m[b];
   if (!(omega > 0)) return 1e9;
   return safety / omega;
 }
@@ -1374,6 +1539,7 @@ double SphereEngine::stable_dt(double safety, int member) {
 SphereEngine::RunPlan SphereEngine::plan_run(double seconds, double dt) {
   RunPlan rp;
   if (!(seconds >= 0)) throw InvalidArgument("run: seconds must not be negative");
+  if (advect_only && !has_tracer) throw InvalidArgument("advect_only: set a tracer first (Sphere.tracer)");
   if (seconds == 0) return rp;
   if (!(dt > 0)) dt = stable_dt_all(1.5);
   const double limit = stable_dt_all(2.0 * std::sqrt(2.0));

@@ -49,6 +49,7 @@ struct StageArgs {
   int stage;        // 0..3
   double c;         // 0.5 dt, 0.5 dt, dt, dt/6
   const double *filt;  // [2][M]: zeta/delta and phi factors by n (last stage)
+  int zero = 0;        // advect-only: the flow's tendencies are zero (cpp/sphere.cpp:411-415)
 };
 
 }  // namespace
