@@ -636,7 +636,8 @@ static void allow_max_shared_memory() {
   LMW_CUDA(cudaFuncSetAttribute(sph_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(sph_grid_in, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_syn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_ana, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_ana<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_ana<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   done_for_device = dev;
 }
@@ -1102,7 +1103,10 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
     split_grid<<<dim3(d.nh / sp.jb, B), GRID_THREADS, 5 * static_cast<size_t>(sp.jb) * fft_row<true>(d.nlon) * sizeof(float2), stream>>>(d, t, sd, fgrid,
                                                                                                                                hsgrid);
   if (which < 0 || which == 2)
-    split_ana<<<dim3(d.M, 2, sp.ntiles), SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
+    if (sp.ana_both)
+      split_ana<true><<<dim3(d.M, 1, sp.ntiles), SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
+    else
+      split_ana<false><<<dim3(d.M, 2, sp.ntiles), SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
 }
 
 void SphereEngine::launch_stage(int stage, double dt) {
@@ -1363,10 +1367,12 @@ void SphereEngine::autotune_split() {
   for (int ns = 2; ns <= SPLIT_MAX_STAGES; ns++) {
     const size_t bs = std::max(ns * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
     if (bs <= sp.budget_bytes) cands.push_back({0, 0, 0, ns, bs, 1e30});
-    const size_t ba = std::max(sp.ana_res_bytes + ns * sp.ana_stage_bytes + SPLIT_MARGIN, sp.ana_min_bytes);
-    if (ba <= sp.budget_bytes) cands.push_back({2, 0, 0, ns, ba, 1e30});
+    for (int both = 0; both <= 1; both++) {
+      const size_t ba = std::max(sp.ana_res_bytes + ns * sp.ana_stage_bytes + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
+      if (ba <= sp.budget_bytes) cands.push_back({2, both, 0, ns, ba, 1e30});
+    }
   }
-  const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana;
+  const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both;
   const size_t sms0 = sp.smem_syn, sma0 = sp.smem_ana;
   auto apply = [&](const Cand &c) {
     sp.jb = jb0;
@@ -1375,6 +1381,7 @@ void SphereEngine::autotune_split() {
     sp.smem_syn = sms0;
     sp.ns_ana = nsa0;
     sp.smem_ana = sma0;
+    sp.ana_both = ab0;
     if (c.which == 1) {
       sp.jb = c.jb;
       sp.fgrp = c.fg;
@@ -1384,6 +1391,7 @@ void SphereEngine::autotune_split() {
     } else {
       sp.ns_ana = c.ns;
       sp.smem_ana = c.bytes;
+      sp.ana_both = c.jb;  // the analysis candidates carry the variant in jb
     }
   };
   // two rounds in opposite orders; each candidate keeps its faster round
@@ -1406,6 +1414,7 @@ void SphereEngine::autotune_split() {
   sp.smem_syn = bs ? bs->bytes : sms0;
   sp.ns_ana = ba ? ba->ns : nsa0;
   sp.smem_ana = ba ? ba->bytes : sma0;
+  sp.ana_both = ba ? ba->jb : ab0;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   check_split_status();
@@ -1417,6 +1426,7 @@ void SphereEngine::split_plan(int *out) const {
   out[1] = split ? split->fgrp : 0;
   out[2] = split ? split->ns_syn : 0;
   out[3] = split ? split->ns_ana : 0;
+  out[4] = split ? split->ana_both : 0;
 }
 
 // the split path keeps its synthesis operands packed from the state; pack them after a change from outside

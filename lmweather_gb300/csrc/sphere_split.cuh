@@ -57,7 +57,8 @@ struct SplitPlan {
   int ns_syn = 2, ns_ana = 2;  // pipeline stages
   int jb = 1;                 // latitude pairs per grid CTA
   int fgrp = 3;               // FFT stages per shared-memory pass
-  size_t syn_stage_bytes = 0, syn_min_bytes = 0, ana_res_bytes = 0, ana_stage_bytes = 0, ana_min_bytes = 0, budget_bytes = 0;
+  int ana_both = 0;           // analysis CTAs handle both parities of m
+  size_t syn_stage_bytes = 0, syn_min_bytes = 0, ana_res_bytes = 0, ana_stage_bytes = 0, ana_min_bytes = 0, ana_both_min_bytes = 0, budget_bytes = 0;
 };
 
 struct SplitDev {
@@ -198,8 +199,10 @@ struct TwoGemm {
   uint32_t acc[2][2];
 };
 
-__device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, uint8_t *pipe, uint64_t *full, uint64_t *empty, uint64_t *done,
-                             int *err) {
+// it0: iterations this CTA's pipeline already ran (a second call continues the barriers' phases); done_phase:
+// the phase of `done` this call completes
+__device__ __forceinline__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, uint8_t *pipe, uint64_t *full, uint64_t *empty, uint64_t *done,
+                             int *err, int it0 = 0, uint32_t done_phase = 0) {
   const int tid = threadIdx.x;
   const bool astream = G.a[0] != nullptr;
   const int a_bytes = astream ? G.aRmax * SPLIT_BK * 2 : 0;
@@ -212,8 +215,9 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
   if (tid == 0) {
     // producer: bulk copies of each (operand, chunk)
     for (int it = 0; it < total; it++) {
-      const int st = it % ns, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
-      if (it >= ns && !mbar_wait_bounded(su32(&empty[st]), ((it / ns) - 1) & 1)) {
+      const int git = it0 + it;
+      const int st = git % ns, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
+      if (git >= ns && !mbar_wait_bounded(su32(&empty[st]), ((git / ns) - 1) & 1)) {
         s_fail = 1;
         atomicExch(err, 2);
         break;
@@ -236,8 +240,9 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
     bool started[2][2] = {{false, false}, {false, false}};
     bool ok = true;
     for (int it = 0; it < total && ok; it++) {
-      const int st = it % ns, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
-      if (!mbar_wait_bounded(su32(&full[st]), (it / ns) & 1)) {
+      const int git = it0 + it;
+      const int st = git % ns, g = it < G.nchunk[0] ? 0 : 1, c = g == 0 ? it : it - G.nchunk[0];
+      if (!mbar_wait_bounded(su32(&full[st]), (git / ns) & 1)) {
         s_fail = 1;
         atomicExch(err, 3);
         ok = false;
@@ -267,7 +272,7 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
     if (ok) asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(done)) : "memory");
   }
   __syncthreads();
-  if (s_fail == 0 && tid == 0 && !mbar_wait_bounded(su32(done), 0)) {
+  if (s_fail == 0 && tid == 0 && !mbar_wait_bounded(su32(done), done_phase)) {
     s_fail = 1;
     atomicExch(err, 4);
   }
@@ -514,23 +519,47 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict
 }
 
 // ------------------------------------------------------------------------------------------- analysis + RK4
-// grid: (M, 2, ntiles). D columns: H at [0, ra16), P at [ra16, 2 ra16)
+// BOTH = false: grid (M, 2, ntiles), one parity s = blockIdx.y per CTA. BOTH = true: grid (M, 1, ntiles), both
+// parities in one CTA one after the other (the GEMM pipeline's barriers continue their phases), so the epilogue
+// walks every n of m in order and the FP64 state is read and written with unit stride. Accumulator columns of
+// parity s: H at [cb_s, cb_s + ra_s), P at [cb_s + ra_s, cb_s + 2 ra_s), cb_0 = 0, cb_1 = 2 ra_0 (BOTH).
+template <bool BOTH>
 __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
                                                              int B, int ns, double2 *x0, double2 *xs, double2 *acc) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
-  const int m = blockIdx.x, s = blockIdx.y, tile = blockIdx.z;
+  const int m = blockIdx.x, tile = blockIdx.z;
+  const int s_first = BOTH ? 0 : blockIdx.y, s_last = BOTH ? 1 : blockIdx.y;
   const int mt = min(sd.nbt, B - tile * sd.nbt);
-  const int R = s == 0 ? (d.N - m) / 2 + 1 : (d.N - m + 1) / 2;  // coefficients of this parity
-  if (R == 0) return;
-  const int ra16 = sd.ra16[2 * m + s];
+  const int R0 = (d.N - m) / 2 + 1, R1 = (d.N - m + 1) / 2;  // coefficients of each parity
+  if ((s_first ? R1 : R0) == 0) return;
+  const int ra0 = sd.ra16[2 * m], ra1 = sd.ra16[2 * m + 1];
+  const int cb1 = BOTH ? 2 * ra0 : 0;                               // cb_0 = 0
+  const int ld = BOTH ? 2 * (ra0 + ra1) : 2 * (s_first ? ra1 : ra0);  // accumulator columns (and dsm row length)
   uint32_t ncols = 32;
-  while (ncols < static_cast<uint32_t>(2 * ra16)) ncols <<= 1;
+  while (ncols < static_cast<uint32_t>(ld)) ncols <<= 1;
   const int nchunk = sd.nh64 / SPLIT_BK;
   // resident A operands: H (rAH rows) then P (rAP rows), every chunk and piece, in the chunk layout
   const int aH_bytes = sd.pieces * nchunk * sd.rAH * 128, aP_bytes = sd.pieces * nchunk * sd.rAP * 128;
   uint8_t *aH = smem, *aP = smem + aH_bytes, *pipe = smem + aH_bytes + aP_bytes;
+  // while two threads run the GEMM pipeline, the others ask L2 for the FP64 state lines the epilogue will read
+  if (threadIdx.x >= 64) {
+    const int cnt = BOTH ? d.N - m + 1 : (s_first ? R1 : R0);
+    for (int e = threadIdx.x - 64; e < mt * cnt; e += blockDim.x - 64) {
+      const int ml = e / cnt, j = e - ml * cnt;
+      const int off = BOTH ? j : s_first + 2 * j;
+      const size_t base = static_cast<size_t>(tile * sd.nbt + ml) * 3 * d.ntri + d.tri[m] + off;
+#pragma unroll
+      for (int f = 0; f < 3; f++) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(x0 + base + static_cast<size_t>(f) * d.ntri));
+        if (sa.stage > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(acc + base + static_cast<size_t>(f) * d.ntri));
+      }
+    }
+  }
+  bool ok = true;
+  for (int s = s_first; s <= s_last && ok; s++) {
+  if ((s ? R1 : R0) == 0) break;
   {
     // gather the folded grid values of this (m, s) into the resident A operands: P quantities a, b, u, e at
     // parity s and H quantities a, b, v at parity 1 - s. One work item = (member, quantity, 8 latitudes): eight
@@ -579,20 +608,10 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
     }
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  // while two threads run the GEMM pipeline, the others ask L2 for the FP64 state lines the epilogue will read
-  if (threadIdx.x >= 64) {
-    for (int e = threadIdx.x - 64; e < mt * R; e += blockDim.x - 64) {
-      const int ml = e / R, r = e - ml * R;
-      const size_t base = static_cast<size_t>(tile * sd.nbt + ml) * 3 * d.ntri + d.tri[m] + s + 2 * r;
-#pragma unroll
-      for (int f = 0; f < 3; f++) {
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(x0 + base + static_cast<size_t>(f) * d.ntri));
-        if (sa.stage > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(acc + base + static_cast<size_t>(f) * d.ntri));
-      }
-    }
-  }
-  split_setup(&tslot, ncols, full, empty, &done, ns);
+  if (s == s_first) split_setup(&tslot, ncols, full, empty, &done, ns);
+  else __syncthreads();
   const uint32_t tmem = tslot;
+  const int ra16 = s ? ra1 : ra0;
   TwoGemm G;
   G.a[0] = G.a[1] = nullptr;
   G.a_ps[0] = G.a_ps[1] = 0;
@@ -607,39 +626,43 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
   G.bR = ra16;
   G.nchunk[0] = G.nchunk[1] = nchunk;
   G.kseg[0] = G.kseg[1] = 1 << 30;
-  G.acc[0][0] = G.acc[0][1] = tmem;
-  G.acc[1][0] = G.acc[1][1] = tmem + ra16;
-  const bool ok = run_two_gemm(G, sd.pieces, sd.terms, ns, pipe, full, empty, &done, sd.err);
-  // accumulators -> shared memory [row][2 ra16] (the pipeline buffers are free now)
+  G.acc[0][0] = G.acc[0][1] = tmem + (s ? cb1 : 0);
+  G.acc[1][0] = G.acc[1][1] = tmem + (s ? cb1 : 0) + ra16;
+  ok = run_two_gemm(G, sd.pieces, sd.terms, ns, pipe, full, empty, &done, sd.err, (s - s_first) * 2 * nchunk, static_cast<uint32_t>(s - s_first));
+  }
+  const uint32_t tmem = tslot;
+  // accumulators -> shared memory [row][ld] (the operand and pipeline buffers are free now)
   float *dsm = reinterpret_cast<float *>(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = warp * 32 + lane;
   if (ok && warp * 32 < 8 * mt) {
     const uint32_t lanebase = tmem + (static_cast<uint32_t>(warp * 32) << 16);
     int c = 0;
-    for (; c + 32 <= 2 * ra16; c += 32) {
+    for (; c + 32 <= ld; c += 32) {
       float v[32];
       tmem_ld32(lanebase + c, v);
       if (row < 8 * mt) {
 #pragma unroll
-        for (int i = 0; i < 32; i++) dsm[row * (2 * ra16) + c + i] = v[i];
+        for (int i = 0; i < 32; i++) dsm[row * ld + c + i] = v[i];
       }
     }
-    for (; c < 2 * ra16; c += 8) {
+    for (; c < ld; c += 8) {
       float v[8];
       tmem_ld8(lanebase + c, v);
       if (row < 8 * mt) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) dsm[row * (2 * ra16) + c + i] = v[i];
+        for (int i = 0; i < 8; i++) dsm[row * ld + c + i] = v[i];
       }
     }
   }
   __syncthreads();
   if (ok) {
-    const int ld = 2 * ra16;
-    for (int e = threadIdx.x; e < mt * R; e += blockDim.x) {
-      const int ml = e / R, r = e - ml * R;
+    const int cnt = BOTH ? d.N - m + 1 : (s_first ? R1 : R0);
+    for (int e = threadIdx.x; e < mt * cnt; e += blockDim.x) {
+      const int ml = e / cnt, j = e - ml * cnt;
+      const int s = BOTH ? (j & 1) : s_first, r = BOTH ? (j >> 1) : j;
       const int b = tile * sd.nbt + ml, n = m + s + 2 * r;
-      const float *H = dsm + (ml * 6) * ld + r, *P = dsm + (ml * 8) * ld + ra16 + r;
+      const int cbs = s ? cb1 : 0, ras = s ? ra1 : ra0;
+      const float *H = dsm + (ml * 6) * ld + cbs + r, *P = dsm + (ml * 8) * ld + cbs + ras + r;
       const float2 aH = make_float2(H[0 * ld], H[1 * ld]), bH = make_float2(H[2 * ld], H[3 * ld]), vH = make_float2(H[4 * ld], H[5 * ld]);
       const float2 aP = make_float2(P[0 * ld], P[1 * ld]), bP = make_float2(P[2 * ld], P[3 * ld]);
       const float2 uP = make_float2(P[4 * ld], P[5 * ld]), eP = make_float2(P[6 * ld], P[7 * ld]);
@@ -823,6 +846,9 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   sp.ana_res_bytes = ana_res;
   sp.ana_stage_bytes = ana_stage;
   sp.ana_min_bytes = static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float);
+  int ra_pair = 32;
+  for (int m = 0; m <= N; m++) ra_pair = std::max(ra_pair, sp.ra16[2 * m] + sp.ra16[2 * m + 1]);
+  sp.ana_both_min_bytes = static_cast<size_t>(sp.rAP) * 2 * ra_pair * sizeof(float);
   sp.budget_bytes = budget;
 }
 
