@@ -79,6 +79,13 @@ int lmw_sphere_set_omega(lmw_sphere *s, int member, double omega);
 int lmw_sphere_set_diffusion(lmw_sphere *s, double nu4);
 /* Sphere::set_orography_grid (cpp/sphere.hpp:47, cpp/sphere.cpp:105-109) */
 int lmw_sphere_set_orography_grid(lmw_sphere *s, int member, const double *hs, size_t n);
+/* exact point values from the spectral state (Sphere::height_at, wind_at, vorticity_at, tracer_at,
+ * cpp/sphere.cpp:287-299, 592-637): which 0 height (m), 1 zonal wind u, 2 meridional wind v (m/s), 3 vorticity,
+ * 4 tracer; lat, lon in radians */
+int lmw_sphere_probe(lmw_sphere *s, int member, int which, double lat, double lon, double *out);
+/* Sphere::mode_coefficient (cpp/sphere.cpp:639-643) and Sphere::wave_crest (cpp/sphere.cpp:645-652) */
+int lmw_sphere_mode_coefficient(lmw_sphere *s, int member, int n, int m, int imag, double *out);
+int lmw_sphere_wave_crest(lmw_sphere *s, int member, int m, double lat, double *out);
 /* Sphere::set_tracer_grid (cpp/sphere.cpp:264-270): a passive tracer q from its grid (nlat*nlon, analysed as
  * analyze_scalar does); the grid's synthesis becomes the reference of the tracer errors. FP64 precision only. The
  * tracer is advected with the flow, dq = A(q delta) - D(U q, V q) (cpp/sphere.cpp:250-263), filtered like Phi. */

@@ -87,6 +87,9 @@ _SIGS = {
     "lmw_ensemble_member_grid": (_I, [_P, _I, _I, _DP, _SZ]),
     "lmw_sphere_split_plan": (_I, [_P, _IP]),
     "lmw_sphere_set_tracer_grid": (_I, [_P, _I, _DP, _SZ]),
+    "lmw_sphere_probe": (_I, [_P, _I, _I, _D, _D, _DP]),
+    "lmw_sphere_mode_coefficient": (_I, [_P, _I, _I, _I, _I, _DP]),
+    "lmw_sphere_wave_crest": (_I, [_P, _I, _I, _D, _DP]),
     "lmw_sphere_set_advect_only": (_I, [_P, _I]),
     "lmw_sphere_tracer_state": (_I, [_P, _I, _DP]),
     "lmw_sphere_set_tracer_state": (_I, [_P, _I, _DP]),
@@ -256,6 +259,34 @@ class Sphere:
     def turbulence(self, seed: int, mean_height=8000.0, max_wind=30.0, nforce=21, member: int = 0):
         _check(self._lib.lmw_sphere_turbulence(self._h, member, seed, mean_height, max_wind, nforce))
         return self
+
+    # ---- point probes (cpp/sphere.cpp:287-299, 592-652): exact synthesis at (lat, lon) in radians
+    def _probe(self, which, lat, lon, member):
+        out = _D()
+        _check(self._lib.lmw_sphere_probe(self._h, member, which, lat, lon, C.byref(out)))
+        return out.value
+
+    def height_at(self, lat: float, lon: float, member: int = 0) -> float:
+        return self._probe(0, lat, lon, member)
+
+    def wind_at(self, lat: float, lon: float, zonal: bool, member: int = 0) -> float:
+        return self._probe(1 if zonal else 2, lat, lon, member)
+
+    def vorticity_at(self, lat: float, lon: float, member: int = 0) -> float:
+        return self._probe(3, lat, lon, member)
+
+    def tracer_at(self, lat: float, lon: float, member: int = 0) -> float:
+        return self._probe(4, lat, lon, member)
+
+    def mode_coefficient(self, n: int, m: int, imag: bool = False, member: int = 0) -> float:
+        out = _D()
+        _check(self._lib.lmw_sphere_mode_coefficient(self._h, member, n, m, 1 if imag else 0, C.byref(out)))
+        return out.value
+
+    def wave_crest(self, m: int, lat: float, member: int = 0) -> float:
+        out = _D()
+        _check(self._lib.lmw_sphere_wave_crest(self._h, member, m, lat, C.byref(out)))
+        return out.value
 
     # ---- passive tracer (cpp/sphere.cpp:250-300), FP64 precision
     def set_tracer_grid(self, q, member: int = 0):

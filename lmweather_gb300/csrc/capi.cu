@@ -178,6 +178,24 @@ int lmw_sphere_set_orography_grid(lmw_sphere *s, int member, const double *hs, s
     s->e->set_orography(hs, n, member);
   });
 }
+int lmw_sphere_probe(lmw_sphere *s, int member, int which, double lat, double lon, double *out) {
+  return SPH({
+    need(out != nullptr, "null buffer");
+    *out = s->e->probe(which, lat, lon, member);
+  });
+}
+int lmw_sphere_mode_coefficient(lmw_sphere *s, int member, int n, int m, int imag, double *out) {
+  return SPH({
+    need(out != nullptr, "null buffer");
+    *out = s->e->mode_coefficient(n, m, imag != 0, member);
+  });
+}
+int lmw_sphere_wave_crest(lmw_sphere *s, int member, int m, double lat, double *out) {
+  return SPH({
+    need(out != nullptr, "null buffer");
+    *out = s->e->wave_crest(m, lat, member);
+  });
+}
 int lmw_sphere_set_tracer_grid(lmw_sphere *s, int member, const double *q, size_t n) {
   return SPH({
     need(q != nullptr, "grid pointer is null");

@@ -125,6 +125,12 @@ class SphereEngine {
   // which: 0 height, 1 u, 2 v, 3 vorticity
   void grid(int which, double *out, int member);
   void spectrum(double *ke, double *pe, int member);
+  // exact point values at (lat, lon) in radians from the spectral state (cpp/sphere.cpp:287-299, 592-637): which
+  // 0 height, 1 zonal wind u, 2 meridional wind v, 3 vorticity, 4 tracer
+  double probe(int which, double lat, double lon, int member);
+  // cpp/sphere.cpp:639-652: h's spectral component (n, m), and the longitude of a crest of h's zonal harmonic m
+  double mode_coefficient(int n, int m, bool imag, int member);
+  double wave_crest(int m, double lat, int member);
   void enqueue_step(double dt);
   // passive tracer q (cpp/sphere.cpp:250-263, 264-300), FP64 precision only: set from a grid per member, advected
   // by the flow (or by a frozen flow in advect-only mode), filtered like Phi

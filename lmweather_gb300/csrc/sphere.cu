@@ -1638,6 +1638,73 @@ void SphereEngine::grid(int which, double *out, int member) {
 }
 
 // cpp/sphere.cpp:536-551 (from the spectral state)
+// ------------------------------------------------------------------------------------------------ point probes
+double SphereEngine::probe(int which, double lat, double lon, int member) {
+  check_member(*this, member);
+  if (which < 0 || which > 4) throw InvalidArgument("probe: which must be 0 (height), 1 (u), 2 (v), 3 (vorticity) or 4 (tracer)");
+  if (which == 4 && !has_tracer) throw RuntimeError("no tracer: set one with tracer() first");
+  const size_t ns = nspec_ref() * 2;
+  std::vector<double> z(ns), dl(ns), f(ns), q(ns);
+  get_state(z.data(), dl.data(), f.data(), member);
+  if (which == 4) tracer_state(q.data(), member);
+  auto at = [&](const std::vector<double> &v, int m, int n) { return cplx(v[2 * (static_cast<size_t>(m) * M + n)], v[2 * (static_cast<size_t>(m) * M + n) + 1]); };
+  const double mu = std::sin(lat), a = p.radius;
+  std::vector<double> col;
+  double sum = 0;
+  for (int m = 0; m <= N; m++) {
+    legendre_column(m, N, mu, col);
+    cplx g(0, 0);
+    if (which == 1 || which == 2) {
+      cplx sp(0, 0), sc(0, 0), hp(0, 0), hc(0, 0);
+      for (int n = std::max(m, 1); n <= N; n++) {
+        const double k = -a * a / (n * (n + 1.0));
+        const double P = col[n - m];
+        const double H = -n * legendre_eps(n + 1, m) * col[n + 1 - m] + (n > m ? (n + 1) * legendre_eps(n, m) * col[n - 1 - m] : 0.0);
+        const cplx ps = at(z, m, n) * k, ch = at(dl, m, n) * k;
+        sp += ps * P;
+        sc += ch * P;
+        hp += ps * H;
+        hc += ch * H;
+      }
+      const cplx im(0, static_cast<double>(m));
+      g = which == 1 ? (im * sc - hp) / a : (im * sp + hc) / a;
+    } else {
+      const std::vector<double> &src = which == 0 ? f : (which == 3 ? z : q);
+      for (int n = m; n <= N; n++) g += at(src, m, n) * col[n - m];
+    }
+    sum += (m == 0 ? 1.0 : 2.0) * (g * std::exp(cplx(0, m * lon))).real();
+  }
+  if (which == 0) return sum / p.gravity;
+  if (which == 1 || which == 2) return sum / std::cos(lat);
+  return sum;
+}
+
+double SphereEngine::mode_coefficient(int n, int m, bool imag, int member) {
+  check_member(*this, member);
+  if (m < 0 || n < m || n > N) throw InvalidArgument("mode (n, m) outside the truncation");
+  const size_t ns = nspec_ref() * 2;
+  std::vector<double> f(ns);
+  get_state(nullptr, nullptr, f.data(), member);
+  const size_t i = static_cast<size_t>(m) * M + n;
+  const cplx c = cplx(f[2 * i], f[2 * i + 1]) / p.gravity;
+  return imag ? c.imag() : c.real();
+}
+
+double SphereEngine::wave_crest(int m, double lat, int member) {
+  check_member(*this, member);
+  if (m < 1 || m > N) throw InvalidArgument("zonal wavenumber must be between 1 and the truncation");
+  const size_t ns = nspec_ref() * 2;
+  std::vector<double> f(ns), col;
+  get_state(nullptr, nullptr, f.data(), member);
+  legendre_column(m, N, std::sin(lat), col);
+  cplx g(0, 0);
+  for (int n = m; n <= N; n++) {
+    const size_t i = static_cast<size_t>(m) * M + n;
+    g += cplx(f[2 * i], f[2 * i + 1]) * col[n - m];
+  }
+  return -std::arg(g) / m;
+}
+
 void SphereEngine::spectrum(double *ke, double *pe, int member) {
   std::vector<double> z(2 * nspec_ref()), dd(2 * nspec_ref()), ph(2 * nspec_ref());
   get_state(z.data(), dd.data(), ph.data(), member);

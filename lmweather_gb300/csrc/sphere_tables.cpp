@@ -36,6 +36,8 @@ void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
   }
 }
 
+double legendre_eps(int n, int m) { return eps_nm(n, m); }
+
 void legendre_column(int m, int nmax, double mu, std::vector<double> &out) {
   out.assign(static_cast<size_t>(nmax + 2 - m), 0.0);
   double c = std::sqrt(std::max(0.0, 1 - mu * mu)), p = 1 / std::sqrt(2.0);

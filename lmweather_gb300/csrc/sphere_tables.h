@@ -14,6 +14,8 @@ using cplx = std::complex<double>;
 void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w);
 // cpp/sphere.cpp:66-73, same arithmetic; out has nmax + 2 - m entries
 void legendre_column(int m, int nmax, double mu, std::vector<double> &out);
+// the recurrence coefficient of cpp/sphere.cpp:11
+double legendre_eps(int n, int m);
 // cpp/sphere.cpp:21-45 (radix-2, sign -1 forward, unnormalised)
 void fft_host(std::vector<cplx> &a, int sign);
 
