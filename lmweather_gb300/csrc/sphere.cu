@@ -188,7 +188,7 @@ __device__ __forceinline__ void dif_group(C2 *s, int rows, int n, int logn, int 
   }
 }
 // inverse transform (decimation in time) of `rows` rows in bit-reversed order, in place
-// fmax: stages per group (1..3)
+// fmax: stages per group (1..3; four-stage groups raise the kernels' register count and cost occupancy)
 template <class C2, bool PAD = false>
 __device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw, int fmax = 3) {
   for (int st = 0; st < logn;) {
