@@ -220,8 +220,9 @@ int lmw_ensemble_member_grid(lmw_ensemble *e, int member, int which, double *out
 int lmw_ensemble_stream(lmw_ensemble *e, int group, void **stream);
 /* the split path's launch plan as the engine's autotuner measured it at creation: out[0] latitude pairs per grid
  * CTA, out[1] FFT stages per shared-memory pass, out[2] synthesis and out[3] analysis pipeline stages, out[4] 1
- * when an analysis CTA handles both parities of m (zeros when the engine is not in split precision; out has 5
- * entries). No reference counterpart. */
+ * when an analysis CTA handles both parities of m, out[5] the analysis CTA count (0: one per work item; else
+ * persistent CTAs) (zeros when the engine is not in split precision; out has 6 entries). No reference
+ * counterpart. */
 int lmw_sphere_split_plan(lmw_sphere *s, int *out);
 int lmw_ensemble_split_plan(lmw_ensemble *e, int group, int *out);
 int lmw_ensemble_kernel_times(lmw_ensemble *e, int group, int reps, double *ms);

@@ -153,7 +153,8 @@ class SphereEngine {
   // engine stream): out[0] synthesis, out[1] grid (FFTs + products), out[2] analysis + RK4 update. x0 unchanged.
   void kernel_times(double dt, int reps, double *out);
   // the split path's measured launch plan: latitude pairs per grid CTA, FFT stages per pass, synthesis and
-  // analysis pipeline stages, both parities per analysis CTA (5 values; zeros without the split path)
+  // analysis pipeline stages, both parities per analysis CTA, analysis CTA count (6 values; zeros without the split
+  // path)
   void split_plan(int *out) const;
 
  private:

@@ -1103,10 +1103,14 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
     split_grid<<<dim3(d.nh / sp.jb, B), GRID_THREADS, 5 * static_cast<size_t>(sp.jb) * fft_row<true>(d.nlon) * sizeof(float2), stream>>>(d, t, sd, fgrid,
                                                                                                                                hsgrid);
   if (which < 0 || which == 2)
+  {
+    const int items = d.M * (sp.ana_both ? 1 : 2) * sp.ntiles;
+    const int grid = sp.ana_grid > 0 ? std::min(items, sp.ana_grid) : items;
     if (sp.ana_both)
-      split_ana<true><<<dim3(d.M, 1, sp.ntiles), SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
+      split_ana<true><<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
     else
-      split_ana<false><<<dim3(d.M, 2, sp.ntiles), SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
+      split_ana<false><<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
+  }
 }
 
 void SphereEngine::launch_stage(int stage, double dt) {
@@ -1323,7 +1327,7 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
 
 // Measured choice of the split path's launch plan: latitude pairs per grid CTA (4, 2, 1), FFT stages fused per
 // shared-memory pass (3 or 2), and the pipeline depth of the synthesis and analysis kernels (2-4 stages where
-// they fit). Each kernel is timed alone for every candidate (CUDA events on the engine stream, stage 1 on the
+// they fit) and the analysis variant (one parity or both per CTA). Each kernel is timed alone for every candidate (CUDA events on the engine stream, stage 1 on the
 // present state, which leaves the state unchanged); the arithmetic does not depend on the choice.
 void SphereEngine::autotune_split() {
   if (!split) return;
@@ -1369,10 +1373,12 @@ void SphereEngine::autotune_split() {
     if (bs <= sp.budget_bytes) cands.push_back({0, 0, 0, ns, bs, 1e30});
     for (int both = 0; both <= 1; both++) {
       const size_t ba = std::max(sp.ana_res_bytes + ns * sp.ana_stage_bytes + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
-      if (ba <= sp.budget_bytes) cands.push_back({2, both, 0, ns, ba, 1e30});
+      if (ba > sp.budget_bytes) continue;
+      // one CTA per work item (persistent CTAs, ana_grid > 0, measured no faster on GB300 and are not tried)
+      cands.push_back({2, both, 0, ns, ba, 1e30});
     }
   }
-  const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both;
+  const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both, ag0 = sp.ana_grid;
   const size_t sms0 = sp.smem_syn, sma0 = sp.smem_ana;
   auto apply = [&](const Cand &c) {
     sp.jb = jb0;
@@ -1382,6 +1388,7 @@ void SphereEngine::autotune_split() {
     sp.ns_ana = nsa0;
     sp.smem_ana = sma0;
     sp.ana_both = ab0;
+    sp.ana_grid = ag0;
     if (c.which == 1) {
       sp.jb = c.jb;
       sp.fgrp = c.fg;
@@ -1391,7 +1398,8 @@ void SphereEngine::autotune_split() {
     } else {
       sp.ns_ana = c.ns;
       sp.smem_ana = c.bytes;
-      sp.ana_both = c.jb;  // the analysis candidates carry the variant in jb
+      sp.ana_both = c.jb;  // the analysis candidates carry the variant in jb and the CTA count in fg
+      sp.ana_grid = c.fg;
     }
   };
   // two rounds in opposite orders; each candidate keeps its faster round
@@ -1415,6 +1423,7 @@ void SphereEngine::autotune_split() {
   sp.ns_ana = ba ? ba->ns : nsa0;
   sp.smem_ana = ba ? ba->bytes : sma0;
   sp.ana_both = ba ? ba->jb : ab0;
+  sp.ana_grid = ba ? ba->fg : ag0;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   check_split_status();
@@ -1427,6 +1436,7 @@ void SphereEngine::split_plan(int *out) const {
   out[2] = split ? split->ns_syn : 0;
   out[3] = split ? split->ns_ana : 0;
   out[4] = split ? split->ana_both : 0;
+  out[5] = split ? split->ana_grid : 0;
 }
 
 // the split path keeps its synthesis operands packed from the state; pack them after a change from outside

@@ -58,11 +58,13 @@ struct SplitPlan {
   int jb = 1;                 // latitude pairs per grid CTA
   int fgrp = 3;               // FFT stages per shared-memory pass
   int ana_both = 0;           // analysis CTAs handle both parities of m
+  int ana_grid = 0;           // analysis CTAs (0: one per work item)
+  int ra_pair = 32;           // largest ra16[2m] + ra16[2m + 1]
   size_t syn_stage_bytes = 0, syn_min_bytes = 0, ana_res_bytes = 0, ana_stage_bytes = 0, ana_min_bytes = 0, ana_both_min_bytes = 0, budget_bytes = 0;
 };
 
 struct SplitDev {
-  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb, fgrp;
+  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb, fgrp, ana_cols_one, ana_cols_both;
   const int *ke16, *kp64, *ra16;
   const long *tS_off, *tA_off, *aS_off, *aSH_off;
   long tS_size, tA_size, aSP_size, aSH_size, aAP_size, aAH_size;
@@ -201,7 +203,7 @@ struct TwoGemm {
 
 // it0: iterations this CTA's pipeline already ran (a second call continues the barriers' phases); done_phase:
 // the phase of `done` this call completes
-__device__ __forceinline__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, uint8_t *pipe, uint64_t *full, uint64_t *empty, uint64_t *done,
+__device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, uint8_t *pipe, uint64_t *full, uint64_t *empty, uint64_t *done,
                              int *err, int it0 = 0, uint32_t done_phase = 0) {
   const int tid = threadIdx.x;
   const bool astream = G.a[0] != nullptr;
@@ -529,20 +531,30 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
-  const int m = blockIdx.x, tile = blockIdx.z;
-  const int s_first = BOTH ? 0 : blockIdx.y, s_last = BOTH ? 1 : blockIdx.y;
-  const int mt = min(sd.nbt, B - tile * sd.nbt);
-  const int R0 = (d.N - m) / 2 + 1, R1 = (d.N - m + 1) / 2;  // coefficients of each parity
-  if ((s_first ? R1 : R0) == 0) return;
-  const int ra0 = sd.ra16[2 * m], ra1 = sd.ra16[2 * m + 1];
-  const int cb1 = BOTH ? 2 * ra0 : 0;                               // cb_0 = 0
-  const int ld = BOTH ? 2 * (ra0 + ra1) : 2 * (s_first ? ra1 : ra0);  // accumulator columns (and dsm row length)
+  // work items (m, parity or both, member tile), m fastest; a CTA takes items blockIdx.x, blockIdx.x + gridDim.x, ...
+  // with one TMEM allocation and one set of barriers whose phases continue from item to item
+  const int nitems = d.M * (BOTH ? 1 : 2) * sd.ntiles;
   uint32_t ncols = 32;
-  while (ncols < static_cast<uint32_t>(ld)) ncols <<= 1;
+  while (ncols < static_cast<uint32_t>(BOTH ? sd.ana_cols_both : sd.ana_cols_one)) ncols <<= 1;
   const int nchunk = sd.nh64 / SPLIT_BK;
   // resident A operands: H (rAH rows) then P (rAP rows), every chunk and piece, in the chunk layout
   const int aH_bytes = sd.pieces * nchunk * sd.rAH * 128, aP_bytes = sd.pieces * nchunk * sd.rAP * 128;
   uint8_t *aH = smem, *aP = smem + aH_bytes, *pipe = smem + aH_bytes + aP_bytes;
+  bool ok = true, setup_done = false;
+  int pipe_it = 0, calls = 0;
+  for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+  const int m = item % d.M, rest = item / d.M;
+  const int s_first = BOTH ? 0 : rest % 2, s_last = BOTH ? 1 : s_first;
+  const int tile = BOTH ? rest : rest / 2;
+  const int mt = min(sd.nbt, B - tile * sd.nbt);
+  const int R0 = (d.N - m) / 2 + 1, R1 = (d.N - m + 1) / 2;  // coefficients of each parity
+  if ((s_first ? R1 : R0) == 0) continue;
+  const int ra0 = sd.ra16[2 * m], ra1 = sd.ra16[2 * m + 1];
+  const int cb1 = BOTH ? 2 * ra0 : 0;                               // cb_0 = 0
+  const int ld = BOTH ? 2 * (ra0 + ra1) : 2 * (s_first ? ra1 : ra0);  // accumulator columns (and dsm row length)
+  // the previous item's epilogue has finished reading shared memory and tensor memory
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
   // while two threads run the GEMM pipeline, the others ask L2 for the FP64 state lines the epilogue will read
   if (threadIdx.x >= 64) {
     const int cnt = BOTH ? d.N - m + 1 : (s_first ? R1 : R0);
@@ -557,7 +569,6 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
       }
     }
   }
-  bool ok = true;
   for (int s = s_first; s <= s_last && ok; s++) {
   if ((s ? R1 : R0) == 0) break;
   {
@@ -608,8 +619,12 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
     }
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  if (s == s_first) split_setup(&tslot, ncols, full, empty, &done, ns);
-  else __syncthreads();
+  if (!setup_done) {
+    split_setup(&tslot, ncols, full, empty, &done, ns);
+    setup_done = true;
+  } else {
+    __syncthreads();
+  }
   const uint32_t tmem = tslot;
   const int ra16 = s ? ra1 : ra0;
   TwoGemm G;
@@ -628,7 +643,9 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
   G.kseg[0] = G.kseg[1] = 1 << 30;
   G.acc[0][0] = G.acc[0][1] = tmem + (s ? cb1 : 0);
   G.acc[1][0] = G.acc[1][1] = tmem + (s ? cb1 : 0) + ra16;
-  ok = run_two_gemm(G, sd.pieces, sd.terms, ns, pipe, full, empty, &done, sd.err, (s - s_first) * 2 * nchunk, static_cast<uint32_t>(s - s_first));
+  ok = run_two_gemm(G, sd.pieces, sd.terms, ns, pipe, full, empty, &done, sd.err, pipe_it, static_cast<uint32_t>(calls & 1));
+  pipe_it += 2 * nchunk;
+  calls++;
   }
   const uint32_t tmem = tslot;
   // accumulators -> shared memory [row][ld] (the operand and pipeline buffers are free now)
@@ -697,7 +714,8 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
       pack_syn_coef(d, sd, kfac, b, m, n, nv[0], nv[1], nv[2]);
     }
   }
-  split_teardown(tmem, ncols);
+  }
+  if (setup_done) split_teardown(tslot, ncols);
 }
 
 }  // namespace
@@ -846,9 +864,8 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   sp.ana_res_bytes = ana_res;
   sp.ana_stage_bytes = ana_stage;
   sp.ana_min_bytes = static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float);
-  int ra_pair = 32;
-  for (int m = 0; m <= N; m++) ra_pair = std::max(ra_pair, sp.ra16[2 * m] + sp.ra16[2 * m + 1]);
-  sp.ana_both_min_bytes = static_cast<size_t>(sp.rAP) * 2 * ra_pair * sizeof(float);
+  for (int m = 0; m <= N; m++) sp.ra_pair = std::max(sp.ra_pair, sp.ra16[2 * m] + sp.ra16[2 * m + 1]);
+  sp.ana_both_min_bytes = static_cast<size_t>(sp.rAP) * 2 * sp.ra_pair * sizeof(float);
   sp.budget_bytes = budget;
 }
 
@@ -866,6 +883,8 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.rSH = sp.rSH;
   s.jb = sp.jb;
   s.fgrp = sp.fgrp;
+  s.ana_cols_one = 2 * sp.ra_max;
+  s.ana_cols_both = 2 * sp.ra_pair;
   s.ke16 = sp.ke16_d.p;
   s.kp64 = sp.kp64_d.p;
   s.ra16 = sp.ra16_d.p;
