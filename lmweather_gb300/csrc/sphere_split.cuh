@@ -27,6 +27,7 @@
 
 #include "sphere_common.cuh"
 #include "sphere_tables.h"
+#include "tc_common.cuh"
 
 namespace lmw {
 
@@ -120,71 +121,16 @@ __device__ __forceinline__ void fsplit(float x, __nv_bfloat16 *out, long stride,
 }
 
 // ------------------------------------------------------------------------------------------- tcgen05 helpers
-__device__ __forceinline__ uint32_t su32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-__device__ __forceinline__ uint64_t gtimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-constexpr unsigned long long SPLIT_WAIT_NS = 2000000000ull;
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase) {
-  const uint64_t t0 = gtimer();
-  while (true) {
-    uint32_t done;
-    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-                 : "=r"(done)
-                 : "r"(bar), "r"(phase)
-                 : "memory");
-    if (done) return true;
-    if (gtimer() - t0 > SPLIT_WAIT_NS) return false;
-    __nanosleep(20);
-  }
-}
-// descriptor for the chunk layout: K-direction core matrices 128 B apart, 8-row groups 1024 B apart
-__device__ __forceinline__ uint64_t chunk_desc(uint32_t saddr) {
-  uint64_t d = static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
-  d |= static_cast<uint64_t>(128u >> 4) << 16;
-  d |= static_cast<uint64_t>(1024u >> 4) << 32;
-  d |= static_cast<uint64_t>(1) << 46;
-  return d;
-}
-__device__ __forceinline__ uint32_t idesc_m128(int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(128 >> 4) << 24);
-}
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst), "l"(src), "r"(bytes),
-               "r"(bar)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr)
-               : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,"
-      "%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]),
-        "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
-        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-        "=r"(r[31])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
+// (tc_common.cuh: bounded mbarrier waits, bulk copies, chunk-layout descriptors, TMEM loads)
+using tc::bulk_g2s;
+using tc::chunk_desc;
+using tc::gtimer;
+using tc::idesc_m128;
+using tc::su32;
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase) { return tc::wait(bar, phase); }
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) { tc::expect_tx(bar, bytes); }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) { tc::ld8(taddr, v); }
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) { tc::ld32(taddr, v); }
 
 // One CTA's two GEMMs (H then P). Operand g = 0 (H) / 1 (P): nchunk[g] K chunks of 64. A is either streamed
 // with B (a[g] != nullptr: chunk c of aR[g] rows at a[g] + c * aR[g] * 64, pieces a_ps[g] apart) or resident in

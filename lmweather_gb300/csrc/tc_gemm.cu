@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "tc_common.cuh"
 #include "tc_gemm.h"
 
 namespace lmw {
@@ -17,15 +18,8 @@ constexpr int A_TILE = 128 * BK * 2;
 constexpr int B_TILE_MAX = 256 * BK * 2;
 // three A pieces, three B pieces, plus slack so that no descriptor can address past the allocation
 constexpr int SMEM_BYTES = 3 * A_TILE + 3 * B_TILE_MAX + 16384;
-constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return tc::su32(p); }
 
 // shared-memory matrix descriptor: start address, leading (K-direction) and stride (8-row group) byte offsets,
 // descriptor version 1, no swizzle
@@ -41,21 +35,6 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t
 // instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N
 __device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);
-}
-
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, unsigned long long limit_ns) {
-  const uint64_t t0 = globaltimer();
-  while (true) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(phase)
-        : "memory");
-    if (done) return true;
-    if (globaltimer() - t0 > limit_ns) return false;
-    __nanosleep(32);
-  }
 }
 
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
@@ -138,10 +117,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&bar)) : "memory");
-      if (!mbar_wait(smem_u32(&bar), phase, WAIT_NS)) {
+      if (!tc::wait(smem_u32(&bar), phase)) {
         status = 1;
         atomicExch(err, 1);
-        mbar_wait(smem_u32(&bar), phase, WAIT_NS);  // give the MMAs in flight one more bounded chance
+        tc::wait(smem_u32(&bar), phase);  // give the MMAs in flight one more bounded chance
       }
     }
     phase ^= 1;
