@@ -526,8 +526,10 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
     const long sstride = static_cast<long>(B) * d.nh;  // between slots/parities of fold[m][slot][parity][member][jh]
     const float2 *gm = sd.fold + static_cast<long>(m) * 10 * sstride + static_cast<long>(tile * sd.nbt) * d.nh;
     const int nkb = sd.nh64 >> 3;
+    // consecutive threads take different operand rows of the same 8-latitude block: their 16-byte stores land in
+    // different rows of the core matrices (different banks)
     for (int e = threadIdx.x; e < mt * 7 * nkb; e += blockDim.x) {
-      const int kb = e % nkb, rest = e / nkb, qi = rest % 7, ml = rest / 7;
+      const int kb = e / (mt * 7), rest = e - kb * (mt * 7), qi = rest % 7, ml = rest / 7;
       // qi 0..3: P slots 0, 1, 2, 4 at parity s; 4..6: H slots 0, 1, 3 at parity 1 - s
       const int slot = qi < 3 ? qi : (qi == 3 ? 4 : (qi == 6 ? 3 : qi - 4));
       const int par = qi < 4 ? s : ph;
@@ -594,7 +596,9 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
   calls++;
   }
   const uint32_t tmem = tslot;
-  // accumulators -> shared memory [row][ld] (the operand and pipeline buffers are free now)
+  // accumulators -> shared memory [row][ld + 1] (the operand and pipeline buffers are free now); the odd row
+  // stride puts the rows that one warp writes at once on different banks
+  const int ldp = ld + 1;
   float *dsm = reinterpret_cast<float *>(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = warp * 32 + lane;
   if (ok && warp * 32 < 8 * mt) {
@@ -605,7 +609,7 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
       tmem_ld32(lanebase + c, v);
       if (row < 8 * mt) {
 #pragma unroll
-        for (int i = 0; i < 32; i++) dsm[row * ld + c + i] = v[i];
+        for (int i = 0; i < 32; i++) dsm[row * ldp + c + i] = v[i];
       }
     }
     for (; c < ld; c += 8) {
@@ -613,7 +617,7 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
       tmem_ld8(lanebase + c, v);
       if (row < 8 * mt) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) dsm[row * ld + c + i] = v[i];
+        for (int i = 0; i < 8; i++) dsm[row * ldp + c + i] = v[i];
       }
     }
   }
@@ -625,10 +629,10 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
       const int s = BOTH ? (j & 1) : s_first, r = BOTH ? (j >> 1) : j;
       const int b = tile * sd.nbt + ml, n = m + s + 2 * r;
       const int cbs = s ? cb1 : 0, ras = s ? ra1 : ra0;
-      const float *H = dsm + (ml * 6) * ld + cbs + r, *P = dsm + (ml * 8) * ld + cbs + ras + r;
-      const float2 aH = make_float2(H[0 * ld], H[1 * ld]), bH = make_float2(H[2 * ld], H[3 * ld]), vH = make_float2(H[4 * ld], H[5 * ld]);
-      const float2 aP = make_float2(P[0 * ld], P[1 * ld]), bP = make_float2(P[2 * ld], P[3 * ld]);
-      const float2 uP = make_float2(P[4 * ld], P[5 * ld]), eP = make_float2(P[6 * ld], P[7 * ld]);
+      const float *H = dsm + (ml * 6) * ldp + cbs + r, *P = dsm + (ml * 8) * ldp + cbs + ras + r;
+      const float2 aH = make_float2(H[0 * ldp], H[1 * ldp]), bH = make_float2(H[2 * ldp], H[3 * ldp]), vH = make_float2(H[4 * ldp], H[5 * ldp]);
+      const float2 aP = make_float2(P[0 * ldp], P[1 * ldp]), bP = make_float2(P[2 * ldp], P[3 * ldp]);
+      const float2 uP = make_float2(P[4 * ldp], P[5 * ldp]), eP = make_float2(P[6 * ldp], P[7 * ldp]);
       const float mm = static_cast<float>(m);
       // cpp/sphere.cpp:380-389
       float2 kz = csub(bH, imul(aP, mm));
@@ -799,19 +803,19 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   const size_t ana_stage = static_cast<size_t>(pieces) * ra_max * SPLIT_BK * 2;
   // two analysis CTAs per SM when a 3-stage pipeline fits in half of the shared memory
   const size_t half = SPLIT_HALF_SM;
-  if (ana_res + 3 * ana_stage + SPLIT_MARGIN <= half && static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float) <= half)
+  if (ana_res + 3 * ana_stage + SPLIT_MARGIN <= half && static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float) <= half)
     sp.ns_ana = 3;
   else
     sp.ns_ana = static_cast<int>(std::min<size_t>(SPLIT_MAX_STAGES, (budget - SPLIT_MARGIN - ana_res) / ana_stage));
   if (sp.ns_ana < 2) throw InvalidArgument("split precision: the analysis pipeline does not fit in shared memory");
-  sp.smem_ana = std::max(ana_res + sp.ns_ana * ana_stage + SPLIT_MARGIN, static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float));
+  sp.smem_ana = std::max(ana_res + sp.ns_ana * ana_stage + SPLIT_MARGIN, static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float));
   sp.syn_stage_bytes = syn_stage;
   sp.syn_min_bytes = static_cast<size_t>(4 * 8 * sp.nbt * 33 * sizeof(float));
   sp.ana_res_bytes = ana_res;
   sp.ana_stage_bytes = ana_stage;
-  sp.ana_min_bytes = static_cast<size_t>(sp.rAP) * 2 * ra_max * sizeof(float);
+  sp.ana_min_bytes = static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float);
   for (int m = 0; m <= N; m++) sp.ra_pair = std::max(sp.ra_pair, sp.ra16[2 * m] + sp.ra16[2 * m + 1]);
-  sp.ana_both_min_bytes = static_cast<size_t>(sp.rAP) * 2 * sp.ra_pair * sizeof(float);
+  sp.ana_both_min_bytes = static_cast<size_t>(sp.rAP) * (2 * sp.ra_pair + 1) * sizeof(float);
   sp.budget_bytes = budget;
 }
 
