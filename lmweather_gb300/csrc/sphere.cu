@@ -1098,12 +1098,13 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   sa.stage = stage;
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
   sa.filt = filt;
-  if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
+  if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles, sp.syn_split), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
   if (which < 0 || which == 1)
     split_grid<<<dim3(d.nh / sp.jb, B), GRID_THREADS, 5 * static_cast<size_t>(sp.jb) * fft_row<true>(d.nlon) * sizeof(float2), stream>>>(d, t, sd, fgrid,
                                                                                                                                hsgrid);
   if (which < 0 || which == 2)
   {
+    if (sp.ana_both && 2 * sp.ra_pair > 512) throw InvalidArgument("split precision: both parities' accumulators exceed tensor memory");
     const int items = d.M * (sp.ana_both ? 1 : 2) * sp.ntiles;
     const int grid = sp.ana_grid > 0 ? std::min(items, sp.ana_grid) : items;
     if (sp.ana_both)
@@ -1372,6 +1373,7 @@ void SphereEngine::autotune_split() {
     const size_t bs = std::max(ns * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
     if (bs <= sp.budget_bytes) cands.push_back({0, 0, 0, ns, bs, 1e30});
     for (int both = 0; both <= 1; both++) {
+      if (both && 2 * sp.ra_pair > 512) continue;  // both parities' accumulators must fit the 512 tensor-memory columns
       const size_t ba = std::max(sp.ana_res_bytes + ns * sp.ana_stage_bytes + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
       if (ba > sp.budget_bytes) continue;
       // one CTA per work item (persistent CTAs, ana_grid > 0, measured no faster on GB300 and are not tried)

@@ -57,6 +57,7 @@ struct SplitPlan {
   size_t smem_syn = 0, smem_ana = 0;
   int ns_syn = 2, ns_ana = 2;  // pipeline stages
   int jb = 1;                 // latitude pairs per grid CTA
+  int syn_nh = 16, syn_split = 1;  // latitudes per synthesis CTA and slices of nh16
   int fgrp = 3;               // FFT stages per shared-memory pass
   int ana_both = 0;           // analysis CTAs handle both parities of m
   int ana_grid = 0;           // analysis CTAs (0: one per work item)
@@ -65,7 +66,7 @@ struct SplitPlan {
 };
 
 struct SplitDev {
-  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb, fgrp, ana_cols_one, ana_cols_both;
+  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb, fgrp, ana_cols_one, ana_cols_both, syn_nh;
   const int *ke16, *kp64, *ra16;
   const long *tS_off, *tA_off, *aS_off, *aSH_off;
   long tS_size, tA_size, aSP_size, aSH_size, aAP_size, aAH_size;
@@ -142,6 +143,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) { tc::ld32(t
 struct TwoGemm {
   const __nv_bfloat16 *a[2], *b[2];
   long a_ps[2], b_ps[2];
+  long b_cs;  // elements between consecutive K chunks of B (bR * 64 unless B is a row slice of a wider table)
   uint32_t a_res[2];
   int aR[2], aRmax, bR, nchunk[2], kseg[2];
   uint32_t acc[2][2];
@@ -176,7 +178,7 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
       for (int p = 0; p < pieces; p++) {
         if (astream)
           bulk_g2s(su32(base + p * a_bytes), G.a[g] + p * G.a_ps[g] + static_cast<long>(c) * G.aR[g] * 64, abytes, su32(&full[st]));
-        bulk_g2s(su32(base + pieces * a_bytes + p * b_bytes), G.b[g] + p * G.b_ps[g] + static_cast<long>(c) * G.bR * 64, bbytes,
+        bulk_g2s(su32(base + pieces * a_bytes + p * b_bytes), G.b[g] + p * G.b_ps[g] + static_cast<long>(c) * G.b_cs, bbytes,
                  su32(&full[st]));
       }
     }
@@ -260,9 +262,11 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
+  // blockIdx.z: latitude slice [jh0, jh0 + nh16) of the table's sd.nh16 rows (two slices at T341, where four
+  // accumulators of all latitudes would exceed the 512 tensor-memory columns)
   const int m = blockIdx.x, tile = blockIdx.y;
   const int mt = min(sd.nbt, B - tile * sd.nbt);
-  const int nh16 = sd.nh16;
+  const int nh16 = sd.syn_nh, jh0 = blockIdx.z * nh16;
   uint32_t ncols = 32;
   while (ncols < static_cast<uint32_t>(4 * nh16)) ncols <<= 1;
   split_setup(&tslot, ncols, full, empty, &done, ns);
@@ -275,9 +279,10 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
   G.a_ps[0] = sd.aSH_size;
   G.a_ps[1] = sd.aSP_size;
   G.a_res[0] = G.a_res[1] = 0;
-  G.b[0] = sd.tS_H + sd.tS_off[m];
-  G.b[1] = sd.tS_P + sd.tS_off[m];
+  G.b[0] = sd.tS_H + sd.tS_off[m] + static_cast<long>(jh0) * 64;  // rows jh0.. of every chunk (8-row groups are 512 elements)
+  G.b[1] = sd.tS_P + sd.tS_off[m] + static_cast<long>(jh0) * 64;
   G.b_ps[0] = G.b_ps[1] = sd.tS_size;
+  G.b_cs = static_cast<long>(sd.nh16) * 64;
   G.aR[0] = sd.rSH;
   G.aR[1] = sd.rSP;
   G.aRmax = sd.rSP;
@@ -318,7 +323,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
     // south E + O, north O - E; U = (i m chi P - psi H) / a, V = (i m psi P + chi H) / a (cpp/sphere.cpp:200-201)
     const float mm = static_cast<float>(m), ia = static_cast<float>(1.0 / d.a);
     for (int e = threadIdx.x; e < mt * 32; e += blockDim.x) {
-      const int i = e & 31, ml = e >> 5, jh = cb + i;
+      const int i = e & 31, ml = e >> 5, jh = jh0 + cb + i;
       if (i >= wcols || jh >= d.nh) continue;
       const float *PE = tile_s + (2 * rows + ml * 8) * 33 + i, *PO = tile_s + (3 * rows + ml * 8) * 33 + i;
       const float *HE = tile_s + (0 * rows + ml * 4) * 33 + i, *HO = tile_s + (1 * rows + ml * 4) * 33 + i;
@@ -587,6 +592,7 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
   G.aR[1] = sd.rAP;
   G.aRmax = sd.rAP;
   G.bR = ra16;
+  G.b_cs = static_cast<long>(ra16) * 64;
   G.nchunk[0] = G.nchunk[1] = nchunk;
   G.kseg[0] = G.kseg[1] = 1 << 30;
   G.acc[0][0] = G.acc[0][1] = tmem + (s ? cb1 : 0);
@@ -673,13 +679,16 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
 // Pack the tables, size the operand buffers (once per engine).
 inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int terms) {
   const int N = h.N, M = h.M, nh = h.nh;
-  if (pad16(nh) * 4 > 512) throw InvalidArgument("split precision supports truncations up to 170 (the synthesis needs 4 x nlat/2 tensor-memory columns)");
+  // the synthesis keeps four accumulators of its latitudes in the 512 tensor-memory columns: slices of at most 128
+  if (pad16(nh) > 256) throw InvalidArgument("split precision supports truncations up to 341");
   sp.terms = terms;
   sp.pieces = terms == 6 ? 3 : 2;
   sp.nbt = std::min(B, SPLIT_NBT);
   sp.ntiles = (B + sp.nbt - 1) / sp.nbt;
   sp.nh16 = pad16(nh);
   sp.nh64 = pad64(nh);
+  sp.syn_split = 4 * sp.nh16 > 512 ? 2 : 1;
+  sp.syn_nh = sp.nh16 / sp.syn_split;
   sp.rSP = 8 * sp.nbt;
   sp.rSH = pad8(4 * sp.nbt);
   sp.rAP = 8 * sp.nbt;
@@ -780,7 +789,7 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   upl(sp.aSH_off_d, sp.aSH_off);
   const int pieces = sp.pieces;
   const size_t budget = 220 * 1024;
-  const size_t syn_stage = static_cast<size_t>(pieces) * (sp.rSP + sp.nh16) * SPLIT_BK * 2;
+  const size_t syn_stage = static_cast<size_t>(pieces) * (sp.rSP + sp.syn_nh) * SPLIT_BK * 2;
   // the pipeline never needs more stages than a CTA has chunks (two GEMMs of kp64 / 64 chunks); two CTAs per SM
   // when two stages fit in half of the shared memory
   int max_chunks = 0;
@@ -832,6 +841,7 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.rSP = sp.rSP;
   s.rSH = sp.rSH;
   s.jb = sp.jb;
+  s.syn_nh = sp.syn_nh;
   s.fgrp = sp.fgrp;
   s.ana_cols_one = 2 * sp.ra_max;
   s.ana_cols_both = 2 * sp.ra_pair;

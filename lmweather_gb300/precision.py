@@ -36,9 +36,6 @@ def study(T: int, days: float, seed: int = 1, modes=("fp64", "fp32", "split3", "
     out = {"truncation": T, "dt_s": dt, "days": days, "steps": int(round(seconds / dt)), "runs": {}}
     ref = None
     for name in modes:
-        if T > 170 and name.startswith("split"):
-            out["runs"][name] = {"unavailable": "the split path covers truncations up to 170"}
-            continue
         s = lw.Sphere(T, diffusion=nu, max_truncation=max(T, 170), **cfg[name])
         s.turbulence(seed, 8000.0, 30.0, T // 2)
         mu, w = s.gauss()
