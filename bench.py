@@ -462,6 +462,8 @@ def other_workloads(lw, lib, args, ens):
 
     res = study(170, 2.0)
     out.append({"config": "2: sphere T170 precision study, 2 model days at 240 s", **res})
+    res = study(341, 2.0)
+    out.append({"config": "2: sphere T341 precision study, 2 model days at 150 s", **res})
     # config 4: the learned surrogate at T42 (bounded: see surrogate_workload)
     out.append(surrogate_workload(lw))
     # the ensemble in the other precisions (one 2-day run each)
