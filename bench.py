@@ -17,7 +17,8 @@ FP32 accumulation, FP32 FFTs and products, FP64 state). Inputs are synthetic and
   cpu_baseline  the oracle (the reference algorithm restated in C) timed per member-step on every host core,
                 scaled to the workload's member-step counts
   workloads     the other configurations: T42 plain FP64 (config 0), the 1024 x 512 beta-plane (config 1), the
-                T170 precision study (config 2) and the ensemble in the other precisions
+                T170 and T341 precision studies (config 2), the learned surrogate (config 4, bounded training) and
+                the ensemble in the other precisions
 
 `--impl reference` times the reference's CPU algorithm (the oracle port: the reference checkout is absent on the
 GPU host) on the same workload with all host cores and prints the same line with "impl": "reference".
