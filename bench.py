@@ -210,11 +210,13 @@ def run_reference(args, rank, world):
         return 0
     build_oracle()
     cores = os.cpu_count() or 1
-    # member-step counts of the 2-day workload (per truncation: members x steps at the engine's stable step)
-    steps = {21: 512 * 186, 42: 384 * 341, 85: 128 * 640}
-    sample = {21: (6, 929.0), 42: (3, 506.7), 85: (1, 270.0)}
+    # member-step counts of the 2-day workload: members x steps at each group's stable step (the reference's
+    # stable_dt(1.5), smallest over the group, of the seeded initial states: T21 965.4 s, T42 528.4 s, T85 280.5 s,
+    # the same steps the GPU run takes)
+    steps = {21: 512 * 179, 42: 384 * 327, 85: 128 * 616}
+    sample = {21: (6, 965.4), 42: (3, 528.4), 85: (1, 280.5)}
     for _ in range(args.warmup):
-        cpu_ensemble_rate(steps, {21: (1, 929.0), 42: (1, 506.7), 85: (1, 270.0)}, cores)
+        cpu_ensemble_rate(steps, {21: (1, 965.4), 42: (1, 528.4), 85: (1, 280.5)}, cores)
     vals, costs = [], None
     for _ in range(args.steps):
         v, costs, _ = cpu_ensemble_rate(steps, sample, cores)
