@@ -221,7 +221,8 @@ int lmw_ensemble_stream(lmw_ensemble *e, int group, void **stream);
 /* the split path's launch plan as the engine's autotuner measured it at creation: out[0] latitude pairs per grid
  * CTA, out[1] FFT stages per shared-memory pass, out[2] synthesis and out[3] analysis pipeline stages, out[4] 1
  * when an analysis CTA handles both parities of m, out[5] the analysis CTA count (0: one per work item; else
- * persistent CTAs) (zeros when the engine is not in split precision; out has 6 entries). No reference
+ * persistent CTAs), out[6] 1 when the grid kernel writes the analysis operands (else the analysis gathers them
+ * from an FP32 fold) (zeros when the engine is not in split precision; out has 7 entries). No reference
  * counterpart. */
 int lmw_sphere_split_plan(lmw_sphere *s, int *out);
 int lmw_ensemble_split_plan(lmw_ensemble *e, int group, int *out);

@@ -315,10 +315,10 @@ class Sphere:
 
     def split_plan(self) -> dict:
         """The autotuned launch plan of the split path (zeros in the other precisions)."""
-        out = np.zeros(6, np.int32)
+        out = np.zeros(7, np.int32)
         _check(self._lib.lmw_sphere_split_plan(self._h, out.ctypes.data_as(_IP)))
         return dict(zip(("lat_pairs_per_grid_cta", "fft_stages_per_pass", "synthesis_stages", "analysis_stages", "analysis_both_parities",
-                                 "analysis_ctas"),
+                                 "analysis_ctas", "grid_writes_operands"),
                         out.tolist()))
 
     def get_state(self, member: int = 0):
@@ -554,10 +554,10 @@ class Ensemble:
 
     def split_plan(self, group: int) -> dict:
         """The autotuned launch plan of a truncation group's split path."""
-        out = np.zeros(6, np.int32)
+        out = np.zeros(7, np.int32)
         _check(self._lib.lmw_ensemble_split_plan(self._h, group, out.ctypes.data_as(_IP)))
         return dict(zip(("lat_pairs_per_grid_cta", "fft_stages_per_pass", "synthesis_stages", "analysis_stages", "analysis_both_parities",
-                                 "analysis_ctas"),
+                                 "analysis_ctas", "grid_writes_operands"),
                         out.tolist()))
 
     def member_state(self, i: int):

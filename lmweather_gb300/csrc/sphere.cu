@@ -636,9 +636,12 @@ static void allow_max_shared_memory() {
   LMW_CUDA(cudaFuncSetAttribute(sph_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(sph_grid_in, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_syn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_ana<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_ana<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_ana<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_ana<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_ana<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_ana<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   done_for_device = dev;
 }
 
@@ -1099,18 +1102,20 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
   sa.filt = filt;
   if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles, sp.syn_split), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
-  if (which < 0 || which == 1)
-    split_grid<<<dim3(d.nh / sp.jb, B), GRID_THREADS, 5 * static_cast<size_t>(sp.jb) * fft_row<true>(d.nlon) * sizeof(float2), stream>>>(d, t, sd, fgrid,
-                                                                                                                               hsgrid);
-  if (which < 0 || which == 2)
-  {
+  if (which < 0 || which == 1) {
+    const dim3 grid(d.nh / sp.jb, B);
+    const size_t bytes = 5 * static_cast<size_t>(sp.jb) * fft_row<true>(d.nlon) * sizeof(float2);
+    if (sp.direct)
+      split_grid<true><<<grid, GRID_THREADS, bytes, stream>>>(d, t, sd, fgrid, hsgrid);
+    else
+      split_grid<false><<<grid, GRID_THREADS, bytes, stream>>>(d, t, sd, fgrid, hsgrid);
+  }
+  if (which < 0 || which == 2) {
     if (sp.ana_both && 2 * sp.ra_pair > 512) throw InvalidArgument("split precision: both parities' accumulators exceed tensor memory");
     const int items = d.M * (sp.ana_both ? 1 : 2) * sp.ntiles;
     const int grid = sp.ana_grid > 0 ? std::min(items, sp.ana_grid) : items;
-    if (sp.ana_both)
-      split_ana<true><<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
-    else
-      split_ana<false><<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
+    auto *k = sp.ana_both ? (sp.direct ? split_ana<true, true> : split_ana<true, false>) : (sp.direct ? split_ana<false, true> : split_ana<false, false>);
+    k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
   }
 }
 
@@ -1361,26 +1366,34 @@ void SphereEngine::autotune_split() {
   for (int r = 0; r < 10; r++)
     for (int k = 0; k < 3; k++) launch(k);
   struct Cand {
-    int which, jb, fg, ns;
+    int which, jb, fg, ns, dir;
     size_t bytes;
     double best;
   };
   std::vector<Cand> cands;
-  for (int jb = SPLIT_JB_MAX; jb >= 1; jb /= 2)
-    if (nh % jb == 0)
-      for (int fg = 3; fg >= 2; fg--) cands.push_back({1, jb, fg, 0, 0, 1e30});
+  int dev = 0, optin = 0;
+  LMW_CUDA(cudaGetDevice(&dev));
+  LMW_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  // the grid and analysis candidates come in two variants of their interface (dir 1: the grid kernel writes the
+  // analysis operands, which the analysis streams; dir 0: FP32 fold, gathered by the analysis)
+  for (int dir = 1; dir >= 0; dir--)
+    for (int jb = SPLIT_JB_MAX; jb >= 1; jb /= 2)
+      if (nh % jb == 0 && 5 * static_cast<size_t>(jb) * fft_row<true>(nlon) * sizeof(float2) <= static_cast<size_t>(optin - 2048))
+        for (int fg = 3; fg >= 2; fg--) cands.push_back({1, jb, fg, 0, dir, 0, 1e30});
   for (int ns = 2; ns <= SPLIT_MAX_STAGES; ns++) {
     const size_t bs = std::max(ns * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
-    if (bs <= sp.budget_bytes) cands.push_back({0, 0, 0, ns, bs, 1e30});
-    for (int both = 0; both <= 1; both++) {
-      if (both && 2 * sp.ra_pair > 512) continue;  // both parities' accumulators must fit the 512 tensor-memory columns
-      const size_t ba = std::max(sp.ana_res_bytes + ns * sp.ana_stage_bytes + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
-      if (ba > sp.budget_bytes) continue;
-      // one CTA per work item (persistent CTAs, ana_grid > 0, measured no faster on GB300 and are not tried)
-      cands.push_back({2, both, 0, ns, ba, 1e30});
-    }
+    if (bs <= sp.budget_bytes) cands.push_back({0, 0, 0, ns, 0, bs, 1e30});
+    for (int dir = 1; dir >= 0; dir--)
+      for (int both = 0; both <= 1; both++) {
+        if (both && 2 * sp.ra_pair > 512) continue;  // both parities' accumulators must fit the 512 tensor-memory columns
+        const size_t ba = std::max(sp.ana_res_bytes_v[dir] + ns * sp.ana_stage_bytes_v[dir] + SPLIT_MARGIN,
+                                   both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
+        if (ba > sp.budget_bytes) continue;
+        // one CTA per work item (persistent CTAs, ana_grid > 0, measured no faster on GB300 and are not tried)
+        cands.push_back({2, both, 0, ns, dir, ba, 1e30});
+      }
   }
-  const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both, ag0 = sp.ana_grid;
+  const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both, ag0 = sp.ana_grid, dir0 = sp.direct;
   const size_t sms0 = sp.smem_syn, sma0 = sp.smem_ana;
   auto apply = [&](const Cand &c) {
     sp.jb = jb0;
@@ -1391,9 +1404,11 @@ void SphereEngine::autotune_split() {
     sp.smem_ana = sma0;
     sp.ana_both = ab0;
     sp.ana_grid = ag0;
+    sp.direct = dir0;
     if (c.which == 1) {
       sp.jb = c.jb;
       sp.fgrp = c.fg;
+      sp.direct = c.dir;
     } else if (c.which == 0) {
       sp.ns_syn = c.ns;
       sp.smem_syn = c.bytes;
@@ -1402,6 +1417,7 @@ void SphereEngine::autotune_split() {
       sp.smem_ana = c.bytes;
       sp.ana_both = c.jb;  // the analysis candidates carry the variant in jb and the CTA count in fg
       sp.ana_grid = c.fg;
+      sp.direct = c.dir;
     }
   };
   // two rounds in opposite orders; each candidate keeps its faster round
@@ -1411,13 +1427,24 @@ void SphereEngine::autotune_split() {
       apply(c);
       c.best = std::min(c.best, timed(c.which));
     }
-  auto pick = [&](int which) -> const Cand * {
+  auto pick = [&](int which, int dir) -> const Cand * {
     const Cand *b = nullptr;
     for (const Cand &c : cands)
-      if (c.which == which && (!b || c.best < b->best)) b = &c;
+      if (c.which == which && (which == 0 || c.dir == dir) && (!b || c.best < b->best)) b = &c;
     return b;
   };
-  const Cand *bg = pick(1), *bs = pick(0), *ba = pick(2);
+  // the interface variant with the lower grid + analysis time, then its best candidates
+  int dir = dir0;
+  double tbest = 1e30;
+  for (int v = 0; v <= 1; v++) {
+    const Cand *g = pick(1, v), *a = pick(2, v);
+    if (g && a && g->best + a->best < tbest) {
+      tbest = g->best + a->best;
+      dir = v;
+    }
+  }
+  const Cand *bg = pick(1, dir), *bs = pick(0, 0), *ba = pick(2, dir);
+  sp.direct = dir;
   sp.jb = bg ? bg->jb : jb0;
   sp.fgrp = bg ? bg->fg : fg0;
   sp.ns_syn = bs ? bs->ns : nss0;
@@ -1439,6 +1466,7 @@ void SphereEngine::split_plan(int *out) const {
   out[3] = split ? split->ns_ana : 0;
   out[4] = split ? split->ana_both : 0;
   out[5] = split ? split->ana_grid : 0;
+  out[6] = split ? split->direct : 0;
 }
 
 // the split path keeps its synthesis operands packed from the state; pack them after a change from outside

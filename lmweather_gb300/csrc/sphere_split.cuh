@@ -38,7 +38,7 @@ constexpr int SPLIT_MARGIN = 16384;  // an M = 128 MMA reads 16 KB past an A bas
 constexpr int SPLIT_THREADS = 128;
 constexpr int SPLIT_ANA_THREADS = 256;  // analysis: 8 warps for the gather and the RK4 epilogue, warps 0-3 read TMEM
 constexpr int SPLIT_NQ = 16;  // per (member, jh, m): U, V, zeta, Phi Fourier coefficients at the southern and northern latitude
-constexpr int SPLIT_JB_MAX = 4;  // latitude pairs per grid CTA
+constexpr int SPLIT_JB_MAX = 8;  // latitude pairs per grid CTA
 // dynamic shared memory per CTA when two CTAs share an SM (228 KB per SM, 1 KB reserved per CTA, static barriers)
 constexpr size_t SPLIT_HALF_SM = 115456;
 
@@ -59,10 +59,12 @@ struct SplitPlan {
   int jb = 1;                 // latitude pairs per grid CTA
   int syn_nh = 16, syn_split = 1;  // latitudes per synthesis CTA and slices of nh16
   int fgrp = 3;               // FFT stages per shared-memory pass
+  int direct = 1;             // the grid kernel writes the analysis operands (else the FP32 fold, gathered)
   int ana_both = 0;           // analysis CTAs handle both parities of m
   int ana_grid = 0;           // analysis CTAs (0: one per work item)
   int ra_pair = 32;           // largest ra16[2m] + ra16[2m + 1]
-  size_t syn_stage_bytes = 0, syn_min_bytes = 0, ana_res_bytes = 0, ana_stage_bytes = 0, ana_min_bytes = 0, ana_both_min_bytes = 0, budget_bytes = 0;
+  size_t syn_stage_bytes = 0, syn_min_bytes = 0, ana_min_bytes = 0, ana_both_min_bytes = 0, budget_bytes = 0;
+  size_t ana_res_bytes_v[2] = {0, 0}, ana_stage_bytes_v[2] = {0, 0};  // per variant: [0] gathered A, [1] streamed A
 };
 
 struct SplitDev {
@@ -346,14 +348,18 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
 }
 
 // ------------------------------------------------------------------------------------------- grid (FP32)
-// grid: (nh / jb, B). Fourier records of jb latitude pairs -> FFTs and products -> folded values, written to
-// fold[m][slot][parity][member][jh] (jb consecutive latitudes per store)
-__global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
+// grid: (nh / jb, B). Fourier records of jb latitude pairs -> FFTs and products -> folded values. DIRECT: written
+// as the analysis operands (BF16 pieces in the chunk layout, jb consecutive latitudes per store), which the
+// analysis streams with bulk copies; otherwise written m-major as FP32 fold[m][slot][parity][member][jh] (jb
+// latitudes per store), which the analysis gathers (cheaper for a few members, where jb is small)
+template <bool DIRECT>
+__global__ void __launch_bounds__(GRID_THREADS, 3) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
                                                            const double *__restrict__ hsgrid) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float2 *sm = reinterpret_cast<float2 *>(smraw);  // rows f * jb + p: U, V, zeta, Phi and the fifth product of pair p
-  const int JB = sd.jb, B = gridDim.y;
+  const int JB = sd.jb;
   const int b = blockIdx.y, jh0 = blockIdx.x * JB;
+  const int tile = b / sd.nbt, ml = b - tile * sd.nbt;
   const int n = d.nlon, M = d.M, rl = fft_row<true>(n);  // padded rows: element i at fft_at<true>(i)
   for (int e = threadIdx.x; e < 4 * JB * rl; e += blockDim.x) sm[e] = make_float2(0, 0);
   __syncthreads();
@@ -405,9 +411,10 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
   __syncthreads();
   fft_forward_dif<float2, true>(sm, 5 * JB, n, d.logn, t.tw, sd.fgrp);
   const float inv = 1.0f / n, hinv = 0.5f * inv;
-  for (int m = threadIdx.x; m < M; m += blockDim.x) {
-#pragma unroll
-    for (int r = 0; r < 5; r++) {
+  // one work item per (m, slot r): the folded values of this CTA's latitude pairs at both parities
+  for (int e = threadIdx.x; e < M * 5; e += blockDim.x) {
+    const int m = e % M, r = e / M;
+    {
       float2 f0[SPLIT_JB_MAX], f1[SPLIT_JB_MAX];
 #pragma unroll
       for (int pr = 0; pr < SPLIT_JB_MAX; pr++) {
@@ -424,19 +431,79 @@ __global__ void __launch_bounds__(GRID_THREADS) split_grid(SphDev d, SphTab<floa
         f0[pr] = cadd(Xs, Xn);
         f1[pr] = csub(Xs, Xn);
       }
-      float2 *o0 = sd.fold + ((static_cast<long>(m) * 10 + r * 2 + 0) * B + b) * d.nh + jh0;
-      float2 *o1 = sd.fold + ((static_cast<long>(m) * 10 + r * 2 + 1) * B + b) * d.nh + jh0;
-      if (JB == 4) {
-        reinterpret_cast<float4 *>(o0)[0] = make_float4(f0[0].x, f0[0].y, f0[1].x, f0[1].y);
-        reinterpret_cast<float4 *>(o0)[1] = make_float4(f0[2].x, f0[2].y, f0[3].x, f0[3].y);
-        reinterpret_cast<float4 *>(o1)[0] = make_float4(f1[0].x, f1[0].y, f1[1].x, f1[1].y);
-        reinterpret_cast<float4 *>(o1)[1] = make_float4(f1[2].x, f1[2].y, f1[3].x, f1[3].y);
-      } else {
+      if (!DIRECT) {
 #pragma unroll
-        for (int pr = 0; pr < SPLIT_JB_MAX; pr++) {
-          if (pr >= JB) break;
-          o0[pr] = f0[pr];
-          o1[pr] = f1[pr];
+        for (int par = 0; par < 2; par++) {
+          const float2 *fv = par ? f1 : f0;
+          float2 *o = sd.fold + ((static_cast<long>(m) * 10 + r * 2 + par) * gridDim.y + b) * d.nh + jh0;
+          if (JB >= 2) {
+#pragma unroll
+            for (int pr = 0; pr < SPLIT_JB_MAX; pr += 2) {
+              if (pr >= JB) break;
+              reinterpret_cast<float4 *>(o)[pr / 2] = make_float4(fv[pr].x, fv[pr].y, fv[pr + 1].x, fv[pr + 1].y);
+            }
+          } else {
+            o[0] = fv[0];
+          }
+        }
+        continue;
+      }
+      // the folded values go straight into the analysis operands (BF16 pieces, chunk layout): slot r at parity p
+      // is a P row of (m, s = p) for r = 0, 1, 2, 4 and an H row of (m, s = 1 - p) for r = 0, 1, 3
+#pragma unroll
+      for (int par = 0; par < 2; par++) {
+        const float2 *fv = par ? f1 : f0;
+#pragma unroll
+        for (int isH = 0; isH < 2; isH++) {
+          if (isH ? (r == 2 || r == 4) : (r == 3)) continue;
+          const int s_op = isH ? 1 - par : par;
+          const int R = isH ? sd.rAH : sd.rAP;
+          const int q = isH ? (r == 3 ? 2 : r) : (r == 4 ? 3 : r);
+          const int row0 = isH ? ml * 6 + 2 * q : ml * 8 + 2 * q;
+          __nv_bfloat16 *opnd = (isH ? sd.aA_H : sd.aA_P) + ((static_cast<long>(m) * 2 + s_op) * sd.ntiles + tile) * R * sd.nh64;
+          const long pstride = isH ? sd.aAH_size : sd.aAP_size;
+#pragma unroll
+          for (int ri = 0; ri < 2; ri++) {
+            __nv_bfloat16 pc[3][SPLIT_JB_MAX];
+#pragma unroll
+            for (int pr = 0; pr < SPLIT_JB_MAX; pr++) {
+              const float x = pr < JB ? (ri ? fv[pr].y : fv[pr].x) : 0.0f;
+              const __nv_bfloat16 h = __float2bfloat16_rn(x);
+              const float r1 = x - __bfloat162float(h);
+              const __nv_bfloat16 l = __float2bfloat16_rn(r1);
+              pc[0][pr] = h;
+              pc[1][pr] = l;
+              pc[2][pr] = __float2bfloat16_rn(r1 - __bfloat162float(l));
+            }
+            __nv_bfloat16 *dst = opnd + tile_off(row0 + ri, jh0, R);
+#pragma unroll
+            for (int pi = 0; pi < 3; pi++) {
+              if (pi >= sd.pieces) break;
+              __nv_bfloat16 *dp = dst + pi * pstride;
+              if (JB == 8) {
+                uint4 w;
+                __nv_bfloat16 *wp = reinterpret_cast<__nv_bfloat16 *>(&w);
+#pragma unroll
+                for (int j = 0; j < 8; j++) wp[j] = pc[pi][j];
+                *reinterpret_cast<uint4 *>(dp) = w;
+              } else if (JB == 4) {
+                uint2 w;
+                __nv_bfloat16 *wp = reinterpret_cast<__nv_bfloat16 *>(&w);
+                wp[0] = pc[pi][0];
+                wp[1] = pc[pi][1];
+                wp[2] = pc[pi][2];
+                wp[3] = pc[pi][3];
+                *reinterpret_cast<uint2 *>(dp) = w;
+              } else if (JB == 2) {
+                __nv_bfloat162 w;
+                w.x = pc[pi][0];
+                w.y = pc[pi][1];
+                *reinterpret_cast<__nv_bfloat162 *>(dp) = w;
+              } else {
+                dp[0] = pc[pi][0];
+              }
+            }
+          }
         }
       }
     }
@@ -476,7 +543,7 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict
 // parities in one CTA one after the other (the GEMM pipeline's barriers continue their phases), so the epilogue
 // walks every n of m in order and the FP64 state is read and written with unit stride. Accumulator columns of
 // parity s: H at [cb_s, cb_s + ra_s), P at [cb_s + ra_s, cb_s + 2 ra_s), cb_0 = 0, cb_1 = 2 ra_0 (BOTH).
-template <bool BOTH>
+template <bool BOTH, bool DIRECT>
 __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
                                                              int B, int ns, double2 *x0, double2 *xs, double2 *acc) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -487,9 +554,10 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
   const int nitems = d.M * (BOTH ? 1 : 2) * sd.ntiles;
   uint32_t ncols = 32;
   while (ncols < static_cast<uint32_t>(BOTH ? sd.ana_cols_both : sd.ana_cols_one)) ncols <<= 1;
+  // DIRECT: A operands streamed with the tables; otherwise gathered from the FP32 fold into resident shared memory
+  // (H rows then P rows, every chunk and piece, in the chunk layout) ahead of the pipeline buffers
   const int nchunk = sd.nh64 / SPLIT_BK;
-  // resident A operands: H (rAH rows) then P (rAP rows), every chunk and piece, in the chunk layout
-  const int aH_bytes = sd.pieces * nchunk * sd.rAH * 128, aP_bytes = sd.pieces * nchunk * sd.rAP * 128;
+  const int aH_bytes = DIRECT ? 0 : sd.pieces * nchunk * sd.rAH * 128, aP_bytes = DIRECT ? 0 : sd.pieces * nchunk * sd.rAP * 128;
   uint8_t *aH = smem, *aP = smem + aH_bytes, *pipe = smem + aH_bytes + aP_bytes;
   bool ok = true, setup_done = false;
   int pipe_it = 0, calls = 0;
@@ -522,7 +590,7 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
   }
   for (int s = s_first; s <= s_last && ok; s++) {
   if ((s ? R1 : R0) == 0) break;
-  {
+  if (!DIRECT) {
     // gather the folded grid values of this (m, s) into the resident A operands: P quantities a, b, u, e at
     // parity s and H quantities a, b, v at parity 1 - s. One work item = (member, quantity, 8 latitudes): eight
     // consecutive float2 loads, then one 16-byte store per (real/imaginary row, piece) into the chunk layout.
@@ -581,10 +649,18 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
   const uint32_t tmem = tslot;
   const int ra16 = s ? ra1 : ra0;
   TwoGemm G;
-  G.a[0] = G.a[1] = nullptr;
-  G.a_ps[0] = G.a_ps[1] = 0;
-  G.a_res[0] = su32(aH);
-  G.a_res[1] = su32(aP);
+  if (DIRECT) {
+    G.a[0] = sd.aA_H + ((static_cast<long>(m) * 2 + s) * sd.ntiles + tile) * sd.rAH * sd.nh64;
+    G.a[1] = sd.aA_P + ((static_cast<long>(m) * 2 + s) * sd.ntiles + tile) * sd.rAP * sd.nh64;
+    G.a_ps[0] = sd.aAH_size;
+    G.a_ps[1] = sd.aAP_size;
+    G.a_res[0] = G.a_res[1] = 0;
+  } else {
+    G.a[0] = G.a[1] = nullptr;
+    G.a_ps[0] = G.a_ps[1] = 0;
+    G.a_res[0] = su32(aH);
+    G.a_res[1] = su32(aP);
+  }
   G.b[0] = sd.tA_H + sd.tA_off[2 * m + s];
   G.b[1] = sd.tA_P + sd.tA_off[2 * m + s];
   G.b_ps[0] = G.b_ps[1] = sd.tA_size;
@@ -807,9 +883,15 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
       sp.jb = jb;
       break;
     }
+  // the analysis either gathers its A operands into resident shared memory (variant 0) or streams them with
+  // its tables (variant 1, the default for batches)
   const size_t nchunk = sp.nh64 / SPLIT_BK;
-  const size_t ana_res = static_cast<size_t>(pieces) * nchunk * (sp.rAH + sp.rAP) * 128;
-  const size_t ana_stage = static_cast<size_t>(pieces) * ra_max * SPLIT_BK * 2;
+  sp.ana_res_bytes_v[0] = static_cast<size_t>(pieces) * nchunk * (sp.rAH + sp.rAP) * 128;
+  sp.ana_stage_bytes_v[0] = static_cast<size_t>(pieces) * ra_max * SPLIT_BK * 2;
+  sp.ana_res_bytes_v[1] = 0;
+  sp.ana_stage_bytes_v[1] = static_cast<size_t>(pieces) * (sp.rAP + ra_max) * SPLIT_BK * 2;
+  sp.direct = sp.nbt >= 8 ? 1 : 0;
+  const size_t ana_res = sp.ana_res_bytes_v[sp.direct], ana_stage = sp.ana_stage_bytes_v[sp.direct];
   // two analysis CTAs per SM when a 3-stage pipeline fits in half of the shared memory
   const size_t half = SPLIT_HALF_SM;
   if (ana_res + 3 * ana_stage + SPLIT_MARGIN <= half && static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float) <= half)
@@ -820,8 +902,6 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   sp.smem_ana = std::max(ana_res + sp.ns_ana * ana_stage + SPLIT_MARGIN, static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float));
   sp.syn_stage_bytes = syn_stage;
   sp.syn_min_bytes = static_cast<size_t>(4 * 8 * sp.nbt * 33 * sizeof(float));
-  sp.ana_res_bytes = ana_res;
-  sp.ana_stage_bytes = ana_stage;
   sp.ana_min_bytes = static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float);
   for (int m = 0; m <= N; m++) sp.ra_pair = std::max(sp.ra_pair, sp.ra16[2 * m] + sp.ra16[2 * m + 1]);
   sp.ana_both_min_bytes = static_cast<size_t>(sp.rAP) * (2 * sp.ra_pair + 1) * sizeof(float);
