@@ -168,6 +168,19 @@ int lmw_plane_stable_dt(lmw_plane *p, double safety, double *out);
 int lmw_plane_time(const lmw_plane *p, double *out);
 /* Plane diagnostics (cpp/plane.cpp:191-243): out[4] = mean_depth, energy, max_speed, pv_anomaly_rms */
 int lmw_plane_diagnostics(lmw_plane *p, double *out);
+/* Plane::h_at / u_at / v_at (cpp/plane.hpp:49-51, cpp/plane.cpp:245-264): bilinear value of field `kind`
+ * (0 h, 1 u, 2 v) at (x, y) metres, each field on its own points, periodic in x, rows clamped; computed on the
+ * device (bitwise the reference's). A non-finite point is invalid_argument. */
+int lmw_plane_probe(lmw_plane *p, int kind, double x, double y, double *out);
+/* Plane::zeta_at_corner (cpp/plane.hpp:59, cpp/plane.cpp:220-226), corners i in 0..nx, j in 0..ny */
+int lmw_plane_zeta_at_corner(lmw_plane *p, int i, int j, double *out);
+/* Plane::zonal_amplitude / zonal_crest / v_zonal_crest / harmonic_energy (cpp/plane.hpp:52-58,
+ * cpp/plane.cpp:266-310): zonal harmonics of rows, summed on the device; invalid_argument with the
+ * reference's message when m or the row is out of range */
+int lmw_plane_zonal_amplitude(lmw_plane *p, int m, int j, double *out);
+int lmw_plane_zonal_crest(lmw_plane *p, int m, int j, double *out);
+int lmw_plane_v_zonal_crest(lmw_plane *p, int m, int j, double *out);
+int lmw_plane_harmonic_energy(lmw_plane *p, int m, double *out);
 /* the handle's CUDA stream (a cudaStream_t) */
 int lmw_plane_stream(const lmw_plane *p, void **stream);
 

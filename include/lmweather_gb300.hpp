@@ -282,6 +282,15 @@ class Plane {
     refresh();
   }
   double coriolis(double y) const { return p_.f0 + p_.beta * (y - 0.5 * p_.ly); }
+  // point and harmonic diagnostics (cpp/plane.hpp:49-59), computed on the device
+  double h_at(double x, double y) const { return scalar(lmw_plane_probe, 0, x, y); }
+  double u_at(double x, double y) const { return scalar(lmw_plane_probe, 1, x, y); }
+  double v_at(double x, double y) const { return scalar(lmw_plane_probe, 2, x, y); }
+  double zeta_at_corner(int i, int j) const { return scalar(lmw_plane_zeta_at_corner, i, j); }
+  double zonal_amplitude(int m, int j) const { return scalar(lmw_plane_zonal_amplitude, m, j); }
+  double zonal_crest(int m, int j) const { return scalar(lmw_plane_zonal_crest, m, j); }
+  double v_zonal_crest(int m, int j) const { return scalar(lmw_plane_v_zonal_crest, m, j); }
+  double harmonic_energy(int m) const { return scalar(lmw_plane_harmonic_energy, m); }
 
   lmw_plane *handle() const { return h_; }
 
@@ -300,6 +309,11 @@ class Plane {
     double out[4];
     check(lmw_plane_diagnostics(h_, out));
     return out[i];
+  }
+  template <class F, class... A> double scalar(F fn, A... args) const {
+    double out = 0;
+    check(fn(h_, args..., &out));
+    return out;
   }
 };
 

@@ -9,6 +9,7 @@ CPU fallback: without the compiled library (lmweather_gb300/_lib/liblmw_gb300.so
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 
 import numpy as np
@@ -77,6 +78,12 @@ _SIGS = {
     "lmw_plane_stable_dt": (_I, [_P, _D, _DP]),
     "lmw_plane_time": (_I, [_P, _DP]),
     "lmw_plane_diagnostics": (_I, [_P, _DP]),
+    "lmw_plane_probe": (_I, [_P, _I, _D, _D, _DP]),
+    "lmw_plane_zeta_at_corner": (_I, [_P, _I, _I, _DP]),
+    "lmw_plane_zonal_amplitude": (_I, [_P, _I, _I, _DP]),
+    "lmw_plane_zonal_crest": (_I, [_P, _I, _I, _DP]),
+    "lmw_plane_v_zonal_crest": (_I, [_P, _I, _I, _DP]),
+    "lmw_plane_harmonic_energy": (_I, [_P, _I, _DP]),
     "lmw_ensemble_create": (_I, [_I, _IP, C.POINTER(C.c_uint64), _DP, _DP, _D, _D, _D, _I, _I, _PP]),
     "lmw_ensemble_destroy": (_I, [_P]),
     "lmw_ensemble_run": (_I, [_P, _D]),
@@ -506,6 +513,61 @@ class Plane:
 
     def max_speed(self) -> float:
         return self.diagnostics()["max_speed"]
+
+    def pv_anomaly_rms(self) -> float:
+        return self.diagnostics()["pv_anomaly_rms"]
+
+    # the wx.* derived quantities (cpp/main.cpp:445-450)
+    def wave_speed(self) -> float:
+        return math.sqrt(self.params["gravity"] * self.params["depth"])
+
+    def rossby_radius(self) -> float:
+        if self.params["f0"] == 0:
+            raise ValueError("Plane.rossby_radius: f0 is zero")
+        return math.sqrt(self.params["gravity"] * self.params["depth"]) / abs(self.params["f0"])
+
+    def fields(self, h, u, v):
+        """The wx builder's fields(h, u, v) (cpp/main.cpp:409-431) with Python callables f(x, y) of numpy arrays:
+        h = depth + h(x, y) at cell centres, u at the west faces, v at the interior south faces (the walls zero)."""
+        nx, ny, dx, dy = self.nx, self.ny, self.dx(), self.dy()
+        xc, yc = (np.arange(nx) + 0.5) * dx, (np.arange(ny) + 0.5) * dy
+        hh = self.params["depth"] + np.broadcast_to(h(xc[None, :], yc[:, None]), (ny, nx))
+        uu = np.broadcast_to(u((np.arange(nx) * dx)[None, :], yc[:, None]), (ny, nx))
+        vv = np.zeros((ny + 1, nx))
+        vv[1:ny] = np.broadcast_to(v(xc[None, :], (np.arange(1, ny) * dy)[:, None]), (ny - 1, nx))
+        for name, g in (("height", hh), ("u", uu), ("v", vv)):
+            if not np.all(np.isfinite(g)):
+                raise ValueError(f"Plane.fields: the {name} expression is not finite")
+        return self.set_h_from_grid(hh).set_u_from_grid(uu).set_v_from_grid(vv)
+
+    def _scalar(self, fn, *args) -> float:
+        out = _D()
+        _check(fn(self._h, *args, C.byref(out)))
+        return out.value
+
+    def h_at(self, x: float, y: float) -> float:
+        return self._scalar(self._lib.lmw_plane_probe, 0, x, y)
+
+    def u_at(self, x: float, y: float) -> float:
+        return self._scalar(self._lib.lmw_plane_probe, 1, x, y)
+
+    def v_at(self, x: float, y: float) -> float:
+        return self._scalar(self._lib.lmw_plane_probe, 2, x, y)
+
+    def zeta_at_corner(self, i: int, j: int) -> float:
+        return self._scalar(self._lib.lmw_plane_zeta_at_corner, i, j)
+
+    def zonal_amplitude(self, m: int, j: int) -> float:
+        return self._scalar(self._lib.lmw_plane_zonal_amplitude, m, j)
+
+    def zonal_crest(self, m: int, j: int) -> float:
+        return self._scalar(self._lib.lmw_plane_zonal_crest, m, j)
+
+    def v_zonal_crest(self, m: int, j: int) -> float:
+        return self._scalar(self._lib.lmw_plane_v_zonal_crest, m, j)
+
+    def harmonic_energy(self, m: int) -> float:
+        return self._scalar(self._lib.lmw_plane_harmonic_energy, m)
 
 
 class Ensemble:

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # (source, extra flags)
 UNITS = [
-    ("plane.cu", ["--fmad=false"]),
+    ("plane.cu", ["--fmad=false", "-Xcompiler=-ffp-contract=off"]),
     ("sphere.cu", []),
     ("ensemble.cu", []),
     ("sphere32.cu", []),

@@ -359,6 +359,12 @@ int lmw_plane_run(lmw_plane *p, double seconds, double dt) { return PLN(p->e->ru
 int lmw_plane_stable_dt(lmw_plane *p, double safety, double *out) { return PLN(*out = p->e->stable_dt(safety)); }
 int lmw_plane_time(const lmw_plane *p, double *out) { return PLN(*out = p->e->t); }
 int lmw_plane_diagnostics(lmw_plane *p, double *out) { return PLN(p->e->diagnostics(out)); }
+int lmw_plane_probe(lmw_plane *p, int kind, double x, double y, double *out) { return PLN(*out = p->e->probe(kind, x, y)); }
+int lmw_plane_zeta_at_corner(lmw_plane *p, int i, int j, double *out) { return PLN(*out = p->e->zeta_at_corner(i, j)); }
+int lmw_plane_zonal_amplitude(lmw_plane *p, int m, int j, double *out) { return PLN(*out = p->e->zonal_amplitude(m, j)); }
+int lmw_plane_zonal_crest(lmw_plane *p, int m, int j, double *out) { return PLN(*out = p->e->zonal_crest(m, j)); }
+int lmw_plane_v_zonal_crest(lmw_plane *p, int m, int j, double *out) { return PLN(*out = p->e->v_zonal_crest(m, j)); }
+int lmw_plane_harmonic_energy(lmw_plane *p, int m, double *out) { return PLN(*out = p->e->harmonic_energy(m)); }
 int lmw_plane_step_noalloc(int nx, int ny, double lx, double ly, double gravity, double depth, double f0, double beta,
                            double viscosity, double drag, int linear, double *h, double *u, double *v, double dt, int steps,
                            void *stream) {

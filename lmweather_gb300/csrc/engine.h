@@ -39,6 +39,13 @@ class PlaneEngine {
   double stable_dt(double safety);
   // mean_depth, energy, max_speed, pv_anomaly_rms
   void diagnostics(double *out);
+  // point and harmonic diagnostics of cpp/plane.cpp:220-310, computed on the device
+  double probe(int kind, double x, double y);  // kind 0 h_at, 1 u_at, 2 v_at
+  double zeta_at_corner(int i, int j);
+  double zonal_amplitude(int m, int j);
+  double zonal_crest(int m, int j);
+  double v_zonal_crest(int m, int j);
+  double harmonic_energy(int m);
   // device pointers of the state (h, u, v), valid until the engine is destroyed
   void device_state(double **h, double **u, double **v) {
     *h = h0.p; *u = u0.p; *v = v0.p;
@@ -52,7 +59,7 @@ class PlaneEngine {
 
  private:
   DevBuf<double> h0, u0, v0, ha, ua, va, hb, ub, vb, ah, au, av;
-  DevBuf<double> part;
+  DevBuf<double> part, diag;
   DevBuf<Reduce> dred;
   HostBuf<Reduce> hred;
   HostBuf<double> stage;
@@ -61,6 +68,8 @@ class PlaneEngine {
   double graph_dt = 0;
   int graph_steps = 0;
   void reduce(Reduce &r);
+  double read_scalars(int n, double *out);
+  void row_harmonic(int kind, int m, int j, double shift, double *re, double *im);
   void upload(double *dst, const double *src, size_t n);
   void launch_chunk(double dt, int steps);
 };

@@ -208,6 +208,78 @@ __global__ void plane_reduce_final(const double *part, int nblk, Reduce *out) {
   else out->max[k - RED_SUMS] = a;
 }
 
+// ---------------------------------------------------------------- point and harmonic diagnostics
+// One thread: kind 0..2 -> bilinear value of h, u or v at (x, y) (cpp/plane.cpp:245-264: each field on its own
+// points, periodic in x, rows clamped); kind 3 -> relative vorticity at corner (ci, cj) (cpp/plane.cpp:220-226).
+// Compiled without FMA contraction, so the value is the reference's bit for bit.
+__global__ void plane_point(PlaneDev p, const double *__restrict__ h, const double *__restrict__ u, const double *__restrict__ v, int kind,
+                            double x, double y, int ci, int cj, double *out) {
+  const int nx = p.nx, ny = p.ny;
+  if (kind == 3) {
+    const int im = (ci + nx - 1) % nx;
+    const double dvdx = (v[static_cast<size_t>(cj) * nx + ci % nx] - v[static_cast<size_t>(cj) * nx + im]) / p.dxx;
+    const double uj = cj < ny ? u[static_cast<size_t>(cj) * nx + ci % nx] : u[static_cast<size_t>(ny - 1) * nx + ci % nx];
+    const double ujm = cj > 0 ? u[static_cast<size_t>(cj - 1) * nx + ci % nx] : u[ci % nx];
+    out[0] = dvdx - (uj - ujm) / p.dyy;
+    return;
+  }
+  const double xs = kind == 1 ? 0.0 : 0.5, ys = kind == 2 ? 0.0 : 0.5;
+  const double fx = x / p.dxx - xs, fy = y / p.dyy - ys;
+  const int rows = kind == 2 ? ny + 1 : ny;
+  const double fl = floor(fx);
+  const int i0 = static_cast<int>(fl), j0 = static_cast<int>(floor(fy));
+  const double ax = fx - fl, ay = fy - floor(fy);
+  const double *f = kind == 0 ? h : kind == 1 ? u : v;
+  auto get = [&](int i, int j) {
+    i = wrapx(i, nx);
+    j = max(0, min(rows - 1, j));
+    return f[static_cast<size_t>(j) * nx + i];
+  };
+  out[0] = (1 - ax) * ((1 - ay) * get(i0, j0) + ay * get(i0, j0 + 1)) + ax * ((1 - ay) * get(i0 + 1, j0) + ay * get(i0 + 1, j0 + 1));
+}
+
+constexpr int HARM_THREADS = 256;
+constexpr double kPiPlane = 3.14159265358979323846;
+
+// one CTA per row: c_m = (1/nx) sum_i f_i exp(-2 pi i m (i + shift) / nx) of rows j0.. of f (cpp/plane.cpp:266-270);
+// out[r] = (re, im)
+__global__ void __launch_bounds__(HARM_THREADS) plane_row_harmonics(const double *__restrict__ f, int nx, int j0, int m, double shift,
+                                                                    double2 *out) {
+  __shared__ double red[2][HARM_THREADS / 32];
+  const double *row = f + static_cast<size_t>(j0 + blockIdx.x) * nx;
+  double cr = 0, ci = 0;
+  for (int i = threadIdx.x; i < nx; i += HARM_THREADS) {
+    const double th = -2 * kPiPlane * m * (i + shift) / nx;
+    double sn, cs;
+    sincos(th, &sn, &cs);
+    cr += row[i] * cs;
+    ci += row[i] * sn;
+  }
+  cr = warp_sum(cr);
+  ci = warp_sum(ci);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][wid] = cr;
+    red[1][wid] = ci;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int w = 0; w < HARM_THREADS / 32; w++) {
+      a += red[0][w];
+      b += red[1][w];
+    }
+    out[blockIdx.x] = make_double2(a / static_cast<double>(nx), b / static_cast<double>(nx));
+  }
+}
+
+// sum over rows of |c_m|^2 divided by ny (cpp/plane.cpp:291-299), one thread in row order
+__global__ void plane_harmonic_energy_sum(const double2 *__restrict__ c, int rows, int ny, double *out) {
+  double s = 0;
+  for (int r = 0; r < rows; r++) s += c[r].x * c[r].x + c[r].y * c[r].y;
+  out[0] = s / ny;
+}
+
 PlaneDev make_dev(const PlaneConfig &c) {
   PlaneDev d;
   d.nx = c.nx;
@@ -310,6 +382,7 @@ PlaneEngine::PlaneEngine(const PlaneConfig &c) : p(c) {
   dred.alloc(1);
   hred.alloc(1);
   stage.alloc(nvpt());
+  diag.alloc(2 + 4 * static_cast<size_t>(c.ny));  // one scalar, then a complex per row of u and v
   reset();
 }
 
@@ -567,6 +640,89 @@ void PlaneEngine::run(double seconds, double dt) {
       throw RuntimeError("run: dt = " + fmt_f(hstep) + " s exceeds the RK4 stability limit of about " + fmt_f(now) + " s reached at t = " +
                          fmt_f(t) + " s (the flow accelerated): use a smaller dt");
   }
+}
+
+// the small diagnostics read back a few doubles through the pinned staging buffer
+double PlaneEngine::read_scalars(int n, double *out) {
+  LMW_LAUNCH_CHECK();
+  LMW_CUDA(cudaMemcpyAsync(stage.p, diag.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  for (int k = 0; k < n; k++) out[k] = stage.p[k];
+  return out[0];
+}
+
+// cpp/plane.cpp:245-264 (h_at, u_at, v_at); any finite point is read in bounds (periodic x, clamped rows)
+double PlaneEngine::probe(int kind, double x, double y) {
+  if (kind < 0 || kind > 2) throw InvalidArgument("field must be 0 (h), 1 (u) or 2 (v)");
+  if (!std::isfinite(x) || !std::isfinite(y)) throw InvalidArgument("point outside the domain");
+  plane_point<<<1, 1, 0, stream>>>(make_dev(p), h0.p, u0.p, v0.p, kind, x, y, 0, 0, diag.p);
+  g_launches += 1;
+  double r;
+  return read_scalars(1, &r);
+}
+
+// cpp/plane.cpp:220-226; corners i in 0..nx, j in 0..ny
+double PlaneEngine::zeta_at_corner(int i, int j) {
+  if (i < 0 || i > p.nx || j < 0 || j > p.ny) throw InvalidArgument("corner outside the grid");
+  plane_point<<<1, 1, 0, stream>>>(make_dev(p), h0.p, u0.p, v0.p, 3, 0.0, 0.0, i, j, diag.p);
+  g_launches += 1;
+  double r;
+  return read_scalars(1, &r);
+}
+
+void PlaneEngine::row_harmonic(int kind, int m, int j, double shift, double *re, double *im) {
+  const double *f = kind == 0 ? h0.p : kind == 1 ? u0.p : v0.p;
+  plane_row_harmonics<<<1, HARM_THREADS, 0, stream>>>(f, p.nx, j, m, shift, reinterpret_cast<double2 *>(diag.p));
+  g_launches += 1;
+  double c[2];
+  read_scalars(2, c);
+  *re = c[0];
+  *im = c[1];
+}
+
+// crest x of f ~ cos(2 pi m x / lx + ph), in [0, lx/m) (cpp/plane.cpp:284-289)
+static double crest_x(const PlaneConfig &p, int m, double re, double im) {
+  const double ph = std::atan2(im, re);
+  double x = -ph / (2 * kPiPlane * m) * p.lx;
+  const double per = p.lx / m;
+  x = std::fmod(x, per);
+  return x < 0 ? x + per : x;
+}
+
+// cpp/plane.cpp:271-277
+double PlaneEngine::zonal_amplitude(int m, int j) {
+  if (m < 1 || m >= p.nx / 2 || j < 0 || j >= p.ny) throw InvalidArgument("zonal harmonic or row out of range");
+  double re, im;
+  row_harmonic(0, m, j, 0.5, &re, &im);
+  return 2 * std::hypot(re, im);
+}
+
+// cpp/plane.cpp:278-290
+double PlaneEngine::zonal_crest(int m, int j) {
+  if (m < 1 || m >= p.nx / 2 || j < 0 || j >= p.ny) throw InvalidArgument("zonal harmonic or row out of range");
+  double re, im;
+  row_harmonic(0, m, j, 0.5, &re, &im);
+  return crest_x(p, m, re, im);
+}
+
+// cpp/plane.cpp:300-310 (v rows 1..ny-1)
+double PlaneEngine::v_zonal_crest(int m, int j) {
+  if (m < 1 || m >= p.nx / 2 || j < 1 || j >= p.ny) throw InvalidArgument("zonal harmonic or v row out of range");
+  double re, im;
+  row_harmonic(2, m, j, 0.5, &re, &im);
+  return crest_x(p, m, re, im);
+}
+
+// cpp/plane.cpp:291-299: every u row and the interior v rows, one CTA per row, summed on the device
+double PlaneEngine::harmonic_energy(int m) {
+  if (m < 1 || m >= p.nx / 2) throw InvalidArgument("zonal harmonic out of range");
+  double2 *c = reinterpret_cast<double2 *>(diag.p) + 1;
+  plane_row_harmonics<<<p.ny, HARM_THREADS, 0, stream>>>(u0.p, p.nx, 0, m, 0.0, c);
+  plane_row_harmonics<<<p.ny - 1, HARM_THREADS, 0, stream>>>(v0.p, p.nx, 1, m, 0.5, c + p.ny);
+  plane_harmonic_energy_sum<<<1, 1, 0, stream>>>(c, 2 * p.ny - 1, p.ny, diag.p);
+  g_launches += 3;
+  double r;
+  return read_scalars(1, &r);
 }
 
 // cpp/plane.cpp:191-243: mean_depth, energy, max_speed, pv_anomaly_rms

@@ -1109,6 +1109,105 @@ double or_plane_pv_anomaly_rms(const or_plane *p) {
   return sqrt(s / (double)cnt);
 }
 
+/* cpp/plane.cpp:220-226: relative vorticity at corner (i, j), i in 0..nx, j in 0..ny (free slip at the walls) */
+double or_plane_zeta_at_corner(const or_plane *p, int i, int j) {
+  const int nx = p->nx, ny = p->ny;
+  int im = (i + nx - 1) % nx;
+  double dvdx = (p->v[(size_t)j * nx + i % nx] - p->v[(size_t)j * nx + im]) / pdx(p);
+  double uj = j < ny ? p->u[(size_t)j * nx + i % nx] : p->u[(size_t)(ny - 1) * nx + i % nx];
+  double ujm = j > 0 ? p->u[(size_t)(j - 1) * nx + i % nx] : p->u[i % nx];
+  return dvdx - (uj - ujm) / pdy(p);
+}
+
+/* cpp/plane.cpp:245-264: bilinear interpolation on the points of field `kind` (0 h at cell centres, 1 u at west
+ * faces, 2 v at south faces), periodic in x and clamped in y */
+double or_plane_probe(const or_plane *p, int kind, double x, double y) {
+  double dxx = p->lx / p->nx, dyy = p->ly / p->ny;
+  double xs = kind == 1 ? 0.0 : 0.5, ys = kind == 2 ? 0.0 : 0.5;
+  double fx = x / dxx - xs, fy = y / dyy - ys;
+  int rows = kind == 2 ? p->ny + 1 : p->ny;
+  double fl = floor(fx);
+  int i0 = (int)fl, j0 = (int)floor(fy);
+  double ax = fx - fl, ay = fy - floor(fy);
+  const double *f = kind == 0 ? p->h : kind == 1 ? p->u : p->v;
+  double g[2][2];
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++) {
+      int i = (((i0 + a) % p->nx) + p->nx) % p->nx;
+      int j = j0 + b;
+      j = j < 0 ? 0 : (j > rows - 1 ? rows - 1 : j);
+      g[a][b] = f[(size_t)j * p->nx + i];
+    }
+  return (1 - ax) * ((1 - ay) * g[0][0] + ay * g[0][1]) + ax * ((1 - ay) * g[1][0] + ay * g[1][1]);
+}
+
+/* cpp/plane.cpp:266-270: c_m = (1/nx) sum_i row_i exp(-2 pi i m (i + shift) / nx) of row j of field `kind`
+ * (0 h, 1 u, 2 v); exp(i theta) = cos(theta) + i sin(theta) */
+void or_plane_row_harmonic(const or_plane *p, int kind, int m, int j, double shift, double *re, double *im) {
+  const int nx = p->nx;
+  const double *row = (kind == 0 ? p->h : kind == 1 ? p->u : p->v) + (size_t)j * nx;
+  double cr = 0, ci = 0;
+  for (int i = 0; i < nx; i++) {
+    double th = -2 * kPi * m * (i + shift) / nx;
+    cr += row[i] * cos(th);
+    ci += row[i] * sin(th);
+  }
+  *re = cr / (double)nx;
+  *im = ci / (double)nx;
+}
+
+/* cpp/plane.cpp:271-277; returns 0, or 1 when m or j is out of range */
+int or_plane_zonal_amplitude(const or_plane *p, int m, int j, double *out) {
+  if (m < 1 || m >= p->nx / 2 || j < 0 || j >= p->ny) return 1;
+  double re, im;
+  or_plane_row_harmonic(p, 0, m, j, 0.5, &re, &im);
+  *out = 2 * hypot(re, im);
+  return 0;
+}
+
+/* crest position of a harmonic: cpp/plane.cpp:284-289 and 305-309 */
+static double crest_of(const or_plane *p, int m, double re, double im) {
+  double ph = atan2(im, re);
+  double x = -ph / (2 * kPi * m) * p->lx;
+  double per = p->lx / m;
+  x = fmod(x, per);
+  return x < 0 ? x + per : x;
+}
+
+/* cpp/plane.cpp:278-290 */
+int or_plane_zonal_crest(const or_plane *p, int m, int j, double *out) {
+  if (m < 1 || m >= p->nx / 2 || j < 0 || j >= p->ny) return 1;
+  double re, im;
+  or_plane_row_harmonic(p, 0, m, j, 0.5, &re, &im);
+  *out = crest_of(p, m, re, im);
+  return 0;
+}
+
+/* cpp/plane.cpp:300-310 (v rows 1..ny-1) */
+int or_plane_v_zonal_crest(const or_plane *p, int m, int j, double *out) {
+  if (m < 1 || m >= p->nx / 2 || j < 1 || j >= p->ny) return 1;
+  double re, im;
+  or_plane_row_harmonic(p, 2, m, j, 0.5, &re, &im);
+  *out = crest_of(p, m, re, im);
+  return 0;
+}
+
+/* cpp/plane.cpp:291-299: (sum over u rows of |c_m|^2 + sum over interior v rows of |c_m|^2) / ny */
+int or_plane_harmonic_energy(const or_plane *p, int m, double *out) {
+  if (m < 1 || m >= p->nx / 2) return 1;
+  double s = 0, re, im;
+  for (int j = 0; j < p->ny; j++) {
+    or_plane_row_harmonic(p, 1, m, j, 0.0, &re, &im);
+    s += re * re + im * im;
+  }
+  for (int j = 1; j < p->ny; j++) {
+    or_plane_row_harmonic(p, 2, m, j, 0.5, &re, &im);
+    s += re * re + im * im;
+  }
+  *out = s / p->ny;
+  return 0;
+}
+
 /* Zonal jet in geostrophic balance plus white height noise: the reference has no such initialiser, so this
  * is this project's own definition (the benchmark recipe). u = u0 sech^2((y - ly/2) / width) at the u points
  * (cell-centre rows). h(y) integrates g dh/dy = -f u by the trapezoid rule between cell centres, shifted so the

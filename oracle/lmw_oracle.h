@@ -93,6 +93,15 @@ double or_plane_mean_depth(const or_plane *p);
 double or_plane_energy(const or_plane *p);
 double or_plane_max_speed(const or_plane *p);
 double or_plane_pv_anomaly_rms(const or_plane *p);
+double or_plane_zeta_at_corner(const or_plane *p, int i, int j);
+/* kind: 0 h, 1 u, 2 v */
+double or_plane_probe(const or_plane *p, int kind, double x, double y);
+void or_plane_row_harmonic(const or_plane *p, int kind, int m, int j, double shift, double *re, double *im);
+/* these four return 1 (invalid_argument) when the harmonic or the row is out of range */
+int or_plane_zonal_amplitude(const or_plane *p, int m, int j, double *out);
+int or_plane_zonal_crest(const or_plane *p, int m, int j, double *out);
+int or_plane_v_zonal_crest(const or_plane *p, int m, int j, double *out);
+int or_plane_harmonic_energy(const or_plane *p, int m, double *out);
 /* geostrophic zonal jet plus white height noise (grids h, u; v = 0) */
 void or_plane_jet_grids(const or_plane *p, double u0, double width, double noise_rms, uint64_t seed, double *h, double *u);
 

@@ -224,4 +224,18 @@ void ref_plane_diagnostics(void *h, double *out) {
   out[3] = p->potential_vorticity_anomaly_rms();
 }
 
+// the plane's point and harmonic diagnostics (cpp/plane.cpp:220-310); a status of 1 is std::invalid_argument
+double ref_plane_probe(void *h, int kind, double x, double y) {
+  auto *p = static_cast<Plane *>(h);
+  return kind == 0 ? p->h_at(x, y) : kind == 1 ? p->u_at(x, y) : p->v_at(x, y);
+}
+double ref_plane_zeta_at_corner(void *h, int i, int j) { return static_cast<Plane *>(h)->zeta_at_corner(i, j); }
+// which: 0 zonal_amplitude(m, j), 1 zonal_crest(m, j), 2 v_zonal_crest(m, j), 3 harmonic_energy(m)
+int ref_plane_harmonic(void *h, int which, int m, int j, double *out, char *err, int len) {
+  auto *p = static_cast<Plane *>(h);
+  return guarded(err, len, [&] {
+    *out = which == 0 ? p->zonal_amplitude(m, j) : which == 1 ? p->zonal_crest(m, j) : which == 2 ? p->v_zonal_crest(m, j) : p->harmonic_energy(m);
+  });
+}
+
 }  // extern "C"

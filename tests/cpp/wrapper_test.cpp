@@ -97,6 +97,17 @@ int main() {
     for (int i = 0; i < pp.nx; i++) hsum += p.h(i, j);
   EXPECT(std::fabs(hsum / (pp.nx * pp.ny) - p.mean_depth()) < 1e-9, "plane accessors read the device state");
   EXPECT(p.v(3, 0) == 0.0 && p.v(3, pp.ny) == 0.0, "walls stay at rest");
+  // device probes agree with the element accessors: at a cell centre h_at is the cell's value
+  EXPECT(p.h_at(p.x_center(5), p.y_center(9)) == p.h(5, 9), "h_at at a cell centre");
+  EXPECT(p.u_at(5 * p.dx(), p.y_center(9)) == p.u(5, 9), "u_at at a west face");
+  EXPECT(std::isfinite(p.zeta_at_corner(pp.nx, pp.ny)) && p.harmonic_energy(3) >= 0, "corner vorticity and harmonic energy");
+  threw = false;
+  try {
+    p.zonal_crest(pp.nx / 2, 0);
+  } catch (const std::invalid_argument &e) {
+    threw = std::string(e.what()).find("zonal harmonic or row out of range") != std::string::npos;
+  }
+  EXPECT(threw, "zonal_crest out of range is invalid_argument with the reference's text");
   if (failures) return 1;
   std::printf("ok\n");
   return 0;

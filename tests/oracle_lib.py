@@ -109,6 +109,12 @@ def oracle() -> C.CDLL:
             "or_plane_max_speed": (D, [P]),
             "or_plane_pv_anomaly_rms": (D, [P]),
             "or_plane_jet_grids": (None, [P, D, D, D, U64, DP, DP]),
+            "or_plane_zeta_at_corner": (D, [P, I, I]),
+            "or_plane_probe": (D, [P, I, D, D]),
+            "or_plane_zonal_amplitude": (I, [P, I, I, DP]),
+            "or_plane_zonal_crest": (I, [P, I, I, DP]),
+            "or_plane_v_zonal_crest": (I, [P, I, I, DP]),
+            "or_plane_harmonic_energy": (I, [P, I, DP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -170,6 +176,9 @@ def reference(variant: str = "") -> C.CDLL:
             "ref_plane_run": (I, [P, D, D, CP, I]),
             "ref_plane_stable_dt": (D, [P, D]),
             "ref_plane_diagnostics": (None, [P, DP]),
+            "ref_plane_probe": (D, [P, I, D, D]),
+            "ref_plane_zeta_at_corner": (D, [P, I, I]),
+            "ref_plane_harmonic": (I, [P, I, I, I, DP, CP, I]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -551,6 +560,36 @@ class OraclePlane:
             "pv_anomaly_rms": L.or_plane_pv_anomaly_rms(self.h),
         }
 
+    def _harm(self, fn, *args):
+        out = D(0.0)
+        if fn(self.h, *args, C.byref(out)):
+            raise OracleError(1, "zonal harmonic or row out of range")
+        return out.value
+
+    def h_at(self, x, y):
+        return self.lib.or_plane_probe(self.h, 0, x, y)
+
+    def u_at(self, x, y):
+        return self.lib.or_plane_probe(self.h, 1, x, y)
+
+    def v_at(self, x, y):
+        return self.lib.or_plane_probe(self.h, 2, x, y)
+
+    def zeta_at_corner(self, i, j):
+        return self.lib.or_plane_zeta_at_corner(self.h, i, j)
+
+    def zonal_amplitude(self, m, j):
+        return self._harm(self.lib.or_plane_zonal_amplitude, m, j)
+
+    def zonal_crest(self, m, j):
+        return self._harm(self.lib.or_plane_zonal_crest, m, j)
+
+    def v_zonal_crest(self, m, j):
+        return self._harm(self.lib.or_plane_v_zonal_crest, m, j)
+
+    def harmonic_energy(self, m):
+        return self._harm(self.lib.or_plane_harmonic_energy, m)
+
     def jet_grids(self, u0=20.0, width=1.0e5, noise_rms=0.1, seed=1):
         h, u = np.zeros((self.ny, self.nx)), np.zeros((self.ny, self.nx))
         self.lib.or_plane_jet_grids(self.h, u0, width, noise_rms, seed, _dp(h), _dp(u))
@@ -611,3 +650,47 @@ class RefPlane:
         out = np.zeros(4)
         self.lib.ref_plane_diagnostics(self.h, _dp(out))
         return dict(zip(["mean_depth", "energy", "max_speed", "pv_anomaly_rms"], out.tolist()))
+
+    def _harm(self, which, m, j=0):
+        out = D(0.0)
+        err = C.create_string_buffer(512)
+        code = self.lib.ref_plane_harmonic(self.h, which, m, j, C.byref(out), err, 512)
+        if code:
+            raise OracleError(code, err.value.decode())
+        return out.value
+
+    def h_at(self, x, y):
+        return self.lib.ref_plane_probe(self.h, 0, x, y)
+
+    def u_at(self, x, y):
+        return self.lib.ref_plane_probe(self.h, 1, x, y)
+
+    def v_at(self, x, y):
+        return self.lib.ref_plane_probe(self.h, 2, x, y)
+
+    def zeta_at_corner(self, i, j):
+        return self.lib.ref_plane_zeta_at_corner(self.h, i, j)
+
+    def zonal_amplitude(self, m, j):
+        return self._harm(0, m, j)
+
+    def zonal_crest(self, m, j):
+        return self._harm(1, m, j)
+
+    def v_zonal_crest(self, m, j):
+        return self._harm(2, m, j)
+
+    def harmonic_energy(self, m):
+        return self._harm(3, m)
+
+
+def plane_fields_grids(nx, ny, lx, ly, depth, h, u, v):
+    """Grids of the wx builder's Plane.fields(h, u, v) (cpp/main.cpp:409-431) from callables f(x, y): h = depth +
+    h(x, y) at cell centres, u at the west faces (i dx, y_j), v at the interior south faces (x_i, j dy), walls 0."""
+    dx, dy = lx / nx, ly / ny
+    xc, yc = (np.arange(nx) + 0.5) * dx, (np.arange(ny) + 0.5) * dy
+    hh = depth + np.broadcast_to(h(xc[None, :], yc[:, None]), (ny, nx))
+    uu = np.broadcast_to(u((np.arange(nx) * dx)[None, :], yc[:, None]), (ny, nx))
+    vv = np.zeros((ny + 1, nx))
+    vv[1:ny] = np.broadcast_to(v(xc[None, :], (np.arange(1, ny) * dy)[:, None]), (ny - 1, nx))
+    return np.ascontiguousarray(hh, np.float64), np.ascontiguousarray(uu, np.float64), vv

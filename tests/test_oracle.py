@@ -9,6 +9,8 @@ import pytest
 
 from conftest import golden
 from oracle_lib import (OracleError, OraclePlane, OracleSphere, RefPlane, RefSphere, _dp, oracle, ref_available)
+from plane_cases import plane_adjustment_case, plane_harmonic_case, plane_rossby_case
+from sphere_cases import gravity_modes_case, rossby_haurwitz_case, spectrum_case
 
 X86 = platform.machine() in ("x86_64", "AMD64")
 
@@ -248,3 +250,125 @@ def test_plane_gravity_wave_known_answer():
     assert abs(p.diagnostics()["mean_depth"] - H) <= 1e-10
     with pytest.raises(OracleError):
         OraclePlane(2, 2, 1.0, 1.0)
+
+
+# ------------------------------------------------------------------- plane point and harmonic diagnostics
+def _wavy_plane(cls, **extra):
+    """A 40 x 24 channel with a seeded smooth state advanced a little, so every field has structure."""
+    p = cls(40, 24, 4e5, 2.4e5, f0=1e-4, beta=2e-11, viscosity=30.0, drag=1e-6, **extra)
+    p.perturb(0.7, 8)
+    p.run(3000.0, 0.0)
+    return p
+
+
+@pytest.mark.skipif(not ref_available(), reason="reference checkout not built here")
+def test_plane_probes_and_harmonics_bitwise_against_compiled_reference():
+    # cpp/plane.cpp:220-310 restated in the oracle: bilinear probes, corner vorticity, zonal harmonics
+    o, r = _wavy_plane(OraclePlane), _wavy_plane(RefPlane)
+    pts = [(0.0, 0.0), (4e5, 2.4e5), (1.23e5, 0.77e5), (3.999e5, 1e3), (2e4, 2.39e5), (5e3, 6e3)]
+    for x, y in pts:
+        assert o.h_at(x, y) == r.h_at(x, y)
+        assert o.u_at(x, y) == r.u_at(x, y)
+        assert o.v_at(x, y) == r.v_at(x, y)
+    for i, j in [(0, 0), (40, 24), (7, 1), (39, 23), (40, 0), (0, 24), (13, 12)]:
+        assert o.zeta_at_corner(i, j) == r.zeta_at_corner(i, j)
+    for m in (1, 2, 5, 19):
+        assert o.harmonic_energy(m) == r.harmonic_energy(m)
+        for j in (0, 11, 23):
+            assert o.zonal_amplitude(m, j) == r.zonal_amplitude(m, j)
+            assert o.zonal_crest(m, j) == r.zonal_crest(m, j)
+        for j in (1, 12, 23):
+            assert o.v_zonal_crest(m, j) == r.v_zonal_crest(m, j)
+    for bad in ((0, 3), (20, 3), (1, -1), (1, 24)):
+        with pytest.raises(OracleError) as e:
+            r.zonal_amplitude(*bad)
+        assert e.value.code == 1 and "out of range" in str(e.value)
+        with pytest.raises(OracleError):
+            o.zonal_amplitude(*bad)
+    with pytest.raises(OracleError):
+        r.v_zonal_crest(1, 0)
+    with pytest.raises(OracleError):
+        o.v_zonal_crest(1, 0)
+
+
+def test_plane_harmonic_known_answers():
+    plane_harmonic_case(OraclePlane)
+
+
+def test_plane_rossby_known_answers():
+    plane_rossby_case(OraclePlane)
+
+
+def test_plane_adjustment_known_answers():
+    plane_adjustment_case(OraclePlane)
+
+
+# ------------------------------------------------------------------- sphere known answers on the oracle
+class _OracleSphereView(OracleSphere):
+    """The oracle sphere with the engine's method names, and the exact point probes of cpp/sphere.cpp:592-652
+    synthesised from its spectral state (height and the wave crest)."""
+
+    def gauss(self):
+        return self.mu, self.w
+
+    def _d(self, key):
+        return self.diagnostics()[key]
+
+    def mean_height(self):
+        return self._d("mean_height")
+
+    def energy(self):
+        return self._d("energy")
+
+    def kinetic_energy(self):
+        return self._d("kinetic_energy")
+
+    def potential_energy(self):
+        return self._d("potential_energy")
+
+    def potential_enstrophy(self):
+        return self._d("enstrophy")
+
+    def max_wind(self):
+        return self._d("max_wind")
+
+    def _phi(self):
+        return self.get_state()[2]
+
+    def mode_coefficient(self, n, m, imag=False):
+        c = self._phi()[m * (self.T + 1) + n] / self.gravity
+        return c.imag if imag else c.real
+
+    def _column(self, m, lat):
+        col = np.zeros(self.T - m + 2)
+        self.lib.or_legendre_column(m, self.T, math.sin(lat), _dp(col))
+        return col
+
+    def wave_crest(self, m, lat):
+        phi, col = self._phi(), self._column(m, lat)
+        g = sum(phi[m * (self.T + 1) + n] * col[n - m] for n in range(m, self.T + 1))
+        return -np.angle(g) / m
+
+    def height_at(self, lat, lon):
+        phi, f = self._phi(), 0.0
+        for m in range(self.T + 1):
+            col = self._column(m, lat)
+            F = sum(phi[m * (self.T + 1) + n] * col[n - m] for n in range(m, self.T + 1))
+            f += (1.0 if m == 0 else 2.0) * (F * np.exp(1j * m * lon)).real
+        return f / self.gravity
+
+
+def _oracle_sphere(T, **kw):
+    return _OracleSphereView(T, **kw)
+
+
+def test_sphere_gravity_modes_known_answers():
+    gravity_modes_case(_oracle_sphere)
+
+
+def test_sphere_spectrum_known_answers():
+    spectrum_case(_oracle_sphere)
+
+
+def test_sphere_rossby_haurwitz_known_answers():
+    rossby_haurwitz_case(_oracle_sphere)

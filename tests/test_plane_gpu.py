@@ -7,6 +7,7 @@ import pytest
 
 from conftest import golden
 from oracle_lib import OraclePlane
+from plane_cases import plane_adjustment_case, plane_harmonic_case, plane_rossby_case
 
 pytestmark = pytest.mark.gpu
 
@@ -107,3 +108,83 @@ def test_plane_deterministic(engine):
         runs.append(p.get())
     for a, b in zip(*runs):
         assert np.array_equal(a, b)
+
+
+# ------------------------------------------------------------------- point and harmonic diagnostics
+def _gpu_plane_class(engine):
+    class GpuPlane(engine.Plane):
+        def set(self, h, u, v):
+            return self.set_h_from_grid(h).set_u_from_grid(u).set_v_from_grid(v)
+
+    return GpuPlane
+
+
+def test_plane_probes_and_harmonics_against_oracle(engine):
+    # cpp/plane.cpp:220-310 on the device: probes and corner vorticity bit for bit (no FMA contraction), harmonics
+    # within 1e-13 of the oracle (the device's sin/cos and its summation order differ from libm's in the last bits)
+    kw = dict(f0=1e-4, beta=2e-11, viscosity=30.0, drag=1e-6)
+    o = OraclePlane(40, 24, 4e5, 2.4e5, **kw).perturb(0.7, 8)
+    p = engine.Plane(40, 24, 4e5, 2.4e5, **kw).perturb(0.7, 8)
+    o.run(3000.0, 0.0)
+    p.run(3000.0, 0.0)
+    for a, b in zip(o.get(), p.get()):
+        assert np.array_equal(a, b)
+    for x, y in [(0.0, 0.0), (4e5, 2.4e5), (1.23e5, 0.77e5), (3.999e5, 1e3), (2e4, 2.39e5), (5e3, 6e3)]:
+        assert p.h_at(x, y) == o.h_at(x, y)
+        assert p.u_at(x, y) == o.u_at(x, y)
+        assert p.v_at(x, y) == o.v_at(x, y)
+    for i, j in [(0, 0), (40, 24), (7, 1), (39, 23), (40, 0), (0, 24), (13, 12)]:
+        assert p.zeta_at_corner(i, j) == o.zeta_at_corner(i, j)
+    # a harmonic is a sum of O(field) terms: its rounding error scales with the field, not with the harmonic
+    # (m = 19 of this smooth state is 1e-12 of m = 1), so the bound is relative to the largest harmonic; crests
+    # are compared where the harmonic stands well above that rounding
+    hmax = max(o.harmonic_energy(m) for m in range(1, 20))
+    amax = max(o.zonal_amplitude(m, j) for m in range(1, 20) for j in (0, 11, 23))
+    for m in (1, 2, 5, 19):
+        assert abs(p.harmonic_energy(m) - o.harmonic_energy(m)) <= 1e-13 * hmax
+        for j in (0, 11, 23):
+            a = o.zonal_amplitude(m, j)
+            assert abs(p.zonal_amplitude(m, j) - a) <= 1e-13 * amax
+            if a > 1e-6 * amax:
+                assert p.zonal_crest(m, j) == pytest.approx(o.zonal_crest(m, j), rel=1e-9, abs=1e-3)
+        for j in (1, 12, 23):
+            if m < 19:
+                assert p.v_zonal_crest(m, j) == pytest.approx(o.v_zonal_crest(m, j), rel=1e-9, abs=1e-3)
+    for bad in ((0, 3), (20, 3), (1, -1), (1, 24)):
+        with pytest.raises(ValueError, match="zonal harmonic or row out of range"):
+            p.zonal_amplitude(*bad)
+    with pytest.raises(ValueError, match="zonal harmonic or v row out of range"):
+        p.v_zonal_crest(1, 0)
+    with pytest.raises(ValueError, match="zonal harmonic out of range"):
+        p.harmonic_energy(20)
+    with pytest.raises(ValueError, match="corner outside the grid"):
+        p.zeta_at_corner(41, 0)
+    with pytest.raises(ValueError, match="point outside the domain"):
+        p.h_at(float("nan"), 0.0)
+
+
+def test_plane_full_size_harmonics_against_oracle(engine):
+    # 1024 x 512: one CTA per row on the device against the oracle's sequential sums
+    rng = np.random.default_rng(11)
+    h = 100.0 + rng.normal(size=(512, 1024))
+    u = rng.normal(size=(512, 1024))
+    v = np.zeros((513, 1024))
+    v[1:512] = rng.normal(size=(511, 1024))
+    o = OraclePlane(1024, 512, 5.12e6, 2.56e6, f0=1e-4, beta=1.6e-11).set(h, u, v)
+    p = engine.Plane(1024, 512, 5.12e6, 2.56e6, f0=1e-4, beta=1.6e-11)
+    p.set_h_from_grid(h).set_u_from_grid(u).set_v_from_grid(v)
+    for m in (1, 7, 100, 511):
+        assert p.harmonic_energy(m) == pytest.approx(o.harmonic_energy(m), rel=1e-12, abs=1e-300)
+        assert p.zonal_amplitude(m, 256) == pytest.approx(o.zonal_amplitude(m, 256), rel=1e-11)
+
+
+def test_plane_harmonic_known_answers(engine):
+    plane_harmonic_case(_gpu_plane_class(engine))
+
+
+def test_plane_rossby_known_answers(engine):
+    plane_rossby_case(_gpu_plane_class(engine))
+
+
+def test_plane_adjustment_known_answers(engine):
+    plane_adjustment_case(_gpu_plane_class(engine))

@@ -14,6 +14,7 @@ import pytest
 
 from conftest import golden
 from oracle_lib import OracleSphere
+from sphere_cases import adjustment_case, gravity_modes_case, rossby_haurwitz_case, spectrum_case
 
 pytestmark = pytest.mark.gpu
 
@@ -268,3 +269,24 @@ def test_split_bf16_path_against_fp64(engine, T, dt, steps):
     print(f"T{T} split vs FP64 after {steps} steps: height L2 3 terms {e3:.3e}, 6 terms {e6:.3e}; state errors 3 terms {z3}")
     assert e3 < 3e-5  # about 16 significant bits per BF16 hi/lo product
     assert e6 < 1e-6
+
+
+# ------------------------------------------------------------------- known answers of the reference's scripts
+def _make(engine):
+    return lambda T, **kw: engine.Sphere(T, **kw)
+
+
+def test_rossby_haurwitz_known_answers(engine):
+    rossby_haurwitz_case(_make(engine))
+
+
+def test_gravity_modes_known_answers(engine):
+    gravity_modes_case(_make(engine))
+
+
+def test_spectrum_known_answers(engine):
+    spectrum_case(_make(engine))
+
+
+def test_adjustment_known_answers(engine):
+    adjustment_case(_make(engine))
