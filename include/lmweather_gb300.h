@@ -95,7 +95,8 @@ int lmw_sphere_set_tracer_grid(lmw_sphere *s, int member, const double *q, size_
 int lmw_sphere_set_advect_only(lmw_sphere *s, int on);
 /* the tracer's spectrum in the reference layout ((T+1)^2 complex), its grid (Sphere::grid_tracer,
  * cpp/sphere.cpp:283) and diagnostics: out[0] tracer_mean, out[1] tracer_mass (area mean of h q), out[2] l2 and
- * out[3] linf error against the grid it was set from (cpp/sphere.cpp:271-284, 571-590) */
+ * out[3] linf error against the grid it was set from, out[4] tracer_min, out[5] tracer_max of the grid
+ * (cpp/sphere.cpp:271-286, 571-590; out has 6 entries); runtime_error without a tracer */
 int lmw_sphere_tracer_state(lmw_sphere *s, int member, double *q);
 int lmw_sphere_set_tracer_state(lmw_sphere *s, int member, const double *q);
 int lmw_sphere_tracer_grid(lmw_sphere *s, int member, double *out, size_t n);

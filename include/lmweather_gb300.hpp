@@ -187,7 +187,7 @@ class Sphere {
     return out[i];
   }
   double tracer_diag(int i) const {
-    double out[4];
+    double out[6];
     check(lmw_sphere_tracer_diagnostics(s_, 0, out));
     return out[i];
   }

@@ -316,9 +316,10 @@ class Sphere:
         return out
 
     def tracer_diagnostics(self, member: int = 0) -> dict:
-        out = np.zeros(4)
+        out = np.zeros(6)
         _check(self._lib.lmw_sphere_tracer_diagnostics(self._h, member, _dp(out)))
-        return dict(zip(("tracer_mean", "tracer_mass", "tracer_error_l2", "tracer_error_linf"), out.tolist()))
+        return dict(zip(("tracer_mean", "tracer_mass", "tracer_error_l2", "tracer_error_linf", "tracer_min", "tracer_max"),
+                        out.tolist()))
 
     def split_plan(self) -> dict:
         """The autotuned launch plan of the split path (zeros in the other precisions)."""

@@ -147,6 +147,7 @@ class SphereEngine {
   void set_tracer_grid(const double *q, size_t n, int member);
   void set_advect_only(bool on);
   void tracer_grid(double *out, int member);
+  void synth_tracer_grid(int member, double *dst_device);
   void tracer_state(double *q_ref_layout, int member);
   void set_tracer_state(const double *q_ref_layout, int member);
   // mean, mass (area mean of h q) and l2 / linf errors against the grid the tracer was set from

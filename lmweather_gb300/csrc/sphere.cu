@@ -871,6 +871,7 @@ void SphereEngine::mark_reference(int member) {
                                                         refgrid.p + static_cast<size_t>(member) * ngrid());
   LMW_LAUNCH_CHECK();
   g_launches += 1;
+  if (has_tracer) synth_tracer_grid(member, refq.p + static_cast<size_t>(member) * ngrid());
   LMW_CUDA(cudaStreamSynchronize(stream));
 }
 
@@ -1207,9 +1208,8 @@ void SphereEngine::set_tracer_grid(const double *qg, size_t n, int member) {
     }
   }
   set_tracer_state(reinterpret_cast<const double *>(spec.data()), member);
-  std::vector<double> ref(ngrid());
-  h.synthesize(spec, ref);
-  LMW_CUDA(cudaMemcpy(refq.p + static_cast<size_t>(member) * ngrid(), ref.data(), ngrid() * sizeof(double), cudaMemcpyHostToDevice));
+  synth_tracer_grid(member, refq.p + static_cast<size_t>(member) * ngrid());
+  LMW_CUDA(cudaStreamSynchronize(stream));
 }
 
 void SphereEngine::set_tracer_state(const double *qr, int member) {
@@ -1242,22 +1242,27 @@ void SphereEngine::tracer_state(double *qr, int member) {
   from_packed(hstage.p, qr);
 }
 
+// the tracer's grid of one member into dst (device), by the same synthesis for the diagnostics and the reference
+// grid, so that a tracer compared with the grid it was just set from has exactly zero error (cpp/sphere.cpp:236-246)
+void SphereEngine::synth_tracer_grid(int member, double *dst) {
+  SphDev d = make_sph(*this, *tab);
+  const size_t fo = static_cast<size_t>(member) * nlat * 2 * M;
+  trc_synth<<<dim3((nh + 31) / 32, M, 1), SYN_THREADS, 0, stream>>>(d, tab64(*tab), reinterpret_cast<const double2 *>(x0.p) + static_cast<size_t>(member) * 3 * ntri,
+                                                                  reinterpret_cast<const double2 *>(tq0.p) + static_cast<size_t>(member) * ntri,
+                                                                  reinterpret_cast<double2 *>(fourq.p) + fo);
+  trc_to_grid<<<dim3(nh, 1), GRID_THREADS, static_cast<size_t>(nlon) * sizeof(double2), stream>>>(d, reinterpret_cast<const double2 *>(fourq.p) + fo, dst);
+  LMW_LAUNCH_CHECK();
+  g_launches += 2;
+}
+
 void SphereEngine::tracer_grid(double *out, int member) {
   check_member(*this, member);
   if (!has_tracer) {
     std::memset(out, 0, ngrid() * sizeof(double));
     return;
   }
-  SphDev d = make_sph(*this, *tab);
   LMW_CUDA(cudaStreamSynchronize(stream));
-  const size_t fo = static_cast<size_t>(member) * nlat * 2 * M;
-  trc_synth<<<dim3((nh + 31) / 32, M, 1), SYN_THREADS, 0, stream>>>(d, tab64(*tab), reinterpret_cast<const double2 *>(x0.p) + static_cast<size_t>(member) * 3 * ntri,
-                                                                  reinterpret_cast<const double2 *>(tq0.p) + static_cast<size_t>(member) * ntri,
-                                                                  reinterpret_cast<double2 *>(fourq.p) + fo);
-  trc_to_grid<<<dim3(nh, 1), GRID_THREADS, static_cast<size_t>(nlon) * sizeof(double2), stream>>>(
-      d, reinterpret_cast<const double2 *>(fourq.p) + fo, tgrid.p + static_cast<size_t>(member) * ngrid());
-  LMW_LAUNCH_CHECK();
-  g_launches += 2;
+  synth_tracer_grid(member, tgrid.p + static_cast<size_t>(member) * ngrid());
   LMW_CUDA(cudaMemcpyAsync(out, tgrid.p + static_cast<size_t>(member) * ngrid(), ngrid() * sizeof(double), cudaMemcpyDeviceToHost, stream));
   LMW_CUDA(cudaStreamSynchronize(stream));
 }
@@ -1266,6 +1271,7 @@ void SphereEngine::tracer_grid(double *out, int member) {
 // against the grid the tracer was set from
 void SphereEngine::tracer_diagnostics(double *out, int member) {
   check_member(*this, member);
+  if (!has_tracer) throw RuntimeError("no tracer: set one with tracer() first");
   std::vector<double> q(ngrid()), hgt(ngrid()), ref(ngrid(), 0.0);
   tracer_grid(q.data(), member);
   grid(0, hgt.data(), member);
@@ -1275,12 +1281,14 @@ void SphereEngine::tracer_diagnostics(double *out, int member) {
   if (has_tracer)
     LMW_CUDA(cudaMemcpy(q00, tq0.p + static_cast<size_t>(member) * ntri * 2, sizeof(q00), cudaMemcpyDeviceToHost));
   const HostTables &h = tab->host;
-  double sum = 0, num = 0, den = 0, mn = 0, mr = 0;
+  double sum = 0, num = 0, den = 0, mn = 0, mr = 0, qmin = q[0], qmax = q[0];
   for (int j = 0; j < nlat; j++) {
     double rowsum = 0;
     for (int k = 0; k < nlon; k++) {
       const size_t i = static_cast<size_t>(j) * nlon + k;
       rowsum += hgt[i] * q[i];
+      qmin = std::min(qmin, q[i]);
+      qmax = std::max(qmax, q[i]);
       const double dd = q[i] - ref[i];
       num += h.w[j] * dd * dd;
       den += h.w[j] * ref[i] * ref[i];
@@ -1293,6 +1301,8 @@ void SphereEngine::tracer_diagnostics(double *out, int member) {
   out[1] = 0.5 * sum;
   out[2] = den > 0 ? std::sqrt(num / den) : 0.0;
   out[3] = mr > 0 ? mn / mr : 0.0;
+  out[4] = qmin;  // cpp/sphere.cpp:285-286
+  out[5] = qmax;
 }
 
 void SphereEngine::kernel_times(double dt, int reps, double *out) {

@@ -209,3 +209,204 @@ def adjustment_case(make):
     nd.run(5.0 * 86400.0, 1800.0)
     assert d.energy() < nd.energy()
     assert abs(d.mean_height() - 5960.0) <= 1e-9
+
+
+def _grids(s, *arrays):
+    shape = (s.nlat, s.nlon)
+    return [np.ascontiguousarray(np.broadcast_to(x, shape), np.float64) for x in arrays]
+
+
+def williamson1(s, alpha, radius=6.37122e6):
+    """Williamson et al. (1992) test case 1: a cosine bell (1000 m, radius a/3, centred at 270 E on the equator)
+    carried by solid-body rotation (one revolution in 12 days) about an axis tilted by alpha, winds frozen."""
+    u0, R, lonc = 2 * math.pi * radius / (12 * 86400.0), radius / 3, 1.5 * math.pi
+    lat, lon = lat_lon(s)
+    s.set_axis_tilt(alpha)
+    u = u0 * (np.cos(lat) * math.cos(alpha) + np.sin(lat) * np.cos(lon) * math.sin(alpha))
+    v = -u0 * np.sin(lon) * math.sin(alpha)
+    r = radius * np.arccos(np.clip(np.cos(lat) * np.cos(lon - lonc), -1.0, 1.0))
+    q = np.where(r < R, 500.0 * (1 + np.cos(math.pi * r / R)), 0.0)
+    s.set_state_grid(*_grids(s, 1000.0, u, v))
+    s.set_tracer_grid(*_grids(s, q))
+    s.set_advect_only(True)
+    return s
+
+
+def williamson2(s, alpha, radius=6.37122e6, omega=7.292e-5, gravity=G):
+    """Williamson et al. (1992) test case 2: steady geostrophic solid-body flow (u0 = 2 pi a / 12 days,
+    g h0 = 2.94e4 m^2/s^2) about an axis tilted by alpha."""
+    u0, h0 = 2 * math.pi * radius / (12 * 86400.0), 2.94e4 / gravity
+    lat, lon = lat_lon(s)
+    s.set_axis_tilt(alpha)
+    u = u0 * (np.cos(lat) * math.cos(alpha) + np.sin(lat) * np.cos(lon) * math.sin(alpha))
+    v = -u0 * np.sin(lon) * math.sin(alpha)
+    t = -np.cos(lon) * np.cos(lat) * math.sin(alpha) + np.sin(lat) * math.cos(alpha)
+    h = h0 - (radius * omega * u0 + 0.5 * u0 * u0) * t * t / gravity
+    s.set_state_grid(*_grids(s, h, u, v))
+    return s
+
+
+def cone(lon, lat):
+    """The conical mountain of test case 5: 2000 m, radius pi/9, centred at 270 E 30 N."""
+    R = math.pi / 9
+    return 2000.0 * (1 - np.sqrt(np.minimum(R * R, (lon - 1.5 * math.pi) ** 2 + (lat - math.pi / 6) ** 2)) / R)
+
+
+def williamson5(s, radius=6.37122e6, omega=7.292e-5, gravity=G):
+    """Williamson et al. (1992) test case 5: zonal flow (20 m/s, h0 = 5960 m) balanced as in test case 2, over the
+    cone; the fluid thickness is that free surface minus the mountain."""
+    u0, h0 = 20.0, 5960.0
+    lat, lon = lat_lon(s)
+    hs = cone(lon, lat)
+    s.set_axis_tilt(0.0)
+    s.set_orography_grid(*_grids(s, hs))
+    h = h0 - (radius * omega * u0 + 0.5 * u0 * u0) * np.sin(lat) ** 2 / gravity - hs
+    s.set_state_grid(*_grids(s, h, u0 * np.cos(lat), 0.0))
+    return s
+
+
+def tracer(s, fn):
+    lat, lon = lat_lon(s)
+    s.set_tracer_grid(*_grids(s, fn(lon, lat)))
+    return s
+
+
+def tracer_at(s, lat, lon):
+    return s.tracer_at(lat * DEG, lon * DEG)
+
+
+def td(s, key):
+    return s.tracer_diagnostics()[key]
+
+
+def williamson2_case(make):
+    """Test case 2 stays put for 5 days at four tilts (errors < 1e-6, mass 1e-9, energy 1e-9); its reference
+    values at T42; and the same flow on an untilted planet does not stay put."""
+    for tilt in (0.0, 0.05, math.pi / 2 - 0.05, math.pi / 2):
+        s = williamson2(make(21), tilt)
+        m0, e0 = s.mean_height(), s.energy()
+        s.run(432000.0, 1800.0)
+        assert abs(s.time() - 432000.0) <= 1e-7
+        assert s.height_error_l2() < 1e-6 and s.height_error_linf() < 1e-6
+        assert abs(s.mean_height() - m0) <= 1e-9
+        assert abs(s.energy() / e0 - 1.0) <= 1e-9
+    s = williamson2(make(42), 0.0)
+    a = 6371220.0
+    u0, h0 = 2 * math.pi * a / (12 * 86400.0), 29400.0 / G
+    assert abs(s.max_wind() - u0) <= 0.02
+    assert abs(height_at(s, 0.0, 0.0) - h0) <= 1e-3
+    assert abs(height_at(s, 90.0, 0.0) - (h0 - (a * 7.292e-5 * u0 + 0.5 * u0 * u0) / G)) <= 1e-3
+    assert abs(s.mean_height() - 2363.02) <= 0.01
+    u1 = 38.6106
+    wrong = fields(make(21), lambda lo, la: 29400.0 / G - (a * 7.292e-5 * u1 + u1 * u1 / 2.0)
+                   * (0 - np.cos(lo) * np.cos(la) * math.sin(1.5) + np.sin(la) * math.cos(1.5)) ** 2 / G,
+                   lambda lo, la: u1 * (np.cos(la) * math.cos(1.5) + np.sin(la) * np.cos(lo) * math.sin(1.5)),
+                   lambda lo, la: 0 - u1 * np.sin(lo) * math.sin(1.5))
+    wrong.run(86400.0, 1800.0)
+    assert wrong.height_error_l2() > 1e-3
+
+
+def tracer_case(make):
+    """Test case 1 over the poles at T42 (half way: two disjoint bells, l2 = sqrt 2; after 12 days back within
+    1e-3), at T21 with hour steps, the bell carried by the real test-case-2 dynamics against the frozen winds, and
+    a divergent flow that conserves the tracer mass h q but not its mean."""
+    s = williamson1(make(42), math.pi / 2 - 0.05)
+    q0, c0 = td(s, "tracer_mean"), tracer_at(s, 0.0, 270.0)
+    assert abs(c0 - 1000.0) <= 5.0
+    assert -4.0 < td(s, "tracer_min") < 0.0
+    assert 985.0 < td(s, "tracer_max") < 1000.0
+    assert abs(tracer_at(s, 0.0, 90.0)) <= 1.5
+    assert td(s, "tracer_error_l2") == 0.0
+    assert abs(s.max_wind() - 2 * math.pi * 6371220.0 / (12 * 86400.0)) <= 0.02
+    s.run(6 * 86400.0, 1800.0)
+    assert abs(tracer_at(s, 0.0, 90.0) - c0) <= 0.1
+    assert abs(td(s, "tracer_error_l2") - math.sqrt(2.0)) <= 1e-3
+    assert abs(td(s, "tracer_error_linf") - 1.0) <= 2e-3
+    s.run(6 * 86400.0, 1800.0)
+    assert td(s, "tracer_error_l2") < 1e-3 and td(s, "tracer_error_linf") < 1e-3
+    assert abs(tracer_at(s, 0.0, 270.0) - c0) <= 0.1
+    assert abs(td(s, "tracer_mean") - q0) <= 1e-9
+    assert abs(s.time() - 12 * 86400.0) <= 1e-3
+    assert s.height_error_l2() == 0.0
+    c = williamson1(make(21), 0.0)
+    cc0 = tracer_at(c, 0.0, 270.0)
+    c.run(12 * 86400.0, 3600.0)
+    assert td(c, "tracer_error_l2") < 3e-3
+    assert abs(tracer_at(c, 0.0, 270.0) - cc0) <= 0.3
+    bell = lambda lo, la: 500.0 * (1 + np.cos(math.pi * np.minimum(1.0, 3.0 * np.arccos(np.cos(la) * np.cos(lo - 1.5 * math.pi)))))
+    d = tracer(williamson2(make(21), 0.05), bell)
+    f = williamson1(make(21), 0.05)
+    assert abs(tracer_at(d, 0.0, 270.0) - tracer_at(f, 0.0, 270.0)) <= 1e-10
+    d.run(3 * 86400.0, 1200.0)
+    f.run(3 * 86400.0, 1200.0)
+    assert abs(tracer_at(d, 20.0, 0.0) - tracer_at(f, 20.0, 0.0)) <= 1e-6
+    assert abs(tracer_at(d, 0.0, 0.0) - tracer_at(f, 0.0, 0.0)) <= 1e-6
+    assert abs(td(d, "tracer_error_l2") - td(f, "tracer_error_l2")) <= 1e-7
+    assert d.height_error_l2() < 1e-6
+    r = tracer(williamson6(make(21)), lambda lo, la: 1.0 + np.sin(la))
+    mass0, mean0 = td(r, "tracer_mass"), td(r, "tracer_mean")
+    assert abs(mean0 - 1.0) <= 1e-9
+    r.run(2 * 86400.0, 1200.0)
+    assert abs(td(r, "tracer_mass") / mass0 - 1.0) <= 1e-4
+    assert -0.5 < td(r, "tracer_min") < 0.0 and 2.0 < td(r, "tracer_max") < 2.5
+
+
+def orography_case(make):
+    """A flat free surface over the cone stays at rest (the same thickness without the mountain collapses); test
+    case 5 at T42 for 15 days conserves mass, energy and enstrophy to truncation error and forms a lee vortex; T21
+    agrees on the global height change."""
+    r = make(21)
+    lat, lon = lat_lon(r)
+    r.set_orography_grid(*_grids(r, cone(lon, lat)))
+    fields(r, lambda lo, la: 5960.0 - cone(lo, la), lambda lo, la: 0 * la, lambda lo, la: 0 * la)
+    e0 = r.energy()
+    assert abs(height_at(r, 30.0, 270.0) - 3960.0) <= 300.0
+    assert abs(height_at(r, 30.0, 90.0) - 5960.0) <= 1.0
+    r.run(86400.0, 1200.0)
+    assert r.max_wind() < 1e-9
+    assert r.height_error_l2() < 1e-12
+    assert abs(r.energy() / e0 - 1.0) <= 1e-12
+    hole = fields(make(21), lambda lo, la: 5960.0 - cone(lo, la), lambda lo, la: 0 * la, lambda lo, la: 0 * la)
+    hole.run(86400.0, 1200.0)
+    assert hole.max_wind() > 10.0 and hole.height_error_l2() > 0.01
+    s = williamson5(make(42))
+    assert abs(s.max_wind() - 20.0) <= 0.02
+    assert abs(s.mean_height() - 5619.9) <= 0.5
+    balanced = 5960.0 - (6371220.0 * 7.292e-5 * 20.0 + 200.0) * 0.25 / G
+    assert abs(height_at(s, 30.0, 270.0) + 2000.0 - balanced) <= 200.0
+    assert abs(height_at(s, 30.0, 90.0) - balanced) <= 0.5
+    m0, e5, q0 = s.mean_height(), s.energy(), s.potential_enstrophy()
+    upstream0 = vorticity_at(s, 30.0, 240.0)
+    s.run(15 * 86400.0, 900.0)
+    assert abs(s.mean_height() - m0) <= 1e-9
+    assert abs(s.energy() / e5 - 1.0) <= 1e-6
+    assert abs(s.potential_enstrophy() / q0 - 1.0) <= 1e-5
+    assert 35.0 < s.max_wind() < 50.0
+    assert vorticity_at(s, 30.0, 300.0) > 2e-5
+    assert abs(vorticity_at(s, 30.0, 240.0) - upstream0) < 1e-5
+    c = williamson5(make(21))
+    c.run(15 * 86400.0, 1200.0)
+    assert abs(c.height_error_l2() - s.height_error_l2()) <= 2e-4
+    assert 0.01 < s.height_error_l2() < 0.02
+
+
+def determinism_case(make, make_plane):
+    """Seeded runs repeat bit for bit on both models; another seed differs (tests/determinism.lms)."""
+    def plane(seed):
+        p = make_plane(40, 20, 4.0e6, 2.0e6, depth=500.0, f0=1e-4, beta=2e-11)
+        p.perturb(1.0, seed)
+        p.run(86400.0, 0.0)
+        return p
+
+    a, b, c = plane(99), plane(99), plane(100)
+    assert a.energy() == b.energy()
+    assert a.h_at(1234567.0, 999999.0) == b.h_at(1234567.0, 999999.0)
+    assert a.h_at(1234567.0, 999999.0) != c.h_at(1234567.0, 999999.0)
+    assert abs(a.mean_depth() - 500.0) <= 1e-9
+    for a2, b2 in zip(a.get(), b.get()):
+        assert np.array_equal(a2, b2)
+    s1, s2 = williamson6(make(21)), williamson6(make(21))
+    s1.run(43200.0, 1200.0)
+    s2.run(43200.0, 1200.0)
+    for x, y in zip(s1.get_state(), s2.get_state()):
+        assert np.array_equal(x, y)

@@ -10,7 +10,7 @@ import pytest
 from conftest import golden
 from oracle_lib import (OracleError, OraclePlane, OracleSphere, RefPlane, RefSphere, _dp, oracle, ref_available)
 from plane_cases import plane_adjustment_case, plane_harmonic_case, plane_rossby_case
-from sphere_cases import gravity_modes_case, rossby_haurwitz_case, spectrum_case
+from sphere_cases import gravity_modes_case, rossby_haurwitz_case, spectrum_case, williamson2_case
 
 X86 = platform.machine() in ("x86_64", "AMD64")
 
@@ -311,6 +311,9 @@ class _OracleSphereView(OracleSphere):
     def gauss(self):
         return self.mu, self.w
 
+    def time(self):
+        return OracleSphere.time.fget(self)
+
     def _d(self, key):
         return self.diagnostics()[key]
 
@@ -331,6 +334,12 @@ class _OracleSphereView(OracleSphere):
 
     def max_wind(self):
         return self._d("max_wind")
+
+    def height_error_l2(self):
+        return self._d("error_l2")
+
+    def height_error_linf(self):
+        return self._d("error_linf")
 
     def _phi(self):
         return self.get_state()[2]
@@ -372,3 +381,7 @@ def test_sphere_spectrum_known_answers():
 
 def test_sphere_rossby_haurwitz_known_answers():
     rossby_haurwitz_case(_oracle_sphere)
+
+
+def test_sphere_williamson2_known_answers():
+    williamson2_case(_oracle_sphere)

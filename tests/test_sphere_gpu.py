@@ -14,7 +14,8 @@ import pytest
 
 from conftest import golden
 from oracle_lib import OracleSphere
-from sphere_cases import adjustment_case, gravity_modes_case, rossby_haurwitz_case, spectrum_case
+from sphere_cases import (adjustment_case, determinism_case, gravity_modes_case, orography_case, rossby_haurwitz_case, spectrum_case,
+                          tracer_case, williamson2_case)
 
 pytestmark = pytest.mark.gpu
 
@@ -290,3 +291,19 @@ def test_spectrum_known_answers(engine):
 
 def test_adjustment_known_answers(engine):
     adjustment_case(_make(engine))
+
+
+def test_williamson2_known_answers(engine):
+    williamson2_case(_make(engine))
+
+
+def test_tracer_known_answers(engine):
+    tracer_case(_make(engine))
+
+
+def test_orography_known_answers(engine):
+    orography_case(_make(engine))
+
+
+def test_determinism_known_answers(engine):
+    determinism_case(_make(engine), engine.Plane)
