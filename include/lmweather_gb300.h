@@ -128,6 +128,13 @@ int lmw_sphere_diagnostics(lmw_sphere *s, int member, double *out);
 int lmw_sphere_grid(lmw_sphere *s, int member, int which, double *out, size_t n);
 /* Sphere::spectrum (cpp/sphere.hpp:63, cpp/sphere.cpp:536-551): T+1 values each */
 int lmw_sphere_spectrum(lmw_sphere *s, int member, double *ke, double *pe);
+/* The wx layer's text files (cpp/main.cpp:328-335, 357-384), numbers as "%.10g": save_csv writes per grid
+ * point "lon lat h u v vorticity tracer orography" (degrees; a blank line after each latitude row),
+ * save_zonal_mean per latitude "lat mean_h mean_u", save_spectrum per degree n >= 1 "n ke pe". A file that cannot
+ * be written is runtime_error "Sphere.save_csv: cannot write <path>" (and likewise). */
+int lmw_sphere_save_csv(lmw_sphere *s, int member, const char *path);
+int lmw_sphere_save_zonal_mean(lmw_sphere *s, int member, const char *path);
+int lmw_sphere_save_spectrum(lmw_sphere *s, int member, const char *path);
 
 /* the handle's CUDA stream (a cudaStream_t), for callers that order their own work or events after it */
 int lmw_sphere_stream(const lmw_sphere *s, void **stream);
@@ -182,6 +189,12 @@ int lmw_plane_zonal_amplitude(lmw_plane *p, int m, int j, double *out);
 int lmw_plane_zonal_crest(lmw_plane *p, int m, int j, double *out);
 int lmw_plane_v_zonal_crest(lmw_plane *p, int m, int j, double *out);
 int lmw_plane_harmonic_energy(lmw_plane *p, int m, double *out);
+/* The wx layer's text files (cpp/main.cpp:464-494), numbers as "%.10g": save_csv per cell "x y h uc vc zeta"
+ * (a blank line after each row), save_row "x h" along row j, save_column "y h" along column i; invalid_argument
+ * for a row or column outside the grid, runtime_error "Plane.save_csv: cannot write <path>" (and likewise). */
+int lmw_plane_save_csv(lmw_plane *p, const char *path);
+int lmw_plane_save_row(lmw_plane *p, int j, const char *path);
+int lmw_plane_save_column(lmw_plane *p, int i, const char *path);
 /* the handle's CUDA stream (a cudaStream_t) */
 int lmw_plane_stream(const lmw_plane *p, void **stream);
 

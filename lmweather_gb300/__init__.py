@@ -84,6 +84,12 @@ _SIGS = {
     "lmw_plane_zonal_crest": (_I, [_P, _I, _I, _DP]),
     "lmw_plane_v_zonal_crest": (_I, [_P, _I, _I, _DP]),
     "lmw_plane_harmonic_energy": (_I, [_P, _I, _DP]),
+    "lmw_plane_save_csv": (_I, [_P, C.c_char_p]),
+    "lmw_plane_save_row": (_I, [_P, _I, C.c_char_p]),
+    "lmw_plane_save_column": (_I, [_P, _I, C.c_char_p]),
+    "lmw_sphere_save_csv": (_I, [_P, _I, C.c_char_p]),
+    "lmw_sphere_save_zonal_mean": (_I, [_P, _I, C.c_char_p]),
+    "lmw_sphere_save_spectrum": (_I, [_P, _I, C.c_char_p]),
     "lmw_ensemble_create": (_I, [_I, _IP, C.POINTER(C.c_uint64), _DP, _DP, _D, _D, _D, _I, _I, _PP]),
     "lmw_ensemble_destroy": (_I, [_P]),
     "lmw_ensemble_run": (_I, [_P, _D]),
@@ -411,6 +417,16 @@ class Sphere:
         _check(self._lib.lmw_sphere_spectrum(self._h, member, _dp(ke), _dp(pe)))
         return ke, pe
 
+    # the wx layer's text files (cpp/main.cpp:328-335, 357-384)
+    def save_csv(self, path: str, member: int = 0):
+        _check(self._lib.lmw_sphere_save_csv(self._h, member, os.fsencode(path)))
+
+    def save_zonal_mean(self, path: str, member: int = 0):
+        _check(self._lib.lmw_sphere_save_zonal_mean(self._h, member, os.fsencode(path)))
+
+    def save_spectrum(self, path: str, member: int = 0):
+        _check(self._lib.lmw_sphere_save_spectrum(self._h, member, os.fsencode(path)))
+
 
 class Plane:
     """GPU C-grid beta-plane channel (cpp/plane.hpp:20-68)."""
@@ -569,6 +585,16 @@ class Plane:
 
     def harmonic_energy(self, m: int) -> float:
         return self._scalar(self._lib.lmw_plane_harmonic_energy, m)
+
+    # the wx layer's text files (cpp/main.cpp:464-494)
+    def save_csv(self, path: str):
+        _check(self._lib.lmw_plane_save_csv(self._h, os.fsencode(path)))
+
+    def save_row(self, j: int, path: str):
+        _check(self._lib.lmw_plane_save_row(self._h, j, os.fsencode(path)))
+
+    def save_column(self, i: int, path: str):
+        _check(self._lib.lmw_plane_save_column(self._h, i, os.fsencode(path)))
 
 
 class Ensemble:

@@ -41,6 +41,17 @@ std::string fmt_f(double x) {
   std::snprintf(b, sizeof b, "%f", x);
   return b;
 }
+std::string fmt_g(double x) {
+  char b[48];
+  std::snprintf(b, sizeof b, "%.10g", x);
+  return b;
+}
+void write_text(const std::string &path, const std::string &text, const char *who) {
+  std::FILE *f = std::fopen(path.c_str(), "wb");
+  if (!f) throw RuntimeError(std::string(who) + ": cannot write " + path);
+  const bool ok = std::fwrite(text.data(), 1, text.size(), f) == text.size();
+  if (std::fclose(f) != 0 || !ok) throw RuntimeError(std::string(who) + ": cannot write " + path);
+}
 }  // namespace lmw
 
 namespace {
@@ -268,6 +279,24 @@ int lmw_sphere_spectrum(lmw_sphere *s, int member, double *ke, double *pe) {
     s->e->spectrum(ke, pe, member);
   });
 }
+int lmw_sphere_save_csv(lmw_sphere *s, int member, const char *path) {
+  return SPH({
+    need(path != nullptr, "Sphere.save_csv: no path");
+    s->e->save_csv(path, member);
+  });
+}
+int lmw_sphere_save_zonal_mean(lmw_sphere *s, int member, const char *path) {
+  return SPH({
+    need(path != nullptr, "Sphere.save_zonal_mean: no path");
+    s->e->save_zonal_mean(path, member);
+  });
+}
+int lmw_sphere_save_spectrum(lmw_sphere *s, int member, const char *path) {
+  return SPH({
+    need(path != nullptr, "Sphere.save_spectrum: no path");
+    s->e->save_spectrum(path, member);
+  });
+}
 
 int lmw_sphere_stream(const lmw_sphere *s, void **stream) { return SPH(*stream = static_cast<void *>(s->e->stream)); }
 int lmw_sphere_kernel_times(lmw_sphere *s, double dt, int reps, double *ms) {
@@ -365,6 +394,24 @@ int lmw_plane_zonal_amplitude(lmw_plane *p, int m, int j, double *out) { return 
 int lmw_plane_zonal_crest(lmw_plane *p, int m, int j, double *out) { return PLN(*out = p->e->zonal_crest(m, j)); }
 int lmw_plane_v_zonal_crest(lmw_plane *p, int m, int j, double *out) { return PLN(*out = p->e->v_zonal_crest(m, j)); }
 int lmw_plane_harmonic_energy(lmw_plane *p, int m, double *out) { return PLN(*out = p->e->harmonic_energy(m)); }
+int lmw_plane_save_csv(lmw_plane *p, const char *path) {
+  return PLN({
+    need(path != nullptr, "Plane.save_csv: no path");
+    p->e->save_csv(path);
+  });
+}
+int lmw_plane_save_row(lmw_plane *p, int j, const char *path) {
+  return PLN({
+    need(path != nullptr, "Plane.save_row: no path");
+    p->e->save_row(j, path);
+  });
+}
+int lmw_plane_save_column(lmw_plane *p, int i, const char *path) {
+  return PLN({
+    need(path != nullptr, "Plane.save_column: no path");
+    p->e->save_column(i, path);
+  });
+}
 int lmw_plane_step_noalloc(int nx, int ny, double lx, double ly, double gravity, double depth, double f0, double beta,
                            double viscosity, double drag, int linear, double *h, double *u, double *v, double dt, int steps,
                            void *stream) {

@@ -46,6 +46,10 @@ class PlaneEngine {
   double zonal_crest(int m, int j);
   double v_zonal_crest(int m, int j);
   double harmonic_energy(int m);
+  // the wx layer's text files (cpp/main.cpp:464-494)
+  void save_csv(const std::string &path);
+  void save_row(int j, const std::string &path);
+  void save_column(int i, const std::string &path);
   // device pointers of the state (h, u, v), valid until the engine is destroyed
   void device_state(double **h, double **u, double **v) {
     *h = h0.p; *u = u0.p; *v = v0.p;
@@ -134,6 +138,10 @@ class SphereEngine {
   // which: 0 height, 1 u, 2 v, 3 vorticity
   void grid(int which, double *out, int member);
   void spectrum(double *ke, double *pe, int member);
+  // the wx layer's text files (cpp/main.cpp:328-335, 357-384)
+  void save_csv(const std::string &path, int member);
+  void save_zonal_mean(const std::string &path, int member);
+  void save_spectrum(const std::string &path, int member);
   // exact point values at (lat, lon) in radians from the spectral state (cpp/sphere.cpp:287-299, 592-637): which
   // 0 height, 1 zonal wind u, 2 meridional wind v, 3 vorticity, 4 tracer
   double probe(int which, double lat, double lon, int member);

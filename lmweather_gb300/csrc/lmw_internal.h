@@ -26,6 +26,10 @@ void cuda_check(cudaError_t e, const char *what, const char *file, int line);
 
 // std::to_string(double) formatting ("%f"), which the reference uses in its run() messages
 std::string fmt_f(double x);
+// the text writers' number format ("%.10g") and file write, with the reference's error text
+// ("<who>: cannot write <path>", a runtime_error) (cpp/main.cpp:84-92)
+std::string fmt_g(double x);
+void write_text(const std::string &path, const std::string &text, const char *who);
 
 // Device buffer owned by an engine object.
 template <class T> struct DevBuf {

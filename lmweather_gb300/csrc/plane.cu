@@ -725,6 +725,55 @@ double PlaneEngine::harmonic_energy(int m) {
   return read_scalars(1, &r);
 }
 
+// ------------------------------------------------------------------------------------------------ text writers
+// cpp/main.cpp:464-478: per cell x y h uc vc zeta (zeta the mean of the four corner vorticities), a blank line after
+// each row; the fields come back once and the host forms the cell values in the reference's order
+void PlaneEngine::save_csv(const std::string &path) {
+  const int nx = p.nx, ny = p.ny;
+  std::vector<double> h(ncell()), u(ncell()), v(nvpt());
+  get(h.data(), u.data(), v.data());
+  const double dxx = dx(), dyy = dy();
+  auto zc = [&](int i, int j) {  // cpp/plane.cpp:220-226
+    const int im = (i + nx - 1) % nx;
+    const double dvdx = (v[static_cast<size_t>(j) * nx + i % nx] - v[static_cast<size_t>(j) * nx + im]) / dxx;
+    const double uj = j < ny ? u[static_cast<size_t>(j) * nx + i % nx] : u[static_cast<size_t>(ny - 1) * nx + i % nx];
+    const double ujm = j > 0 ? u[static_cast<size_t>(j - 1) * nx + i % nx] : u[i % nx];
+    return dvdx - (uj - ujm) / dyy;
+  };
+  std::string t;
+  t.reserve(ncell() * 80);
+  for (int j = 0; j < ny; j++) {
+    for (int i = 0; i < nx; i++) {
+      const size_t e = static_cast<size_t>(j) * nx + i;
+      const double uc = 0.5 * (u[e] + u[static_cast<size_t>(j) * nx + (i + 1) % nx]), vc = 0.5 * (v[e] + v[e + nx]);
+      const double z = 0.25 * (zc(i, j) + zc(i + 1, j) + zc(i, j + 1) + zc(i + 1, j + 1));
+      t += fmt_g((i + 0.5) * dxx) + " " + fmt_g((j + 0.5) * dyy) + " " + fmt_g(h[e]) + " " + fmt_g(uc) + " " + fmt_g(vc) + " " + fmt_g(z) + "\n";
+    }
+    t += "\n";
+  }
+  write_text(path, t, "Plane.save_csv");
+}
+
+// cpp/main.cpp:480-487: x and h along row j
+void PlaneEngine::save_row(int j, const std::string &path) {
+  if (j < 0 || j >= p.ny) throw InvalidArgument("Plane.save_row: row outside the grid");
+  std::vector<double> h(ncell());
+  get(h.data(), nullptr, nullptr);
+  std::string t;
+  for (int i = 0; i < p.nx; i++) t += fmt_g((i + 0.5) * dx()) + " " + fmt_g(h[static_cast<size_t>(j) * p.nx + i]) + "\n";
+  write_text(path, t, "Plane.save_row");
+}
+
+// cpp/main.cpp:488-494: y and h along column i
+void PlaneEngine::save_column(int i, const std::string &path) {
+  if (i < 0 || i >= p.nx) throw InvalidArgument("Plane.save_column: column outside the grid");
+  std::vector<double> h(ncell());
+  get(h.data(), nullptr, nullptr);
+  std::string t;
+  for (int j = 0; j < p.ny; j++) t += fmt_g((j + 0.5) * dy()) + " " + fmt_g(h[static_cast<size_t>(j) * p.nx + i]) + "\n";
+  write_text(path, t, "Plane.save_column");
+}
+
 // cpp/plane.cpp:191-243: mean_depth, energy, max_speed, pv_anomaly_rms
 void PlaneEngine::diagnostics(double *out) {
   Reduce r;

@@ -1755,6 +1755,66 @@ double SphereEngine::wave_crest(int m, double lat, int member) {
   return -std::arg(g) / m;
 }
 
+// ------------------------------------------------------------------------------------------------ text writers
+// The wx layer's files (cpp/main.cpp:328-335, 357-384), written from grids synthesised on the device.
+static constexpr double kDegree = 3.14159265358979323846 / 180.0;
+
+// one line per grid point: lon lat h u v vorticity tracer orography (degrees, m, m/s, 1/s), a blank line after
+// each latitude row
+void SphereEngine::save_csv(const std::string &path, int member) {
+  check_member(*this, member);
+  const size_t n = ngrid();
+  std::vector<double> hh(n), uu(n), vv(n), zz(n), qq(n, 0.0), hs(n);
+  grid(0, hh.data(), member);
+  grid(1, uu.data(), member);
+  grid(2, vv.data(), member);
+  grid(3, zz.data(), member);
+  if (has_tracer) tracer_grid(qq.data(), member);
+  LMW_CUDA(cudaMemcpy(hs.data(), hsgrid.p + static_cast<size_t>(member) * n, n * sizeof(double), cudaMemcpyDeviceToHost));
+  const HostTables &h = tab->host;
+  std::string t;
+  t.reserve(n * 96);
+  for (int j = 0; j < nlat; j++) {
+    const std::string lat = fmt_g(std::asin(h.mu[j]) / kDegree);
+    for (int k = 0; k < nlon; k++) {
+      const size_t i = static_cast<size_t>(j) * nlon + k;
+      t += fmt_g(2 * 3.14159265358979323846 * k / nlon / kDegree) + " " + lat + " " + fmt_g(hh[i]) + " " + fmt_g(uu[i]) + " " + fmt_g(vv[i]) + " " +
+           fmt_g(zz[i]) + " " + fmt_g(qq[i]) + " " + fmt_g(hs[i]) + "\n";
+    }
+    t += "\n";
+  }
+  write_text(path, t, "Sphere.save_csv");
+}
+
+// one line per latitude: lat, zonal means of h and u
+void SphereEngine::save_zonal_mean(const std::string &path, int member) {
+  check_member(*this, member);
+  const size_t n = ngrid();
+  std::vector<double> hh(n), uu(n);
+  grid(0, hh.data(), member);
+  grid(1, uu.data(), member);
+  const HostTables &h = tab->host;
+  std::string t;
+  for (int j = 0; j < nlat; j++) {
+    double sh = 0, su = 0;
+    for (int k = 0; k < nlon; k++) {
+      sh += hh[static_cast<size_t>(j) * nlon + k];
+      su += uu[static_cast<size_t>(j) * nlon + k];
+    }
+    t += fmt_g(std::asin(h.mu[j]) / kDegree) + " " + fmt_g(sh / nlon) + " " + fmt_g(su / nlon) + "\n";
+  }
+  write_text(path, t, "Sphere.save_zonal_mean");
+}
+
+// one line per total wavenumber n >= 1: n, kinetic and potential energy in that degree
+void SphereEngine::save_spectrum(const std::string &path, int member) {
+  std::vector<double> ke(N + 1), pe(N + 1);
+  spectrum(ke.data(), pe.data(), member);
+  std::string t;
+  for (int n = 1; n <= N; n++) t += std::to_string(n) + " " + fmt_g(ke[n]) + " " + fmt_g(pe[n]) + "\n";
+  write_text(path, t, "Sphere.save_spectrum");
+}
+
 void SphereEngine::spectrum(double *ke, double *pe, int member) {
   std::vector<double> z(2 * nspec_ref()), dd(2 * nspec_ref()), ph(2 * nspec_ref());
   get_state(z.data(), dd.data(), ph.data(), member);
