@@ -32,6 +32,7 @@ UNITS = [
     ("tc_gemm.cu", []),
     ("surrogate.cu", []),
     ("sphere_tables.cpp", []),
+    ("wx_capi.cpp", []),
 ]
 
 
@@ -44,7 +45,8 @@ def nvcc() -> str:
 
 def _deps() -> list[str]:
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(ROOT, "include", "lmweather_gb300.h"))
+    inc = os.path.join(ROOT, "include")
+    files += [os.path.join(inc, f) for f in os.listdir(inc)]
     files.append(os.path.abspath(__file__))
     return files
 

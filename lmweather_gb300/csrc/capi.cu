@@ -82,6 +82,8 @@ void need(bool ok, const char *msg) {
 }
 }  // namespace
 
+int lmw::run_guarded(const std::function<void()> &fn) { return guard(fn); }
+
 extern "C" {
 
 const char *lmw_last_error(void) { return g_err.c_str(); }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -30,6 +31,9 @@ std::string fmt_f(double x);
 // ("<who>: cannot write <path>", a runtime_error) (cpp/main.cpp:84-92)
 std::string fmt_g(double x);
 void write_text(const std::string &path, const std::string &text, const char *who);
+// runs fn with the C ABI's exception-to-status mapping and per-thread message (for entry points defined outside
+// capi.cu)
+int run_guarded(const std::function<void()> &fn);
 
 // Device buffer owned by an engine object.
 template <class T> struct DevBuf {

@@ -44,7 +44,7 @@ def test_header_is_plain_c():
     with tempfile.TemporaryDirectory() as d:
         src = os.path.join(d, "t.c")
         with open(src, "w") as f:
-            f.write('#include "lmweather_gb300.h"\nint main(void) { return lmw_version() == 0; }\n')
+            f.write('#include "lmweather_gb300.h"\n#include "lmweather_wx.h"\nint main(void) { return lmw_version() == 0; }\n')
         r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-c", "-I", os.path.join(ROOT, "include"), src, "-o",
                             os.path.join(d, "t.o")], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
