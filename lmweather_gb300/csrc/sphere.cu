@@ -310,7 +310,8 @@ constexpr int ANA_CHUNKS = 8, ANA_THREADS = 32 * ANA_CHUNKS, ANA_Q = 14;
 // x0: state, xs: stage input (written for stages 0-2), acc: RK4 accumulator. All [B][3][ntri].
 template <class R>
 __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, SphTab<R> t, const typename V2<R>::type *__restrict__ fold,
-                                                            StageArgs sa, double2 *x0, double2 *xs, double2 *acc) {
+                                                            StageArgs sa, double2 *__restrict__ x0, double2 *__restrict__ xs,
+                                                            double2 *__restrict__ acc) {
   using C2 = typename V2<R>::type;
   __shared__ R part[ANA_CHUNKS][ANA_Q][33];
   const int b = blockIdx.y;
@@ -359,18 +360,25 @@ __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, SphTab<R> 
   const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
   // the RK4 state accumulates in FP64 whatever the precision of the tendencies
   const double2 k[3] = {make_double2(kz.x, kz.y), make_double2(kd.x, kd.y), make_double2(kf.x, kf.y)};
+  // every load of the three fields is issued before any store (the buffers never alias)
+  double2 xv[3], av[3];
+#pragma unroll
+  for (int f = 0; f < 3; f++) {
+    xv[f] = x0[base + static_cast<size_t>(f) * d.ntri];
+    av[f] = sa.stage > 0 ? acc[base + static_cast<size_t>(f) * d.ntri] : make_double2(0.0, 0.0);
+  }
 #pragma unroll
   for (int f = 0; f < 3; f++) {
     const size_t i = base + static_cast<size_t>(f) * d.ntri;
     if (sa.stage == 0) {
       acc[i] = k[f];
-      xs[i] = cadd(x0[i], cscale(k[f], sa.c));
+      xs[i] = cadd(xv[f], cscale(k[f], sa.c));
     } else if (sa.stage < 3) {
-      acc[i] = cadd(acc[i], cscale(k[f], 2.0));
-      xs[i] = cadd(x0[i], cscale(k[f], sa.c));
+      acc[i] = cadd(av[f], cscale(k[f], 2.0));
+      xs[i] = cadd(xv[f], cscale(k[f], sa.c));
     } else {
       // cpp/sphere.cpp:428-434: x += dt/6 (k1 + 2k2 + 2k3 + k4), then the del^4 filter
-      double2 val = cadd(x0[i], cscale(cadd(acc[i], k[f]), sa.c));
+      double2 val = cadd(xv[f], cscale(cadd(av[f], k[f]), sa.c));
       const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
       x0[i] = q == 0 ? val : cscale(val, fac);
     }
@@ -1116,7 +1124,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
     const int items = d.M * (sp.ana_both ? 1 : 2) * sp.ntiles;
     const int grid = sp.ana_grid > 0 ? std::min(items, sp.ana_grid) : items;
     auto *k = sp.ana_both ? (sp.direct ? split_ana<true, true> : split_ana<true, false>) : (sp.direct ? split_ana<false, true> : split_ana<false, false>);
-    k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xs, acc);
+    k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, nullptr, acc);
   }
 }
 

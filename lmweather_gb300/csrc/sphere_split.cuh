@@ -544,8 +544,9 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict
 // walks every n of m in order and the FP64 state is read and written with unit stride. Accumulator columns of
 // parity s: H at [cb_s, cb_s + ra_s), P at [cb_s + ra_s, cb_s + 2 ra_s), cb_0 = 0, cb_1 = 2 ra_0 (BOTH).
 template <bool BOTH, bool DIRECT>
-__global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
-                                                             int B, int ns, double2 *x0, double2 *xs, double2 *acc) {
+__global__ void __launch_bounds__(SPLIT_ANA_THREADS, 2) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
+                                                             int B, int ns, double2 *__restrict__ x0, double2 *__restrict__ xs,
+                                                             double2 *__restrict__ acc) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
@@ -724,24 +725,32 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 1) split_ana(SphDev d, Spli
       if (q == 0) kz = kd = kf = make_float2(0, 0);
       const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
       const double2 k[3] = {make_double2(kz.x, kz.y), make_double2(kd.x, kd.y), make_double2(kf.x, kf.y)};
+      // every load of the three fields is issued before any store (the buffers never alias)
+      double2 xv[3], av[3];
+#pragma unroll
+      for (int f = 0; f < 3; f++) {
+        xv[f] = x0[base + static_cast<size_t>(f) * d.ntri];
+        av[f] = sa.stage > 0 ? acc[base + static_cast<size_t>(f) * d.ntri] : make_double2(0.0, 0.0);
+      }
       double2 nv[3];
 #pragma unroll
       for (int f = 0; f < 3; f++) {
         const size_t i = base + static_cast<size_t>(f) * d.ntri;
         if (sa.stage == 0) {
           acc[i] = k[f];
-          nv[f] = cadd(x0[i], cscale(k[f], sa.c));
-          xs[i] = nv[f];
+          nv[f] = cadd(xv[f], cscale(k[f], sa.c));
         } else if (sa.stage < 3) {
-          acc[i] = cadd(acc[i], cscale(k[f], 2.0));
-          nv[f] = cadd(x0[i], cscale(k[f], sa.c));
-          xs[i] = nv[f];
+          acc[i] = cadd(av[f], cscale(k[f], 2.0));
+          nv[f] = cadd(xv[f], cscale(k[f], sa.c));
         } else {
-          const double2 val = cadd(x0[i], cscale(cadd(acc[i], k[f]), sa.c));
+          const double2 val = cadd(xv[f], cscale(cadd(av[f], k[f]), sa.c));
           const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
           nv[f] = q == 0 ? val : cscale(val, fac);
           x0[i] = nv[f];
         }
+        // the stage input in FP64 is kept only when a caller asks for it (the split synthesis reads the packed
+        // operands written below)
+        if (xs != nullptr && sa.stage < 3) xs[i] = nv[f];
       }
       pack_syn_coef(d, sd, kfac, b, m, n, nv[0], nv[1], nv[2]);
     }
