@@ -252,6 +252,10 @@ int lmw_ensemble_stream(lmw_ensemble *e, int group, void **stream);
  * from an FP32 fold) (zeros when the engine is not in split precision; out has 7 entries). No reference
  * counterpart. */
 int lmw_sphere_split_plan(lmw_sphere *s, int *out);
+/* replaces the autotuned plan with `plan` (the 7 entries above), checked against the limits the autotuner's
+ * candidates obey (invalid_argument otherwise); every plan computes the same arithmetic. Validation and tuning
+ * hook; no reference counterpart. */
+int lmw_sphere_set_split_plan(lmw_sphere *s, const int *plan);
 int lmw_ensemble_split_plan(lmw_ensemble *e, int group, int *out);
 int lmw_ensemble_kernel_times(lmw_ensemble *e, int group, int reps, double *ms);
 

@@ -99,6 +99,7 @@ _SIGS = {
     "lmw_ensemble_member_diagnostics": (_I, [_P, _I, _DP]),
     "lmw_ensemble_member_grid": (_I, [_P, _I, _I, _DP, _SZ]),
     "lmw_sphere_split_plan": (_I, [_P, _IP]),
+    "lmw_sphere_set_split_plan": (_I, [_P, _IP]),
     "lmw_sphere_set_tracer_grid": (_I, [_P, _I, _DP, _SZ]),
     "lmw_sphere_probe": (_I, [_P, _I, _I, _D, _D, _DP]),
     "lmw_sphere_mode_coefficient": (_I, [_P, _I, _I, _I, _I, _DP]),
@@ -334,6 +335,19 @@ class Sphere:
         return dict(zip(("lat_pairs_per_grid_cta", "fft_stages_per_pass", "synthesis_stages", "analysis_stages", "analysis_both_parities",
                                  "analysis_ctas", "grid_writes_operands"),
                         out.tolist()))
+
+    _PLAN_KEYS = ("lat_pairs_per_grid_cta", "fft_stages_per_pass", "synthesis_stages", "analysis_stages", "analysis_both_parities",
+                  "analysis_ctas", "grid_writes_operands")
+
+    def set_split_plan(self, **plan) -> None:
+        """Replace entries of the autotuned launch plan (keys as split_plan returns them)."""
+        cur = self.split_plan()
+        unknown = set(plan) - set(cur)
+        if unknown:
+            raise ValueError(f"unknown plan entries: {sorted(unknown)}")
+        cur.update(plan)
+        arr = np.array([cur[k] for k in self._PLAN_KEYS], np.int32)
+        _check(self._lib.lmw_sphere_set_split_plan(self._h, arr.ctypes.data_as(_IP)))
 
     def get_state(self, member: int = 0):
         z, d, f = (np.zeros(self.nspec, np.complex128) for _ in range(3))

@@ -699,6 +699,13 @@ int lmw_sphere_split_plan(lmw_sphere *s, int *out) {
     s->e->split_plan(out);
   });
 }
+int lmw_sphere_set_split_plan(lmw_sphere *s, const int *plan) {
+  return guard([&] {
+    need(s != nullptr && s->e != nullptr, "null sphere handle");
+    need(plan != nullptr, "null buffer");
+    s->e->set_split_plan(plan);
+  });
+}
 int lmw_ensemble_split_plan(lmw_ensemble *e, int group, int *out) {
   return guard([&] {
     need(e != nullptr && e->e != nullptr, "null ensemble handle");

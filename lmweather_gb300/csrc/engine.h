@@ -174,6 +174,9 @@ class SphereEngine {
   // analysis pipeline stages, both parities per analysis CTA, analysis CTA count (6 values; zeros without the split
   // path)
   void split_plan(int *out) const;
+  // replaces the autotuned plan (same 7 entries as split_plan); checked against the shared-memory and
+  // tensor-memory limits the autotuner's candidates obey
+  void set_split_plan(const int *in);
 
  private:
   SphereTables *tab = nullptr;

@@ -188,12 +188,15 @@ __device__ __forceinline__ void dif_group(C2 *s, int rows, int n, int logn, int 
   }
 }
 // inverse transform (decimation in time) of `rows` rows in bit-reversed order, in place
-// fmax: stages per group (1..3; four-stage groups raise the kernels' register count and cost occupancy)
-template <class C2, bool PAD = false>
+// fmax: stages per group (1..FMAX); FMAX = 4 (16 elements per thread) raises the register count, so only kernels
+// instantiated for it (with their own occupancy) take four-stage groups
+template <class C2, bool PAD = false, int FMAX = 3>
 __device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw, int fmax = 3) {
+  if (fmax > FMAX) fmax = FMAX;
   for (int st = 0; st < logn;) {
     const int F = logn - st >= fmax ? fmax : logn - st;
-    if (F == 3) dit_group<C2, 3, PAD>(s, rows, n, logn, st, tw);
+    if (FMAX >= 4 && F == 4) dit_group<C2, 4, PAD>(s, rows, n, logn, st, tw);
+    else if (F == 3) dit_group<C2, 3, PAD>(s, rows, n, logn, st, tw);
     else if (F == 2) dit_group<C2, 2, PAD>(s, rows, n, logn, st, tw);
     else dit_group<C2, 1, PAD>(s, rows, n, logn, st, tw);
     __syncthreads();
@@ -201,12 +204,14 @@ __device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__re
   }
 }
 // forward transform (decimation in frequency) of `rows` rows in natural order, output bit-reversed, in place
-template <class C2, bool PAD = false>
+template <class C2, bool PAD = false, int FMAX = 3>
 __device__ void fft_forward_dif(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw, int fmax = 3) {
+  if (fmax > FMAX) fmax = FMAX;
   for (int hi = logn; hi > 0;) {
     const int F = hi >= fmax ? fmax : hi;
     const int st = hi - F;
-    if (F == 3) dif_group<C2, 3, PAD>(s, rows, n, logn, st, tw);
+    if (FMAX >= 4 && F == 4) dif_group<C2, 4, PAD>(s, rows, n, logn, st, tw);
+    else if (F == 3) dif_group<C2, 3, PAD>(s, rows, n, logn, st, tw);
     else if (F == 2) dif_group<C2, 2, PAD>(s, rows, n, logn, st, tw);
     else dif_group<C2, 1, PAD>(s, rows, n, logn, st, tw);
     __syncthreads();
@@ -648,8 +653,10 @@ static void allow_max_shared_memory() {
   LMW_CUDA(cudaFuncSetAttribute(split_ana<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_ana<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_ana<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_grid<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_grid<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   done_for_device = dev;
 }
 
@@ -1114,10 +1121,8 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   if (which < 0 || which == 1) {
     const dim3 grid(d.nh / sp.jb, B);
     const size_t bytes = 5 * static_cast<size_t>(sp.jb) * fft_row<true>(d.nlon) * sizeof(float2);
-    if (sp.direct)
-      split_grid<true><<<grid, GRID_THREADS, bytes, stream>>>(d, t, sd, fgrid, hsgrid);
-    else
-      split_grid<false><<<grid, GRID_THREADS, bytes, stream>>>(d, t, sd, fgrid, hsgrid);
+    auto *k = sp.fgrp >= 4 ? (sp.direct ? split_grid<true, 4> : split_grid<false, 4>) : (sp.direct ? split_grid<true, 3> : split_grid<false, 3>);
+    k<<<grid, GRID_THREADS, bytes, stream>>>(d, t, sd, fgrid, hsgrid);
   }
   if (which < 0 || which == 2) {
     if (sp.ana_both && 2 * sp.ra_pair > 512) throw InvalidArgument("split precision: both parities' accumulators exceed tensor memory");
@@ -1349,8 +1354,8 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
   split_packed = false;
 }
 
-// Measured choice of the split path's launch plan: latitude pairs per grid CTA (4, 2, 1), FFT stages fused per
-// shared-memory pass (3 or 2), and the pipeline depth of the synthesis and analysis kernels (2-4 stages where
+// Measured choice of the split path's launch plan: latitude pairs per grid CTA (8, 4, 2, 1), FFT stages fused per
+// shared-memory pass (4, 3 or 2), and the pipeline depth of the synthesis and analysis kernels (2-4 stages where
 // they fit) and the analysis variant (one parity or both per CTA). Each kernel is timed alone for every candidate (CUDA events on the engine stream, stage 1 on the
 // present state, which leaves the state unchanged); the arithmetic does not depend on the choice.
 void SphereEngine::autotune_split() {
@@ -1397,7 +1402,7 @@ void SphereEngine::autotune_split() {
   for (int dir = 1; dir >= 0; dir--)
     for (int jb = SPLIT_JB_MAX; jb >= 1; jb /= 2)
       if (nh % jb == 0 && 5 * static_cast<size_t>(jb) * fft_row<true>(nlon) * sizeof(float2) <= static_cast<size_t>(optin - 2048))
-        for (int fg = 3; fg >= 2; fg--) cands.push_back({1, jb, fg, 0, dir, 0, 1e30});
+        for (int fg = 4; fg >= 2; fg--) cands.push_back({1, jb, fg, 0, dir, 0, 1e30});
   for (int ns = 2; ns <= SPLIT_MAX_STAGES; ns++) {
     const size_t bs = std::max(ns * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
     if (bs <= sp.budget_bytes) cands.push_back({0, 0, 0, ns, 0, bs, 1e30});
@@ -1485,6 +1490,37 @@ void SphereEngine::split_plan(int *out) const {
   out[4] = split ? split->ana_both : 0;
   out[5] = split ? split->ana_grid : 0;
   out[6] = split ? split->direct : 0;
+}
+
+void SphereEngine::set_split_plan(const int *in) {
+  if (!split) throw InvalidArgument("the engine is not in split precision");
+  SplitPlan &sp = *split;
+  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6];
+  int dev = 0, optin = 0;
+  LMW_CUDA(cudaGetDevice(&dev));
+  LMW_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (!(jb == 1 || jb == 2 || jb == 4 || jb == 8) || jb > SPLIT_JB_MAX || nh % jb != 0 ||
+      5 * static_cast<size_t>(jb) * fft_row<true>(nlon) * sizeof(float2) > static_cast<size_t>(optin - 2048))
+    throw InvalidArgument("split plan: latitude pairs per grid CTA must be 1, 2, 4 or 8, divide the latitude pairs and fit in shared memory");
+  if (fg < 2 || fg > 4) throw InvalidArgument("split plan: FFT stages per pass must be 2, 3 or 4");
+  if (nss < 2 || nss > SPLIT_MAX_STAGES || nsa < 2 || nsa > SPLIT_MAX_STAGES)
+    throw InvalidArgument("split plan: pipeline stages must be between 2 and " + std::to_string(SPLIT_MAX_STAGES));
+  if ((both != 0 && both != 1) || (dir != 0 && dir != 1) || grid < 0) throw InvalidArgument("split plan: flags must be 0 or 1, the CTA count not negative");
+  if (both && 2 * sp.ra_pair > 512) throw InvalidArgument("split plan: both parities' accumulators exceed tensor memory");
+  const size_t bs = std::max(nss * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
+  const size_t ba = std::max(sp.ana_res_bytes_v[dir] + nsa * sp.ana_stage_bytes_v[dir] + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
+  if (bs > sp.budget_bytes || ba > sp.budget_bytes) throw InvalidArgument("split plan: the pipelines do not fit in shared memory");
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  sp.jb = jb;
+  sp.fgrp = fg;
+  sp.ns_syn = nss;
+  sp.smem_syn = bs;
+  sp.ns_ana = nsa;
+  sp.smem_ana = ba;
+  sp.ana_both = both;
+  sp.ana_grid = grid;
+  sp.direct = dir;
+  graphs_clear();
 }
 
 // the split path keeps its synthesis operands packed from the state; pack them after a change from outside

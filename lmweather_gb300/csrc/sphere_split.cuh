@@ -352,8 +352,9 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
 // as the analysis operands (BF16 pieces in the chunk layout, jb consecutive latitudes per store), which the
 // analysis streams with bulk copies; otherwise written m-major as FP32 fold[m][slot][parity][member][jh] (jb
 // latitudes per store), which the analysis gathers (cheaper for a few members, where jb is small)
-template <bool DIRECT>
-__global__ void __launch_bounds__(GRID_THREADS, 3) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
+// FMAX: the largest FFT stage group the instantiation takes (4: sixteen elements per thread, two CTAs per SM)
+template <bool DIRECT, int FMAX>
+__global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
                                                            const double *__restrict__ hsgrid) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float2 *sm = reinterpret_cast<float2 *>(smraw);  // rows f * jb + p: U, V, zeta, Phi and the fifth product of pair p
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(GRID_THREADS, 3) split_grid(SphDev d, SphTab<f
     }
   }
   __syncthreads();
-  fft_inverse_dit<float2, true>(sm, 4 * JB, n, d.logn, t.tw, sd.fgrp);
+  fft_inverse_dit<float2, true, FMAX>(sm, 4 * JB, n, d.logn, t.tw, sd.fgrp);
   const float g = static_cast<float>(d.g);
   for (int e = threadIdx.x; e < JB * n; e += blockDim.x) {
     const int pr = e >> d.logn, k = e & (n - 1);
@@ -409,7 +410,7 @@ __global__ void __launch_bounds__(GRID_THREADS, 3) split_grid(SphDev d, SphTab<f
     rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
   __syncthreads();
-  fft_forward_dif<float2, true>(sm, 5 * JB, n, d.logn, t.tw, sd.fgrp);
+  fft_forward_dif<float2, true, FMAX>(sm, 5 * JB, n, d.logn, t.tw, sd.fgrp);
   const float inv = 1.0f / n, hinv = 0.5f * inv;
   // one work item per (m, slot r): the folded values of this CTA's latitude pairs at both parities
   for (int e = threadIdx.x; e < M * 5; e += blockDim.x) {

@@ -307,3 +307,42 @@ def test_orography_known_answers(engine):
 
 def test_determinism_known_answers(engine):
     determinism_case(_make(engine), engine.Plane)
+
+
+@pytest.mark.parametrize("T,members,terms", [(21, 24, 3), (42, 16, 6), (85, 16, 3)])
+def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
+    """Every launch plan the autotuner may pick (latitude pairs per grid CTA, FFT stages per shared-memory pass,
+    pipeline depths, one or both parities per analysis CTA, and the grid -> analysis interface) gives the same
+    state bit for bit: the plans move the same operations between CTAs and passes, never reorder them."""
+    nu = 6.37122e6 ** 4 / (86400.0 * (T * (T + 1)) ** 2)
+    s = engine.Sphere(T, diffusion=nu, precision=engine.SPLIT_BF16, members=members, split_terms=terms)
+    for b in range(members):
+        s.turbulence(b + 1, 6000.0 + 100.0 * b, 30.0, T // 2, member=b)
+    start = [s.get_state(b) for b in range(members)]
+    dt = 0.8 * min(s.stable_dt(1.5, member=b) for b in range(members))
+    nh = s.nlat // 2
+    plans = []
+    for jb in (1, 2, 4, 8):
+        if nh % jb:
+            continue
+        for fg in (2, 3, 4):
+            plans.append(dict(lat_pairs_per_grid_cta=jb, fft_stages_per_pass=fg))
+    for both in (0, 1):
+        for direct in (0, 1):
+            plans.append(dict(analysis_both_parities=both, grid_writes_operands=direct, analysis_stages=2, synthesis_stages=3))
+    tuned = s.split_plan()
+    results = []
+    for plan in [{}] + plans:
+        s.set_split_plan(**{**tuned, **plan})
+        for b in range(members):
+            s.set_state(*start[b], member=b)
+        for _ in range(3):
+            s.step(dt)
+        results.append([np.concatenate(s.get_state(b)) for b in range(members)])
+    for plan, res in zip(plans, results[1:]):
+        for b in range(members):
+            assert np.array_equal(res[b], results[0][b]), (plan, b)
+    with pytest.raises(ValueError, match="FFT stages per pass"):
+        s.set_split_plan(fft_stages_per_pass=5)
+    with pytest.raises(ValueError, match="latitude pairs"):
+        s.set_split_plan(lat_pairs_per_grid_cta=3)
