@@ -46,6 +46,11 @@ uint64_t lmw_launch_count(void);
  * on the tensor cores completed). Validation hook; no reference counterpart. */
 int lmw_tc_gemm_selftest(const float *A, const float *B, float *D, int N, int K, int terms, int layout, int *kernel_status);
 
+/* The engine's integer-pipe IEEE conversions (binary32 <-> binary64, used where GB300's narrow FP64 pipe would
+ * otherwise convert) against the hardware conversions on nf float and nx double bit patterns; mismatches[0] and
+ * [1] receive the differing counts (0 and 0 expected). Validation hook; no reference counterpart. */
+int lmw_conversion_selftest(const uint32_t *f, int nf, const uint64_t *x, int nx, int *mismatches);
+
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (the roofline of the FP64 paths) */
 int lmw_fp64_peak(double *tflops);
 

@@ -38,6 +38,7 @@ _FP = C.POINTER(C.c_float)
 _SIGS = {
     "lmw_last_error": (C.c_char_p, []),
     "lmw_version": (C.c_char_p, []),
+    "lmw_conversion_selftest": (_I, [C.POINTER(C.c_uint32), _I, C.POINTER(C.c_uint64), _I, _IP]),
     "lmw_launch_count": (C.c_uint64, []),
     "lmw_sphere_create": (_I, [_I, _D, _D, _D, _D, _PP]),
     "lmw_sphere_create_ex": (_I, [_I, _D, _D, _D, _D, _I, _I, _I, _PP]),

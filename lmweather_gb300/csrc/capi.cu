@@ -95,6 +95,12 @@ int lmw_tc_gemm_selftest(const float *A, const float *B, float *D, int N, int K,
     *kernel_status = lmw::tc_gemm_selftest(A, B, D, N, K, terms, layout);
   });
 }
+int lmw_conversion_selftest(const uint32_t *f, int nf, const uint64_t *x, int nx, int *mismatches) {
+  return guard([&] {
+    need(mismatches != nullptr && (nf == 0 || f != nullptr) && (nx == 0 || x != nullptr), "null buffer");
+    lmw::conversion_selftest_run(f, nf, x, nx, mismatches);
+  });
+}
 int lmw_fp64_peak(double *tflops) {
   return guard([&] {
     need(tflops != nullptr, "output pointer is null");

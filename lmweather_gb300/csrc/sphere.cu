@@ -603,6 +603,44 @@ namespace lmw {
 
 // ================================================================================================ engine
 
+// The integer-pipe conversions against the hardware's, bit for bit: mismatches[0] counts float -> double,
+// mismatches[1] double -> float differences (NaNs compare by NaN-ness).
+__global__ void conversion_selftest(const unsigned *__restrict__ fb, int nf, const unsigned long long *__restrict__ db, int nd,
+                                    int *__restrict__ mismatches) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nf) {
+    const float f = __uint_as_float(fb[i]);
+    const double a = f2d_int(f), b = static_cast<double>(f);
+    const bool same = (a != a && b != b) || __double_as_longlong(a) == __double_as_longlong(b);
+    if (!same) atomicAdd(&mismatches[0], 1);
+  }
+  if (i < nd) {
+    const double x = __longlong_as_double(static_cast<long long>(db[i]));
+    const float a = d2f_int(x), b = static_cast<float>(x);
+    const bool same = (a != a && b != b) || __float_as_uint(a) == __float_as_uint(b);
+    if (!same) atomicAdd(&mismatches[1], 1);
+  }
+}
+
+int conversion_selftest_run(const uint32_t *f, int nf, const uint64_t *x, int nx, int *mismatches) {
+  if (nf < 0 || nx < 0) throw InvalidArgument("counts must not be negative");
+  DevBuf<unsigned> fd;
+  DevBuf<unsigned long long> xd;
+  DevBuf<int> md;
+  fd.alloc(std::max(nf, 1));
+  xd.alloc(std::max(nx, 1));
+  md.alloc(2);
+  if (nf) LMW_CUDA(cudaMemcpy(fd.p, f, nf * sizeof(unsigned), cudaMemcpyHostToDevice));
+  if (nx) LMW_CUDA(cudaMemcpy(xd.p, x, nx * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+  LMW_CUDA(cudaMemset(md.p, 0, 2 * sizeof(int)));
+  const int n = std::max(nf, nx);
+  if (n > 0) conversion_selftest<<<(n + 255) / 256, 256>>>(fd.p, nf, xd.p, nx, md.p);
+  LMW_LAUNCH_CHECK();
+  g_launches += 1;
+  LMW_CUDA(cudaMemcpy(mismatches, md.p, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
 static SphDev make_sph(const SphereEngine &e, const SphereTables &t) {
   SphDev d;
   d.N = e.N;
@@ -615,6 +653,7 @@ static SphDev make_sph(const SphereEngine &e, const SphereTables &t) {
   while ((1 << d.logn) < e.nlon) d.logn++;
   d.a = e.p.radius;
   d.g = e.p.gravity;
+  d.inv_a_f = static_cast<float>(1.0 / e.p.radius);
   d.Ps = t.Ps.p;
   d.Hs = t.Hs.p;
   d.Pa = t.Pa.p;

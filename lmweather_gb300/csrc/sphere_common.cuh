@@ -14,6 +14,7 @@ struct SphDev {
   // per member: bit 0 = the Coriolis grid is tilted (read fgrid, else f = om2 mu), bit 1 = orography (read hsgrid)
   const int *gflag;
   const double *om2;  // 2 Omega per member
+  float inv_a_f;      // 1/a rounded to FP32 once on the host (the FP32 kernels' metric factor)
 };
 
 template <class R> struct V2;
@@ -42,6 +43,34 @@ __device__ __forceinline__ double2 cfma(double2 acc, double2 a, double s) { retu
 __device__ __forceinline__ double2 conjd(double2 a) { return make_double2(a.x, -a.y); }
 // (i m) z
 __device__ __forceinline__ double2 imul(double2 z, double m) { return make_double2(-m * z.y, m * z.x); }
+
+// IEEE 754 conversions between binary32 and binary64 on the integer pipe. GB300 executes FP64 arithmetic and
+// FP64 conversions on a narrow pipe (about 2 operations per clock per SM), so the split path's FP64 epilogues
+// convert with integer operations instead; the results are those of the hardware conversions, bit for bit.
+// float -> double is exact: the exponent is rebiased by 1023 - 127 = 896 and the 23 fraction bits become the top
+// of the 52. Zeros, subnormals, infinities and NaNs (exponent field 0 or 255) take the hardware conversion.
+__device__ __forceinline__ double f2d_int(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return static_cast<double>(f);
+  const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  const unsigned lo = u << 29;
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+}
+// double -> float, rounded to nearest with ties to even, for results in the normal binary32 range: binary64
+// exponents 897..1150 become binary32 exponents 1..254, the fraction keeps its top 23 bits and the 29 dropped
+// bits decide the rounding; a carry out of the fraction raises the exponent (to infinity past 254), as IEEE
+// rounding does. Other exponents (zeros, subnormal results, overflow, infinities, NaNs) take the hardware
+// conversion.
+__device__ __forceinline__ float d2f_int(double x) {
+  const unsigned hi = static_cast<unsigned>(__double2hiint(x)), lo = static_cast<unsigned>(__double2loint(x));
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e < 897u || e > 1150u) return static_cast<float>(x);
+  unsigned r = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rem = lo & 0x1fffffffu;
+  r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
+  return __uint_as_float(r | (hi & 0x80000000u));
+}
 
 constexpr int NSLOT = 5;  // A, B, U Phi, V Phi (times w/((1-mu^2)a)) and the Bernoulli function (times w)
 

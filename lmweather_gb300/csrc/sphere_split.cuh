@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
     __syncthreads();
     // Fourier coefficients of both mirror latitudes: P sums south E + O, north E - O; H sums (opposite parity)
     // south E + O, north O - E; U = (i m chi P - psi H) / a, V = (i m psi P + chi H) / a (cpp/sphere.cpp:200-201)
-    const float mm = static_cast<float>(m), ia = static_cast<float>(1.0 / d.a);
+    const float mm = static_cast<float>(m), ia = d.inv_a_f;
     for (int e = threadIdx.x; e < mt * 32; e += blockDim.x) {
       const int i = e & 31, ml = e >> 5, jh = jh0 + cb + i;
       if (i >= wcols || jh >= d.nh) continue;
@@ -362,6 +362,12 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
   const int b = blockIdx.y, jh0 = blockIdx.x * JB;
   const int tile = b / sd.nbt, ml = b - tile * sd.nbt;
   const int n = d.nlon, M = d.M, rl = fft_row<true>(n);  // padded rows: element i at fft_at<true>(i)
+  // the untilted Coriolis parameter 2 Omega mu of the CTA's latitudes (south, north), rounded to FP32 once
+  __shared__ float cor[2 * SPLIT_JB_MAX];
+  if (threadIdx.x < 2 * JB) {
+    const int pr = threadIdx.x >> 1, js = jh0 + pr, j = (threadIdx.x & 1) ? d.nlat - 1 - js : js;
+    cor[threadIdx.x] = static_cast<float>(d.om2[b] * d.mu[j]);
+  }
   for (int e = threadIdx.x; e < 4 * JB * rl; e += blockDim.x) sm[e] = make_float2(0, 0);
   __syncthreads();
   for (int e = threadIdx.x; e < JB * M; e += blockDim.x) {
@@ -398,12 +404,12 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
     const float2 U = rU[kp], V = rV[kp], Z = rZ[kp], P = rP[kp];
     float2 A, Bv, UP, VP, PE;
     {
-      const float eta = Z.x + static_cast<float>((gf & 1) ? fr_s[k] : d.om2[b] * d.mu[js]);
+      const float eta = Z.x + ((gf & 1) ? static_cast<float>(fr_s[k]) : cor[2 * pr]);
       A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
       PE.x = P.x + g * static_cast<float>((gf & 2) ? hr_s[k] : 0.0) + (U.x * U.x + V.x * V.x) * r2om;
     }
     {
-      const float eta = Z.y + static_cast<float>((gf & 1) ? fr_n[k] : d.om2[b] * d.mu[jn]);
+      const float eta = Z.y + ((gf & 1) ? static_cast<float>(fr_n[k]) : cor[2 * pr + 1]);
       A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
       PE.y = P.y + g * static_cast<float>((gf & 2) ? hr_n[k] : 0.0) + (U.y * U.y + V.y * V.y) * r2om;
     }
@@ -523,8 +529,8 @@ __device__ __forceinline__ void pack_syn_coef(const SphDev &d, const SplitDev &s
   const long baseP = sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kp;
   const long baseH = sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kp;
   const double kf = kfac[n];
-  const float v[8] = {static_cast<float>(z.x * kf), static_cast<float>(z.y * kf), static_cast<float>(dl.x * kf), static_cast<float>(dl.y * kf),
-                      static_cast<float>(z.x),      static_cast<float>(z.y),      static_cast<float>(f.x),       static_cast<float>(f.y)};
+  const float v[8] = {d2f_int(z.x * kf), d2f_int(z.y * kf), d2f_int(dl.x * kf), d2f_int(dl.y * kf),
+                      d2f_int(z.x),      d2f_int(z.y),      d2f_int(f.x),       d2f_int(f.y)};
 #pragma unroll
   for (int q = 0; q < 8; q++) fsplit(v[q], sd.aS_P + baseP + tile_off(ml * 8 + q, k, sd.rSP), sd.aSP_size, sd.pieces);
 #pragma unroll
@@ -725,7 +731,8 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, 2) split_ana(SphDev d, Spli
       const int q = d.tri[m] + n - m;
       if (q == 0) kz = kd = kf = make_float2(0, 0);
       const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
-      const double2 k[3] = {make_double2(kz.x, kz.y), make_double2(kd.x, kd.y), make_double2(kf.x, kf.y)};
+      const double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
+                            make_double2(f2d_int(kf.x), f2d_int(kf.y))};
       // every load of the three fields is issued before any store (the buffers never alias)
       double2 xv[3], av[3];
 #pragma unroll

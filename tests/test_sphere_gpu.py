@@ -346,3 +346,32 @@ def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
         s.set_split_plan(fft_stages_per_pass=5)
     with pytest.raises(ValueError, match="latitude pairs"):
         s.set_split_plan(lat_pairs_per_grid_cta=3)
+
+
+def test_integer_pipe_conversions_match_the_hardware(engine):
+    """The split path converts between FP32 and FP64 with integer operations (GB300's FP64 pipe is narrow); the
+    results must be the hardware conversions' bit for bit, rounding ties, carries into the exponent, overflow to
+    infinity, subnormal results, zeros, infinities and NaNs included."""
+    import ctypes as C
+
+    rng = np.random.default_rng(11)
+    f = rng.integers(0, 2 ** 32, 1 << 20, dtype=np.uint64).astype(np.uint32)
+    f = np.concatenate([f, np.array([0, 0x80000000, 1, 0x807fffff, 0x00800000, 0x7f7fffff, 0x7f800000, 0xff800000, 0x7fc00000,
+                                     0x3f800000, 0xbf800001], np.uint32)])
+    x = rng.integers(0, 2 ** 63, 1 << 20, dtype=np.uint64) | (rng.integers(0, 2, 1 << 20, dtype=np.uint64) << np.uint64(63))
+    # values near the binary32 range and rounding boundaries: exponents 860..1180, fractions at and around ties
+    e = rng.integers(860, 1181, 1 << 20, dtype=np.uint64)
+    frac = rng.integers(0, 2 ** 52, 1 << 20, dtype=np.uint64)
+    ties = (frac >> np.uint64(29) << np.uint64(29)) | np.uint64(1 << 28)
+    near = np.where(rng.integers(0, 3, 1 << 20) == 0, ties, np.where(rng.integers(0, 2, 1 << 20) == 0, ties + np.uint64(1), frac))
+    near = near & np.uint64((1 << 52) - 1)
+    y = (e << np.uint64(52)) | near | (rng.integers(0, 2, 1 << 20, dtype=np.uint64) << np.uint64(63))
+    specials = np.array([0, 1 << 63, 0x7ff0000000000000, 0xfff0000000000000, 0x7ff8000000000000, 0x47efffffe0000000,
+                         0x47efffffefffffff, 0x47effffff0000000, 0x3810000000000000, 0x380fffffffffffff, 0x36a0000000000000,
+                         0x3ff0000010000000, 0x3ff0000030000000, 0x3ff0000010000001], np.uint64)
+    x = np.concatenate([x, y, specials])
+    mism = np.zeros(2, np.int32)
+    lib = engine.load_library()
+    engine._check(lib.lmw_conversion_selftest(f.ctypes.data_as(C.POINTER(C.c_uint32)), f.size, x.ctypes.data_as(C.POINTER(C.c_uint64)), x.size,
+                                              mism.ctypes.data_as(C.POINTER(C.c_int))))
+    assert mism.tolist() == [0, 0]
