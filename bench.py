@@ -346,21 +346,38 @@ def run_ours(args, rank, world, local):
     nlat, nh, M = nlon // 2, nlon // 4, T + 1
     ntri = M * (M + 1) // 2
     pieces = 3 if args.precision == "split6" else 2
-    # algorithmic bytes of one launch (each operand read once, each result written once)
+    split = args.precision.startswith("split")
+    direct = bool(grp.get("autotuned_plan", {}).get("grid_writes_operands", 0)) if split else False
+    # algorithmic bytes of one launch (each operand read once, each result written once). Fourier records: 16
+    # floats per (member, latitude pair, m); analysis operands: 14 rows (7 complex quantities) per (member, m,
+    # parity) over the nh latitudes in `pieces` BF16 pieces (direct interface), or the FP32 fold (10 complex
+    # values per (member, m, latitude pair)); synthesis operands: 12 rows per (member, coefficient) in pieces.
+    records = Bm * nh * M * 16 * 4
+    a_ops = Bm * M * 2 * 14 * nh * pieces * 2 if direct else Bm * M * 10 * nh * 8
+    tables = 2 * pieces * nh * ntri * 2
+    s_ops = Bm * 12 * pieces * ntri * 2
     if ktop == 1:
-        moved = Bm * nh * (M * 24 * 4 + 5 * 2 * M * 8) + Bm * 2 * nlat * nlon * 8 * 2
-        what = "E/O synthesis sums in (24 floats per latitude pair and m), folded analysis inputs out (FP32), f and h_s grids in (FP64)"
+        moved = records + a_ops
+        what = ("Fourier records in (16 floats per member, latitude pair and m), analysis operands out ("
+                + ("BF16 pieces" if direct else "FP32 fold") + ")")
     elif ktop == 0:
-        moved = 2 * pieces * nh * ntri * 2 + Bm * 12 * pieces * ntri * 2 + Bm * nh * M * 24 * 4
-        what = "BF16 P and H tables and state operands in, E/O sums out"
+        moved = tables + s_ops + records
+        what = "BF16 P and H table pieces and synthesis operands in, Fourier records out"
     else:
-        moved = 2 * pieces * nh * ntri * 2 + Bm * nh * M * 10 * 8 + Bm * 3 * ntri * 16 * 3 + Bm * 12 * pieces * ntri * 2
-        what = "BF16 tables and folded inputs in, FP64 state/stage/accumulator updated, next synthesis operands out"
+        moved = tables + a_ops + Bm * 3 * ntri * 16 * 3 + s_ops
+        what = ("BF16 table pieces and analysis operands in, FP64 state read, FP64 RK4 accumulator read and written, "
+                "next synthesis operands out")
+    # DRAM bytes per launch measured by ncu (cold caches) for the T85 x 128 group's kernels, from
+    # profiles/split_kernels_t85x128_ensemble.md; the live bench does not run under the profiler
+    ncu_traffic = {(85, 1, 1): 73.8e6, (85, 2, 1): 155.6e6} if args.precision == "split3" else {}
     pk = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
     achieved = moved / (kt[gtop][ktop] * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": f"{names[ktop]} at T{T} x {Bm} members", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": moved, "bytes_counted": what,
+                "frac": achieved / peak, "traffic": ncu_traffic.get((T, ktop, int(direct))),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, cold caches "
+                                  "(profiles/split_kernels_t85x128_ensemble.md)" if (T, ktop, int(direct)) in ncu_traffic else None,
+                "algorithmic_bytes_per_launch": moved, "bytes_counted": what,
                 "launch_ms": kt[gtop][ktop],
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth), of measured" if "hbm_gbs" in pk else "fallback 6.8 TB/s",
                 "stage_kernel_ms": {f"T{groups[g]['truncation']}": dict(zip(["synthesis", "grid", "analysis"], kt[g])) for g in range(len(groups))}}
