@@ -245,6 +245,13 @@ int lmw_ensemble_groups(lmw_ensemble *e, int *ngroups, int *truncations, int *co
 /* one member's spectral state (reference layout of its truncation), diagnostics (as lmw_sphere_diagnostics) and grids */
 int lmw_ensemble_member_state(lmw_ensemble *e, int member, double *zeta, double *delta, double *phi);
 int lmw_ensemble_member_set_state(lmw_ensemble *e, int member, const double *zeta, const double *delta, const double *phi);
+/* every member's state at once (checkpoint and restart of a whole ensemble): each field holds the members in order,
+ * member i in the reference layout ((T_i+1)^2 complex values, interleaved re/im) after the sum over j < i of
+ * (T_j+1)^2 values. The layout conversion runs on the device; one host <-> device copy per run of consecutive
+ * members of one truncation (pinned host memory copies fastest). set_states keeps each member's time. No reference
+ * counterpart (the reference has no ensembles). */
+int lmw_ensemble_get_states(lmw_ensemble *e, double *zeta, double *delta, double *phi);
+int lmw_ensemble_set_states(lmw_ensemble *e, const double *zeta, const double *delta, const double *phi);
 int lmw_ensemble_member_diagnostics(lmw_ensemble *e, int member, double *out);
 int lmw_ensemble_member_grid(lmw_ensemble *e, int member, int which, double *out, size_t n);
 /* the CUDA stream of a truncation group, and its stage-kernel times as lmw_sphere_kernel_times (measurement

@@ -97,6 +97,8 @@ _SIGS = {
     "lmw_ensemble_groups": (_I, [_P, _IP, _IP, _IP, _DP, C.POINTER(C.c_int64)]),
     "lmw_ensemble_member_state": (_I, [_P, _I, _DP, _DP, _DP]),
     "lmw_ensemble_member_set_state": (_I, [_P, _I, _DP, _DP, _DP]),
+    "lmw_ensemble_get_states": (_I, [_P, _DP, _DP, _DP]),
+    "lmw_ensemble_set_states": (_I, [_P, _DP, _DP, _DP]),
     "lmw_ensemble_member_diagnostics": (_I, [_P, _I, _DP]),
     "lmw_ensemble_member_grid": (_I, [_P, _I, _I, _DP, _SZ]),
     "lmw_sphere_split_plan": (_I, [_P, _IP]),
@@ -669,6 +671,29 @@ class Ensemble:
         z, d, f = (np.zeros((T + 1) ** 2, np.complex128) for _ in range(3))
         _check(self._lib.lmw_ensemble_member_state(self._h, i, _dp(z.view(np.float64)), _dp(d.view(np.float64)), _dp(f.view(np.float64))))
         return z, d, f
+
+    def state_size(self) -> int:
+        """Complex values per field over all members: sum of (T_i+1)^2."""
+        return int(sum((int(T) + 1) ** 2 for T in self.truncation))
+
+    def get_states(self, out=None):
+        """Every member's (zeta, delta, phi) at once: each field concatenates the members in order, member i in the
+        reference layout ((T_i+1)^2 complex values). `out` may give three complex128 arrays to fill (pinned memory
+        copies fastest)."""
+        z, d, f = out if out is not None else tuple(np.zeros(self.state_size(), np.complex128) for _ in range(3))
+        for a in (z, d, f):
+            if a.dtype != np.complex128 or a.size != self.state_size() or not a.flags.c_contiguous:
+                raise ValueError("each field needs a contiguous complex128 array of state_size() values")
+        _check(self._lib.lmw_ensemble_get_states(self._h, _dp(z.view(np.float64)), _dp(d.view(np.float64)), _dp(f.view(np.float64))))
+        return z, d, f
+
+    def set_states(self, zeta, delta, phi):
+        """Set every member's state at once (layout as get_states); each member keeps its time."""
+        arrs = [np.ascontiguousarray(a, np.complex128) for a in (zeta, delta, phi)]
+        for a in arrs:
+            if a.size != self.state_size():
+                raise ValueError("each field needs state_size() complex values")
+        _check(self._lib.lmw_ensemble_set_states(self._h, *(_dp(a.view(np.float64)) for a in arrs)))
 
     def member_diagnostics(self, i: int) -> dict:
         out = np.zeros(8)

@@ -496,6 +496,20 @@ int lmw_ensemble_groups(lmw_ensemble *e, int *ngroups, int *truncations, int *co
     }
   });
 }
+int lmw_ensemble_get_states(lmw_ensemble *e, double *zeta, double *delta, double *phi) {
+  return guard([&] {
+    need(e != nullptr && e->e != nullptr, "null ensemble handle");
+    need(zeta != nullptr && delta != nullptr && phi != nullptr, "null buffer");
+    e->e->get_states(zeta, delta, phi);
+  });
+}
+int lmw_ensemble_set_states(lmw_ensemble *e, const double *zeta, const double *delta, const double *phi) {
+  return guard([&] {
+    need(e != nullptr && e->e != nullptr, "null ensemble handle");
+    need(zeta != nullptr && delta != nullptr && phi != nullptr, "null buffer");
+    e->e->set_states(zeta, delta, phi);
+  });
+}
 int lmw_ensemble_member_state(lmw_ensemble *e, int member, double *zeta, double *delta, double *phi) {
   return ENS({
     int k = 0;

@@ -138,6 +138,11 @@ class SphereEngine {
   // which: 0 height, 1 u, 2 v, 3 vorticity
   void grid(int which, double *out, int member);
   void spectrum(double *ke, double *pe, int member);
+  // every member's state in the reference layout, [field][member][(T+1)^2] complex, on the device:
+  // x0 -> that buffer (asynchronous on the engine stream; returns its device pointer), and back
+  double *states_to_ref();
+  double *device_refstates();
+  void states_from_ref();
   // the wx layer's text files (cpp/main.cpp:328-335, 357-384)
   void save_csv(const std::string &path, int member);
   void save_zonal_mean(const std::string &path, int member);
@@ -187,6 +192,8 @@ class SphereEngine {
   void autotune_split();
   // state (packed triangle, complex interleaved), stage input, accumulator
   DevBuf<double> x0, xs, acc;
+  DevBuf<double> refstates;  // every member's state in the reference layout (allocated on first use)
+
   // Fourier coefficients of the synthesised grids, folded analysis inputs
   DevBuf<double> four, fold;
   DevBuf<float> four32, fold32;
@@ -242,6 +249,11 @@ class EnsembleEngine {
   std::vector<int64_t> last_steps;
   void run(double seconds);
   void check_member(int i) const;
+  // every member's spectral state at once in the reference layout, members in order (member i at offset
+  // sum_{j<i} (T_j+1)^2 complex values of each field); one host <-> device copy per run of consecutive members of a
+  // truncation group
+  void get_states(double *zeta, double *delta, double *phi);
+  void set_states(const double *zeta, const double *delta, const double *phi);
   SphereEngine &engine_of(int i, int *k) {
     check_member(i);
     *k = index_in_group[i];

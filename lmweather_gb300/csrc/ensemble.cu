@@ -74,6 +74,50 @@ void EnsembleEngine::run(double seconds) {
   }
 }
 
+// Runs of consecutive members in one group with consecutive indices in it: one copy per run and field.
+template <class F> static void for_runs(const EnsembleEngine &e, F &&fn) {
+  const int n = static_cast<int>(e.members.size());
+  size_t off = 0;  // complex values before member i in each field
+  for (int i = 0; i < n;) {
+    int j = i + 1;
+    while (j < n && e.group_of[j] == e.group_of[i] && e.index_in_group[j] == e.index_in_group[j - 1] + 1) j++;
+    const size_t mm = static_cast<size_t>(e.truncations[e.group_of[i]] + 1) * (e.truncations[e.group_of[i]] + 1);
+    fn(e.group_of[i], e.index_in_group[i], j - i, off, mm);
+    off += mm * (j - i);
+    i = j;
+  }
+}
+
+void EnsembleEngine::get_states(double *zeta, double *delta, double *phi) {
+  std::vector<double *> dev(groups.size());
+  for (size_t g = 0; g < groups.size(); g++) dev[g] = groups[g]->states_to_ref();
+  double *out[3] = {zeta, delta, phi};
+  for_runs(*this, [&](int g, int k0, int cnt, size_t off, size_t mm) {
+    SphereEngine &s = *groups[g];
+    for (int f = 0; f < 3; f++)
+      LMW_CUDA(cudaMemcpyAsync(out[f] + 2 * off, dev[g] + 2 * ((static_cast<size_t>(f) * s.B + k0) * mm), cnt * mm * 2 * sizeof(double),
+                               cudaMemcpyDeviceToHost, s.stream));
+  });
+  for (auto &g : groups) LMW_CUDA(cudaStreamSynchronize(g->stream));
+}
+
+void EnsembleEngine::set_states(const double *zeta, const double *delta, const double *phi) {
+  std::vector<double *> dev(groups.size());
+  for (size_t g = 0; g < groups.size(); g++) {
+    LMW_CUDA(cudaStreamSynchronize(groups[g]->stream));
+    dev[g] = groups[g]->device_refstates();
+  }
+  const double *in[3] = {zeta, delta, phi};
+  for_runs(*this, [&](int g, int k0, int cnt, size_t off, size_t mm) {
+    SphereEngine &s = *groups[g];
+    for (int f = 0; f < 3; f++)
+      LMW_CUDA(cudaMemcpyAsync(dev[g] + 2 * ((static_cast<size_t>(f) * s.B + k0) * mm), in[f] + 2 * off, cnt * mm * 2 * sizeof(double),
+                               cudaMemcpyHostToDevice, s.stream));
+  });
+  for (auto &g : groups) g->states_from_ref();
+  for (auto &g : groups) LMW_CUDA(cudaStreamSynchronize(g->stream));
+}
+
 void EnsembleEngine::check_member(int i) const {
   if (i < 0 || i >= static_cast<int>(members.size())) throw InvalidArgument("member index out of range");
 }

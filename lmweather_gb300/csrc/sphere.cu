@@ -974,6 +974,42 @@ void SphereEngine::from_packed(const double *packed, double *ref) {
     }
 }
 
+// packed triangles [B][3][ntri] <-> reference layout [3][B][M*M] (zeros where n < m). grid: (ceil(M*M/256), 3, B)
+__global__ void state_to_ref(SphDev d, const double2 *__restrict__ x, double2 *__restrict__ ref, int B) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, f = blockIdx.y, b = blockIdx.z;
+  if (i >= d.M * d.M) return;
+  const int m = i / d.M, n = i - m * d.M;
+  ref[(static_cast<size_t>(f) * B + b) * d.M * d.M + i] =
+      n >= m ? x[(static_cast<size_t>(b) * 3 + f) * d.ntri + d.tri[m] + n - m] : make_double2(0.0, 0.0);
+}
+__global__ void state_from_ref(SphDev d, const double2 *__restrict__ ref, double2 *__restrict__ x, int B) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, f = blockIdx.y, b = blockIdx.z;
+  if (i >= d.M * d.M) return;
+  const int m = i / d.M, n = i - m * d.M;
+  if (n >= m) x[(static_cast<size_t>(b) * 3 + f) * d.ntri + d.tri[m] + n - m] = ref[(static_cast<size_t>(f) * B + b) * d.M * d.M + i];
+}
+
+double *SphereEngine::device_refstates() {
+  const size_t need = static_cast<size_t>(3) * B * M * M * 2;
+  if (refstates.n < need) refstates.alloc(need);
+  return refstates.p;
+}
+double *SphereEngine::states_to_ref() {
+  double *r = device_refstates();
+  SphDev d = make_sph(*this, *tab);
+  state_to_ref<<<dim3((M * M + 255) / 256, 3, B), 256, 0, stream>>>(d, reinterpret_cast<const double2 *>(x0.p), reinterpret_cast<double2 *>(r), B);
+  LMW_LAUNCH_CHECK();
+  g_launches += 1;
+  return r;
+}
+void SphereEngine::states_from_ref() {
+  SphDev d = make_sph(*this, *tab);
+  state_from_ref<<<dim3((M * M + 255) / 256, 3, B), 256, 0, stream>>>(d, reinterpret_cast<const double2 *>(refstates.p), reinterpret_cast<double2 *>(x0.p), B);
+  LMW_LAUNCH_CHECK();
+  g_launches += 1;
+  split_packed = false;
+}
+
 void SphereEngine::set_state(const double *zeta, const double *delta, const double *phi, double time, int member) {
   check_member(*this, member);
   split_packed = false;
