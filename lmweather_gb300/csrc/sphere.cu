@@ -39,27 +39,33 @@ struct SphereTables {
 namespace {
 
 // ------------------------------------------------------------------------------------------------ synthesis
-// Block: SYN_CHUNKS warps for one wavenumber m and 32 southern latitudes (lane = latitude). Warp c sums the terms
-// n = m + c, m + c + SYN_CHUNKS, ... (one parity of n - m per warp), so the n-sum runs in SYN_CHUNKS pieces at
-// once; the pieces meet in shared memory. Reading the coefficient-major table is coalesced across the lanes.
-constexpr int SYN_CHUNKS = 8, SYN_THREADS = 32 * SYN_CHUNKS, SYN_Q = 12;
+// Block: one wavenumber m and LATS southern latitudes (thread % LATS = latitude); the SYN_THREADS / LATS thread
+// groups sum the terms n = m + c, m + c + NCH, ... (one parity of n - m per group), so the n-sum runs in NCH pieces
+// at once; the pieces meet in shared memory. Reading the coefficient-major table is coalesced across latitudes.
+// LATS = 32 (8 pieces) in general; LATS = 8 (32 pieces, four times the blocks) for grids of at most 32 latitude
+// pairs (T <= 42), whose launches would otherwise occupy a fraction of the SMs. The choice depends on the grid
+// only, so every member of a truncation is summed in the same order whatever the batch.
+constexpr int SYN_THREADS = 256, SYN_Q = 12;
+constexpr int SYN_CHUNKS = 8;  // n-sum pieces of the 32-latitude blocks (the tracer's synthesis uses this form)
+__host__ __device__ constexpr int syn_lats(int nh) { return nh <= 32 ? 8 : 32; }
 
 // x: [B][3][ntri] (zeta, delta, phi); four: [B][nlat][4][M] (U, V, zeta, Phi)
-template <class R>
+template <class R, int LATS>
 __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, SphTab<R> t, const double2 *__restrict__ x,
                                                          typename V2<R>::type *__restrict__ four) {
   using C2 = typename V2<R>::type;
-  __shared__ R part[SYN_CHUNKS][SYN_Q][33];
+  constexpr int NCH = SYN_THREADS / LATS;
+  __shared__ R part[NCH][SYN_Q][LATS + 1];
   const int b = blockIdx.z, m = blockIdx.y;
-  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
-  const int jh = blockIdx.x * 32 + lane;
+  const int lane = threadIdx.x % LATS, c = threadIdx.x / LATS;
+  const int jh = blockIdx.x * LATS + lane;
   const bool live = jh < d.nh;
   const double2 *xz = x + static_cast<size_t>(b) * 3 * d.ntri, *xd = xz + d.ntri, *xf = xd + d.ntri;
   C2 sp = mk2(R(0), R(0)), sc = sp, hp = sp, hc = sp, zs = sp, fs = sp;
   const int base = d.tri[m];
   if (live) {
 #pragma unroll 2
-    for (int n = m + c; n <= d.N; n += SYN_CHUNKS) {
+    for (int n = m + c; n <= d.N; n += NCH) {
       const int q = base + n - m;
       const R P = t.Ps[static_cast<size_t>(q) * d.nh + jh], H = t.Hs[static_cast<size_t>(q) * d.nh + jh];
       const double2 zd = xz[q], dd = xd[q], fd = xf[q];
@@ -78,22 +84,39 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, SphTab<R> t, 
 #pragma unroll
   for (int i = 0; i < SYN_Q; i++) part[c][i][lane] = v[i];
   __syncthreads();
-  if (threadIdx.x >= 64) return;
-  const int side = threadIdx.x >> 5;  // 0: southern latitude (table latitude), 1: its northern mirror
-  if (!live) return;
-  // even (n - m) pieces are the chunks with even c, odd pieces the chunks with odd c
+  // even (n - m) pieces are those of even c, odd pieces those of odd c, each summed in the order of c
   R e[SYN_Q], o[SYN_Q];
+  if constexpr (NCH <= 8) {
+    if (threadIdx.x >= 2 * LATS || !live) return;
 #pragma unroll
-  for (int i = 0; i < SYN_Q; i++) {
-    R se = 0, so = 0;
+    for (int i = 0; i < SYN_Q; i++) {
+      R se = 0, so = 0;
 #pragma unroll
-    for (int k = 0; k < SYN_CHUNKS; k += 2) {
-      se += part[k][i][lane];
-      so += part[k + 1][i][lane];
+      for (int k = 0; k < NCH; k += 2) {
+        se += part[k][i][lane];
+        so += part[k + 1][i][lane];
+      }
+      e[i] = se;
+      o[i] = so;
     }
-    e[i] = se;
-    o[i] = so;
+  } else {
+    // many pieces: every thread sums one (parity, value, latitude) first
+    __shared__ R red[2][SYN_Q][LATS];
+    for (int w = threadIdx.x; w < 2 * SYN_Q * LATS; w += SYN_THREADS) {
+      const int par = w / (SYN_Q * LATS), i = (w / LATS) % SYN_Q, l = w % LATS;
+      R acc = 0;
+      for (int k = par; k < NCH; k += 2) acc += part[k][i][l];
+      red[par][i][l] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x >= 2 * LATS || !live) return;
+#pragma unroll
+    for (int i = 0; i < SYN_Q; i++) {
+      e[i] = red[0][i][lane];
+      o[i] = red[1][i][lane];
+    }
   }
+  const int side = threadIdx.x / LATS;  // 0: southern latitude (table latitude), 1: its northern mirror
   // southern latitude: even + odd; northern mirror: P sums even - odd, H sums odd - even
   R r[SYN_Q];
 #pragma unroll
@@ -101,7 +124,7 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, SphTab<R> t, 
     const bool hsum = i >= 4 && i < 8;
     r[i] = side == 0 ? e[i] + o[i] : (hsum ? o[i] - e[i] : e[i] - o[i]);
   }
-  const R mm = static_cast<R>(m), ia = static_cast<R>(1.0 / d.a);
+  const R mm = static_cast<R>(m), ia = static_cast<R>(d.inv_a_f);
   const C2 SP = mk2(r[0], r[1]), SC = mk2(r[2], r[3]), HP = mk2(r[4], r[5]), HC = mk2(r[6], r[7]);
   // cpp/sphere.cpp:200-201: fu = (i m sc - hp)/a, fv = (i m sp + hc)/a
   C2 fu = csub(imul(SC, mm), HP), fv = cadd(imul(SP, mm), HC);
@@ -305,23 +328,28 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, SphTab<R> t, 
 }
 
 // ------------------------------------------------------------------------------------------------ analysis + RK4
-// Block: ANA_CHUNKS warps for 32 spectral coefficients (lane = coefficient, coalesced latitude-major tables).
-// Warp c sums the latitude pairs jh = c, c + ANA_CHUNKS, ...; the pieces meet in shared memory and warp 0 forms
-// the tendencies and applies the RK4 stage update.
+// Block: spectral coefficients (thread % COEF = coefficient, coalesced latitude-major tables) and latitude pieces
+// (thread / COEF = c sums the latitude pairs jh = c, c + NCH, ...); the pieces meet in shared memory and the
+// threads of piece 0 form the tendencies and apply the RK4 stage update. ANA_CHUNKS: the pieces of the 32-coefficient
+// blocks (the tracer's analysis uses this form).
 constexpr int ANA_CHUNKS = 8, ANA_THREADS = 32 * ANA_CHUNKS, ANA_Q = 14;
 
 
 
 // x0: state, xs: stage input (written for stages 0-2), acc: RK4 accumulator. All [B][3][ntri].
-template <class R>
+// COEF coefficients per block (thread % COEF) and ANA_THREADS / COEF latitude pieces: 32 x 8 in general, 8 x 32 for
+// grids of at most 32 latitude pairs (T <= 42), chosen by the grid only (ana_coef) like the synthesis's blocks.
+__host__ __device__ constexpr int ana_coef(int nh) { return nh <= 32 ? 8 : 32; }
+template <class R, int COEF>
 __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, SphTab<R> t, const typename V2<R>::type *__restrict__ fold,
                                                             StageArgs sa, double2 *__restrict__ x0, double2 *__restrict__ xs,
                                                             double2 *__restrict__ acc) {
   using C2 = typename V2<R>::type;
-  __shared__ R part[ANA_CHUNKS][ANA_Q][33];
+  constexpr int NCH = ANA_THREADS / COEF;
+  __shared__ R part[NCH][ANA_Q][COEF + 1];
   const int b = blockIdx.y;
-  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
-  const int q = blockIdx.x * 32 + lane;
+  const int lane = threadIdx.x % COEF, c = threadIdx.x / COEF;
+  const int q = blockIdx.x * COEF + lane;
   const bool live = q < d.ntri;
   const int m = live ? d.trim[q] : 0, n = live ? d.trin[q] : 0, par = (n - m) & 1;
   const C2 *fb = fold + static_cast<size_t>(b) * d.nh * NSLOT * 2 * d.M;
@@ -329,7 +357,7 @@ __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, SphTab<R> 
   C2 aP = mk2(R(0), R(0)), bH = aP, bP = aP, aH = aP, uP = aP, vH = aP, eP = aP;
   if (live) {
 #pragma unroll 2
-    for (int jh = c; jh < d.nh; jh += ANA_CHUNKS) {
+    for (int jh = c; jh < d.nh; jh += NCH) {
       const R P = t.Pa[static_cast<size_t>(jh) * d.ntri + q], H = t.Ha[static_cast<size_t>(jh) * d.ntri + q];
       const C2 *g = fb + static_cast<size_t>(jh) * NSLOT * 2 * d.M;
       aP = cfma(aP, g[0 * 2 * d.M + sP], P);
@@ -345,14 +373,29 @@ __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, SphTab<R> 
 #pragma unroll
   for (int i = 0; i < ANA_Q; i++) part[c][i][lane] = v[i];
   __syncthreads();
-  if (c != 0 || !live) return;
   R tsum[ANA_Q];
+  if constexpr (NCH <= 8) {
+    if (c != 0 || !live) return;
 #pragma unroll
-  for (int i = 0; i < ANA_Q; i++) {
-    R acc_i = 0;
+    for (int i = 0; i < ANA_Q; i++) {
+      R acc_i = 0;
 #pragma unroll
-    for (int k = 0; k < ANA_CHUNKS; k++) acc_i += part[k][i][lane];
-    tsum[i] = acc_i;
+      for (int k = 0; k < NCH; k++) acc_i += part[k][i][lane];
+      tsum[i] = acc_i;
+    }
+  } else {
+    // many pieces: every thread sums one (value, coefficient) first, in the order of the pieces
+    __shared__ R red[ANA_Q][COEF];
+    for (int w = threadIdx.x; w < ANA_Q * COEF; w += ANA_THREADS) {
+      const int i = w / COEF, l = w % COEF;
+      R acc_i = 0;
+      for (int k = 0; k < NCH; k++) acc_i += part[k][i][l];
+      red[i][l] = acc_i;
+    }
+    __syncthreads();
+    if (c != 0 || !live) return;
+#pragma unroll
+    for (int i = 0; i < ANA_Q; i++) tsum[i] = red[i][lane];
   }
   aP = mk2(tsum[0], tsum[1]); aH = mk2(tsum[2], tsum[3]); bP = mk2(tsum[4], tsum[5]); bH = mk2(tsum[6], tsum[7]);
   uP = mk2(tsum[8], tsum[9]); vH = mk2(tsum[10], tsum[11]); eP = mk2(tsum[12], tsum[13]);
@@ -908,9 +951,10 @@ void SphereEngine::synth_grids(int member_first, int count) {
   SphDev d = make_sph(*this, *tab);
   const size_t st = static_cast<size_t>(member_first) * 3 * ntri;
   const size_t fo = static_cast<size_t>(member_first) * nlat * 4 * M;
-  dim3 g((nh + 31) / 32, M, count);
-  sph_synth<double><<<g, SYN_THREADS, 0, stream>>>(d, tab64(*tab), reinterpret_cast<const double2 *>(x0.p) + st,
-                                                   reinterpret_cast<double2 *>(four.p) + fo);
+  const int L = syn_lats(nh);
+  dim3 g((nh + L - 1) / L, M, count);
+  auto *k = L == 8 ? sph_synth<double, 8> : sph_synth<double, 32>;
+  k<<<g, SYN_THREADS, 0, stream>>>(d, tab64(*tab), reinterpret_cast<const double2 *>(x0.p) + st, reinterpret_cast<double2 *>(four.p) + fo);
   LMW_LAUNCH_CHECK();
   g_launches += 1;
 }
@@ -1175,10 +1219,20 @@ static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage,
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
   sa.filt = filt;
   sa.zero = zero;
-  if (which < 0 || which == 0) sph_synth<R><<<dim3((d.nh + 31) / 32, d.M, B), SYN_THREADS, 0, stream>>>(d, t, in, four);
+  if (which < 0 || which == 0) {
+    if (syn_lats(d.nh) == 8)
+      sph_synth<R, 8><<<dim3((d.nh + 7) / 8, d.M, B), SYN_THREADS, 0, stream>>>(d, t, in, four);
+    else
+      sph_synth<R, 32><<<dim3((d.nh + 31) / 32, d.M, B), SYN_THREADS, 0, stream>>>(d, t, in, four);
+  }
   if (which < 0 || which == 1) sph_grid<R><<<dim3(d.nh, B), GRID_THREADS, smem, stream>>>(d, t, four, fgrid, hsgrid, fold);
   if (which < 0 || which == 2)
-    sph_analysis<R><<<dim3((d.ntri + 31) / 32, B), ANA_THREADS, 0, stream>>>(d, t, fold, sa, x0, xs, acc);
+  {
+    if (ana_coef(d.nh) == 8)
+      sph_analysis<R, 8><<<dim3((d.ntri + 7) / 8, B), ANA_THREADS, 0, stream>>>(d, t, fold, sa, x0, xs, acc);
+    else
+      sph_analysis<R, 32><<<dim3((d.ntri + 31) / 32, B), ANA_THREADS, 0, stream>>>(d, t, fold, sa, x0, xs, acc);
+  }
 }
 
 // One RK4 stage in split precision: tensor-core synthesis, FP32 grid stage, tensor-core analysis with the RK4
