@@ -418,9 +418,11 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
   __syncthreads();
   fft_forward_dif<float2, true, FMAX>(sm, 5 * JB, n, d.logn, t.tw, sd.fgrp);
   const float inv = 1.0f / n, hinv = 0.5f * inv;
-  // one work item per (m, slot r): the folded values of this CTA's latitude pairs at both parities
+  // one work item per (m, slot r): the folded values of this CTA's latitude pairs at both parities. Direct
+  // operands: the five slots of one m are consecutive threads, so a warp's stores of one row pair land in the
+  // same few core matrices; FP32 fold: consecutive m
   for (int e = threadIdx.x; e < M * 5; e += blockDim.x) {
-    const int m = e % M, r = e / M;
+    const int m = DIRECT ? e / 5 : e % M, r = DIRECT ? e - 5 * (e / 5) : e / M;
     {
       float2 f0[SPLIT_JB_MAX], f1[SPLIT_JB_MAX];
 #pragma unroll
