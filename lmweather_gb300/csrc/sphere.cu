@@ -157,6 +157,17 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, SphTab<R> t, 
 template <bool PAD> __device__ __forceinline__ int fft_at(int i) { return PAD ? i + (i >> 3) : i; }
 template <bool PAD> __host__ __device__ __forceinline__ int fft_row(int n) { return PAD ? n + (n >> 3) : n; }
 
+// FP32 twiddle tables hold tw[k + n/4] = -i tw[k] exactly (built that way), so FP32 groups derive the upper half
+// of each stage's twiddles from the lower half; FP64 tables are the reference's cos/sin values and are all loaded.
+template <class C2> constexpr bool TW_SYM = sizeof(C2) == 8;
+// twiddle products of the butterflies. FP32: explicit single-rounding operations, so a twiddle derived by the
+// rotation and the same twiddle loaded from the table multiply identically whatever the compiler would contract
+// (every stage grouping gives the same bits); FP64: the plain product.
+__device__ __forceinline__ float2 cmul_tw(float2 w, float2 x) {
+  return make_float2(__fmaf_rn(w.x, x.x, -__fmul_rn(w.y, x.y)), __fmaf_rn(w.x, x.y, __fmul_rn(w.y, x.x)));
+}
+__device__ __forceinline__ double2 cmul_tw(double2 w, double2 x) { return cmul(w, x); }
+
 template <class C2, int F, bool PAD>
 __device__ __forceinline__ void dit_group(C2 *s, int rows, int n, int logn, int st, const C2 *__restrict__ tw) {
   constexpr int E = 1 << F;
@@ -171,11 +182,19 @@ __device__ __forceinline__ void dit_group(C2 *s, int rows, int n, int logn, int 
 #pragma unroll
     for (int f = 0; f < F; f++) {
       const int h = 1 << f, stride = halfn >> (st + f);
+      // the stage's h twiddles; FP32: the upper half is the lower half times +i (the table is built with that
+      // symmetry, so the value is the table's), which saves half the twiddle loads
+      C2 wv[E / 2];
+#pragma unroll
+      for (int jj = 0; jj < h; jj++) {
+        if (TW_SYM<C2> && jj >= (h >> 1) && h >= 2) wv[jj] = mk2(-wv[jj - (h >> 1)].y, wv[jj - (h >> 1)].x);
+        else wv[jj] = conjd(tw[((q & lo) + (jj << st)) * stride]);
+      }
 #pragma unroll
       for (int j = 0; j < E; j++) {
         if (j & h) continue;
-        const C2 w = conjd(tw[((q & lo) + ((j & (h - 1)) << st)) * stride]);
-        const C2 t = cmul(w, x[j + h]), u = x[j];
+        const C2 w = wv[j & (h - 1)];
+        const C2 t = cmul_tw(w, x[j + h]), u = x[j];
         x[j] = cadd(u, t);
         x[j + h] = csub(u, t);
       }
@@ -198,12 +217,19 @@ __device__ __forceinline__ void dif_group(C2 *s, int rows, int n, int logn, int 
 #pragma unroll
     for (int f = F - 1; f >= 0; f--) {
       const int h = 1 << f, stride = halfn >> (st + f);
+      // FP32: the upper half of the stage's twiddles is the lower half times -i (see dit_group)
+      C2 wv[E / 2];
+#pragma unroll
+      for (int jj = 0; jj < h; jj++) {
+        if (TW_SYM<C2> && jj >= (h >> 1) && h >= 2) wv[jj] = mk2(wv[jj - (h >> 1)].y, -wv[jj - (h >> 1)].x);
+        else wv[jj] = tw[((q & lo) + (jj << st)) * stride];
+      }
 #pragma unroll
       for (int j = 0; j < E; j++) {
         if (j & h) continue;
         const C2 u = x[j], v = x[j + h];
         x[j] = cadd(u, v);
-        x[j + h] = cmul(csub(u, v), tw[((q & lo) + ((j & (h - 1)) << st)) * stride]);
+        x[j + h] = cmul_tw(wv[j & (h - 1)], csub(u, v));
       }
     }
 #pragma unroll
@@ -827,8 +853,12 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
     up32(tab->r2om32, r2);
     up32(tab->kfac32, kf);
     up32(tab->lapl32, lp);
+    // FP32 twiddles: the first quarter rounded from FP64, the second quarter exactly -i times the first (the
+    // FP32 FFT groups derive those from the first quarter)
     std::vector<float2> t32(tw.size());
-    for (size_t k = 0; k < tw.size(); k++) t32[k] = make_float2(static_cast<float>(tw[k].x), static_cast<float>(tw[k].y));
+    const size_t q4 = tw.size() / 2;
+    for (size_t k = 0; k < tw.size(); k++)
+      t32[k] = k < q4 || q4 == 0 ? make_float2(static_cast<float>(tw[k].x), static_cast<float>(tw[k].y)) : make_float2(t32[k - q4].y, -t32[k - q4].x);
     tab->tw32.alloc(t32.size());
     LMW_CUDA(cudaMemcpy(tab->tw32.p, t32.data(), t32.size() * sizeof(float2), cudaMemcpyHostToDevice));
   }
