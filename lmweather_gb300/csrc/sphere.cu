@@ -1514,7 +1514,7 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
 }
 
 // Measured choice of the split path's launch plan: latitude pairs per grid CTA (8, 4, 2, 1), FFT stages fused per
-// shared-memory pass (4, 3 or 2), and the pipeline depth of the synthesis and analysis kernels (2-4 stages where
+// shared-memory pass (4, 3 or 2), and the pipeline depth of the synthesis and analysis kernels (1-4 stages where
 // they fit) and the analysis variant (one parity or both per CTA). Each kernel is timed alone for every candidate (CUDA events on the engine stream, stage 1 on the
 // present state, which leaves the state unchanged); the arithmetic does not depend on the choice.
 void SphereEngine::autotune_split() {
@@ -1562,7 +1562,8 @@ void SphereEngine::autotune_split() {
     for (int jb = SPLIT_JB_MAX; jb >= 1; jb /= 2)
       if (nh % jb == 0 && 5 * static_cast<size_t>(jb) * fft_row<true>(nlon) * sizeof(float2) <= static_cast<size_t>(optin - 2048))
         for (int fg = 4; fg >= 2; fg--) cands.push_back({1, jb, fg, 0, dir, 0, 1e30});
-  for (int ns = 2; ns <= SPLIT_MAX_STAGES; ns++) {
+  // one stage (no double buffering inside a CTA) leaves room for a third CTA per SM, whose copies overlap the others'
+  for (int ns = 1; ns <= SPLIT_MAX_STAGES; ns++) {
     const size_t bs = std::max(ns * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
     if (bs <= sp.budget_bytes) cands.push_back({0, 0, 0, ns, 0, bs, 1e30});
     for (int dir = 1; dir >= 0; dir--)
@@ -1662,8 +1663,8 @@ void SphereEngine::set_split_plan(const int *in) {
       5 * static_cast<size_t>(jb) * fft_row<true>(nlon) * sizeof(float2) > static_cast<size_t>(optin - 2048))
     throw InvalidArgument("split plan: latitude pairs per grid CTA must be 1, 2, 4 or 8, divide the latitude pairs and fit in shared memory");
   if (fg < 2 || fg > 4) throw InvalidArgument("split plan: FFT stages per pass must be 2, 3 or 4");
-  if (nss < 2 || nss > SPLIT_MAX_STAGES || nsa < 2 || nsa > SPLIT_MAX_STAGES)
-    throw InvalidArgument("split plan: pipeline stages must be between 2 and " + std::to_string(SPLIT_MAX_STAGES));
+  if (nss < 1 || nss > SPLIT_MAX_STAGES || nsa < 1 || nsa > SPLIT_MAX_STAGES)
+    throw InvalidArgument("split plan: pipeline stages must be between 1 and " + std::to_string(SPLIT_MAX_STAGES));
   if ((both != 0 && both != 1) || (dir != 0 && dir != 1) || grid < 0) throw InvalidArgument("split plan: flags must be 0 or 1, the CTA count not negative");
   if (both && 2 * sp.ra_pair > 512) throw InvalidArgument("split plan: both parities' accumulators exceed tensor memory");
   const size_t bs = std::max(nss * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);

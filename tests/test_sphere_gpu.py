@@ -330,6 +330,7 @@ def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
     for both in (0, 1):
         for direct in (0, 1):
             plans.append(dict(analysis_both_parities=both, grid_writes_operands=direct, analysis_stages=2, synthesis_stages=3))
+    plans.append(dict(analysis_stages=1, synthesis_stages=1))
     tuned = s.split_plan()
     results = []
     for plan in [{}] + plans:
