@@ -757,10 +757,9 @@ static void allow_max_shared_memory() {
   LMW_CUDA(cudaFuncSetAttribute(sph_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(sph_grid_in, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_syn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_ana<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_ana<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_ana<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_ana<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  for (auto *k : {split_ana<false, false, 2>, split_ana<true, false, 2>, split_ana<false, true, 2>, split_ana<true, true, 2>,
+                  split_ana<false, false, 3>, split_ana<true, false, 3>, split_ana<false, true, 3>, split_ana<true, true, 3>})
+    LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_grid<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
@@ -1287,7 +1286,11 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
     if (sp.ana_both && 2 * sp.ra_pair > 512) throw InvalidArgument("split precision: both parities' accumulators exceed tensor memory");
     const int items = d.M * (sp.ana_both ? 1 : 2) * sp.ntiles;
     const int grid = sp.ana_grid > 0 ? std::min(items, sp.ana_grid) : items;
-    auto *k = sp.ana_both ? (sp.direct ? split_ana<true, true> : split_ana<true, false>) : (sp.direct ? split_ana<false, true> : split_ana<false, false>);
+    auto *k = sp.ana_minb >= 3
+                  ? (sp.ana_both ? (sp.direct ? split_ana<true, true, 3> : split_ana<true, false, 3>)
+                                 : (sp.direct ? split_ana<false, true, 3> : split_ana<false, false, 3>))
+                  : (sp.ana_both ? (sp.direct ? split_ana<true, true, 2> : split_ana<true, false, 2>)
+                                 : (sp.direct ? split_ana<false, true, 2> : split_ana<false, false, 2>));
     k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, nullptr, acc);
   }
 }
@@ -1551,6 +1554,7 @@ void SphereEngine::autotune_split() {
     int which, jb, fg, ns, dir;
     size_t bytes;
     double best;
+    int mb = 2;  // analysis register budget (CTAs per SM)
   };
   std::vector<Cand> cands;
   int dev = 0, optin = 0;
@@ -1573,10 +1577,13 @@ void SphereEngine::autotune_split() {
                                    both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
         if (ba > sp.budget_bytes) continue;
         // one CTA per work item (persistent CTAs, ana_grid > 0, measured no faster on GB300 and are not tried)
-        cands.push_back({2, both, 0, ns, dir, ba, 1e30});
+        cands.push_back({2, both, 0, ns, dir, ba, 1e30, 2});
+        // the 80-register form only pays where three CTAs fit in shared memory
+        if (3 * (ba + 1024) <= 233472) cands.push_back({2, both, 0, ns, dir, ba, 1e30, 3});
       }
   }
-  const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both, ag0 = sp.ana_grid, dir0 = sp.direct;
+  const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both, ag0 = sp.ana_grid, dir0 = sp.direct,
+            mb0 = sp.ana_minb;
   const size_t sms0 = sp.smem_syn, sma0 = sp.smem_ana;
   auto apply = [&](const Cand &c) {
     sp.jb = jb0;
@@ -1588,6 +1595,7 @@ void SphereEngine::autotune_split() {
     sp.ana_both = ab0;
     sp.ana_grid = ag0;
     sp.direct = dir0;
+    sp.ana_minb = mb0;
     if (c.which == 1) {
       sp.jb = c.jb;
       sp.fgrp = c.fg;
@@ -1601,6 +1609,7 @@ void SphereEngine::autotune_split() {
       sp.ana_both = c.jb;  // the analysis candidates carry the variant in jb and the CTA count in fg
       sp.ana_grid = c.fg;
       sp.direct = c.dir;
+      sp.ana_minb = c.mb;
     }
   };
   // two rounds in opposite orders; each candidate keeps its faster round
@@ -1636,6 +1645,7 @@ void SphereEngine::autotune_split() {
   sp.smem_ana = ba ? ba->bytes : sma0;
   sp.ana_both = ba ? ba->jb : ab0;
   sp.ana_grid = ba ? ba->fg : ag0;
+  sp.ana_minb = ba ? ba->mb : mb0;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   check_split_status();
@@ -1650,12 +1660,13 @@ void SphereEngine::split_plan(int *out) const {
   out[4] = split ? split->ana_both : 0;
   out[5] = split ? split->ana_grid : 0;
   out[6] = split ? split->direct : 0;
+  out[7] = split ? split->ana_minb : 0;
 }
 
 void SphereEngine::set_split_plan(const int *in) {
   if (!split) throw InvalidArgument("the engine is not in split precision");
   SplitPlan &sp = *split;
-  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6];
+  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6], mb = in[7];
   int dev = 0, optin = 0;
   LMW_CUDA(cudaGetDevice(&dev));
   LMW_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -1670,6 +1681,7 @@ void SphereEngine::set_split_plan(const int *in) {
   const size_t bs = std::max(nss * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
   const size_t ba = std::max(sp.ana_res_bytes_v[dir] + nsa * sp.ana_stage_bytes_v[dir] + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
   if (bs > sp.budget_bytes || ba > sp.budget_bytes) throw InvalidArgument("split plan: the pipelines do not fit in shared memory");
+  if (mb != 2 && mb != 3) throw InvalidArgument("split plan: the analysis register budget must be 2 or 3 CTAs per SM");
   LMW_CUDA(cudaStreamSynchronize(stream));
   sp.jb = jb;
   sp.fgrp = fg;
@@ -1680,6 +1692,7 @@ void SphereEngine::set_split_plan(const int *in) {
   sp.ana_both = both;
   sp.ana_grid = grid;
   sp.direct = dir;
+  sp.ana_minb = mb;
   graphs_clear();
 }
 
