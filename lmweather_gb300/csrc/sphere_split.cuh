@@ -45,6 +45,7 @@ constexpr size_t SPLIT_HALF_SM = 115456;
 struct SplitPlan {
   int pieces = 2, terms = 3;
   int nbt = 1, ntiles = 1, nh16 = 16, nh64 = 64, rAP = 8, rAH = 8, rSP = 8, rSH = 8, ra_max = 16;
+  int bka = 64, nha = 64;  // analysis K (latitude) chunk width (64, or the padded latitude count below 64) and padded K
   std::vector<int> ke16, kp64, ra16;
   std::vector<long> tS_off, tA_off, aS_off, aSH_off;
   long tS_size = 0, tA_size = 0, aSP_size = 0, aSH_size = 0, aAP_size = 0, aAH_size = 0;
@@ -69,7 +70,7 @@ struct SplitPlan {
 };
 
 struct SplitDev {
-  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb, fgrp, ana_cols_one, ana_cols_both, syn_nh;
+  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb, fgrp, ana_cols_one, ana_cols_both, syn_nh, bka, nha;
   const int *ke16, *kp64, *ra16;
   const long *tS_off, *tA_off, *aS_off, *aSH_off;
   long tS_size, tA_size, aSP_size, aSH_size, aAP_size, aAH_size;
@@ -85,9 +86,10 @@ namespace {
 __host__ __device__ inline int pad16(int x) { return (x + 15) & ~15; }
 __host__ __device__ inline int pad8(int x) { return (x + 7) & ~7; }
 __host__ __device__ inline int pad64(int x) { return (x + 63) & ~63; }
-// canonical chunked core-matrix order of an R-row operand
-__host__ __device__ inline long tile_off(int r, int k, int R) {
-  return static_cast<long>(k >> 6) * R * 64 + (((r >> 3) << 3) + ((k & 63) >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+// canonical chunked core-matrix order of an R-row operand: K chunks of BK columns (64, or the analysis's
+// latitude chunk width when the grid has fewer latitude pairs), each [8-row group][8-column group][8 x 8]
+__host__ __device__ inline long tile_off(int r, int k, int R, int BK = 64) {
+  return static_cast<long>(k / BK) * R * BK + ((r >> 3) * (BK >> 3) + ((k % BK) >> 3)) * 64 + (r & 7) * 8 + (k & 7);
 }
 
 // round-to-nearest-even float -> bf16 on the host
@@ -136,19 +138,20 @@ __device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) { tc::
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) { tc::ld8(taddr, v); }
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) { tc::ld32(taddr, v); }
 
-// One CTA's two GEMMs (H then P). Operand g = 0 (H) / 1 (P): nchunk[g] K chunks of 64. A is either streamed
-// with B (a[g] != nullptr: chunk c of aR[g] rows at a[g] + c * aR[g] * 64, pieces a_ps[g] apart) or resident in
-// shared memory (a_res[g]: chunk c, piece p at a_res[g] + (p * nchunk[g] + c) * aR[g] * 128 bytes). B chunk c of
-// bR rows at b[g] + c * bR * 64. Accumulators at TMEM columns acc[g][seg], the second segment starting at K =
+// One CTA's two GEMMs (H then P). Operand g = 0 (H) / 1 (P): nchunk[g] K chunks of bk columns. A is either streamed
+// with B (a[g] != nullptr: chunk c of aR[g] rows at a[g] + c * aR[g] * bk, pieces a_ps[g] apart) or resident in
+// shared memory (a_res[g]: chunk c, piece p at a_res[g] + (p * nchunk[g] + c) * aR[g] * bk * 2 bytes). B chunk c of
+// bR rows at b[g] + c * b_cs. Accumulators at TMEM columns acc[g][seg], the second segment starting at K =
 // kseg[g]. Only the first aR[g] accumulator rows are meaningful: an M = 128 MMA also reads whatever lies in the
 // 16 KB after an A base, and the rows it makes from that are never read. Returns false when a bounded wait ran
 // out (the error code is already recorded).
 struct TwoGemm {
   const __nv_bfloat16 *a[2], *b[2];
   long a_ps[2], b_ps[2];
-  long b_cs;  // elements between consecutive K chunks of B (bR * 64 unless B is a row slice of a wider table)
+  long b_cs;  // elements between consecutive K chunks of B (bR * bk unless B is a row slice of a wider table)
   uint32_t a_res[2];
   int aR[2], aRmax, bR, nchunk[2], kseg[2];
+  int bk = SPLIT_BK;  // K columns per chunk (16, 32 or 64)
   uint32_t acc[2][2];
 };
 
@@ -158,8 +161,10 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
                              int *err, int it0 = 0, uint32_t done_phase = 0) {
   const int tid = threadIdx.x;
   const bool astream = G.a[0] != nullptr;
-  const int a_bytes = astream ? G.aRmax * SPLIT_BK * 2 : 0;
-  const int b_bytes = G.bR * SPLIT_BK * 2;
+  const int bk = G.bk;
+  const uint32_t sbo = static_cast<uint32_t>(bk) * 16u;  // bytes between 8-row groups of a chunk
+  const int a_bytes = astream ? G.aRmax * bk * 2 : 0;
+  const int b_bytes = G.bR * bk * 2;
   const int stage_bytes = pieces * (a_bytes + b_bytes);
   const int total = G.nchunk[0] + G.nchunk[1];
   __shared__ int s_fail;
@@ -175,12 +180,12 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
         atomicExch(err, 2);
         break;
       }
-      const uint32_t abytes = astream ? static_cast<uint32_t>(G.aR[g]) * 128u : 0u, bbytes = static_cast<uint32_t>(G.bR) * 128u;
+      const uint32_t abytes = astream ? static_cast<uint32_t>(G.aR[g] * bk * 2) : 0u, bbytes = static_cast<uint32_t>(G.bR * bk * 2);
       mbar_expect(su32(&full[st]), static_cast<uint32_t>(pieces) * (abytes + bbytes));
       uint8_t *base = pipe + st * stage_bytes;
       for (int p = 0; p < pieces; p++) {
         if (astream)
-          bulk_g2s(su32(base + p * a_bytes), G.a[g] + p * G.a_ps[g] + static_cast<long>(c) * G.aR[g] * 64, abytes, su32(&full[st]));
+          bulk_g2s(su32(base + p * a_bytes), G.a[g] + p * G.a_ps[g] + static_cast<long>(c) * G.aR[g] * bk, abytes, su32(&full[st]));
         bulk_g2s(su32(base + pieces * a_bytes + p * b_bytes), G.b[g] + p * G.b_ps[g] + static_cast<long>(c) * G.b_cs, bbytes,
                  su32(&full[st]));
       }
@@ -203,15 +208,15 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       uint8_t *base = pipe + st * stage_bytes;
-      for (int kk = 0; kk < SPLIT_BK; kk += 16) {
-        const int kg = c * SPLIT_BK + kk;
+      for (int kk = 0; kk < bk; kk += 16) {
+        const int kg = c * bk + kk;
         const int seg = kg >= G.kseg[g] ? 1 : 0;
         for (int t = t0; t < 6; t++) {
           const int pa = tp[t][0], pb = tp[t][1];
           const uint32_t abase = astream ? su32(base + pa * a_bytes)
-                                         : G.a_res[g] + static_cast<uint32_t>((pa * G.nchunk[g] + c) * G.aR[g] * 128);
-          const uint64_t ad = chunk_desc(abase + (kk / 8) * 128);
-          const uint64_t bd = chunk_desc(su32(base + pieces * a_bytes + pb * b_bytes + (kk / 8) * 128));
+                                         : G.a_res[g] + static_cast<uint32_t>((pa * G.nchunk[g] + c) * G.aR[g] * bk * 2);
+          const uint64_t ad = chunk_desc(abase + (kk / 8) * 128, sbo);
+          const uint64_t bd = chunk_desc(su32(base + pieces * a_bytes + pb * b_bytes + (kk / 8) * 128), sbo);
           const uint32_t accum = started[g][seg] ? 1u : 0u;
           asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
                            G.acc[g][seg]),
@@ -470,7 +475,7 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
           const int R = isH ? sd.rAH : sd.rAP;
           const int q = isH ? (r == 3 ? 2 : r) : (r == 4 ? 3 : r);
           const int row0 = isH ? ml * 6 + 2 * q : ml * 8 + 2 * q;
-          __nv_bfloat16 *opnd = (isH ? sd.aA_H : sd.aA_P) + ((static_cast<long>(m) * 2 + s_op) * sd.ntiles + tile) * R * sd.nh64;
+          __nv_bfloat16 *opnd = (isH ? sd.aA_H : sd.aA_P) + ((static_cast<long>(m) * 2 + s_op) * sd.ntiles + tile) * R * sd.nha;
           const long pstride = isH ? sd.aAH_size : sd.aAP_size;
 #pragma unroll
           for (int ri = 0; ri < 2; ri++) {
@@ -485,7 +490,7 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
               pc[1][pr] = l;
               pc[2][pr] = __float2bfloat16_rn(r1 - __bfloat162float(l));
             }
-            __nv_bfloat16 *dst = opnd + tile_off(row0 + ri, jh0, R);
+            __nv_bfloat16 *dst = opnd + tile_off(row0 + ri, jh0, R, sd.bka);
 #pragma unroll
             for (int pi = 0; pi < 3; pi++) {
               if (pi >= sd.pieces) break;
@@ -569,8 +574,8 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
   while (ncols < static_cast<uint32_t>(BOTH ? sd.ana_cols_both : sd.ana_cols_one)) ncols <<= 1;
   // DIRECT: A operands streamed with the tables; otherwise gathered from the FP32 fold into resident shared memory
   // (H rows then P rows, every chunk and piece, in the chunk layout) ahead of the pipeline buffers
-  const int nchunk = sd.nh64 / SPLIT_BK;
-  const int aH_bytes = DIRECT ? 0 : sd.pieces * nchunk * sd.rAH * 128, aP_bytes = DIRECT ? 0 : sd.pieces * nchunk * sd.rAP * 128;
+  const int nchunk = sd.nha / sd.bka;
+  const int aH_bytes = DIRECT ? 0 : sd.pieces * nchunk * sd.rAH * sd.bka * 2, aP_bytes = DIRECT ? 0 : sd.pieces * nchunk * sd.rAP * sd.bka * 2;
   uint8_t *aH = smem, *aP = smem + aH_bytes, *pipe = smem + aH_bytes + aP_bytes;
   bool ok = true, setup_done = false;
   int pipe_it = 0, calls = 0;
@@ -608,10 +613,10 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
     // parity s and H quantities a, b, v at parity 1 - s. One work item = (member, quantity, 8 latitudes): eight
     // consecutive float2 loads, then one 16-byte store per (real/imaginary row, piece) into the chunk layout.
     const int ph = 1 - s;
-    const long pstrideP = static_cast<long>(nchunk) * sd.rAP * 64, pstrideH = static_cast<long>(nchunk) * sd.rAH * 64;
+    const long pstrideP = static_cast<long>(nchunk) * sd.rAP * sd.bka, pstrideH = static_cast<long>(nchunk) * sd.rAH * sd.bka;
     const long sstride = static_cast<long>(B) * d.nh;  // between slots/parities of fold[m][slot][parity][member][jh]
     const float2 *gm = sd.fold + static_cast<long>(m) * 10 * sstride + static_cast<long>(tile * sd.nbt) * d.nh;
-    const int nkb = sd.nh64 >> 3;
+    const int nkb = sd.nha >> 3;
     // consecutive threads take different operand rows of the same 8-latitude block: their 16-byte stores land in
     // different rows of the core matrices (different banks)
     for (int e = threadIdx.x; e < mt * 7 * nkb; e += blockDim.x) {
@@ -624,11 +629,10 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
       const float2 *g = gm + static_cast<long>(slot * 2 + par) * sstride + static_cast<long>(ml) * d.nh + j0;
 #pragma unroll
       for (int j = 0; j < 8; j++) v[j] = j0 + j < d.nh ? g[j] : make_float2(0.0f, 0.0f);
-      const int c = j0 >> 6, kin = j0 & 63;
       const bool isP = qi < 4;
       const int R = isP ? sd.rAP : sd.rAH;
       const int row = isP ? ml * 8 + 2 * qi : ml * 6 + 2 * (qi - 4);
-      __nv_bfloat16 *base = reinterpret_cast<__nv_bfloat16 *>(isP ? aP : aH) + static_cast<long>(c) * R * 64;
+      __nv_bfloat16 *base = reinterpret_cast<__nv_bfloat16 *>(isP ? aP : aH);
       const long pstride = isP ? pstrideP : pstrideH;
 #pragma unroll
       for (int ri = 0; ri < 2; ri++) {
@@ -645,7 +649,7 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
           b1[j] = l;
           b2[j] = __float2bfloat16_rn(r1 - __bfloat162float(l));
         }
-        __nv_bfloat16 *dst = base + tile_off(row + ri, kin, R);
+        __nv_bfloat16 *dst = base + tile_off(row + ri, j0, R, sd.bka);
         *reinterpret_cast<uint4 *>(dst) = k0;
         if (sd.pieces > 1) *reinterpret_cast<uint4 *>(dst + pstride) = k1;
         if (sd.pieces > 2) *reinterpret_cast<uint4 *>(dst + 2 * pstride) = k2;
@@ -663,8 +667,8 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
   const int ra16 = s ? ra1 : ra0;
   TwoGemm G;
   if (DIRECT) {
-    G.a[0] = sd.aA_H + ((static_cast<long>(m) * 2 + s) * sd.ntiles + tile) * sd.rAH * sd.nh64;
-    G.a[1] = sd.aA_P + ((static_cast<long>(m) * 2 + s) * sd.ntiles + tile) * sd.rAP * sd.nh64;
+    G.a[0] = sd.aA_H + ((static_cast<long>(m) * 2 + s) * sd.ntiles + tile) * sd.rAH * sd.nha;
+    G.a[1] = sd.aA_P + ((static_cast<long>(m) * 2 + s) * sd.ntiles + tile) * sd.rAP * sd.nha;
     G.a_ps[0] = sd.aAH_size;
     G.a_ps[1] = sd.aAP_size;
     G.a_res[0] = G.a_res[1] = 0;
@@ -681,7 +685,8 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
   G.aR[1] = sd.rAP;
   G.aRmax = sd.rAP;
   G.bR = ra16;
-  G.b_cs = static_cast<long>(ra16) * 64;
+  G.b_cs = static_cast<long>(ra16) * sd.bka;
+  G.bk = sd.bka;
   G.nchunk[0] = G.nchunk[1] = nchunk;
   G.kseg[0] = G.kseg[1] = 1 << 30;
   G.acc[0][0] = G.acc[0][1] = tmem + (s ? cb1 : 0);
@@ -785,6 +790,8 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   sp.ntiles = (B + sp.nbt - 1) / sp.nbt;
   sp.nh16 = pad16(nh);
   sp.nh64 = pad64(nh);
+  sp.bka = nh >= 64 ? 64 : pad16(nh);
+  sp.nha = (nh + sp.bka - 1) / sp.bka * sp.bka;
   sp.syn_split = 4 * sp.nh16 > 512 ? 2 : 1;
   sp.syn_nh = sp.nh16 / sp.syn_split;
   sp.rSP = 8 * sp.nbt;
@@ -814,7 +821,7 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
       const int R = s == 0 ? ke : ko;
       sp.ra16[2 * m + s] = std::max(16, pad16(R));
       sp.tA_off[2 * m + s] = ta;
-      ta += static_cast<long>(sp.ra16[2 * m + s]) * sp.nh64;
+      ta += static_cast<long>(sp.ra16[2 * m + s]) * sp.nha;
       ra_max = std::max(ra_max, sp.ra16[2 * m + s]);
     }
   }
@@ -823,8 +830,8 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   sp.tA_size = ta;
   sp.aSP_size = as;
   sp.aSH_size = ash;
-  sp.aAP_size = static_cast<long>(M) * 2 * sp.ntiles * sp.rAP * sp.nh64;
-  sp.aAH_size = static_cast<long>(M) * 2 * sp.ntiles * sp.rAH * sp.nh64;
+  sp.aAP_size = static_cast<long>(M) * 2 * sp.ntiles * sp.rAP * sp.nha;
+  sp.aAH_size = static_cast<long>(M) * 2 * sp.ntiles * sp.rAH * sp.nha;
   // tables in the chunked core-matrix order, three pieces each
   std::vector<uint16_t> tSP(3 * ts, 0), tSH(3 * ts, 0), tAP(3 * ta, 0), tAH(3 * ta, 0);
   for (int m = 0; m <= N; m++) {
@@ -845,7 +852,7 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
         const int n = m + s + 2 * r;
         const size_t q = static_cast<size_t>(h.tri[m] + n - m);
         for (int jh = 0; jh < nh; jh++) {
-          const long o = sp.tA_off[2 * m + s] + tile_off(r, jh, sp.ra16[2 * m + s]);
+          const long o = sp.tA_off[2 * m + s] + tile_off(r, jh, sp.ra16[2 * m + s], sp.bka);
           split3(h.P[q * nh + jh], &tAP[o], ta);
           split3(h.H[q * nh + jh], &tAH[o], ta);
         }
@@ -907,11 +914,11 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
     }
   // the analysis either gathers its A operands into resident shared memory (variant 0) or streams them with
   // its tables (variant 1, the default for batches)
-  const size_t nchunk = sp.nh64 / SPLIT_BK;
-  sp.ana_res_bytes_v[0] = static_cast<size_t>(pieces) * nchunk * (sp.rAH + sp.rAP) * 128;
-  sp.ana_stage_bytes_v[0] = static_cast<size_t>(pieces) * ra_max * SPLIT_BK * 2;
+  const size_t nchunk = sp.nha / sp.bka;
+  sp.ana_res_bytes_v[0] = static_cast<size_t>(pieces) * nchunk * (sp.rAH + sp.rAP) * sp.bka * 2;
+  sp.ana_stage_bytes_v[0] = static_cast<size_t>(pieces) * ra_max * sp.bka * 2;
   sp.ana_res_bytes_v[1] = 0;
-  sp.ana_stage_bytes_v[1] = static_cast<size_t>(pieces) * (sp.rAP + ra_max) * SPLIT_BK * 2;
+  sp.ana_stage_bytes_v[1] = static_cast<size_t>(pieces) * (sp.rAP + ra_max) * sp.bka * 2;
   sp.direct = sp.nbt >= 8 ? 1 : 0;
   const size_t ana_res = sp.ana_res_bytes_v[sp.direct], ana_stage = sp.ana_stage_bytes_v[sp.direct];
   // two analysis CTAs per SM when a 3-stage pipeline fits in half of the shared memory
@@ -938,6 +945,8 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.ntiles = sp.ntiles;
   s.nh16 = sp.nh16;
   s.nh64 = sp.nh64;
+  s.bka = sp.bka;
+  s.nha = sp.nha;
   s.rAP = sp.rAP;
   s.rAH = sp.rAH;
   s.rSP = sp.rSP;

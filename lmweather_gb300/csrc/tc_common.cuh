@@ -50,12 +50,12 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
                : "memory");
 }
 
-// shared-memory matrix descriptor of the chunk layout: K-direction core matrices 128 B apart, 8-row groups
-// 1024 B apart, no swizzle, descriptor version 1
-__device__ __forceinline__ uint64_t chunk_desc(uint32_t saddr) {
+// shared-memory matrix descriptor of the chunk layout: K-direction core matrices 128 B apart, 8-row groups `sbo`
+// bytes apart (1024 for chunks of 64 K columns, 16 x the chunk width in general), no swizzle, descriptor version 1
+__device__ __forceinline__ uint64_t chunk_desc(uint32_t saddr, uint32_t sbo = 1024u) {
   uint64_t d = static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
   d |= static_cast<uint64_t>(128u >> 4) << 16;
-  d |= static_cast<uint64_t>(1024u >> 4) << 32;
+  d |= static_cast<uint64_t>(sbo >> 4) << 32;
   d |= static_cast<uint64_t>(1) << 46;
   return d;
 }
