@@ -46,14 +46,15 @@ struct SplitPlan {
   int pieces = 2, terms = 3;
   int nbt = 1, ntiles = 1, nh16 = 16, nh64 = 64, rAP = 8, rAH = 8, rSP = 8, rSH = 8, ra_max = 16;
   int bka = 64, nha = 64;  // analysis K (latitude) chunk width (64, or the padded latitude count below 64) and padded K
-  std::vector<int> ke16, kp64, ra16;
+  int bks = 64;            // synthesis K (coefficient) chunk width: 32 up to T85 (less padding per m), 64 above
+  std::vector<int> ke16, kps, ra16;  // kps[m]: synthesis K of m padded to the chunk width bks
   std::vector<long> tS_off, tA_off, aS_off, aSH_off;
   long tS_size = 0, tA_size = 0, aSP_size = 0, aSH_size = 0, aAP_size = 0, aAH_size = 0;
   DevBuf<__nv_bfloat16> tS_P, tS_H, tA_P, tA_H;   // tables (B operands), three pieces each
   DevBuf<__nv_bfloat16> aS_P, aS_H, aA_P, aA_H;   // per-stage operands (A)
   DevBuf<float> dsyn;                             // [member][jh][m][SPLIT_NQ]
   DevBuf<int> err;
-  DevBuf<int> ke16_d, kp64_d, ra16_d;
+  DevBuf<int> ke16_d, kps_d, ra16_d;
   DevBuf<long> tS_off_d, tA_off_d, aS_off_d, aSH_off_d;
   size_t smem_syn = 0, smem_ana = 0;
   int ns_syn = 2, ns_ana = 2;  // pipeline stages
@@ -70,8 +71,8 @@ struct SplitPlan {
 };
 
 struct SplitDev {
-  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb, fgrp, ana_cols_one, ana_cols_both, syn_nh, bka, nha;
-  const int *ke16, *kp64, *ra16;
+  int pieces, terms, nbt, ntiles, nh16, nh64, rAP, rAH, rSP, rSH, jb, fgrp, ana_cols_one, ana_cols_both, syn_nh, bka, nha, bks;
+  const int *ke16, *kps, *ra16;
   const long *tS_off, *tA_off, *aS_off, *aSH_off;
   long tS_size, tA_size, aSP_size, aSH_size, aAP_size, aAH_size;
   const __nv_bfloat16 *tS_P, *tS_H, *tA_P, *tA_H;
@@ -280,22 +281,24 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
   split_setup(&tslot, ncols, full, empty, &done, ns);
   const uint32_t tmem = tslot;
   TwoGemm G;
-  const long kp = sd.kp64[m];
+  const long kp = sd.kps[m];
   const long aoffP = sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kp, aoffH = sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kp;
   G.a[0] = sd.aS_H + aoffH;
   G.a[1] = sd.aS_P + aoffP;
   G.a_ps[0] = sd.aSH_size;
   G.a_ps[1] = sd.aSP_size;
   G.a_res[0] = G.a_res[1] = 0;
-  G.b[0] = sd.tS_H + sd.tS_off[m] + static_cast<long>(jh0) * 64;  // rows jh0.. of every chunk (8-row groups are 512 elements)
-  G.b[1] = sd.tS_P + sd.tS_off[m] + static_cast<long>(jh0) * 64;
+  // rows jh0.. of every chunk (8-row groups are 8 x bks elements)
+  G.b[0] = sd.tS_H + sd.tS_off[m] + static_cast<long>(jh0) * sd.bks;
+  G.b[1] = sd.tS_P + sd.tS_off[m] + static_cast<long>(jh0) * sd.bks;
   G.b_ps[0] = G.b_ps[1] = sd.tS_size;
-  G.b_cs = static_cast<long>(sd.nh16) * 64;
+  G.b_cs = static_cast<long>(sd.nh16) * sd.bks;
+  G.bk = sd.bks;
   G.aR[0] = sd.rSH;
   G.aR[1] = sd.rSP;
   G.aRmax = sd.rSP;
   G.bR = nh16;
-  G.nchunk[0] = G.nchunk[1] = static_cast<int>(kp / SPLIT_BK);
+  G.nchunk[0] = G.nchunk[1] = static_cast<int>(kp / sd.bks);
   G.kseg[0] = G.kseg[1] = sd.ke16[m];
   G.acc[0][0] = tmem;
   G.acc[0][1] = tmem + nh16;
@@ -533,16 +536,16 @@ __device__ __forceinline__ void pack_syn_coef(const SphDev &d, const SplitDev &s
   const int tile = b / sd.nbt, ml = b - tile * sd.nbt;
   const int ke16 = sd.ke16[m];
   const int k = ((n - m) & 1) ? ke16 + ((n - m - 1) >> 1) : ((n - m) >> 1);
-  const long kp = sd.kp64[m];
+  const long kp = sd.kps[m];
   const long baseP = sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kp;
   const long baseH = sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kp;
   const double kf = kfac[n];
   const float v[8] = {d2f_int(z.x * kf), d2f_int(z.y * kf), d2f_int(dl.x * kf), d2f_int(dl.y * kf),
                       d2f_int(z.x),      d2f_int(z.y),      d2f_int(f.x),       d2f_int(f.y)};
 #pragma unroll
-  for (int q = 0; q < 8; q++) fsplit(v[q], sd.aS_P + baseP + tile_off(ml * 8 + q, k, sd.rSP), sd.aSP_size, sd.pieces);
+  for (int q = 0; q < 8; q++) fsplit(v[q], sd.aS_P + baseP + tile_off(ml * 8 + q, k, sd.rSP, sd.bks), sd.aSP_size, sd.pieces);
 #pragma unroll
-  for (int q = 0; q < 4; q++) fsplit(v[q], sd.aS_H + baseH + tile_off(ml * 4 + q, k, sd.rSH), sd.aSH_size, sd.pieces);
+  for (int q = 0; q < 4; q++) fsplit(v[q], sd.aS_H + baseH + tile_off(ml * 4 + q, k, sd.rSH, sd.bks), sd.aSH_size, sd.pieces);
 }
 
 // synthesis operands from a whole state (after the state was set from outside the stepping). grid: (ceil(ntri/128), B)
@@ -791,6 +794,7 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   sp.nh16 = pad16(nh);
   sp.nh64 = pad64(nh);
   sp.bka = nh >= 64 ? 64 : pad16(nh);
+  sp.bks = N <= 85 ? 32 : 64;
   sp.nha = (nh + sp.bka - 1) / sp.bka * sp.bka;
   sp.syn_split = 4 * sp.nh16 > 512 ? 2 : 1;
   sp.syn_nh = sp.nh16 / sp.syn_split;
@@ -799,7 +803,7 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   sp.rAP = 8 * sp.nbt;
   sp.rAH = pad8(6 * sp.nbt);
   sp.ke16.assign(M, 0);
-  sp.kp64.assign(M, 0);
+  sp.kps.assign(M, 0);
   sp.ra16.assign(2 * M, 0);
   sp.tS_off.assign(M, 0);
   sp.tA_off.assign(2 * M, 0);
@@ -810,13 +814,13 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   for (int m = 0; m <= N; m++) {
     const int ke = (N - m) / 2 + 1, ko = (N - m + 1) / 2;
     sp.ke16[m] = pad16(ke);
-    sp.kp64[m] = pad64(sp.ke16[m] + ko);
+    sp.kps[m] = (sp.ke16[m] + ko + sp.bks - 1) / sp.bks * sp.bks;
     sp.tS_off[m] = ts;
-    ts += static_cast<long>(sp.nh16) * sp.kp64[m];
+    ts += static_cast<long>(sp.nh16) * sp.kps[m];
     sp.aS_off[m] = as;
-    as += static_cast<long>(sp.ntiles) * sp.rSP * sp.kp64[m];
+    as += static_cast<long>(sp.ntiles) * sp.rSP * sp.kps[m];
     sp.aSH_off[m] = ash;
-    ash += static_cast<long>(sp.ntiles) * sp.rSH * sp.kp64[m];
+    ash += static_cast<long>(sp.ntiles) * sp.rSH * sp.kps[m];
     for (int s = 0; s < 2; s++) {
       const int R = s == 0 ? ke : ko;
       sp.ra16[2 * m + s] = std::max(16, pad16(R));
@@ -835,13 +839,13 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   // tables in the chunked core-matrix order, three pieces each
   std::vector<uint16_t> tSP(3 * ts, 0), tSH(3 * ts, 0), tAP(3 * ta, 0), tAH(3 * ta, 0);
   for (int m = 0; m <= N; m++) {
-    const int ke16 = sp.ke16[m], kpm = sp.kp64[m];
+    const int ke16 = sp.ke16[m], kpm = sp.kps[m];
     for (int k = 0; k < kpm; k++) {
       const int n = k < ke16 ? m + 2 * k : m + 1 + 2 * (k - ke16);
       if (n > N || (k < ke16 && ((n - m) & 1))) continue;
       const size_t q = static_cast<size_t>(h.tri[m] + n - m);
       for (int jh = 0; jh < nh; jh++) {
-        const long o = sp.tS_off[m] + tile_off(jh, k, sp.nh16);
+        const long o = sp.tS_off[m] + tile_off(jh, k, sp.nh16, sp.bks);
         split3(h.P[q * nh + jh], &tSP[o], ts);
         split3(h.H[q * nh + jh], &tSH[o], ts);
       }
@@ -886,7 +890,7 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
     LMW_CUDA(cudaMemcpy(dst.p, src.data(), src.size() * sizeof(long), cudaMemcpyHostToDevice));
   };
   upi(sp.ke16_d, sp.ke16);
-  upi(sp.kp64_d, sp.kp64);
+  upi(sp.kps_d, sp.kps);
   upi(sp.ra16_d, sp.ra16);
   upl(sp.tS_off_d, sp.tS_off);
   upl(sp.tA_off_d, sp.tA_off);
@@ -894,11 +898,11 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   upl(sp.aSH_off_d, sp.aSH_off);
   const int pieces = sp.pieces;
   const size_t budget = 220 * 1024;
-  const size_t syn_stage = static_cast<size_t>(pieces) * (sp.rSP + sp.syn_nh) * SPLIT_BK * 2;
-  // the pipeline never needs more stages than a CTA has chunks (two GEMMs of kp64 / 64 chunks); two CTAs per SM
+  const size_t syn_stage = static_cast<size_t>(pieces) * (sp.rSP + sp.syn_nh) * sp.bks * 2;
+  // the pipeline never needs more stages than a CTA has chunks (two GEMMs of kps / bks chunks); two CTAs per SM
   // when two stages fit in half of the shared memory
   int max_chunks = 0;
-  for (int m = 0; m <= N; m++) max_chunks = std::max(max_chunks, 2 * static_cast<int>(sp.kp64[m] / SPLIT_BK));
+  for (int m = 0; m <= N; m++) max_chunks = std::max(max_chunks, 2 * static_cast<int>(sp.kps[m] / sp.bks));
   const size_t half_budget = SPLIT_HALF_SM;
   if (2 * syn_stage + SPLIT_MARGIN <= half_budget) sp.ns_syn = static_cast<int>(std::min<size_t>(std::min(SPLIT_MAX_STAGES, max_chunks), (half_budget - SPLIT_MARGIN) / syn_stage));
   else sp.ns_syn = static_cast<int>(std::min<size_t>(std::min(SPLIT_MAX_STAGES, max_chunks), (budget - SPLIT_MARGIN) / syn_stage));
@@ -946,6 +950,7 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.nh16 = sp.nh16;
   s.nh64 = sp.nh64;
   s.bka = sp.bka;
+  s.bks = sp.bks;
   s.nha = sp.nha;
   s.rAP = sp.rAP;
   s.rAH = sp.rAH;
@@ -957,7 +962,7 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.ana_cols_one = 2 * sp.ra_max;
   s.ana_cols_both = 2 * sp.ra_pair;
   s.ke16 = sp.ke16_d.p;
-  s.kp64 = sp.kp64_d.p;
+  s.kps = sp.kps_d.p;
   s.ra16 = sp.ra16_d.p;
   s.tS_off = sp.tS_off_d.p;
   s.tA_off = sp.tA_off_d.p;
