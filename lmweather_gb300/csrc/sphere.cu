@@ -1516,7 +1516,7 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
   split_packed = false;
 }
 
-// Measured choice of the split path's launch plan: latitude pairs per grid CTA (8, 4, 2, 1), FFT stages fused per
+// Measured choice of the split path's launch plan (each candidate timed after its producer kernel): latitude pairs per grid CTA (8, 4, 2, 1), FFT stages fused per
 // shared-memory pass (4, 3 or 2), and the pipeline depth of the synthesis and analysis kernels (1-4 stages where
 // they fit) and the analysis variant (one parity or both per CTA). Each kernel is timed alone for every candidate (CUDA events on the engine stream, stage 1 on the
 // present state, which leaves the state unchanged); the arithmetic does not depend on the choice.
@@ -1535,16 +1535,25 @@ void SphereEngine::autotune_split() {
                 which);
     g_launches += 1;
   };
+  // a candidate is timed right after the kernel that produces its input (the analysis after the grid kernel, the
+  // grid kernel after the synthesis, the synthesis after the analysis), so the caches hold what they hold in a run
   auto timed = [&](int which) {
+    const int prev = (which + 2) % 3;
+    launch(prev);
     launch(which);
-    LMW_CUDA(cudaEventRecord(e0, stream));
-    for (int r = 0; r < 5; r++) launch(which);
-    LMW_CUDA(cudaEventRecord(e1, stream));
-    LMW_LAUNCH_CHECK();
-    LMW_CUDA(cudaEventSynchronize(e1));
-    float ms = 0;
-    LMW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    return static_cast<double>(ms);
+    double total = 0;
+    for (int r = 0; r < 5; r++) {
+      launch(prev);
+      LMW_CUDA(cudaEventRecord(e0, stream));
+      launch(which);
+      LMW_CUDA(cudaEventRecord(e1, stream));
+      LMW_LAUNCH_CHECK();
+      LMW_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      LMW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      total += ms;
+    }
+    return total;
   };
   ensure_packed();
   // warm the device (clocks) on the default plan before any measurement

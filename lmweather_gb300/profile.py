@@ -4,8 +4,8 @@
     ncu --metrics gpu__time_duration.sum --clock-control none --csv python -m lmweather_gb300.profile --case t42 --steps 4
 
 Cases: t42 (config-0 sphere), t85, t170 (dt 240 s), t341 (dt 150 s), plane (1024 x 512 beta-plane jet, dt 60 s),
-ens (an ensemble of --members spheres at --truncation, the groups of the benchmark ensemble). One untimed warm-up
-step runs first.
+ens (an ensemble of --members spheres at --truncation, the groups of the benchmark ensemble; --plan forces split
+plan entries so a capture can use the plan a benchmark run chose). One untimed warm-up step runs first.
 """
 from __future__ import annotations
 
@@ -24,6 +24,7 @@ def main() -> int:
     ap.add_argument("--split-terms", type=int, default=3)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--precision", type=int, default=0)
+    ap.add_argument("--plan", default="", help="split plan entries to force, e.g. analysis_stages=1,analysis_ctas_per_sm=3")
     args = ap.parse_args()
     import lmweather_gb300 as lw
     from lmweather_gb300 import build
@@ -60,6 +61,10 @@ def main() -> int:
         s = lw.Sphere(T, diffusion=nu, precision=args.precision, members=B, split_terms=args.split_terms)
         for b in range(B):
             s.turbulence(b + 1, 5000.0 + 5000.0 * b / B, 30.0, T // 2, member=b)
+        if args.plan:
+            s.set_split_plan(**{k: int(v) for k, v in (kv.split("=") for kv in args.plan.split(","))})
+        if args.precision == lw.SPLIT_BF16:
+            print("plan", s.split_plan())
         dt = 0.9 * min(s.stable_dt(1.5, member=b) for b in range(B))
         s.step(dt)
         t0 = time.perf_counter()
