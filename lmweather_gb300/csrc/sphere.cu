@@ -152,10 +152,11 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, SphTab<R> t, 
 // combine (indices i0 + j 2^st), applies the F stages' butterflies in registers and stores them back, so each
 // group costs one pass through shared memory and one barrier instead of F. The butterflies, their order and
 // the twiddle factors are those of the plain radix-2 transform, so the results are bit for bit the same.
-// Rows may be padded (PAD): element i of a row sits at i + i / 8 and rows are n + n / 8 long, which spreads the
-// strided accesses of the first stage groups over the shared-memory banks.
-template <bool PAD> __device__ __forceinline__ int fft_at(int i) { return PAD ? i + (i >> 3) : i; }
-template <bool PAD> __host__ __device__ __forceinline__ int fft_row(int n) { return PAD ? n + (n >> 3) : n; }
+// Rows may be padded (PAD = p > 0): element i of a row sits at i + i / 2^p and rows are n + n / 2^p long, which spreads
+// the strided accesses of the first stage groups over the shared-memory banks (p = 3 for groups of up to eight
+// elements, p = 4 for the sixteen-element groups).
+template <int PAD> __device__ __forceinline__ int fft_at(int i) { return PAD ? i + (i >> PAD) : i; }
+template <int PAD> __host__ __device__ __forceinline__ int fft_row(int n) { return PAD ? n + (n >> PAD) : n; }
 
 // FP32 twiddle tables hold tw[k + n/4] = -i tw[k] exactly (built that way), so FP32 groups derive the upper half
 // of each stage's twiddles from the lower half; FP64 tables are the reference's cos/sin values and are all loaded.
@@ -168,7 +169,7 @@ __device__ __forceinline__ float2 cmul_tw(float2 w, float2 x) {
 }
 __device__ __forceinline__ double2 cmul_tw(double2 w, double2 x) { return cmul(w, x); }
 
-template <class C2, int F, bool PAD>
+template <class C2, int F, int PAD>
 __device__ __forceinline__ void dit_group(C2 *s, int rows, int n, int logn, int st, const C2 *__restrict__ tw) {
   constexpr int E = 1 << F;
   const int halfn = n >> 1, lo = (1 << st) - 1;
@@ -203,7 +204,7 @@ __device__ __forceinline__ void dit_group(C2 *s, int rows, int n, int logn, int 
     for (int j = 0; j < E; j++) row[fft_at<PAD>(i0 + (j << st))] = x[j];
   }
 }
-template <class C2, int F, bool PAD>
+template <class C2, int F, int PAD>
 __device__ __forceinline__ void dif_group(C2 *s, int rows, int n, int logn, int st, const C2 *__restrict__ tw) {
   constexpr int E = 1 << F;
   const int halfn = n >> 1, lo = (1 << st) - 1;
@@ -239,7 +240,7 @@ __device__ __forceinline__ void dif_group(C2 *s, int rows, int n, int logn, int 
 // inverse transform (decimation in time) of `rows` rows in bit-reversed order, in place
 // fmax: stages per group (1..FMAX); FMAX = 4 (16 elements per thread) raises the register count, so only kernels
 // instantiated for it (with their own occupancy) take four-stage groups
-template <class C2, bool PAD = false, int FMAX = 3>
+template <class C2, int PAD = 0, int FMAX = 3>
 __device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw, int fmax = 3) {
   if (fmax > FMAX) fmax = FMAX;
   for (int st = 0; st < logn;) {
@@ -253,7 +254,7 @@ __device__ void fft_inverse_dit(C2 *s, int rows, int n, int logn, const C2 *__re
   }
 }
 // forward transform (decimation in frequency) of `rows` rows in natural order, output bit-reversed, in place
-template <class C2, bool PAD = false, int FMAX = 3>
+template <class C2, int PAD = 0, int FMAX = 3>
 __device__ void fft_forward_dif(C2 *s, int rows, int n, int logn, const C2 *__restrict__ tw, int fmax = 3) {
   if (fmax > FMAX) fmax = FMAX;
   for (int hi = logn; hi > 0;) {
@@ -272,7 +273,7 @@ __device__ __forceinline__ int bitrev(int k, int logn) { return static_cast<int>
 // Load the Fourier coefficients of `rows` fields at latitudes js (real part) and jn (imaginary part) into
 // bit-reversed rows: Y[m] = X_s[m] + i X_n[m], Y[n-m] = conj(X_s[m]) + i conj(X_n[m]); Im X[0] is dropped
 // as in cpp/sphere.cpp:132.
-template <class C2, bool PAD = false>
+template <class C2, int PAD = 0>
 __device__ void load_pair_spectra(C2 *s, int rows, const SphDev &d, const C2 *__restrict__ fs, const C2 *__restrict__ fn, int fstride) {
   const int n = d.nlon, rl = fft_row<PAD>(n);
   for (int e = threadIdx.x; e < rows * rl; e += blockDim.x) s[e] = mk2(decltype(C2::x)(0), decltype(C2::x)(0));
@@ -303,11 +304,11 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, SphTab<R> t, 
   extern __shared__ __align__(16) unsigned char smraw[];
   C2 *sm = reinterpret_cast<C2 *>(smraw);
   const int b = blockIdx.y, jh = blockIdx.x;
-  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon, rl = fft_row<true>(n);  // padded rows
+  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon, rl = fft_row<3>(n);  // padded rows
   const C2 *f_s = four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M;
   const C2 *f_n = four + (static_cast<size_t>(b) * d.nlat + jn) * 4 * d.M;
-  load_pair_spectra<C2, true>(sm, 4, d, f_s, f_n, d.M);
-  fft_inverse_dit<C2, true>(sm, 4, n, d.logn, t.tw);
+  load_pair_spectra<C2, 3>(sm, 4, d, f_s, f_n, d.M);
+  fft_inverse_dit<C2, 3>(sm, 4, n, d.logn, t.tw);
   // nonlinear products, cpp/sphere.cpp:348-359 (real part: southern latitude, imaginary part: northern)
   const R r2om = t.r2om[js], g = static_cast<R>(d.g);  // 1 / (2 (1 - mu^2)), the same at the mirror latitude
   const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, SphTab<R> t, 
   const double f0s = d.om2[b] * d.mu[js], f0n = d.om2[b] * d.mu[jn];
   C2 *rU = sm, *rV = sm + rl, *rZ = sm + 2 * rl, *rP = sm + 3 * rl, *rE = sm + 4 * rl;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const int kp = fft_at<true>(k);
+    const int kp = fft_at<3>(k);
     const C2 U = rU[kp], V = rV[kp], Z = rZ[kp], P = rP[kp];
     C2 A, Bv, UP, VP, PE;
     {
@@ -332,14 +333,14 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, SphTab<R> t, 
     rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
   __syncthreads();
-  fft_forward_dif<C2, true>(sm, NSLOT, n, d.logn, t.tw);
+  fft_forward_dif<C2, 3>(sm, NSLOT, n, d.logn, t.tw);
   // separate the two latitudes, normalise by nlon (cpp/sphere.cpp:128), weight and fold
   const R inv = R(1) / n, wd = t.wd[js], wj = t.w[js];
   C2 *o = fold + (static_cast<size_t>(b) * d.nh + jh) * NSLOT * 2 * d.M;
   for (int e = threadIdx.x; e < NSLOT * d.M; e += blockDim.x) {
     const int r = e / d.M, m = e - r * d.M;
     const C2 *row = sm + static_cast<size_t>(r) * rl;
-    const C2 Ym = row[fft_at<true>(bitrev(m, d.logn))], Yc = conjd(row[fft_at<true>(bitrev((n - m) & (n - 1), d.logn))]);
+    const C2 Ym = row[fft_at<3>(bitrev(m, d.logn))], Yc = conjd(row[fft_at<3>(bitrev((n - m) & (n - 1), d.logn))]);
     // X_s = (Ym + conj(Y_{n-m}))/2, X_n = -i (Ym - conj(Y_{n-m}))/2
     const R hinv = R(0.5) * inv;
     C2 Xs = cscale(cadd(Ym, Yc), hinv);
@@ -1242,7 +1243,7 @@ template <class R>
 static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage, double dt, const double *filt, const double2 *in,
                           typename V2<R>::type *four, typename V2<R>::type *fold, double2 *x0, double2 *xs, double2 *acc,
                           const double *fgrid, const double *hsgrid, cudaStream_t stream, int which = -1, int zero = 0) {
-  const size_t smem = 5 * static_cast<size_t>(fft_row<true>(d.nlon)) * sizeof(typename V2<R>::type);  // padded FFT rows
+  const size_t smem = 5 * static_cast<size_t>(fft_row<3>(d.nlon)) * sizeof(typename V2<R>::type);  // padded FFT rows
   StageArgs sa;
   sa.stage = stage;
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
@@ -1278,7 +1279,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles, sp.syn_split), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
   if (which < 0 || which == 1) {
     const dim3 grid(d.nh / sp.jb, B);
-    const size_t bytes = 5 * static_cast<size_t>(sp.jb) * fft_row<true>(d.nlon) * sizeof(float2);
+    const size_t bytes = 5 * static_cast<size_t>(sp.jb) * fft_row<3>(d.nlon) * sizeof(float2);
     auto *k = sp.fgrp >= 4 ? (sp.direct ? split_grid<true, 4> : split_grid<false, 4>) : (sp.direct ? split_grid<true, 3> : split_grid<false, 3>);
     k<<<grid, GRID_THREADS, bytes, stream>>>(d, t, sd, fgrid, hsgrid);
   }
@@ -1349,7 +1350,7 @@ void SphereEngine::tracer_stage(int stage, double dt, int part) {
   if (part == 0) {
     trc_synth<<<dim3((nh + 31) / 32, M, B), SYN_THREADS, 0, stream>>>(d, tab64(*tab), in, qin, reinterpret_cast<double2 *>(fourq.p));
   } else if (part == 1) {
-    const size_t smem = 4 * static_cast<size_t>(fft_row<true>(nlon)) * sizeof(double2);
+    const size_t smem = 4 * static_cast<size_t>(fft_row<3>(nlon)) * sizeof(double2);
     trc_grid<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, tab64(*tab), reinterpret_cast<const double2 *>(four.p),
                                                           reinterpret_cast<const double2 *>(fourq.p), reinterpret_cast<double2 *>(foldq.p));
   } else {
@@ -1573,7 +1574,7 @@ void SphereEngine::autotune_split() {
   // analysis operands, which the analysis streams; dir 0: FP32 fold, gathered by the analysis)
   for (int dir = 1; dir >= 0; dir--)
     for (int jb = SPLIT_JB_MAX; jb >= 1; jb /= 2)
-      if (nh % jb == 0 && 5 * static_cast<size_t>(jb) * fft_row<true>(nlon) * sizeof(float2) <= static_cast<size_t>(optin - 2048))
+      if (nh % jb == 0 && 5 * static_cast<size_t>(jb) * fft_row<3>(nlon) * sizeof(float2) <= static_cast<size_t>(optin - 2048))
         for (int fg = 4; fg >= 2; fg--) cands.push_back({1, jb, fg, 0, dir, 0, 1e30});
   // one stage (no double buffering inside a CTA) leaves room for a third CTA per SM, whose copies overlap the others'
   for (int ns = 1; ns <= SPLIT_MAX_STAGES; ns++) {
@@ -1680,7 +1681,7 @@ void SphereEngine::set_split_plan(const int *in) {
   LMW_CUDA(cudaGetDevice(&dev));
   LMW_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   if (!(jb == 1 || jb == 2 || jb == 4 || jb == 8) || jb > SPLIT_JB_MAX || nh % jb != 0 ||
-      5 * static_cast<size_t>(jb) * fft_row<true>(nlon) * sizeof(float2) > static_cast<size_t>(optin - 2048))
+      5 * static_cast<size_t>(jb) * fft_row<3>(nlon) * sizeof(float2) > static_cast<size_t>(optin - 2048))
     throw InvalidArgument("split plan: latitude pairs per grid CTA must be 1, 2, 4 or 8, divide the latitude pairs and fit in shared memory");
   if (fg < 2 || fg > 4) throw InvalidArgument("split plan: FFT stages per pass must be 2, 3 or 4");
   if (nss < 1 || nss > SPLIT_MAX_STAGES || nsa < 1 || nsa > SPLIT_MAX_STAGES)

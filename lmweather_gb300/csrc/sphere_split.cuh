@@ -370,7 +370,8 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
   const int JB = sd.jb;
   const int b = blockIdx.y, jh0 = blockIdx.x * JB;
   const int tile = b / sd.nbt, ml = b - tile * sd.nbt;
-  const int n = d.nlon, M = d.M, rl = fft_row<true>(n);  // padded rows: element i at fft_at<true>(i)
+  constexpr int PSG = FMAX >= 4 ? 4 : 3;  // row padding: one element per 16 for sixteen-element FFT groups, else per 8
+  const int n = d.nlon, M = d.M, rl = fft_row<PSG>(n);  // padded rows: element i at fft_at<PSG>(i)
   // the untilted Coriolis parameter 2 Omega mu of the CTA's latitudes (south, north), rounded to FP32 once
   __shared__ float cor[2 * SPLIT_JB_MAX];
   if (threadIdx.x < 2 * JB) {
@@ -391,13 +392,13 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
       float2 *row = sm + static_cast<size_t>(f * JB + pr) * rl;
       if (m == 0) row[0] = make_float2(a.x, c.x);
       else {
-        row[fft_at<true>(bitrev(m, d.logn))] = make_float2(a.x - c.y, a.y + c.x);
-        row[fft_at<true>(bitrev(n - m, d.logn))] = make_float2(a.x + c.y, c.x - a.y);
+        row[fft_at<PSG>(bitrev(m, d.logn))] = make_float2(a.x - c.y, a.y + c.x);
+        row[fft_at<PSG>(bitrev(n - m, d.logn))] = make_float2(a.x + c.y, c.x - a.y);
       }
     }
   }
   __syncthreads();
-  fft_inverse_dit<float2, true, FMAX>(sm, 4 * JB, n, d.logn, t.tw, sd.fgrp);
+  fft_inverse_dit<float2, PSG, FMAX>(sm, 4 * JB, n, d.logn, t.tw, sd.fgrp);
   const float g = static_cast<float>(d.g);
   for (int e = threadIdx.x; e < JB * n; e += blockDim.x) {
     const int pr = e >> d.logn, k = e & (n - 1);
@@ -409,7 +410,7 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
     float2 *rU = sm + static_cast<size_t>(0 * JB + pr) * rl, *rV = sm + static_cast<size_t>(1 * JB + pr) * rl;
     float2 *rZ = sm + static_cast<size_t>(2 * JB + pr) * rl, *rP = sm + static_cast<size_t>(3 * JB + pr) * rl;
     float2 *rE = sm + static_cast<size_t>(4 * JB + pr) * rl;
-    const int kp = fft_at<true>(k);
+    const int kp = fft_at<PSG>(k);
     const float2 U = rU[kp], V = rV[kp], Z = rZ[kp], P = rP[kp];
     float2 A, Bv, UP, VP, PE;
     {
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
     rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
   __syncthreads();
-  fft_forward_dif<float2, true, FMAX>(sm, 5 * JB, n, d.logn, t.tw, sd.fgrp);
+  fft_forward_dif<float2, PSG, FMAX>(sm, 5 * JB, n, d.logn, t.tw, sd.fgrp);
   const float inv = 1.0f / n, hinv = 0.5f * inv;
   // one work item per (m, slot r): the folded values of this CTA's latitude pairs at both parities. Direct
   // operands: the five slots of one m are consecutive threads, so a warp's stores of one row pair land in the
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
         if (pr >= JB) break;
         const int js = jh0 + pr;
         const float2 *row = sm + static_cast<size_t>(r * JB + pr) * rl;
-        const float2 Ym = row[fft_at<true>(bitrev(m, d.logn))], Yc = conjd(row[fft_at<true>(bitrev((n - m) & (n - 1), d.logn))]);
+        const float2 Ym = row[fft_at<PSG>(bitrev(m, d.logn))], Yc = conjd(row[fft_at<PSG>(bitrev((n - m) & (n - 1), d.logn))]);
         float2 Xs = cscale(cadd(Ym, Yc), hinv);
         const float2 tt = csub(Ym, Yc);
         float2 Xn = make_float2(hinv * tt.y, -hinv * tt.x);

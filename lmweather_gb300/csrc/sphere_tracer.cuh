@@ -63,29 +63,29 @@ __global__ void __launch_bounds__(GRID_THREADS) trc_grid(SphDev d, SphTab<double
   extern __shared__ __align__(16) unsigned char smraw[];
   double2 *sm = reinterpret_cast<double2 *>(smraw);
   const int b = blockIdx.y, jh = blockIdx.x;
-  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon, rl = fft_row<true>(n);
-  load_pair_spectra<double2, true>(sm, 2, d, four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M,
+  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon, rl = fft_row<3>(n);
+  load_pair_spectra<double2, 3>(sm, 2, d, four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M,
                                    four + (static_cast<size_t>(b) * d.nlat + jn) * 4 * d.M, d.M);
-  load_pair_spectra<double2, true>(sm + 2 * rl, 2, d, fourq + (static_cast<size_t>(b) * d.nlat + js) * 2 * d.M,
+  load_pair_spectra<double2, 3>(sm + 2 * rl, 2, d, fourq + (static_cast<size_t>(b) * d.nlat + js) * 2 * d.M,
                                    fourq + (static_cast<size_t>(b) * d.nlat + jn) * 2 * d.M, d.M);
-  fft_inverse_dit<double2, true>(sm, 4, n, d.logn, t.tw);
+  fft_inverse_dit<double2, 3>(sm, 4, n, d.logn, t.tw);
   // cpp/sphere.cpp:255-258: A = U q, B = V q, C = q delta (real part: southern latitude, imaginary: northern)
   double2 *rU = sm, *rV = sm + rl, *rQ = sm + 2 * rl, *rD = sm + 3 * rl;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const int kp = fft_at<true>(k);
+    const int kp = fft_at<3>(k);
     const double2 U = rU[kp], V = rV[kp], Q = rQ[kp], D = rD[kp];
     rU[kp] = make_double2(U.x * Q.x, U.y * Q.y);
     rV[kp] = make_double2(V.x * Q.x, V.y * Q.y);
     rQ[kp] = make_double2(Q.x * D.x, Q.y * D.y);
   }
   __syncthreads();
-  fft_forward_dif<double2, true>(sm, TRC_SLOT, n, d.logn, t.tw);
+  fft_forward_dif<double2, 3>(sm, TRC_SLOT, n, d.logn, t.tw);
   const double inv = 1.0 / n, wd = t.wd[js], wj = t.w[js];
   double2 *o = foldq + (static_cast<size_t>(b) * d.nh + jh) * TRC_SLOT * 2 * d.M;
   for (int e = threadIdx.x; e < TRC_SLOT * d.M; e += blockDim.x) {
     const int r = e / d.M, m = e - r * d.M;
     const double2 *row = sm + static_cast<size_t>(r) * rl;
-    const double2 Ym = row[fft_at<true>(bitrev(m, d.logn))], Yc = conjd(row[fft_at<true>(bitrev((n - m) & (n - 1), d.logn))]);
+    const double2 Ym = row[fft_at<3>(bitrev(m, d.logn))], Yc = conjd(row[fft_at<3>(bitrev((n - m) & (n - 1), d.logn))]);
     const double hinv = 0.5 * inv;
     double2 Xs = cscale(cadd(Ym, Yc), hinv);
     const double2 tt = csub(Ym, Yc);
