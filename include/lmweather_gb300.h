@@ -51,6 +51,11 @@ int lmw_tc_gemm_selftest(const float *A, const float *B, float *D, int N, int K,
  * [1] receive the differing counts (0 and 0 expected). Validation hook; no reference counterpart. */
 int lmw_conversion_selftest(const uint32_t *f, int nf, const uint64_t *x, int nx, int *mismatches);
 
+/* The tensor-core kernels' bounded mbarrier wait, exercised: one wait on a phase that completes and one on a phase
+ * that nothing completes, which must give up after timeout_us (1 us .. 1 s) and say so; *completed and *ran_out
+ * receive 1 when both behave. The context stays usable. Failure-detection hook; no reference counterpart. */
+int lmw_wait_selftest(int timeout_us, int *completed, int *ran_out);
+
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (the roofline of the FP64 paths) */
 int lmw_fp64_peak(double *tflops);
 
@@ -268,6 +273,10 @@ int lmw_sphere_split_plan(lmw_sphere *s, int *out);
  * candidates obey (invalid_argument otherwise); every plan computes the same arithmetic. Validation and tuning
  * hook; no reference counterpart. */
 int lmw_sphere_set_split_plan(lmw_sphere *s, const int *plan);
+/* writes `code` into a split-precision engine's error word, as a tensor-core wait that ran out does: the next step
+ * or guard check fails with LMW_DEVICE_ERROR ("a wait on the tensor cores timed out ..."). Failure-detection
+ * hook (the failure is made on the host); no reference counterpart. */
+int lmw_sphere_inject_split_error(lmw_sphere *s, int code);
 int lmw_ensemble_split_plan(lmw_ensemble *e, int group, int *out);
 int lmw_ensemble_kernel_times(lmw_ensemble *e, int group, int reps, double *ms);
 

@@ -39,6 +39,8 @@ _SIGS = {
     "lmw_last_error": (C.c_char_p, []),
     "lmw_version": (C.c_char_p, []),
     "lmw_conversion_selftest": (_I, [C.POINTER(C.c_uint32), _I, C.POINTER(C.c_uint64), _I, _IP]),
+    "lmw_wait_selftest": (_I, [_I, _IP, _IP]),
+    "lmw_sphere_inject_split_error": (_I, [_P, _I]),
     "lmw_launch_count": (C.c_uint64, []),
     "lmw_sphere_create": (_I, [_I, _D, _D, _D, _D, _PP]),
     "lmw_sphere_create_ex": (_I, [_I, _D, _D, _D, _D, _I, _I, _I, _PP]),

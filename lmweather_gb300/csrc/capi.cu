@@ -101,6 +101,12 @@ int lmw_conversion_selftest(const uint32_t *f, int nf, const uint64_t *x, int nx
     lmw::conversion_selftest_run(f, nf, x, nx, mismatches);
   });
 }
+int lmw_wait_selftest(int timeout_us, int *completed, int *ran_out) {
+  return guard([&] {
+    need(completed != nullptr && ran_out != nullptr, "null buffer");
+    lmw::wait_selftest_run(timeout_us, completed, ran_out);
+  });
+}
 int lmw_fp64_peak(double *tflops) {
   return guard([&] {
     need(tflops != nullptr, "output pointer is null");
@@ -717,6 +723,12 @@ int lmw_sphere_split_plan(lmw_sphere *s, int *out) {
     need(s != nullptr && s->e != nullptr, "null sphere handle");
     need(out != nullptr, "null buffer");
     s->e->split_plan(out);
+  });
+}
+int lmw_sphere_inject_split_error(lmw_sphere *s, int code) {
+  return guard([&] {
+    need(s != nullptr && s->e != nullptr, "null sphere handle");
+    s->e->inject_split_error(code);
   });
 }
 int lmw_sphere_set_split_plan(lmw_sphere *s, const int *plan) {

@@ -182,6 +182,8 @@ class SphereEngine {
   // replaces the autotuned plan (same 7 entries as split_plan); checked against the shared-memory and
   // tensor-memory limits the autotuner's candidates obey
   void set_split_plan(const int *in);
+  // writes `code` into the split path's error word, as a tensor-core wait that ran out does (failure tests)
+  void inject_split_error(int code);
 
  private:
   SphereTables *tab = nullptr;

@@ -86,6 +86,7 @@ extern thread_local uint64_t g_launches;
 // FP64 FMA throughput of the current device (TFLOP/s), from a dependent-chain DFMA kernel on every SM
 double measure_fp64_peak();
 int conversion_selftest_run(const uint32_t *f, int nf, const uint64_t *x, int nx, int *mismatches);
+int wait_selftest_run(int timeout_us, int *completed, int *ran_out);
 
 // Device-wide reduction results of one guard/diagnostic pass.
 struct Reduce {

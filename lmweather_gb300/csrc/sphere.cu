@@ -692,6 +692,45 @@ __global__ void conversion_selftest(const unsigned *__restrict__ fb, int nf, con
   }
 }
 
+// The bounded mbarrier wait of the tensor-core kernels, exercised on purpose: barrier 0 completes its phase (one
+// arrival), barrier 1 never does (nothing arrives on it), so its wait must give up after timeout_ns and report it.
+// out[0] = 1 when the completed phase was seen, out[1] = 1 when the other wait ran out.
+__global__ void wait_selftest(unsigned long long timeout_ns, int *out) {
+  __shared__ __align__(8) uint64_t bars[2];
+  if (threadIdx.x == 0) {
+    tc::bar_init(tc::su32(&bars[0]), 1);
+    tc::bar_init(tc::su32(&bars[1]), 1);
+    tc::bar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::su32(&bars[0])) : "memory");
+    out[0] = tc::wait_for(tc::su32(&bars[0]), 0, timeout_ns) ? 1 : 0;
+    out[1] = tc::wait_for(tc::su32(&bars[1]), 0, timeout_ns) ? 0 : 1;
+  }
+}
+
+int wait_selftest_run(int timeout_us, int *completed, int *ran_out) {
+  if (timeout_us < 1 || timeout_us > 1000000) throw InvalidArgument("timeout must be between 1 us and 1 s");
+  DevBuf<int> o;
+  o.alloc(2);
+  LMW_CUDA(cudaMemset(o.p, 0, 2 * sizeof(int)));
+  wait_selftest<<<1, 32>>>(static_cast<unsigned long long>(timeout_us) * 1000ull, o.p);
+  LMW_LAUNCH_CHECK();
+  g_launches += 1;
+  int h[2] = {0, 0};
+  LMW_CUDA(cudaMemcpy(h, o.p, sizeof h, cudaMemcpyDeviceToHost));
+  *completed = h[0];
+  *ran_out = h[1];
+  return 0;
+}
+
+void SphereEngine::inject_split_error(int code) {
+  if (!split) throw InvalidArgument("the engine is not in split precision");
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  LMW_CUDA(cudaMemcpy(split->err.p, &code, sizeof(int), cudaMemcpyHostToDevice));
+}
+
 int conversion_selftest_run(const uint32_t *f, int nf, const uint64_t *x, int nx, int *mismatches) {
   if (nf < 0 || nx < 0) throw InvalidArgument("counts must not be negative");
   DevBuf<unsigned> fd;

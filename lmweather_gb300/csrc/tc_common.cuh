@@ -18,8 +18,8 @@ __device__ __forceinline__ uint64_t gtimer() {
   return t;
 }
 
-// true when the phase completed, false when the wait ran out
-__device__ __forceinline__ bool wait(uint32_t bar, uint32_t phase) {
+// true when the phase completed, false when the wait ran out after `ns` nanoseconds
+__device__ __forceinline__ bool wait_for(uint32_t bar, uint32_t phase, unsigned long long ns) {
   const uint64_t t0 = gtimer();
   while (true) {
     uint32_t done;
@@ -28,10 +28,11 @@ __device__ __forceinline__ bool wait(uint32_t bar, uint32_t phase) {
                  : "r"(bar), "r"(phase)
                  : "memory");
     if (done) return true;
-    if (gtimer() - t0 > WAIT_NS) return false;
+    if (gtimer() - t0 > ns) return false;
     __nanosleep(20);
   }
 }
+__device__ __forceinline__ bool wait(uint32_t bar, uint32_t phase) { return wait_for(bar, phase, WAIT_NS); }
 
 __device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
