@@ -1617,8 +1617,15 @@ void SphereEngine::autotune_split() {
         for (int fg = 4; fg >= 2; fg--) cands.push_back({1, jb, fg, 0, dir, 0, 1e30});
   // one stage (no double buffering inside a CTA) leaves room for a third CTA per SM, whose copies overlap the others'
   for (int ns = 1; ns <= SPLIT_MAX_STAGES; ns++) {
-    const size_t bs = std::max(ns * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
-    if (bs <= sp.budget_bytes) cands.push_back({0, 0, 0, ns, 0, bs, 1e30});
+    // synthesis: latitude slices per (m, tile) (each CTA keeps four accumulators of its slice in tensor memory,
+    // so narrower slices let more CTAs share an SM) at this pipeline depth
+    for (int sl = 1; sl <= 4; sl *= 2) {
+      const int snh = sp.nh16 / sl;
+      if (sp.nh16 % sl != 0 || snh < 16 || snh % 16 != 0 || 4 * snh > 512) continue;
+      const size_t st = static_cast<size_t>(sp.pieces) * (sp.rSP + snh) * sp.bks * 2;
+      const size_t bs = std::max(ns * st + SPLIT_MARGIN, sp.syn_min_bytes);
+      if (bs <= sp.budget_bytes) cands.push_back({0, sl, 0, ns, 0, bs, 1e30});
+    }
     for (int dir = 1; dir >= 0; dir--)
       for (int both = 0; both <= 1; both++) {
         if (both && 2 * sp.ra_pair > 512) continue;  // both parities' accumulators must fit the 512 tensor-memory columns
@@ -1632,7 +1639,7 @@ void SphereEngine::autotune_split() {
       }
   }
   const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both, ag0 = sp.ana_grid, dir0 = sp.direct,
-            mb0 = sp.ana_minb;
+            mb0 = sp.ana_minb, sl0 = sp.syn_split;
   const size_t sms0 = sp.smem_syn, sma0 = sp.smem_ana;
   auto apply = [&](const Cand &c) {
     sp.jb = jb0;
@@ -1645,6 +1652,8 @@ void SphereEngine::autotune_split() {
     sp.ana_grid = ag0;
     sp.direct = dir0;
     sp.ana_minb = mb0;
+    sp.syn_split = sl0;
+    sp.syn_nh = sp.nh16 / sl0;
     if (c.which == 1) {
       sp.jb = c.jb;
       sp.fgrp = c.fg;
@@ -1652,6 +1661,8 @@ void SphereEngine::autotune_split() {
     } else if (c.which == 0) {
       sp.ns_syn = c.ns;
       sp.smem_syn = c.bytes;
+      sp.syn_split = c.jb;  // the synthesis candidates carry their latitude slices in jb
+      sp.syn_nh = sp.nh16 / c.jb;
     } else {
       sp.ns_ana = c.ns;
       sp.smem_ana = c.bytes;
@@ -1690,6 +1701,8 @@ void SphereEngine::autotune_split() {
   sp.fgrp = bg ? bg->fg : fg0;
   sp.ns_syn = bs ? bs->ns : nss0;
   sp.smem_syn = bs ? bs->bytes : sms0;
+  sp.syn_split = bs ? bs->jb : sl0;
+  sp.syn_nh = sp.nh16 / sp.syn_split;
   sp.ns_ana = ba ? ba->ns : nsa0;
   sp.smem_ana = ba ? ba->bytes : sma0;
   sp.ana_both = ba ? ba->jb : ab0;
@@ -1710,12 +1723,13 @@ void SphereEngine::split_plan(int *out) const {
   out[5] = split ? split->ana_grid : 0;
   out[6] = split ? split->direct : 0;
   out[7] = split ? split->ana_minb : 0;
+  out[8] = split ? split->syn_split : 0;
 }
 
 void SphereEngine::set_split_plan(const int *in) {
   if (!split) throw InvalidArgument("the engine is not in split precision");
   SplitPlan &sp = *split;
-  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6], mb = in[7];
+  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6], mb = in[7], sl = in[8];
   int dev = 0, optin = 0;
   LMW_CUDA(cudaGetDevice(&dev));
   LMW_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -1727,7 +1741,9 @@ void SphereEngine::set_split_plan(const int *in) {
     throw InvalidArgument("split plan: pipeline stages must be between 1 and " + std::to_string(SPLIT_MAX_STAGES));
   if ((both != 0 && both != 1) || (dir != 0 && dir != 1) || grid < 0) throw InvalidArgument("split plan: flags must be 0 or 1, the CTA count not negative");
   if (both && 2 * sp.ra_pair > 512) throw InvalidArgument("split plan: both parities' accumulators exceed tensor memory");
-  const size_t bs = std::max(nss * sp.syn_stage_bytes + SPLIT_MARGIN, sp.syn_min_bytes);
+  if (!(sl == 1 || sl == 2 || sl == 4) || sp.nh16 % sl != 0 || (sp.nh16 / sl) % 16 != 0 || 4 * (sp.nh16 / sl) > 512)
+    throw InvalidArgument("split plan: synthesis latitude slices must be 1, 2 or 4, leave slices of a multiple of 16 latitudes and fit tensor memory");
+  const size_t bs = std::max(nss * static_cast<size_t>(sp.pieces) * (sp.rSP + sp.nh16 / sl) * sp.bks * 2 + SPLIT_MARGIN, sp.syn_min_bytes);
   const size_t ba = std::max(sp.ana_res_bytes_v[dir] + nsa * sp.ana_stage_bytes_v[dir] + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
   if (bs > sp.budget_bytes || ba > sp.budget_bytes) throw InvalidArgument("split plan: the pipelines do not fit in shared memory");
   if (mb != 2 && mb != 3) throw InvalidArgument("split plan: the analysis register budget must be 2 or 3 CTAs per SM");
@@ -1742,6 +1758,8 @@ void SphereEngine::set_split_plan(const int *in) {
   sp.ana_grid = grid;
   sp.direct = dir;
   sp.ana_minb = mb;
+  sp.syn_split = sl;
+  sp.syn_nh = sp.nh16 / sl;
   graphs_clear();
 }
 

@@ -332,6 +332,8 @@ def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
             plans.append(dict(analysis_both_parities=both, grid_writes_operands=direct, analysis_stages=2, synthesis_stages=3))
     plans.append(dict(analysis_stages=1, synthesis_stages=1))
     plans.append(dict(analysis_stages=1, analysis_both_parities=0, analysis_ctas_per_sm=3))
+    if s.nlat // 2 >= 32:
+        plans.append(dict(synthesis_latitude_slices=2, synthesis_stages=2))
     tuned = s.split_plan()
     results = []
     for plan in [{}] + plans:
