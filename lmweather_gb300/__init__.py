@@ -39,6 +39,7 @@ _SIGS = {
     "lmw_last_error": (C.c_char_p, []),
     "lmw_version": (C.c_char_p, []),
     "lmw_conversion_selftest": (_I, [C.POINTER(C.c_uint32), _I, C.POINTER(C.c_uint64), _I, _IP]),
+    "lmw_division_selftest": (_I, [C.POINTER(C.c_uint64), _I, C.POINTER(C.c_double), _I, C.POINTER(C.c_longlong)]),
     "lmw_wait_selftest": (_I, [_I, _IP, _IP]),
     "lmw_sphere_inject_split_error": (_I, [_P, _I]),
     "lmw_launch_count": (C.c_uint64, []),

@@ -101,6 +101,12 @@ int lmw_conversion_selftest(const uint32_t *f, int nf, const uint64_t *x, int nx
     lmw::conversion_selftest_run(f, nf, x, nx, mismatches);
   });
 }
+int lmw_division_selftest(const uint64_t *x, int nx, const double *divisors, int nd, long long *counts) {
+  return guard([&] {
+    need(counts != nullptr && (nx == 0 || x != nullptr) && (nd == 0 || divisors != nullptr), "null buffer");
+    lmw::division_selftest_run(x, nx, divisors, nd, counts);
+  });
+}
 int lmw_wait_selftest(int timeout_us, int *completed, int *ran_out) {
   return guard([&] {
     need(completed != nullptr && ran_out != nullptr, "null buffer");

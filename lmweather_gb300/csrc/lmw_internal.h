@@ -87,6 +87,7 @@ extern thread_local uint64_t g_launches;
 double measure_fp64_peak();
 int conversion_selftest_run(const uint32_t *f, int nf, const uint64_t *x, int nx, int *mismatches);
 int wait_selftest_run(int timeout_us, int *completed, int *ran_out);
+void division_selftest_run(const uint64_t *x, int nx, const double *y, int ny, long long *counts);
 
 // Device-wide reduction results of one guard/diagnostic pass.
 struct Reduce {

@@ -188,3 +188,50 @@ def test_plane_rossby_known_answers(engine):
 
 def test_plane_adjustment_known_answers(engine):
     plane_adjustment_case(_gpu_plane_class(engine))
+
+
+def _division_inputs(rng, n):
+    """Dividends: random bit patterns over every exponent (zeros, subnormals, infinities and NaNs included),
+    stencil-like differences of magnitude 1e-12 .. 1e6, and the special values."""
+    raw = rng.integers(0, 2 ** 63, n, dtype=np.uint64) | (rng.integers(0, 2, n, dtype=np.uint64) << np.uint64(63))
+    mag = 10.0 ** rng.uniform(-12, 6, n) * np.where(rng.integers(0, 2, n) == 0, -1.0, 1.0)
+    specials = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324, 2.2250738585072014e-308, 1.7976931348623157e308,
+                         -1.7976931348623157e308, 1.0, -1.0, 3.0, 0.1], np.float64)
+    return np.concatenate([raw, mag.view(np.uint64), specials.view(np.uint64)]), mag
+
+
+def _division_counts(lib, x, divisors):
+    import ctypes as C
+
+    counts = np.zeros(2, np.int64)
+    d = np.ascontiguousarray(divisors, np.float64)
+    st = lib.lmw_division_selftest(x.ctypes.data_as(C.POINTER(C.c_uint64)), x.size, d.ctypes.data_as(C.POINTER(C.c_double)), d.size,
+                                   counts.ctypes.data_as(C.POINTER(C.c_longlong)))
+    return st, counts
+
+
+def test_fixed_divisor_division_is_the_ieee_division(engine):
+    """The stencil's division by a grid spacing (reciprocal, Markstein correction, exact acceptance test) gives the
+    IEEE quotient bit for bit on every dividend, and the fast path answers all but a tiny fraction of stencil-like
+    dividends (the rest fall back to the IEEE division)."""
+    rng = np.random.default_rng(23)
+    x, mag = _division_inputs(rng, 1 << 20)
+    plane_spacings = [5000.0, 2500.0, 5000.0 ** 2, 2500.0 ** 2, 1.0e5, 1.0e10, 3906.25, 1953.125 ** 2, 1.0e6 / 20, (1.0e6 / 20) ** 2]
+    others = [1.0, 3.0, 1.0 / 3.0, 0.1, -7.5, 2.0 ** -1021, 2.0 ** 1021, 1.5 * 2.0 ** 1020, 2.2250738585072014e-308 * 4.0]
+    logu = 10.0 ** rng.uniform(-300, 300, 24)
+    divisors = np.array(plane_spacings + others + list(logu) + list(-rng.uniform(0.5, 2.0, 4)), np.float64)
+    lib = engine.load_library()
+    st, counts = _division_counts(lib, x, divisors)
+    assert st == 0
+    assert counts[0] == 0, f"{counts[0]} quotients differ from the IEEE division"
+    # stencil-like dividends by the plane's spacings: the fast path answers them
+    st, counts = _division_counts(lib, mag.view(np.uint64), plane_spacings)
+    assert st == 0 and counts[0] == 0
+    assert counts[1] >= 0.999 * mag.size * len(plane_spacings), counts
+    # multiples of the divisor: exact quotients
+    mult = np.concatenate([np.arange(-4096, 4097, dtype=np.float64) * 5000.0, np.arange(1, 4097, dtype=np.float64) * 2.5e7])
+    st, counts = _division_counts(lib, mult.view(np.uint64), [5000.0, 2.5e7])
+    assert st == 0 and counts[0] == 0
+    # a divisor whose reciprocal is not a normal number is refused
+    st, counts = _division_counts(lib, x[:4], [1.0e308])
+    assert st == 1  # LMW_INVALID_ARGUMENT
