@@ -51,11 +51,11 @@ int lmw_tc_gemm_selftest(const float *A, const float *B, float *D, int N, int K,
  * [1] receive the differing counts (0 and 0 expected). Validation hook; no reference counterpart. */
 int lmw_conversion_selftest(const uint32_t *f, int nf, const uint64_t *x, int nx, int *mismatches);
 
-/* The plane stencil's division by a fixed grid spacing (reciprocal, one residual correction and an exact
- * acceptance test, four FP64 operations where the IEEE division takes about ten) against the IEEE division, on every
- * pair of nx double bit patterns and nd divisors (normal numbers with normal reciprocals). counts[0] receives the
- * pairs whose results differ in any bit (0 expected), counts[1] those the fast path answered without falling back
- * to the IEEE division. Validation hook; no reference counterpart. */
+/* The plane stencil's division by a fixed grid spacing (two-term reciprocal and an exact acceptance test, three
+ * FP64 operations, falling back to the IEEE division when the test fails) against the IEEE division, on every pair
+ * of nx double bit patterns and nd divisors (normal numbers with normal reciprocals). counts (2 entries) receives:
+ * [0] the pairs whose quotients differ in any bit (0 expected), [1] the pairs the fast path answered without
+ * falling back. Validation hook; no reference counterpart. */
 int lmw_division_selftest(const uint64_t *x, int nx, const double *divisors, int nd, long long *counts);
 
 /* The tensor-core kernels' bounded mbarrier wait, exercised: one wait on a phase that completes and one on a phase

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "fixed_div.cuh"
 
 namespace lmw {
 namespace {
@@ -21,53 +22,15 @@ constexpr int TX = 32, TY = 8;
 
 struct PlaneDev {
   int nx, ny, lin;
-  double dxx, dyy, dxx2, dyy2, g, depth, f0, beta, visc, drag, ly;
-  double rdxx, rdyy, rdxx2, rdyy2;  // RN(1 / divisor), for div_fixed
+  double dxx, dyy, dxx2, dyy2, g, depth, f0, beta, visc, drag, ly, hly;  // hly = 0.5 ly (exact)
+  double zh[4], zl[4];  // two-term reciprocals of dxx, dyy, dxx2, dyy2 (in that order), for div_fixed
   int fastdiv;                      // every divisor and its reciprocal are normal numbers
 };
 
-constexpr unsigned long long kAbs = 0x7fffffffffffffffull, kMant = 0x000fffffffffffffull;
-
-// x / y correctly rounded (round to nearest even), for a divisor y fixed for the run and its reciprocal
-// rz = RN(1 / y) computed once on the host. GB300's FP64 pipe is narrow and an IEEE division costs about ten
-// FP64 operations; this costs four. q0 = RN(x rz) is refined once with its exact-by-FMA residual,
-// q1 = RN(q0 + (x - q0 y) rz) (the correction step of P. Markstein, "Computation of elementary functions on the
-// IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990), and q1 is then ACCEPTED only on a proof that it
-// is the rounded quotient: with gap the distance from |q1| to the next double toward zero (the smaller of its two
-// neighbour gaps) and T = |y| gap / 2 (a power-of-two scaling of y, formed exactly on the integer pipe), the FMA
-// residual r1 = RN(x - q1 y) satisfies |r1| < T only if |x - q1 y| < T (rounding is monotone and T is a double),
-// that is |x / y - q1| < gap / 2, which puts x / y strictly inside q1's rounding interval. Zero dividends return
-// x rz (a signed zero with the quotient's sign); everything else that is not accepted (ties, non-finite values,
-// quotients or bounds outside the normal range) takes the IEEE division, so the result is RN(x / y) for every x.
-__device__ __forceinline__ double div_fixed(double x, double y, double rz, int &fast) {
-  const double q0 = __dmul_rn(x, rz);
-  const double r0 = __fma_rn(-q0, y, x);
-  const double q1 = __fma_rn(r0, rz, q0);
-  const double r1 = __fma_rn(-q1, y, x);
-  const unsigned long long bx = static_cast<unsigned long long>(__double_as_longlong(x));
-  const unsigned long long bq = static_cast<unsigned long long>(__double_as_longlong(q1)) & kAbs;
-  const unsigned long long by = static_cast<unsigned long long>(__double_as_longlong(y)) & kAbs;
-  const unsigned long long br = static_cast<unsigned long long>(__double_as_longlong(r1)) & kAbs;
-  if ((bx & kAbs) == 0) {
-    fast = 1;
-    return q0;
-  }
-  const int eq = static_cast<int>(bq >> 52);
-  // biased exponent of T: |y| times 2^(exponent of gap - 1), gap = ulp(q1), halved when q1 is a power of two
-  const int et = static_cast<int>(by >> 52) + eq - 1023 - 53 - ((bq & kMant) == 0 ? 1 : 0);
-  if (eq >= 1 && eq <= 2046 && et >= 1 && et <= 2046 &&
-      br < ((static_cast<unsigned long long>(et) << 52) | (by & kMant))) {
-    fast = 1;
-    return q1;
-  }
-  fast = 0;
-  return x / y;
-}
-
 // the stencil's divisions by the grid spacings: div_fixed when the host found the spacings normal, else IEEE
-__device__ __forceinline__ double div_by(const PlaneDev &p, double x, double y, double rz) {
+__device__ __forceinline__ double div_by(const PlaneDev &p, double x, double y, int k) {
   int fast;
-  return p.fastdiv ? div_fixed(x, y, rz, fast) : x / y;
+  return p.fastdiv ? div_fixed(x, y, p.zh[k], p.zl[k], fast) : x / y;
 }
 
 __device__ __forceinline__ int wrapx(int i, int nx) { return ((i % nx) + nx) % nx; }
@@ -115,13 +78,13 @@ __global__ void __launch_bounds__(TX *TY) plane_stage(PlaneDev p, int stage, dou
     int je = j0 + ly;
     double eta = 0;
     if (je <= ny) {
-      double f = p.f0 + p.beta * (je * p.dyy - 0.5 * p.ly);
+      double f = p.f0 + p.beta * (je * p.dyy - p.hly);
       double zeta = 0;
       if (!p.lin) {
-        double dvdx = div_by(p, sv[ly + 1][lx + 1] - sv[ly + 1][lx], p.dxx, p.rdxx);
+        double dvdx = div_by(p, sv[ly + 1][lx + 1] - sv[ly + 1][lx], p.dxx, 0);
         double uj = je < ny ? su[ly + 1][lx + 1] : su[ly][lx + 1];
         double ujm = je > 0 ? su[ly][lx + 1] : su[ly + 1][lx + 1];
-        zeta = dvdx - div_by(p, uj - ujm, p.dyy, p.rdyy);
+        zeta = dvdx - div_by(p, uj - ujm, p.dyy, 1);
       }
       eta = f + zeta;
     }
@@ -137,10 +100,10 @@ __global__ void __launch_bounds__(TX *TY) plane_stage(PlaneDev p, int stage, dou
   {
     double q = 0.5 * (sE[ty][tx] + sE[ty + 1][tx]);
     double vbar = 0.25 * (sv[ty + 1][tx] + sv[ty + 1][tx + 1] + sv[ty + 2][tx] + sv[ty + 2][tx + 1]);
-    double r = q * vbar - div_by(p, sB[ty + 1][tx + 1] - sB[ty + 1][tx], p.dxx, p.rdxx) - p.drag * U;
+    double r = q * vbar - div_by(p, sB[ty + 1][tx + 1] - sB[ty + 1][tx], p.dxx, 0) - p.drag * U;
     if (p.visc != 0) {
       double uy1 = j + 1 < ny ? su[ty + 2][tx + 1] : U, uy0 = j > 0 ? su[ty][tx + 1] : U;
-      r += p.visc * (div_by(p, su[ty + 1][tx + 2] - 2 * U + su[ty + 1][tx], p.dxx2, p.rdxx2) + div_by(p, uy1 - 2 * U + uy0, p.dyy2, p.rdyy2));
+      r += p.visc * (div_by(p, su[ty + 1][tx + 2] - 2 * U + su[ty + 1][tx], p.dxx2, 2) + div_by(p, uy1 - 2 * U + uy0, p.dyy2, 3));
     }
     du = r;
   }
@@ -149,10 +112,10 @@ __global__ void __launch_bounds__(TX *TY) plane_stage(PlaneDev p, int stage, dou
   if (j >= 1) {
     double q = 0.5 * (sE[ty][tx] + sE[ty][tx + 1]);
     double ubar = 0.25 * (su[ty][tx + 1] + su[ty][tx + 2] + su[ty + 1][tx + 1] + su[ty + 1][tx + 2]);
-    double r = -q * ubar - div_by(p, sB[ty + 1][tx + 1] - sB[ty][tx + 1], p.dyy, p.rdyy) - p.drag * V;
+    double r = -q * ubar - div_by(p, sB[ty + 1][tx + 1] - sB[ty][tx + 1], p.dyy, 1) - p.drag * V;
     if (p.visc != 0) {
       double vy1 = j + 1 < ny ? sv[ty + 2][tx + 1] : 0.0, vy0 = j - 1 > 0 ? sv[ty][tx + 1] : 0.0;
-      r += p.visc * (div_by(p, sv[ty + 1][tx + 2] - 2 * V + sv[ty + 1][tx], p.dxx2, p.rdxx2) + div_by(p, vy1 - 2 * V + vy0, p.dyy2, p.rdyy2));
+      r += p.visc * (div_by(p, sv[ty + 1][tx + 2] - 2 * V + sv[ty + 1][tx], p.dxx2, 2) + div_by(p, vy1 - 2 * V + vy0, p.dyy2, 3));
     }
     dv = r;
   }
@@ -165,7 +128,7 @@ __global__ void __launch_bounds__(TX *TY) plane_stage(PlaneDev p, int stage, dou
     double fn = 0, fs = 0;
     if (j + 1 < ny) fn = (p.lin ? p.depth : 0.5 * (Hc + sh[ty + 2][tx + 1])) * sv[ty + 2][tx + 1];
     if (j > 0) fs = (p.lin ? p.depth : 0.5 * (sh[ty][tx + 1] + Hc)) * V;
-    dh = -(div_by(p, fe - fw, p.dxx, p.rdxx) + div_by(p, fn - fs, p.dyy, p.rdyy));
+    dh = -(div_by(p, fe - fw, p.dxx, 0) + div_by(p, fn - fs, p.dyy, 1));
   }
   const size_t o = static_cast<size_t>(j) * nx + i;
   // RK4 bookkeeping: cpp/plane.cpp:146-156 (acc = k1 + 2 k2 + 2 k3, state += dt/6 (acc + k4))
@@ -344,17 +307,11 @@ PlaneDev make_dev(const PlaneConfig &c) {
   d.visc = c.viscosity;
   d.drag = c.drag;
   d.ly = c.ly;
+  d.hly = 0.5 * c.ly;
   const double dv[4] = {d.dxx, d.dyy, d.dxx2, d.dyy2};
-  double rv[4];
   d.fastdiv = 1;
-  for (int k = 0; k < 4; k++) {
-    rv[k] = 1.0 / dv[k];
-    if (std::fpclassify(dv[k]) != FP_NORMAL || std::fpclassify(rv[k]) != FP_NORMAL) d.fastdiv = 0;
-  }
-  d.rdxx = rv[0];
-  d.rdyy = rv[1];
-  d.rdxx2 = rv[2];
-  d.rdyy2 = rv[3];
+  for (int k = 0; k < 4; k++)
+    if (!fixed_div_reciprocal(dv[k], d.zh[k], d.zl[k])) d.fastdiv = 0;
   return d;
 }
 
@@ -381,7 +338,8 @@ static __device__ __align__(256) double g_noalloc_scratch[9 * kNoAllocFieldCap];
 // div_fixed against the IEEE division on every pair (x[i], y[k]): counts[0] = results that differ in any bit,
 // counts[1] = pairs the fast path answered (the rest took the IEEE division)
 __global__ void division_selftest(const unsigned long long *__restrict__ xb, int nx, const double *__restrict__ y,
-                                  const double *__restrict__ rz, int ny, unsigned long long *counts) {
+                                  const double *__restrict__ zh, const double *__restrict__ zl, int ny,
+                                  unsigned long long *counts) {
   const long long total = static_cast<long long>(nx) * ny;
   unsigned long long bad = 0, fastn = 0;
   for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
@@ -389,7 +347,7 @@ __global__ void division_selftest(const unsigned long long *__restrict__ xb, int
     const double x = __longlong_as_double(static_cast<long long>(xb[e % nx]));
     const int k = static_cast<int>(e / nx);
     int fast = 0;
-    const double a = div_fixed(x, y[k], rz[k], fast);
+    const double a = div_fixed(x, y[k], zh[k], zl[k], fast);
     const double b = x / y[k];
     bad += __double_as_longlong(a) != __double_as_longlong(b) ? 1 : 0;
     fastn += fast;
@@ -402,31 +360,32 @@ __global__ void division_selftest(const unsigned long long *__restrict__ xb, int
 
 void division_selftest_run(const uint64_t *x, int nx, const double *y, int ny, long long *counts) {
   if (nx < 0 || ny < 0 || nx > (1 << 26) || ny > 4096) throw InvalidArgument("counts out of range");
-  std::vector<double> rz(std::max(ny, 1));
-  for (int k = 0; k < ny; k++) {
-    rz[k] = 1.0 / y[k];
-    if (std::fpclassify(y[k]) != FP_NORMAL || std::fpclassify(rz[k]) != FP_NORMAL)
+  std::vector<double> zh(std::max(ny, 1)), zl(std::max(ny, 1));
+  for (int k = 0; k < ny; k++)
+    if (!fixed_div_reciprocal(y[k], zh[k], zl[k]))
       throw InvalidArgument("divisor " + std::to_string(k) + " or its reciprocal is not a normal number");
-  }
   DevBuf<unsigned long long> xd, cd;
-  DevBuf<double> yd, rd;
+  DevBuf<double> yd, hd, ld;
   xd.alloc(std::max(nx, 1));
   yd.alloc(std::max(ny, 1));
-  rd.alloc(std::max(ny, 1));
+  hd.alloc(std::max(ny, 1));
+  ld.alloc(std::max(ny, 1));
   cd.alloc(2);
   if (nx) LMW_CUDA(cudaMemcpy(xd.p, x, nx * sizeof(unsigned long long), cudaMemcpyHostToDevice));
-  if (ny) LMW_CUDA(cudaMemcpy(yd.p, y, ny * sizeof(double), cudaMemcpyHostToDevice));
-  if (ny) LMW_CUDA(cudaMemcpy(rd.p, rz.data(), ny * sizeof(double), cudaMemcpyHostToDevice));
+  if (ny) {
+    LMW_CUDA(cudaMemcpy(yd.p, y, ny * sizeof(double), cudaMemcpyHostToDevice));
+    LMW_CUDA(cudaMemcpy(hd.p, zh.data(), ny * sizeof(double), cudaMemcpyHostToDevice));
+    LMW_CUDA(cudaMemcpy(ld.p, zl.data(), ny * sizeof(double), cudaMemcpyHostToDevice));
+  }
   LMW_CUDA(cudaMemset(cd.p, 0, 2 * sizeof(unsigned long long)));
   if (nx > 0 && ny > 0) {
-    division_selftest<<<1024, 256>>>(xd.p, nx, yd.p, rd.p, ny, cd.p);
+    division_selftest<<<1024, 256>>>(xd.p, nx, yd.p, hd.p, ld.p, ny, cd.p);
     LMW_LAUNCH_CHECK();
     g_launches += 1;
   }
   unsigned long long c[2];
   LMW_CUDA(cudaMemcpy(c, cd.p, sizeof(c), cudaMemcpyDeviceToHost));
-  counts[0] = static_cast<long long>(c[0]);
-  counts[1] = static_cast<long long>(c[1]);
+  for (int k = 0; k < 2; k++) counts[k] = static_cast<long long>(c[k]);
 }
 
 // Device address of g_noalloc_scratch on the current device. In host code the symbol's name is only a host-side

@@ -20,6 +20,7 @@
 #include <functional>
 
 #include "engine.h"
+#include "fixed_div.cuh"
 #include "sphere_common.cuh"
 #include "sphere_tables.h"
 
@@ -129,8 +130,14 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, SphTab<R> t, 
   // cpp/sphere.cpp:200-201: fu = (i m sc - hp)/a, fv = (i m sp + hc)/a
   C2 fu = csub(imul(SC, mm), HP), fv = cadd(imul(SP, mm), HC);
   if (sizeof(R) == 8) {
-    fu = mk2(R(fu.x / d.a), R(fu.y / d.a));
-    fv = mk2(R(fv.x / d.a), R(fv.y / d.a));
+    if (d.div_a) {  // the same quotients as the IEEE division, in three FP64 operations each
+      int fast;
+      fu = mk2(R(div_fixed(fu.x, d.a, d.inv_a, d.inv_a_l, fast)), R(div_fixed(fu.y, d.a, d.inv_a, d.inv_a_l, fast)));
+      fv = mk2(R(div_fixed(fv.x, d.a, d.inv_a, d.inv_a_l, fast)), R(div_fixed(fv.y, d.a, d.inv_a, d.inv_a_l, fast)));
+    } else {
+      fu = mk2(R(fu.x / d.a), R(fu.y / d.a));
+      fv = mk2(R(fv.x / d.a), R(fv.y / d.a));
+    }
   } else {
     fu = cscale(fu, ia);
     fv = cscale(fv, ia);
@@ -763,6 +770,7 @@ static SphDev make_sph(const SphereEngine &e, const SphereTables &t) {
   d.a = e.p.radius;
   d.g = e.p.gravity;
   d.inv_a_f = static_cast<float>(1.0 / e.p.radius);
+  d.div_a = fixed_div_reciprocal(e.p.radius, d.inv_a, d.inv_a_l) ? 1 : 0;
   d.Ps = t.Ps.p;
   d.Hs = t.Hs.p;
   d.Pa = t.Pa.p;

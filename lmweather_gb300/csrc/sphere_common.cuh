@@ -15,6 +15,8 @@ struct SphDev {
   const int *gflag;
   const double *om2;  // 2 Omega per member
   float inv_a_f;      // 1/a rounded to FP32 once on the host (the FP32 kernels' metric factor)
+  double inv_a, inv_a_l;  // 1/a as a two-term sum, for the FP64 synthesis's correctly rounded division (div_fixed)
+  int div_a;          // a and 1/a are normal numbers (else the synthesis divides plainly)
 };
 
 template <class R> struct V2;

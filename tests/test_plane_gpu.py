@@ -211,9 +211,9 @@ def _division_counts(lib, x, divisors):
 
 
 def test_fixed_divisor_division_is_the_ieee_division(engine):
-    """The stencil's division by a grid spacing (reciprocal, Markstein correction, exact acceptance test) gives the
-    IEEE quotient bit for bit on every dividend, and the fast path answers all but a tiny fraction of stencil-like
-    dividends (the rest fall back to the IEEE division)."""
+    """The stencil's division by a grid spacing (two-term reciprocal, exact acceptance test) gives the IEEE quotient
+    bit for bit on every dividend, and the fast path answers all but a tiny fraction of stencil-like dividends (the
+    rest fall back to the IEEE division)."""
     rng = np.random.default_rng(23)
     x, mag = _division_inputs(rng, 1 << 20)
     plane_spacings = [5000.0, 2500.0, 5000.0 ** 2, 2500.0 ** 2, 1.0e5, 1.0e10, 3906.25, 1953.125 ** 2, 1.0e6 / 20, (1.0e6 / 20) ** 2]
