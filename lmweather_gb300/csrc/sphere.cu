@@ -321,21 +321,25 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_grid(SphDev d, SphTab<R> t, 
   const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
   const double *hr_s = hsgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *hr_n = hsgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
   const int gf = d.gflag[b];
-  const double f0s = d.om2[b] * d.mu[js], f0n = d.om2[b] * d.mu[jn];
+  // the FP64 Coriolis and orography values in the arithmetic type; FP32 rounds them on the integer pipe (the
+  // hardware conversion's values, without the narrow FP64 pipe)
+  const R f0s = to_arith<R>(d.om2[b] * d.mu[js]), f0n = to_arith<R>(d.om2[b] * d.mu[jn]);
   C2 *rU = sm, *rV = sm + rl, *rZ = sm + 2 * rl, *rP = sm + 3 * rl, *rE = sm + 4 * rl;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
     const int kp = fft_at<3>(k);
     const C2 U = rU[kp], V = rV[kp], Z = rZ[kp], P = rP[kp];
     C2 A, Bv, UP, VP, PE;
     {
-      R eta = Z.x + static_cast<R>((gf & 1) ? fr_s[k] : f0s);
+      R eta = Z.x + ((gf & 1) ? to_arith<R>(fr_s[k]) : f0s);
+      const R hs = (gf & 2) ? to_arith<R>(hr_s[k]) : R(0);
       A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
-      PE.x = P.x + g * static_cast<R>((gf & 2) ? hr_s[k] : 0.0) + (U.x * U.x + V.x * V.x) * r2om;
+      PE.x = P.x + g * hs + (U.x * U.x + V.x * V.x) * r2om;
     }
     {
-      R eta = Z.y + static_cast<R>((gf & 1) ? fr_n[k] : f0n);
+      R eta = Z.y + ((gf & 1) ? to_arith<R>(fr_n[k]) : f0n);
+      const R hs = (gf & 2) ? to_arith<R>(hr_n[k]) : R(0);
       A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
-      PE.y = P.y + g * static_cast<R>((gf & 2) ? hr_n[k] : 0.0) + (U.y * U.y + V.y * V.y) * r2om;
+      PE.y = P.y + g * hs + (U.y * U.y + V.y * V.y) * r2om;
     }
     rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
@@ -1323,7 +1327,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   sa.stage = stage;
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
   sa.filt = filt;
-  if (which < 0 || which == 0) split_syn<<<dim3(d.M, sp.ntiles, sp.syn_split), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
+  if (which < 0 || which == 0) split_syn<<<dim3(sp.ntiles, sp.syn_split, d.M), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
   if (which < 0 || which == 1) {
     const dim3 grid(d.nh / sp.jb, B);
     const size_t bytes = 5 * static_cast<size_t>(sp.jb) * fft_row<3>(d.nlon) * sizeof(float2);

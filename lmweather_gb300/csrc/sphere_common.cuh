@@ -74,6 +74,11 @@ __device__ __forceinline__ float d2f_int(double x) {
   return __uint_as_float(r | (hi & 0x80000000u));
 }
 
+// a double in the kernel's arithmetic type: itself for FP64, d2f_int (the hardware's rounding) for FP32
+template <class R> __device__ __forceinline__ R to_arith(double x);
+template <> __device__ __forceinline__ double to_arith<double>(double x) { return x; }
+template <> __device__ __forceinline__ float to_arith<float>(double x) { return d2f_int(x); }
+
 constexpr int NSLOT = 5;  // A, B, U Phi, V Phi (times w/((1-mu^2)a)) and the Bernoulli function (times w)
 
 struct StageArgs {

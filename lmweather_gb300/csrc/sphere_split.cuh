@@ -266,16 +266,18 @@ __device__ __forceinline__ void split_teardown(uint32_t tmem, uint32_t ncols) {
 }
 
 // ------------------------------------------------------------------------------------------- synthesis
-// grid: (M, ntiles). D columns: H E/O at [0, nh16), [nh16, 2 nh16); P E/O at [2 nh16, 3 nh16), [3 nh16, 4 nh16)
+// grid: (ntiles, latitude slices, M). D columns: H E/O at [0, nh16), [nh16, 2 nh16); P E/O at [2 nh16, 3 nh16), [3 nh16, 4 nh16)
 __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev sd, int B, int ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
-  // blockIdx.z: latitude slice [jh0, jh0 + nh16) of the table's sd.nh16 rows (two slices at T341, where four
+  // blockIdx.y: latitude slice [jh0, jh0 + nh16) of the table's sd.nh16 rows (two slices at T341, where four
   // accumulators of all latitudes would exceed the 512 tensor-memory columns)
-  const int m = blockIdx.x, tile = blockIdx.y;
+  // m is the slowest grid index: CTAs start in order of decreasing work (K shrinks with m), and the small
+  // high-m CTAs fill the last wave
+  const int m = blockIdx.z, tile = blockIdx.x;
   const int mt = min(sd.nbt, B - tile * sd.nbt);
-  const int nh16 = sd.syn_nh, jh0 = blockIdx.z * nh16;
+  const int nh16 = sd.syn_nh, jh0 = blockIdx.y * nh16;
   uint32_t ncols = 32;
   while (ncols < static_cast<uint32_t>(4 * nh16)) ncols <<= 1;
   split_setup(&tslot, ncols, full, empty, &done, ns);
@@ -413,15 +415,19 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
     const int kp = fft_at<PSG>(k);
     const float2 U = rU[kp], V = rV[kp], Z = rZ[kp], P = rP[kp];
     float2 A, Bv, UP, VP, PE;
+    // the FP64 Coriolis and orography rows (tilted or mountain members only) are rounded to FP32 on the integer
+    // pipe: the same values as the hardware conversion, without the narrow FP64 pipe
     {
-      const float eta = Z.x + ((gf & 1) ? static_cast<float>(fr_s[k]) : cor[2 * pr]);
+      const float eta = Z.x + ((gf & 1) ? d2f_int(fr_s[k]) : cor[2 * pr]);
+      const float hs = (gf & 2) ? d2f_int(hr_s[k]) : 0.0f;
       A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
-      PE.x = P.x + g * static_cast<float>((gf & 2) ? hr_s[k] : 0.0) + (U.x * U.x + V.x * V.x) * r2om;
+      PE.x = P.x + g * hs + (U.x * U.x + V.x * V.x) * r2om;
     }
     {
-      const float eta = Z.y + ((gf & 1) ? static_cast<float>(fr_n[k]) : cor[2 * pr + 1]);
+      const float eta = Z.y + ((gf & 1) ? d2f_int(fr_n[k]) : cor[2 * pr + 1]);
+      const float hs = (gf & 2) ? d2f_int(hr_n[k]) : 0.0f;
       A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
-      PE.y = P.y + g * static_cast<float>((gf & 2) ? hr_n[k] : 0.0) + (U.y * U.y + V.y * V.y) * r2om;
+      PE.y = P.y + g * hs + (U.y * U.y + V.y * V.y) * r2om;
     }
     rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
@@ -571,9 +577,13 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
-  // work items (m, parity or both, member tile), m fastest; a CTA takes items blockIdx.x, blockIdx.x + gridDim.x, ...
-  // with one TMEM allocation and one set of barriers whose phases continue from item to item
-  const int nitems = d.M * (BOTH ? 1 : 2) * sd.ntiles;
+  // work items (m, parity or both, member tile); a CTA takes items blockIdx.x, blockIdx.x + gridDim.x, ... with one
+  // TMEM allocation and one set of barriers whose phases continue from item to item. With one CTA per item, m is
+  // the slowest index (CTAs start in order of decreasing work: fewer coefficients as m grows, so the small items
+  // fill the last wave); with fewer CTAs, m is the fastest (each CTA gets a mix of m)
+  const int per_m = (BOTH ? 1 : 2) * sd.ntiles;
+  const int nitems = d.M * per_m;
+  const bool m_slowest = static_cast<int>(gridDim.x) >= nitems;
   uint32_t ncols = 32;
   while (ncols < static_cast<uint32_t>(BOTH ? sd.ana_cols_both : sd.ana_cols_one)) ncols <<= 1;
   // DIRECT: A operands streamed with the tables; otherwise gathered from the FP32 fold into resident shared memory
@@ -584,7 +594,7 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
   bool ok = true, setup_done = false;
   int pipe_it = 0, calls = 0;
   for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-  const int m = item % d.M, rest = item / d.M;
+  const int m = m_slowest ? item / per_m : item % d.M, rest = m_slowest ? item % per_m : item / d.M;
   const int s_first = BOTH ? 0 : rest % 2, s_last = BOTH ? 1 : s_first;
   const int tile = BOTH ? rest : rest / 2;
   const int mt = min(sd.nbt, B - tile * sd.nbt);
