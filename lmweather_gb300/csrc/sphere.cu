@@ -70,7 +70,9 @@ __global__ void __launch_bounds__(SYN_THREADS) sph_synth(SphDev d, SphTab<R> t, 
       const int q = base + n - m;
       const R P = t.Ps[static_cast<size_t>(q) * d.nh + jh], H = t.Hs[static_cast<size_t>(q) * d.nh + jh];
       const double2 zd = xz[q], dd = xd[q], fd = xf[q];
-      const C2 z = mk2(R(zd.x), R(zd.y)), dl = mk2(R(dd.x), R(dd.y)), f = mk2(R(fd.x), R(fd.y));
+      // FP32: the state is rounded on the integer pipe (the hardware conversion's values)
+      const C2 z = mk2(to_arith<R>(zd.x), to_arith<R>(zd.y)), dl = mk2(to_arith<R>(dd.x), to_arith<R>(dd.y)),
+               f = mk2(to_arith<R>(fd.x), to_arith<R>(fd.y));
       const R k = t.kfac[n];  // psi = -a^2/(n(n+1)) zeta, cpp/sphere.cpp:185-190
       const C2 psi = cscale(z, k), chi = cscale(dl, k);
       sp = cfma(sp, psi, P);
@@ -444,8 +446,9 @@ __global__ void __launch_bounds__(ANA_THREADS) sph_analysis(SphDev d, SphTab<R> 
   C2 kf = csub(vH, imul(uP, mm));
   if (q == 0 || sa.zero) kz = kd = kf = mk2(R(0), R(0));  // cpp/sphere.cpp:387-389
   const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
-  // the RK4 state accumulates in FP64 whatever the precision of the tendencies
-  const double2 k[3] = {make_double2(kz.x, kz.y), make_double2(kd.x, kd.y), make_double2(kf.x, kf.y)};
+  // the RK4 state accumulates in FP64 whatever the precision of the tendencies (FP32 widened on the integer pipe)
+  const double2 k[3] = {make_double2(from_arith(kz.x), from_arith(kz.y)), make_double2(from_arith(kd.x), from_arith(kd.y)),
+                        make_double2(from_arith(kf.x), from_arith(kf.y))};
   // every load of the three fields is issued before any store (the buffers never alias)
   double2 xv[3], av[3];
 #pragma unroll

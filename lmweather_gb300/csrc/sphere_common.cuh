@@ -78,6 +78,9 @@ __device__ __forceinline__ float d2f_int(double x) {
 template <class R> __device__ __forceinline__ R to_arith(double x);
 template <> __device__ __forceinline__ double to_arith<double>(double x) { return x; }
 template <> __device__ __forceinline__ float to_arith<float>(double x) { return d2f_int(x); }
+// a value of the kernel's arithmetic type widened to double: itself for FP64, f2d_int (exact) for FP32
+__device__ __forceinline__ double from_arith(double x) { return x; }
+__device__ __forceinline__ double from_arith(float x) { return f2d_int(x); }
 
 constexpr int NSLOT = 5;  // A, B, U Phi, V Phi (times w/((1-mu^2)a)) and the Bernoulli function (times w)
 
