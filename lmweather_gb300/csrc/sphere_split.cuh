@@ -45,7 +45,8 @@ constexpr size_t SPLIT_HALF_SM = 115456;
 struct SplitPlan {
   int pieces = 2, terms = 3;
   int nbt = 1, ntiles = 1, nh16 = 16, nh64 = 64, rAP = 8, rAH = 8, rSP = 8, rSH = 8, ra_max = 16;
-  int bka = 64, nha = 64;  // analysis K (latitude) chunk width (64, or the padded latitude count below 64) and padded K
+  int bka = 32, nha = 64;  // analysis K (latitude) chunk width (32, or the padded latitude count below 32; 64-wide
+                           // chunks measured slower at T85) and padded K
   int bks = 64;            // synthesis K (coefficient) chunk width: 32 up to T85 (less padding per m), 64 above
   std::vector<int> ke16, kps, ra16;  // kps[m]: synthesis K of m padded to the chunk width bks
   std::vector<long> tS_off, tA_off, aS_off, aSH_off;
@@ -804,7 +805,7 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   sp.ntiles = (B + sp.nbt - 1) / sp.nbt;
   sp.nh16 = pad16(nh);
   sp.nh64 = pad64(nh);
-  sp.bka = nh >= 64 ? 64 : pad16(nh);
+  sp.bka = nh >= 32 ? 32 : pad16(nh);
   sp.bks = N <= 85 ? 32 : 64;
   sp.nha = (nh + sp.bka - 1) / sp.bka * sp.bka;
   sp.syn_split = 4 * sp.nh16 > 512 ? 2 : 1;
