@@ -169,6 +169,34 @@ def _cpu_member_steps(args):
     return T, (time.perf_counter() - t0) / steps
 
 
+def cpu_single_rate(config: str, budget_s: float = 2.0) -> dict:
+    """1-core sim-days/s of the reference algorithm (the oracle port, one thread, in this process) on a bounded
+    sample of a single-run configuration: RK4 steps of the same seeded initial state, timed until `budget_s`."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import OraclePlane, OracleSphere
+
+    if config == "plane":
+        o = OraclePlane(1024, 512, 1024 * 5000.0, 512 * 5000.0, f0=1e-4, beta=1.6e-11, gravity=9.81, depth=100.0)
+        h, u = o.jet_grids(20.0, 1.0e5, 0.1, 1)
+        o.set(h, u, np.zeros((513, 1024)))
+        dt = 60.0
+    else:
+        T, dt = (42, 900.0) if config == "t42" else (170, 240.0)
+        o = OracleSphere(T, diffusion=nu4(T))
+        h, u, v = o.turbulence_grids(1, 8000.0, 30.0, T // 2)
+        o.set_state_grid(h, u, v)
+    o.step(dt)
+    n, t0 = 0, time.perf_counter()
+    while n < 2 or time.perf_counter() - t0 < budget_s:
+        o.step(dt)
+        n += 1
+    el = time.perf_counter() - t0
+    return {"value": n * dt / 86400.0 / el, "unit": "sim-days/s", "cores": 1, "kind": "port",
+            "sample": f"{n} RK4 steps of {dt:g} s of the same seeded initial state, oracle port, one thread ({el:.1f} s)"}
+
+
 def cpu_ensemble_rate(group_steps: dict, sample_steps: dict, cores: int):
     """Member-sim-days/s of the reference algorithm on `cores` host cores: every core times member-steps of each
     truncation at once (a bounded sample), and the workload's member-step counts are divided over the cores."""
@@ -468,7 +496,8 @@ def other_workloads(lw, lib, args, ens):
         s.run(480 * 900.0, 900.0)
         ts.append(time.perf_counter() - t0)
     out.append({"config": "0: sphere T42 plain FP64, 480 x 900 s", "value": 5.0 / min(ts), "unit": "sim-days/s",
-                "parity": "within 1e-12 norm-relative of the reference's own run (tests/test_sphere_gpu.py)"})
+                "parity": "within 1e-12 norm-relative of the reference's own run (tests/test_sphere_gpu.py)",
+                "cpu_1core": cpu_single_rate("t42")})
     s.close()
     # config 1: beta-plane 1024 x 512, dt 60 s
     p = lw.Plane(1024, 512, 1024 * 5000.0, 512 * 5000.0, f0=1e-4, beta=1.6e-11, gravity=9.81, depth=100.0)
@@ -478,13 +507,13 @@ def other_workloads(lw, lib, args, ens):
     p.run(1024 * 60.0, 60.0)
     el = time.perf_counter() - t0
     out.append({"config": "1: beta-plane 1024 x 512 C-grid FP64, dt 60 s", "value": 1024 * 60.0 / 86400.0 / el, "unit": "sim-days/s",
-                "parity": "bitwise identical to the reference (tests/test_plane_gpu.py)"})
+                "parity": "bitwise identical to the reference (tests/test_plane_gpu.py)", "cpu_1core": cpu_single_rate("plane")})
     p.close()
     # config 2: T170 precision study, 2 model days
     from lmweather_gb300.precision import study
 
     res = study(170, 2.0)
-    out.append({"config": "2: sphere T170 precision study, 2 model days at 240 s", **res})
+    out.append({"config": "2: sphere T170 precision study, 2 model days at 240 s", **res, "cpu_1core_fp64": cpu_single_rate("t170", 3.0)})
     res = study(341, 2.0)
     out.append({"config": "2: sphere T341 precision study, 2 model days at 150 s", **res})
     # config 4: the learned surrogate at T42 (bounded: see surrogate_workload)
