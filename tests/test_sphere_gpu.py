@@ -312,8 +312,9 @@ def test_determinism_known_answers(engine):
 @pytest.mark.parametrize("T,members,terms", [(21, 24, 3), (42, 16, 6), (85, 16, 3)])
 def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
     """Every launch plan the autotuner may pick (latitude pairs per grid CTA, FFT stages per shared-memory pass,
-    pipeline depths, one or both parities per analysis CTA, and the grid -> analysis interface) gives the same
-    state bit for bit: the plans move the same operations between CTAs and passes, never reorder them."""
+    pipeline depths, one or both parities per analysis CTA, and the grid -> analysis interface), and analysis CTAs
+    that loop over several work items, give the same state bit for bit: the plans move the same operations between
+    CTAs and passes, never reorder them."""
     nu = 6.37122e6 ** 4 / (86400.0 * (T * (T + 1)) ** 2)
     s = engine.Sphere(T, diffusion=nu, precision=engine.SPLIT_BF16, members=members, split_terms=terms)
     for b in range(members):
@@ -332,6 +333,9 @@ def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
             plans.append(dict(analysis_both_parities=both, grid_writes_operands=direct, analysis_stages=2, synthesis_stages=3))
     plans.append(dict(analysis_stages=1, synthesis_stages=1))
     plans.append(dict(analysis_stages=1, analysis_both_parities=0, analysis_ctas_per_sm=3))
+    # fewer analysis CTAs than work items: each CTA loops over items (m fastest), its barriers' phases continuing
+    for both in (0, 1):
+        plans.append(dict(analysis_ctas=37, analysis_both_parities=both, analysis_stages=2))
     if s.nlat // 2 >= 32:
         plans.append(dict(synthesis_latitude_slices=2, synthesis_stages=2))
     tuned = s.split_plan()
