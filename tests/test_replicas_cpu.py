@@ -62,3 +62,14 @@ def test_reference_arm_runs_on_rank_zero_only():
 
     args = argparse.Namespace(steps=1, warmup=0)
     assert bench.run_reference(args, rank=1, world=2) == 0
+
+
+@pytest.mark.parametrize("config", ["t42", "plane"])
+def test_single_config_cpu_timing(config):
+    """The 1-core CPU figure beside configs 0 and 1: the oracle port stepping the seeded state, a bounded sample."""
+    import bench
+
+    bench.build_oracle()
+    r = bench.cpu_single_rate(config, budget_s=0.05)
+    assert r["cores"] == 1 and r["kind"] == "port" and r["unit"] == "sim-days/s"
+    assert r["value"] > 0 and "RK4 steps" in r["sample"]
