@@ -816,9 +816,10 @@ static void allow_max_shared_memory() {
                   split_ana<false, false, 3>, split_ana<true, false, 3>, split_ana<false, true, 3>, split_ana<true, true, 3>,
                   split_ana<false, false, 4>, split_ana<true, false, 4>, split_ana<false, true, 4>, split_ana<true, true, 4>})
     LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  for (auto *k : {split_grid<false, 3, 3>, split_grid<true, 3, 3>, split_grid<false, 4, 2>, split_grid<true, 4, 2>,
-                  split_grid<false, 4, 3>, split_grid<true, 4, 3>})
-    LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_grid<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   done_for_device = dev;
 }
 
@@ -1334,12 +1335,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   if (which < 0 || which == 1) {
     const dim3 grid(d.nh / sp.jb, B);
     const size_t bytes = 5 * static_cast<size_t>(sp.jb) * fft_row<3>(d.nlon) * sizeof(float2);
-    // four-stage groups: the 80-register form where three CTAs' rows fit in shared memory (it measured faster there),
-    // else the spill-free 128-register form
-    const bool three = 3 * (bytes + 2048) <= 233472;
-    auto *k = sp.fgrp < 4 ? (sp.direct ? split_grid<true, 3, 3> : split_grid<false, 3, 3>)
-              : three     ? (sp.direct ? split_grid<true, 4, 3> : split_grid<false, 4, 3>)
-                          : (sp.direct ? split_grid<true, 4, 2> : split_grid<false, 4, 2>);
+    auto *k = sp.fgrp >= 4 ? (sp.direct ? split_grid<true, 4> : split_grid<false, 4>) : (sp.direct ? split_grid<true, 3> : split_grid<false, 3>);
     k<<<grid, GRID_THREADS, bytes, stream>>>(d, t, sd, fgrid, hsgrid);
   }
   if (which < 0 || which == 2) {

@@ -364,11 +364,9 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
 // as the analysis operands (BF16 pieces in the chunk layout, jb consecutive latitudes per store), which the
 // analysis streams with bulk copies; otherwise written m-major as FP32 fold[m][slot][parity][member][jh] (jb
 // latitudes per store), which the analysis gathers (cheaper for a few members, where jb is small)
-// FMAX: the largest FFT stage group the instantiation takes (4: sixteen elements per thread). MINB: CTAs per SM
-// the register budget allows (2: up to 128 registers a thread, spill-free for four-stage groups; 3: up to 80, taken
-// where three CTAs' FFT rows fit in shared memory, at the cost of a few spilled values)
-template <bool DIRECT, int FMAX, int MINB>
-__global__ void __launch_bounds__(GRID_THREADS, MINB) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
+// FMAX: the largest FFT stage group the instantiation takes (4: sixteen elements per thread, two CTAs per SM)
+template <bool DIRECT, int FMAX>
+__global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
                                                            const double *__restrict__ hsgrid) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float2 *sm = reinterpret_cast<float2 *>(smraw);  // rows f * jb + p: U, V, zeta, Phi and the fifth product of pair p
