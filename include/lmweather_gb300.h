@@ -274,7 +274,7 @@ int lmw_ensemble_stream(lmw_ensemble *e, int group, void **stream);
  * when an analysis CTA handles both parities of m, out[5] the analysis CTA count (0: one per work item; else
  * persistent CTAs), out[6] 1 when the grid kernel writes the analysis operands (else the analysis gathers them
  * from an FP32 fold), out[7] the analysis kernel's register budget in CTAs per SM (2: 128 registers a thread, 3:
- * 80, 4: 64), out[8] the synthesis's latitude slices per (m, member tile) (1, 2 or 4) (zeros when the engine is not in
+ * 80), out[8] the synthesis's latitude slices per (m, member tile) (1, 2 or 4) (zeros when the engine is not in
  * split precision; out has 9 entries). No reference counterpart. */
 int lmw_sphere_split_plan(lmw_sphere *s, int *out);
 /* replaces the autotuned plan with `plan` (the 9 entries above), checked against the limits the autotuner's

@@ -813,8 +813,7 @@ static void allow_max_shared_memory() {
   LMW_CUDA(cudaFuncSetAttribute(sph_grid_in, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_syn, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   for (auto *k : {split_ana<false, false, 2>, split_ana<true, false, 2>, split_ana<false, true, 2>, split_ana<true, true, 2>,
-                  split_ana<false, false, 3>, split_ana<true, false, 3>, split_ana<false, true, 3>, split_ana<true, true, 3>,
-                  split_ana<false, false, 4>, split_ana<true, false, 4>, split_ana<false, true, 4>, split_ana<true, true, 4>})
+                  split_ana<false, false, 3>, split_ana<true, false, 3>, split_ana<false, true, 3>, split_ana<true, true, 3>})
     LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_grid<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
@@ -1342,10 +1341,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
     if (sp.ana_both && 2 * sp.ra_pair > 512) throw InvalidArgument("split precision: both parities' accumulators exceed tensor memory");
     const int items = d.M * (sp.ana_both ? 1 : 2) * sp.ntiles;
     const int grid = sp.ana_grid > 0 ? std::min(items, sp.ana_grid) : items;
-    auto *k = sp.ana_minb >= 4
-                  ? (sp.ana_both ? (sp.direct ? split_ana<true, true, 4> : split_ana<true, false, 4>)
-                                 : (sp.direct ? split_ana<false, true, 4> : split_ana<false, false, 4>))
-              : sp.ana_minb == 3
+    auto *k = sp.ana_minb >= 3
                   ? (sp.ana_both ? (sp.direct ? split_ana<true, true, 3> : split_ana<true, false, 3>)
                                  : (sp.direct ? split_ana<false, true, 3> : split_ana<false, false, 3>))
                   : (sp.ana_both ? (sp.direct ? split_ana<true, true, 2> : split_ana<true, false, 2>)
@@ -1653,10 +1649,8 @@ void SphereEngine::autotune_split() {
         if (ba > sp.budget_bytes) continue;
         // one CTA per work item (persistent CTAs, ana_grid > 0, measured no faster on GB300 and are not tried)
         cands.push_back({2, both, 0, ns, dir, ba, 1e30, 2});
-        // the 80- and 64-register forms only pay where three or four CTAs fit in shared memory (and four in the
-        // 512 tensor-memory columns)
+        // the 80-register form only pays where three CTAs fit in shared memory
         if (3 * (ba + 1024) <= 233472) cands.push_back({2, both, 0, ns, dir, ba, 1e30, 3});
-        if (4 * (ba + 1024) <= 233472 && 4 * ana_tmem_cols(sp, both) <= 512) cands.push_back({2, both, 0, ns, dir, ba, 1e30, 4});
       }
   }
   const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both, ag0 = sp.ana_grid, dir0 = sp.direct,
@@ -1767,8 +1761,7 @@ void SphereEngine::set_split_plan(const int *in) {
   const size_t bs = std::max(nss * static_cast<size_t>(sp.pieces) * (sp.rSP + sp.nh16 / sl) * sp.bks * 2 + SPLIT_MARGIN, sp.syn_min_bytes);
   const size_t ba = std::max(sp.ana_res_bytes_v[dir] + nsa * sp.ana_stage_bytes_v[dir] + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
   if (bs > sp.budget_bytes || ba > sp.budget_bytes) throw InvalidArgument("split plan: the pipelines do not fit in shared memory");
-  if (mb < 2 || mb > 4) throw InvalidArgument("split plan: the analysis register budget must be 2, 3 or 4 CTAs per SM");
-  if (mb == 4 && 4 * ana_tmem_cols(sp, both) > 512) throw InvalidArgument("split plan: four analysis CTAs per SM exceed tensor memory");
+  if (mb != 2 && mb != 3) throw InvalidArgument("split plan: the analysis register budget must be 2 or 3 CTAs per SM");
   LMW_CUDA(cudaStreamSynchronize(stream));
   sp.jb = jb;
   sp.fgrp = fg;

@@ -65,7 +65,7 @@ struct SplitPlan {
   int direct = 1;             // the grid kernel writes the analysis operands (else the FP32 fold, gathered)
   int ana_both = 0;           // analysis CTAs handle both parities of m
   int ana_grid = 0;           // analysis CTAs (0: one per work item)
-  int ana_minb = 2;           // analysis register budget: CTAs per SM (2, 3 or 4)
+  int ana_minb = 2;           // analysis register budget: CTAs per SM (2 or 3)
   int ra_pair = 32;           // largest ra16[2m] + ra16[2m + 1]
   size_t syn_stage_bytes = 0, syn_min_bytes = 0, ana_min_bytes = 0, ana_both_min_bytes = 0, budget_bytes = 0;
   size_t ana_res_bytes_v[2] = {0, 0}, ana_stage_bytes_v[2] = {0, 0};  // per variant: [0] gathered A, [1] streamed A
@@ -569,8 +569,8 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict
 // parities in one CTA one after the other (the GEMM pipeline's barriers continue their phases), so the epilogue
 // walks every n of m in order and the FP64 state is read and written with unit stride. Accumulator columns of
 // parity s: H at [cb_s, cb_s + ra_s), P at [cb_s + ra_s, cb_s + 2 ra_s), cb_0 = 0, cb_1 = 2 ra_0 (BOTH).
-// MINB: CTAs per SM the register budget allows (2: up to 128 registers a thread; 3: up to 80, 4: up to 64, for
-// plans whose shared memory admits three or four CTAs per SM)
+// MINB: CTAs per SM the register budget allows (2: up to 128 registers a thread; 3: up to 80, for plans whose
+// shared memory admits three CTAs per SM)
 template <bool BOTH, bool DIRECT, int MINB>
 __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
                                                              int B, int ns, double2 *__restrict__ x0, double2 *__restrict__ xs,
@@ -793,14 +793,6 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
 }
 
 }  // namespace
-
-// tensor-memory columns one analysis CTA allocates (the power of two that holds its accumulators)
-inline int ana_tmem_cols(const SplitPlan &sp, int both) {
-  const int need = both ? 2 * sp.ra_pair : 2 * sp.ra_max;
-  int c = 32;
-  while (c < need) c <<= 1;
-  return c;
-}
 
 // Pack the tables, size the operand buffers (once per engine).
 inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int terms) {

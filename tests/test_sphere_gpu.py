@@ -333,7 +333,6 @@ def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
             plans.append(dict(analysis_both_parities=both, grid_writes_operands=direct, analysis_stages=2, synthesis_stages=3))
     plans.append(dict(analysis_stages=1, synthesis_stages=1))
     plans.append(dict(analysis_stages=1, analysis_both_parities=0, analysis_ctas_per_sm=3))
-    plans.append(dict(analysis_stages=1, analysis_both_parities=0, analysis_ctas_per_sm=4))
     # fewer analysis CTAs than work items: each CTA loops over items (m fastest), its barriers' phases continuing
     for both in (0, 1):
         plans.append(dict(analysis_ctas=37, analysis_both_parities=both, analysis_stages=2))
