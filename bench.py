@@ -18,7 +18,8 @@ FP32 accumulation, FP32 FFTs and products, FP64 state). Inputs are synthetic and
                 scaled to the workload's member-step counts
   workloads     the other configurations: T42 plain FP64 (config 0), the 1024 x 512 beta-plane (config 1), the
                 T170 and T341 precision studies (config 2), the learned surrogate (config 4, bounded training) and
-                the ensemble in the other precisions
+                the ensemble in the other precisions; configs 0, 1 and the T170 study carry the oracle timed on one
+                host core beside them (cpu_1core, a bounded sample of RK4 steps of the same seeded state)
 
 `--impl reference` times the reference's CPU algorithm (the oracle port: the reference checkout is absent on the
 GPU host) on the same workload with all host cores and prints the same line with "impl": "reference".
