@@ -154,20 +154,79 @@ def peaks() -> dict:
 
 
 # ----------------------------------------------------------------------------------------------- CPU side (oracle)
-def _cpu_member_steps(args):
-    """One worker: seconds per RK4 step of one member at truncation T (oracle port, one thread)."""
-    T, steps, dt = args
+# The CPU measurement runs whole RK4 member-steps of the workload on every host core for a measured interval:
+# each core holds one member of each truncation (its own seeded state, the workload's steps) and runs member-steps
+# in the workload's proportions of member-steps per truncation (T21 512 x 179, T42 384 x 327, T85 128 x 616 at
+# the stable steps of the 2-day runs), always the truncation furthest behind its share, so a sample's member-days
+# per second estimate the whole workload's. The value is the member-days the cores actually simulated over the
+# measured wall time.
+_CPU_STATE = {}
+
+
+def _cpu_init(specs):
+    """Pool initialiser: one oracle sphere per truncation from a seeded balanced-turbulence state (the cost of a
+    member-step does not depend on the member's mean height or rotation rate)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import OracleSphere
 
-    o = OracleSphere(T, diffusion=nu4(T))
-    h, u, v = o.turbulence_grids(7, 8000.0, 30.0, T // 2)
-    o.set_state_grid(h, u, v)
-    o.step(dt)
+    for T, dt, seed, hbar, om in specs:
+        o = OracleSphere(T, omega=om, diffusion=nu4(T))
+        h, u, v = o.turbulence_grids(seed, hbar, 30.0, T // 2)
+        o.set_state_grid(h, u, v)
+        _CPU_STATE[T] = (o, dt)
+    _CPU_STATE["done"] = {T: 0 for T, *_ in specs}
+
+
+def _cpu_run_for(args):
+    """Run member-steps for `seconds` of wall time; returns (member-steps per truncation, member-days, elapsed)."""
+    seconds, shares = args
+    done = _CPU_STATE["done"]
+    steps = {T: 0 for T in shares}
+    days = 0.0
     t0 = time.perf_counter()
-    for _ in range(steps):
+    while True:
+        total = sum(done.values()) + 1
+        T = max(shares, key=lambda k: shares[k] * total - done[k])
+        o, dt = _CPU_STATE[T]
         o.step(dt)
-    return T, (time.perf_counter() - t0) / steps
+        done[T] += 1
+        steps[T] += 1
+        days += dt / 86400.0
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            return steps, days, el
+
+
+class CpuEnsemble:
+    """The reference's algorithm (the oracle port) on `cores` host cores, one process per core (spawn)."""
+
+    def __init__(self, group_steps: dict, dts: dict, cores: int):
+        total = sum(group_steps.values())
+        self.shares = {T: n / total for T, n in group_steps.items()}
+        self.cores = cores
+        ctx = mp.get_context("spawn")
+        specs = [(T, dts[T], 7 + T, 8000.0, OMEGA) for T in sorted(group_steps)]
+        self.pool = ctx.Pool(cores, initializer=_cpu_init, initargs=(specs,))
+        self.pool.map(_cpu_run_for, [(0.05, self.shares)] * cores)  # every worker built its tables and states
+
+    def run(self, seconds: float) -> dict:
+        """All cores run member-steps for `seconds`; member-days simulated over the wall time of the whole pass."""
+        t0 = time.perf_counter()
+        res = self.pool.map(_cpu_run_for, [(seconds, self.shares)] * self.cores)
+        wall = time.perf_counter() - t0
+        steps = {T: sum(r[0][T] for r in res) for T in self.shares}
+        days = sum(r[1] for r in res)
+        return {"value": days / wall, "member_days": days, "wall_s": wall, "member_steps": steps}
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+# the 2-day workload's member-step counts and stable steps (the reference's stable_dt(1.5), smallest over the group,
+# of the seeded initial states: the same steps the GPU run takes)
+GROUP_STEPS = {21: 512 * 179, 42: 384 * 327, 85: 128 * 616}
+GROUP_DT = {21: 965.4, 42: 528.4, 85: 280.5}
 
 
 def cpu_single_rate(config: str, budget_s: float = 2.0) -> dict:
@@ -198,28 +257,6 @@ def cpu_single_rate(config: str, budget_s: float = 2.0) -> dict:
             "sample": f"{n} RK4 steps of {dt:g} s of the same seeded initial state, oracle port, one thread ({el:.1f} s)"}
 
 
-def cpu_ensemble_rate(group_steps: dict, sample_steps: dict, cores: int):
-    """Member-sim-days/s of the reference algorithm on `cores` host cores: every core times member-steps of each
-    truncation at once (a bounded sample), and the workload's member-step counts are divided over the cores."""
-    ctx = mp.get_context("spawn")
-    jobs = []
-    for c in range(cores):
-        for T, (n, dt) in sample_steps.items():
-            jobs.append((T, n, dt))
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_member_steps, jobs)
-    wall = time.perf_counter() - t0
-    per = {}
-    for T, sec in res:
-        per.setdefault(T, []).append(sec)
-    cost = {T: statistics.median(v) for T, v in per.items()}
-    cpu_seconds = sum(group_steps[T] * cost[T] for T in group_steps)  # one core
-    member_days = 1024 * DAYS
-    rate = member_days / (cpu_seconds / cores)
-    return rate, cost, wall
-
-
 def build_oracle():
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import build_oracle as bo
@@ -227,38 +264,34 @@ def build_oracle():
     bo(with_ref=False)
 
 
-GROUP_STEPS_NOMINAL = None
-
-
 def ensemble_member_steps(groups):
     return {g["truncation"]: g["members"] * g["steps"] for g in groups}
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU algorithm on every host core (the reference checkout is absent on the GPU host, so the oracle
+    port, bitwise equal to it, runs): each bench step is a timed pass of whole member-steps of the workload."""
     if rank != 0:
         return 0
     build_oracle()
     cores = os.cpu_count() or 1
-    # member-step counts of the 2-day workload: members x steps at each group's stable step (the reference's
-    # stable_dt(1.5), smallest over the group, of the seeded initial states: T21 965.4 s, T42 528.4 s, T85 280.5 s,
-    # the same steps the GPU run takes)
-    steps = {21: 512 * 179, 42: 384 * 327, 85: 128 * 616}
-    sample = {21: (6, 965.4), 42: (3, 528.4), 85: (1, 280.5)}
+    cpu = CpuEnsemble(GROUP_STEPS, GROUP_DT, cores)
     for _ in range(args.warmup):
-        cpu_ensemble_rate(steps, {21: (1, 965.4), 42: (1, 528.4), 85: (1, 280.5)}, cores)
-    vals, costs = [], None
-    for _ in range(args.steps):
-        v, costs, _ = cpu_ensemble_rate(steps, sample, cores)
-        vals.append(v)
-    value = statistics.median(vals)
-    ms = 1024 * DAYS / value * 1e3
-    smp = (f"per bench step every one of {cores} cores times 6 T21, 3 T42 and 1 T85 member-steps (oracle port, one thread each); "
-           f"the 2-day workload's member-step counts (T21 {steps[21]}, T42 {steps[42]}, T85 {steps[85]}) are divided over the cores")
+        cpu.run(1.0)
+    runs = [cpu.run(args.ref_seconds) for _ in range(args.steps)]
+    cpu.close()
+    days = sum(r["member_days"] for r in runs)
+    wall = sum(r["wall_s"] for r in runs)
+    value = days / wall
+    steps = {T: sum(r["member_steps"][T] for r in runs) for T in GROUP_STEPS}
+    smp = (f"{args.steps} timed passes of {args.ref_seconds:g} s on {cores} cores (oracle port, one process per core): "
+           f"{steps[21]} T21, {steps[42]} T42 and {steps[85]} T85 member-steps executed ({days:.3f} member-days in {wall:.1f} s), "
+           "in the 2-day workload's proportions of member-steps per truncation")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "member-sim-days/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded balanced turbulence)", "config": WORKLOAD,
+            "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded balanced turbulence)", "config": WORKLOAD,
             "cpu_baseline": {"value": value, "unit": "member-sim-days/s", "cores": cores, "kind": "port", "sample": smp,
-                             "member_step_seconds": {str(k): v for k, v in (costs or {}).items()}},
+                             "member_steps": {str(k): v for k, v in steps.items()}},
             "e2e": {"value": value, "unit": "member-sim-days/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -271,8 +304,11 @@ def run_ours(args, rank, world, local):
     import numpy as np
     import torch
 
+    cpu_pool = None
     if rank == 0 and world == 1:
-        build_oracle()  # before any CUDA work (the CPU baseline's worker pool starts by spawn)
+        build_oracle()
+        # the CPU baseline's worker pool starts (by spawn) before any CUDA work
+        cpu_pool = CpuEnsemble(GROUP_STEPS, GROUP_DT, os.cpu_count() or 1)
     torch.cuda.set_device(local)
     from lmweather_gb300 import build as b
 
@@ -445,17 +481,16 @@ def run_ours(args, rank, world, local):
     if rank == 0:
         workloads = other_workloads(lw, lib, args, ens)
 
-    # --- CPU baseline (rank 0, N = 1): the oracle on every host core
+    # --- CPU baseline (rank 0, N = 1): the oracle on every host core, a timed pass of whole member-steps
     cpu = None
-    if rank == 0 and world == 1:
-        cores = os.cpu_count() or 1
-        steps = ensemble_member_steps(groups)
-        dts = {g["truncation"]: g["dt"] for g in groups}
-        rate, cost, wall = cpu_ensemble_rate(steps, {21: (6, dts[21]), 42: (3, dts[42]), 85: (1, dts[85])}, cores)
-        cpu = {"value": rate, "unit": "member-sim-days/s", "cores": cores, "kind": "port",
-               "sample": f"every one of {cores} cores timed 6 T21, 3 T42 and 1 T85 member-steps of the oracle ({wall:.1f} s); the "
-                         f"workload's member-step counts {steps} divided over the cores",
-               "member_step_seconds": {str(k): v for k, v in cost.items()}}
+    if cpu_pool is not None:
+        r = cpu_pool.run(args.ref_seconds)
+        cpu_pool.close()
+        cpu = {"value": r["value"], "unit": "member-sim-days/s", "cores": cpu_pool.cores, "kind": "port",
+               "sample": f"one timed pass of {r['wall_s']:.1f} s on {cpu_pool.cores} cores (oracle port, one process per core): "
+                         f"{r['member_steps'][21]} T21, {r['member_steps'][42]} T42 and {r['member_steps'][85]} T85 member-steps executed "
+                         f"({r['member_days']:.3f} member-days), in the workload's proportions of member-steps per truncation",
+               "member_steps": {str(k): v for k, v in r["member_steps"].items()}}
 
     clocks = clk.summary()
     if rank == 0:
@@ -511,11 +546,9 @@ def other_workloads(lw, lib, args, ens):
                 "parity": "bitwise identical to the reference (tests/test_plane_gpu.py)", "cpu_1core": cpu_single_rate("plane")})
     p.close()
     # config 2: T170 precision study, 2 model days
-    from lmweather_gb300.precision import study
-
-    res = study(170, 2.0)
+    res = precision_study(170, 2.0)
     out.append({"config": "2: sphere T170 precision study, 2 model days at 240 s", **res, "cpu_1core_fp64": cpu_single_rate("t170", 3.0)})
-    res = study(341, 2.0)
+    res = precision_study(341, 2.0, modes=("fp64", "fp32", "split3", "split6"))
     out.append({"config": "2: sphere T341 precision study, 2 model days at 150 s", **res})
     # config 4: the learned surrogate at T42 (bounded: see surrogate_workload)
     out.append(surrogate_workload(lw))
@@ -539,15 +572,15 @@ def surrogate_workload(lw, trajectories=1024, windows=80, epochs=60, members=102
     """Config 4 within the benchmark's time: the T42 residual MLP (5676 -> 4096 x 3 -> 5676, GELU, BF16 on tcgen05)
     trained on `trajectories` x `windows` solver pairs (split-precision RK4 data, FP64 state; 6-hour windows of
     900 s steps, mean height 8000 m), then a hybrid rollout of `members` held-out members over `rollout_windows`
-    windows with FP64 RK4 checking every 4th window and taking over above 1e-3. The full configuration (204,800
-    pairs, 100 epochs, 80 rollout windows) is python -m lmweather_gb300.surrogate_study."""
+    windows with split-precision RK4 checking every 4th window and FP64 RK4 taking over above 1e-3. The full
+    configuration (204,800 pairs, 100 epochs, 80 rollout windows) is python bench.py --study surrogate."""
     t0 = time.perf_counter()
     sur = lw.Surrogate(42, hidden=4096, seed=1)
     gen_s = sur.generate(trajectories, windows, seed0=1_000_000, hmin=8000.0, hmax=8000.0, precision=lw.SPLIT_BF16)
     fit = sur.fit(epochs, batch=512, lr=3e-4, lr_min=3e-5, val_fraction=0.1, seed=1, loss="energy")
     train_ms, fwd_ms = sur.time(512, 10)
     _, fwd1024 = sur.time(1024, 10)
-    r = sur.rollout(members, seed0=9_000_001, windows=rollout_windows, check_every=4, threshold=1e-3, check_precision=lw.FP64,
+    r = sur.rollout(members, seed0=9_000_001, windows=rollout_windows, check_every=4, threshold=1e-3, check_precision=lw.SPLIT_BF16,
                     ref_windows=4, hmin=8000.0, hmax=8000.0)
     sur.close()
     fl = 2 * (5676 * 4096 * 2 + 4096 * 4096 * 2)
@@ -565,6 +598,168 @@ def surrogate_workload(lw, trajectories=1024, windows=80, epochs=60, members=102
             "forward_tflops_batch1024": fl * 1024 / (fwd1024 * 1e-3) / 1e12, "wall_s": time.perf_counter() - t0}
 
 
+# ----------------------------------------------------------------------------------------------- studies and cases
+# Step sizes inside the reference's RK4 limit for an 8000 m layer over two days (a 450 s step at T170 exceeds the
+# reference's own limit of 316 s for this state, and at 300 s the limit falls below the step on day 2).
+STUDY_STEP = {42: 900.0, 85: 450.0, 170: 240.0, 341: 150.0}
+
+
+def weighted_l2(a, b, w):
+    import numpy as np
+
+    wt = w[:, None]
+    return float(np.sqrt((wt * (a - b) ** 2).sum() / (wt * b ** 2).sum()))
+
+
+def precision_study(T: int, days: float, seed: int = 1, modes=("fp64", "fp32", "split3", "split6", "split3_plain", "split6_plain")) -> dict:
+    """The same seeded state run in FP64, FP32 and split-BF16 (3 and 6 products per term; the default form keeps the
+    linear terms of the tendencies in FP64, the "_plain" form sends every term through the BF16 products) for `days`;
+    errors against the FP64 run (relative L2 of the height, area-weighted with the Gauss weights; L-infinity;
+    relative drift of energy and potential enstrophy) and speeds."""
+    import lmweather_gb300 as lw
+    import numpy as np
+
+    dt = STUDY_STEP.get(T, 300.0 * 170 / T)
+    cfg = {"fp64": dict(precision=lw.FP64), "fp32": dict(precision=lw.FP32),
+           "split3": dict(precision=lw.SPLIT_BF16, split_terms=3), "split6": dict(precision=lw.SPLIT_BF16, split_terms=6),
+           "split3_plain": dict(precision=lw.SPLIT_BF16, split_terms=3), "split6_plain": dict(precision=lw.SPLIT_BF16, split_terms=6)}
+    seconds = days * 86400.0
+    out = {"truncation": T, "dt_s": dt, "days": days, "steps": int(round(seconds / dt)), "runs": {}}
+    ref = None
+    for name in modes:
+        s = lw.Sphere(T, diffusion=nu4(T), max_truncation=max(T, 170), **cfg[name])
+        if name.endswith("_plain"):
+            s.set_split_form(False)
+        s.turbulence(seed, 8000.0, 30.0, T // 2)
+        mu, w = s.gauss()
+        st = s.get_state()
+        s.run(64 * dt, dt)  # warm the graphs; the studied span starts from the same state after it
+        s.set_state(*st)
+        t0 = time.perf_counter()
+        s.run(seconds, dt)
+        el = time.perf_counter() - t0
+        h = s.grid_height()
+        d = s.diagnostics()
+        rec = {"seconds": el, "sim_days_per_s": days / el, "ms_per_step": el / (seconds / dt) * 1e3}
+        if ref is None:
+            ref = (h, d)
+        else:
+            hr, dr = ref
+            rec.update(height_l2=weighted_l2(h, hr, w), height_linf=float(np.abs(h - hr).max() / np.abs(hr).max()),
+                       energy_drift=abs(d["energy"] - dr["energy"]) / abs(dr["energy"]),
+                       enstrophy_drift=abs(d["enstrophy"] - dr["enstrophy"]) / abs(dr["enstrophy"]))
+            rec["speedup_vs_fp64"] = out["runs"]["fp64"]["seconds"] / el
+        out["runs"][name] = rec
+        s.close()
+    return out
+
+
+def run_case(args) -> int:
+    """One named workload for a fixed number of RK4 steps (the command that profiler captures wrap): t42 (config-0
+    sphere), t85, t170, t341, plane (1024 x 512 beta-plane jet, dt 60 s), ens (an ensemble of --members spheres at
+    --truncation, the groups of the benchmark ensemble; --plan forces split plan entries, e.g.
+    analysis_stages=1,analysis_ctas_per_sm=3), mlp (training steps of the surrogate's network). One untimed warm-up
+    step runs first."""
+    import lmweather_gb300 as lw
+    from lmweather_gb300 import build
+
+    build.build()
+    if args.case == "plane":
+        p = lw.Plane(1024, 512, 1024 * 5000.0, 512 * 5000.0, f0=1e-4, beta=1.6e-11, gravity=9.81, depth=100.0)
+        p.jet(20.0, 1.0e5, 0.1, 1)
+        p.step(60.0)
+        t0 = time.perf_counter()
+        for _ in range(args.case_steps):
+            p.step(60.0)
+        print(f"plane 1024x512: {args.case_steps} steps in {time.perf_counter() - t0:.4f} s")
+        return 0
+    if args.case == "mlp":
+        import numpy as np
+
+        rng = np.random.default_rng(1)
+        net = lw.Mlp(5676, 4096, 5676, max_batch=args.batch, seed=1, last_layer_scale=0.1)
+        x = rng.standard_normal((args.batch, 5676)).astype(np.float32)
+        t = 0.1 * rng.standard_normal((args.batch, 5676)).astype(np.float32)
+        net.backward(x, t)
+        t0 = time.perf_counter()
+        for _ in range(args.case_steps):
+            net.backward(x, t)
+            net.adam(1e-4)
+        print(f"mlp 5676-4096x3-5676 batch {args.batch}: {args.case_steps} training steps in {time.perf_counter() - t0:.4f} s")
+        return 0
+    prec = {"fp64": lw.FP64, "fp32": lw.FP32, "split3": lw.SPLIT_BF16, "split6": lw.SPLIT_BF16}[args.precision]
+    terms = 6 if args.precision == "split6" else 3
+    if args.case == "ens":
+        T, B = args.truncation, args.members
+        s = lw.Sphere(T, diffusion=nu4(T), precision=prec, members=B, split_terms=terms)
+        for b in range(B):
+            s.turbulence(b + 1, 5000.0 + 5000.0 * b / B, 30.0, T // 2, member=b)
+        if args.plan:
+            s.set_split_plan(**{k: int(v) for k, v in (kv.split("=") for kv in args.plan.split(","))})
+        if prec == lw.SPLIT_BF16:
+            print("plan", s.split_plan())
+        dt = 0.9 * min(s.stable_dt(1.5, member=b) for b in range(B))
+        s.step(dt)
+        t0 = time.perf_counter()
+        for _ in range(args.case_steps):
+            s.step(dt)
+        print(f"ensemble T{T} x {B}: {args.case_steps} steps in {time.perf_counter() - t0:.4f} s")
+        return 0
+    T = {"t42": 42, "t85": 85, "t170": 170, "t341": 341}[args.case]
+    dt = STUDY_STEP[T]
+    s = lw.Sphere(T, diffusion=nu4(T), precision=prec, max_truncation=max(T, 170), split_terms=terms)
+    s.turbulence(1, 8000.0, 30.0, T // 2)
+    s.step(dt)
+    t0 = time.perf_counter()
+    for _ in range(args.case_steps):
+        s.step(dt)
+    print(f"sphere T{T}: {args.case_steps} steps in {time.perf_counter() - t0:.4f} s")
+    return 0
+
+
+def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, epochs=100, batch=512, lr=3e-4, lr_min=3e-5,
+                    hmin=8000.0, hmax=8000.0, members=1024, rollout_windows=80, check_every=4, threshold=1e-3, ref_windows=4, seed=1,
+                    check_precision=None, loss="energy", thresholds=(), clip=2.0, data_precision=0) -> dict:
+    """The learned surrogate end to end: solver trajectories (balanced turbulence on training seeds, RK4 at 900 s,
+    del^4 with a 1-day e-folding at n = T; pairs (state, state + 6 h) from every window; the last tenth of the
+    trajectories held out) -> training on the GPU -> validation errors per 6-hour window -> a hybrid rollout of
+    held-out members in which RK4 checks every `check_every`-th window and takes members over, timed against plain
+    FP64 RK4 on the same members. Errors: relative L2 of the height grid over one window (area-weighted, from the
+    Phi coefficients) against RK4 from the same start state."""
+    import lmweather_gb300 as lw
+
+    if check_precision is None:
+        check_precision = lw.SPLIT_BF16
+    sur = lw.Surrogate(truncation, hidden=hidden, seed=seed)
+    sur.set_clip(clip)
+    gen_s = sur.generate(trajectories, windows, seed0=1_000_000 * seed, hmin=hmin, hmax=hmax, precision=data_precision)
+    fit = sur.fit(epochs, batch=batch, lr=lr, lr_min=lr_min, val_fraction=0.1, seed=seed, loss=loss)
+    hist_loss, _ = sur.history()
+    train_ms, fwd_ms = sur.time(batch, 10)
+    out = {"truncation": truncation, "features": sur.features, "hidden": hidden, "pairs": trajectories * windows,
+           "trajectories": trajectories, "windows_per_trajectory": windows, "mean_height_range_m": [hmin, hmax],
+           "data_precision": ["fp64", "fp32", "split3"][data_precision], "generate_s": gen_s, "loss": loss, "clip_ratio": clip,
+           "epochs": epochs, "lr": [lr, lr_min], "fit": fit, "loss_by_epoch": [round(v, 4) for v in hist_loss.tolist()],
+           "train_step_ms": train_ms, "forward_ms_batch": fwd_ms, "batch": batch,
+           "check_precision": ["fp64", "fp32", "split3"][check_precision]}
+    if members > 0 and rollout_windows > 0:
+        r = sur.rollout(members, seed0=9_000_000 + seed, windows=rollout_windows, check_every=check_every, threshold=threshold,
+                        check_precision=check_precision, ref_windows=ref_windows, hmin=hmin, hmax=hmax)
+        r["speedup_hybrid_vs_rk4"] = r["hybrid_rate"] / r["rk4_rate"]
+        r["speedup_network_vs_rk4"] = r["network_rate"] / r["rk4_rate"]
+        out["rollout"] = dict(members=members, windows=rollout_windows, check_every=check_every, threshold=threshold, **r)
+        sweep = []
+        for th in thresholds:
+            q = sur.rollout(members, seed0=9_000_000 + seed, windows=rollout_windows, check_every=check_every, threshold=th,
+                            check_precision=check_precision, ref_windows=ref_windows, hmin=hmin, hmax=hmax)
+            sweep.append({"threshold": th, "taken_over": q["taken_over"], "err_mean": q["err_mean"], "err_max": q["err_max"],
+                          "speedup_hybrid_vs_rk4": q["hybrid_rate"] / q["rk4_rate"]})
+        if sweep:
+            out["threshold_sweep"] = sweep
+    sur.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -573,8 +768,43 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="split3", choices=["split3", "split6", "fp32", "fp64"])
     ap.add_argument("--quick", action="store_true", help="skip the other configurations")
+    ap.add_argument("--ref-seconds", type=float, default=12.0, help="wall seconds of one timed CPU pass")
+    # a named workload for profiler captures, instead of the benchmark
+    ap.add_argument("--case", choices=["t42", "t85", "t170", "t341", "plane", "ens", "mlp"])
+    ap.add_argument("--case-steps", type=int, default=4)
+    ap.add_argument("--truncation", type=int, default=85)
+    ap.add_argument("--members", type=int, default=128)
+    ap.add_argument("--batch", type=int, default=512)
+    ap.add_argument("--plan", default="", help="split plan entries to force in the ens case")
+    # a study, instead of the benchmark: the precision study (--truncation, --days) or the surrogate end to end
+    ap.add_argument("--study", choices=["precision", "surrogate"])
+    ap.add_argument("--days", type=float, default=2.0)
+    ap.add_argument("--trajectories", type=int, default=2560)
+    ap.add_argument("--windows", type=int, default=80)
+    ap.add_argument("--epochs", type=int, default=100)
+    ap.add_argument("--rollout-windows", type=int, default=80)
+    ap.add_argument("--rollout-members", type=int, default=1024)
+    ap.add_argument("--threshold", type=float, default=1e-3)
+    ap.add_argument("--check-precision", default="split3", choices=["fp64", "split3"])
+    ap.add_argument("--sweep", default="", help="comma-separated extra take-over thresholds")
     args = ap.parse_args()
     rank, world, local = dist_env()
+    if args.case:
+        return run_case(args)
+    if args.study:
+        from lmweather_gb300 import build
+
+        build.build()
+        if args.study == "precision":
+            print(json.dumps(precision_study(args.truncation, args.days)))
+        else:
+            import lmweather_gb300 as lw
+
+            print(json.dumps(surrogate_study(42, trajectories=args.trajectories, windows=args.windows, epochs=args.epochs, batch=args.batch,
+                                             members=args.rollout_members, rollout_windows=args.rollout_windows, threshold=args.threshold,
+                                             check_precision=lw.SPLIT_BF16 if args.check_precision == "split3" else lw.FP64,
+                                             thresholds=tuple(float(v) for v in args.sweep.split(",") if v))))
+        return 0
     if args.impl == "reference":
         return run_reference(args, rank, world)
     return run_ours(args, rank, world, local)

@@ -38,6 +38,10 @@ const char *lmw_last_error(void);
 const char *lmw_version(void);
 /* number of this library's kernel launches issued by the calling thread so far */
 uint64_t lmw_launch_count(void);
+/* number of device (cudaMalloc) and pinned host (cudaMallocHost) allocations this library has made so far, over
+ * all threads. No reference counterpart (accounting hook: lets a caller check that an entry point allocates
+ * nothing). */
+uint64_t lmw_alloc_count(void);
 
 /* The engine's split-BF16 tensor-core GEMM (tcgen05, FP32 accumulation in tensor memory) on one problem from
  * host arrays: D (128 x N) = A (128 x K) * B (N x K)^T with A and B split on the device into `terms` = 1 (BF16),
@@ -63,9 +67,6 @@ int lmw_division_selftest(const uint64_t *x, int nx, const double *divisors, int
  * receive 1 when both behave. The context stays usable. Failure-detection hook; no reference counterpart. */
 int lmw_wait_selftest(int timeout_us, int *completed, int *ran_out);
 
-/* Measured FP64 FMA throughput of the current device in TFLOP/s (the roofline of the FP64 paths) */
-int lmw_fp64_peak(double *tflops);
-
 /* ---------------------------------------------------------------------------------------- sphere */
 
 /* Sphere::Sphere(int truncation, const SphereParams &) (cpp/sphere.hpp:29, cpp/sphere.cpp:75-103).
@@ -84,6 +85,15 @@ int lmw_sphere_destroy(lmw_sphere *s);
 int lmw_sphere_dims(const lmw_sphere *s, int *truncation, int *nlat, int *nlon, int *members);
 /* Sphere::gauss_mu / gauss_weights (cpp/sphere.hpp:93-94): nlat values each */
 int lmw_sphere_gauss(const lmw_sphere *s, double *mu, double *w);
+/* The reference's transform test hooks (cpp/sphere.hpp:96-99), in FP64 on the device. Grids are nlat*nlon
+ * values ([lat][lon], latitude ascending); spectra are the reference layout, (T+1)^2 complex values interleaved
+ * re/im at index m*(T+1)+n (entries with n < m are zero). n must be nlat*nlon ("grid size mismatch").
+ * Sphere::analyze_scalar (cpp/sphere.cpp:138-149): spec_nm = sum_j w_j F_m(grid)_j P_nm(mu_j) */
+int lmw_sphere_analyze_scalar(lmw_sphere *s, const double *grid, size_t n, double *spec);
+/* Sphere::synthesize_scalar (cpp/sphere.cpp:150-162): the grid of a spectrum */
+int lmw_sphere_synthesize_scalar(lmw_sphere *s, const double *spec, double *grid, size_t n);
+/* Sphere::analyze_divergence (cpp/sphere.cpp:164-177): spec_nm = sum_j w_j/((1-mu_j^2) a) (i m A_m P_nm - B_m H_nm) */
+int lmw_sphere_analyze_divergence(lmw_sphere *s, const double *A, const double *B, size_t n, double *spec);
 /* Sphere::time (cpp/sphere.hpp:34) of one member */
 int lmw_sphere_time(const lmw_sphere *s, int member, double *out);
 /* Sphere::set_state_grid (cpp/sphere.hpp:39, cpp/sphere.cpp:217-234); n = nlat*nlon values per grid */
@@ -222,14 +232,17 @@ int lmw_plane_stream(const lmw_plane *p, void **stream);
  *
  * h, u (nx*ny doubles) and v (nx*(ny+1) doubles) are caller-owned DEVICE pointers in the layouts above; they
  * are advanced in place by `steps` RK4 steps of size dt with the same kernels, and the same bits, as
- * lmw_plane_step. The parameters mean what they mean in lmw_plane_create. The call only enqueues work on
+ * lmw_plane_step. Rows 0 and ny of v are the channel walls: the call sets them to zero on `stream` before the
+ * first step, as lmw_plane_set_v does for the handle. The parameters mean what they mean in lmw_plane_create. The call only enqueues work on
  * `stream` (a cudaStream_t; NULL is the default stream) and returns; the fields are ready when the stream
  * reaches that point. It calls no cudaMalloc, cudaFree or other allocating routine: the stage inputs and the
  * accumulator live in one fixed device array that every GPU loading this library reserves until the process
  * exits (about 19 MB). Grids above 262144 cells (nx*ny) are rejected with LMW_INVALID_ARGUMENT.
  *
- * The first call on a device looks up that array's device address (once per device, with that device
- * current); make that first call before any stream capture. Every call shares the array and it keeps the last
+ * The first call in a CUDA context looks up that array's device address in that context (once per context,
+ * with it current; the array is loaded again at another address after cudaDeviceReset or in a second context
+ * made on the same device, and such a context gets its own look-up); make that first call before any stream
+ * capture. Every call shares the array and it keeps the last
  * call's contents (each step overwrites what it reads, so nothing needs clearing): calls whose work overlaps on
  * the GPU, on different streams or different threads, race on it and must be serialised by the caller. */
 int lmw_plane_step_noalloc(int nx, int ny, double lx, double ly, double gravity, double depth, double f0, double beta,
@@ -281,6 +294,16 @@ int lmw_sphere_split_plan(lmw_sphere *s, int *out);
  * candidates obey (invalid_argument otherwise); every plan computes the same arithmetic. Validation and tuning
  * hook; no reference counterpart. */
 int lmw_sphere_set_split_plan(lmw_sphere *s, const int *plan);
+/* The split path's treatment of the linear terms of the tendencies (cpp/sphere.cpp:338-390 computes every term
+ * on the grid). linear_exact = 1 (the default): the terms that are linear in the state are added in FP64 in
+ * spectral space by the analysis epilogue -- n(n+1)/a^2 Phi in d delta, -Phi_mean delta in d Phi (the mean
+ * height's gravity-wave term; D(U, V) = delta holds exactly for n <= T) and, for an untilted axis, the Coriolis
+ * terms -D(fU, fV) and D(fV, -fU) with f = 2 Omega mu, which couple n - 1, n and n + 1 -- and only the nonlinear
+ * products (U zeta, V zeta, U Phi', V Phi', E) go through the BF16 pieces. linear_exact = 0: every term through the
+ * BF16 GEMMs (the plain split form). Mathematically the same tendencies; the forms differ in rounding only.
+ * No reference counterpart (precision choice). */
+int lmw_sphere_set_split_form(lmw_sphere *s, int linear_exact);
+int lmw_ensemble_set_split_form(lmw_ensemble *e, int linear_exact);
 /* writes `code` into a split-precision engine's error word, as a tensor-core wait that ran out does: the next step
  * or guard check fails with LMW_DEVICE_ERROR ("a wait on the tensor cores timed out ..."). Failure-detection
  * hook (the failure is made on the host); no reference counterpart. */
@@ -358,6 +381,15 @@ int lmw_surrogate_reset(lmw_surrogate *s, uint64_t seed);
 /* adaptive gradient clipping of training: the global gradient norm is held to at most ratio times its running
  * mean (default 2; 0 switches clipping off) */
 int lmw_surrogate_set_clip(lmw_surrogate *s, double ratio);
+/* on != 0 (the default): each training pair entering a batch is first mapped by a random symmetry of the untilted
+ * equations, the same for the state and its successor -- a rotation about the polar axis (coefficient (m, n) times
+ * e^{i m a}) and, for half of the pairs, the reflection mu -> -mu (Phi and delta times (-1)^(n-m), zeta times
+ * -(-1)^(n-m)). No reference counterpart. */
+int lmw_surrogate_set_augment(lmw_surrogate *s, int on);
+/* decay in (0, 1): the trained network is the exponential moving average (this decay per step) of the weights over
+ * the second half of lmw_surrogate_fit's steps (the default, 0.9995); 0: the last weights. No reference
+ * counterpart. */
+int lmw_surrogate_set_averaging(lmw_surrogate *s, double decay);
 /* per epoch of the last fit: mean training loss and mean global gradient norm per step (count = epochs; at most
  * max values written) */
 int lmw_surrogate_history(lmw_surrogate *s, int max, double *loss, double *grad_norm, int *count);

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -170,6 +171,23 @@ class Sphere {
   std::vector<double> grid_vorticity() const { return grid(3); }
   const std::vector<double> &gauss_weights() const { return w_; }
   const std::vector<double> &gauss_mu() const { return mu_; }
+
+  // exposed for tests (cpp/sphere.hpp:96-99): spectra in the reference layout, (T+1)^2 values at m*(T+1)+n
+  using cplx = std::complex<double>;
+  void analyze_scalar(const std::vector<double> &grid, std::vector<cplx> &spec) const {
+    spec.assign(static_cast<size_t>(N_ + 1) * (N_ + 1), cplx(0, 0));
+    check(lmw_sphere_analyze_scalar(s_, grid.data(), grid.size(), reinterpret_cast<double *>(spec.data())));
+  }
+  void synthesize_scalar(const std::vector<cplx> &spec, std::vector<double> &grid) const {
+    if (spec.size() != static_cast<size_t>(N_ + 1) * (N_ + 1)) throw std::invalid_argument("spectrum size mismatch");
+    grid.assign(static_cast<size_t>(nlat_) * nlon_, 0.0);
+    check(lmw_sphere_synthesize_scalar(s_, reinterpret_cast<const double *>(spec.data()), grid.data(), grid.size()));
+  }
+  void analyze_divergence(const std::vector<double> &A, const std::vector<double> &B, std::vector<cplx> &spec) const {
+    if (A.size() != B.size()) throw std::invalid_argument("grid size mismatch");
+    spec.assign(static_cast<size_t>(N_ + 1) * (N_ + 1), cplx(0, 0));
+    check(lmw_sphere_analyze_divergence(s_, A.data(), B.data(), A.size(), reinterpret_cast<double *>(spec.data())));
+  }
 
   // the engine handle, for the entry points beyond the reference's class (precision, ensembles, state I/O)
   lmw_sphere *handle() const { return s_; }

@@ -42,7 +42,10 @@ _SIGS = {
     "lmw_division_selftest": (_I, [C.POINTER(C.c_uint64), _I, C.POINTER(C.c_double), _I, C.POINTER(C.c_longlong)]),
     "lmw_wait_selftest": (_I, [_I, _IP, _IP]),
     "lmw_sphere_inject_split_error": (_I, [_P, _I]),
+    "lmw_sphere_set_split_form": (_I, [_P, _I]),
+    "lmw_ensemble_set_split_form": (_I, [_P, _I]),
     "lmw_launch_count": (C.c_uint64, []),
+    "lmw_alloc_count": (C.c_uint64, []),
     "lmw_sphere_create": (_I, [_I, _D, _D, _D, _D, _PP]),
     "lmw_sphere_create_ex": (_I, [_I, _D, _D, _D, _D, _I, _I, _I, _PP]),
     "lmw_sphere_create_split": (_I, [_I, _D, _D, _D, _D, _I, _I, _I, _PP]),
@@ -50,6 +53,9 @@ _SIGS = {
     "lmw_sphere_dims": (_I, [_P, _IP, _IP, _IP, _IP]),
     "lmw_sphere_gauss": (_I, [_P, _DP, _DP]),
     "lmw_sphere_time": (_I, [_P, _I, _DP]),
+    "lmw_sphere_analyze_scalar": (_I, [_P, _DP, _SZ, _DP]),
+    "lmw_sphere_synthesize_scalar": (_I, [_P, _DP, _DP, _SZ]),
+    "lmw_sphere_analyze_divergence": (_I, [_P, _DP, _DP, _SZ, _DP]),
     "lmw_sphere_set_state_grid": (_I, [_P, _I, _DP, _DP, _DP, _SZ]),
     "lmw_sphere_set_axis_tilt": (_I, [_P, _I, _D]),
     "lmw_sphere_set_omega": (_I, [_P, _I, _D]),
@@ -137,6 +143,8 @@ _SIGS = {
     "lmw_surrogate_time": (_I, [_P, _I, _I, _DP, _DP]),
     "lmw_surrogate_reset": (_I, [_P, _U64]),
     "lmw_surrogate_set_clip": (_I, [_P, _D]),
+    "lmw_surrogate_set_augment": (_I, [_P, _I]),
+    "lmw_surrogate_set_averaging": (_I, [_P, _D]),
     "lmw_surrogate_history": (_I, [_P, _I, _DP, _DP, _IP]),
 }
 
@@ -159,6 +167,11 @@ def load_library() -> C.CDLL:
 
 def launch_count() -> int:
     return int(load_library().lmw_launch_count())
+
+
+def alloc_count() -> int:
+    """Device and pinned-host allocations the library has made so far (all threads)."""
+    return int(load_library().lmw_alloc_count())
 
 
 def _check(code: int) -> None:
@@ -233,6 +246,30 @@ class Sphere:
         mu, w = np.zeros(self.nlat), np.zeros(self.nlat)
         _check(self._lib.lmw_sphere_gauss(self._h, _dp(mu), _dp(w)))
         return mu, w
+
+    # the reference's transform test hooks (cpp/sphere.hpp:96-99)
+    def analyze_scalar(self, grid):
+        g = np.ascontiguousarray(grid, dtype=np.float64).reshape(-1)
+        spec = np.zeros(self.nspec, dtype=np.complex128)
+        _check(self._lib.lmw_sphere_analyze_scalar(self._h, _dp(g), g.size, _dp(spec)))
+        return spec
+
+    def synthesize_scalar(self, spec):
+        sp = np.ascontiguousarray(spec, dtype=np.complex128).reshape(-1)
+        if sp.size != self.nspec:
+            raise ValueError("spectrum size mismatch")
+        grid = np.zeros((self.nlat, self.nlon))
+        _check(self._lib.lmw_sphere_synthesize_scalar(self._h, _dp(sp), _dp(grid), grid.size))
+        return grid
+
+    def analyze_divergence(self, A, B):
+        a = np.ascontiguousarray(A, dtype=np.float64).reshape(-1)
+        b = np.ascontiguousarray(B, dtype=np.float64).reshape(-1)
+        if a.size != b.size:
+            raise ValueError("grid size mismatch")
+        spec = np.zeros(self.nspec, dtype=np.complex128)
+        _check(self._lib.lmw_sphere_analyze_divergence(self._h, _dp(a), _dp(b), a.size, _dp(spec)))
+        return spec
 
     def time(self, member: int = 0) -> float:
         t = _D()
@@ -352,6 +389,11 @@ class Sphere:
         cur.update(plan)
         arr = np.array([cur[k] for k in self._PLAN_KEYS], np.int32)
         _check(self._lib.lmw_sphere_set_split_plan(self._h, arr.ctypes.data_as(_IP)))
+
+    def set_split_form(self, linear_exact: bool) -> None:
+        """Split path: True (the default) adds the linear terms of the tendencies in FP64 spectral space and sends only
+        the nonlinear products through the BF16 pieces; False sends every term through the BF16 GEMMs."""
+        _check(self._lib.lmw_sphere_set_split_form(self._h, 1 if linear_exact else 0))
 
     def get_state(self, member: int = 0):
         z, d, f = (np.zeros(self.nspec, np.complex128) for _ in range(3))
@@ -659,6 +701,10 @@ class Ensemble:
                                              st.ctypes.data_as(C.POINTER(C.c_int64))))
         return [dict(truncation=int(tr[g]), members=int(cnt[g]), dt=float(dt[g]), steps=int(st[g])) for g in range(G)]
 
+    def set_split_form(self, linear_exact: bool) -> None:
+        """Sphere.set_split_form for every truncation group."""
+        _check(self._lib.lmw_ensemble_set_split_form(self._h, 1 if linear_exact else 0))
+
     def split_plan(self, group: int) -> dict:
         """The autotuned launch plan of a truncation group's split path."""
         out = np.zeros(9, np.int32)
@@ -830,6 +876,14 @@ class Surrogate:
 
     def set_clip(self, ratio: float):
         _check(self._lib.lmw_surrogate_set_clip(self._h, ratio))
+
+    def set_averaging(self, decay: float):
+        """Moving average of the weights over the second half of fit() (decay per step; 0: the last weights)."""
+        _check(self._lib.lmw_surrogate_set_averaging(self._h, decay))
+
+    def set_augment(self, on: bool):
+        """Random rotations about the polar axis and equatorial reflections of the training pairs (default on)."""
+        _check(self._lib.lmw_surrogate_set_augment(self._h, 1 if on else 0))
 
     def history(self):
         n = _I()

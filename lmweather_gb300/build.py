@@ -26,9 +26,7 @@ UNITS = [
     ("plane.cu", ["--fmad=false", "-Xcompiler=-ffp-contract=off"]),
     ("sphere.cu", []),
     ("ensemble.cu", []),
-    ("sphere32.cu", []),
     ("capi.cu", []),
-    ("peak.cu", []),
     ("tc_gemm.cu", []),
     ("surrogate.cu", []),
     ("sphere_tables.cpp", []),

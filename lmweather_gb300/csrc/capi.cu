@@ -89,6 +89,7 @@ extern "C" {
 const char *lmw_last_error(void) { return g_err.c_str(); }
 const char *lmw_version(void) { return "lmweather-gb300 0.1.0"; }
 uint64_t lmw_launch_count(void) { return lmw::g_launches; }
+uint64_t lmw_alloc_count(void) { return lmw::alloc_counter().load(); }
 int lmw_tc_gemm_selftest(const float *A, const float *B, float *D, int N, int K, int terms, int layout, int *kernel_status) {
   return guard([&] {
     need(A && B && D && kernel_status, "pointer is null");
@@ -111,12 +112,6 @@ int lmw_wait_selftest(int timeout_us, int *completed, int *ran_out) {
   return guard([&] {
     need(completed != nullptr && ran_out != nullptr, "null buffer");
     lmw::wait_selftest_run(timeout_us, completed, ran_out);
-  });
-}
-int lmw_fp64_peak(double *tflops) {
-  return guard([&] {
-    need(tflops != nullptr, "output pointer is null");
-    *tflops = lmw::measure_fp64_peak();
   });
 }
 
@@ -186,6 +181,24 @@ int lmw_sphere_gauss(const lmw_sphere *s, double *mu, double *w) {
     lmw::gauss_legendre(s->e->nlat, x, ww);
     if (mu) std::copy(x.begin(), x.end(), mu);
     if (w) std::copy(ww.begin(), ww.end(), w);
+  });
+}
+int lmw_sphere_analyze_scalar(lmw_sphere *s, const double *grid, size_t n, double *spec) {
+  return SPH({
+    need(grid && spec, "grid or spectrum pointer is null");
+    s->e->analyze_scalar(grid, n, spec);
+  });
+}
+int lmw_sphere_synthesize_scalar(lmw_sphere *s, const double *spec, double *grid, size_t n) {
+  return SPH({
+    need(grid && spec, "grid or spectrum pointer is null");
+    s->e->synthesize_scalar(spec, grid, n);
+  });
+}
+int lmw_sphere_analyze_divergence(lmw_sphere *s, const double *A, const double *B, size_t n, double *spec) {
+  return SPH({
+    need(A && B && spec, "grid or spectrum pointer is null");
+    s->e->analyze_divergence(A, B, n, spec);
   });
 }
 int lmw_sphere_time(const lmw_sphere *s, int member, double *out) {
@@ -744,6 +757,18 @@ int lmw_sphere_set_split_plan(lmw_sphere *s, const int *plan) {
     s->e->set_split_plan(plan);
   });
 }
+int lmw_sphere_set_split_form(lmw_sphere *s, int linear_exact) {
+  return guard([&] {
+    need(s != nullptr && s->e != nullptr, "null sphere handle");
+    s->e->set_split_form(linear_exact);
+  });
+}
+int lmw_ensemble_set_split_form(lmw_ensemble *e, int linear_exact) {
+  return guard([&] {
+    need(e != nullptr && e->e != nullptr, "null ensemble handle");
+    for (auto &g : e->e->groups) g->set_split_form(linear_exact);
+  });
+}
 int lmw_ensemble_split_plan(lmw_ensemble *e, int group, int *out) {
   return guard([&] {
     need(e != nullptr && e->e != nullptr, "null ensemble handle");
@@ -753,6 +778,10 @@ int lmw_ensemble_split_plan(lmw_ensemble *e, int group, int *out) {
   });
 }
 int lmw_surrogate_reset(lmw_surrogate *s, uint64_t seed) { return SUR(s, s->s->reset(seed)); }
+int lmw_surrogate_set_augment(lmw_surrogate *s, int on) { return SUR(s, s->s->augment = on != 0); }
+int lmw_surrogate_set_averaging(lmw_surrogate *s, double decay) {
+  return SUR(s, need(decay >= 0 && decay < 1, "the averaging decay must lie in [0, 1)"); s->s->ema = decay);
+}
 int lmw_surrogate_set_clip(lmw_surrogate *s, double ratio) {
   return SUR(s, need(ratio >= 0, "the clipping ratio must not be negative"); s->s->clip_ratio = ratio);
 }

@@ -143,6 +143,11 @@ class SphereEngine {
   double *states_to_ref();
   double *device_refstates();
   void states_from_ref();
+  // the reference's transform test hooks (cpp/sphere.hpp:96-99), FP64 on the device: grids [nlat][nlon],
+  // spectra in the reference layout ((T+1)^2 complex, interleaved)
+  void analyze_scalar(const double *grid, size_t n, double *spec);
+  void synthesize_scalar(const double *spec, double *grid, size_t n);
+  void analyze_divergence(const double *A, const double *B, size_t n, double *spec);
   // the wx layer's text files (cpp/main.cpp:328-335, 357-384)
   void save_csv(const std::string &path, int member);
   void save_zonal_mean(const std::string &path, int member);
@@ -182,6 +187,9 @@ class SphereEngine {
   // replaces the autotuned plan (same 7 entries as split_plan); checked against the shared-memory and
   // tensor-memory limits the autotuner's candidates obey
   void set_split_plan(const int *in);
+  // 1 (default): the linear terms of the tendencies in FP64 spectral space, the nonlinear products through the BF16
+  // pieces; 0: every term through the BF16 GEMMs
+  void set_split_form(int linear_exact);
   // writes `code` into the split path's error word, as a tensor-core wait that ran out does (failure tests)
   void inject_split_error(int code);
 
@@ -192,9 +200,12 @@ class SphereEngine {
   void check_split_status();
   void ensure_packed();
   void autotune_split();
-  // state (packed triangle, complex interleaved), stage input, accumulator
-  DevBuf<double> x0, xs, acc;
+  // state (packed triangle, complex interleaved), stage input, accumulator; a second stage input (split form)
+  DevBuf<double> x0, xs, acc, xs2;
+  double2 *XS2() { return reinterpret_cast<double2 *>(xs2.p); }
   DevBuf<double> refstates;  // every member's state in the reference layout (allocated on first use)
+  DevBuf<double> hookspec;   // one spectrum in the reference layout for the transform hooks (allocated on first use)
+  void hook_analysis(const double *A, const double *B, size_t n, double *spec);
 
   // Fourier coefficients of the synthesised grids, folded analysis inputs
   DevBuf<double> four, fold;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <functional>
 #include <stdexcept>
@@ -35,6 +36,13 @@ void write_text(const std::string &path, const std::string &text, const char *wh
 // capi.cu)
 int run_guarded(const std::function<void()> &fn);
 
+// Counts this library's device and pinned-host allocations (cudaMalloc, cudaMallocHost), process-wide; a
+// caller can check that an entry point which promises not to allocate leaves it unchanged.
+inline std::atomic<uint64_t> &alloc_counter() {
+  static std::atomic<uint64_t> n{0};
+  return n;
+}
+
 // Device buffer owned by an engine object.
 template <class T> struct DevBuf {
   T *p = nullptr;
@@ -47,6 +55,7 @@ template <class T> struct DevBuf {
     release();
     if (count == 0) return;
     LMW_CUDA(cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(T)));
+    alloc_counter().fetch_add(1, std::memory_order_relaxed);
     n = count;
   }
   void zero(cudaStream_t s) {
@@ -76,6 +85,7 @@ template <class T> struct HostBuf {
     n = 0;
     if (count == 0) return;
     LMW_CUDA(cudaMallocHost(reinterpret_cast<void **>(&p), count * sizeof(T)));
+    alloc_counter().fetch_add(1, std::memory_order_relaxed);
     n = count;
   }
 };
@@ -83,8 +93,6 @@ template <class T> struct HostBuf {
 // Counts this library's kernel launches (for the benchmark's launch accounting).
 extern thread_local uint64_t g_launches;
 
-// FP64 FMA throughput of the current device (TFLOP/s), from a dependent-chain DFMA kernel on every SM
-double measure_fp64_peak();
 int conversion_selftest_run(const uint32_t *f, int nf, const uint64_t *x, int nx, int *mismatches);
 int wait_selftest_run(int timeout_us, int *completed, int *ran_out);
 void division_selftest_run(const uint64_t *x, int nx, const double *y, int ny, long long *counts);

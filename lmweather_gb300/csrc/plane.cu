@@ -388,22 +388,52 @@ void division_selftest_run(const uint64_t *x, int nx, const double *y, int ny, l
   for (int k = 0; k < 2; k++) counts[k] = static_cast<long long>(c[k]);
 }
 
-// Device address of g_noalloc_scratch on the current device. In host code the symbol's name is only a host-side
-// stand-in, never a device address; the address is looked up once per device (with that device current) and
-// cached. The first call on a device does this look-up.
-static double *noalloc_scratch() {
-  static std::mutex mu;
-  static double *addr[64] = {nullptr};
-  int dev = 0;
-  LMW_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) throw InvalidArgument("lmw_plane_step_noalloc: device ordinal out of range");
-  std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
+// Device address of g_noalloc_scratch in the calling thread's current CUDA context. In host code the symbol's
+// name is only a host-side stand-in, never a device address. A module's globals live in one context: after
+// cudaDeviceReset, or in a second context made on the same device with the driver API, the array is loaded
+// again at another address. So the address is cached per context (keyed by the driver's unique context id,
+// which is never reused within a process) and looked up, with that context current, on the first call made
+// in it.
+using CtxGetCurrentFn = int (*)(void **);
+using CtxGetIdFn = int (*)(void *, unsigned long long *);
+static unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  if (!get_current || !get_id) throw DeviceError("lmw_plane_step_noalloc: the driver offers no context id (cuCtxGetId)");
+  void *ctx = nullptr;
+  if (get_current(&ctx) != 0) throw DeviceError("lmw_plane_step_noalloc: cuCtxGetCurrent failed");
+  if (ctx == nullptr) {
+    // no context bound to this thread yet: a runtime call on the module binds the device's primary context
     void *p = nullptr;
     LMW_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    addr[dev] = static_cast<double *>(p);
+    if (get_current(&ctx) != 0 || ctx == nullptr) throw DeviceError("lmw_plane_step_noalloc: no current CUDA context");
   }
-  return addr[dev];
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != 0) throw DeviceError("lmw_plane_step_noalloc: cuCtxGetId failed");
+  return id;
+}
+
+static double *noalloc_scratch() {
+  static std::mutex mu;
+  static std::vector<std::pair<unsigned long long, double *>> cache;  // (context id, array address)
+  const unsigned long long id = current_context_id();
+  std::lock_guard<std::mutex> lock(mu);
+  for (const auto &e : cache)
+    if (e.first == id) return e.second;
+  void *p = nullptr;
+  LMW_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  cache.emplace_back(id, static_cast<double *>(p));
+  return static_cast<double *>(p);
 }
 
 void plane_step_noalloc(const PlaneConfig &c, double *h, double *u, double *v, double dt, int steps, cudaStream_t stream) {
@@ -418,6 +448,10 @@ void plane_step_noalloc(const PlaneConfig &c, double *h, double *u, double *v, d
   if (steps < 0) throw InvalidArgument("lmw_plane_step_noalloc: steps must not be negative");
   if (!std::isfinite(dt)) throw InvalidArgument("lmw_plane_step_noalloc: dt must be finite");
   double *sc = noalloc_scratch();
+  // rows 0 and ny of v are the walls; the model keeps them at zero (lmw_plane_set_v does the same), and a
+  // nonzero value there would never be cleared (dv = 0 on the walls) and would enter the fluxes and vorticity
+  LMW_CUDA(cudaMemsetAsync(v, 0, static_cast<size_t>(c.nx) * sizeof(double), stream));
+  LMW_CUDA(cudaMemsetAsync(v + static_cast<size_t>(c.ny) * c.nx, 0, static_cast<size_t>(c.nx) * sizeof(double), stream));
   double *ha = sc, *ua = sc + kNoAllocFieldCap, *va = sc + 2 * kNoAllocFieldCap;
   double *hb = sc + 3 * kNoAllocFieldCap, *ub = sc + 4 * kNoAllocFieldCap, *vb = sc + 5 * kNoAllocFieldCap;
   double *ah = sc + 6 * kNoAllocFieldCap, *au = sc + 7 * kNoAllocFieldCap, *av = sc + 8 * kNoAllocFieldCap;

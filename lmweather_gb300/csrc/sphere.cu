@@ -613,25 +613,50 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_diag(SphDev d, const double2
 __global__ void __launch_bounds__(GRID_THREADS) sph_diag_final(SphDev d, const double *__restrict__ rows, const double2 *__restrict__ x,
                                                                int member0, Reduce *out) {
   __shared__ double red[GRID_THREADS / 32];
+  __shared__ double part[9][GRID_THREADS / 32];
   const int b = member0 + blockIdx.x;
   const double2 *xb = x + static_cast<size_t>(b) * 3 * d.ntri;
   double s = 0;
   for (int i = threadIdx.x; i < 3 * d.ntri; i += blockDim.x) s += hypot(xb[i].x, xb[i].y);
   s = block_sum(s, red);
+  // the latitude rows in parallel: sums 0-4 (weighted), maxima 5-8, each thread a strided subset of rows, then
+  // the warps' and the block's partials
+  double v[9] = {0, 0, 0, 0, 0, 0, -INFINITY, 0, 0};
+  for (int j = threadIdx.x; j < d.nlat; j += blockDim.x) {
+    const double *rw = rows + (static_cast<size_t>(b) * d.nlat + j) * DIAG_K;
+    v[0] += d.w[j] * rw[0] / d.nlon;
+    v[1] += d.w[j] * rw[1] / d.nlon;
+    v[2] += d.w[j] * rw[2] / d.nlon;
+    v[3] += d.w[j] * rw[3];
+    v[4] += d.w[j] * rw[4];
+    v[5] = fmax(v[5], rw[5]);
+    v[6] = fmax(v[6], rw[6]);
+    v[7] = fmax(v[7], rw[7]);
+    v[8] = fmax(v[8], rw[8]);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      const double u = __shfl_down_sync(0xffffffffu, v[k], o);
+      v[k] = k < 5 ? v[k] + u : fmax(v[k], u);
+    }
+    if (lane == 0) part[k][wid] = v[k];
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
     Reduce r;
     double ke = 0, pe = 0, en = 0, num = 0, den = 0, wmax = 0, hmax = -INFINITY, dmax = 0, rmax = 0;
-    for (int j = 0; j < d.nlat; j++) {
-      const double *rw = rows + (static_cast<size_t>(b) * d.nlat + j) * DIAG_K;
-      ke += d.w[j] * rw[0] / d.nlon;
-      pe += d.w[j] * rw[1] / d.nlon;
-      en += d.w[j] * rw[2] / d.nlon;
-      num += d.w[j] * rw[3];
-      den += d.w[j] * rw[4];
-      wmax = fmax(wmax, rw[5]);
-      hmax = fmax(hmax, rw[6]);
-      dmax = fmax(dmax, rw[7]);
-      rmax = fmax(rmax, rw[8]);
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); w++) {
+      ke += part[0][w];
+      pe += part[1][w];
+      en += part[2][w];
+      num += part[3][w];
+      den += part[4][w];
+      wmax = fmax(wmax, part[5][w]);
+      hmax = fmax(hmax, part[6][w]);
+      dmax = fmax(dmax, part[7][w]);
+      rmax = fmax(rmax, part[8][w]);
     }
     r.sum[0] = 0.5 * ke;
     r.sum[1] = 0.5 * pe;
@@ -661,6 +686,74 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_phi_grid(SphDev d, const dou
     out[(static_cast<size_t>(b) * d.nlat + js) * n + k] = sm[k].x;
     out[(static_cast<size_t>(b) * d.nlat + jn) * n + k] = sm[k].y;
   }
+}
+
+// ------------------------------------------------------------------------------------------------ transform hooks
+// The reference's scalar transforms exposed for tests (cpp/sphere.cpp:138-177), in FP64 on the device.
+// sph_hook_fold: per latitude pair, forward FFTs of A (and B when given), the weight (mode 0: w, the scalar
+// analysis; mode 1: w / ((1 - mu^2) a), the divergence operator) and the hemispheric fold into
+// fold[jh][row][parity][M] (parity 0: south + north, parity 1: south - north).
+__global__ void __launch_bounds__(GRID_THREADS) sph_hook_fold(SphDev d, const double *__restrict__ A, const double *__restrict__ B, int mode,
+                                                              double2 *__restrict__ fold) {
+  extern __shared__ double2 sm[];
+  const int jh = blockIdx.x, js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
+  const int rows = B ? 2 : 1;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const size_t os = static_cast<size_t>(js) * n + k, on = static_cast<size_t>(jn) * n + k;
+    sm[k] = make_double2(A[os], A[on]);
+    if (B) sm[n + k] = make_double2(B[os], B[on]);
+  }
+  __syncthreads();
+  fft_forward_dif(sm, rows, n, d.logn, d.tw);
+  const double inv = 1.0 / n, wt = mode ? d.wd[js] : d.w[js];
+  double2 *o = fold + static_cast<size_t>(jh) * rows * 2 * d.M;
+  for (int e = threadIdx.x; e < rows * d.M; e += blockDim.x) {
+    const int r = e / d.M, m = e - r * d.M;
+    const double2 *row = sm + static_cast<size_t>(r) * n;
+    const double2 Ym = row[bitrev(m, d.logn)], Yc = conjd(row[bitrev((n - m) & (n - 1), d.logn)]);
+    double2 Xs = cscale(cadd(Ym, Yc), 0.5 * inv);
+    const double2 t = csub(Ym, Yc);
+    double2 Xn = make_double2(0.5 * inv * t.y, -0.5 * inv * t.x);
+    Xs = cscale(Xs, wt);
+    Xn = cscale(Xn, wt);
+    o[(r * 2 + 0) * d.M + m] = cadd(Xs, Xn);
+    o[(r * 2 + 1) * d.M + m] = csub(Xs, Xn);
+  }
+}
+
+// mode 0: spec = sum_j w F_m(A) P (analyze_scalar); mode 1: spec = sum_j wd (i m F_m(A) P - F_m(B) H)
+// (analyze_divergence). Written into the reference layout spec[m (T+1) + n], or (packed != 0) into the engine's
+// packed triangle spec[q].
+__global__ void __launch_bounds__(ANA_THREADS) sph_hook_analysis(SphDev d, const double2 *__restrict__ fold, int mode, double2 *__restrict__ spec,
+                                                                 int packed = 0) {
+  const int q = blockIdx.x * ANA_THREADS + threadIdx.x;
+  if (q >= d.ntri) return;
+  const int m = d.trim[q], n = d.trin[q], par = (n - m) & 1;
+  const int rows = mode ? 2 : 1;
+  double2 a = make_double2(0, 0), b = a;
+  for (int jh = 0; jh < d.nh; jh++) {
+    const double2 *g = fold + static_cast<size_t>(jh) * rows * 2 * d.M;
+    a = cfma(a, g[par * d.M + m], d.Pa[static_cast<size_t>(jh) * d.ntri + q]);
+    if (mode) b = cfma(b, g[(2 + 1 - par) * d.M + m], d.Ha[static_cast<size_t>(jh) * d.ntri + q]);
+  }
+  spec[packed ? static_cast<size_t>(q) : static_cast<size_t>(m) * d.M + n] = mode ? csub(imul(a, static_cast<double>(m)), b) : a;
+}
+
+// F_m at both mirror latitudes of latitude pair jh from a spectrum in the reference layout (even n - m terms
+// first, then the odd ones), into the Phi slot of four[lat][4][M] (the inverse FFTs follow in sph_phi_grid)
+__global__ void sph_hook_synth(SphDev d, const double2 *__restrict__ spec, double2 *__restrict__ four) {
+  const int jh = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+  if (jh >= d.nh) return;
+  double2 se = make_double2(0, 0), so = se;
+  for (int n = m; n <= d.N; n++) {
+    const int q = d.tri[m] + n - m;
+    const double P = d.Ps[static_cast<size_t>(q) * d.nh + jh];
+    if ((n - m) & 1) so = cfma(so, spec[static_cast<size_t>(m) * d.M + n], P);
+    else se = cfma(se, spec[static_cast<size_t>(m) * d.M + n], P);
+  }
+  const int js = jh, jn = d.nlat - 1 - jh;
+  four[(static_cast<size_t>(js) * 4 + 3) * d.M + m] = cadd(se, so);
+  four[(static_cast<size_t>(jn) * 4 + 3) * d.M + m] = csub(se, so);
 }
 
 const double kPi = 3.14159265358979323846;
@@ -932,6 +1025,7 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   const size_t nst = static_cast<size_t>(B) * 3 * ntri * 2;
   x0.alloc(nst);
   xs.alloc(nst);
+  if (p.precision == kSplitBF16) xs2.alloc(nst);
   acc.alloc(nst);
   four.alloc(static_cast<size_t>(B) * nlat * 4 * M * 2);
   fold.alloc(static_cast<size_t>(B) * nh * NSLOT * 2 * M * 2);
@@ -959,6 +1053,8 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
 
   }
   x0.zero(stream);
+  xs.zero(stream);
+  xs2.zero(stream);
   hsgrid.zero(stream);
   refgrid.zero(stream);
   allow_max_shared_memory();
@@ -1082,6 +1178,52 @@ void SphereEngine::set_state_grid(const double *h, const double *u, const double
   analyze_grids_to_state(member);
   t[member] = 0;
   mark_reference(member);
+}
+
+// cpp/sphere.cpp:138-149, 150-162, 164-177: the transforms of one field, through device scratch (the member-0
+// transform buffers, which every stage overwrites anyway)
+void SphereEngine::hook_analysis(const double *A, const double *Bg, size_t n, double *spec) {
+  if (n != ngrid()) throw InvalidArgument("grid size mismatch");
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  if (hookspec.n < 2 * nspec_ref()) hookspec.alloc(2 * nspec_ref());
+  SphDev d = make_sph(*this, *tab);
+  std::memcpy(hstage.p, A, n * sizeof(double));
+  if (Bg) std::memcpy(hstage.p + n, Bg, n * sizeof(double));
+  LMW_CUDA(cudaMemcpyAsync(gridin.p, hstage.p, (Bg ? 2 : 1) * n * sizeof(double), cudaMemcpyHostToDevice, stream));
+  LMW_CUDA(cudaMemsetAsync(hookspec.p, 0, hookspec.bytes(), stream));
+  const size_t smem = 2 * static_cast<size_t>(nlon) * sizeof(double2);
+  sph_hook_fold<<<nh, GRID_THREADS, smem, stream>>>(d, gridin.p, Bg ? gridin.p + n : nullptr, Bg ? 1 : 0, reinterpret_cast<double2 *>(fold.p));
+  sph_hook_analysis<<<(ntri + ANA_THREADS - 1) / ANA_THREADS, ANA_THREADS, 0, stream>>>(d, reinterpret_cast<const double2 *>(fold.p), Bg ? 1 : 0,
+                                                                                        reinterpret_cast<double2 *>(hookspec.p));
+  LMW_LAUNCH_CHECK();
+  g_launches += 2;
+  LMW_CUDA(cudaMemcpyAsync(hstage.p, hookspec.p, 2 * nspec_ref() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  std::memcpy(spec, hstage.p, 2 * nspec_ref() * sizeof(double));
+}
+
+void SphereEngine::analyze_scalar(const double *grid, size_t n, double *spec) { hook_analysis(grid, nullptr, n, spec); }
+
+void SphereEngine::analyze_divergence(const double *A, const double *Bg, size_t n, double *spec) {
+  if (!A || !Bg) throw InvalidArgument("analyze_divergence: null grid");
+  hook_analysis(A, Bg, n, spec);
+}
+
+void SphereEngine::synthesize_scalar(const double *spec, double *grid, size_t n) {
+  if (n != ngrid()) throw InvalidArgument("grid size mismatch");
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  if (hookspec.n < 2 * nspec_ref()) hookspec.alloc(2 * nspec_ref());
+  SphDev d = make_sph(*this, *tab);
+  std::memcpy(hstage.p, spec, 2 * nspec_ref() * sizeof(double));
+  LMW_CUDA(cudaMemcpyAsync(hookspec.p, hstage.p, 2 * nspec_ref() * sizeof(double), cudaMemcpyHostToDevice, stream));
+  sph_hook_synth<<<dim3((nh + 127) / 128, M), 128, 0, stream>>>(d, reinterpret_cast<const double2 *>(hookspec.p), reinterpret_cast<double2 *>(four.p));
+  const size_t smem = static_cast<size_t>(nlon) * sizeof(double2);
+  sph_phi_grid<<<dim3(nh, 1), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), gridin.p);
+  LMW_LAUNCH_CHECK();
+  g_launches += 2;
+  LMW_CUDA(cudaMemcpyAsync(hstage.p, gridin.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  std::memcpy(grid, hstage.p, n * sizeof(double));
 }
 
 void SphereEngine::to_packed(const double *ref, double *packed) {
@@ -1321,9 +1463,11 @@ static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage,
 
 // One RK4 stage in split precision: tensor-core synthesis, FP32 grid stage, tensor-core analysis with the RK4
 // update (which also packs the next stage's synthesis operands)
+// xs, xs2: the FP64 stage inputs the linear-exact form keeps, in turn (stage 0 writes xs, 1 reads xs and writes xs2,
+// 2 reads xs2 and writes xs, 3 reads xs): an analysis CTA reads neighbouring coefficients that other CTAs update
 static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan &sp, const double *kfac64, int B, int stage, double dt,
-                        const double *filt, float2 *fold, double2 *x0, double2 *xs, double2 *acc, const double *fgrid, const double *hsgrid,
-                        cudaStream_t stream, int which = -1) {
+                        const double *filt, float2 *fold, double2 *x0, double2 *xs, double2 *xs2, double2 *acc, const double *fgrid,
+                        const double *hsgrid, cudaStream_t stream, int which = -1) {
   SplitDev sd = split_dev(sp);
   sd.fold = fold;
   StageArgs sa;
@@ -1346,7 +1490,9 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
                                  : (sp.direct ? split_ana<false, true, 3> : split_ana<false, false, 3>))
                   : (sp.ana_both ? (sp.direct ? split_ana<true, true, 2> : split_ana<true, false, 2>)
                                  : (sp.direct ? split_ana<false, true, 2> : split_ana<false, false, 2>));
-    k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, nullptr, acc);
+    const double2 *xin = stage == 1 || stage == 3 ? xs : (stage == 2 ? xs2 : nullptr);
+    double2 *xout = !sp.lin_exact || stage == 3 ? nullptr : (stage == 1 ? xs2 : xs);
+    k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xin, xout, acc);
   }
 }
 
@@ -1372,7 +1518,7 @@ void SphereEngine::launch_stage(int stage, double dt) {
                          X0, XS, AC, fgrid.p, hsgrid.p, stream);
     g_launches += 3;
   } else {
-    split_stage(d, tab32(*tab), *split, tab->kfac.p, B, stage, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, AC, fgrid.p,
+    split_stage(d, tab32(*tab), *split, tab->kfac.p, B, stage, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, XS2(), AC, fgrid.p,
                 hsgrid.p, stream);
     g_launches += 3;
   }
@@ -1425,19 +1571,21 @@ void SphereEngine::set_tracer_grid(const double *qg, size_t n, int member) {
   check_member(*this, member);
   if (n != ngrid()) throw InvalidArgument("grid size mismatch");
   ensure_tracer();
-  const HostTables &h = tab->host;
-  // analyze_scalar, cpp/sphere.cpp:138-149: spec_nm = sum_j w_j F_m(j) P_nm(j), F_m = FFT(row) / nlon
-  std::vector<cplx> spec(nspec_ref(), cplx(0, 0)), row(nlon);
-  for (int j = 0; j < nlat; j++) {
-    for (int k = 0; k < nlon; k++) row[k] = cplx(qg[static_cast<size_t>(j) * nlon + k], 0.0);
-    fft_host(row, -1);
-    for (int m = 0; m <= N; m++) {
-      const cplx fm = row[m] / static_cast<double>(nlon);
-      const cplx f = fm * h.w[j];
-      for (int nn = m; nn <= N; nn++) spec[static_cast<size_t>(m) * M + nn] += f * h.Pj(j, m, nn);
-    }
+  // analyze_scalar (cpp/sphere.cpp:138-149) on the device, straight into the member's packed tracer state
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  std::memcpy(hstage.p, qg, n * sizeof(double));
+  LMW_CUDA(cudaMemcpyAsync(gridin.p, hstage.p, n * sizeof(double), cudaMemcpyHostToDevice, stream));
+  SphDev d = make_sph(*this, *tab);
+  const size_t smem = 2 * static_cast<size_t>(nlon) * sizeof(double2);
+  sph_hook_fold<<<nh, GRID_THREADS, smem, stream>>>(d, gridin.p, nullptr, 0, reinterpret_cast<double2 *>(fold.p));
+  sph_hook_analysis<<<(ntri + ANA_THREADS - 1) / ANA_THREADS, ANA_THREADS, 0, stream>>>(
+      d, reinterpret_cast<const double2 *>(fold.p), 0, reinterpret_cast<double2 *>(tq0.p) + static_cast<size_t>(member) * ntri, 1);
+  LMW_LAUNCH_CHECK();
+  g_launches += 2;
+  if (!has_tracer) {
+    has_tracer = true;
+    graphs_clear();
   }
-  set_tracer_state(reinterpret_cast<const double *>(spec.data()), member);
   synth_tracer_grid(member, refq.p + static_cast<size_t>(member) * ngrid());
   LMW_CUDA(cudaStreamSynchronize(stream));
 }
@@ -1548,7 +1696,7 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
       stage_kernels<float>(d, tab32(*tab), B, 1, dt, filt.p, X0, reinterpret_cast<float2 *>(four32.p), reinterpret_cast<float2 *>(fold32.p),
                            X0, XS, AC, fgrid.p, hsgrid.p, stream, which);
     else
-      split_stage(d, tab32(*tab), *split, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, AC, fgrid.p,
+      split_stage(d, tab32(*tab), *split, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, XS2(), AC, fgrid.p,
                   hsgrid.p, stream, which);
   };
   cudaEvent_t e0, e1;
@@ -1586,7 +1734,7 @@ void SphereEngine::autotune_split() {
   LMW_CUDA(cudaEventCreate(&e0));
   LMW_CUDA(cudaEventCreate(&e1));
   auto launch = [&](int which) {
-    split_stage(d, tab32(*tab), sp, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, AC, fgrid.p, hsgrid.p, stream,
+    split_stage(d, tab32(*tab), sp, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, XS2(), AC, fgrid.p, hsgrid.p, stream,
                 which);
     g_launches += 1;
   };
@@ -1739,6 +1887,15 @@ void SphereEngine::split_plan(int *out) const {
   out[6] = split ? split->direct : 0;
   out[7] = split ? split->ana_minb : 0;
   out[8] = split ? split->syn_split : 0;
+}
+
+void SphereEngine::set_split_form(int linear_exact) {
+  if (!split) throw InvalidArgument("the engine is not in split precision");
+  if (linear_exact != 0 && linear_exact != 1) throw InvalidArgument("split form: linear_exact must be 0 or 1");
+  LMW_CUDA(cudaStreamSynchronize(stream));
+  split->lin_exact = linear_exact;
+  split_packed = false;  // the synthesis operands of Phi_00 differ between the forms
+  graphs_clear();
 }
 
 void SphereEngine::set_split_plan(const int *in) {

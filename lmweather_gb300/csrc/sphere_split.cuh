@@ -67,6 +67,11 @@ struct SplitPlan {
   int ana_grid = 0;           // analysis CTAs (0: one per work item)
   int ana_minb = 2;           // analysis register budget: CTAs per SM (2 or 3)
   int ra_pair = 32;           // largest ra16[2m] + ra16[2m + 1]
+  // 1: the linear terms of the tendencies (gravity-wave terms of the mean height, the Laplacian of Phi, the
+  // untilted Coriolis terms) in FP64 spectral space; only the nonlinear products go through the BF16 pieces.
+  // 0: every term through the BF16 GEMMs (the plain split form)
+  int lin_exact = 1;
+  DevBuf<double> lin;         // per coefficient q: eps_{n+1} n/(n+1), eps_n (n+1)/n, m/(n(n+1)) (3 x ntri)
   size_t syn_stage_bytes = 0, syn_min_bytes = 0, ana_min_bytes = 0, ana_both_min_bytes = 0, budget_bytes = 0;
   size_t ana_res_bytes_v[2] = {0, 0}, ana_stage_bytes_v[2] = {0, 0};  // per variant: [0] gathered A, [1] streamed A
 };
@@ -81,6 +86,8 @@ struct SplitDev {
   float *dsyn;   // [member][jh][m][16]: U, V, zeta, Phi at the southern then the northern latitude (complex)
   float2 *fold;  // [m][slot][parity][member][jh]: folded analysis inputs
   int *err;
+  int lin_exact;        // see SplitPlan::lin_exact
+  const double *lin;    // [3][ntri]: the spectral Coriolis coefficients
 };
 
 namespace {
@@ -169,8 +176,12 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
   const int b_bytes = G.bR * bk * 2;
   const int stage_bytes = pieces * (a_bytes + b_bytes);
   const int total = G.nchunk[0] + G.nchunk[1];
-  __shared__ int s_fail;
-  if (tid == 0) s_fail = 0;
+  __shared__ int s_fail, s_issued, s_consumed;
+  if (tid == 0) {
+    s_fail = 0;
+    s_issued = 0;
+    s_consumed = 0;
+  }
   __syncthreads();
   if (tid == 0) {
     // producer: bulk copies of each (operand, chunk)
@@ -191,6 +202,7 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
         bulk_g2s(su32(base + pieces * a_bytes + p * b_bytes), G.b[g] + p * G.b_ps[g] + static_cast<long>(c) * G.b_cs, bbytes,
                  su32(&full[st]));
       }
+      s_issued = it + 1;
     }
   } else if (tid == 32) {
     // MMA issuer
@@ -208,6 +220,7 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
         ok = false;
         break;
       }
+      s_consumed = it + 1;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       uint8_t *base = pipe + st * stage_bytes;
       for (int kk = 0; kk < bk; kk += 16) {
@@ -229,12 +242,26 @@ __device__ bool run_two_gemm(const TwoGemm &G, int pieces, int terms, int ns, ui
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&empty[st])) : "memory");
     }
-    if (ok) asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(done)) : "memory");
+    // completes `done` once every MMA this thread issued has finished (also after a failed wait, so that the
+    // CTA can drain its own work before it frees tensor memory)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(done)) : "memory");
   }
   __syncthreads();
-  if (s_fail == 0 && tid == 0 && !mbar_wait_bounded(su32(done), done_phase)) {
-    s_fail = 1;
-    atomicExch(err, 4);
+  if (tid == 0) {
+    if (s_fail == 0) {
+      if (!mbar_wait_bounded(su32(done), done_phase)) {
+        s_fail = 1;
+        atomicExch(err, 4);
+      }
+    } else {
+      // a wait ran out: before the CTA returns (and frees its tensor memory and shared memory), wait a bounded
+      // time for its own MMAs and for the bulk copies it issued that no MMA consumed
+      tc::wait_for(su32(done), done_phase, 200000000ull);
+      for (int it = s_consumed; it < s_issued; it++) {
+        const int git = it0 + it;
+        tc::wait_for(su32(&full[git % ns]), (git / ns) & 1, 200000000ull);
+      }
+    }
   }
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -418,17 +445,20 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
     float2 A, Bv, UP, VP, PE;
     // the FP64 Coriolis and orography rows (tilted or mountain members only) are rounded to FP32 on the integer
     // pipe: the same values as the hardware conversion, without the narrow FP64 pipe
+    // linear-exact form: the untilted Coriolis parameter and Phi leave eta and Phi + E (their terms are added in
+    // FP64 spectral space by the analysis), and P is Phi' (the synthesis left out Phi_00)
+    const bool lx = sd.lin_exact != 0;
     {
-      const float eta = Z.x + ((gf & 1) ? d2f_int(fr_s[k]) : cor[2 * pr]);
+      const float eta = Z.x + ((gf & 1) ? d2f_int(fr_s[k]) : (lx ? 0.0f : cor[2 * pr]));
       const float hs = (gf & 2) ? d2f_int(hr_s[k]) : 0.0f;
       A.x = U.x * eta; Bv.x = V.x * eta; UP.x = U.x * P.x; VP.x = V.x * P.x;
-      PE.x = P.x + g * hs + (U.x * U.x + V.x * V.x) * r2om;
+      PE.x = (lx ? 0.0f : P.x) + g * hs + (U.x * U.x + V.x * V.x) * r2om;
     }
     {
-      const float eta = Z.y + ((gf & 1) ? d2f_int(fr_n[k]) : cor[2 * pr + 1]);
+      const float eta = Z.y + ((gf & 1) ? d2f_int(fr_n[k]) : (lx ? 0.0f : cor[2 * pr + 1]));
       const float hs = (gf & 2) ? d2f_int(hr_n[k]) : 0.0f;
       A.y = U.y * eta; Bv.y = V.y * eta; UP.y = U.y * P.y; VP.y = V.y * P.y;
-      PE.y = P.y + g * hs + (U.y * U.y + V.y * V.y) * r2om;
+      PE.y = (lx ? 0.0f : P.y) + g * hs + (U.y * U.y + V.y * V.y) * r2om;
     }
     rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
@@ -548,8 +578,10 @@ __device__ __forceinline__ void pack_syn_coef(const SphDev &d, const SplitDev &s
   const long baseP = sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kp;
   const long baseH = sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kp;
   const double kf = kfac[n];
+  // the linear-exact form synthesises Phi' = Phi - Phi_00 P_00: the mean enters the tendencies in FP64
+  const bool mean = sd.lin_exact && n == 0;
   const float v[8] = {d2f_int(z.x * kf), d2f_int(z.y * kf), d2f_int(dl.x * kf), d2f_int(dl.y * kf),
-                      d2f_int(z.x),      d2f_int(z.y),      d2f_int(f.x),       d2f_int(f.y)};
+                      d2f_int(z.x),      d2f_int(z.y),      mean ? 0.0f : d2f_int(f.x), mean ? 0.0f : d2f_int(f.y)};
 #pragma unroll
   for (int q = 0; q < 8; q++) fsplit(v[q], sd.aS_P + baseP + tile_off(ml * 8 + q, k, sd.rSP, sd.bks), sd.aSP_size, sd.pieces);
 #pragma unroll
@@ -573,8 +605,8 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict
 // shared memory admits three CTAs per SM)
 template <bool BOTH, bool DIRECT, int MINB>
 __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
-                                                             int B, int ns, double2 *__restrict__ x0, double2 *__restrict__ xs,
-                                                             double2 *__restrict__ acc) {
+                                                             int B, int ns, double2 *__restrict__ x0, const double2 *__restrict__ xin,
+                                                             double2 *__restrict__ xout, double2 *__restrict__ acc) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
@@ -756,8 +788,35 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
       const int q = d.tri[m] + n - m;
       if (q == 0) kz = kd = kf = make_float2(0, 0);
       const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
-      const double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
-                            make_double2(f2d_int(kf.x), f2d_int(kf.y))};
+      double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
+                      make_double2(f2d_int(kf.x), f2d_int(kf.y))};
+      if (sd.lin_exact && q != 0) {
+        // the linear terms in FP64 from the stage input y (x0 at stage 0, else the previous stage's output, a
+        // separate buffer: neighbouring n belong to other CTAs): n(n+1)/a^2 Phi_n in d delta; -Phi_mean delta_n in
+        // d Phi (D(U, V) = delta exactly for n <= T); for an untilted axis the Coriolis terms -D(f U, f V) and
+        // D(f V, -f U) with f = 2 Omega mu, which couple n - 1, n, n + 1 of the same m
+        const double2 *y = (sa.stage == 0 ? x0 : xin) + static_cast<size_t>(b) * 3 * d.ntri;
+        const int qq = q;
+        const double2 yz = y[qq], yd = y[d.ntri + qq], yf = y[2 * d.ntri + qq];
+        const double phibar = x0[static_cast<size_t>(b) * 3 * d.ntri + 2 * d.ntri].x * d.Ps[0];
+        const double lp = d.lapl[n];
+        k[1].x += lp * yf.x;
+        k[1].y += lp * yf.y;
+        k[2].x -= phibar * yd.x;
+        k[2].y -= phibar * yd.y;
+        if (!(d.gflag[b] & 1)) {
+          const double om = d.om2[b];
+          const double cA = sd.lin[qq], cB = sd.lin[d.ntri + qq], cC = sd.lin[2 * d.ntri + qq];
+          const double2 zu = n < d.N ? y[qq + 1] : make_double2(0, 0), du = n < d.N ? y[d.ntri + qq + 1] : make_double2(0, 0);
+          const double2 zl = n > m ? y[qq - 1] : make_double2(0, 0), dd = n > m ? y[d.ntri + qq - 1] : make_double2(0, 0);
+          // -D(fU, fV)_n = -2 Omega (cA delta_{n+1} + cB delta_{n-1} - i cC zeta_n)
+          k[0].x -= om * (cA * du.x + cB * dd.x + cC * yz.y);
+          k[0].y -= om * (cA * du.y + cB * dd.y - cC * yz.x);
+          // D(fV, -fU)_n = 2 Omega (cA zeta_{n+1} + cB zeta_{n-1} + i cC delta_n)
+          k[1].x += om * (cA * zu.x + cB * zl.x - cC * yd.y);
+          k[1].y += om * (cA * zu.y + cB * zl.y + cC * yd.x);
+        }
+      }
       // every load of the three fields is issued before any store (the buffers never alias)
       double2 xv[3], av[3];
 #pragma unroll
@@ -781,9 +840,9 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
           nv[f] = q == 0 ? val : cscale(val, fac);
           x0[i] = nv[f];
         }
-        // the stage input in FP64 is kept only when a caller asks for it (the split synthesis reads the packed
-        // operands written below)
-        if (xs != nullptr && sa.stage < 3) xs[i] = nv[f];
+        // the next stage input in FP64 is kept when a caller asks for it (the linear-exact form reads it; the
+        // split synthesis reads the packed operands written below)
+        if (xout != nullptr && sa.stage < 3) xout[i] = nv[f];
       }
       pack_syn_coef(d, sd, kfac, b, m, n, nv[0], nv[1], nv[2]);
     }
@@ -951,6 +1010,19 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   for (int m = 0; m <= N; m++) sp.ra_pair = std::max(sp.ra_pair, sp.ra16[2 * m] + sp.ra16[2 * m + 1]);
   sp.ana_both_min_bytes = static_cast<size_t>(sp.rAP) * (2 * sp.ra_pair + 1) * sizeof(float);
   sp.budget_bytes = budget;
+  // coefficients of the spectral Coriolis terms (eps of cpp/sphere.cpp:11): for q = (m, n), eps_{n+1} n/(n+1)
+  // (n < T), eps_n (n+1)/n (n > m) and m/(n(n+1)) (n >= 1)
+  std::vector<double> lin(3 * static_cast<size_t>(h.ntri), 0.0);
+  auto eps = [](int n, int m) { return std::sqrt(static_cast<double>(n * n - m * m) / static_cast<double>(4 * n * n - 1)); };
+  for (int m = 0; m <= N; m++)
+    for (int n = std::max(m, 1); n <= N; n++) {
+      const size_t q = static_cast<size_t>(h.tri[m] + n - m);
+      lin[q] = n < N ? eps(n + 1, m) * n / (n + 1.0) : 0.0;
+      lin[h.ntri + q] = n > m ? eps(n, m) * (n + 1.0) / n : 0.0;
+      lin[2 * h.ntri + q] = static_cast<double>(m) / (static_cast<double>(n) * (n + 1));
+    }
+  sp.lin.alloc(lin.size());
+  LMW_CUDA(cudaMemcpy(sp.lin.p, lin.data(), lin.size() * sizeof(double), cudaMemcpyHostToDevice));
 }
 
 inline SplitDev split_dev(const SplitPlan &sp) {
@@ -997,6 +1069,8 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.dsyn = sp.dsyn.p;
   s.fold = nullptr;
   s.err = sp.err.p;
+  s.lin_exact = sp.lin_exact;
+  s.lin = sp.lin.p;
   return s;
 }
 

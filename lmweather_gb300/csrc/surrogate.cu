@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(128, 1) mlp_gemm(GemmArgs g) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[S], empty[S], done;
   __shared__ uint32_t tslot;
-  __shared__ int fail;
+  __shared__ int fail, issued, consumed;
   constexpr int STAGE = (128 + BN) * BK * 2;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n0 = blockIdx.x * BN, m0 = blockIdx.y * 128;
@@ -77,6 +77,8 @@ __global__ void __launch_bounds__(128, 1) mlp_gemm(GemmArgs g) {
     tc::bar_init(tc::su32(&done), 1);
     tc::bar_init_fence();
     fail = 0;
+    issued = 0;
+    consumed = 0;
   }
   tc::fence_before();
   __syncthreads();
@@ -98,6 +100,7 @@ __global__ void __launch_bounds__(128, 1) mlp_gemm(GemmArgs g) {
 #pragma unroll
       for (int j = 0; j < BN / 128; j++)
         tc::bulk_g2s(tc::su32(base + (j + 1) * TILE * 2), g.B + (static_cast<long>((n0 >> 7) + j) * nk + it) * TILE, TILE * 2, bar);
+      issued = it + 1;
     }
   } else if (tid == 32) {
     const uint32_t idesc = tc::idesc_m128(BN);
@@ -110,6 +113,7 @@ __global__ void __launch_bounds__(128, 1) mlp_gemm(GemmArgs g) {
         ok = false;
         break;
       }
+      consumed = it + 1;
       tc::fence_after();
       const uint32_t base = tc::su32(smem + st * STAGE);
 #pragma unroll
@@ -117,12 +121,23 @@ __global__ void __launch_bounds__(128, 1) mlp_gemm(GemmArgs g) {
         tc::mma(tmem, tc::chunk_desc(base + kk * 256), tc::chunk_desc(base + TILE * 2 + kk * 256), idesc, (it | kk) != 0 ? 1u : 0u);
       tc::commit(tc::su32(&empty[st]));
     }
-    if (ok) tc::commit(tc::su32(&done));
+    // completes `done` when every MMA issued so far has finished (after a failed wait too: the CTA drains its
+    // own work before it frees tensor memory)
+    tc::commit(tc::su32(&done));
   }
   __syncthreads();
-  if (tid == 0 && !fail && !tc::wait(tc::su32(&done), 0)) {
-    fail = 1;
-    atomicExch(g.err, 3);
+  if (tid == 0) {
+    if (!fail) {
+      if (!tc::wait(tc::su32(&done), 0)) {
+        fail = 1;
+        atomicExch(g.err, 3);
+      }
+    } else {
+      // a wait ran out: wait a bounded time for the MMAs in flight and for the bulk copies issued but not
+      // consumed, so that none lands after the CTA has released its shared and tensor memory
+      tc::wait_for(tc::su32(&done), 0, 200000000ull);
+      for (int it = consumed; it < issued; it++) tc::wait_for(tc::su32(&full[it % S]), (it / S) & 1, 200000000ull);
+    }
   }
   __syncthreads();
   tc::fence_after();
@@ -280,6 +295,8 @@ struct AdamArgs {
   float lr, b1, b2, eps, c1, c2;
   int update;
   const float *scale;  // gradient scale from the clipping kernel (null: 1)
+  float *ema;          // exponential moving average of the master weights (null: none), decay ema_decay
+  float ema_decay;
 };
 
 // Adam on a 64 x 64 tile of W [nout][nin] (FP32 row-major), then the BF16 blocked copies W [nout][nin] and
@@ -299,6 +316,7 @@ __global__ void adam_tile(AdamArgs a) {
       a.m[i] = m;
       a.v[i] = v;
       a.w[i] = w;
+      if (a.ema) a.ema[i] = a.ema_decay * a.ema[i] + (1.0f - a.ema_decay) * w;
     }
     s[rr][cc] = __float2bfloat16_rn(w);
   }
@@ -317,7 +335,7 @@ __global__ void adam_tile(AdamArgs a) {
 }
 
 __global__ void adam_vec(float *w, float *m, float *v, const float *g, int n, float lr, float b1, float b2, float eps, float c1, float c2,
-                         const float *scale) {
+                         const float *scale, float *ema, float ema_decay) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float gi = g[i] * (scale ? *scale : 1.0f);
@@ -326,6 +344,7 @@ __global__ void adam_vec(float *w, float *m, float *v, const float *g, int n, fl
   w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
   m[i] = mi;
   v[i] = vi;
+  if (ema) ema[i] = ema_decay * ema[i] + (1.0f - ema_decay) * w[i];
 }
 
 // sum of squares of n values into *acc (double)
@@ -655,15 +674,44 @@ void Mlp::adam(double lr, double beta1, double beta2, double eps, double clip_ra
   }
   for (int l = 0; l < NL; l++) {
     Layer &Ly = L[l];
+    const bool avg = ema_decay > 0 && Ly.we.p != nullptr;
     AdamArgs a{Ly.w.p, Ly.m.p, Ly.v.p, Ly.gw.p, Ly.wb.p, Ly.wt.p, Ly.nout, Ly.nin, static_cast<float>(lr), static_cast<float>(beta1), static_cast<float>(beta2),
-               static_cast<float>(eps), c1, c2, 1, scale};
+               static_cast<float>(eps), c1, c2, 1, scale, avg ? Ly.we.p : nullptr, static_cast<float>(ema_decay)};
     adam_tile<<<dim3(Ly.nin / 64, Ly.nout / 64), 256, 0, stream>>>(a);
     LMW_LAUNCH_CHECK();
     adam_vec<<<(Ly.nout + 255) / 256, 256, 0, stream>>>(Ly.b.p, Ly.mb.p, Ly.vb.p, Ly.gb.p, Ly.nout, static_cast<float>(lr), static_cast<float>(beta1),
-                                                       static_cast<float>(beta2), static_cast<float>(eps), c1, c2, scale);
+                                                       static_cast<float>(beta2), static_cast<float>(eps), c1, c2, scale, avg ? Ly.be.p : nullptr,
+                                                       static_cast<float>(ema_decay));
     LMW_LAUNCH_CHECK();
     g_launches += 2;
   }
+}
+
+// averaged weights: the moving average starts at the present master weights; ema_apply makes the average the
+// network's weights (master and BF16 copies)
+void Mlp::ema_begin(double decay) {
+  if (!(decay > 0 && decay < 1)) throw InvalidArgument("the averaging decay must lie in (0, 1)");
+  ema_decay = decay;
+  for (int l = 0; l < NL; l++) {
+    Layer &Ly = L[l];
+    if (!Ly.we.p) {
+      Ly.we.alloc(Ly.w.n);
+      Ly.be.alloc(Ly.b.n);
+    }
+    LMW_CUDA(cudaMemcpyAsync(Ly.we.p, Ly.w.p, Ly.w.bytes(), cudaMemcpyDeviceToDevice, stream));
+    LMW_CUDA(cudaMemcpyAsync(Ly.be.p, Ly.b.p, Ly.b.bytes(), cudaMemcpyDeviceToDevice, stream));
+  }
+}
+
+void Mlp::ema_apply() {
+  if (!(ema_decay > 0)) return;
+  for (int l = 0; l < NL; l++) {
+    Layer &Ly = L[l];
+    LMW_CUDA(cudaMemcpyAsync(Ly.w.p, Ly.we.p, Ly.w.bytes(), cudaMemcpyDeviceToDevice, stream));
+    LMW_CUDA(cudaMemcpyAsync(Ly.b.p, Ly.be.p, Ly.b.bytes(), cudaMemcpyDeviceToDevice, stream));
+    publish(l);
+  }
+  ema_decay = 0;
 }
 
 double Mlp::take_grad_norm_sum() {
@@ -795,23 +843,59 @@ __global__ void pair_stats(const float *__restrict__ snaps, int nwin, int dp, lo
   o[2] = d2;
 }
 
-// batch of pairs -> normalised BF16 input (blocked) and normalised increments (row-major FP32)
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// batch of pairs -> normalised BF16 input (blocked) and normalised increments (row-major FP32). With aug_seed != 0
+// every pair is first mapped by a symmetry of the untilted shallow-water equations, the same for state and
+// successor (the dynamics commute with both): a rotation about the polar axis by a random angle a (coefficient
+// (m, n) times e^{i m a}) and, for half of the pairs, the reflection mu -> -mu (Phi and delta coefficients times
+// (-1)^(n-m), zeta's times -(-1)^(n-m): vorticity is odd under the reflection, as the Coriolis parameter is).
+// fmq[f]: feature f's m, n - m and field (packed m | (n - m) << 8 | field << 16) for the complex pair it belongs to.
 __global__ void gather_pairs(const float *__restrict__ snaps, const int *__restrict__ idx, int nwin, int dp, int nfeat, const float *__restrict__ mu,
                              const float *__restrict__ isig, const float *__restrict__ sigd, const float *__restrict__ outmask, bf16 *__restrict__ x0,
-                             float *__restrict__ target) {
+                             float *__restrict__ target, const int *__restrict__ fmq = nullptr, uint64_t aug_seed = 0) {
   const int b = blockIdx.x;
   const long p = idx[b];
   const long traj = p / nwin, w = p % nwin;
   const float *xs = snaps + (traj * (nwin + 1) + w) * dp, *xn = xs + dp;
+  const uint64_t r = aug_seed ? mix64(aug_seed + 0x9E3779B97F4A7C15ULL * static_cast<uint64_t>(b + 1)) : 0;
+  const float turn = static_cast<float>(r >> 40) * (1.0f / 16777216.0f);  // a / (2 pi), 24 random bits
+  const bool reflect = aug_seed && ((r >> 7) & 1);
   for (int f8 = threadIdx.x * 8; f8 < dp; f8 += blockDim.x * 8) {
     uint4 val;
     bf16 *pv = reinterpret_cast<bf16 *>(&val);
+    float xv[8], dv[8];
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       const int f = f8 + j;
-      const float x = xs[f];
-      pv[j] = __float2bfloat16_rn(f < nfeat ? (x - mu[f]) * isig[f] : 0.0f);
-      if (target) target[static_cast<long>(b) * dp + f] = outmask[f] > 0.0f ? (xn[f] - x) / sigd[f] : 0.0f;
+      xv[j] = f < nfeat ? xs[f] : 0.0f;
+      dv[j] = f < nfeat ? xn[f] - xs[f] : 0.0f;
+    }
+    if (aug_seed) {
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        const int f = f8 + j;
+        if (f >= nfeat) break;
+        const int code = fmq[f], m = code & 255, nm = (code >> 8) & 255, q = code >> 16;
+        float sn, cs;
+        sincospif(2.0f * turn * static_cast<float>(m), &sn, &cs);
+        const float sg = reflect ? (((nm & 1) ? -1.0f : 1.0f) * (q == 0 ? -1.0f : 1.0f)) : 1.0f;
+        const float xr = xv[j], xi = xv[j + 1], dr = dv[j], di = dv[j + 1];
+        xv[j] = sg * (xr * cs - xi * sn);
+        xv[j + 1] = sg * (xr * sn + xi * cs);
+        dv[j] = sg * (dr * cs - di * sn);
+        dv[j + 1] = sg * (dr * sn + di * cs);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int f = f8 + j;
+      pv[j] = __float2bfloat16_rn(f < nfeat ? (xv[j] - mu[f]) * isig[f] : 0.0f);
+      if (target) target[static_cast<long>(b) * dp + f] = outmask[f] > 0.0f ? dv[j] / sigd[f] : 0.0f;
     }
     *reinterpret_cast<uint4 *>(x0 + boff(b, f8, dp)) = val;
   }
@@ -952,6 +1036,16 @@ Surrogate::Surrogate(int truncation, int hidden_, uint64_t seed, double window_s
   outmask.alloc(dp);
   cw.alloc(dp);
   errs.alloc(2 * 1024);
+  // per feature: m, n - m and field, for the symmetry augmentation of training pairs
+  {
+    std::vector<int> code(dp, 0);
+    for (int q = 0; q < 3; q++)
+      for (int m = 0, tri = 0; m <= T; m++)
+        for (int n = m; n <= T; n++, tri++)
+          for (int ri = 0; ri < 2; ri++) code[(q * ntri + tri) * 2 + ri] = m | ((n - m) << 8) | (q << 16);
+    fmq.alloc(dp);
+    LMW_CUDA(cudaMemcpyAsync(fmq.p, code.data(), dp * sizeof(int), cudaMemcpyHostToDevice, stream));
+  }
   // Phi coefficient weights for the area-mean square of the height grid
   std::vector<float> c(dp, 0.0f);
   for (int m = 0, tri = 0; m <= T; m++)
@@ -1162,11 +1256,14 @@ SurrogateStats Surrogate::fit(int epochs, int batch, double lr, double lr_min, d
     std::shuffle(ids.begin(), ids.end(), rng);
     LMW_CUDA(cudaMemcpyAsync(order.p, ids.data(), ntrain * sizeof(int), cudaMemcpyHostToDevice, stream));
     for (int s = 0; s < spe; s++, step++) {
+      // the trained network is the moving average of the weights over the second half of the steps
+      if (ema > 0 && step == total / 2) net->ema_begin(ema);
       const double warm = std::min(1.0, static_cast<double>(step + 1) / static_cast<double>(warmup));
       const double lr_t =
           warm * (lr_min + 0.5 * (lr - lr_min) * (1.0 + std::cos(M_PI * static_cast<double>(step) / static_cast<double>(std::max<long>(1, total)))));
+      const uint64_t aug = augment ? (shuffle_seed * 0x2545F4914F6CDD1DULL + static_cast<uint64_t>(step) + 1) | 1ULL : 0ULL;
       gather_pairs<<<batch, 256, 0, stream>>>(snaps.p, order.p + static_cast<long>(s) * batch, nwin, dp, nfeat, mu.p, sig.p, sigd.p, outmask.p, net->x0.p,
-                                              net->target.p);
+                                              net->target.p, fmq.p, aug);
       LMW_LAUNCH_CHECK();
       net->forward(batch);
       net->backward(batch);
@@ -1179,6 +1276,8 @@ SurrogateStats Surrogate::fit(int epochs, int batch, double lr, double lr_min, d
     // keep the host's copy of the order alive until the stream has consumed it
     LMW_CUDA(cudaStreamSynchronize(stream));
   }
+  net->ema_apply();
+  LMW_CUDA(cudaStreamSynchronize(stream));
   st.seconds = seconds_since(t0);
   st.steps = static_cast<double>(total);
   st.train_loss = last_loss;
@@ -1345,10 +1444,20 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
       gc.members = g->n;
       gc.precision = kFP64;
       g->e = std::make_unique<SphereEngine>(gc);
-      copy_members_launch(check->device_state(), rows_d.p, g->e->device_state(), nullptr, g->n, nfeat, check->stream);
-      copy_members_launch(check->device_state(), rows_d.p, rs_state.p, g->ids.p, g->n, nfeat, check->stream);
+      if (check_precision == kFP64) {
+        copy_members_launch(check->device_state(), rows_d.p, g->e->device_state(), nullptr, g->n, nfeat, check->stream);
+        LMW_CUDA(cudaStreamSynchronize(check->stream));
+        g->e->state_written();
+      } else {
+        // the check ran in reduced precision: plain FP64 RK4 recomputes the window of the members it takes over
+        copy_members_launch(rs_start.p, g->ids.p, g->e->device_state(), nullptr, g->n, nfeat, check->stream);
+        LMW_CUDA(cudaStreamSynchronize(check->stream));
+        g->e->state_written();
+        rk4_window(*g->e);
+        LMW_CUDA(cudaStreamSynchronize(g->e->stream));
+      }
+      copy_members_launch(g->e->device_state(), nullptr, rs_state.p, g->ids.p, g->n, nfeat, check->stream);
       LMW_CUDA(cudaStreamSynchronize(check->stream));
-      g->e->state_written();
       taken += g->n;
       groups.push_back(std::move(g));
       LMW_CUDA(cudaMemcpyAsync(rs_mode.p, mode.data(), members * sizeof(int), cudaMemcpyHostToDevice, stream));

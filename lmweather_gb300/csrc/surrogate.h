@@ -31,6 +31,7 @@ class Mlp {
   struct Layer {
     int nin = 0, nout = 0;  // padded
     DevBuf<float> w, b, m, v, mb, vb, gw, gb;
+    DevBuf<float> we, be;  // moving averages of w and b (allocated by ema_begin)
     DevBuf<__nv_bfloat16> wb, wt;  // blocked W [nout][nin] and W^T [nin][nout]
   };
   Layer L[NL];
@@ -57,6 +58,11 @@ class Mlp {
   void backward(int batch);                // y, target, mask -> gradients; loss accumulated into loss_acc
   // clip_ratio > 0: the global gradient norm is clipped to clip_ratio times its running mean (on the device)
   void adam(double lr, double beta1, double beta2, double eps, double clip_ratio = 0.0);
+  // moving average of the master weights, updated by every adam() step from ema_begin on (decay per step);
+  // ema_apply() makes the average the network's weights and stops the averaging
+  double ema_decay = 0;
+  void ema_begin(double decay);
+  void ema_apply();
   double take_grad_norm_sum();             // synchronises; the summed gradient norms since the last call
   double take_loss();                      // synchronises; returns and clears the accumulated loss
   void check_status();
@@ -87,6 +93,12 @@ class Surrogate {
   int T = 42, ntri = 0, nfeat = 0, hidden = 4096;
   double window = 21600.0, dt = 900.0;
   double clip_ratio = 2.0;  // adaptive gradient clipping of training (0: off)
+  // training pairs mapped by a random symmetry of the untilted equations (a rotation about the polar axis and,
+  // for half of them, the equatorial reflection) each time they enter a batch
+  bool augment = true;
+  // decay of the moving average of the weights kept over the last half of a fit and used as the trained network
+  // (0: the last weights)
+  double ema = 0.9995;
   std::vector<double> hist_loss, hist_gnorm;  // per epoch of the last fit: mean loss and gradient norm per step
   SphereConfig cfg;
   std::unique_ptr<Mlp> net;
@@ -96,6 +108,7 @@ class Surrogate {
   int ntraj = 0, nwin = 0;
   DevBuf<float> snaps;
   DevBuf<float> mu, sig, sigd, outmask, cw;
+  DevBuf<int> fmq;  // per feature: m | (n - m) << 8 | field << 16
   DevBuf<int> idx;
   DevBuf<double> errs;
   bool have_norm = false;

@@ -78,6 +78,44 @@ int main() {
     threw = true;
   }
   EXPECT(threw, "tracer_at without a tracer is runtime_error");
+  // the transform test hooks through the C ABI, restating the reference's T21 round trip: a seeded spectrum is
+  // synthesised and analysed back to 1e-12; the divergence operator of the solid-body winds U = u cos(lat),
+  // V = 0 is zero, and D(V, -U) is the vorticity 2 u0 sin(lat) / a, which is (n, m) = (1, 0) alone
+  {
+    lg::Sphere s21(21, sp);
+    std::vector<lg::Sphere::cplx> spec(22 * 22, 0), back, div, vor;
+    unsigned seed = 5;
+    auto rnd = [&] {
+      seed = seed * 1664525u + 1013904223u;
+      return (seed >> 8) / 16777216.0 - 0.5;
+    };
+    for (int m = 0; m <= 21; m++)
+      for (int n = m; n <= 21; n++) spec[m * 22 + n] = lg::Sphere::cplx(rnd(), m == 0 ? 0.0 : rnd());
+    std::vector<double> g;
+    s21.synthesize_scalar(spec, g);
+    s21.analyze_scalar(g, back);
+    double worst = 0;
+    for (size_t i = 0; i < spec.size(); i++) worst = std::max(worst, std::abs(back[i] - spec[i]));
+    EXPECT(worst < 1e-12, "T21 spectral round trip through the hooks");
+    const int nl = s21.nlat(), nn = s21.nlon();
+    std::vector<double> U(nl * nn), V(nl * nn, 0.0), mU(nl * nn);
+    for (int j = 0; j < nl; j++)
+      for (int k = 0; k < nn; k++) {
+        U[j * nn + k] = 10 * std::cos(s21.lat(j)) * std::cos(s21.lat(j));
+        mU[j * nn + k] = -U[j * nn + k];
+      }
+    s21.analyze_divergence(U, V, div);
+    s21.analyze_divergence(V, mU, vor);
+    double dmax = 0;
+    for (const auto &c : div) dmax = std::max(dmax, std::abs(c));
+    EXPECT(dmax < 1e-18, "solid-body winds have no divergence");
+    // zeta = 2 u0 mu / a = (2 u0 / a) sqrt(2/3) P_1^0(mu) with P_1^0 = sqrt(3/2) mu
+    EXPECT(std::fabs(vor[1].real() - 2 * 10 / sp.radius * std::sqrt(2.0 / 3.0)) < 1e-12 * 2 * 10 / sp.radius, "solid-body vorticity");
+    double rest = 0;
+    for (size_t i = 0; i < vor.size(); i++)
+      if (i != 1) rest = std::max(rest, std::abs(vor[i]));
+    EXPECT(rest < 1e-12 * 2 * 10 / sp.radius, "solid-body vorticity has one mode");
+  }
   // plane: mass conservation and element accessors
   lg::PlaneParams pp;
   pp.nx = 64;

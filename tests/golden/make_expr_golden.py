@@ -3,9 +3,10 @@
 lmweather's builders compile expression strings with lmnum::Expr (cpp/expr.hpp, a header with no dependencies).
 This script writes a small C++ driver, compiles it here against that header where it lies in the reference
 checkout, evaluates every case below with it and records the result bits (C99 hex float) or the exact error text.
-It runs only where the reference checkout exists; the fixture it writes is committed so the tests need neither.
+It runs only where the reference checkout exists (given as the argument, or $LMW_REFERENCE_DIR, or a checkout named
+`reference` beside this repository); the fixture it writes is committed so the tests need neither.
 
-    python tests/golden/make_expr_golden.py
+    python tests/golden/make_expr_golden.py [<lmweather checkout>]
 """
 from __future__ import annotations
 
@@ -16,7 +17,8 @@ import sys
 import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_CPP = "/root/reference/cpp"
+sys.path.insert(0, os.path.dirname(HERE))
+from oracle_lib import reference_dir  # noqa: E402
 OUT = os.path.join(HERE, "expr_cases.json")
 
 DRIVER = r"""
@@ -73,8 +75,10 @@ CASES = [
 
 
 def main() -> None:
-    if not os.path.isdir(REF_CPP):
+    ref = sys.argv[1] if len(sys.argv) > 1 else reference_dir()
+    if not ref or not os.path.isfile(os.path.join(ref, "cpp", "expr.hpp")):
         sys.exit("the reference checkout is absent: the committed fixture stands")
+    REF_CPP = os.path.join(ref, "cpp")
     with tempfile.TemporaryDirectory() as d:
         src = os.path.join(d, "expr_driver.cpp")
         exe = os.path.join(d, "expr_driver")

@@ -16,6 +16,16 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 _lock = threading.Lock()
 
+
+def reference_dir() -> str | None:
+    """The lmweather checkout the reference-side checks read: $LMW_REFERENCE_DIR, else a checkout named `reference`
+    beside this repository; None when neither holds cpp/sphere.cpp (the checks that need it are skipped and the
+    committed golden fixtures, made by the reference, stand in)."""
+    for cand in (os.environ.get("LMW_REFERENCE_DIR"), os.path.join(os.path.dirname(ROOT), "reference")):
+        if cand and os.path.exists(os.path.join(cand, "cpp", "sphere.cpp")):
+            return os.path.abspath(cand)
+    return None
+
 D = C.c_double
 I = C.c_int
 P = C.c_void_p
@@ -32,9 +42,10 @@ def _dp(a: np.ndarray | None):
 
 def build_oracle(with_ref: bool = True) -> None:
     """Compile the oracle (and the reference harness where the reference checkout exists)."""
-    target = "all" if with_ref else "oracle"
+    ref = reference_dir() if with_ref else None
+    target = "all" if ref else "oracle"
     with _lock:
-        subprocess.run(["make", "-s", "-C", ORACLE_DIR, target], check=True)
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, target] + ([f"REF={ref}"] if ref else []), check=True)
 
 
 _ORACLE = None

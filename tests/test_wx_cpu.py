@@ -13,10 +13,11 @@ import subprocess
 import pytest
 
 from lmweather_gb300.wx import Wx, WxError, eval_expression
+from oracle_lib import reference_dir
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-REF = "/root/reference"
+REF = reference_dir() or ""
 # sha256 of lmweather 0.1.4's schema/lmweather.dsl.json (12,049 bytes: 8 Wx, 44 Sphere and 29 Plane methods)
 SCHEMA_SHA256 = "62a74d57af48db2325d29b44ccf5e7d9546820c3f56e5a5d321d1fbaa99ac21b"
 

@@ -42,8 +42,11 @@ def test_noalloc_step_matches_handle_step_on_two_calls(engine):
     th, tu, tv = (torch.from_numpy(x.copy()).cuda() for x in (h0, u0, v0))
     torch.cuda.synchronize()
     for call in range(2):
+        allocs = engine.alloc_count()
         _call(f, engine, th, tu, tv, 60.0, 7)
         torch.cuda.synchronize()
+        # the library made no device or pinned-host allocation during the call
+        assert engine.alloc_count() == allocs, call
         for _ in range(7):
             ref.step(60.0)
         h, u, v = ref.get()
@@ -51,6 +54,28 @@ def test_noalloc_step_matches_handle_step_on_two_calls(engine):
         assert np.array_equal(th.cpu().numpy(), h), call
         assert np.array_equal(tu.cpu().numpy(), u), call
         assert np.array_equal(tv.cpu().numpy(), v), call
+
+
+def test_noalloc_clears_the_wall_rows_of_v(engine):
+    # rows 0 and ny of v are walls; a caller's nonzero values there are cleared before the first step, so the
+    # result equals the handle's step from the same interior state
+    torch = pytest.importorskip("torch")
+    f = _noalloc(engine.load_library())
+    ref = engine.Plane(NX, NY, LX, LY, **PARAMS)
+    ref.jet(20.0, 5.0e4, 0.1, 5)
+    h0, u0, v0 = ref.get()
+    vbad = v0.copy()
+    vbad[0, :] = 1.0
+    vbad[-1, :] = -2.0
+    th, tu, tv = (torch.from_numpy(x.copy()).cuda() for x in (h0, u0, vbad))
+    _call(f, engine, th, tu, tv, 60.0, 3)
+    torch.cuda.synchronize()
+    for _ in range(3):
+        ref.step(60.0)
+    h, u, v = ref.get()
+    assert np.array_equal(th.cpu().numpy(), h)
+    assert np.array_equal(tu.cpu().numpy(), u)
+    assert np.array_equal(tv.cpu().numpy(), v)
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch(engine):
