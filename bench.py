@@ -354,7 +354,11 @@ def run_ours(args, rank, world, local):
             e0 = torch.cuda.Event(enable_timing=True)
             e0.record(torch.cuda.current_stream())
             torch.cuda.current_stream().synchronize()
+            if k == 0:
+                lw.profiler_range(True)  # a profiler run with --profile-from-start off captures the first timed run
             ens.run(seconds)
+            if k == 0:
+                lw.profiler_range(False)
             ends = []
             for st in streams:
                 e = torch.cuda.Event(enable_timing=True)
@@ -492,6 +496,15 @@ def run_ours(args, rank, world, local):
                          f"({r['member_days']:.3f} member-days), in the workload's proportions of member-steps per truncation",
                "member_steps": {str(k): v for k, v in r["member_steps"].items()}}
 
+    # the like-for-like figure: the same ensemble in FP64 on the GPU against the FP64 CPU arm
+    like = None
+    fp64_value = next((w["value"] for w in workloads if w.get("config") == "3: ensemble in fp64"), None)
+    if args.precision == "fp64":
+        fp64_value = value
+    if cpu is not None and fp64_value:
+        like = {"gpu_fp64": fp64_value, "cpu_fp64": cpu["value"], "ratio": fp64_value / cpu["value"], "unit": "member-sim-days/s",
+                "what": "the same 1024-member ensemble in FP64 on the GPU (one 2-day run) against the CPU baseline above"}
+
     clocks = clk.summary()
     if rank == 0:
         cfg = dict(WORKLOAD)
@@ -505,7 +518,7 @@ def run_ours(args, rank, world, local):
                 if args.precision.startswith("split") else args.precision,
                 "data": "synthetic (seeded balanced turbulence)", "config": cfg,
                 "e2e": {"value": e2e, "unit": "member-sim-days/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
-                "gpu_launches": int(launches), "error": errs, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "gpu_launches": int(launches), "error": errs, "roofline": roofline, "cpu_baseline": cpu, "like_for_like": like, "clocks": clocks,
                 "workloads": workloads}
         print(json.dumps(line), flush=True)
     ens.close()
@@ -539,17 +552,22 @@ def other_workloads(lw, lib, args, ens):
     p = lw.Plane(1024, 512, 1024 * 5000.0, 512 * 5000.0, f0=1e-4, beta=1.6e-11, gravity=9.81, depth=100.0)
     p.jet(20.0, 1.0e5, 0.1, 1)
     p.run(64 * 60.0, 60.0)
+    p.jet(20.0, 1.0e5, 0.1, 1)
     t0 = time.perf_counter()
-    p.run(1024 * 60.0, 60.0)
+    p.run(5000 * 60.0, 60.0)
     el = time.perf_counter() - t0
-    out.append({"config": "1: beta-plane 1024 x 512 C-grid FP64, dt 60 s", "value": 1024 * 60.0 / 86400.0 / el, "unit": "sim-days/s",
-                "parity": "bitwise identical to the reference (tests/test_plane_gpu.py)", "cpu_1core": cpu_single_rate("plane")})
+    out.append({"config": "1: beta-plane 1024 x 512 C-grid FP64, dt 60 s, 5000 steps", "value": 5000 * 60.0 / 86400.0 / el, "unit": "sim-days/s",
+                "parity": "bitwise identical to the reference's own 5000-step run (tests/test_plane_gpu.py, SHA-256 of h, u, v)",
+                "cpu_1core": cpu_single_rate("plane")})
     p.close()
     # config 2: T170 precision study, 2 model days
+    step_note = ("the configuration names 450 s (T170) and 225 s (T341); both exceed the reference's own RK4 limit for this "
+                 "state (316 s and 159 s; Sphere::run refuses them, cpp/sphere.cpp:463), so the study steps at 240 s and 150 s")
     res = precision_study(170, 2.0)
-    out.append({"config": "2: sphere T170 precision study, 2 model days at 240 s", **res, "cpu_1core_fp64": cpu_single_rate("t170", 3.0)})
+    out.append({"config": "2: sphere T170 precision study, 2 model days at 240 s", **res, "deviation": step_note,
+                "cpu_1core_fp64": cpu_single_rate("t170", 3.0)})
     res = precision_study(341, 2.0, modes=("fp64", "fp32", "split3", "split6"))
-    out.append({"config": "2: sphere T341 precision study, 2 model days at 150 s", **res})
+    out.append({"config": "2: sphere T341 precision study, 2 model days at 150 s", **res, "deviation": step_note})
     # config 4: the learned surrogate at T42 (bounded: see surrogate_workload)
     out.append(surrogate_workload(lw))
     # the ensemble in the other precisions (one 2-day run each)
@@ -659,7 +677,8 @@ def run_case(args) -> int:
     sphere), t85, t170, t341, plane (1024 x 512 beta-plane jet, dt 60 s), ens (an ensemble of --members spheres at
     --truncation, the groups of the benchmark ensemble; --plan forces split plan entries, e.g.
     analysis_stages=1,analysis_ctas_per_sm=3), mlp (training steps of the surrogate's network). One untimed warm-up
-    step runs first."""
+    step runs first; the stepped region is bracketed by cudaProfilerStart/Stop, so a profiler run with
+    --profile-from-start off captures only its launches."""
     import lmweather_gb300 as lw
     from lmweather_gb300 import build
 
@@ -668,9 +687,11 @@ def run_case(args) -> int:
         p = lw.Plane(1024, 512, 1024 * 5000.0, 512 * 5000.0, f0=1e-4, beta=1.6e-11, gravity=9.81, depth=100.0)
         p.jet(20.0, 1.0e5, 0.1, 1)
         p.step(60.0)
+        lw.profiler_range(True)
         t0 = time.perf_counter()
         for _ in range(args.case_steps):
             p.step(60.0)
+        lw.profiler_range(False)
         print(f"plane 1024x512: {args.case_steps} steps in {time.perf_counter() - t0:.4f} s")
         return 0
     if args.case == "mlp":
@@ -681,10 +702,12 @@ def run_case(args) -> int:
         x = rng.standard_normal((args.batch, 5676)).astype(np.float32)
         t = 0.1 * rng.standard_normal((args.batch, 5676)).astype(np.float32)
         net.backward(x, t)
+        lw.profiler_range(True)
         t0 = time.perf_counter()
         for _ in range(args.case_steps):
             net.backward(x, t)
             net.adam(1e-4)
+        lw.profiler_range(False)
         print(f"mlp 5676-4096x3-5676 batch {args.batch}: {args.case_steps} training steps in {time.perf_counter() - t0:.4f} s")
         return 0
     prec = {"fp64": lw.FP64, "fp32": lw.FP32, "split3": lw.SPLIT_BF16, "split6": lw.SPLIT_BF16}[args.precision]
@@ -700,9 +723,11 @@ def run_case(args) -> int:
             print("plan", s.split_plan())
         dt = 0.9 * min(s.stable_dt(1.5, member=b) for b in range(B))
         s.step(dt)
+        lw.profiler_range(True)
         t0 = time.perf_counter()
         for _ in range(args.case_steps):
             s.step(dt)
+        lw.profiler_range(False)
         print(f"ensemble T{T} x {B}: {args.case_steps} steps in {time.perf_counter() - t0:.4f} s")
         return 0
     T = {"t42": 42, "t85": 85, "t170": 170, "t341": 341}[args.case]
@@ -710,16 +735,19 @@ def run_case(args) -> int:
     s = lw.Sphere(T, diffusion=nu4(T), precision=prec, max_truncation=max(T, 170), split_terms=terms)
     s.turbulence(1, 8000.0, 30.0, T // 2)
     s.step(dt)
+    lw.profiler_range(True)
     t0 = time.perf_counter()
     for _ in range(args.case_steps):
         s.step(dt)
+    lw.profiler_range(False)
     print(f"sphere T{T}: {args.case_steps} steps in {time.perf_counter() - t0:.4f} s")
     return 0
 
 
 def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, epochs=100, batch=512, lr=3e-4, lr_min=3e-5,
                     hmin=8000.0, hmax=8000.0, members=1024, rollout_windows=80, check_every=4, threshold=1e-3, ref_windows=4, seed=1,
-                    check_precision=None, loss="energy", thresholds=(), clip=2.0, data_precision=0) -> dict:
+                    check_precision=None, loss="energy", thresholds=(), clip=2.0, data_precision=0, augment=True, averaging=0.9995,
+                    sym_average=8) -> dict:
     """The learned surrogate end to end: solver trajectories (balanced turbulence on training seeds, RK4 at 900 s,
     del^4 with a 1-day e-folding at n = T; pairs (state, state + 6 h) from every window; the last tenth of the
     trajectories held out) -> training on the GPU -> validation errors per 6-hour window -> a hybrid rollout of
@@ -732,6 +760,9 @@ def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, e
         check_precision = lw.SPLIT_BF16
     sur = lw.Surrogate(truncation, hidden=hidden, seed=seed)
     sur.set_clip(clip)
+    sur.set_augment(augment)
+    sur.set_averaging(averaging)
+    sur.set_symmetry_average(sym_average)
     gen_s = sur.generate(trajectories, windows, seed0=1_000_000 * seed, hmin=hmin, hmax=hmax, precision=data_precision)
     fit = sur.fit(epochs, batch=batch, lr=lr, lr_min=lr_min, val_fraction=0.1, seed=seed, loss=loss)
     hist_loss, _ = sur.history()
@@ -740,7 +771,8 @@ def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, e
            "trajectories": trajectories, "windows_per_trajectory": windows, "mean_height_range_m": [hmin, hmax],
            "data_precision": ["fp64", "fp32", "split3"][data_precision], "generate_s": gen_s, "loss": loss, "clip_ratio": clip,
            "epochs": epochs, "lr": [lr, lr_min], "fit": fit, "loss_by_epoch": [round(v, 4) for v in hist_loss.tolist()],
-           "train_step_ms": train_ms, "forward_ms_batch": fwd_ms, "batch": batch,
+           "train_step_ms": train_ms, "forward_ms_batch": fwd_ms, "batch": batch, "augment": augment, "averaging": averaging,
+           "symmetry_maps_averaged": sym_average,
            "check_precision": ["fp64", "fp32", "split3"][check_precision]}
     if members > 0 and rollout_windows > 0:
         r = sur.rollout(members, seed0=9_000_000 + seed, windows=rollout_windows, check_every=check_every, threshold=threshold,
@@ -787,6 +819,11 @@ def main():
     ap.add_argument("--threshold", type=float, default=1e-3)
     ap.add_argument("--check-precision", default="split3", choices=["fp64", "split3"])
     ap.add_argument("--sweep", default="", help="comma-separated extra take-over thresholds")
+    ap.add_argument("--augment", type=int, default=1, help="symmetry augmentation of the training pairs (1/0)")
+    ap.add_argument("--averaging", type=float, default=0.9995, help="weight averaging decay (0: last weights)")
+    ap.add_argument("--sym-average", type=int, default=8, help="symmetry maps averaged at inference (1: plain network)")
+    ap.add_argument("--lr-min", type=float, default=3e-5)
+    ap.add_argument("--data-precision", default="split3", choices=["fp64", "split3"])
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.case:
@@ -801,9 +838,11 @@ def main():
             import lmweather_gb300 as lw
 
             print(json.dumps(surrogate_study(42, trajectories=args.trajectories, windows=args.windows, epochs=args.epochs, batch=args.batch,
-                                             members=args.rollout_members, rollout_windows=args.rollout_windows, threshold=args.threshold,
-                                             check_precision=lw.SPLIT_BF16 if args.check_precision == "split3" else lw.FP64,
-                                             thresholds=tuple(float(v) for v in args.sweep.split(",") if v))))
+                                             lr_min=args.lr_min, members=args.rollout_members, rollout_windows=args.rollout_windows,
+                                             threshold=args.threshold, check_precision=lw.SPLIT_BF16 if args.check_precision == "split3" else lw.FP64,
+                                             thresholds=tuple(float(v) for v in args.sweep.split(",") if v), augment=bool(args.augment),
+                                             averaging=args.averaging, data_precision=2 if args.data_precision == "split3" else 0,
+                                             sym_average=args.sym_average)))
         return 0
     if args.impl == "reference":
         return run_reference(args, rank, world)

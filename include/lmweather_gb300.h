@@ -42,6 +42,9 @@ uint64_t lmw_launch_count(void);
  * all threads. No reference counterpart (accounting hook: lets a caller check that an entry point allocates
  * nothing). */
 uint64_t lmw_alloc_count(void);
+/* on != 0: cudaProfilerStart(), else cudaProfilerStop() -- the region a profiler started with
+ * --profile-from-start off captures. No reference counterpart (measurement hook). */
+int lmw_profiler_range(int on);
 
 /* The engine's split-BF16 tensor-core GEMM (tcgen05, FP32 accumulation in tensor memory) on one problem from
  * host arrays: D (128 x N) = A (128 x K) * B (N x K)^T with A and B split on the device into `terms` = 1 (BF16),
@@ -390,6 +393,12 @@ int lmw_surrogate_set_augment(lmw_surrogate *s, int on);
  * the second half of lmw_surrogate_fit's steps (the default, 0.9995); 0: the last weights. No reference
  * counterpart. */
 int lmw_surrogate_set_averaging(lmw_surrogate *s, double decay);
+/* maps = 1: the network advances a state as it is. maps = 2k (the default 8): the network is applied to the state
+ * under k rotations about the polar axis by multiples of 2 pi / k, each without and with the equatorial
+ * reflection, each increment is mapped back, and the 2k increments are averaged (the exact dynamics commute with
+ * these maps). Used by lmw_surrogate_advance, _rollout and the validation errors of _fit. No reference
+ * counterpart. */
+int lmw_surrogate_set_symmetry_average(lmw_surrogate *s, int maps);
 /* per epoch of the last fit: mean training loss and mean global gradient norm per step (count = epochs; at most
  * max values written) */
 int lmw_surrogate_history(lmw_surrogate *s, int max, double *loss, double *grad_norm, int *count);

@@ -46,6 +46,7 @@ _SIGS = {
     "lmw_ensemble_set_split_form": (_I, [_P, _I]),
     "lmw_launch_count": (C.c_uint64, []),
     "lmw_alloc_count": (C.c_uint64, []),
+    "lmw_profiler_range": (_I, [_I]),
     "lmw_sphere_create": (_I, [_I, _D, _D, _D, _D, _PP]),
     "lmw_sphere_create_ex": (_I, [_I, _D, _D, _D, _D, _I, _I, _I, _PP]),
     "lmw_sphere_create_split": (_I, [_I, _D, _D, _D, _D, _I, _I, _I, _PP]),
@@ -145,6 +146,7 @@ _SIGS = {
     "lmw_surrogate_set_clip": (_I, [_P, _D]),
     "lmw_surrogate_set_augment": (_I, [_P, _I]),
     "lmw_surrogate_set_averaging": (_I, [_P, _D]),
+    "lmw_surrogate_set_symmetry_average": (_I, [_P, _I]),
     "lmw_surrogate_history": (_I, [_P, _I, _DP, _DP, _IP]),
 }
 
@@ -167,6 +169,11 @@ def load_library() -> C.CDLL:
 
 def launch_count() -> int:
     return int(load_library().lmw_launch_count())
+
+
+def profiler_range(on: bool) -> None:
+    """Start (True) or stop (False) the region a profiler run with --profile-from-start off captures."""
+    _check(load_library().lmw_profiler_range(1 if on else 0))
 
 
 def alloc_count() -> int:
@@ -880,6 +887,10 @@ class Surrogate:
     def set_averaging(self, decay: float):
         """Moving average of the weights over the second half of fit() (decay per step; 0: the last weights)."""
         _check(self._lib.lmw_surrogate_set_averaging(self._h, decay))
+
+    def set_symmetry_average(self, maps: int):
+        """Average the network's increments over `maps` rotations/reflections of the input (1: the plain network)."""
+        _check(self._lib.lmw_surrogate_set_symmetry_average(self._h, maps))
 
     def set_augment(self, on: bool):
         """Random rotations about the polar axis and equatorial reflections of the training pairs (default on)."""

@@ -1,4 +1,6 @@
 // The C ABI (include/lmweather_gb300.h): exceptions become status codes, the message is kept per thread.
+#include <cuda_profiler_api.h>
+
 #include <cstdio>
 #include <exception>
 #include <new>
@@ -90,6 +92,9 @@ const char *lmw_last_error(void) { return g_err.c_str(); }
 const char *lmw_version(void) { return "lmweather-gb300 0.1.0"; }
 uint64_t lmw_launch_count(void) { return lmw::g_launches; }
 uint64_t lmw_alloc_count(void) { return lmw::alloc_counter().load(); }
+int lmw_profiler_range(int on) {
+  return guard([&] { LMW_CUDA(on ? cudaProfilerStart() : cudaProfilerStop()); });
+}
 int lmw_tc_gemm_selftest(const float *A, const float *B, float *D, int N, int K, int terms, int layout, int *kernel_status) {
   return guard([&] {
     need(A && B && D && kernel_status, "pointer is null");
@@ -779,6 +784,10 @@ int lmw_ensemble_split_plan(lmw_ensemble *e, int group, int *out) {
 }
 int lmw_surrogate_reset(lmw_surrogate *s, uint64_t seed) { return SUR(s, s->s->reset(seed)); }
 int lmw_surrogate_set_augment(lmw_surrogate *s, int on) { return SUR(s, s->s->augment = on != 0); }
+int lmw_surrogate_set_symmetry_average(lmw_surrogate *s, int maps) {
+  return SUR(s, need(maps == 1 || (maps >= 2 && maps <= 64 && maps % 2 == 0), "the symmetry maps must be 1 or an even number up to 64");
+             s->s->sym_average = maps);
+}
 int lmw_surrogate_set_averaging(lmw_surrogate *s, double decay) {
   return SUR(s, need(decay >= 0 && decay < 1, "the averaging decay must lie in [0, 1)"); s->s->ema = decay);
 }

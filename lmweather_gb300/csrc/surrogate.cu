@@ -849,22 +849,47 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
-// batch of pairs -> normalised BF16 input (blocked) and normalised increments (row-major FP32). With aug_seed != 0
-// every pair is first mapped by a symmetry of the untilted shallow-water equations, the same for state and
-// successor (the dynamics commute with both): a rotation about the polar axis by a random angle a (coefficient
-// (m, n) times e^{i m a}) and, for half of the pairs, the reflection mu -> -mu (Phi and delta coefficients times
-// (-1)^(n-m), zeta's times -(-1)^(n-m): vorticity is odd under the reflection, as the Coriolis parameter is).
-// fmq[f]: feature f's m, n - m and field (packed m | (n - m) << 8 | field << 16) for the complex pair it belongs to.
+// the map of row b: a random one per row (24 random bits of angle, one of reflection) when map.seed != 0
+__device__ __forceinline__ void sym_of_row(const SymMap &map, int b, float &t, bool &rf) {
+  if (map.seed) {
+    const uint64_t r = mix64(map.seed + 0x9E3779B97F4A7C15ULL * static_cast<uint64_t>(b + 1));
+    t = static_cast<float>(r >> 40) * (1.0f / 16777216.0f);
+    rf = (r >> 7) & 1;
+  } else {
+    t = map.turn;
+    rf = map.reflect != 0;
+  }
+}
+
+// coefficient (re, im) of a feature pair under the map: rotation by 2 pi t about the polar axis (sign < 0: the
+// inverse rotation) then, with rf, the equatorial reflection. code = m | (n - m) << 8 | field << 16.
+__device__ __forceinline__ void sym_apply(int code, float t, bool rf, float sign, float &re, float &im) {
+  const int m = code & 255, nm = (code >> 8) & 255, q = code >> 16;
+  float sn, cs;
+  sincospif(2.0f * t * static_cast<float>(m), &sn, &cs);
+  sn *= sign;
+  const float sg = rf ? (((nm & 1) ? -1.0f : 1.0f) * (q == 0 ? -1.0f : 1.0f)) : 1.0f;
+  const float xr = re, xi = im;
+  re = sg * (xr * cs - xi * sn);
+  im = sg * (xr * sn + xi * cs);
+}
+
+// batch of pairs -> normalised BF16 input (blocked) and normalised increments (row-major FP32). With fmq given
+// and a map other than the identity, every pair is first mapped by a symmetry of the untilted shallow-water
+// equations, the same for state and successor (the dynamics commute with it): a rotation about the polar axis
+// (coefficient (m, n) times e^{i m a}) and, with the reflection mu -> -mu, Phi and delta coefficients times
+// (-1)^(n-m) and zeta's times -(-1)^(n-m) (vorticity is odd under the reflection, as the Coriolis parameter is).
 __global__ void gather_pairs(const float *__restrict__ snaps, const int *__restrict__ idx, int nwin, int dp, int nfeat, const float *__restrict__ mu,
                              const float *__restrict__ isig, const float *__restrict__ sigd, const float *__restrict__ outmask, bf16 *__restrict__ x0,
-                             float *__restrict__ target, const int *__restrict__ fmq = nullptr, uint64_t aug_seed = 0) {
+                             float *__restrict__ target, const int *__restrict__ fmq = nullptr, SymMap map = SymMap()) {
   const int b = blockIdx.x;
   const long p = idx[b];
   const long traj = p / nwin, w = p % nwin;
   const float *xs = snaps + (traj * (nwin + 1) + w) * dp, *xn = xs + dp;
-  const uint64_t r = aug_seed ? mix64(aug_seed + 0x9E3779B97F4A7C15ULL * static_cast<uint64_t>(b + 1)) : 0;
-  const float turn = static_cast<float>(r >> 40) * (1.0f / 16777216.0f);  // a / (2 pi), 24 random bits
-  const bool reflect = aug_seed && ((r >> 7) & 1);
+  float turn = 0.0f;
+  bool reflect = false;
+  sym_of_row(map, b, turn, reflect);
+  const bool mapped = fmq != nullptr && (map.seed != 0 || map.turn != 0.0f || map.reflect != 0);
   for (int f8 = threadIdx.x * 8; f8 < dp; f8 += blockDim.x * 8) {
     uint4 val;
     bf16 *pv = reinterpret_cast<bf16 *>(&val);
@@ -875,20 +900,13 @@ __global__ void gather_pairs(const float *__restrict__ snaps, const int *__restr
       xv[j] = f < nfeat ? xs[f] : 0.0f;
       dv[j] = f < nfeat ? xn[f] - xs[f] : 0.0f;
     }
-    if (aug_seed) {
+    if (mapped) {
 #pragma unroll
       for (int j = 0; j < 8; j += 2) {
         const int f = f8 + j;
         if (f >= nfeat) break;
-        const int code = fmq[f], m = code & 255, nm = (code >> 8) & 255, q = code >> 16;
-        float sn, cs;
-        sincospif(2.0f * turn * static_cast<float>(m), &sn, &cs);
-        const float sg = reflect ? (((nm & 1) ? -1.0f : 1.0f) * (q == 0 ? -1.0f : 1.0f)) : 1.0f;
-        const float xr = xv[j], xi = xv[j + 1], dr = dv[j], di = dv[j + 1];
-        xv[j] = sg * (xr * cs - xi * sn);
-        xv[j + 1] = sg * (xr * sn + xi * cs);
-        dv[j] = sg * (dr * cs - di * sn);
-        dv[j + 1] = sg * (dr * sn + di * cs);
+        sym_apply(fmq[f], turn, reflect, 1.0f, xv[j], xv[j + 1]);
+        sym_apply(fmq[f], turn, reflect, 1.0f, dv[j], dv[j + 1]);
       }
     }
 #pragma unroll
@@ -914,9 +932,10 @@ __device__ double block_sum(double v, double *red) {
 
 // relative L2 height error of the network's prediction and of persistence, per pair (Phi coefficients weighted
 // 1 for m = 0 and 2 for m > 0: the area mean of the squared grid field)
+// inc: the predicted increments [count][dp] (un-normalised), or null for sigd * y
 __global__ void pair_errors(const float *__restrict__ snaps, const int *__restrict__ idx, int nwin, int dp, const float *__restrict__ y,
                             const float *__restrict__ sigd, const float *__restrict__ outmask, const float *__restrict__ cw, int count,
-                            double *__restrict__ err, double *__restrict__ pers) {
+                            double *__restrict__ err, double *__restrict__ pers, const float *__restrict__ inc = nullptr) {
   __shared__ double red[32];
   const int b = blockIdx.x;
   if (b >= count) return;
@@ -928,7 +947,9 @@ __global__ void pair_errors(const float *__restrict__ snaps, const int *__restri
     const double c = cw[f];
     if (c == 0.0) continue;
     const double x = xs[f], t = xn[f];
-    const double pred = x + (outmask[f] > 0.0f ? static_cast<double>(sigd[f]) * y[static_cast<long>(b) * dp + f] : 0.0);
+    const double pred = x + (outmask[f] > 0.0f ? (inc ? static_cast<double>(inc[static_cast<long>(b) * dp + f])
+                                                       : static_cast<double>(sigd[f]) * y[static_cast<long>(b) * dp + f])
+                                               : 0.0);
     num += c * (pred - t) * (pred - t);
     den += c * t * t;
     pn += c * (x - t) * (x - t);
@@ -942,30 +963,70 @@ __global__ void pair_errors(const float *__restrict__ snaps, const int *__restri
   }
 }
 
-// FP64 states [count][nfeat] -> normalised BF16 input rows (rows >= count zero)
+// FP64 states [count][nfeat] -> (mapped by `map` when fmq is given) normalised BF16 input rows (rows >= count zero)
 __global__ void pack_states(const double *__restrict__ st, int count, int nfeat, int dp, const float *__restrict__ mu, const float *__restrict__ isig,
-                            bf16 *__restrict__ x0) {
+                            bf16 *__restrict__ x0, const int *__restrict__ fmq = nullptr, SymMap map = SymMap()) {
   const int b = blockIdx.x;
+  float turn = 0.0f;
+  bool reflect = false;
+  sym_of_row(map, b, turn, reflect);
   for (int f8 = threadIdx.x * 8; f8 < dp; f8 += blockDim.x * 8) {
     uint4 val;
     bf16 *pv = reinterpret_cast<bf16 *>(&val);
+    float xv[8];
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       const int f = f8 + j;
-      pv[j] = __float2bfloat16_rn(b < count && f < nfeat ? static_cast<float>((st[static_cast<long>(b) * nfeat + f] - mu[f]) * isig[f]) : 0.0f);
+      xv[j] = b < count && f < nfeat ? static_cast<float>(st[static_cast<long>(b) * nfeat + f]) : 0.0f;
+    }
+    if (fmq) {
+#pragma unroll
+      for (int j = 0; j < 8; j += 2)
+        if (f8 + j < nfeat) sym_apply(fmq[f8 + j], turn, reflect, 1.0f, xv[j], xv[j + 1]);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int f = f8 + j;
+      pv[j] = __float2bfloat16_rn(b < count && f < nfeat ? (xv[j] - mu[f]) * isig[f] : 0.0f);
     }
     *reinterpret_cast<uint4 *>(x0 + boff(b, f8, dp)) = val;
   }
 }
 
-// x += sigd * y for the members still on the network (mode 0)
-__global__ void apply_increment(double *__restrict__ st, int count, int nfeat, int dp, const float *__restrict__ y, const float *__restrict__ sigd,
-                                const float *__restrict__ outmask, const int *__restrict__ mode) {
+// inc[b][f] (+)= weight * map^-1 (sigd * y) for rows b < count: the network's increment in the mapped frame taken
+// back to the state's frame (first != 0 overwrites)
+__global__ void accumulate_increment(const float *__restrict__ y, const float *__restrict__ sigd, const float *__restrict__ outmask, int count,
+                                     int nfeat, int dp, const int *__restrict__ fmq, SymMap map, float weight, int first, float *__restrict__ inc) {
+  const int b = blockIdx.x;
+  if (b >= count) return;
+  float turn = 0.0f;
+  bool reflect = false;
+  sym_of_row(map, b, turn, reflect);
+  for (int f = threadIdx.x * 2; f < dp; f += blockDim.x * 2) {
+    float re = 0.0f, im = 0.0f;
+    if (f < nfeat) {
+      re = outmask[f] > 0.0f ? sigd[f] * y[static_cast<long>(b) * dp + f] : 0.0f;
+      im = outmask[f + 1] > 0.0f ? sigd[f + 1] * y[static_cast<long>(b) * dp + f + 1] : 0.0f;
+      // the inverse map: the reflection is its own inverse and commutes with the rotations
+      sym_apply(fmq[f], turn, false, -1.0f, re, im);
+      if (reflect) sym_apply(fmq[f], 0.0f, true, 1.0f, re, im);
+      if (outmask[f] <= 0.0f) re = 0.0f;
+      if (outmask[f + 1] <= 0.0f) im = 0.0f;
+    }
+    float *o = inc + static_cast<long>(b) * dp + f;
+    o[0] = first ? weight * re : o[0] + weight * re;
+    o[1] = first ? weight * im : o[1] + weight * im;
+  }
+}
+
+// x += inc for the members still on the network (mode 0)
+__global__ void apply_increment(double *__restrict__ st, int count, int nfeat, int dp, const float *__restrict__ inc, const float *__restrict__ outmask,
+                                const int *__restrict__ mode) {
   const long total = static_cast<long>(count) * nfeat;
   for (long i = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; i < total; i += static_cast<long>(gridDim.x) * blockDim.x) {
     const int b = static_cast<int>(i / nfeat), f = static_cast<int>(i % nfeat);
     if (mode && mode[b]) continue;
-    if (outmask[f] > 0.0f) st[i] += static_cast<double>(sigd[f]) * static_cast<double>(y[static_cast<long>(b) * dp + f]);
+    if (outmask[f] > 0.0f) st[i] += static_cast<double>(inc[static_cast<long>(b) * dp + f]);
   }
 }
 
@@ -1036,7 +1097,8 @@ Surrogate::Surrogate(int truncation, int hidden_, uint64_t seed, double window_s
   outmask.alloc(dp);
   cw.alloc(dp);
   errs.alloc(2 * 1024);
-  // per feature: m, n - m and field, for the symmetry augmentation of training pairs
+  incbuf.alloc(static_cast<size_t>(net->max_batch) * dp);
+  // per feature: m, n - m and field, for the symmetry maps of training pairs and of inference
   {
     std::vector<int> code(dp, 0);
     for (int q = 0; q < 3; q++)
@@ -1199,10 +1261,16 @@ void Surrogate::evaluate(int p0, int p1, std::vector<double> &err, std::vector<d
     const int batch = (cnt + 127) / 128 * 128;
     for (int i = 0; i < batch; i++) ids[i] = s + std::min(i, cnt - 1);
     LMW_CUDA(cudaMemcpyAsync(idx.p, ids.data(), batch * sizeof(int), cudaMemcpyHostToDevice, stream));
-    gather_pairs<<<batch, 256, 0, stream>>>(snaps.p, idx.p, nwin, dp, nfeat, mu.p, sig.p, sigd.p, outmask.p, net->x0.p, nullptr);
-    LMW_LAUNCH_CHECK();
-    net->forward(batch);
-    pair_errors<<<cnt, 256, 0, stream>>>(snaps.p, idx.p, nwin, dp, net->y.p, sigd.p, outmask.p, cw.p, cnt, errs.p, errs.p + mb);
+    for (int k = 0; k < sym_average; k++) {
+      const SymMap map = sym_map(k);
+      gather_pairs<<<batch, 256, 0, stream>>>(snaps.p, idx.p, nwin, dp, nfeat, mu.p, sig.p, sigd.p, outmask.p, net->x0.p, nullptr, fmq.p, map);
+      LMW_LAUNCH_CHECK();
+      net->forward(batch);
+      accumulate_increment<<<batch, 256, 0, stream>>>(net->y.p, sigd.p, outmask.p, cnt, nfeat, dp, fmq.p, map, 1.0f / sym_average, k == 0,
+                                                      incbuf.p);
+      LMW_LAUNCH_CHECK();
+    }
+    pair_errors<<<cnt, 256, 0, stream>>>(snaps.p, idx.p, nwin, dp, net->y.p, sigd.p, outmask.p, cw.p, cnt, errs.p, errs.p + mb, incbuf.p);
     LMW_LAUNCH_CHECK();
     LMW_CUDA(cudaMemcpyAsync(h.data(), errs.p, 2 * mb * sizeof(double), cudaMemcpyDeviceToHost, stream));
     LMW_CUDA(cudaStreamSynchronize(stream));
@@ -1261,7 +1329,8 @@ SurrogateStats Surrogate::fit(int epochs, int batch, double lr, double lr_min, d
       const double warm = std::min(1.0, static_cast<double>(step + 1) / static_cast<double>(warmup));
       const double lr_t =
           warm * (lr_min + 0.5 * (lr - lr_min) * (1.0 + std::cos(M_PI * static_cast<double>(step) / static_cast<double>(std::max<long>(1, total)))));
-      const uint64_t aug = augment ? (shuffle_seed * 0x2545F4914F6CDD1DULL + static_cast<uint64_t>(step) + 1) | 1ULL : 0ULL;
+      SymMap aug;
+      aug.seed = augment ? (shuffle_seed * 0x2545F4914F6CDD1DULL + static_cast<uint64_t>(step) + 1) | 1ULL : 0ULL;
       gather_pairs<<<batch, 256, 0, stream>>>(snaps.p, order.p + static_cast<long>(s) * batch, nwin, dp, nfeat, mu.p, sig.p, sigd.p, outmask.p, net->x0.p,
                                               net->target.p, fmq.p, aug);
       LMW_LAUNCH_CHECK();
@@ -1289,19 +1358,37 @@ SurrogateStats Surrogate::fit(int epochs, int batch, double lr, double lr_min, d
   return st;
 }
 
+// the k-th of the sym_average maps of inference: rotations by multiples of 2 pi / (sym_average / 2), each without
+// and with the reflection (a single map: the identity)
+SymMap Surrogate::sym_map(int k) const {
+  SymMap m;
+  if (sym_average <= 1) return m;
+  const int nrot = sym_average / 2;
+  m.turn = static_cast<float>(k / 2) / static_cast<float>(nrot);
+  m.reflect = k & 1;
+  return m;
+}
+
 void Surrogate::advance_states(double *states, int count, const int *mode) {
   if (!have_norm) throw InvalidArgument("the network has no normalisation yet: fit it first");
   const int dp = net->dim[0], mb = net->max_batch;
   for (int s = 0; s < count; s += mb) {
     const int cnt = std::min(mb, count - s);
     const int batch = (cnt + 127) / 128 * 128;
-    pack_states<<<batch, 256, 0, stream>>>(states + static_cast<long>(s) * nfeat, cnt, nfeat, dp, mu.p, sig.p, net->x0.p);
+    for (int k = 0; k < sym_average; k++) {
+      const SymMap map = sym_map(k);
+      pack_states<<<batch, 256, 0, stream>>>(states + static_cast<long>(s) * nfeat, cnt, nfeat, dp, mu.p, sig.p, net->x0.p, fmq.p, map);
+      LMW_LAUNCH_CHECK();
+      net->forward(batch);
+      accumulate_increment<<<batch, 256, 0, stream>>>(net->y.p, sigd.p, outmask.p, cnt, nfeat, dp, fmq.p, map, 1.0f / sym_average, k == 0,
+                                                      incbuf.p);
+      LMW_LAUNCH_CHECK();
+      g_launches += 2;
+    }
+    apply_increment<<<grid_for(static_cast<long>(cnt) * nfeat, 256), 256, 0, stream>>>(states + static_cast<long>(s) * nfeat, cnt, nfeat, dp, incbuf.p,
+                                                                                      outmask.p, mode ? mode + s : nullptr);
     LMW_LAUNCH_CHECK();
-    net->forward(batch);
-    apply_increment<<<grid_for(static_cast<long>(cnt) * nfeat, 256), 256, 0, stream>>>(states + static_cast<long>(s) * nfeat, cnt, nfeat, dp, net->y.p,
-                                                                                      sigd.p, outmask.p, mode ? mode + s : nullptr);
-    LMW_LAUNCH_CHECK();
-    g_launches += 2;
+    g_launches += 1;
   }
 }
 

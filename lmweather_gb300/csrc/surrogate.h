@@ -80,6 +80,15 @@ void mlp_gemm_f32(const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, 
 // host row-major [rows][cols] FP32 -> BF16 blocked (cols padded to a multiple of 64, rows to 128) and back
 void to_blocked(const float *host, int rows, int cols, int rows_p, int cols_p, __nv_bfloat16 *dev, cudaStream_t s);
 
+// A symmetry map of the untilted shallow-water equations on spectral states: rotation by 2 pi `turn` about the polar
+// axis (coefficient (m, n) times e^{i m 2 pi turn}), then, with `reflect`, the equatorial reflection (Phi and delta
+// times (-1)^(n-m), zeta times -(-1)^(n-m)). seed != 0: a random map per batch row instead.
+struct SymMap {
+  uint64_t seed = 0;
+  float turn = 0.0f;
+  int reflect = 0;
+};
+
 struct SurrogateStats {
   double train_loss = 0, val_err_mean = 0, val_err_median = 0, val_err_p90 = 0, val_err_max = 0, val_persist_mean = 0, val_untrained_mean = 0;
   double seconds = 0, steps = 0;
@@ -109,6 +118,12 @@ class Surrogate {
   DevBuf<float> snaps;
   DevBuf<float> mu, sig, sigd, outmask, cw;
   DevBuf<int> fmq;  // per feature: m | (n - m) << 8 | field << 16
+  // inference averages the network's increments over this many symmetry maps of the input (rotations about the
+  // polar axis by multiples of 2 pi / (n / 2), each without and with the equatorial reflection), each increment
+  // mapped back to the state's frame; 1: the plain network
+  int sym_average = 8;
+  DevBuf<float> incbuf;  // averaged increments of one batch [batch][dp]
+  SymMap sym_map(int k) const;
   DevBuf<int> idx;
   DevBuf<double> errs;
   bool have_norm = false;

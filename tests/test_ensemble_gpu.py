@@ -3,6 +3,8 @@ member's guard failure stops the run with the reference's message."""
 import numpy as np
 import pytest
 
+from oracle_lib import OracleSphere
+
 pytestmark = pytest.mark.gpu
 
 A = 6.37122e6
@@ -29,6 +31,36 @@ def test_ensemble_members_match_single_runs(engine):
             scale = np.abs(b).max()
             assert np.abs(a - b).max() <= 1e-13 * scale
         assert ens.member_diagnostics(i)["mean_height"] == pytest.approx(heights[i], rel=1e-12)  # the recipe's mean
+
+
+def test_ensemble_members_against_oracle(engine, oracle_built):
+    # one member of each truncation of the benchmark ensemble, with the rotation rate scaled by 0.5 or 2 and mean
+    # heights other than 8000 m, against the oracle (the reference's algorithm in C, bitwise equal to it) from the
+    # member's initial state at the group's own step, for at least 64 steps of every group
+    tr = [85, 21, 42]
+    seeds = [7001, 7002, 7003]
+    heights = [6300.0, 9400.0, 5200.0]
+    omegas = [7.292e-5 * 2.0, 7.292e-5 * 0.5, 7.292e-5 * 2.0]
+    ens = engine.Ensemble(tr, seeds, heights, omegas, precision=engine.FP64)
+    start = [ens.member_state(i) for i in range(3)]
+    whole = ens.get_states()
+    ens.run(86400.0)  # a day at the groups' stable steps (each run takes them from the current states)
+    seconds = 65 * {g["truncation"]: g for g in ens.groups()}[21]["dt"]
+    ens.set_states(*whole)
+    ens.run(seconds)
+    groups = {g["truncation"]: g for g in ens.groups()}
+    assert all(g["steps"] >= 64 for g in groups.values()), groups
+    for i, T in enumerate(tr):
+        o = OracleSphere(T, omega=omegas[i], diffusion=nu4(T))
+        o.set_state(*start[i])
+        o.run(seconds, groups[T]["dt"])
+        got, ref = ens.member_state(i), o.get_state()
+        wind = max(np.abs(ref[0]).max(), np.abs(ref[1]).max())
+        ez, ed = np.abs(got[0] - ref[0]).max() / wind, np.abs(got[1] - ref[1]).max() / wind
+        ef = np.abs(got[2] - ref[2]).max() / np.abs(ref[2]).max()
+        print(f"T{T} member vs oracle after {groups[T]['steps']} steps: zeta {ez:.2e} delta {ed:.2e} Phi {ef:.2e}")
+        assert ez <= 1e-12 and ed <= 1e-12 and ef <= 1e-12, (T, ez, ed, ef)
+        assert ens.member_diagnostics(i)["energy"] == pytest.approx(o.diagnostics()["energy"], rel=1e-12)
 
 
 def test_ensemble_split_precision_close_to_fp64(engine):

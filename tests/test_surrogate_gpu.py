@@ -127,10 +127,14 @@ def test_advance_keeps_mass_and_is_per_member(trained, engine):
     assert not np.array_equal(out[0], st[0])
 
 
-def test_rollout_takeover_semantics(trained, engine):
+@pytest.mark.parametrize("check", ["fp64", "split3"])
+def test_rollout_takeover_semantics(trained, engine, check):
     sur, _ = trained
-    # threshold 0 and a check every window: every member is taken over at the first check, so the hybrid is RK4
-    r0 = sur.rollout(8, seed0=900, windows=3, check_every=1, threshold=0.0, ref_windows=1, hmin=7000.0, hmax=7000.0, with_states=True)
+    # threshold 0 and a check every window: every member is taken over at the first check, so the hybrid is plain
+    # FP64 RK4 (a split-precision check is only the judge: the window of a member it takes over is recomputed in FP64)
+    cp = engine.FP64 if check == "fp64" else engine.SPLIT_BF16
+    r0 = sur.rollout(8, seed0=900, windows=3, check_every=1, threshold=0.0, ref_windows=1, hmin=7000.0, hmax=7000.0, with_states=True,
+                     check_precision=cp)
     assert r0["taken_over"] == 8 and r0["checks"] == 3 and r0["frac_over"] == 1.0
     # a plain RK4 run of the same members ends in the same states bit for bit
     T = 21
