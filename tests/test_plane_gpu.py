@@ -48,6 +48,38 @@ def test_plane_nonlinear_viscous_run_bitwise(engine):
         assert d[k] == pytest.approx(ref, rel=1e-13, abs=1e-300), k
 
 
+def test_plane_config1_5000_steps_bitwise_against_reference_run(engine):
+    # the stated length of the configuration: 5000 RK4 steps of 60 s at 1024 x 512 from the seeded jet, compared with
+    # the reference's own run (tests/golden/make_plane_config1.py keeps SHA-256 digests of its h, u, v after 1000
+    # and 5000 steps; the plane's parity bar is bitwise)
+    import hashlib
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "plane_config1_5000.json")) as f:
+        g = json.load(f)
+
+    def digest(a):
+        return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+    nx, ny, L = g["nx"], g["ny"], g["dx"]
+    p = engine.Plane(nx, ny, nx * L, ny * L, **g["params"])
+    p.jet(*g["jet"])
+    h, u, v = p.get()
+    assert (digest(h), digest(u), digest(v)) == (g["initial"]["h"], g["initial"]["u"], g["initial"]["v"])
+    done = 0
+    for cp in g["checkpoints"]:
+        p.run((cp["steps"] - done) * g["dt"], g["dt"])
+        done = cp["steps"]
+        h, u, v = p.get()
+        assert h[256, 512] == cp["samples"]["h[256,512]"] and u[128, 100] == cp["samples"]["u[128,100]"], cp["steps"]
+        assert (digest(h), digest(u), digest(v)) == (cp["h"], cp["u"], cp["v"]), cp["steps"]
+        d = p.diagnostics()
+        for k in ("mean_depth", "energy", "max_speed"):
+            assert d[k] == pytest.approx(cp["diagnostics"][k], rel=1e-13), (k, cp["steps"])
+    assert p.time() == pytest.approx(5000 * 60.0)
+
+
 def test_plane_config1_full_size_bitwise_against_oracle(engine):
     # 1024 x 512 cells, dx = dy = 5 km, f0 = 1e-4, beta = 1.6e-11, H = 100 m, jet 20 sech^2(y/100 km) + 0.1 m noise
     nx, ny, L = 1024, 512, 5000.0

@@ -127,6 +127,60 @@ def test_advance_keeps_mass_and_is_per_member(trained, engine):
     assert not np.array_equal(out[0], st[0])
 
 
+def _packed_map(st, T, quarter_turns, reflect):
+    """The symmetry map of packed states [member][6 ntri] (zeta, delta, Phi; (m, n) in triangle order, re/im):
+    rotation by quarter_turns x 90 degrees about the polar axis (coefficient times i^(m quarter_turns)), then the
+    equatorial reflection (Phi, delta times (-1)^(n-m), zeta times -(-1)^(n-m))."""
+    out = st.copy()
+    ntri = (T + 1) * (T + 2) // 2
+    for q in range(3):
+        tri = 0
+        for m in range(T + 1):
+            for n in range(m, T + 1):
+                f = (q * ntri + tri) * 2
+                c = (st[:, f] + 1j * st[:, f + 1]) * (1j ** ((m * quarter_turns) % 4))
+                if reflect:
+                    c = c * ((-1.0) ** (n - m)) * (-1.0 if q == 0 else 1.0)
+                out[:, f], out[:, f + 1] = c.real, c.imag
+                tri += 1
+    return out
+
+
+def test_symmetry_averaged_network_is_equivariant(trained, engine):
+    # with the increments averaged over the eight maps {0, 90, 180, 270 degrees} x {no reflection, reflection},
+    # advancing a mapped state gives the mapped advance of the state (up to the order of the FP32 sums), as the
+    # exact dynamics do; the plain network (one map) is not equivariant
+    sur, _ = trained
+    T = 21
+    s = engine.Sphere(T, diffusion=6.37122e6 ** 4 / (86400.0 * (T * (T + 1)) ** 2), members=2)
+    for b in range(2):
+        s.turbulence(seed=11 + b, mean_height=8000.0, max_wind=30.0, nforce=10, member=b)
+    rows = []
+    for b in range(2):
+        z, d, f = s.get_state(member=b)
+        packed = []
+        for fld in (z, d, f):
+            for m in range(T + 1):
+                for n in range(m, T + 1):
+                    c = fld[m * (T + 1) + n]
+                    packed += [c.real, c.imag]
+        rows.append(packed)
+    st = np.array(rows)
+    for maps, tol in ((8, 1e-5), (1, None)):
+        sur.set_symmetry_average(maps)
+        base = sur.advance(st)
+        inc = base - st
+        for qt, rf in ((1, False), (2, True), (3, True)):
+            got = sur.advance(_packed_map(st, T, qt, rf)) - _packed_map(st, T, qt, rf)
+            want = _packed_map(inc, T, qt, rf)
+            rel = np.abs(got - want).max() / np.abs(want).max()
+            if tol is not None:
+                assert rel < tol, (qt, rf, rel)
+            else:
+                assert rel > 1e-4, (qt, rf, rel)
+    sur.set_symmetry_average(8)
+
+
 @pytest.mark.parametrize("check", ["fp64", "split3"])
 def test_rollout_takeover_semantics(trained, engine, check):
     sur, _ = trained
