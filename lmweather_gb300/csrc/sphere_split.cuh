@@ -39,9 +39,6 @@ constexpr int SPLIT_THREADS = 128;
 constexpr int SPLIT_ANA_THREADS = 256;  // analysis: 8 warps for the gather and the RK4 epilogue, warps 0-3 read TMEM
 constexpr int SPLIT_NQ = 16;  // per (member, jh, m): U, V, zeta, Phi Fourier coefficients at the southern and northern latitude
 constexpr int SPLIT_JB_MAX = 8;  // latitude pairs per grid CTA
-constexpr int SPLIT_PACK_ROWS = 12;  // synthesis operand rows per coefficient: 8 against P, 4 against H
-// shared memory of the analysis epilogue's operand staging: per warp [3 pieces][12 rows][32 items] BF16
-constexpr size_t SPLIT_PACK_BYTES = static_cast<size_t>(SPLIT_ANA_THREADS / 32) * 3 * SPLIT_PACK_ROWS * 32 * 2;
 // dynamic shared memory per CTA when two CTAs share an SM (228 KB per SM, 1 KB reserved per CTA, static barriers)
 constexpr size_t SPLIT_HALF_SM = 115456;
 
@@ -773,145 +770,81 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
   }
   __syncthreads();
   if (ok) {
-    // work items (member, operand column k) of the CTA's columns of m: even n - m at k = (n - m) / 2 in [0, ke16),
-    // odd n - m at ke16 + (n - m - 1) / 2; a parity's columns padded to a multiple of 8 (the padding columns of the
-    // operands are written with zeros, which they hold anyway), so every 8 consecutive items are 8 consecutive
-    // columns of one member. Each warp stages the next synthesis operands of its 32 items in shared memory and
-    // writes them as 16-byte runs (8 columns of one operand row), instead of one 2-byte store per value.
-    const int ke16 = sd.ke16[m];
-    const int kbase = BOTH ? 0 : (s_first ? ke16 : 0);
-    const int ncol = BOTH ? ke16 + pad8(R1) : (s_first ? pad8(R1) : ke16);
-    const int ntask = mt * ncol;
-    const int stage_off = (8 * mt * ldp * 4 + 15) & ~15;
-    __nv_bfloat16 *sb = reinterpret_cast<__nv_bfloat16 *>(smem + stage_off) + warp * (SPLIT_PACK_ROWS * 3 * 32);
-    const long kpm = sd.kps[m];
-    const long baseP = sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kpm;
-    const long baseH = sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kpm;
-    for (int e0 = warp * 32; e0 < ntask; e0 += blockDim.x) {
-      const int e = e0 + lane;
-      const int ml = e / ncol, kc = kbase + (e - ml * ncol);
-      const int s = kc >= ke16 ? 1 : 0, r = s ? kc - ke16 : kc;
-      const int n = m + s + 2 * r;
-      const bool live = e < ntask && r < (s ? R1 : R0);
-      // BF16 pieces of operand value x into the warp's staging rows [piece][row][lane]
-      auto put = [&](int i, float x) {
-        const __nv_bfloat16 h = __float2bfloat16_rn(x);
-        sb[(0 * SPLIT_PACK_ROWS + i) * 32 + lane] = h;
-        if (sd.pieces > 1) {
-          const float r1 = x - __bfloat162float(h);
-          const __nv_bfloat16 l = __float2bfloat16_rn(r1);
-          sb[(1 * SPLIT_PACK_ROWS + i) * 32 + lane] = l;
-          if (sd.pieces > 2) sb[(2 * SPLIT_PACK_ROWS + i) * 32 + lane] = __float2bfloat16_rn(r1 - __bfloat162float(l));
+    const int cnt = BOTH ? d.N - m + 1 : (s_first ? R1 : R0);
+    for (int e = threadIdx.x; e < mt * cnt; e += blockDim.x) {
+      const int ml = e / cnt, j = e - ml * cnt;
+      const int s = BOTH ? (j & 1) : s_first, r = BOTH ? (j >> 1) : j;
+      const int b = tile * sd.nbt + ml, n = m + s + 2 * r;
+      const int cbs = s ? cb1 : 0, ras = s ? ra1 : ra0;
+      const float *H = dsm + (ml * 6) * ldp + cbs + r, *P = dsm + (ml * 8) * ldp + cbs + ras + r;
+      const float2 aH = make_float2(H[0 * ldp], H[1 * ldp]), bH = make_float2(H[2 * ldp], H[3 * ldp]), vH = make_float2(H[4 * ldp], H[5 * ldp]);
+      const float2 aP = make_float2(P[0 * ldp], P[1 * ldp]), bP = make_float2(P[2 * ldp], P[3 * ldp]);
+      const float2 uP = make_float2(P[4 * ldp], P[5 * ldp]), eP = make_float2(P[6 * ldp], P[7 * ldp]);
+      const float mm = static_cast<float>(m);
+      // cpp/sphere.cpp:380-389
+      float2 kz = csub(bH, imul(aP, mm));
+      float2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
+      float2 kf = csub(vH, imul(uP, mm));
+      const int q = d.tri[m] + n - m;
+      if (q == 0) kz = kd = kf = make_float2(0, 0);
+      const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
+      double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
+                      make_double2(f2d_int(kf.x), f2d_int(kf.y))};
+      if (sd.lin_exact && q != 0) {
+        // the linear terms in FP64 from the stage input y (x0 at stage 0, else the previous stage's output, a
+        // separate buffer: neighbouring n belong to other CTAs): n(n+1)/a^2 Phi_n in d delta; -Phi_mean delta_n in
+        // d Phi (D(U, V) = delta exactly for n <= T); for an untilted axis the Coriolis terms -D(f U, f V) and
+        // D(f V, -f U) with f = 2 Omega mu, which couple n - 1, n, n + 1 of the same m
+        const double2 *y = (sa.stage == 0 ? x0 : xin) + static_cast<size_t>(b) * 3 * d.ntri;
+        const int qq = q;
+        const double2 yz = y[qq], yd = y[d.ntri + qq], yf = y[2 * d.ntri + qq];
+        const double phibar = x0[static_cast<size_t>(b) * 3 * d.ntri + 2 * d.ntri].x * d.Ps[0];
+        const double lp = d.lapl[n];
+        k[1].x += lp * yf.x;
+        k[1].y += lp * yf.y;
+        k[2].x -= phibar * yd.x;
+        k[2].y -= phibar * yd.y;
+        if (!(d.gflag[b] & 1)) {
+          const double om = d.om2[b];
+          const double cA = sd.lin[qq], cB = sd.lin[d.ntri + qq], cC = sd.lin[2 * d.ntri + qq];
+          const double2 zu = n < d.N ? y[qq + 1] : make_double2(0, 0), du = n < d.N ? y[d.ntri + qq + 1] : make_double2(0, 0);
+          const double2 zl = n > m ? y[qq - 1] : make_double2(0, 0), dd = n > m ? y[d.ntri + qq - 1] : make_double2(0, 0);
+          // -D(fU, fV)_n = -2 Omega (cA delta_{n+1} + cB delta_{n-1} - i cC zeta_n)
+          k[0].x -= om * (cA * du.x + cB * dd.x + cC * yz.y);
+          k[0].y -= om * (cA * du.y + cB * dd.y - cC * yz.x);
+          // D(fV, -fU)_n = 2 Omega (cA zeta_{n+1} + cB zeta_{n-1} + i cC delta_n)
+          k[1].x += om * (cA * zu.x + cB * zl.x - cC * yd.y);
+          k[1].y += om * (cA * zu.y + cB * zl.y + cC * yd.x);
         }
-      };
-      if (!live) {
-#pragma unroll
-        for (int i = 0; i < SPLIT_PACK_ROWS; i++) put(i, 0.0f);
-      } else {
-        const int b = tile * sd.nbt + ml;
-        const int cbs = s ? cb1 : 0, ras = s ? ra1 : ra0;
-        const float *H = dsm + (ml * 6) * ldp + cbs + r, *P = dsm + (ml * 8) * ldp + cbs + ras + r;
-        const float2 aH = make_float2(H[0 * ldp], H[1 * ldp]), bH = make_float2(H[2 * ldp], H[3 * ldp]), vH = make_float2(H[4 * ldp], H[5 * ldp]);
-        const float2 aP = make_float2(P[0 * ldp], P[1 * ldp]), bP = make_float2(P[2 * ldp], P[3 * ldp]);
-        const float2 uP = make_float2(P[4 * ldp], P[5 * ldp]), eP = make_float2(P[6 * ldp], P[7 * ldp]);
-        const float mm = static_cast<float>(m);
-        // cpp/sphere.cpp:380-389
-        float2 kz = csub(bH, imul(aP, mm));
-        float2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
-        float2 kf = csub(vH, imul(uP, mm));
-        const int q = d.tri[m] + n - m;
-        if (q == 0) kz = kd = kf = make_float2(0, 0);
-        const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
-        double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
-                        make_double2(f2d_int(kf.x), f2d_int(kf.y))};
-        // every load of the three fields is issued before any store (the buffers never alias)
-        double2 xv[3], av[3];
-#pragma unroll
-        for (int f = 0; f < 3; f++) {
-          xv[f] = x0[base + static_cast<size_t>(f) * d.ntri];
-          av[f] = sa.stage > 0 ? acc[base + static_cast<size_t>(f) * d.ntri] : make_double2(0.0, 0.0);
-        }
-        if (sd.lin_exact && q != 0) {
-          // the linear terms in FP64 from the stage input y (x0 at stage 0, else the previous stage's output, a
-          // separate buffer: neighbouring n belong to other CTAs): n(n+1)/a^2 Phi_n in d delta; -Phi_mean delta_n in
-          // d Phi (D(U, V) = delta exactly for n <= T); for an untilted axis the Coriolis terms -D(f U, f V) and
-          // D(f V, -f U) with f = 2 Omega mu, which couple n - 1, n, n + 1 of the same m
-          const double2 *y = (sa.stage == 0 ? x0 : xin) + static_cast<size_t>(b) * 3 * d.ntri;
-          const int qq = q;
-          const double2 yz = sa.stage == 0 ? xv[0] : y[qq], yd = sa.stage == 0 ? xv[1] : y[d.ntri + qq],
-                        yf = sa.stage == 0 ? xv[2] : y[2 * d.ntri + qq];
-          const double phibar = x0[static_cast<size_t>(b) * 3 * d.ntri + 2 * d.ntri].x * d.Ps[0];
-          const double lp = d.lapl[n];
-          k[1].x += lp * yf.x;
-          k[1].y += lp * yf.y;
-          k[2].x -= phibar * yd.x;
-          k[2].y -= phibar * yd.y;
-          if (!(d.gflag[b] & 1)) {
-            const double om = d.om2[b];
-            const double cA = sd.lin[qq], cB = sd.lin[d.ntri + qq], cC = sd.lin[2 * d.ntri + qq];
-            const double2 zu = n < d.N ? y[qq + 1] : make_double2(0, 0), du = n < d.N ? y[d.ntri + qq + 1] : make_double2(0, 0);
-            const double2 zl = n > m ? y[qq - 1] : make_double2(0, 0), dd = n > m ? y[d.ntri + qq - 1] : make_double2(0, 0);
-            // -D(fU, fV)_n = -2 Omega (cA delta_{n+1} + cB delta_{n-1} - i cC zeta_n)
-            k[0].x -= om * (cA * du.x + cB * dd.x + cC * yz.y);
-            k[0].y -= om * (cA * du.y + cB * dd.y - cC * yz.x);
-            // D(fV, -fU)_n = 2 Omega (cA zeta_{n+1} + cB zeta_{n-1} + i cC delta_n)
-            k[1].x += om * (cA * zu.x + cB * zl.x - cC * yd.y);
-            k[1].y += om * (cA * zu.y + cB * zl.y + cC * yd.x);
-          }
-        }
-        double2 nv[3];
-#pragma unroll
-        for (int f = 0; f < 3; f++) {
-          const size_t i = base + static_cast<size_t>(f) * d.ntri;
-          if (sa.stage == 0) {
-            acc[i] = k[f];
-            nv[f] = cadd(xv[f], cscale(k[f], sa.c));
-          } else if (sa.stage < 3) {
-            acc[i] = cadd(av[f], cscale(k[f], 2.0));
-            nv[f] = cadd(xv[f], cscale(k[f], sa.c));
-          } else {
-            const double2 val = cadd(xv[f], cscale(cadd(av[f], k[f]), sa.c));
-            const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
-            nv[f] = q == 0 ? val : cscale(val, fac);
-            x0[i] = nv[f];
-          }
-          // the next stage input in FP64 is kept when a caller asks for it (the linear-exact form reads it; the
-          // split synthesis reads the packed operands written below)
-          if (xout != nullptr && sa.stage < 3) xout[i] = nv[f];
-        }
-        // the next synthesis operands of this coefficient (psi, chi, zeta, Phi on P rows; psi, chi on H rows), as
-        // pack_syn_coef forms them
-        const double kfn = kfac[n];
-        const bool mean = sd.lin_exact && n == 0;
-        const float psr = d2f_int(nv[0].x * kfn), psi = d2f_int(nv[0].y * kfn), chr = d2f_int(nv[1].x * kfn), chi = d2f_int(nv[1].y * kfn);
-        put(0, psr);
-        put(1, psi);
-        put(2, chr);
-        put(3, chi);
-        put(4, d2f_int(nv[0].x));
-        put(5, d2f_int(nv[0].y));
-        put(6, mean ? 0.0f : d2f_int(nv[2].x));
-        put(7, mean ? 0.0f : d2f_int(nv[2].y));
-        put(8, psr);
-        put(9, psi);
-        put(10, chr);
-        put(11, chi);
       }
-      __syncwarp();
-      // 16-byte runs: (piece, group of 8 items, operand row); consecutive lanes take consecutive rows of a group, so
-      // the 8 P rows of a member fill one 128-byte core-matrix row block
-      const int nvec = sd.pieces * 4 * SPLIT_PACK_ROWS;
-      for (int v = lane; v < nvec; v += 32) {
-        const int rr = v % SPLIT_PACK_ROWS, g = (v / SPLIT_PACK_ROWS) & 3, pc = v / (4 * SPLIT_PACK_ROWS);
-        const int eg = e0 + 8 * g;
-        if (eg >= ntask) continue;
-        const int mlg = eg / ncol, kg = kbase + (eg - mlg * ncol);
-        const uint4 val = *reinterpret_cast<const uint4 *>(sb + (pc * SPLIT_PACK_ROWS + rr) * 32 + 8 * g);
-        __nv_bfloat16 *dst = rr < 8 ? sd.aS_P + baseP + pc * sd.aSP_size + tile_off(mlg * 8 + rr, kg, sd.rSP, sd.bks)
-                                    : sd.aS_H + baseH + pc * sd.aSH_size + tile_off(mlg * 4 + rr - 8, kg, sd.rSH, sd.bks);
-        *reinterpret_cast<uint4 *>(dst) = val;
+      // every load of the three fields is issued before any store (the buffers never alias)
+      double2 xv[3], av[3];
+#pragma unroll
+      for (int f = 0; f < 3; f++) {
+        xv[f] = x0[base + static_cast<size_t>(f) * d.ntri];
+        av[f] = sa.stage > 0 ? acc[base + static_cast<size_t>(f) * d.ntri] : make_double2(0.0, 0.0);
       }
-      __syncwarp();
+      double2 nv[3];
+#pragma unroll
+      for (int f = 0; f < 3; f++) {
+        const size_t i = base + static_cast<size_t>(f) * d.ntri;
+        if (sa.stage == 0) {
+          acc[i] = k[f];
+          nv[f] = cadd(xv[f], cscale(k[f], sa.c));
+        } else if (sa.stage < 3) {
+          acc[i] = cadd(av[f], cscale(k[f], 2.0));
+          nv[f] = cadd(xv[f], cscale(k[f], sa.c));
+        } else {
+          const double2 val = cadd(xv[f], cscale(cadd(av[f], k[f]), sa.c));
+          const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
+          nv[f] = q == 0 ? val : cscale(val, fac);
+          x0[i] = nv[f];
+        }
+        // the next stage input in FP64 is kept when a caller asks for it (the linear-exact form reads it; the
+        // split synthesis reads the packed operands written below)
+        if (xout != nullptr && sa.stage < 3) xout[i] = nv[f];
+      }
+      pack_syn_coef(d, sd, kfac, b, m, n, nv[0], nv[1], nv[2]);
     }
   }
   }
@@ -1065,18 +998,17 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   const size_t ana_res = sp.ana_res_bytes_v[sp.direct], ana_stage = sp.ana_stage_bytes_v[sp.direct];
   // two analysis CTAs per SM when a 3-stage pipeline fits in half of the shared memory
   const size_t half = SPLIT_HALF_SM;
-  const size_t ana_epi = ((static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float) + 15) & ~static_cast<size_t>(15)) + SPLIT_PACK_BYTES;
-  if (ana_res + 3 * ana_stage + SPLIT_MARGIN <= half && ana_epi <= half)
+  if (ana_res + 3 * ana_stage + SPLIT_MARGIN <= half && static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float) <= half)
     sp.ns_ana = 3;
   else
     sp.ns_ana = static_cast<int>(std::min<size_t>(SPLIT_MAX_STAGES, (budget - SPLIT_MARGIN - ana_res) / ana_stage));
   if (sp.ns_ana < 2) throw InvalidArgument("split precision: the analysis pipeline does not fit in shared memory");
-  sp.smem_ana = std::max(ana_res + sp.ns_ana * ana_stage + SPLIT_MARGIN, ana_epi);
+  sp.smem_ana = std::max(ana_res + sp.ns_ana * ana_stage + SPLIT_MARGIN, static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float));
   sp.syn_stage_bytes = syn_stage;
   sp.syn_min_bytes = static_cast<size_t>(4 * 8 * sp.nbt * 33 * sizeof(float));
-  sp.ana_min_bytes = ana_epi;
+  sp.ana_min_bytes = static_cast<size_t>(sp.rAP) * (2 * ra_max + 1) * sizeof(float);
   for (int m = 0; m <= N; m++) sp.ra_pair = std::max(sp.ra_pair, sp.ra16[2 * m] + sp.ra16[2 * m + 1]);
-  sp.ana_both_min_bytes = ((static_cast<size_t>(sp.rAP) * (2 * sp.ra_pair + 1) * sizeof(float) + 15) & ~static_cast<size_t>(15)) + SPLIT_PACK_BYTES;
+  sp.ana_both_min_bytes = static_cast<size_t>(sp.rAP) * (2 * sp.ra_pair + 1) * sizeof(float);
   sp.budget_bytes = budget;
   // coefficients of the spectral Coriolis terms (eps of cpp/sphere.cpp:11): for q = (m, n), eps_{n+1} n/(n+1)
   // (n < T), eps_n (n+1)/n (n > m) and m/(n(n+1)) (n >= 1)

@@ -280,6 +280,25 @@ def test_split_bf16_path_against_fp64(engine, T, dt, steps):
     assert e6 < 1e-6
 
 
+def test_split3_t170_two_days_within_the_target(engine):
+    # the precision target at full length: T170, seeded balanced turbulence (8000 m, 30 m/s, n <= 85), 2 model days
+    # at 240 s (720 steps); the three-product split (linear terms in FP64) within 1e-6 relative height L2 of FP64
+    T, dt = 170, 240.0
+    nu = 6.37122e6 ** 4 / (86400.0 * (T * (T + 1)) ** 2)
+    grids = {}
+    for key, kw in (("fp64", dict(precision=engine.FP64)), ("s3", dict(precision=engine.SPLIT_BF16, split_terms=3))):
+        s = engine.Sphere(T, diffusion=nu, **kw)
+        s.turbulence(1, 8000.0, 30.0, T // 2)
+        s.run(2 * 86400.0, dt)
+        grids[key] = s.grid_height()
+        s.close()
+    mu, w = engine.Sphere(T).gauss()
+    wt = w[:, None]
+    err = np.sqrt((wt * (grids["s3"] - grids["fp64"]) ** 2).sum() / (wt * grids["fp64"] ** 2).sum())
+    print(f"T170 split3 vs FP64 after 2 days: height L2 {err:.3e}")
+    assert err < 1e-6
+
+
 # ------------------------------------------------------------------- known answers of the reference's scripts
 def _make(engine):
     return lambda T, **kw: engine.Sphere(T, **kw)
