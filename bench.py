@@ -586,12 +586,13 @@ def other_workloads(lw, lib, args, ens):
     return out
 
 
-def surrogate_workload(lw, trajectories=1024, windows=80, epochs=60, members=1024, rollout_windows=16):
-    """Config 4 within the benchmark's time: the T42 residual MLP (5676 -> 4096 x 3 -> 5676, GELU, BF16 on tcgen05)
-    trained on `trajectories` x `windows` solver pairs (split-precision RK4 data, FP64 state; 6-hour windows of
-    900 s steps, mean height 8000 m), then a hybrid rollout of `members` held-out members over `rollout_windows`
-    windows with split-precision RK4 checking every 4th window and FP64 RK4 taking over above 1e-3. The full
-    configuration (204,800 pairs, 100 epochs, 80 rollout windows) is python bench.py --study surrogate."""
+def surrogate_workload(lw, trajectories=2560, windows=80, epochs=100, members=1024, rollout_windows=16):
+    """Config 4 inside the benchmark: the T42 residual MLP (5676 -> 4096 x 3 -> 5676, GELU, BF16 on tcgen05) trained
+    on the configured 204,800 solver pairs (`trajectories` x `windows`; split-precision RK4 data, FP64 state; 6-hour
+    windows of 900 s steps, mean height 8000 m) for `epochs` epochs with symmetry-augmented batches and averaged
+    weights, then a hybrid rollout of `members` held-out members over `rollout_windows` windows (the 8-map
+    averaged network; split-precision RK4 checking every 4th window, FP64 RK4 taking over above 1e-3). The 80-window
+    rollout is python bench.py --study surrogate."""
     t0 = time.perf_counter()
     sur = lw.Surrogate(42, hidden=4096, seed=1)
     gen_s = sur.generate(trajectories, windows, seed0=1_000_000, hmin=8000.0, hmax=8000.0, precision=lw.SPLIT_BF16)
@@ -602,10 +603,12 @@ def surrogate_workload(lw, trajectories=1024, windows=80, epochs=60, members=102
                     ref_windows=4, hmin=8000.0, hmax=8000.0)
     sur.close()
     fl = 2 * (5676 * 4096 * 2 + 4096 * 4096 * 2)
-    return {"config": "4: learned surrogate T42, 6-hour windows (bounded training)",
+    maps = 8  # the inference average over symmetry maps (the library default)
+    return {"config": "4: learned surrogate T42, 6-hour windows (configured training, 16-window rollout)",
             "unit": "member-sim-days/s",
-            "network_only": members * 0.25 / (fwd1024 * 1e-3), "hybrid": r["hybrid_rate"], "plain_rk4_fp64": r["rk4_rate"],
-            "speedup_network_vs_rk4": members * 0.25 / (fwd1024 * 1e-3) / r["rk4_rate"],
+            "network_only": members * 0.25 / (maps * fwd1024 * 1e-3), "network_in_rollout": r["network_rate"],
+            "hybrid": r["hybrid_rate"], "plain_rk4_fp64": r["rk4_rate"],
+            "speedup_network_vs_rk4": members * 0.25 / (maps * fwd1024 * 1e-3) / r["rk4_rate"],
             "speedup_hybrid_vs_rk4": r["hybrid_rate"] / r["rk4_rate"],
             "window_height_error": {"validation_mean": fit["val_err_mean"], "validation_p90": fit["val_err_p90"],
                                     "persistence_mean": fit["val_persist_mean"], "untrained_mean": fit["val_untrained_mean"],
