@@ -750,7 +750,7 @@ def run_case(args) -> int:
 def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, epochs=100, batch=512, lr=3e-4, lr_min=3e-5,
                     hmin=8000.0, hmax=8000.0, members=1024, rollout_windows=80, check_every=4, threshold=1e-3, ref_windows=4, seed=1,
                     check_precision=None, loss="energy", thresholds=(), clip=2.0, data_precision=0, augment=True, averaging=0.9995,
-                    sym_average=8) -> dict:
+                    sym_average=8, kinetic_weight=1.0) -> dict:
     """The learned surrogate end to end: solver trajectories (balanced turbulence on training seeds, RK4 at 900 s,
     del^4 with a 1-day e-folding at n = T; pairs (state, state + 6 h) from every window; the last tenth of the
     trajectories held out) -> training on the GPU -> validation errors per 6-hour window -> a hybrid rollout of
@@ -766,6 +766,7 @@ def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, e
     sur.set_augment(augment)
     sur.set_averaging(averaging)
     sur.set_symmetry_average(sym_average)
+    sur.set_kinetic_weight(kinetic_weight)
     gen_s = sur.generate(trajectories, windows, seed0=1_000_000 * seed, hmin=hmin, hmax=hmax, precision=data_precision)
     fit = sur.fit(epochs, batch=batch, lr=lr, lr_min=lr_min, val_fraction=0.1, seed=seed, loss=loss)
     hist_loss, _ = sur.history()
@@ -775,7 +776,7 @@ def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, e
            "data_precision": ["fp64", "fp32", "split3"][data_precision], "generate_s": gen_s, "loss": loss, "clip_ratio": clip,
            "epochs": epochs, "lr": [lr, lr_min], "fit": fit, "loss_by_epoch": [round(v, 4) for v in hist_loss.tolist()],
            "train_step_ms": train_ms, "forward_ms_batch": fwd_ms, "batch": batch, "augment": augment, "averaging": averaging,
-           "symmetry_maps_averaged": sym_average,
+           "symmetry_maps_averaged": sym_average, "kinetic_weight": kinetic_weight,
            "check_precision": ["fp64", "fp32", "split3"][check_precision]}
     if members > 0 and rollout_windows > 0:
         r = sur.rollout(members, seed0=9_000_000 + seed, windows=rollout_windows, check_every=check_every, threshold=threshold,
@@ -825,6 +826,7 @@ def main():
     ap.add_argument("--augment", type=int, default=1, help="symmetry augmentation of the training pairs (1/0)")
     ap.add_argument("--averaging", type=float, default=0.9995, help="weight averaging decay (0: last weights)")
     ap.add_argument("--sym-average", type=int, default=8, help="symmetry maps averaged at inference (1: plain network)")
+    ap.add_argument("--kinetic-weight", type=float, default=1.0, help="weight of the kinetic-energy part of the loss")
     ap.add_argument("--lr-min", type=float, default=3e-5)
     ap.add_argument("--data-precision", default="split3", choices=["fp64", "split3"])
     args = ap.parse_args()
@@ -845,7 +847,7 @@ def main():
                                              threshold=args.threshold, check_precision=lw.SPLIT_BF16 if args.check_precision == "split3" else lw.FP64,
                                              thresholds=tuple(float(v) for v in args.sweep.split(",") if v), augment=bool(args.augment),
                                              averaging=args.averaging, data_precision=2 if args.data_precision == "split3" else 0,
-                                             sym_average=args.sym_average)))
+                                             sym_average=args.sym_average, kinetic_weight=args.kinetic_weight)))
         return 0
     if args.impl == "reference":
         return run_reference(args, rank, world)

@@ -393,6 +393,10 @@ int lmw_surrogate_set_augment(lmw_surrogate *s, int on);
  * the second half of lmw_surrogate_fit's steps (the default, 0.9995); 0: the last weights. No reference
  * counterpart. */
 int lmw_surrogate_set_averaging(lmw_surrogate *s, double decay);
+/* weight of the kinetic-energy part of the energy-norm training loss against the available potential energy
+ * (default 1, the energy norm; below 1 leans the fit toward the height field). Set before the first fit. No
+ * reference counterpart. */
+int lmw_surrogate_set_kinetic_weight(lmw_surrogate *s, double weight);
 /* maps = 1: the network advances a state as it is. maps = 2k (the default 8): the network is applied to the state
  * under k rotations about the polar axis by multiples of 2 pi / k, each without and with the equatorial
  * reflection, each increment is mapped back, and the 2k increments are averaged (the exact dynamics commute with

@@ -147,6 +147,7 @@ _SIGS = {
     "lmw_surrogate_set_augment": (_I, [_P, _I]),
     "lmw_surrogate_set_averaging": (_I, [_P, _D]),
     "lmw_surrogate_set_symmetry_average": (_I, [_P, _I]),
+    "lmw_surrogate_set_kinetic_weight": (_I, [_P, _D]),
     "lmw_surrogate_history": (_I, [_P, _I, _DP, _DP, _IP]),
 }
 
@@ -887,6 +888,10 @@ class Surrogate:
     def set_averaging(self, decay: float):
         """Moving average of the weights over the second half of fit() (decay per step; 0: the last weights)."""
         _check(self._lib.lmw_surrogate_set_averaging(self._h, decay))
+
+    def set_kinetic_weight(self, weight: float):
+        """Weight of the kinetic-energy part of the training loss (1: the energy norm). Before the first fit."""
+        _check(self._lib.lmw_surrogate_set_kinetic_weight(self._h, weight))
 
     def set_symmetry_average(self, maps: int):
         """Average the network's increments over `maps` rotations/reflections of the input (1: the plain network)."""

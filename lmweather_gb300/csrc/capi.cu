@@ -788,6 +788,10 @@ int lmw_surrogate_set_symmetry_average(lmw_surrogate *s, int maps) {
   return SUR(s, need(maps == 1 || (maps >= 2 && maps <= 64 && maps % 2 == 0), "the symmetry maps must be 1 or an even number up to 64");
              s->s->sym_average = maps);
 }
+int lmw_surrogate_set_kinetic_weight(lmw_surrogate *s, double weight) {
+  return SUR(s, need(weight > 0 && weight <= 16, "the kinetic-energy weight must lie in (0, 16]"); need(!s->s->have_norm, "set the loss weights before the first fit");
+             s->s->ke_weight = weight);
+}
 int lmw_surrogate_set_averaging(lmw_surrogate *s, double decay) {
   return SUR(s, need(decay >= 0 && decay < 1, "the averaging decay must lie in [0, 1)"); s->s->ema = decay);
 }

@@ -1463,8 +1463,9 @@ static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage,
 
 // One RK4 stage in split precision: tensor-core synthesis, FP32 grid stage, tensor-core analysis with the RK4
 // update (which also packs the next stage's synthesis operands)
-// xs, xs2: the FP64 stage inputs the linear-exact form keeps, in turn (stage 0 writes xs, 1 reads xs and writes xs2,
-// 2 reads xs2 and writes xs, 3 reads xs): an analysis CTA reads neighbouring coefficients that other CTAs update
+// xs, xs2: the stage inputs (rounded to FP32, in the first half of each FP64 buffer) that the linear-exact form keeps,
+// in turn (stage 0 writes xs, 1 reads xs and writes xs2, 2 reads xs2 and writes xs, 3 reads xs): an analysis CTA
+// reads neighbouring coefficients that other CTAs update
 static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan &sp, const double *kfac64, int B, int stage, double dt,
                         const double *filt, float2 *fold, double2 *x0, double2 *xs, double2 *xs2, double2 *acc, const double *fgrid,
                         const double *hsgrid, cudaStream_t stream, int which = -1) {
@@ -1490,8 +1491,9 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
                                  : (sp.direct ? split_ana<false, true, 3> : split_ana<false, false, 3>))
                   : (sp.ana_both ? (sp.direct ? split_ana<true, true, 2> : split_ana<true, false, 2>)
                                  : (sp.direct ? split_ana<false, true, 2> : split_ana<false, false, 2>));
-    const double2 *xin = stage == 1 || stage == 3 ? xs : (stage == 2 ? xs2 : nullptr);
-    double2 *xout = !sp.lin_exact || stage == 3 ? nullptr : (stage == 1 ? xs2 : xs);
+    float2 *ys = reinterpret_cast<float2 *>(xs), *ys2 = reinterpret_cast<float2 *>(xs2);
+    const float2 *xin = stage == 1 || stage == 3 ? ys : (stage == 2 ? ys2 : nullptr);
+    float2 *xout = !sp.lin_exact || stage == 3 ? nullptr : (stage == 1 ? ys2 : ys);
     k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xin, xout, acc);
   }
 }

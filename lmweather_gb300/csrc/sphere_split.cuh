@@ -71,7 +71,7 @@ struct SplitPlan {
   // untilted Coriolis terms) in FP64 spectral space; only the nonlinear products go through the BF16 pieces.
   // 0: every term through the BF16 GEMMs (the plain split form)
   int lin_exact = 1;
-  DevBuf<double> lin;         // per coefficient q: eps_{n+1} n/(n+1), eps_n (n+1)/n, m/(n(n+1)) (3 x ntri)
+  DevBuf<float> lin32;        // per coefficient q: eps_{n+1} n/(n+1), eps_n (n+1)/n, m/(n(n+1)) (3 x ntri), FP32
   size_t syn_stage_bytes = 0, syn_min_bytes = 0, ana_min_bytes = 0, ana_both_min_bytes = 0, budget_bytes = 0;
   size_t ana_res_bytes_v[2] = {0, 0}, ana_stage_bytes_v[2] = {0, 0};  // per variant: [0] gathered A, [1] streamed A
 };
@@ -87,7 +87,7 @@ struct SplitDev {
   float2 *fold;  // [m][slot][parity][member][jh]: folded analysis inputs
   int *err;
   int lin_exact;        // see SplitPlan::lin_exact
-  const double *lin;    // [3][ntri]: the spectral Coriolis coefficients
+  const float *lin32;   // [3][ntri]: the spectral Coriolis coefficients
 };
 
 namespace {
@@ -577,11 +577,13 @@ __device__ __forceinline__ void pack_syn_coef(const SphDev &d, const SplitDev &s
   const long kp = sd.kps[m];
   const long baseP = sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kp;
   const long baseH = sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kp;
-  const double kf = kfac[n];
-  // the linear-exact form synthesises Phi' = Phi - Phi_00 P_00: the mean enters the tendencies in FP64
+  // psi, chi = -a^2 / (n (n + 1)) (zeta, delta) in FP32 (the operands carry 16 or 24 bits); conversions on the
+  // integer pipe, no FP64 arithmetic
+  const float kf = d2f_int(kfac[n]);
+  const float zx = d2f_int(z.x), zy = d2f_int(z.y), dx = d2f_int(dl.x), dy = d2f_int(dl.y);
+  // the linear-exact form synthesises Phi' = Phi - Phi_00 P_00: the mean enters the tendencies separately
   const bool mean = sd.lin_exact && n == 0;
-  const float v[8] = {d2f_int(z.x * kf), d2f_int(z.y * kf), d2f_int(dl.x * kf), d2f_int(dl.y * kf),
-                      d2f_int(z.x),      d2f_int(z.y),      mean ? 0.0f : d2f_int(f.x), mean ? 0.0f : d2f_int(f.y)};
+  const float v[8] = {zx * kf, zy * kf, dx * kf, dy * kf, zx, zy, mean ? 0.0f : d2f_int(f.x), mean ? 0.0f : d2f_int(f.y)};
 #pragma unroll
   for (int q = 0; q < 8; q++) fsplit(v[q], sd.aS_P + baseP + tile_off(ml * 8 + q, k, sd.rSP, sd.bks), sd.aSP_size, sd.pieces);
 #pragma unroll
@@ -605,8 +607,8 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict
 // shared memory admits three CTAs per SM)
 template <bool BOTH, bool DIRECT, int MINB>
 __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
-                                                             int B, int ns, double2 *__restrict__ x0, const double2 *__restrict__ xin,
-                                                             double2 *__restrict__ xout, double2 *__restrict__ acc) {
+                                                             int B, int ns, double2 *__restrict__ x0, const float2 *__restrict__ xin,
+                                                             float2 *__restrict__ xout, double2 *__restrict__ acc) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
@@ -786,37 +788,44 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
       float2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
       float2 kf = csub(vH, imul(uP, mm));
       const int q = d.tri[m] + n - m;
-      if (q == 0) kz = kd = kf = make_float2(0, 0);
       const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
-      double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
-                      make_double2(f2d_int(kf.x), f2d_int(kf.y))};
       if (sd.lin_exact && q != 0) {
-        // the linear terms in FP64 from the stage input y (x0 at stage 0, else the previous stage's output, a
-        // separate buffer: neighbouring n belong to other CTAs): n(n+1)/a^2 Phi_n in d delta; -Phi_mean delta_n in
-        // d Phi (D(U, V) = delta exactly for n <= T); for an untilted axis the Coriolis terms -D(f U, f V) and
-        // D(f V, -f U) with f = 2 Omega mu, which couple n - 1, n, n + 1 of the same m
-        const double2 *y = (sa.stage == 0 ? x0 : xin) + static_cast<size_t>(b) * 3 * d.ntri;
-        const int qq = q;
-        const double2 yz = y[qq], yd = y[d.ntri + qq], yf = y[2 * d.ntri + qq];
-        const double phibar = x0[static_cast<size_t>(b) * 3 * d.ntri + 2 * d.ntri].x * d.Ps[0];
-        const double lp = d.lapl[n];
-        k[1].x += lp * yf.x;
-        k[1].y += lp * yf.y;
-        k[2].x -= phibar * yd.x;
-        k[2].y -= phibar * yd.y;
+        // the terms linear in the stage input y, in FP32 like the rest of the tendencies but outside the BF16 products
+        // (x0 at stage 0, else the previous stage's output rounded to FP32 in a separate buffer: neighbouring n belong
+        // to other CTAs): n(n+1)/a^2 Phi_n in d delta; -Phi_mean delta_n in d Phi (D(U, V) = delta exactly for n <= T);
+        // for an untilted axis the Coriolis terms -D(f U, f V) and D(f V, -f U) with f = 2 Omega mu, which couple
+        // n - 1, n, n + 1 of the same m
+        const size_t mb = static_cast<size_t>(b) * 3 * d.ntri;
+        auto yat = [&](int field, int qq) -> float2 {
+          if (sa.stage == 0) {
+            const double2 v = x0[mb + static_cast<size_t>(field) * d.ntri + qq];
+            return make_float2(d2f_int(v.x), d2f_int(v.y));
+          }
+          return xin[mb + static_cast<size_t>(field) * d.ntri + qq];
+        };
+        const float2 yz = yat(0, q), yd = yat(1, q), yf = yat(2, q);
+        const float phibar = d2f_int(x0[mb + 2 * d.ntri].x) * t.Ps[0];
+        const float lp = t.lapl[n];
+        kd.x += lp * yf.x;
+        kd.y += lp * yf.y;
+        kf.x -= phibar * yd.x;
+        kf.y -= phibar * yd.y;
         if (!(d.gflag[b] & 1)) {
-          const double om = d.om2[b];
-          const double cA = sd.lin[qq], cB = sd.lin[d.ntri + qq], cC = sd.lin[2 * d.ntri + qq];
-          const double2 zu = n < d.N ? y[qq + 1] : make_double2(0, 0), du = n < d.N ? y[d.ntri + qq + 1] : make_double2(0, 0);
-          const double2 zl = n > m ? y[qq - 1] : make_double2(0, 0), dd = n > m ? y[d.ntri + qq - 1] : make_double2(0, 0);
+          const float om = static_cast<float>(d.om2[b]);
+          const float cA = sd.lin32[q], cB = sd.lin32[d.ntri + q], cC = sd.lin32[2 * d.ntri + q];
+          const float2 zu = n < d.N ? yat(0, q + 1) : make_float2(0, 0), du = n < d.N ? yat(1, q + 1) : make_float2(0, 0);
+          const float2 zl = n > m ? yat(0, q - 1) : make_float2(0, 0), dd = n > m ? yat(1, q - 1) : make_float2(0, 0);
           // -D(fU, fV)_n = -2 Omega (cA delta_{n+1} + cB delta_{n-1} - i cC zeta_n)
-          k[0].x -= om * (cA * du.x + cB * dd.x + cC * yz.y);
-          k[0].y -= om * (cA * du.y + cB * dd.y - cC * yz.x);
+          kz.x -= om * (cA * du.x + cB * dd.x + cC * yz.y);
+          kz.y -= om * (cA * du.y + cB * dd.y - cC * yz.x);
           // D(fV, -fU)_n = 2 Omega (cA zeta_{n+1} + cB zeta_{n-1} + i cC delta_n)
-          k[1].x += om * (cA * zu.x + cB * zl.x - cC * yd.y);
-          k[1].y += om * (cA * zu.y + cB * zl.y + cC * yd.x);
+          kd.x += om * (cA * zu.x + cB * zl.x - cC * yd.y);
+          kd.y += om * (cA * zu.y + cB * zl.y + cC * yd.x);
         }
       }
+      if (q == 0) kz = kd = kf = make_float2(0, 0);
+      const double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
+                            make_double2(f2d_int(kf.x), f2d_int(kf.y))};
       // every load of the three fields is issued before any store (the buffers never alias)
       double2 xv[3], av[3];
 #pragma unroll
@@ -840,9 +849,9 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
           nv[f] = q == 0 ? val : cscale(val, fac);
           x0[i] = nv[f];
         }
-        // the next stage input in FP64 is kept when a caller asks for it (the linear-exact form reads it; the
-        // split synthesis reads the packed operands written below)
-        if (xout != nullptr && sa.stage < 3) xout[i] = nv[f];
+        // the next stage input rounded to FP32 is kept when a caller asks for it (the linear-exact form reads it;
+        // the split synthesis reads the packed operands written below)
+        if (xout != nullptr && sa.stage < 3) xout[i] = make_float2(d2f_int(nv[f].x), d2f_int(nv[f].y));
       }
       pack_syn_coef(d, sd, kfac, b, m, n, nv[0], nv[1], nv[2]);
     }
@@ -1021,8 +1030,9 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
       lin[h.ntri + q] = n > m ? eps(n, m) * (n + 1.0) / n : 0.0;
       lin[2 * h.ntri + q] = static_cast<double>(m) / (static_cast<double>(n) * (n + 1));
     }
-  sp.lin.alloc(lin.size());
-  LMW_CUDA(cudaMemcpy(sp.lin.p, lin.data(), lin.size() * sizeof(double), cudaMemcpyHostToDevice));
+  std::vector<float> lin32(lin.begin(), lin.end());
+  sp.lin32.alloc(lin32.size());
+  LMW_CUDA(cudaMemcpy(sp.lin32.p, lin32.data(), lin32.size() * sizeof(float), cudaMemcpyHostToDevice));
 }
 
 inline SplitDev split_dev(const SplitPlan &sp) {
@@ -1070,7 +1080,7 @@ inline SplitDev split_dev(const SplitPlan &sp) {
   s.fold = nullptr;
   s.err = sp.err.p;
   s.lin_exact = sp.lin_exact;
-  s.lin = sp.lin.p;
+  s.lin32 = sp.lin32.p;
   return s;
 }
 

@@ -1228,7 +1228,7 @@ void Surrogate::normalise(int ntrain) {
       // Phibar a^2 / (n (n + 1)) |zeta, delta|^2 and available potential energy |Phi|^2, both times 2 for m > 0
       const double cm = fm[f] == 0 ? 1.0 : 2.0;
       const double n = fn[f];
-      const double e = fq[f] == 2 ? 1.0 : phibar * a2 / (n * (n + 1.0));
+      const double e = fq[f] == 2 ? 1.0 : ke_weight * phibar * a2 / (n * (n + 1.0));
       hloss[f] = static_cast<float>(cm * e * rd * rd);
       lsum += hloss[f];
       lcount++;

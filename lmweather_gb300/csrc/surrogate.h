@@ -131,6 +131,9 @@ class Surrogate {
   // training loss: 0 = mean square of the per-n normalised increments, 1 = energy norm of the increment error
   // (kinetic energy of the vorticity/divergence errors plus available potential energy of the Phi errors)
   int loss_mode = 1;
+  // weight of the kinetic-energy part of the energy-norm loss against the available potential energy (1: the
+  // energy norm itself; below 1 leans the fit toward the height field)
+  double ke_weight = 1.0;
 
   void reset(uint64_t seed);  // a fresh network and optimiser (the data stay)
   void generate(int trajectories, int windows, uint64_t seed0, double hmin, double hmax, int precision, int batch_members);
