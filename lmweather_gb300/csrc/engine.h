@@ -237,7 +237,7 @@ class SphereEngine {
   void launch_chunk(double dt, int steps);
   void synth_grids(int member_first, int count);  // state x0 -> Fourier coefficients of U, V, zeta, phi
   void reduce_guard(Reduce &r, int member);
-  void reduce_guard_all();
+  void reduce_guard_all(bool exact = true);
   double limit_from(const Reduce &r, int b, double safety) const;
   void analyze_grids_to_state(int member);
   void to_packed(const double *ref_layout, double *packed);

@@ -673,6 +673,38 @@ __global__ void __launch_bounds__(GRID_THREADS) sph_diag_final(SphDev d, const d
   }
 }
 
+// The stability re-check of the reduced-precision engines (cpp/sphere.cpp:473-483 needs only the largest wind
+// speed and height on the grid): FP32 inverse FFTs of U, V and Phi from the FP32 synthesis, per latitude row the
+// maxima into rows[.][5] and rows[.][6] (the other entries zero), combined by sph_diag_final
+__global__ void __launch_bounds__(GRID_THREADS) sph_guard32(SphDev d, SphTab<float> t, const float2 *__restrict__ four, double *__restrict__ rows) {
+  extern __shared__ float2 smf[];
+  __shared__ double red[GRID_THREADS / 32];
+  const int b = blockIdx.y, jh = blockIdx.x;
+  const int js = jh, jn = d.nlat - 1 - jh, n = d.nlon;
+  const float2 *f_s = four + (static_cast<size_t>(b) * d.nlat + js) * 4 * d.M;
+  const float2 *f_n = four + (static_cast<size_t>(b) * d.nlat + jn) * 4 * d.M;
+  load_pair_spectra(smf, 4, d, f_s, f_n, d.M);
+  fft_inverse_dit(smf, 4, n, d.logn, t.tw);
+  const float ic = static_cast<float>(1.0 / d.cosl[js]), ig = static_cast<float>(1.0 / d.g);
+  for (int side = 0; side < 2; side++) {
+    const int j = side == 0 ? js : jn;
+    float wmax = 0.0f, hmax = -INFINITY;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const float2 U = smf[k], V = smf[n + k], P = smf[3 * n + k];
+      const float u = (side ? U.y : U.x) * ic, v = (side ? V.y : V.x) * ic;
+      wmax = fmaxf(wmax, sqrtf(u * u + v * v));
+      hmax = fmaxf(hmax, (side ? P.y : P.x) * ig);
+    }
+    const double w = block_max(static_cast<double>(wmax), red), h = block_max(static_cast<double>(hmax), red);
+    if (threadIdx.x == 0) {
+      double *o = rows + (static_cast<size_t>(b) * d.nlat + j) * DIAG_K;
+      for (int i = 0; i < DIAG_K; i++) o[i] = 0.0;
+      o[5] = w;
+      o[6] = h;
+    }
+  }
+}
+
 // synthesis of a single field's grid (reference grid for mark_reference): Phi rows of `four` -> grid
 __global__ void __launch_bounds__(GRID_THREADS) sph_phi_grid(SphDev d, const double2 *__restrict__ four, double *__restrict__ out) {
   extern __shared__ double2 sm[];
@@ -2009,13 +2041,24 @@ void SphereEngine::reduce_guard(Reduce &r, int member) {
   r = hred.p[0];
 }
 
-// guard reductions of every member in one pass (FP64 synthesis and grid reductions), read back once
-void SphereEngine::reduce_guard_all() {
+// guard reductions of every member in one pass, read back once: FP64 synthesis and grid reductions, or (exact =
+// false, reduced-precision engines) the FP32 synthesis and the FP32 maxima of the stability re-check
+void SphereEngine::reduce_guard_all(bool exact) {
   SphDev d = make_sph(*this, *tab);
-  synth_grids(0, B);
-  const size_t smem = 4 * static_cast<size_t>(nlon) * sizeof(double2);
-  sph_diag<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), fgrid.p, hsgrid.p, refgrid.p, diagrows.p,
-                                                        nullptr);
+  if (!exact && p.precision != kFP64 && !has_tracer) {
+    const int L = syn_lats(nh);
+    auto *k = L == 8 ? sph_synth<float, 8> : sph_synth<float, 32>;
+    k<<<dim3((nh + L - 1) / L, M, B), SYN_THREADS, 0, stream>>>(d, tab32(*tab), reinterpret_cast<const double2 *>(x0.p),
+                                                              reinterpret_cast<float2 *>(four32.p));
+    sph_guard32<<<dim3(nh, B), GRID_THREADS, 4 * static_cast<size_t>(nlon) * sizeof(float2), stream>>>(
+        d, tab32(*tab), reinterpret_cast<const float2 *>(four32.p), diagrows.p);
+    g_launches += 2;
+  } else {
+    synth_grids(0, B);
+    const size_t smem = 4 * static_cast<size_t>(nlon) * sizeof(double2);
+    sph_diag<<<dim3(nh, B), GRID_THREADS, smem, stream>>>(d, reinterpret_cast<const double2 *>(four.p), fgrid.p, hsgrid.p, refgrid.p, diagrows.p,
+                                                          nullptr);
+  }
   sph_diag_final<<<B, GRID_THREADS, 0, stream>>>(d, diagrows.p, reinterpret_cast<const double2 *>(x0.p), 0, dred.p);
   if (has_tracer) trc_abs_sum<<<B, GRID_THREADS, 0, stream>>>(d, reinterpret_cast<const double2 *>(tq0.p), dred.p);
   LMW_LAUNCH_CHECK();
@@ -2059,8 +2102,14 @@ SphereEngine::RunPlan SphereEngine::plan_run(double seconds, double dt) {
   if (!(seconds >= 0)) throw InvalidArgument("run: seconds must not be negative");
   if (advect_only && !has_tracer) throw InvalidArgument("advect_only: set a tracer first (Sphere.tracer)");
   if (seconds == 0) return rp;
-  if (!(dt > 0)) dt = stable_dt_all(1.5);
-  const double limit = stable_dt_all(2.0 * std::sqrt(2.0));
+  // one guard reduction gives both the automatic step (stable_dt(1.5)) and the limit (cpp/sphere.cpp:461-466)
+  reduce_guard_all();
+  double auto_dt = 1e300, limit = 1e300;
+  for (int b = 0; b < B; b++) {
+    auto_dt = std::min(auto_dt, limit_from(hred.p[b], b, 1.5));
+    limit = std::min(limit, limit_from(hred.p[b], b, 2.0 * std::sqrt(2.0)));
+  }
+  if (!(dt > 0)) dt = auto_dt;
   if (!(dt <= limit))
     throw InvalidArgument("run: dt = " + fmt_f(dt) + " s exceeds the RK4 stability limit of about " + fmt_f(limit) +
                           " s for the present state: use a smaller dt");
@@ -2093,7 +2142,8 @@ void SphereEngine::guard(RunPlan &rp) {
   const bool last = rp.i >= rp.n;
   if (!rp.guard_due && !last) return;
   check_split_status();
-  reduce_guard_all();
+  // reduced-precision engines re-check with FP32 grids (a decision about the stability margin, not a result)
+  reduce_guard_all(false);
   for (int b = 0; b < B; b++) {
     const Reduce &r = hred.p[b];
     if (!std::isfinite(r.sum[5])) throw RuntimeError("the integration blew up (not finite): use a smaller dt");
