@@ -290,10 +290,13 @@ int lmw_ensemble_stream(lmw_ensemble *e, int group, void **stream);
  * when an analysis CTA handles both parities of m, out[5] the analysis CTA count (0: one per work item; else
  * persistent CTAs), out[6] 1 when the grid kernel writes the analysis operands (else the analysis gathers them
  * from an FP32 fold), out[7] the analysis kernel's register budget in CTAs per SM (2: 128 registers a thread, 3:
- * 80), out[8] the synthesis's latitude slices per (m, member tile) (1, 2 or 4) (zeros when the engine is not in
- * split precision; out has 9 entries). No reference counterpart. */
+ * 80), out[8] the synthesis's latitude slices per (m, member tile) (1, 2 or 4), out[9] 0 for the analysis kernel
+ * that alternates its MMAs and its epilogue, else the CTAs per SM (1 or 2) of the warp-specialised persistent
+ * analysis (one warp streams operands, one issues MMAs into two tensor-memory accumulators, eight run the epilogue
+ * of the previous item) (zeros when the engine is not in split precision; out has 10 entries). No reference
+ * counterpart. */
 int lmw_sphere_split_plan(lmw_sphere *s, int *out);
-/* replaces the autotuned plan with `plan` (the 9 entries above), checked against the limits the autotuner's
+/* replaces the autotuned plan with `plan` (the 10 entries above), checked against the limits the autotuner's
  * candidates obey (invalid_argument otherwise); every plan computes the same arithmetic. Validation and tuning
  * hook; no reference counterpart. */
 int lmw_sphere_set_split_plan(lmw_sphere *s, const int *plan);

@@ -940,6 +940,8 @@ static void allow_max_shared_memory() {
   for (auto *k : {split_ana<false, false, 2>, split_ana<true, false, 2>, split_ana<false, true, 2>, split_ana<true, true, 2>,
                   split_ana<false, false, 3>, split_ana<true, false, 3>, split_ana<false, true, 3>, split_ana<true, true, 3>})
     LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  for (auto *k : {split_ana_ws<false, 1>, split_ana_ws<true, 1>, split_ana_ws<false, 2>, split_ana_ws<true, 2>})
+    LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_grid<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
@@ -1082,6 +1084,11 @@ SphereEngine::SphereEngine(const SphereConfig &c) : p(c) {
   if (p.precision == kSplitBF16) {
     split = new SplitPlan();
     build_split_plan(*split, h, B, p.split_terms);
+    {
+      int dev = 0;
+      LMW_CUDA(cudaGetDevice(&dev));
+      LMW_CUDA(cudaDeviceGetAttribute(&split->nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
 
   }
   x0.zero(stream);
@@ -1517,15 +1524,26 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   if (which < 0 || which == 2) {
     if (sp.ana_both && 2 * sp.ra_pair > 512) throw InvalidArgument("split precision: both parities' accumulators exceed tensor memory");
     const int items = d.M * (sp.ana_both ? 1 : 2) * sp.ntiles;
+    float2 *ys = reinterpret_cast<float2 *>(xs), *ys2 = reinterpret_cast<float2 *>(xs2);
+    const float2 *xin = stage == 1 || stage == 3 ? ys : (stage == 2 ? ys2 : nullptr);
+    float2 *xout = !sp.lin_exact || stage == 3 ? nullptr : (stage == 1 ? ys2 : ys);
+    if (sp.ana_ws > 0 && sp.direct) {
+      size_t smem = 0;
+      int buf_cols = 0, slot = 0;
+      if (!ws_layout(sp, sp.ana_both, sp.ns_ana, sp.ana_ws, &smem, &buf_cols, &slot))
+        throw InvalidArgument("split precision: the warp-specialised analysis does not fit");
+      const int grid = std::min(items, sp.nsm * sp.ana_ws);
+      auto *k = sp.ana_ws == 2 ? (sp.ana_both ? split_ana_ws<true, 2> : split_ana_ws<false, 2>)
+                               : (sp.ana_both ? split_ana_ws<true, 1> : split_ana_ws<false, 1>);
+      k<<<grid, SPLIT_WS_THREADS, smem, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, buf_cols, slot, x0, xin, xout, acc);
+      return;
+    }
     const int grid = sp.ana_grid > 0 ? std::min(items, sp.ana_grid) : items;
     auto *k = sp.ana_minb >= 3
                   ? (sp.ana_both ? (sp.direct ? split_ana<true, true, 3> : split_ana<true, false, 3>)
                                  : (sp.direct ? split_ana<false, true, 3> : split_ana<false, false, 3>))
                   : (sp.ana_both ? (sp.direct ? split_ana<true, true, 2> : split_ana<true, false, 2>)
                                  : (sp.direct ? split_ana<false, true, 2> : split_ana<false, false, 2>));
-    float2 *ys = reinterpret_cast<float2 *>(xs), *ys2 = reinterpret_cast<float2 *>(xs2);
-    const float2 *xin = stage == 1 || stage == 3 ? ys : (stage == 2 ? ys2 : nullptr);
-    float2 *xout = !sp.lin_exact || stage == 3 ? nullptr : (stage == 1 ? ys2 : ys);
     k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xin, xout, acc);
   }
 }
@@ -1801,6 +1819,7 @@ void SphereEngine::autotune_split() {
     size_t bytes;
     double best;
     int mb = 2;  // analysis register budget (CTAs per SM)
+    int ws = 0;  // analysis: the warp-specialised form with this many CTAs per SM
   };
   std::vector<Cand> cands;
   int dev = 0, optin = 0;
@@ -1833,10 +1852,17 @@ void SphereEngine::autotune_split() {
         cands.push_back({2, both, 0, ns, dir, ba, 1e30, 2});
         // the 80-register form only pays where three CTAs fit in shared memory
         if (3 * (ba + 1024) <= 233472) cands.push_back({2, both, 0, ns, dir, ba, 1e30, 3});
+        // the warp-specialised persistent form (direct operands), one or two CTAs per SM
+        if (dir == 1 && ns >= 2)
+          for (int ctas = 1; ctas <= 2; ctas++) {
+            size_t wsm = 0;
+            int bc = 0, sl = 0;
+            if (ws_layout(sp, both, ns, ctas, &wsm, &bc, &sl)) cands.push_back({2, both, 0, ns, dir, wsm, 1e30, 2, ctas});
+          }
       }
   }
   const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both, ag0 = sp.ana_grid, dir0 = sp.direct,
-            mb0 = sp.ana_minb, sl0 = sp.syn_split;
+            mb0 = sp.ana_minb, sl0 = sp.syn_split, ws0 = sp.ana_ws;
   const size_t sms0 = sp.smem_syn, sma0 = sp.smem_ana;
   auto apply = [&](const Cand &c) {
     sp.jb = jb0;
@@ -1849,6 +1875,7 @@ void SphereEngine::autotune_split() {
     sp.ana_grid = ag0;
     sp.direct = dir0;
     sp.ana_minb = mb0;
+    sp.ana_ws = ws0;
     sp.syn_split = sl0;
     sp.syn_nh = sp.nh16 / sl0;
     if (c.which == 1) {
@@ -1867,6 +1894,7 @@ void SphereEngine::autotune_split() {
       sp.ana_grid = c.fg;
       sp.direct = c.dir;
       sp.ana_minb = c.mb;
+      sp.ana_ws = c.ws;
     }
   };
   // two rounds in opposite orders; each candidate keeps its faster round
@@ -1905,6 +1933,7 @@ void SphereEngine::autotune_split() {
   sp.ana_both = ba ? ba->jb : ab0;
   sp.ana_grid = ba ? ba->fg : ag0;
   sp.ana_minb = ba ? ba->mb : mb0;
+  sp.ana_ws = ba ? ba->ws : ws0;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   check_split_status();
@@ -1921,6 +1950,7 @@ void SphereEngine::split_plan(int *out) const {
   out[6] = split ? split->direct : 0;
   out[7] = split ? split->ana_minb : 0;
   out[8] = split ? split->syn_split : 0;
+  out[9] = split ? split->ana_ws : 0;
 }
 
 void SphereEngine::set_split_form(int linear_exact) {
@@ -1935,7 +1965,7 @@ void SphereEngine::set_split_form(int linear_exact) {
 void SphereEngine::set_split_plan(const int *in) {
   if (!split) throw InvalidArgument("the engine is not in split precision");
   SplitPlan &sp = *split;
-  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6], mb = in[7], sl = in[8];
+  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6], mb = in[7], sl = in[8], ws = in[9];
   int dev = 0, optin = 0;
   LMW_CUDA(cudaGetDevice(&dev));
   LMW_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -1953,6 +1983,13 @@ void SphereEngine::set_split_plan(const int *in) {
   const size_t ba = std::max(sp.ana_res_bytes_v[dir] + nsa * sp.ana_stage_bytes_v[dir] + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
   if (bs > sp.budget_bytes || ba > sp.budget_bytes) throw InvalidArgument("split plan: the pipelines do not fit in shared memory");
   if (mb != 2 && mb != 3) throw InvalidArgument("split plan: the analysis register budget must be 2 or 3 CTAs per SM");
+  size_t wsm = 0;
+  if (ws != 0) {
+    int bc = 0, slot = 0;
+    if (!dir || nsa < 2 || !ws_layout(sp, both, nsa, ws, &wsm, &bc, &slot))
+      throw InvalidArgument("split plan: the warp-specialised analysis takes 1 or 2 CTAs per SM, direct operands, at least 2 stages, and must fit "
+                            "shared and tensor memory");
+  }
   LMW_CUDA(cudaStreamSynchronize(stream));
   sp.jb = jb;
   sp.fgrp = fg;
@@ -1964,6 +2001,8 @@ void SphereEngine::set_split_plan(const int *in) {
   sp.ana_grid = grid;
   sp.direct = dir;
   sp.ana_minb = mb;
+  sp.ana_ws = ws;
+  if (ws) sp.smem_ana = wsm;
   sp.syn_split = sl;
   sp.syn_nh = sp.nh16 / sl;
   graphs_clear();

@@ -66,6 +66,8 @@ struct SplitPlan {
   int ana_both = 0;           // analysis CTAs handle both parities of m
   int ana_grid = 0;           // analysis CTAs (0: one per work item)
   int ana_minb = 2;           // analysis register budget: CTAs per SM (2 or 3)
+  int ana_ws = 0;             // 0: split_ana; 1 or 2: the warp-specialised persistent form with that many CTAs per SM
+  int nsm = 152;              // multiprocessors of the device (the persistent grid)
   int ra_pair = 32;           // largest ra16[2m] + ra16[2m + 1]
   // 1: the linear terms of the tendencies (gravity-wave terms of the mean height, the Laplacian of Phi, the
   // untilted Coriolis terms) in FP64 spectral space; only the nonlinear products go through the BF16 pieces.
@@ -599,6 +601,95 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict
 }
 
 // ------------------------------------------------------------------------------------------- analysis + RK4
+// The analysis epilogue of one coefficient (member b = tile member ml, wavenumber m, parity s, index r: n = m + s + 2r)
+// from the accumulators staged in shared memory (dsm, row stride ldp): the tendencies (cpp/sphere.cpp:380-389) with
+// the linear terms of the linear-exact form, the RK4 stage update of the FP64 state, the next stage input and the
+// next synthesis operands. Shared by both analysis kernels, so both give the same bits.
+__device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, const SphTab<float> &t, const double *__restrict__ kfac, const StageArgs &sa,
+                                         double2 *__restrict__ x0, const float2 *__restrict__ xin, float2 *__restrict__ xout,
+                                         double2 *__restrict__ acc, const float *dsm, int ldp, int m, int tile, int ml, int s, int r, int cb1,
+                                         int ra0, int ra1) {
+  const int b = tile * sd.nbt + ml, n = m + s + 2 * r;
+  const int cbs = s ? cb1 : 0, ras = s ? ra1 : ra0;
+  const float *H = dsm + (ml * 6) * ldp + cbs + r, *P = dsm + (ml * 8) * ldp + cbs + ras + r;
+  const float2 aH = make_float2(H[0 * ldp], H[1 * ldp]), bH = make_float2(H[2 * ldp], H[3 * ldp]), vH = make_float2(H[4 * ldp], H[5 * ldp]);
+  const float2 aP = make_float2(P[0 * ldp], P[1 * ldp]), bP = make_float2(P[2 * ldp], P[3 * ldp]);
+  const float2 uP = make_float2(P[4 * ldp], P[5 * ldp]), eP = make_float2(P[6 * ldp], P[7 * ldp]);
+  const float mm = static_cast<float>(m);
+  // cpp/sphere.cpp:380-389
+  float2 kz = csub(bH, imul(aP, mm));
+  float2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
+  float2 kf = csub(vH, imul(uP, mm));
+  const int q = d.tri[m] + n - m;
+  const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
+  if (sd.lin_exact && q != 0) {
+    // the terms linear in the stage input y, in FP32 like the rest of the tendencies but outside the BF16 products
+    // (x0 at stage 0, else the previous stage's output rounded to FP32 in a separate buffer: neighbouring n belong
+    // to other CTAs): n(n+1)/a^2 Phi_n in d delta; -Phi_mean delta_n in d Phi (D(U, V) = delta exactly for n <= T);
+    // for an untilted axis the Coriolis terms -D(f U, f V) and D(f V, -f U) with f = 2 Omega mu, which couple
+    // n - 1, n, n + 1 of the same m
+    const size_t mb = static_cast<size_t>(b) * 3 * d.ntri;
+    auto yat = [&](int field, int qq) -> float2 {
+      if (sa.stage == 0) {
+        const double2 v = x0[mb + static_cast<size_t>(field) * d.ntri + qq];
+        return make_float2(d2f_int(v.x), d2f_int(v.y));
+      }
+      return xin[mb + static_cast<size_t>(field) * d.ntri + qq];
+    };
+    const float2 yz = yat(0, q), yd = yat(1, q), yf = yat(2, q);
+    const float phibar = d2f_int(x0[mb + 2 * d.ntri].x) * t.Ps[0];
+    const float lp = t.lapl[n];
+    kd.x += lp * yf.x;
+    kd.y += lp * yf.y;
+    kf.x -= phibar * yd.x;
+    kf.y -= phibar * yd.y;
+    if (!(d.gflag[b] & 1)) {
+      const float om = static_cast<float>(d.om2[b]);
+      const float cA = sd.lin32[q], cB = sd.lin32[d.ntri + q], cC = sd.lin32[2 * d.ntri + q];
+      const float2 zu = n < d.N ? yat(0, q + 1) : make_float2(0, 0), du = n < d.N ? yat(1, q + 1) : make_float2(0, 0);
+      const float2 zl = n > m ? yat(0, q - 1) : make_float2(0, 0), dd = n > m ? yat(1, q - 1) : make_float2(0, 0);
+      // -D(fU, fV)_n = -2 Omega (cA delta_{n+1} + cB delta_{n-1} - i cC zeta_n)
+      kz.x -= om * (cA * du.x + cB * dd.x + cC * yz.y);
+      kz.y -= om * (cA * du.y + cB * dd.y - cC * yz.x);
+      // D(fV, -fU)_n = 2 Omega (cA zeta_{n+1} + cB zeta_{n-1} + i cC delta_n)
+      kd.x += om * (cA * zu.x + cB * zl.x - cC * yd.y);
+      kd.y += om * (cA * zu.y + cB * zl.y + cC * yd.x);
+    }
+  }
+  if (q == 0) kz = kd = kf = make_float2(0, 0);
+  const double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
+                        make_double2(f2d_int(kf.x), f2d_int(kf.y))};
+  // every load of the three fields is issued before any store (the buffers never alias)
+  double2 xv[3], av[3];
+#pragma unroll
+  for (int f = 0; f < 3; f++) {
+    xv[f] = x0[base + static_cast<size_t>(f) * d.ntri];
+    av[f] = sa.stage > 0 ? acc[base + static_cast<size_t>(f) * d.ntri] : make_double2(0.0, 0.0);
+  }
+  double2 nv[3];
+#pragma unroll
+  for (int f = 0; f < 3; f++) {
+    const size_t i = base + static_cast<size_t>(f) * d.ntri;
+    if (sa.stage == 0) {
+      acc[i] = k[f];
+      nv[f] = cadd(xv[f], cscale(k[f], sa.c));
+    } else if (sa.stage < 3) {
+      acc[i] = cadd(av[f], cscale(k[f], 2.0));
+      nv[f] = cadd(xv[f], cscale(k[f], sa.c));
+    } else {
+      const double2 val = cadd(xv[f], cscale(cadd(av[f], k[f]), sa.c));
+      const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
+      nv[f] = q == 0 ? val : cscale(val, fac);
+      x0[i] = nv[f];
+    }
+    // the next stage input rounded to FP32 is kept when a caller asks for it (the linear-exact form reads it;
+    // the split synthesis reads the packed operands written below)
+    if (xout != nullptr && sa.stage < 3) xout[i] = make_float2(d2f_int(nv[f].x), d2f_int(nv[f].y));
+  }
+  pack_syn_coef(d, sd, kfac, b, m, n, nv[0], nv[1], nv[2]);
+}
+
+
 // BOTH = false: grid (M, 2, ntiles), one parity s = blockIdx.y per CTA. BOTH = true: grid (M, 1, ntiles), both
 // parities in one CTA one after the other (the GEMM pipeline's barriers continue their phases), so the epilogue
 // walks every n of m in order and the FP64 state is read and written with unit stride. Accumulator columns of
@@ -641,20 +732,6 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
   // the previous item's epilogue has finished reading shared memory and tensor memory
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  // while two threads run the GEMM pipeline, the others ask L2 for the FP64 state lines the epilogue will read
-  if (threadIdx.x >= 64) {
-    const int cnt = BOTH ? d.N - m + 1 : (s_first ? R1 : R0);
-    for (int e = threadIdx.x - 64; e < mt * cnt; e += blockDim.x - 64) {
-      const int ml = e / cnt, j = e - ml * cnt;
-      const int off = BOTH ? j : s_first + 2 * j;
-      const size_t base = static_cast<size_t>(tile * sd.nbt + ml) * 3 * d.ntri + d.tri[m] + off;
-#pragma unroll
-      for (int f = 0; f < 3; f++) {
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(x0 + base + static_cast<size_t>(f) * d.ntri));
-        if (sa.stage > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(acc + base + static_cast<size_t>(f) * d.ntri));
-      }
-    }
-  }
   for (int s = s_first; s <= s_last && ok; s++) {
   if ((s ? R1 : R0) == 0) break;
   if (!DIRECT) {
@@ -776,88 +853,236 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
     for (int e = threadIdx.x; e < mt * cnt; e += blockDim.x) {
       const int ml = e / cnt, j = e - ml * cnt;
       const int s = BOTH ? (j & 1) : s_first, r = BOTH ? (j >> 1) : j;
-      const int b = tile * sd.nbt + ml, n = m + s + 2 * r;
-      const int cbs = s ? cb1 : 0, ras = s ? ra1 : ra0;
-      const float *H = dsm + (ml * 6) * ldp + cbs + r, *P = dsm + (ml * 8) * ldp + cbs + ras + r;
-      const float2 aH = make_float2(H[0 * ldp], H[1 * ldp]), bH = make_float2(H[2 * ldp], H[3 * ldp]), vH = make_float2(H[4 * ldp], H[5 * ldp]);
-      const float2 aP = make_float2(P[0 * ldp], P[1 * ldp]), bP = make_float2(P[2 * ldp], P[3 * ldp]);
-      const float2 uP = make_float2(P[4 * ldp], P[5 * ldp]), eP = make_float2(P[6 * ldp], P[7 * ldp]);
-      const float mm = static_cast<float>(m);
-      // cpp/sphere.cpp:380-389
-      float2 kz = csub(bH, imul(aP, mm));
-      float2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
-      float2 kf = csub(vH, imul(uP, mm));
-      const int q = d.tri[m] + n - m;
-      const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
-      if (sd.lin_exact && q != 0) {
-        // the terms linear in the stage input y, in FP32 like the rest of the tendencies but outside the BF16 products
-        // (x0 at stage 0, else the previous stage's output rounded to FP32 in a separate buffer: neighbouring n belong
-        // to other CTAs): n(n+1)/a^2 Phi_n in d delta; -Phi_mean delta_n in d Phi (D(U, V) = delta exactly for n <= T);
-        // for an untilted axis the Coriolis terms -D(f U, f V) and D(f V, -f U) with f = 2 Omega mu, which couple
-        // n - 1, n, n + 1 of the same m
-        const size_t mb = static_cast<size_t>(b) * 3 * d.ntri;
-        auto yat = [&](int field, int qq) -> float2 {
-          if (sa.stage == 0) {
-            const double2 v = x0[mb + static_cast<size_t>(field) * d.ntri + qq];
-            return make_float2(d2f_int(v.x), d2f_int(v.y));
-          }
-          return xin[mb + static_cast<size_t>(field) * d.ntri + qq];
-        };
-        const float2 yz = yat(0, q), yd = yat(1, q), yf = yat(2, q);
-        const float phibar = d2f_int(x0[mb + 2 * d.ntri].x) * t.Ps[0];
-        const float lp = t.lapl[n];
-        kd.x += lp * yf.x;
-        kd.y += lp * yf.y;
-        kf.x -= phibar * yd.x;
-        kf.y -= phibar * yd.y;
-        if (!(d.gflag[b] & 1)) {
-          const float om = static_cast<float>(d.om2[b]);
-          const float cA = sd.lin32[q], cB = sd.lin32[d.ntri + q], cC = sd.lin32[2 * d.ntri + q];
-          const float2 zu = n < d.N ? yat(0, q + 1) : make_float2(0, 0), du = n < d.N ? yat(1, q + 1) : make_float2(0, 0);
-          const float2 zl = n > m ? yat(0, q - 1) : make_float2(0, 0), dd = n > m ? yat(1, q - 1) : make_float2(0, 0);
-          // -D(fU, fV)_n = -2 Omega (cA delta_{n+1} + cB delta_{n-1} - i cC zeta_n)
-          kz.x -= om * (cA * du.x + cB * dd.x + cC * yz.y);
-          kz.y -= om * (cA * du.y + cB * dd.y - cC * yz.x);
-          // D(fV, -fU)_n = 2 Omega (cA zeta_{n+1} + cB zeta_{n-1} + i cC delta_n)
-          kd.x += om * (cA * zu.x + cB * zl.x - cC * yd.y);
-          kd.y += om * (cA * zu.y + cB * zl.y + cC * yd.x);
-        }
-      }
-      if (q == 0) kz = kd = kf = make_float2(0, 0);
-      const double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
-                            make_double2(f2d_int(kf.x), f2d_int(kf.y))};
-      // every load of the three fields is issued before any store (the buffers never alias)
-      double2 xv[3], av[3];
-#pragma unroll
-      for (int f = 0; f < 3; f++) {
-        xv[f] = x0[base + static_cast<size_t>(f) * d.ntri];
-        av[f] = sa.stage > 0 ? acc[base + static_cast<size_t>(f) * d.ntri] : make_double2(0.0, 0.0);
-      }
-      double2 nv[3];
-#pragma unroll
-      for (int f = 0; f < 3; f++) {
-        const size_t i = base + static_cast<size_t>(f) * d.ntri;
-        if (sa.stage == 0) {
-          acc[i] = k[f];
-          nv[f] = cadd(xv[f], cscale(k[f], sa.c));
-        } else if (sa.stage < 3) {
-          acc[i] = cadd(av[f], cscale(k[f], 2.0));
-          nv[f] = cadd(xv[f], cscale(k[f], sa.c));
-        } else {
-          const double2 val = cadd(xv[f], cscale(cadd(av[f], k[f]), sa.c));
-          const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
-          nv[f] = q == 0 ? val : cscale(val, fac);
-          x0[i] = nv[f];
-        }
-        // the next stage input rounded to FP32 is kept when a caller asks for it (the linear-exact form reads it;
-        // the split synthesis reads the packed operands written below)
-        if (xout != nullptr && sa.stage < 3) xout[i] = make_float2(d2f_int(nv[f].x), d2f_int(nv[f].y));
-      }
-      pack_syn_coef(d, sd, kfac, b, m, n, nv[0], nv[1], nv[2]);
+      ana_coef(d, sd, t, kfac, sa, x0, xin, xout, acc, dsm, ldp, m, tile, ml, s, r, cb1, ra0, ra1);
     }
   }
   }
   if (setup_done) split_teardown(tslot, ncols);
+}
+
+// ------------------------------------------------------------------------------------------- analysis, warp-specialised
+// The same work as split_ana (direct operands), by persistent CTAs whose warps take roles, so that one item's
+// epilogue runs while the next item's operands load and multiply: thread 0 streams the H and P chunks of the CTA's
+// items (m, parity or both, member tile) through a ring of ns fixed-size stages; thread 32 issues the MMAs of item i
+// into tensor-memory accumulator buffer i % 2 and commits it to accf[i % 2]; warps 2..9 (256 threads) wait for it,
+// copy it to shared memory, release the buffer (acce[i % 2]) and run the epilogue (ana_coef, the same arithmetic as
+// split_ana). Items are visited with m the fastest index. Every wait is bounded; after a failure each role stops,
+// the CTA drains its own copies and MMAs and frees its tensor memory.
+constexpr int SPLIT_WS_THREADS = 320;
+constexpr int SPLIT_WS_EPI = 256;  // epilogue threads (warps 2..9)
+template <bool BOTH, int CTAS>
+__global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
+                                                                    int B, int ns, int buf_cols, int slot_bytes, double2 *__restrict__ x0,
+                                                                    const float2 *__restrict__ xin, float2 *__restrict__ xout,
+                                                                    double2 *__restrict__ acc) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], accf[2], acce[2], done;
+  __shared__ uint32_t tslot;
+  __shared__ int s_fail, s_issued, s_consumed, s_epi_ok;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int per_m = (BOTH ? 1 : 2) * sd.ntiles;
+  const int nitems = d.M * per_m;
+  const int nchunk = sd.nha / sd.bka;
+  const int bk = sd.bka;
+  const uint32_t ncols = 2u * static_cast<uint32_t>(buf_cols);
+  uint8_t *pipe = smem;
+  float *dsm = reinterpret_cast<float *>(smem + static_cast<size_t>(ns) * slot_bytes);
+  const int a_bytes = sd.rAP * bk * 2;  // A piece region of a stage (the H operand's 6 rows per member fit in it)
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tslot)), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int st = 0; st < ns; st++) {
+      tc::bar_init(su32(&full[st]), 1);
+      tc::bar_init(su32(&empty[st]), 1);
+    }
+    for (int b2 = 0; b2 < 2; b2++) {
+      tc::bar_init(su32(&accf[b2]), 1);
+      tc::bar_init(su32(&acce[b2]), 1);
+    }
+    tc::bar_init(su32(&done), 1);
+    tc::bar_init_fence();
+    s_fail = 0;
+    s_issued = 0;
+    s_consumed = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tslot;
+  // the item sequence every role walks: (m, parity or both, tile), m fastest
+  auto item_of = [&](int item, int &m, int &s_first, int &s_last, int &tile, int &R0, int &R1) {
+    m = item % d.M;
+    const int rest = item / d.M;
+    s_first = BOTH ? 0 : rest % 2;
+    tile = BOTH ? rest : rest / 2;
+    R0 = (d.N - m) / 2 + 1;
+    R1 = (d.N - m + 1) / 2;
+    s_last = BOTH ? (R1 > 0 ? 1 : 0) : s_first;
+  };
+  if (tid == 0) {
+    // producer
+    int git = 0;
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      int m, s_first, s_last, tile, R0, R1;
+      item_of(item, m, s_first, s_last, tile, R0, R1);
+      if ((s_first ? R1 : R0) == 0) continue;
+      for (int s = s_first; s <= s_last && ok; s++) {
+        const int ra = sd.ra16[2 * m + s];
+        const uint32_t bbytes = static_cast<uint32_t>(ra * bk * 2);
+        for (int g = 0; g < 2 && ok; g++) {
+          const int aR = g == 0 ? sd.rAH : sd.rAP;
+          const uint32_t abytes = static_cast<uint32_t>(aR * bk * 2);
+          const __nv_bfloat16 *A = (g == 0 ? sd.aA_H : sd.aA_P) + ((static_cast<long>(m) * 2 + s) * sd.ntiles + tile) * aR * sd.nha;
+          const long aps = g == 0 ? sd.aAH_size : sd.aAP_size;
+          const __nv_bfloat16 *Bt = (g == 0 ? sd.tA_H : sd.tA_P) + sd.tA_off[2 * m + s];
+          for (int c = 0; c < nchunk; c++, git++) {
+            const int st = git % ns;
+            if (git >= ns && !mbar_wait_bounded(su32(&empty[st]), ((git / ns) - 1) & 1)) {
+              s_fail = 1;
+              atomicExch(sd.err, 2);
+              ok = false;
+              break;
+            }
+            mbar_expect(su32(&full[st]), static_cast<uint32_t>(sd.pieces) * (abytes + bbytes));
+            uint8_t *base = pipe + static_cast<size_t>(st) * slot_bytes;
+            for (int p = 0; p < sd.pieces; p++) {
+              bulk_g2s(su32(base + p * a_bytes), A + p * aps + static_cast<long>(c) * aR * bk, abytes, su32(&full[st]));
+              bulk_g2s(su32(base + sd.pieces * a_bytes + p * static_cast<int>(bbytes)), Bt + p * sd.tA_size + static_cast<long>(c) * ra * bk, bbytes,
+                       su32(&full[st]));
+            }
+            s_issued = git + 1;
+          }
+        }
+      }
+    }
+  } else if (tid == 32) {
+    // MMA issuer
+    const int tp[6][2] = {{2, 0}, {1, 1}, {0, 2}, {1, 0}, {0, 1}, {0, 0}};
+    const int t0 = sd.terms == 6 ? 0 : (sd.terms == 3 ? 3 : 5);
+    const uint32_t sbo = static_cast<uint32_t>(bk) * 16u;
+    int git = 0, it = 0;
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      int m, s_first, s_last, tile, R0, R1;
+      item_of(item, m, s_first, s_last, tile, R0, R1);
+      if ((s_first ? R1 : R0) == 0) continue;
+      const int bb = it & 1;
+      // the epilogue has copied out what this buffer held two items ago
+      if (it >= 2 && !mbar_wait_bounded(su32(&acce[bb]), ((it >> 1) - 1) & 1)) {
+        s_fail = 1;
+        atomicExch(sd.err, 5);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int ra0 = sd.ra16[2 * m];
+      const int cb1 = BOTH ? 2 * ra0 : 0;
+      for (int s = s_first; s <= s_last && ok; s++) {
+        const int ra = sd.ra16[2 * m + s];
+        const uint32_t idesc = idesc_m128(ra);
+        const int bbytes = ra * bk * 2;
+        for (int g = 0; g < 2 && ok; g++) {
+          const uint32_t accc = tmem + static_cast<uint32_t>(bb * buf_cols + (s ? cb1 : 0) + (g ? ra : 0));
+          for (int c = 0; c < nchunk; c++, git++) {
+            const int st = git % ns;
+            if (!mbar_wait_bounded(su32(&full[st]), (git / ns) & 1)) {
+              s_fail = 1;
+              atomicExch(sd.err, 3);
+              ok = false;
+              break;
+            }
+            s_consumed = git + 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            uint8_t *base = pipe + static_cast<size_t>(st) * slot_bytes;
+            for (int kk = 0; kk < bk; kk += 16) {
+              for (int tt = t0; tt < 6; tt++) {
+                const int pa = tp[tt][0], pb = tp[tt][1];
+                const uint64_t ad = chunk_desc(su32(base + pa * a_bytes + (kk / 8) * 128), sbo);
+                const uint64_t bd = chunk_desc(su32(base + sd.pieces * a_bytes + pb * bbytes + (kk / 8) * 128), sbo);
+                const uint32_t accum = (c > 0 || kk > 0 || tt > t0) ? 1u : 0u;
+                asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(accc),
+                             "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+                             : "memory");
+              }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&empty[st])) : "memory");
+          }
+        }
+      }
+      if (!ok) break;
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&accf[bb])) : "memory");
+      it++;
+    }
+    // completes `done` when every MMA issued has finished (the drain after a failure waits on it)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&done)) : "memory");
+  } else if (warp >= 2) {
+    // epilogue warps
+    const int et = tid - 64;
+    int it = 0;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+      int m, s_first, s_last, tile, R0, R1;
+      item_of(item, m, s_first, s_last, tile, R0, R1);
+      if ((s_first ? R1 : R0) == 0) continue;
+      const int bb = it & 1;
+      if (et == 0) s_epi_ok = mbar_wait_bounded(su32(&accf[bb]), (it >> 1) & 1) ? 1 : 0;
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (!s_epi_ok) {
+        if (et == 0) {
+          s_fail = 1;
+          atomicExch(sd.err, 6);
+        }
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int mt = min(sd.nbt, B - tile * sd.nbt);
+      const int ra0 = sd.ra16[2 * m], ra1 = sd.ra16[2 * m + 1];
+      const int cb1 = BOTH ? 2 * ra0 : 0;
+      const int ld = BOTH ? 2 * (ra0 + (s_last ? ra1 : 0)) : 2 * (s_first ? ra1 : ra0);
+      const int ldp = ld + 1;
+      // accumulators -> shared memory: warp w reads tensor-memory lanes 32 (w % 4) .. + 31; warps 2..5 take the even
+      // 32-column blocks, warps 6..9 the odd ones
+      const int quarter = warp & 3, row = quarter * 32 + lane;
+      const uint32_t lanebase = tmem + static_cast<uint32_t>(bb * buf_cols) + (static_cast<uint32_t>(quarter * 32) << 16);
+      if (quarter * 32 < 8 * mt) {
+        for (int c = (warp < 6 ? 0 : 32); c < ld; c += 64) {
+          float v[32];
+          tmem_ld32(lanebase + c, v);
+          if (row < 8 * mt) {
+#pragma unroll
+            for (int i = 0; i < 32; i++) dsm[row * ldp + c + i] = v[i];
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (et == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&acce[bb])) : "memory");
+      const int cnt = BOTH ? d.N - m + 1 : (s_first ? R1 : R0);
+      for (int e = et; e < mt * cnt; e += SPLIT_WS_EPI) {
+        const int ml = e / cnt, j = e - ml * cnt;
+        const int s = BOTH ? (j & 1) : s_first, r = BOTH ? (j >> 1) : j;
+        ana_coef(d, sd, t, kfac, sa, x0, xin, xout, acc, dsm, ldp, m, tile, ml, s, r, cb1, ra0, ra1);
+      }
+      // the shared accumulator copy is free for the next item
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      it++;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    // every MMA issued has finished (and its arrivals landed) before the CTA releases its memory; after a failure the
+    // waits are short and also cover the copies no MMA consumed
+    if (!s_fail) {
+      if (!mbar_wait_bounded(su32(&done), 0)) atomicExch(sd.err, 4);
+    } else {
+      tc::wait_for(su32(&done), 0, 200000000ull);
+      for (int g2 = s_consumed; g2 < s_issued; g2++) tc::wait_for(su32(&full[g2 % ns]), (g2 / ns) & 1, 200000000ull);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
 }
 
 }  // namespace
@@ -1033,6 +1258,25 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   std::vector<float> lin32(lin.begin(), lin.end());
   sp.lin32.alloc(lin32.size());
   LMW_CUDA(cudaMemcpy(sp.lin32.p, lin32.data(), lin32.size() * sizeof(float), cudaMemcpyHostToDevice));
+}
+
+// shared-memory layout of the warp-specialised analysis for one parity (both = 0) or both per item and ns stages:
+// stage slots of a fixed size, then the accumulator copy, then the margin an M = 128 MMA may read past an A base.
+// Returns false when the form does not fit (tensor memory: two accumulator buffers per CTA, `ctas` CTAs per SM).
+inline bool ws_layout(const SplitPlan &sp, int both, int ns, int ctas, size_t *smem, int *buf_cols, int *slot) {
+  const int ldmax = both ? 2 * sp.ra_pair : 2 * sp.ra_max;
+  int bc = 32;
+  while (bc < ldmax) bc <<= 1;
+  const size_t sl = static_cast<size_t>(sp.pieces) * (sp.rAP + sp.ra_max) * sp.bka * 2;
+  const size_t dsm = (static_cast<size_t>(sp.rAP) * (ldmax + 1) * sizeof(float) + 15) & ~static_cast<size_t>(15);
+  const size_t total = ns * sl + dsm + SPLIT_MARGIN;
+  *smem = total;
+  *buf_cols = bc;
+  *slot = static_cast<int>(sl);
+  if (2 * bc * ctas > 512) return false;
+  if (total > sp.budget_bytes) return false;
+  if (ctas == 2 && 2 * (total + 1024 + 2048) > 233472) return false;
+  return ctas == 1 || ctas == 2;
 }
 
 inline SplitDev split_dev(const SplitPlan &sp) {

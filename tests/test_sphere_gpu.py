@@ -365,10 +365,26 @@ def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
         plans.append(dict(analysis_ctas=37, analysis_both_parities=both, analysis_stages=2))
     if s.nlat // 2 >= 32:
         plans.append(dict(synthesis_latitude_slices=2, synthesis_stages=2))
+    # the warp-specialised persistent analysis (operands streamed by one thread, MMAs by another into two
+    # tensor-memory accumulators, the epilogue of the previous item by eight warps), where it fits
+    ws_plans = []
+    for both in (0, 1):
+        for ctas in (1, 2):
+            for ns in (2, 3):
+                ws_plans.append(dict(analysis_warp_specialised=ctas, analysis_both_parities=both, grid_writes_operands=1, analysis_stages=ns))
     tuned = s.split_plan()
+    accepted = []
+    for plan in ws_plans:
+        try:
+            s.set_split_plan(**{**tuned, **plan})
+            accepted.append(plan)
+        except ValueError:
+            pass
+    assert dict(analysis_warp_specialised=1, analysis_both_parities=0, grid_writes_operands=1, analysis_stages=2) in accepted
+    plans += accepted
     results = []
     for plan in [{}] + plans:
-        s.set_split_plan(**{**tuned, **plan})
+        s.set_split_plan(**{**tuned, **({} if not plan else {"analysis_warp_specialised": 0}), **plan})
         for b in range(members):
             s.set_state(*start[b], member=b)
         for _ in range(3):
