@@ -1504,8 +1504,9 @@ static void stage_kernels(const SphDev &d, const SphTab<R> &t, int B, int stage,
 // update (which also packs the next stage's synthesis operands)
 // xs, xs2: the stage inputs (rounded to FP32, in the first half of each FP64 buffer) that the linear-exact form keeps,
 // in turn (stage 0 writes xs, 1 reads xs and writes xs2, 2 reads xs2 and writes xs, 3 reads xs): an analysis CTA
-// reads neighbouring coefficients that other CTAs update
-static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan &sp, const double *kfac64, int B, int stage, double dt,
+// reads neighbouring coefficients that other CTAs update. The second half of xs holds the state rounded to FP32
+// (written by the last stage and by split_pack_state); acc is the FP32 RK4 accumulator (first half).
+static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan &sp, int B, int stage, double dt,
                         const double *filt, float2 *fold, double2 *x0, double2 *xs, double2 *xs2, double2 *acc, const double *fgrid,
                         const double *hsgrid, cudaStream_t stream, int which = -1) {
   SplitDev sd = split_dev(sp);
@@ -1513,6 +1514,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   StageArgs sa;
   sa.stage = stage;
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
+  sa.c32 = static_cast<float>(sa.c);
   sa.filt = filt;
   if (which < 0 || which == 0) split_syn<<<dim3(sp.ntiles, sp.syn_split, d.M), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
   if (which < 0 || which == 1) {
@@ -1525,6 +1527,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
     if (sp.ana_both && 2 * sp.ra_pair > 512) throw InvalidArgument("split precision: both parities' accumulators exceed tensor memory");
     const int items = d.M * (sp.ana_both ? 1 : 2) * sp.ntiles;
     float2 *ys = reinterpret_cast<float2 *>(xs), *ys2 = reinterpret_cast<float2 *>(xs2);
+    float2 *xf = ys + static_cast<size_t>(B) * 3 * d.ntri, *ac = reinterpret_cast<float2 *>(acc);
     const float2 *xin = stage == 1 || stage == 3 ? ys : (stage == 2 ? ys2 : nullptr);
     float2 *xout = !sp.lin_exact || stage == 3 ? nullptr : (stage == 1 ? ys2 : ys);
     if (sp.ana_ws > 0 && sp.direct) {
@@ -1535,7 +1538,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
       const int grid = std::min(items, sp.nsm * sp.ana_ws);
       auto *k = sp.ana_ws == 2 ? (sp.ana_both ? split_ana_ws<true, 2> : split_ana_ws<false, 2>)
                                : (sp.ana_both ? split_ana_ws<true, 1> : split_ana_ws<false, 1>);
-      k<<<grid, SPLIT_WS_THREADS, smem, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, buf_cols, slot, x0, xin, xout, acc);
+      k<<<grid, SPLIT_WS_THREADS, smem, stream>>>(d, sd, t, sa, B, sp.ns_ana, buf_cols, slot, x0, xf, xin, xout, ac);
       return;
     }
     const int grid = sp.ana_grid > 0 ? std::min(items, sp.ana_grid) : items;
@@ -1544,7 +1547,7 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
                                  : (sp.direct ? split_ana<false, true, 3> : split_ana<false, false, 3>))
                   : (sp.ana_both ? (sp.direct ? split_ana<true, true, 2> : split_ana<true, false, 2>)
                                  : (sp.direct ? split_ana<false, true, 2> : split_ana<false, false, 2>));
-    k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, kfac64, sa, B, sp.ns_ana, x0, xin, xout, acc);
+    k<<<grid, SPLIT_ANA_THREADS, sp.smem_ana, stream>>>(d, sd, t, sa, B, sp.ns_ana, x0, xf, xin, xout, ac);
   }
 }
 
@@ -1570,7 +1573,7 @@ void SphereEngine::launch_stage(int stage, double dt) {
                          X0, XS, AC, fgrid.p, hsgrid.p, stream);
     g_launches += 3;
   } else {
-    split_stage(d, tab32(*tab), *split, tab->kfac.p, B, stage, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, XS2(), AC, fgrid.p,
+    split_stage(d, tab32(*tab), *split, B, stage, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, XS2(), AC, fgrid.p,
                 hsgrid.p, stream);
     g_launches += 3;
   }
@@ -1737,6 +1740,7 @@ void SphereEngine::tracer_diagnostics(double *out, int member) {
 
 void SphereEngine::kernel_times(double dt, int reps, double *out) {
   upload_filter(dt);
+  ensure_packed();
   SphDev d = make_sph(*this, *tab);
   double2 *X0 = reinterpret_cast<double2 *>(x0.p), *XS = reinterpret_cast<double2 *>(xs.p), *AC = reinterpret_cast<double2 *>(acc.p);
   // stage 1 reads x0 and writes the stage input and the accumulator: x0 is unchanged
@@ -1748,7 +1752,7 @@ void SphereEngine::kernel_times(double dt, int reps, double *out) {
       stage_kernels<float>(d, tab32(*tab), B, 1, dt, filt.p, X0, reinterpret_cast<float2 *>(four32.p), reinterpret_cast<float2 *>(fold32.p),
                            X0, XS, AC, fgrid.p, hsgrid.p, stream, which);
     else
-      split_stage(d, tab32(*tab), *split, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, XS2(), AC, fgrid.p,
+      split_stage(d, tab32(*tab), *split, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, XS2(), AC, fgrid.p,
                   hsgrid.p, stream, which);
   };
   cudaEvent_t e0, e1;
@@ -1786,7 +1790,7 @@ void SphereEngine::autotune_split() {
   LMW_CUDA(cudaEventCreate(&e0));
   LMW_CUDA(cudaEventCreate(&e1));
   auto launch = [&](int which) {
-    split_stage(d, tab32(*tab), sp, tab->kfac.p, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, XS2(), AC, fgrid.p, hsgrid.p, stream,
+    split_stage(d, tab32(*tab), sp, B, 1, dt, filt.p, reinterpret_cast<float2 *>(fold32.p), X0, XS, XS2(), AC, fgrid.p, hsgrid.p, stream,
                 which);
     g_launches += 1;
   };
@@ -2012,7 +2016,8 @@ void SphereEngine::set_split_plan(const int *in) {
 void SphereEngine::ensure_packed() {
   if (!split || split_packed) return;
   SphDev d = make_sph(*this, *tab);
-  split_pack_state<<<dim3((ntri + 127) / 128, B), 128, 0, stream>>>(d, split_dev(*split), tab->kfac.p, reinterpret_cast<const double2 *>(x0.p));
+  split_pack_state<<<dim3((ntri + 127) / 128, B), 128, 0, stream>>>(d, split_dev(*split), tab->kfac32.p, reinterpret_cast<const double2 *>(x0.p),
+                                                                     reinterpret_cast<float2 *>(xs.p) + static_cast<size_t>(B) * 3 * ntri);
   LMW_LAUNCH_CHECK();
   g_launches += 1;
   split_packed = true;

@@ -87,6 +87,7 @@ constexpr int NSLOT = 5;  // A, B, U Phi, V Phi (times w/((1-mu^2)a)) and the Be
 struct StageArgs {
   int stage;        // 0..3
   double c;         // 0.5 dt, 0.5 dt, dt, dt/6
+  float c32 = 0.0f;    // c rounded to FP32 (the split path's stages 0-2)
   const double *filt;  // [2][M]: zeta/delta and phi factors by n (last stage)
   int zero = 0;        // advect-only: the flow's tendencies are zero (cpp/sphere.cpp:411-415)
 };

@@ -569,46 +569,53 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
 }
 
 // ------------------------------------------------------------------------------------------- synthesis operands
-// The next synthesis operands for coefficient (member b, m, n) from its state value: psi, chi, zeta, Phi (P
-// rows) and psi, chi (H rows) at column k(n) of wavenumber m.
-__device__ __forceinline__ void pack_syn_coef(const SphDev &d, const SplitDev &sd, const double *__restrict__ kfac, int b, int m, int n,
-                                              double2 z, double2 dl, double2 f) {
+// The next synthesis operands for coefficient (member b, m, n) from its value rounded to FP32: psi, chi, zeta, Phi
+// (P rows) and psi, chi (H rows) at column k(n) of wavenumber m; kf = -a^2 / (n (n + 1)) in FP32.
+__device__ __forceinline__ void pack_syn_coef(const SphDev &d, const SplitDev &sd, float kf, int b, int m, int n, float2 z, float2 dl, float2 f) {
   const int tile = b / sd.nbt, ml = b - tile * sd.nbt;
   const int ke16 = sd.ke16[m];
   const int k = ((n - m) & 1) ? ke16 + ((n - m - 1) >> 1) : ((n - m) >> 1);
   const long kp = sd.kps[m];
   const long baseP = sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kp;
   const long baseH = sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kp;
-  // psi, chi = -a^2 / (n (n + 1)) (zeta, delta) in FP32 (the operands carry 16 or 24 bits); conversions on the
-  // integer pipe, no FP64 arithmetic
-  const float kf = d2f_int(kfac[n]);
-  const float zx = d2f_int(z.x), zy = d2f_int(z.y), dx = d2f_int(dl.x), dy = d2f_int(dl.y);
   // the linear-exact form synthesises Phi' = Phi - Phi_00 P_00: the mean enters the tendencies separately
   const bool mean = sd.lin_exact && n == 0;
-  const float v[8] = {zx * kf, zy * kf, dx * kf, dy * kf, zx, zy, mean ? 0.0f : d2f_int(f.x), mean ? 0.0f : d2f_int(f.y)};
+  const float v[8] = {z.x * kf, z.y * kf, dl.x * kf, dl.y * kf, z.x, z.y, mean ? 0.0f : f.x, mean ? 0.0f : f.y};
 #pragma unroll
   for (int q = 0; q < 8; q++) fsplit(v[q], sd.aS_P + baseP + tile_off(ml * 8 + q, k, sd.rSP, sd.bks), sd.aSP_size, sd.pieces);
 #pragma unroll
   for (int q = 0; q < 4; q++) fsplit(v[q], sd.aS_H + baseH + tile_off(ml * 4 + q, k, sd.rSH, sd.bks), sd.aSH_size, sd.pieces);
 }
 
-// synthesis operands from a whole state (after the state was set from outside the stepping). grid: (ceil(ntri/128), B)
-__global__ void split_pack_state(SphDev d, SplitDev sd, const double *__restrict__ kfac, const double2 *__restrict__ x) {
+__device__ __forceinline__ float2 d2f2(double2 v) { return make_float2(d2f_int(v.x), d2f_int(v.y)); }
+
+// After the state was set from outside the stepping: its FP32 copy xf (stages 0-2 read it) and the synthesis
+// operands. grid: (ceil(ntri/128), B)
+__global__ void split_pack_state(SphDev d, SplitDev sd, const float *__restrict__ kfac32, const double2 *__restrict__ x, float2 *__restrict__ xf) {
   const int b = blockIdx.y, q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= d.ntri) return;
-  const double2 *xb = x + static_cast<size_t>(b) * 3 * d.ntri;
-  pack_syn_coef(d, sd, kfac, b, d.trim[q], d.trin[q], xb[q], xb[d.ntri + q], xb[2 * d.ntri + q]);
+  const size_t i = static_cast<size_t>(b) * 3 * d.ntri + q;
+  const float2 z = d2f2(x[i]), dl = d2f2(x[i + d.ntri]), f = d2f2(x[i + 2 * d.ntri]);
+  xf[i] = z;
+  xf[i + d.ntri] = dl;
+  xf[i + 2 * d.ntri] = f;
+  const int n = d.trin[q];
+  pack_syn_coef(d, sd, kfac32[n], b, d.trim[q], n, z, dl, f);
 }
 
 // ------------------------------------------------------------------------------------------- analysis + RK4
 // The analysis epilogue of one coefficient (member b = tile member ml, wavenumber m, parity s, index r: n = m + s + 2r)
 // from the accumulators staged in shared memory (dsm, row stride ldp): the tendencies (cpp/sphere.cpp:380-389) with
-// the linear terms of the linear-exact form, the RK4 stage update of the FP64 state, the next stage input and the
-// next synthesis operands. Shared by both analysis kernels, so both give the same bits.
-__device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, const SphTab<float> &t, const double *__restrict__ kfac, const StageArgs &sa,
-                                         double2 *__restrict__ x0, const float2 *__restrict__ xin, float2 *__restrict__ xout,
-                                         double2 *__restrict__ acc, const float *dsm, int ldp, int m, int tile, int ml, int s, int r, int cb1,
-                                         int ra0, int ra1) {
+// the linear terms of the linear-exact form, the RK4 stage update, the next stage input and the next synthesis
+// operands. Shared by both analysis kernels, so both give the same bits.
+// Precision: the state x0 is FP64 and only the last stage touches it (x0 + c (k1 + 2 k2 + 2 k3 + k4), del^4
+// filter, in FP64); xf holds it rounded to FP32. The tendencies are FP32 (their nonlinear part carries the BF16
+// pieces' 2^-16 rounding), so the accumulator k1 + 2 k2 + 2 k3 (acc) and the stage inputs xf + c k of stages 0-2,
+// which the next stage only reads in FP32, are formed in FP32.
+__device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, const SphTab<float> &t, const StageArgs &sa,
+                                         double2 *__restrict__ x0, float2 *__restrict__ xf, const float2 *__restrict__ xin,
+                                         float2 *__restrict__ xout, float2 *__restrict__ acc, const float *dsm, int ldp, int m, int tile, int ml,
+                                         int s, int r, int cb1, int ra0, int ra1) {
   const int b = tile * sd.nbt + ml, n = m + s + 2 * r;
   const int cbs = s ? cb1 : 0, ras = s ? ra1 : ra0;
   const float *H = dsm + (ml * 6) * ldp + cbs + r, *P = dsm + (ml * 8) * ldp + cbs + ras + r;
@@ -621,23 +628,18 @@ __device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, co
   float2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
   float2 kf = csub(vH, imul(uP, mm));
   const int q = d.tri[m] + n - m;
-  const size_t base = static_cast<size_t>(b) * 3 * d.ntri + q;
+  const size_t mb = static_cast<size_t>(b) * 3 * d.ntri, base = mb + q;
+  // the stage input in FP32: the state's copy at stage 0, else the previous stage's output (a separate buffer:
+  // neighbouring n belong to other CTAs)
+  const float2 *yin = sa.stage == 0 ? xf : xin;
   if (sd.lin_exact && q != 0) {
-    // the terms linear in the stage input y, in FP32 like the rest of the tendencies but outside the BF16 products
-    // (x0 at stage 0, else the previous stage's output rounded to FP32 in a separate buffer: neighbouring n belong
-    // to other CTAs): n(n+1)/a^2 Phi_n in d delta; -Phi_mean delta_n in d Phi (D(U, V) = delta exactly for n <= T);
-    // for an untilted axis the Coriolis terms -D(f U, f V) and D(f V, -f U) with f = 2 Omega mu, which couple
-    // n - 1, n, n + 1 of the same m
-    const size_t mb = static_cast<size_t>(b) * 3 * d.ntri;
-    auto yat = [&](int field, int qq) -> float2 {
-      if (sa.stage == 0) {
-        const double2 v = x0[mb + static_cast<size_t>(field) * d.ntri + qq];
-        return make_float2(d2f_int(v.x), d2f_int(v.y));
-      }
-      return xin[mb + static_cast<size_t>(field) * d.ntri + qq];
-    };
+    // the terms linear in the stage input y, in FP32 like the rest of the tendencies but outside the BF16 products:
+    // n(n+1)/a^2 Phi_n in d delta; -Phi_mean delta_n in d Phi (D(U, V) = delta exactly for n <= T); for an untilted
+    // axis the Coriolis terms -D(f U, f V) and D(f V, -f U) with f = 2 Omega mu, which couple n - 1, n, n + 1 of
+    // the same m
+    auto yat = [&](int field, int qq) -> float2 { return yin[mb + static_cast<size_t>(field) * d.ntri + qq]; };
     const float2 yz = yat(0, q), yd = yat(1, q), yf = yat(2, q);
-    const float phibar = d2f_int(x0[mb + 2 * d.ntri].x) * t.Ps[0];
+    const float phibar = xf[mb + 2 * d.ntri].x * t.Ps[0];
     const float lp = t.lapl[n];
     kd.x += lp * yf.x;
     kd.y += lp * yf.y;
@@ -657,36 +659,46 @@ __device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, co
     }
   }
   if (q == 0) kz = kd = kf = make_float2(0, 0);
-  const double2 k[3] = {make_double2(f2d_int(kz.x), f2d_int(kz.y)), make_double2(f2d_int(kd.x), f2d_int(kd.y)),
-                        make_double2(f2d_int(kf.x), f2d_int(kf.y))};
-  // every load of the three fields is issued before any store (the buffers never alias)
-  double2 xv[3], av[3];
+  const float2 k[3] = {kz, kd, kf};
+  float2 nv[3];
+  if (sa.stage < 3) {
+    // every load of the three fields is issued before any store (the buffers never alias)
+    float2 yv[3], av[3];
 #pragma unroll
-  for (int f = 0; f < 3; f++) {
-    xv[f] = x0[base + static_cast<size_t>(f) * d.ntri];
-    av[f] = sa.stage > 0 ? acc[base + static_cast<size_t>(f) * d.ntri] : make_double2(0.0, 0.0);
-  }
-  double2 nv[3];
-#pragma unroll
-  for (int f = 0; f < 3; f++) {
-    const size_t i = base + static_cast<size_t>(f) * d.ntri;
-    if (sa.stage == 0) {
-      acc[i] = k[f];
-      nv[f] = cadd(xv[f], cscale(k[f], sa.c));
-    } else if (sa.stage < 3) {
-      acc[i] = cadd(av[f], cscale(k[f], 2.0));
-      nv[f] = cadd(xv[f], cscale(k[f], sa.c));
-    } else {
-      const double2 val = cadd(xv[f], cscale(cadd(av[f], k[f]), sa.c));
-      const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
-      nv[f] = q == 0 ? val : cscale(val, fac);
-      x0[i] = nv[f];
+    for (int f = 0; f < 3; f++) {
+      yv[f] = xf[base + static_cast<size_t>(f) * d.ntri];
+      av[f] = sa.stage > 0 ? acc[base + static_cast<size_t>(f) * d.ntri] : make_float2(0.0f, 0.0f);
     }
-    // the next stage input rounded to FP32 is kept when a caller asks for it (the linear-exact form reads it;
-    // the split synthesis reads the packed operands written below)
-    if (xout != nullptr && sa.stage < 3) xout[i] = make_float2(d2f_int(nv[f].x), d2f_int(nv[f].y));
+#pragma unroll
+    for (int f = 0; f < 3; f++) {
+      const size_t i = base + static_cast<size_t>(f) * d.ntri;
+      acc[i] = sa.stage == 0 ? k[f] : make_float2(fmaf(2.0f, k[f].x, av[f].x), fmaf(2.0f, k[f].y, av[f].y));
+      nv[f] = make_float2(fmaf(sa.c32, k[f].x, yv[f].x), fmaf(sa.c32, k[f].y, yv[f].y));
+      // the next stage input is kept when the linear-exact form reads it (the split synthesis reads the packed
+      // operands written below)
+      if (xout != nullptr) xout[i] = nv[f];
+    }
+  } else {
+    double2 xv[3];
+    float2 av[3];
+#pragma unroll
+    for (int f = 0; f < 3; f++) {
+      xv[f] = x0[base + static_cast<size_t>(f) * d.ntri];
+      av[f] = acc[base + static_cast<size_t>(f) * d.ntri];
+    }
+#pragma unroll
+    for (int f = 0; f < 3; f++) {
+      const size_t i = base + static_cast<size_t>(f) * d.ntri;
+      const double2 sum = make_double2(f2d_int(av[f].x + k[f].x), f2d_int(av[f].y + k[f].y));
+      const double2 val = make_double2(fma(sa.c, sum.x, xv[f].x), fma(sa.c, sum.y, xv[f].y));
+      const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
+      const double2 x1 = q == 0 ? val : cscale(val, fac);
+      x0[i] = x1;
+      nv[f] = d2f2(x1);
+      xf[i] = nv[f];
+    }
   }
-  pack_syn_coef(d, sd, kfac, b, m, n, nv[0], nv[1], nv[2]);
+  pack_syn_coef(d, sd, t.kfac[n], b, m, n, nv[0], nv[1], nv[2]);
 }
 
 
@@ -697,9 +709,9 @@ __device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, co
 // MINB: CTAs per SM the register budget allows (2: up to 128 registers a thread; 3: up to 80, for plans whose
 // shared memory admits three CTAs per SM)
 template <bool BOTH, bool DIRECT, int MINB>
-__global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
-                                                             int B, int ns, double2 *__restrict__ x0, const float2 *__restrict__ xin,
-                                                             float2 *__restrict__ xout, double2 *__restrict__ acc) {
+__global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, SplitDev sd, SphTab<float> t, StageArgs sa, int B, int ns,
+                                                             double2 *__restrict__ x0, float2 *__restrict__ xf, const float2 *__restrict__ xin,
+                                                             float2 *__restrict__ xout, float2 *__restrict__ acc) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], done;
   __shared__ uint32_t tslot;
@@ -853,7 +865,7 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
     for (int e = threadIdx.x; e < mt * cnt; e += blockDim.x) {
       const int ml = e / cnt, j = e - ml * cnt;
       const int s = BOTH ? (j & 1) : s_first, r = BOTH ? (j >> 1) : j;
-      ana_coef(d, sd, t, kfac, sa, x0, xin, xout, acc, dsm, ldp, m, tile, ml, s, r, cb1, ra0, ra1);
+      ana_coef(d, sd, t, sa, x0, xf, xin, xout, acc, dsm, ldp, m, tile, ml, s, r, cb1, ra0, ra1);
     }
   }
   }
@@ -871,10 +883,10 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
 constexpr int SPLIT_WS_THREADS = 320;
 constexpr int SPLIT_WS_EPI = 256;  // epilogue threads (warps 2..9)
 template <bool BOTH, int CTAS>
-__global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d, SplitDev sd, SphTab<float> t, const double *__restrict__ kfac, StageArgs sa,
-                                                                    int B, int ns, int buf_cols, int slot_bytes, double2 *__restrict__ x0,
-                                                                    const float2 *__restrict__ xin, float2 *__restrict__ xout,
-                                                                    double2 *__restrict__ acc) {
+__global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d, SplitDev sd, SphTab<float> t, StageArgs sa, int B, int ns,
+                                                                       int buf_cols, int slot_bytes, double2 *__restrict__ x0, float2 *__restrict__ xf,
+                                                                       const float2 *__restrict__ xin, float2 *__restrict__ xout,
+                                                                       float2 *__restrict__ acc) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], accf[2], acce[2], done;
   __shared__ uint32_t tslot;
@@ -1062,7 +1074,7 @@ __global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d,
       for (int e = et; e < mt * cnt; e += SPLIT_WS_EPI) {
         const int ml = e / cnt, j = e - ml * cnt;
         const int s = BOTH ? (j & 1) : s_first, r = BOTH ? (j >> 1) : j;
-        ana_coef(d, sd, t, kfac, sa, x0, xin, xout, acc, dsm, ldp, m, tile, ml, s, r, cb1, ra0, ra1);
+        ana_coef(d, sd, t, sa, x0, xf, xin, xout, acc, dsm, ldp, m, tile, ml, s, r, cb1, ra0, ra1);
       }
       // the shared accumulator copy is free for the next item
       asm volatile("bar.sync 1, 256;" ::: "memory");
