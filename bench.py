@@ -586,34 +586,47 @@ def other_workloads(lw, lib, args, ens):
     return out
 
 
-def surrogate_workload(lw, trajectories=2560, windows=80, epochs=100, members=1024, rollout_windows=16):
+def surrogate_workload(lw, trajectories=2560, windows=80, epochs=100, members=1024, rollout_windows=80, member_windows=16,
+                       kinetic_weight=0.25):
     """Config 4 inside the benchmark: the T42 residual MLP (5676 -> 4096 x 3 -> 5676, GELU, BF16 on tcgen05) trained
     on the configured 204,800 solver pairs (`trajectories` x `windows`; split-precision RK4 data, FP64 state; 6-hour
-    windows of 900 s steps, mean height 8000 m) for `epochs` epochs with symmetry-augmented batches and averaged
-    weights, then a hybrid rollout of `members` held-out members over `rollout_windows` windows (the 8-map
-    averaged network; split-precision RK4 checking every 4th window, FP64 RK4 taking over above 1e-3). The 80-window
-    rollout is python bench.py --study surrogate."""
+    windows of 900 s steps, mean height 8000 m) for `epochs` epochs with symmetry-augmented batches, averaged
+    weights and the kinetic-energy part of the loss weighted by `kinetic_weight`, then hybrid rollouts of `members`
+    held-out members (the 8-map averaged network; split-precision RK4 checking every 4th window against the 1e-3
+    threshold): over the configured 20 days (`rollout_windows`) with FP64 RK4 replacing each failed window (the
+    network keeps the member), and over `member_windows` windows with FP64 RK4 taking failed members over for good."""
     t0 = time.perf_counter()
     sur = lw.Surrogate(42, hidden=4096, seed=1)
+    sur.set_kinetic_weight(kinetic_weight)
     gen_s = sur.generate(trajectories, windows, seed0=1_000_000, hmin=8000.0, hmax=8000.0, precision=lw.SPLIT_BF16)
     fit = sur.fit(epochs, batch=512, lr=3e-4, lr_min=3e-5, val_fraction=0.1, seed=1, loss="energy")
     train_ms, fwd_ms = sur.time(512, 10)
     _, fwd1024 = sur.time(1024, 10)
+    sur.set_takeover("window")
     r = sur.rollout(members, seed0=9_000_001, windows=rollout_windows, check_every=4, threshold=1e-3, check_precision=lw.SPLIT_BF16,
                     ref_windows=4, hmin=8000.0, hmax=8000.0)
+    sur.set_takeover("member")
+    rm = sur.rollout(members, seed0=9_000_001, windows=member_windows, check_every=4, threshold=1e-3, check_precision=lw.SPLIT_BF16,
+                     ref_windows=4, hmin=8000.0, hmax=8000.0)
     sur.close()
     fl = 2 * (5676 * 4096 * 2 + 4096 * 4096 * 2)
     maps = 8  # the inference average over symmetry maps (the library default)
-    return {"config": "4: learned surrogate T42, 6-hour windows (configured training, 16-window rollout)",
+    return {"config": "4: learned surrogate T42, 6-hour windows (configured training, 20-day rollout)",
             "unit": "member-sim-days/s",
             "network_only": members * 0.25 / (maps * fwd1024 * 1e-3), "network_in_rollout": r["network_rate"],
             "hybrid": r["hybrid_rate"], "plain_rk4_fp64": r["rk4_rate"],
             "speedup_network_vs_rk4": members * 0.25 / (maps * fwd1024 * 1e-3) / r["rk4_rate"],
             "speedup_hybrid_vs_rk4": r["hybrid_rate"] / r["rk4_rate"],
+            "takeover": "window: FP64 RK4 replaces each checked window over the threshold, the network keeps the member",
             "window_height_error": {"validation_mean": fit["val_err_mean"], "validation_p90": fit["val_err_p90"],
                                     "persistence_mean": fit["val_persist_mean"], "untrained_mean": fit["val_untrained_mean"],
-                                    "rollout_checks_median": r["err_median"], "rollout_checks_max": r["err_max"]},
-            "taken_over": r["taken_over"], "threshold": 1e-3, "members": members, "rollout_windows": rollout_windows,
+                                    "rollout_checks_median": r["err_median"], "rollout_checks_p90": r["err_p90"],
+                                    "rollout_checks_max": r["err_max"], "rollout_checks_over_threshold": r["frac_over"]},
+            "windows_replaced": r["taken_over"], "checks": r["checks"],
+            "member_takeover": {"rollout_windows": member_windows, "taken_over": rm["taken_over"], "hybrid": rm["hybrid_rate"],
+                                "speedup_hybrid_vs_rk4": rm["hybrid_rate"] / rm["rk4_rate"],
+                                "rollout_checks_over_threshold": rm["frac_over"]},
+            "threshold": 1e-3, "members": members, "rollout_windows": rollout_windows, "kinetic_weight": kinetic_weight,
             "pairs": trajectories * windows, "epochs": epochs, "generate_s": gen_s, "train_s": fit["seconds"],
             "train_step_ms_batch512": train_ms, "forward_ms_batch1024": fwd1024,
             "forward_tflops_batch1024": fl * 1024 / (fwd1024 * 1e-3) / 1e12, "wall_s": time.perf_counter() - t0}
@@ -750,7 +763,7 @@ def run_case(args) -> int:
 def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, epochs=100, batch=512, lr=3e-4, lr_min=3e-5,
                     hmin=8000.0, hmax=8000.0, members=1024, rollout_windows=80, check_every=4, threshold=1e-3, ref_windows=4, seed=1,
                     check_precision=None, loss="energy", thresholds=(), clip=2.0, data_precision=0, augment=True, averaging=0.9995,
-                    sym_average=8, kinetic_weight=1.0) -> dict:
+                    sym_average=8, kinetic_weight=1.0, takeovers=("member",)) -> dict:
     """The learned surrogate end to end: solver trajectories (balanced turbulence on training seeds, RK4 at 900 s,
     del^4 with a 1-day e-folding at n = T; pairs (state, state + 6 h) from every window; the last tenth of the
     trajectories held out) -> training on the GPU -> validation errors per 6-hour window -> a hybrid rollout of
@@ -779,19 +792,23 @@ def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, e
            "symmetry_maps_averaged": sym_average, "kinetic_weight": kinetic_weight,
            "check_precision": ["fp64", "fp32", "split3"][check_precision]}
     if members > 0 and rollout_windows > 0:
-        r = sur.rollout(members, seed0=9_000_000 + seed, windows=rollout_windows, check_every=check_every, threshold=threshold,
-                        check_precision=check_precision, ref_windows=ref_windows, hmin=hmin, hmax=hmax)
-        r["speedup_hybrid_vs_rk4"] = r["hybrid_rate"] / r["rk4_rate"]
-        r["speedup_network_vs_rk4"] = r["network_rate"] / r["rk4_rate"]
-        out["rollout"] = dict(members=members, windows=rollout_windows, check_every=check_every, threshold=threshold, **r)
-        sweep = []
-        for th in thresholds:
-            q = sur.rollout(members, seed0=9_000_000 + seed, windows=rollout_windows, check_every=check_every, threshold=th,
+        for tk in takeovers:
+            # "member": RK4 takes a failed member over for good; "window": RK4 replaces the failed window only
+            sur.set_takeover(tk)
+            key = "rollout" if tk == takeovers[0] else f"rollout_{tk}"
+            r = sur.rollout(members, seed0=9_000_000 + seed, windows=rollout_windows, check_every=check_every, threshold=threshold,
                             check_precision=check_precision, ref_windows=ref_windows, hmin=hmin, hmax=hmax)
-            sweep.append({"threshold": th, "taken_over": q["taken_over"], "err_mean": q["err_mean"], "err_max": q["err_max"],
-                          "speedup_hybrid_vs_rk4": q["hybrid_rate"] / q["rk4_rate"]})
-        if sweep:
-            out["threshold_sweep"] = sweep
+            r["speedup_hybrid_vs_rk4"] = r["hybrid_rate"] / r["rk4_rate"]
+            r["speedup_network_vs_rk4"] = r["network_rate"] / r["rk4_rate"]
+            out[key] = dict(takeover=tk, members=members, windows=rollout_windows, check_every=check_every, threshold=threshold, **r)
+            sweep = []
+            for th in thresholds:
+                q = sur.rollout(members, seed0=9_000_000 + seed, windows=rollout_windows, check_every=check_every, threshold=th,
+                                check_precision=check_precision, ref_windows=ref_windows, hmin=hmin, hmax=hmax)
+                sweep.append({"threshold": th, "taken_over": q["taken_over"], "err_mean": q["err_mean"], "err_max": q["err_max"],
+                              "speedup_hybrid_vs_rk4": q["hybrid_rate"] / q["rk4_rate"]})
+            if sweep:
+                out["threshold_sweep" if tk == takeovers[0] else f"threshold_sweep_{tk}"] = sweep
     sur.close()
     return out
 
@@ -826,7 +843,9 @@ def main():
     ap.add_argument("--augment", type=int, default=1, help="symmetry augmentation of the training pairs (1/0)")
     ap.add_argument("--averaging", type=float, default=0.9995, help="weight averaging decay (0: last weights)")
     ap.add_argument("--sym-average", type=int, default=8, help="symmetry maps averaged at inference (1: plain network)")
-    ap.add_argument("--kinetic-weight", type=float, default=1.0, help="weight of the kinetic-energy part of the loss")
+    ap.add_argument("--kinetic-weight", type=float, default=0.25, help="weight of the kinetic-energy part of the loss")
+    ap.add_argument("--takeover", default="window,member", help="rollout takeover modes to run (window: RK4 replaces a failed window; "
+                    "member: RK4 keeps a failed member)")
     ap.add_argument("--lr-min", type=float, default=3e-5)
     ap.add_argument("--data-precision", default="split3", choices=["fp64", "split3"])
     args = ap.parse_args()
@@ -847,7 +866,8 @@ def main():
                                              threshold=args.threshold, check_precision=lw.SPLIT_BF16 if args.check_precision == "split3" else lw.FP64,
                                              thresholds=tuple(float(v) for v in args.sweep.split(",") if v), augment=bool(args.augment),
                                              averaging=args.averaging, data_precision=2 if args.data_precision == "split3" else 0,
-                                             sym_average=args.sym_average, kinetic_weight=args.kinetic_weight)))
+                                             sym_average=args.sym_average, kinetic_weight=args.kinetic_weight,
+                                             takeovers=tuple(args.takeover.split(",")))))
         return 0
     if args.impl == "reference":
         return run_reference(args, rank, world)

@@ -400,6 +400,11 @@ int lmw_surrogate_set_averaging(lmw_surrogate *s, double decay);
  * (default 1, the energy norm; below 1 leans the fit toward the height field). Set before the first fit. No
  * reference counterpart. */
 int lmw_surrogate_set_kinetic_weight(lmw_surrogate *s, double weight);
+/* what lmw_surrogate_rollout does with a member whose checked window exceeds the threshold: mode 0 (the default)
+ * -- RK4 takes the member over for the rest of the rollout; mode 1 -- RK4's result (plain FP64) replaces that
+ * window and the network keeps advancing the member (RK4 as the per-window fallback; out[4] of the rollout then
+ * counts replaced member-windows). No reference counterpart. */
+int lmw_surrogate_set_takeover(lmw_surrogate *s, int mode);
 /* maps = 1: the network advances a state as it is. maps = 2k (the default 8): the network is applied to the state
  * under k rotations about the polar axis by multiples of 2 pi / k, each without and with the equatorial
  * reflection, each increment is mapped back, and the 2k increments are averaged (the exact dynamics commute with

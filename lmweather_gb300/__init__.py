@@ -148,6 +148,7 @@ _SIGS = {
     "lmw_surrogate_set_averaging": (_I, [_P, _D]),
     "lmw_surrogate_set_symmetry_average": (_I, [_P, _I]),
     "lmw_surrogate_set_kinetic_weight": (_I, [_P, _D]),
+    "lmw_surrogate_set_takeover": (_I, [_P, _I]),
     "lmw_surrogate_history": (_I, [_P, _I, _DP, _DP, _IP]),
 }
 
@@ -893,6 +894,13 @@ class Surrogate:
     def set_kinetic_weight(self, weight: float):
         """Weight of the kinetic-energy part of the training loss (1: the energy norm). Before the first fit."""
         _check(self._lib.lmw_surrogate_set_kinetic_weight(self._h, weight))
+
+    def set_takeover(self, mode: str):
+        """What a failed rollout check does: "member" (RK4 advances the member from then on, the default) or
+        "window" (RK4's result replaces that window; the network keeps the member)."""
+        if mode not in ("member", "window"):
+            raise ValueError("the takeover mode must be 'member' or 'window'")
+        _check(self._lib.lmw_surrogate_set_takeover(self._h, 0 if mode == "member" else 1))
 
     def set_symmetry_average(self, maps: int):
         """Average the network's increments over `maps` rotations/reflections of the input (1: the plain network)."""

@@ -792,6 +792,9 @@ int lmw_surrogate_set_kinetic_weight(lmw_surrogate *s, double weight) {
   return SUR(s, need(weight > 0 && weight <= 16, "the kinetic-energy weight must lie in (0, 16]"); need(!s->s->have_norm, "set the loss weights before the first fit");
              s->s->ke_weight = weight);
 }
+int lmw_surrogate_set_takeover(lmw_surrogate *s, int mode) {
+  return SUR(s, need(mode == 0 || mode == 1, "the takeover mode must be 0 (member) or 1 (window)"); s->s->takeover_mode = mode);
+}
 int lmw_surrogate_set_averaging(lmw_surrogate *s, double decay) {
   return SUR(s, need(decay >= 0 && decay < 1, "the averaging decay must lie in [0, 1)"); s->s->ema = decay);
 }

@@ -1394,8 +1394,10 @@ void Surrogate::advance_states(double *states, int count, const int *mode) {
 
 // Hybrid rollout. Every window the network advances the members it still owns; every check_every-th window plain
 // RK4 recomputes that window from the same start states, the per-window height error of every network member is
-// recorded, and a member whose error exceeds the threshold is taken over: its state becomes the RK4 state and RK4
-// advances it from then on (a takeover group: one more batched engine per check that took members over).
+// recorded, and a member whose error exceeds the threshold is taken over: its state becomes the RK4 state and
+// (takeover_mode 0) RK4 advances it from then on (a takeover group: one more batched engine per check that took
+// members over), or (takeover_mode 1) the network keeps advancing it from the RK4 state (out[4] then counts the
+// member-windows RK4 replaced).
 // out[0] hybrid seconds, [1] network seconds, [2] check seconds, [3] takeover seconds, [4] members taken over,
 // [5] checks, [6] median window error, [7] max, [8] fraction of checked windows over the threshold,
 // [9] plain RK4 seconds for ref windows (measured on the same members), [10] ref windows, [11] hybrid
@@ -1546,6 +1548,12 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
       copy_members_launch(g->e->device_state(), nullptr, rs_state.p, g->ids.p, g->n, nfeat, check->stream);
       LMW_CUDA(cudaStreamSynchronize(check->stream));
       taken += g->n;
+      if (takeover_mode == 1) {
+        // per-window fallback: the replaced window's members stay with the network
+        for (int b : fresh) mode[b] = 0;
+        t_check += seconds_since(tc0);
+        continue;
+      }
       groups.push_back(std::move(g));
       LMW_CUDA(cudaMemcpyAsync(rs_mode.p, mode.data(), members * sizeof(int), cudaMemcpyHostToDevice, stream));
       netids = keep;

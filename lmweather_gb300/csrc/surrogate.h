@@ -134,6 +134,9 @@ class Surrogate {
   // weight of the kinetic-energy part of the energy-norm loss against the available potential energy (1: the
   // energy norm itself; below 1 leans the fit toward the height field)
   double ke_weight = 1.0;
+  // what a failed check does: 0 = RK4 takes the member over for the rest of the rollout; 1 = RK4's result
+  // replaces that window of the member and the network keeps advancing it (RK4 as the per-window fallback)
+  int takeover_mode = 0;
 
   void reset(uint64_t seed);  // a fresh network and optimiser (the data stay)
   void generate(int trajectories, int windows, uint64_t seed0, double hmin, double hmax, int precision, int batch_members);

@@ -181,15 +181,17 @@ def test_symmetry_averaged_network_is_equivariant(trained, engine):
     sur.set_symmetry_average(8)
 
 
-@pytest.mark.parametrize("check", ["fp64", "split3"])
-def test_rollout_takeover_semantics(trained, engine, check):
+@pytest.mark.parametrize("check,takeover", [("fp64", "member"), ("split3", "member"), ("split3", "window")])
+def test_rollout_takeover_semantics(trained, engine, check, takeover):
     sur, _ = trained
-    # threshold 0 and a check every window: every member is taken over at the first check, so the hybrid is plain
-    # FP64 RK4 (a split-precision check is only the judge: the window of a member it takes over is recomputed in FP64)
+    # threshold 0 and a check every window: every member is taken over at the first check (member mode), or every
+    # window of every member is replaced (window mode), so the hybrid is plain FP64 RK4 (a split-precision check is
+    # only the judge: the window of a member it takes over is recomputed in FP64)
     cp = engine.FP64 if check == "fp64" else engine.SPLIT_BF16
+    sur.set_takeover(takeover)
     r0 = sur.rollout(8, seed0=900, windows=3, check_every=1, threshold=0.0, ref_windows=1, hmin=7000.0, hmax=7000.0, with_states=True,
                      check_precision=cp)
-    assert r0["taken_over"] == 8 and r0["checks"] == 3 and r0["frac_over"] == 1.0
+    assert r0["taken_over"] == (8 if takeover == "member" else 24) and r0["checks"] == 3 and r0["frac_over"] == 1.0
     # a plain RK4 run of the same members ends in the same states bit for bit
     T = 21
     ref = engine.Sphere(T, diffusion=6.37122e6 ** 4 / (86400.0 * (T * (T + 1)) ** 2), members=8)
@@ -210,3 +212,6 @@ def test_rollout_takeover_semantics(trained, engine, check):
     assert r1["taken_over"] == 0 and r1["checks"] == 2
     assert r1["window_errors"].shape == (2, 8) and np.all(r1["window_errors"] > 0)
     assert r1["hybrid_rate"] > 0 and r1["rk4_rate"] > 0
+    sur.set_takeover("member")
+    with pytest.raises(ValueError):
+        sur.set_takeover("never")
