@@ -277,6 +277,142 @@ __device__ void fft_forward_dif(C2 *s, int rows, int n, int logn, const C2 *__re
     hi = st;
   }
 }
+// Compile-time forms of the same groups: the transform length 2^LOGN, the group's first stage ST and its size F
+// are template constants, so every element and twiddle address of a thread is its base plus an immediate (no
+// per-element index arithmetic). Where the padding lets a group's elements sit at a fixed step from their first
+// one (rows unpadded, ST >= PAD, or a first group no wider than the padding period) the step is a constant;
+// otherwise the element offsets are computed as in dit_group. Same butterflies, twiddles and order as
+// dit_group / dif_group, so the same bits.
+template <int PAD, int ST, int F> __host__ __device__ constexpr bool fft_fixed_step() { return PAD == 0 || ST >= PAD || (ST == 0 && F <= PAD); }
+template <int PAD, int ST> __host__ __device__ constexpr int fft_step() { return PAD == 0 ? (1 << ST) : (ST >= PAD ? (1 << ST) + (1 << (ST - PAD)) : 1); }
+
+template <class C2, int F, int PAD, int LOGN, int ST>
+__device__ __forceinline__ void dit_group_c(C2 *s, int rows, const C2 *__restrict__ tw) {
+  constexpr int E = 1 << F, N = 1 << LOGN, HALFN = N >> 1, LO = (1 << ST) - 1, QB = LOGN - F, RL = PAD ? N + (N >> PAD) : N;
+  constexpr bool FIXED = fft_fixed_step<PAD, ST, F>();
+  constexpr int STEP = fft_step<PAD, ST>();
+  for (int e = threadIdx.x; e < (rows << QB); e += blockDim.x) {
+    const int r = e >> QB, q = e & ((1 << QB) - 1);
+    const int i0 = ((q >> ST) << (ST + F)) + (q & LO);
+    C2 *row = s + r * RL, *p0 = row + fft_at<PAD>(i0);
+    C2 x[E];
+#pragma unroll
+    for (int j = 0; j < E; j++) x[j] = FIXED ? p0[j * STEP] : row[fft_at<PAD>(i0 + (j << ST))];
+#pragma unroll
+    for (int f = 0; f < F; f++) {
+      const int h = 1 << f, stride = HALFN >> (ST + f);
+      const C2 *twb = tw + (q & LO) * stride;
+      C2 wv[E / 2];
+#pragma unroll
+      for (int jj = 0; jj < h; jj++) {
+        if (TW_SYM<C2> && jj >= (h >> 1) && h >= 2) wv[jj] = mk2(-wv[jj - (h >> 1)].y, wv[jj - (h >> 1)].x);
+        else wv[jj] = conjd(twb[(jj << ST) * stride]);
+      }
+#pragma unroll
+      for (int j = 0; j < E; j++) {
+        if (j & h) continue;
+        const C2 w = wv[j & (h - 1)];
+        const C2 t = cmul_tw(w, x[j + h]), u = x[j];
+        x[j] = cadd(u, t);
+        x[j + h] = csub(u, t);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+      if (FIXED) p0[j * STEP] = x[j];
+      else row[fft_at<PAD>(i0 + (j << ST))] = x[j];
+    }
+  }
+}
+template <class C2, int F, int PAD, int LOGN, int ST>
+__device__ __forceinline__ void dif_group_c(C2 *s, int rows, const C2 *__restrict__ tw) {
+  constexpr int E = 1 << F, N = 1 << LOGN, HALFN = N >> 1, LO = (1 << ST) - 1, QB = LOGN - F, RL = PAD ? N + (N >> PAD) : N;
+  constexpr bool FIXED = fft_fixed_step<PAD, ST, F>();
+  constexpr int STEP = fft_step<PAD, ST>();
+  for (int e = threadIdx.x; e < (rows << QB); e += blockDim.x) {
+    const int r = e >> QB, q = e & ((1 << QB) - 1);
+    const int i0 = ((q >> ST) << (ST + F)) + (q & LO);
+    C2 *row = s + r * RL, *p0 = row + fft_at<PAD>(i0);
+    C2 x[E];
+#pragma unroll
+    for (int j = 0; j < E; j++) x[j] = FIXED ? p0[j * STEP] : row[fft_at<PAD>(i0 + (j << ST))];
+#pragma unroll
+    for (int f = F - 1; f >= 0; f--) {
+      const int h = 1 << f, stride = HALFN >> (ST + f);
+      const C2 *twb = tw + (q & LO) * stride;
+      C2 wv[E / 2];
+#pragma unroll
+      for (int jj = 0; jj < h; jj++) {
+        if (TW_SYM<C2> && jj >= (h >> 1) && h >= 2) wv[jj] = mk2(wv[jj - (h >> 1)].y, -wv[jj - (h >> 1)].x);
+        else wv[jj] = twb[(jj << ST) * stride];
+      }
+#pragma unroll
+      for (int j = 0; j < E; j++) {
+        if (j & h) continue;
+        const C2 u = x[j], v = x[j + h];
+        x[j] = cadd(u, v);
+        x[j + h] = cmul_tw(wv[j & (h - 1)], csub(u, v));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+      if (FIXED) p0[j * STEP] = x[j];
+      else row[fft_at<PAD>(i0 + (j << ST))] = x[j];
+    }
+  }
+}
+// the group schedules of fft_inverse_dit / fft_forward_dif for a stage-group size FG, unrolled at compile time
+template <class C2, int PAD, int LOGN, int FG, int ST = 0>
+__device__ __forceinline__ void dit_sched(C2 *s, int rows, const C2 *__restrict__ tw) {
+  if constexpr (ST < LOGN) {
+    constexpr int F = LOGN - ST >= FG ? FG : LOGN - ST;
+    dit_group_c<C2, F, PAD, LOGN, ST>(s, rows, tw);
+    __syncthreads();
+    dit_sched<C2, PAD, LOGN, FG, ST + F>(s, rows, tw);
+  }
+}
+template <class C2, int PAD, int LOGN, int FG, int HI = LOGN>
+__device__ __forceinline__ void dif_sched(C2 *s, int rows, const C2 *__restrict__ tw) {
+  if constexpr (HI > 0) {
+    constexpr int F = HI >= FG ? FG : HI;
+    dif_group_c<C2, F, PAD, LOGN, HI - F>(s, rows, tw);
+    __syncthreads();
+    dif_sched<C2, PAD, LOGN, FG, HI - F>(s, rows, tw);
+  }
+}
+// fft_inverse_dit / fft_forward_dif for a length 2^LOGN fixed at compile time (fmax: stages per group, 2..FMAX)
+template <class C2, int PAD, int FMAX, int LOGN>
+__device__ void fft_inverse_dit_c(C2 *s, int rows, const C2 *__restrict__ tw, int fmax) {
+  if constexpr (FMAX >= 4) {
+    if (fmax >= 4) {
+      dit_sched<C2, PAD, LOGN, 4>(s, rows, tw);
+      return;
+    }
+  }
+  if constexpr (FMAX >= 3) {
+    if (fmax >= 3) {
+      dit_sched<C2, PAD, LOGN, 3>(s, rows, tw);
+      return;
+    }
+  }
+  dit_sched<C2, PAD, LOGN, 2>(s, rows, tw);
+}
+template <class C2, int PAD, int FMAX, int LOGN>
+__device__ void fft_forward_dif_c(C2 *s, int rows, const C2 *__restrict__ tw, int fmax) {
+  if constexpr (FMAX >= 4) {
+    if (fmax >= 4) {
+      dif_sched<C2, PAD, LOGN, 4>(s, rows, tw);
+      return;
+    }
+  }
+  if constexpr (FMAX >= 3) {
+    if (fmax >= 3) {
+      dif_sched<C2, PAD, LOGN, 3>(s, rows, tw);
+      return;
+    }
+  }
+  dif_sched<C2, PAD, LOGN, 2>(s, rows, tw);
+}
 __device__ __forceinline__ int bitrev(int k, int logn) { return static_cast<int>(__brev(static_cast<unsigned>(k)) >> (32 - logn)); }
 
 // Load the Fourier coefficients of `rows` fields at latitudes js (real part) and jn (imaginary part) into
@@ -942,10 +1078,9 @@ static void allow_max_shared_memory() {
     LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   for (auto *k : {split_ana_ws<false, 1>, split_ana_ws<true, 1>, split_ana_ws<false, 2>, split_ana_ws<true, 2>})
     LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_grid<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_grid<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
-  LMW_CUDA(cudaFuncSetAttribute(split_grid<true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  for (int logn : {0, 6, 7, 8, 9, 10})
+    for (int fmax : {3, 4})
+      for (int direct : {0, 1}) LMW_CUDA(cudaFuncSetAttribute(split_grid_kernel(direct, fmax, logn), cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   done_for_device = dev;
 }
 
@@ -1520,7 +1655,9 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   if (which < 0 || which == 1) {
     const dim3 grid(d.nh / sp.jb, B);
     const size_t bytes = 5 * static_cast<size_t>(sp.jb) * fft_row<3>(d.nlon) * sizeof(float2);
-    auto *k = sp.fgrp >= 4 ? (sp.direct ? split_grid<true, 4> : split_grid<false, 4>) : (sp.direct ? split_grid<true, 3> : split_grid<false, 3>);
+    // the FFT group bound sets the kernel's register budget: 4 (sixteen elements a thread) two CTAs per SM,
+    // else three
+    auto *k = split_grid_kernel(sp.direct, sp.fgrp >= 4 ? 4 : 3, sp.grid_fixed ? d.logn : 0);
     k<<<grid, GRID_THREADS, bytes, stream>>>(d, t, sd, fgrid, hsgrid);
   }
   if (which < 0 || which == 2) {
@@ -1955,6 +2092,7 @@ void SphereEngine::split_plan(int *out) const {
   out[7] = split ? split->ana_minb : 0;
   out[8] = split ? split->syn_split : 0;
   out[9] = split ? split->ana_ws : 0;
+  out[10] = split ? split->grid_fixed : 0;
 }
 
 void SphereEngine::set_split_form(int linear_exact) {
@@ -1969,7 +2107,7 @@ void SphereEngine::set_split_form(int linear_exact) {
 void SphereEngine::set_split_plan(const int *in) {
   if (!split) throw InvalidArgument("the engine is not in split precision");
   SplitPlan &sp = *split;
-  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6], mb = in[7], sl = in[8], ws = in[9];
+  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6], mb = in[7], sl = in[8], ws = in[9], gfix = in[10];
   int dev = 0, optin = 0;
   LMW_CUDA(cudaGetDevice(&dev));
   LMW_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -1987,6 +2125,7 @@ void SphereEngine::set_split_plan(const int *in) {
   const size_t ba = std::max(sp.ana_res_bytes_v[dir] + nsa * sp.ana_stage_bytes_v[dir] + SPLIT_MARGIN, both ? sp.ana_both_min_bytes : sp.ana_min_bytes);
   if (bs > sp.budget_bytes || ba > sp.budget_bytes) throw InvalidArgument("split plan: the pipelines do not fit in shared memory");
   if (mb != 2 && mb != 3) throw InvalidArgument("split plan: the analysis register budget must be 2 or 3 CTAs per SM");
+  if (gfix != 0 && gfix != 1) throw InvalidArgument("split plan: the grid kernel's fixed-length flag must be 0 or 1");
   size_t wsm = 0;
   if (ws != 0) {
     int bc = 0, slot = 0;
@@ -2006,6 +2145,7 @@ void SphereEngine::set_split_plan(const int *in) {
   sp.direct = dir;
   sp.ana_minb = mb;
   sp.ana_ws = ws;
+  sp.grid_fixed = gfix;
   if (ws) sp.smem_ana = wsm;
   sp.syn_split = sl;
   sp.syn_nh = sp.nh16 / sl;

@@ -67,6 +67,7 @@ struct SplitPlan {
   int ana_grid = 0;           // analysis CTAs (0: one per work item)
   int ana_minb = 2;           // analysis register budget: CTAs per SM (2 or 3)
   int ana_ws = 0;             // 0: split_ana; 1 or 2: the warp-specialised persistent form with that many CTAs per SM
+  int grid_fixed = 1;         // 1: the grid kernel compiled for the transform length (lengths 2^6..2^10); 0: any length
   int nsm = 152;              // multiprocessors of the device (the persistent grid)
   int ra_pair = 32;           // largest ra16[2m] + ra16[2m + 1]
   // 1: the linear terms of the tendencies (gravity-wave terms of the mean height, the Laplacian of Phi, the
@@ -394,7 +395,9 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
 // analysis streams with bulk copies; otherwise written m-major as FP32 fold[m][slot][parity][member][jh] (jb
 // latitudes per store), which the analysis gathers (cheaper for a few members, where jb is small)
 // FMAX: the largest FFT stage group the instantiation takes (4: sixteen elements per thread, two CTAs per SM)
-template <bool DIRECT, int FMAX>
+// LOGN: log2 of the transform length when it is fixed at compile time (the FFT groups then address shared memory
+// with immediates), 0 for any length
+template <bool DIRECT, int FMAX, int LOGN>
 __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
                                                            const double *__restrict__ hsgrid) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -403,7 +406,8 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
   const int b = blockIdx.y, jh0 = blockIdx.x * JB;
   const int tile = b / sd.nbt, ml = b - tile * sd.nbt;
   constexpr int PSG = FMAX >= 4 ? 4 : 3;  // row padding: one element per 16 for sixteen-element FFT groups, else per 8
-  const int n = d.nlon, M = d.M, rl = fft_row<PSG>(n);  // padded rows: element i at fft_at<PSG>(i)
+  const int logn = LOGN ? LOGN : d.logn;
+  const int n = 1 << logn, M = d.M, rl = fft_row<PSG>(n);  // padded rows: element i at fft_at<PSG>(i)
   // the untilted Coriolis parameter 2 Omega mu of the CTA's latitudes (south, north), rounded to FP32 once
   __shared__ float cor[2 * SPLIT_JB_MAX];
   if (threadIdx.x < 2 * JB) {
@@ -424,16 +428,17 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
       float2 *row = sm + static_cast<size_t>(f * JB + pr) * rl;
       if (m == 0) row[0] = make_float2(a.x, c.x);
       else {
-        row[fft_at<PSG>(bitrev(m, d.logn))] = make_float2(a.x - c.y, a.y + c.x);
-        row[fft_at<PSG>(bitrev(n - m, d.logn))] = make_float2(a.x + c.y, c.x - a.y);
+        row[fft_at<PSG>(bitrev(m, logn))] = make_float2(a.x - c.y, a.y + c.x);
+        row[fft_at<PSG>(bitrev(n - m, logn))] = make_float2(a.x + c.y, c.x - a.y);
       }
     }
   }
   __syncthreads();
-  fft_inverse_dit<float2, PSG, FMAX>(sm, 4 * JB, n, d.logn, t.tw, sd.fgrp);
+  if constexpr (LOGN > 0) fft_inverse_dit_c<float2, PSG, FMAX, LOGN>(sm, 4 * JB, t.tw, sd.fgrp);
+  else fft_inverse_dit<float2, PSG, FMAX>(sm, 4 * JB, n, logn, t.tw, sd.fgrp);
   const float g = static_cast<float>(d.g);
   for (int e = threadIdx.x; e < JB * n; e += blockDim.x) {
-    const int pr = e >> d.logn, k = e & (n - 1);
+    const int pr = e >> logn, k = e & (n - 1);
     const int js = jh0 + pr, jn = d.nlat - 1 - js;
     const float r2om = t.r2om[js];
     const double *fr_s = fgrid + (static_cast<size_t>(b) * d.nlat + js) * n, *fr_n = fgrid + (static_cast<size_t>(b) * d.nlat + jn) * n;
@@ -465,7 +470,8 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
     rU[kp] = A; rV[kp] = Bv; rZ[kp] = UP; rP[kp] = VP; rE[kp] = PE;
   }
   __syncthreads();
-  fft_forward_dif<float2, PSG, FMAX>(sm, 5 * JB, n, d.logn, t.tw, sd.fgrp);
+  if constexpr (LOGN > 0) fft_forward_dif_c<float2, PSG, FMAX, LOGN>(sm, 5 * JB, t.tw, sd.fgrp);
+  else fft_forward_dif<float2, PSG, FMAX>(sm, 5 * JB, n, logn, t.tw, sd.fgrp);
   const float inv = 1.0f / n, hinv = 0.5f * inv;
   // one work item per (m, slot r): the folded values of this CTA's latitude pairs at both parities. Direct
   // operands: the five slots of one m are consecutive threads, so a warp's stores of one row pair land in the
@@ -479,7 +485,7 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
         if (pr >= JB) break;
         const int js = jh0 + pr;
         const float2 *row = sm + static_cast<size_t>(r * JB + pr) * rl;
-        const float2 Ym = row[fft_at<PSG>(bitrev(m, d.logn))], Yc = conjd(row[fft_at<PSG>(bitrev((n - m) & (n - 1), d.logn))]);
+        const float2 Ym = row[fft_at<PSG>(bitrev(m, logn))], Yc = conjd(row[fft_at<PSG>(bitrev((n - m) & (n - 1), logn))]);
         float2 Xs = cscale(cadd(Ym, Yc), hinv);
         const float2 tt = csub(Ym, Yc);
         float2 Xn = make_float2(hinv * tt.y, -hinv * tt.x);
@@ -489,7 +495,7 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
         f0[pr] = cadd(Xs, Xn);
         f1[pr] = csub(Xs, Xn);
       }
-      if (!DIRECT) {
+      if constexpr (!DIRECT) {
 #pragma unroll
         for (int par = 0; par < 2; par++) {
           const float2 *fv = par ? f1 : f0;
@@ -504,8 +510,7 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
             o[0] = fv[0];
           }
         }
-        continue;
-      }
+      } else {
       // the folded values go straight into the analysis operands (BF16 pieces, chunk layout): slot r at parity p
       // is a P row of (m, s = p) for r = 0, 1, 2, 4 and an H row of (m, s = 1 - p) for r = 0, 1, 3
 #pragma unroll
@@ -564,8 +569,27 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX >= 4 ? 2 : 3) split_grid(Sp
           }
         }
       }
+      }
     }
   }
+}
+
+// the grid kernel instantiation for a plan: operand form, FFT group bound and transform length (lengths 2^6 to
+// 2^10, T21 to T341, compiled for their length; others take the any-length form)
+using SplitGridFn = void (*)(SphDev, SphTab<float>, SplitDev, const double *, const double *);
+template <bool DIRECT, int FMAX> inline SplitGridFn split_grid_for(int logn) {
+  switch (logn) {
+    case 6: return split_grid<DIRECT, FMAX, 6>;
+    case 7: return split_grid<DIRECT, FMAX, 7>;
+    case 8: return split_grid<DIRECT, FMAX, 8>;
+    case 9: return split_grid<DIRECT, FMAX, 9>;
+    case 10: return split_grid<DIRECT, FMAX, 10>;
+    default: return split_grid<DIRECT, FMAX, 0>;
+  }
+}
+inline SplitGridFn split_grid_kernel(int direct, int fmax, int logn) {
+  if (fmax >= 4) return direct ? split_grid_for<true, 4>(logn) : split_grid_for<false, 4>(logn);
+  return direct ? split_grid_for<true, 3>(logn) : split_grid_for<false, 3>(logn);
 }
 
 // ------------------------------------------------------------------------------------------- synthesis operands

@@ -365,6 +365,9 @@ def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
         plans.append(dict(analysis_ctas=37, analysis_both_parities=both, analysis_stages=2))
     if s.nlat // 2 >= 32:
         plans.append(dict(synthesis_latitude_slices=2, synthesis_stages=2))
+    # the grid kernel's any-length form against the one compiled for the transform length, at each FFT group size
+    for fg in (2, 3, 4):
+        plans.append(dict(grid_fixed_length=0, fft_stages_per_pass=fg))
     # the warp-specialised persistent analysis (operands streamed by one thread, MMAs by another into two
     # tensor-memory accumulators, the epilogue of the previous item by eight warps), where it fits
     ws_plans = []
