@@ -294,10 +294,12 @@ int lmw_ensemble_stream(lmw_ensemble *e, int group, void **stream);
  * that alternates its MMAs and its epilogue, else the CTAs per SM (1 or 2) of the warp-specialised persistent
  * analysis (one warp streams operands, one issues MMAs into two tensor-memory accumulators, eight run the epilogue
  * of the previous item), out[10] 1 when the grid kernel is the one compiled for the transform length (lengths
- * 2^6 to 2^10; its FFT groups address shared memory with immediates), 0 for the any-length form (zeros when the
- * engine is not in split precision; out has 11 entries). No reference counterpart. */
+ * 2^6 to 2^10; its FFT groups address shared memory with immediates), 0 for the any-length form, out[11] 0 for the
+ * synthesis kernel that alternates its MMAs and its epilogue, else the CTAs per SM (1 or 2) of the warp-specialised
+ * persistent synthesis (zeros when the engine is not in split precision; out has 12 entries). No reference
+ * counterpart. */
 int lmw_sphere_split_plan(lmw_sphere *s, int *out);
-/* replaces the autotuned plan with `plan` (the 11 entries above), checked against the limits the autotuner's
+/* replaces the autotuned plan with `plan` (the 12 entries above), checked against the limits the autotuner's
  * candidates obey (invalid_argument otherwise); every plan computes the same arithmetic. Validation and tuning
  * hook; no reference counterpart. */
 int lmw_sphere_set_split_plan(lmw_sphere *s, const int *plan);

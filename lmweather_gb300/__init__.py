@@ -382,13 +382,13 @@ class Sphere:
 
     def split_plan(self) -> dict:
         """The autotuned launch plan of the split path (zeros in the other precisions)."""
-        out = np.zeros(11, np.int32)
+        out = np.zeros(12, np.int32)
         _check(self._lib.lmw_sphere_split_plan(self._h, out.ctypes.data_as(_IP)))
         return dict(zip(self._PLAN_KEYS, out.tolist()))
 
     _PLAN_KEYS = ("lat_pairs_per_grid_cta", "fft_stages_per_pass", "synthesis_stages", "analysis_stages", "analysis_both_parities",
                   "analysis_ctas", "grid_writes_operands", "analysis_ctas_per_sm", "synthesis_latitude_slices",
-                  "analysis_warp_specialised", "grid_fixed_length")
+                  "analysis_warp_specialised", "grid_fixed_length", "synthesis_warp_specialised")
 
     def set_split_plan(self, **plan) -> None:
         """Replace entries of the autotuned launch plan (keys as split_plan returns them)."""
@@ -717,7 +717,7 @@ class Ensemble:
 
     def split_plan(self, group: int) -> dict:
         """The autotuned launch plan of a truncation group's split path."""
-        out = np.zeros(11, np.int32)
+        out = np.zeros(12, np.int32)
         _check(self._lib.lmw_ensemble_split_plan(self._h, group, out.ctypes.data_as(_IP)))
         return dict(zip(Sphere._PLAN_KEYS, out.tolist()))
 

@@ -1078,6 +1078,8 @@ static void allow_max_shared_memory() {
     LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   for (auto *k : {split_ana_ws<false, 1>, split_ana_ws<true, 1>, split_ana_ws<false, 2>, split_ana_ws<true, 2>})
     LMW_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_syn_ws<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  LMW_CUDA(cudaFuncSetAttribute(split_syn_ws<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
   for (int logn : {0, 6, 7, 8, 9, 10})
     for (int fmax : {3, 4})
       for (int direct : {0, 1}) LMW_CUDA(cudaFuncSetAttribute(split_grid_kernel(direct, fmax, logn), cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
@@ -1651,7 +1653,19 @@ static void split_stage(const SphDev &d, const SphTab<float> &t, const SplitPlan
   sa.c = stage < 2 ? 0.5 * dt : (stage == 2 ? dt : dt / 6);
   sa.c32 = static_cast<float>(sa.c);
   sa.filt = filt;
-  if (which < 0 || which == 0) split_syn<<<dim3(sp.ntiles, sp.syn_split, d.M), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
+  if (which < 0 || which == 0) {
+    if (sp.syn_ws > 0) {
+      size_t smem = 0;
+      int buf_cols = 0, slot = 0;
+      if (!syn_ws_layout(sp, sp.syn_split, sp.ns_syn, sp.syn_ws, &smem, &buf_cols, &slot))
+        throw InvalidArgument("split precision: the warp-specialised synthesis does not fit");
+      const int items = d.M * sp.ntiles * sp.syn_split;
+      auto *k = sp.syn_ws == 2 ? split_syn_ws<2> : split_syn_ws<1>;
+      k<<<std::min(items, sp.nsm * sp.syn_ws), SPLIT_SYN_WS_THREADS, smem, stream>>>(d, sd, B, sp.ns_syn, buf_cols, slot);
+    } else {
+      split_syn<<<dim3(sp.ntiles, sp.syn_split, d.M), SPLIT_THREADS, sp.smem_syn, stream>>>(d, sd, B, sp.ns_syn);
+    }
+  }
   if (which < 0 || which == 1) {
     const dim3 grid(d.nh / sp.jb, B);
     const size_t bytes = 5 * static_cast<size_t>(sp.jb) * fft_row<3>(d.nlon) * sizeof(float2);
@@ -1960,7 +1974,7 @@ void SphereEngine::autotune_split() {
     size_t bytes;
     double best;
     int mb = 2;  // analysis register budget (CTAs per SM)
-    int ws = 0;  // analysis: the warp-specialised form with this many CTAs per SM
+    int ws = 0;  // the warp-specialised form (analysis or synthesis) with this many CTAs per SM
   };
   std::vector<Cand> cands;
   int dev = 0, optin = 0;
@@ -1982,6 +1996,13 @@ void SphereEngine::autotune_split() {
       const size_t st = static_cast<size_t>(sp.pieces) * (sp.rSP + snh) * sp.bks * 2;
       const size_t bs = std::max(ns * st + SPLIT_MARGIN, sp.syn_min_bytes);
       if (bs <= sp.budget_bytes) cands.push_back({0, sl, 0, ns, 0, bs, 1e30});
+      // the warp-specialised persistent form, one or two CTAs per SM
+      if (ns >= 2)
+        for (int ctas = 1; ctas <= 2; ctas++) {
+          size_t wsm = 0;
+          int bc = 0, slot = 0;
+          if (syn_ws_layout(sp, sl, ns, ctas, &wsm, &bc, &slot)) cands.push_back({0, sl, 0, ns, 0, wsm, 1e30, 2, ctas});
+        }
     }
     for (int dir = 1; dir >= 0; dir--)
       for (int both = 0; both <= 1; both++) {
@@ -2003,7 +2024,7 @@ void SphereEngine::autotune_split() {
       }
   }
   const int jb0 = sp.jb, fg0 = sp.fgrp, nss0 = sp.ns_syn, nsa0 = sp.ns_ana, ab0 = sp.ana_both, ag0 = sp.ana_grid, dir0 = sp.direct,
-            mb0 = sp.ana_minb, sl0 = sp.syn_split, ws0 = sp.ana_ws;
+            mb0 = sp.ana_minb, sl0 = sp.syn_split, ws0 = sp.ana_ws, sws0 = sp.syn_ws;
   const size_t sms0 = sp.smem_syn, sma0 = sp.smem_ana;
   auto apply = [&](const Cand &c) {
     sp.jb = jb0;
@@ -2017,6 +2038,7 @@ void SphereEngine::autotune_split() {
     sp.direct = dir0;
     sp.ana_minb = mb0;
     sp.ana_ws = ws0;
+    sp.syn_ws = sws0;
     sp.syn_split = sl0;
     sp.syn_nh = sp.nh16 / sl0;
     if (c.which == 1) {
@@ -2028,6 +2050,7 @@ void SphereEngine::autotune_split() {
       sp.smem_syn = c.bytes;
       sp.syn_split = c.jb;  // the synthesis candidates carry their latitude slices in jb
       sp.syn_nh = sp.nh16 / c.jb;
+      sp.syn_ws = c.ws;
     } else {
       sp.ns_ana = c.ns;
       sp.smem_ana = c.bytes;
@@ -2069,6 +2092,7 @@ void SphereEngine::autotune_split() {
   sp.smem_syn = bs ? bs->bytes : sms0;
   sp.syn_split = bs ? bs->jb : sl0;
   sp.syn_nh = sp.nh16 / sp.syn_split;
+  sp.syn_ws = bs ? bs->ws : sws0;
   sp.ns_ana = ba ? ba->ns : nsa0;
   sp.smem_ana = ba ? ba->bytes : sma0;
   sp.ana_both = ba ? ba->jb : ab0;
@@ -2093,6 +2117,7 @@ void SphereEngine::split_plan(int *out) const {
   out[8] = split ? split->syn_split : 0;
   out[9] = split ? split->ana_ws : 0;
   out[10] = split ? split->grid_fixed : 0;
+  out[11] = split ? split->syn_ws : 0;
 }
 
 void SphereEngine::set_split_form(int linear_exact) {
@@ -2107,7 +2132,7 @@ void SphereEngine::set_split_form(int linear_exact) {
 void SphereEngine::set_split_plan(const int *in) {
   if (!split) throw InvalidArgument("the engine is not in split precision");
   SplitPlan &sp = *split;
-  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6], mb = in[7], sl = in[8], ws = in[9], gfix = in[10];
+  const int jb = in[0], fg = in[1], nss = in[2], nsa = in[3], both = in[4], grid = in[5], dir = in[6], mb = in[7], sl = in[8], ws = in[9], gfix = in[10], sws = in[11];
   int dev = 0, optin = 0;
   LMW_CUDA(cudaGetDevice(&dev));
   LMW_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -2126,6 +2151,13 @@ void SphereEngine::set_split_plan(const int *in) {
   if (bs > sp.budget_bytes || ba > sp.budget_bytes) throw InvalidArgument("split plan: the pipelines do not fit in shared memory");
   if (mb != 2 && mb != 3) throw InvalidArgument("split plan: the analysis register budget must be 2 or 3 CTAs per SM");
   if (gfix != 0 && gfix != 1) throw InvalidArgument("split plan: the grid kernel's fixed-length flag must be 0 or 1");
+  size_t swsm = 0;
+  if (sws != 0) {
+    int bc = 0, slot = 0;
+    if (nss < 2 || !syn_ws_layout(sp, sl, nss, sws, &swsm, &bc, &slot))
+      throw InvalidArgument("split plan: the warp-specialised synthesis takes 1 or 2 CTAs per SM, at least 2 stages, and must fit shared "
+                            "and tensor memory");
+  }
   size_t wsm = 0;
   if (ws != 0) {
     int bc = 0, slot = 0;
@@ -2146,7 +2178,9 @@ void SphereEngine::set_split_plan(const int *in) {
   sp.ana_minb = mb;
   sp.ana_ws = ws;
   sp.grid_fixed = gfix;
+  sp.syn_ws = sws;
   if (ws) sp.smem_ana = wsm;
+  if (sws) sp.smem_syn = swsm;
   sp.syn_split = sl;
   sp.syn_nh = sp.nh16 / sl;
   graphs_clear();

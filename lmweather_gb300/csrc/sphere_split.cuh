@@ -35,6 +35,8 @@ constexpr int SPLIT_NBT = 16;  // members per tile: 8 quantities x 16 members = 
 constexpr int SPLIT_BK = 64;
 constexpr int SPLIT_MAX_STAGES = 4;
 constexpr int SPLIT_MARGIN = 16384;  // an M = 128 MMA reads 16 KB past an A base: every A base keeps 16 KB of allocation
+constexpr int SPLIT_WS_THREADS = 320;  // warp-specialised kernels: producer warp, MMA warp, 8 epilogue warps
+constexpr int SPLIT_WS_EPI = 256;      // epilogue threads (warps 2..9)
 constexpr int SPLIT_THREADS = 128;
 constexpr int SPLIT_ANA_THREADS = 256;  // analysis: 8 warps for the gather and the RK4 epilogue, warps 0-3 read TMEM
 constexpr int SPLIT_NQ = 16;  // per (member, jh, m): U, V, zeta, Phi Fourier coefficients at the southern and northern latitude
@@ -68,6 +70,7 @@ struct SplitPlan {
   int ana_minb = 2;           // analysis register budget: CTAs per SM (2 or 3)
   int ana_ws = 0;             // 0: split_ana; 1 or 2: the warp-specialised persistent form with that many CTAs per SM
   int grid_fixed = 1;         // 1: the grid kernel compiled for the transform length (lengths 2^6..2^10); 0: any length
+  int syn_ws = 0;             // 0: split_syn; 1 or 2: the warp-specialised persistent synthesis with that many CTAs per SM
   int nsm = 152;              // multiprocessors of the device (the persistent grid)
   int ra_pair = 32;           // largest ra16[2m] + ra16[2m + 1]
   // 1: the linear terms of the tendencies (gravity-wave terms of the mean height, the Laplacian of Phi, the
@@ -387,6 +390,243 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
     }
   }
   split_teardown(tmem, ncols);
+}
+
+// ------------------------------------------------------------------------------------------- synthesis, warp-specialised
+// The same work as split_syn, by persistent CTAs whose warps take roles (as split_ana_ws): thread 0 streams the H
+// and P operand and table chunks of the CTA's items (m, member tile, latitude slice; m the fastest index) through
+// a ring of ns fixed-size stages; thread 32 issues the MMAs of item i into tensor-memory buffer i % 2 (four
+// accumulators H E/O, P E/O of nh columns each) and commits it to accf[i % 2]; warps 2..9 copy a finished buffer
+// to shared memory, release it (acce) and write the item's Fourier records while the next item loads and
+// multiplies. Same products in the same order as split_syn, same epilogue arithmetic: the same bits. Every wait is
+// bounded; after a failure each role stops and the CTA drains its own copies and MMAs before it frees its memory.
+constexpr int SPLIT_SYN_WS_THREADS = 320;
+template <int CTAS>
+__global__ void __launch_bounds__(SPLIT_SYN_WS_THREADS, CTAS) split_syn_ws(SphDev d, SplitDev sd, int B, int ns, int buf_cols, int slot_bytes) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t full[SPLIT_MAX_STAGES], empty[SPLIT_MAX_STAGES], accf[2], acce[2], done;
+  __shared__ uint32_t tslot;
+  __shared__ int s_fail, s_issued, s_consumed, s_epi_ok;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nh = sd.syn_nh, nsl = sd.nh16 / nh;  // latitudes per slice, slices
+  const int nitems = d.M * sd.ntiles * nsl;
+  const int bk = sd.bks;
+  const uint32_t ncols = 2u * static_cast<uint32_t>(buf_cols);
+  uint8_t *pipe = smem;
+  const int ldp = nh + 1;
+  // staging of a finished buffer: H E, H O (rSH rows each), P E, P O (rSP rows each), row stride nh + 1
+  float *stg = reinterpret_cast<float *>(smem + static_cast<size_t>(ns) * slot_bytes);
+  const int a_bytes = sd.rSP * bk * 2;  // A piece region of a stage (the H operand's rows fit in it)
+  const int b_bytes = nh * bk * 2;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tslot)), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int st = 0; st < ns; st++) {
+      tc::bar_init(su32(&full[st]), 1);
+      tc::bar_init(su32(&empty[st]), 1);
+    }
+    for (int b2 = 0; b2 < 2; b2++) {
+      tc::bar_init(su32(&accf[b2]), 1);
+      tc::bar_init(su32(&acce[b2]), 1);
+    }
+    tc::bar_init(su32(&done), 1);
+    tc::bar_init_fence();
+    s_fail = 0;
+    s_issued = 0;
+    s_consumed = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tslot;
+  auto item_of = [&](int item, int &m, int &tile, int &jh0) {
+    m = item % d.M;
+    const int rest = item / d.M;
+    tile = rest % sd.ntiles;
+    jh0 = (rest / sd.ntiles) * nh;
+  };
+  if (tid == 0) {
+    // producer
+    int git = 0;
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      int m, tile, jh0;
+      item_of(item, m, tile, jh0);
+      const long kp = sd.kps[m];
+      const int nchunk = static_cast<int>(kp / bk);
+      for (int g = 0; g < 2 && ok; g++) {
+        const int aR = g == 0 ? sd.rSH : sd.rSP;
+        const uint32_t abytes = static_cast<uint32_t>(aR * bk * 2);
+        const __nv_bfloat16 *A = g == 0 ? sd.aS_H + sd.aSH_off[m] + static_cast<long>(tile) * sd.rSH * kp
+                                        : sd.aS_P + sd.aS_off[m] + static_cast<long>(tile) * sd.rSP * kp;
+        const long aps = g == 0 ? sd.aSH_size : sd.aSP_size;
+        const __nv_bfloat16 *Bt = (g == 0 ? sd.tS_H : sd.tS_P) + sd.tS_off[m] + static_cast<long>(jh0) * bk;
+        const long b_cs = static_cast<long>(sd.nh16) * bk;
+        for (int c = 0; c < nchunk; c++, git++) {
+          const int st = git % ns;
+          if (git >= ns && !mbar_wait_bounded(su32(&empty[st]), ((git / ns) - 1) & 1)) {
+            s_fail = 1;
+            atomicExch(sd.err, 2);
+            ok = false;
+            break;
+          }
+          mbar_expect(su32(&full[st]), static_cast<uint32_t>(sd.pieces) * (abytes + static_cast<uint32_t>(b_bytes)));
+          uint8_t *base = pipe + static_cast<size_t>(st) * slot_bytes;
+          for (int p = 0; p < sd.pieces; p++) {
+            bulk_g2s(su32(base + p * a_bytes), A + p * aps + static_cast<long>(c) * aR * bk, abytes, su32(&full[st]));
+            bulk_g2s(su32(base + sd.pieces * a_bytes + p * b_bytes), Bt + p * sd.tS_size + static_cast<long>(c) * b_cs,
+                     static_cast<uint32_t>(b_bytes), su32(&full[st]));
+          }
+          s_issued = git + 1;
+        }
+      }
+    }
+  } else if (tid == 32) {
+    // MMA issuer: per operand g, K columns below ke16[m] (even n) into the E accumulator, the rest into O
+    const int tp[6][2] = {{2, 0}, {1, 1}, {0, 2}, {1, 0}, {0, 1}, {0, 0}};
+    const int t0 = sd.terms == 6 ? 0 : (sd.terms == 3 ? 3 : 5);
+    const uint32_t sbo = static_cast<uint32_t>(bk) * 16u;
+    const uint32_t idesc = idesc_m128(nh);
+    int git = 0, it = 0;
+    bool ok = true;
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      int m, tile, jh0;
+      item_of(item, m, tile, jh0);
+      const int nchunk = static_cast<int>(sd.kps[m] / bk), kseg = sd.ke16[m];
+      const int bb = it & 1;
+      if (it >= 2 && !mbar_wait_bounded(su32(&acce[bb]), ((it >> 1) - 1) & 1)) {
+        s_fail = 1;
+        atomicExch(sd.err, 5);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int g = 0; g < 2 && ok; g++) {
+        bool started[2] = {false, false};
+        for (int c = 0; c < nchunk; c++, git++) {
+          const int st = git % ns;
+          if (!mbar_wait_bounded(su32(&full[st]), (git / ns) & 1)) {
+            s_fail = 1;
+            atomicExch(sd.err, 3);
+            ok = false;
+            break;
+          }
+          s_consumed = git + 1;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          uint8_t *base = pipe + static_cast<size_t>(st) * slot_bytes;
+          for (int kk = 0; kk < bk; kk += 16) {
+            const int seg = c * bk + kk >= kseg ? 1 : 0;
+            const uint32_t accc = tmem + static_cast<uint32_t>(bb * buf_cols + (2 * g + seg) * nh);
+            for (int tt = t0; tt < 6; tt++) {
+              const int pa = tp[tt][0], pb = tp[tt][1];
+              const uint64_t ad = chunk_desc(su32(base + pa * a_bytes + (kk / 8) * 128), sbo);
+              const uint64_t bd = chunk_desc(su32(base + sd.pieces * a_bytes + pb * b_bytes + (kk / 8) * 128), sbo);
+              const uint32_t accum = started[seg] ? 1u : 0u;
+              asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(accc),
+                           "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+                           : "memory");
+              started[seg] = true;
+            }
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&empty[st])) : "memory");
+        }
+      }
+      if (!ok) break;
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&accf[bb])) : "memory");
+      it++;
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(&done)) : "memory");
+  } else if (warp >= 2) {
+    // epilogue warps
+    const int et = tid - 64;
+    int it = 0;
+    const float ia = d.inv_a_f;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+      int m, tile, jh0;
+      item_of(item, m, tile, jh0);
+      const int bb = it & 1;
+      if (et == 0) s_epi_ok = mbar_wait_bounded(su32(&accf[bb]), (it >> 1) & 1) ? 1 : 0;
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (!s_epi_ok) {
+        if (et == 0) {
+          s_fail = 1;
+          atomicExch(sd.err, 6);
+        }
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int mt = min(sd.nbt, B - tile * sd.nbt);
+      // accumulators -> staging: warp w reads lanes 32 (w % 4) .. + 31; warps 2..5 the even 32-column blocks of
+      // the four accumulators, warps 6..9 the odd ones. H accumulators hold rSH meaningful rows, P rSP
+      const int quarter = warp & 3, row = quarter * 32 + lane;
+      const uint32_t lanebase = tmem + static_cast<uint32_t>(bb * buf_cols) + (static_cast<uint32_t>(quarter * 32) << 16);
+      const int nblk = (nh + 31) / 32;
+      for (int a4 = 0; a4 < 4; a4++) {
+        const int rows_a = a4 < 2 ? sd.rSH : sd.rSP;
+        if (quarter * 32 >= rows_a) continue;
+        float *dst = stg + static_cast<size_t>(a4 < 2 ? a4 * sd.rSH : 2 * sd.rSH + (a4 - 2) * sd.rSP) * ldp;
+        for (int cbk = (warp < 6 ? 0 : 1); cbk < nblk; cbk += 2) {
+          const int c0 = cbk * 32;
+          float v[32];
+          if (c0 + 32 <= nh) {
+            tmem_ld32(lanebase + a4 * nh + c0, v);
+          } else {
+            tmem_ld8(lanebase + a4 * nh + c0, v);
+            tmem_ld8(lanebase + a4 * nh + c0 + 8, v + 8);
+          }
+          if (row < rows_a) {
+            const int w = min(32, nh - c0);
+#pragma unroll
+            for (int i = 0; i < 32; i++)
+              if (i < w) dst[row * ldp + c0 + i] = v[i];
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (et == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&acce[bb])) : "memory");
+      // Fourier coefficients of both mirror latitudes (as split_syn): P sums south E + O, north E - O; H sums
+      // south E + O, north O - E; U = (i m chi P - psi H) / a, V = (i m psi P + chi H) / a (cpp/sphere.cpp:200-201)
+      const float mm = static_cast<float>(m);
+      const float *HE0 = stg, *HO0 = stg + static_cast<size_t>(sd.rSH) * ldp, *PE0 = stg + static_cast<size_t>(2 * sd.rSH) * ldp,
+                  *PO0 = stg + static_cast<size_t>(2 * sd.rSH + sd.rSP) * ldp;
+      for (int e = et; e < mt * nh; e += SPLIT_WS_EPI) {
+        const int ml = e / nh, i = e - ml * nh, jh = jh0 + i;
+        if (jh >= d.nh) continue;
+        const float *PE = PE0 + (ml * 8) * ldp + i, *PO = PO0 + (ml * 8) * ldp + i;
+        const float *HE = HE0 + (ml * 4) * ldp + i, *HO = HO0 + (ml * 4) * ldp + i;
+        float4 *dst = reinterpret_cast<float4 *>(sd.dsyn + ((static_cast<long>(tile * sd.nbt + ml) * d.nh + jh) * d.M + m) * SPLIT_NQ);
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+          float pv[8], hv[4];
+#pragma unroll
+          for (int q = 0; q < 8; q++) pv[q] = side == 0 ? PE[q * ldp] + PO[q * ldp] : PE[q * ldp] - PO[q * ldp];
+#pragma unroll
+          for (int q = 0; q < 4; q++) hv[q] = side == 0 ? HE[q * ldp] + HO[q * ldp] : HO[q * ldp] - HE[q * ldp];
+          const float2 U = cscale(csub(imul(make_float2(pv[2], pv[3]), mm), make_float2(hv[0], hv[1])), ia);
+          const float2 V = cscale(cadd(imul(make_float2(pv[0], pv[1]), mm), make_float2(hv[2], hv[3])), ia);
+          dst[2 * side] = make_float4(U.x, U.y, V.x, V.y);
+          dst[2 * side + 1] = make_float4(pv[4], pv[5], pv[6], pv[7]);
+        }
+      }
+      // the staging is free for the next item
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      it++;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (!s_fail) {
+      if (!mbar_wait_bounded(su32(&done), 0)) atomicExch(sd.err, 4);
+    } else {
+      tc::wait_for(su32(&done), 0, 200000000ull);
+      for (int g2 = s_consumed; g2 < s_issued; g2++) tc::wait_for(su32(&full[g2 % ns]), (g2 / ns) & 1, 200000000ull);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
 }
 
 // ------------------------------------------------------------------------------------------- grid (FP32)
@@ -904,8 +1144,6 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
 // copy it to shared memory, release the buffer (acce[i % 2]) and run the epilogue (ana_coef, the same arithmetic as
 // split_ana). Items are visited with m the fastest index. Every wait is bounded; after a failure each role stops,
 // the CTA drains its own copies and MMAs and frees its tensor memory.
-constexpr int SPLIT_WS_THREADS = 320;
-constexpr int SPLIT_WS_EPI = 256;  // epilogue threads (warps 2..9)
 template <bool BOTH, int CTAS>
 __global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d, SplitDev sd, SphTab<float> t, StageArgs sa, int B, int ns,
                                                                        int buf_cols, int slot_bytes, double2 *__restrict__ x0, float2 *__restrict__ xf,
@@ -1309,6 +1547,28 @@ inline bool ws_layout(const SplitPlan &sp, int both, int ns, int ctas, size_t *s
   *smem = total;
   *buf_cols = bc;
   *slot = static_cast<int>(sl);
+  if (2 * bc * ctas > 512) return false;
+  if (total > sp.budget_bytes) return false;
+  if (ctas == 2 && 2 * (total + 1024 + 2048) > 233472) return false;
+  return ctas == 1 || ctas == 2;
+}
+
+// shared-memory layout of the warp-specialised synthesis with `sl` latitude slices and ns stages: stage slots,
+// then the staging of one accumulator buffer (H E/O with rSH rows, P E/O with rSP rows, stride nh + 1), then the
+// margin an M = 128 MMA may read past an A base. Returns false when it does not fit (tensor memory: two buffers of
+// four nh-column accumulators per CTA, `ctas` CTAs per SM).
+inline bool syn_ws_layout(const SplitPlan &sp, int sl, int ns, int ctas, size_t *smem, int *buf_cols, int *slot) {
+  if (sl < 1 || sp.nh16 % sl != 0) return false;
+  const int nh = sp.nh16 / sl;
+  if (nh < 16 || nh % 16 != 0 || nh > 256) return false;
+  int bc = 32;
+  while (bc < 4 * nh) bc <<= 1;
+  const size_t st = static_cast<size_t>(sp.pieces) * (sp.rSP + nh) * sp.bks * 2;
+  const size_t stg = (static_cast<size_t>(2 * sp.rSH + 2 * sp.rSP) * (nh + 1) * sizeof(float) + 15) & ~static_cast<size_t>(15);
+  const size_t total = ns * st + stg + SPLIT_MARGIN;
+  *smem = total;
+  *buf_cols = bc;
+  *slot = static_cast<int>(st);
   if (2 * bc * ctas > 512) return false;
   if (total > sp.budget_bytes) return false;
   if (ctas == 2 && 2 * (total + 1024 + 2048) > 233472) return false;

@@ -375,6 +375,11 @@ def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
         for ctas in (1, 2):
             for ns in (2, 3):
                 ws_plans.append(dict(analysis_warp_specialised=ctas, analysis_both_parities=both, grid_writes_operands=1, analysis_stages=ns))
+    # the warp-specialised persistent synthesis (operand and table chunks streamed by one thread, MMAs by another
+    # into two tensor-memory buffers, the previous item's records written by eight warps), where it fits
+    for sl in (1, 2):
+        for ctas in (1, 2):
+            ws_plans.append(dict(synthesis_warp_specialised=ctas, synthesis_latitude_slices=sl, synthesis_stages=2))
     tuned = s.split_plan()
     accepted = []
     for plan in ws_plans:
@@ -387,7 +392,7 @@ def test_split_plans_compute_the_same_arithmetic(engine, T, members, terms):
     plans += accepted
     results = []
     for plan in [{}] + plans:
-        s.set_split_plan(**{**tuned, **({} if not plan else {"analysis_warp_specialised": 0}), **plan})
+        s.set_split_plan(**{**tuned, **({} if not plan else {"analysis_warp_specialised": 0, "synthesis_warp_specialised": 0}), **plan})
         for b in range(members):
             s.set_state(*start[b], member=b)
         for _ in range(3):
