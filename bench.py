@@ -796,7 +796,7 @@ def run_case(args) -> int:
 def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, epochs=100, batch=512, lr=3e-4, lr_min=3e-5,
                     hmin=8000.0, hmax=8000.0, members=1024, rollout_windows=80, check_every=4, threshold=1e-3, ref_windows=4, seed=1,
                     check_precision=None, loss="energy", thresholds=(), clip=2.0, data_precision=0, augment=True, averaging=0.9995,
-                    sym_average=8, kinetic_weight=1.0, takeovers=("member",)) -> dict:
+                    sym_average=8, kinetic_weight=1.0, takeovers=("member",), drift_trajectories=0, drift_windows=8, drift_epochs=50) -> dict:
     """The learned surrogate end to end: solver trajectories (balanced turbulence on training seeds, RK4 at 900 s,
     del^4 with a 1-day e-folding at n = T; pairs (state, state + 6 h) from every window; the last tenth of the
     trajectories held out) -> training on the GPU -> validation errors per 6-hour window -> a hybrid rollout of
@@ -815,6 +815,15 @@ def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, e
     sur.set_kinetic_weight(kinetic_weight)
     gen_s = sur.generate(trajectories, windows, seed0=1_000_000 * seed, hmin=hmin, hmax=hmax, precision=data_precision)
     fit = sur.fit(epochs, batch=batch, lr=lr, lr_min=lr_min, val_fraction=0.1, seed=seed, loss=loss)
+    drift = None
+    if drift_trajectories > 0:
+        # more training trajectories from states the trained network advanced drift_windows windows, then a
+        # continued fit on all training trajectories (the held-out validation trajectories stay the same)
+        gen2 = sur.generate_drifted(drift_trajectories, drift_windows, seed0=3_000_000 * seed, hmin=hmin, hmax=hmax, precision=data_precision)
+        fit2 = sur.fit(drift_epochs, batch=batch, lr=lr, lr_min=lr_min, val_fraction=0.1, seed=seed + 1, loss=loss)
+        drift = {"trajectories": drift_trajectories, "network_windows": drift_windows, "epochs": drift_epochs, "generate_s": gen2,
+                 "fit_before": fit}
+        fit = fit2
     hist_loss, _ = sur.history()
     train_ms, fwd_ms = sur.time(batch, 10)
     out = {"truncation": truncation, "features": sur.features, "hidden": hidden, "pairs": trajectories * windows,
@@ -822,7 +831,7 @@ def surrogate_study(truncation=42, hidden=4096, trajectories=2560, windows=80, e
            "data_precision": ["fp64", "fp32", "split3"][data_precision], "generate_s": gen_s, "loss": loss, "clip_ratio": clip,
            "epochs": epochs, "lr": [lr, lr_min], "fit": fit, "loss_by_epoch": [round(v, 4) for v in hist_loss.tolist()],
            "train_step_ms": train_ms, "forward_ms_batch": fwd_ms, "batch": batch, "augment": augment, "averaging": averaging,
-           "symmetry_maps_averaged": sym_average, "kinetic_weight": kinetic_weight,
+           "symmetry_maps_averaged": sym_average, "kinetic_weight": kinetic_weight, "drift": drift,
            "check_precision": ["fp64", "fp32", "split3"][check_precision]}
     if members > 0 and rollout_windows > 0:
         for tk in takeovers:
@@ -880,6 +889,9 @@ def main():
     ap.add_argument("--takeover", default="window,member", help="rollout takeover modes to run (window: RK4 replaces a failed window; "
                     "member: RK4 keeps a failed member)")
     ap.add_argument("--lr-min", type=float, default=3e-5)
+    ap.add_argument("--drift-trajectories", type=int, default=0, help="training trajectories added from network-advanced states")
+    ap.add_argument("--drift-windows", type=int, default=8, help="network windows before those trajectories start")
+    ap.add_argument("--drift-epochs", type=int, default=50, help="epochs of the continued fit after adding them")
     ap.add_argument("--data-precision", default="split3", choices=["fp64", "split3"])
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -900,7 +912,8 @@ def main():
                                              thresholds=tuple(float(v) for v in args.sweep.split(",") if v), augment=bool(args.augment),
                                              averaging=args.averaging, data_precision=2 if args.data_precision == "split3" else 0,
                                              sym_average=args.sym_average, kinetic_weight=args.kinetic_weight,
-                                             takeovers=tuple(args.takeover.split(",")))))
+                                             takeovers=tuple(args.takeover.split(",")), drift_trajectories=args.drift_trajectories,
+                                             drift_windows=args.drift_windows, drift_epochs=args.drift_epochs)))
         return 0
     if args.impl == "reference":
         return run_reference(args, rank, world)

@@ -361,6 +361,13 @@ int lmw_surrogate_dims(lmw_surrogate *s, int *dims);
  * on the device. seconds = wall time. */
 int lmw_surrogate_generate(lmw_surrogate *s, int trajectories, int windows, uint64_t seed0, double hmin, double hmax, int precision,
                            double *seconds);
+/* after a fit: `trajectories` more training trajectories (seeds seed0 + i, heights from seed0 as above) that start
+ * where the network takes a state -- balanced turbulence advanced net_windows windows by the network -- and then
+ * record the generated window count of RK4 in `precision`. They are placed before the existing trajectories; the
+ * held-out validation trajectories of the first fit stay held out, and the normalisation stays. A following fit
+ * continues from the current weights. No reference counterpart. */
+int lmw_surrogate_generate_drifted(lmw_surrogate *s, int trajectories, int net_windows, uint64_t seed0, double hmin, double hmax, int precision,
+                                   double *seconds);
 /* Adam with a cosine learning rate from lr to lr_min over `epochs` epochs of the training trajectories (the last
  * val_fraction of the trajectories are held out). loss_mode 0: mean square of the per-n normalised increments;
  * 1: energy norm of the increment error (kinetic energy of the vorticity and divergence errors plus available

@@ -137,6 +137,7 @@ _SIGS = {
     "lmw_surrogate_destroy": (_I, [_P]),
     "lmw_surrogate_dims": (_I, [_P, _IP]),
     "lmw_surrogate_generate": (_I, [_P, _I, _I, _U64, _D, _D, _I, _DP]),
+    "lmw_surrogate_generate_drifted": (_I, [_P, _I, _I, _U64, _D, _D, _I, _DP]),
     "lmw_surrogate_fit": (_I, [_P, _I, _I, _D, _D, _D, _U64, _I, _DP]),
     "lmw_surrogate_evaluate": (_I, [_P, _I, _I, _DP, _DP]),
     "lmw_surrogate_advance": (_I, [_P, _I, _DP]),
@@ -873,6 +874,12 @@ class Surrogate:
     def generate(self, trajectories: int, windows: int, seed0: int = 1, hmin=5000.0, hmax=10000.0, precision: int = FP64) -> float:
         sec = _D()
         _check(self._lib.lmw_surrogate_generate(self._h, trajectories, windows, seed0, hmin, hmax, precision, C.byref(sec)))
+        return sec.value
+
+    def generate_drifted(self, trajectories: int, net_windows: int, seed0: int = 2, hmin=5000.0, hmax=10000.0, precision: int = FP64) -> float:
+        """After a fit: more training trajectories starting from states the network advanced net_windows windows."""
+        sec = _D()
+        _check(self._lib.lmw_surrogate_generate_drifted(self._h, trajectories, net_windows, seed0, hmin, hmax, precision, C.byref(sec)))
         return sec.value
 
     def fit(self, epochs: int, batch: int = 512, lr=3e-4, lr_min=3e-5, val_fraction=0.1, seed: int = 1, loss: str = "energy") -> dict:

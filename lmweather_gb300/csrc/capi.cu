@@ -699,6 +699,11 @@ int lmw_surrogate_generate(lmw_surrogate *s, int trajectories, int windows, uint
   return SUR(s, need(precision >= 0 && precision <= 2, "precision must be 0 (FP64), 1 (FP32) or 2 (split BF16)");
              s->s->generate(trajectories, windows, seed0, hmin, hmax, precision, 1024); if (seconds) *seconds = s->s->gen_seconds);
 }
+int lmw_surrogate_generate_drifted(lmw_surrogate *s, int trajectories, int net_windows, uint64_t seed0, double hmin, double hmax, int precision,
+                                   double *seconds) {
+  return SUR(s, need(precision >= 0 && precision <= 2, "precision must be 0 (FP64), 1 (FP32) or 2 (split BF16)");
+             s->s->generate_drifted(trajectories, net_windows, seed0, hmin, hmax, precision, 1024); if (seconds) *seconds = s->s->gen_seconds);
+}
 int lmw_surrogate_fit(lmw_surrogate *s, int epochs, int batch, double lr, double lr_min, double val_fraction, uint64_t shuffle_seed,
                       int loss_mode, double *stats) {
   return SUR(s, need(loss_mode == 0 || loss_mode == 1, "loss mode must be 0 or 1");

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <utility>
 #include <cstdint>
 #include <functional>
 #include <stdexcept>
@@ -67,6 +68,10 @@ template <class T> struct DevBuf {
     n = 0;
   }
   size_t bytes() const { return n * sizeof(T); }
+  void swap(DevBuf &o) {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+  }
 };
 
 // Pinned host staging buffer.

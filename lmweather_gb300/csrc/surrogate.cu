@@ -1135,6 +1135,7 @@ void Surrogate::generate(int trajectories, int windows, uint64_t seed0, double h
   ntraj = trajectories;
   nwin = windows;
   have_norm = false;
+  val_traj = 0;
   const int dp = net->dim[0];
   snaps.alloc(static_cast<size_t>(ntraj) * (nwin + 1) * dp);
   std::mt19937_64 rng(seed0);
@@ -1156,6 +1157,46 @@ void Surrogate::generate(int trajectories, int windows, uint64_t seed0, double h
     }
     LMW_CUDA(cudaStreamSynchronize(e.stream));
   }
+  gen_seconds = seconds_since(t0);
+}
+
+void Surrogate::generate_drifted(int trajectories, int net_windows, uint64_t seed0, double hmin, double hmax, int precision, int batch_members) {
+  if (trajectories < 1 || net_windows < 1) throw InvalidArgument("need at least one trajectory and one network window");
+  if (!(hmin > 0) || !(hmax >= hmin)) throw InvalidArgument("mean heights must be positive and ordered");
+  if (!have_norm || ntraj < 2) throw InvalidArgument("fit the network on generated data before generating from its states");
+  const auto t0 = std::chrono::steady_clock::now();
+  const int dp = net->dim[0];
+  const size_t per = static_cast<size_t>(nwin + 1) * dp;
+  DevBuf<float> grown;
+  grown.alloc((static_cast<size_t>(trajectories) + ntraj) * per);
+  LMW_CUDA(cudaMemcpyAsync(grown.p + static_cast<size_t>(trajectories) * per, snaps.p, static_cast<size_t>(ntraj) * per * sizeof(float),
+                           cudaMemcpyDeviceToDevice, stream));
+  std::mt19937_64 rng(seed0);
+  std::uniform_real_distribution<double> U(hmin, hmax);
+  std::vector<double> H(trajectories);
+  for (double &h : H) h = U(rng);
+  const int bm = std::max(1, batch_members);
+  const int total = trajectories + ntraj;
+  for (int t0j = 0; t0j < trajectories; t0j += bm) {
+    const int k = std::min(bm, trajectories - t0j);
+    SphereConfig c = cfg;
+    c.members = k;
+    c.precision = precision;
+    SphereEngine e(c);
+    for (int j = 0; j < k; j++) e.turbulence(seed0 + static_cast<uint64_t>(t0j + j), H[t0j + j], 30.0, T / 2, j);
+    LMW_CUDA(cudaStreamSynchronize(e.stream));
+    for (int w = 0; w < net_windows; w++) advance_states(e.device_state(), k, nullptr);
+    LMW_CUDA(cudaStreamSynchronize(stream));
+    e.state_written();
+    for (int w = 0; w <= nwin; w++) {
+      if (w > 0) e.run(window, dt);
+      snapshot<<<grid_for(static_cast<long>(k) * dp, 256), 256, 0, e.stream>>>(e.device_state(), k, nfeat, grown.p, t0j, nwin + 1, w, dp);
+      LMW_LAUNCH_CHECK();
+    }
+    LMW_CUDA(cudaStreamSynchronize(e.stream));
+  }
+  snaps.swap(grown);
+  ntraj = total;
   gen_seconds = seconds_since(t0);
 }
 
@@ -1295,10 +1336,12 @@ SurrogateStats Surrogate::fit(int epochs, int batch, double lr, double lr_min, d
   check_batch(batch, net->max_batch);
   if (!(val_fraction > 0 && val_fraction < 1)) throw InvalidArgument("the validation fraction must lie in (0, 1)");
   SurrogateStats st;
-  const int nval_traj = std::max(1, static_cast<int>(std::lround(ntraj * val_fraction)));
+  // the held-out trajectories are fixed by the first fit (trajectories added later go before them)
+  const int nval_traj = val_traj > 0 ? val_traj : std::max(1, static_cast<int>(std::lround(ntraj * val_fraction)));
   const int ntrain_traj = ntraj - nval_traj;
   if (ntrain_traj < 1) throw InvalidArgument("no training trajectories left after the validation split");
   if (!have_norm) normalise(ntrain_traj);
+  val_traj = nval_traj;
   const int ntrain = ntrain_traj * nwin, p_val0 = ntrain, p_val1 = ntraj * nwin;
   if (ntrain < batch) throw InvalidArgument("fewer training pairs than one batch");
   std::vector<double> e, p;

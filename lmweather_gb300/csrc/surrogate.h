@@ -140,6 +140,11 @@ class Surrogate {
 
   void reset(uint64_t seed);  // a fresh network and optimiser (the data stay)
   void generate(int trajectories, int windows, uint64_t seed0, double hmin, double hmax, int precision, int batch_members);
+  // more training trajectories that start where the network takes a state: seeded balanced turbulence advanced
+  // net_windows windows by the network, then `windows` windows of RK4 recorded as generate() does. They go before
+  // the existing trajectories, so the held-out validation trajectories stay the same (val_traj)
+  void generate_drifted(int trajectories, int net_windows, uint64_t seed0, double hmin, double hmax, int precision, int batch_members);
+  int val_traj = 0;  // held-out trajectories at the end of the data, fixed by the first fit
   void normalise(int ntrain_trajectories);
   SurrogateStats fit(int epochs, int batch, double lr, double lr_min, double val_fraction, uint64_t shuffle_seed);
   // per-window height errors of the current network on pairs [p0, p1): out[i] (network), pers[i] (persistence)

@@ -215,3 +215,20 @@ def test_rollout_takeover_semantics(trained, engine, check, takeover):
     sur.set_takeover("member")
     with pytest.raises(ValueError):
         sur.set_takeover("never")
+
+
+def test_drifted_trajectories_keep_the_held_out_set(engine):
+    # trajectories started from network-advanced states go before the existing ones: the held-out validation
+    # trajectories of the first fit stay the same, so the same network scores the same validation error
+    sur = engine.Surrogate(21, hidden=256, seed=5)
+    sur.generate(40, 4, seed0=300, hmin=8000.0, hmax=8000.0)
+    st = sur.fit(2, batch=128, lr=1e-3, lr_min=1e-4, val_fraction=0.1, seed=2)
+    sur.generate_drifted(24, 2, seed0=700, hmin=8000.0, hmax=8000.0)
+    again = sur.fit(0, batch=128, val_fraction=0.1, seed=3)
+    assert again["val_err_mean"] == pytest.approx(st["val_err_mean"], rel=1e-9)
+    # and a continued fit trains on the larger set
+    more = sur.fit(2, batch=128, lr=1e-3, lr_min=1e-4, val_fraction=0.1, seed=4)
+    assert np.isfinite(more["val_err_mean"]) and more["val_err_mean"] > 0
+    with pytest.raises(ValueError):
+        engine.Surrogate(21, hidden=256, seed=6).generate_drifted(8, 1)
+    sur.close()
