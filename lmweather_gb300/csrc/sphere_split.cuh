@@ -853,6 +853,14 @@ __device__ __forceinline__ void pack_syn_coef(const SphDev &d, const SplitDev &s
 
 __device__ __forceinline__ float2 d2f2(double2 v) { return make_float2(d2f_int(v.x), d2f_int(v.y)); }
 
+// The split path's private FP32 buffers (the state's copy, the RK4 accumulator, the stage inputs) order each m's
+// coefficients by parity: n - m even first (index (n - m) / 2), then odd ((N - m) / 2 + 1 + (n - m - 1) / 2), so an
+// analysis work item of one parity reads and writes them with unit stride. The FP64 state keeps the triangle order.
+__device__ __forceinline__ int par_index(const SphDev &d, int m, int n) {
+  const int k = n - m;
+  return d.tri[m] + ((k & 1) ? (d.N - m) / 2 + 1 + (k >> 1) : (k >> 1));
+}
+
 // After the state was set from outside the stepping: its FP32 copy xf (stages 0-2 read it) and the synthesis
 // operands. grid: (ceil(ntri/128), B)
 __global__ void split_pack_state(SphDev d, SplitDev sd, const float *__restrict__ kfac32, const double2 *__restrict__ x, float2 *__restrict__ xf) {
@@ -860,11 +868,12 @@ __global__ void split_pack_state(SphDev d, SplitDev sd, const float *__restrict_
   if (q >= d.ntri) return;
   const size_t i = static_cast<size_t>(b) * 3 * d.ntri + q;
   const float2 z = d2f2(x[i]), dl = d2f2(x[i + d.ntri]), f = d2f2(x[i + 2 * d.ntri]);
-  xf[i] = z;
-  xf[i + d.ntri] = dl;
-  xf[i + 2 * d.ntri] = f;
-  const int n = d.trin[q];
-  pack_syn_coef(d, sd, kfac32[n], b, d.trim[q], n, z, dl, f);
+  const int n = d.trin[q], m = d.trim[q];
+  const size_t ip = static_cast<size_t>(b) * 3 * d.ntri + par_index(d, m, n);
+  xf[ip] = z;
+  xf[ip + d.ntri] = dl;
+  xf[ip + 2 * d.ntri] = f;
+  pack_syn_coef(d, sd, kfac32[n], b, m, n, z, dl, f);
 }
 
 // ------------------------------------------------------------------------------------------- analysis + RK4
@@ -892,7 +901,11 @@ __device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, co
   float2 kd = cadd(cadd(imul(bP, mm), aH), cscale(eP, t.lapl[n]));
   float2 kf = csub(vH, imul(uP, mm));
   const int q = d.tri[m] + n - m;
-  const size_t mb = static_cast<size_t>(b) * 3 * d.ntri, base = mb + q;
+  // the FP64 state in triangle order (q); the FP32 buffers in parity order: this coefficient at qp, its
+  // neighbours n + 1 and n - 1 (the other parity) at qu and ql
+  const int ne = (d.N - m) / 2 + 1;  // coefficients of even n - m
+  const int qp = d.tri[m] + (s ? ne + r : r), qu = d.tri[m] + (s ? r + 1 : ne + r), ql = d.tri[m] + (s ? r : ne + r - 1);
+  const size_t mb = static_cast<size_t>(b) * 3 * d.ntri, base = mb + q, basep = mb + qp;
   // the stage input in FP32: the state's copy at stage 0, else the previous stage's output (a separate buffer:
   // neighbouring n belong to other CTAs)
   const float2 *yin = sa.stage == 0 ? xf : xin;
@@ -902,7 +915,7 @@ __device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, co
     // axis the Coriolis terms -D(f U, f V) and D(f V, -f U) with f = 2 Omega mu, which couple n - 1, n, n + 1 of
     // the same m
     auto yat = [&](int field, int qq) -> float2 { return yin[mb + static_cast<size_t>(field) * d.ntri + qq]; };
-    const float2 yz = yat(0, q), yd = yat(1, q), yf = yat(2, q);
+    const float2 yz = yat(0, qp), yd = yat(1, qp), yf = yat(2, qp);
     const float phibar = xf[mb + 2 * d.ntri].x * t.Ps[0];
     const float lp = t.lapl[n];
     kd.x += lp * yf.x;
@@ -912,8 +925,8 @@ __device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, co
     if (!(d.gflag[b] & 1)) {
       const float om = static_cast<float>(d.om2[b]);
       const float cA = sd.lin32[q], cB = sd.lin32[d.ntri + q], cC = sd.lin32[2 * d.ntri + q];
-      const float2 zu = n < d.N ? yat(0, q + 1) : make_float2(0, 0), du = n < d.N ? yat(1, q + 1) : make_float2(0, 0);
-      const float2 zl = n > m ? yat(0, q - 1) : make_float2(0, 0), dd = n > m ? yat(1, q - 1) : make_float2(0, 0);
+      const float2 zu = n < d.N ? yat(0, qu) : make_float2(0, 0), du = n < d.N ? yat(1, qu) : make_float2(0, 0);
+      const float2 zl = n > m ? yat(0, ql) : make_float2(0, 0), dd = n > m ? yat(1, ql) : make_float2(0, 0);
       // -D(fU, fV)_n = -2 Omega (cA delta_{n+1} + cB delta_{n-1} - i cC zeta_n)
       kz.x -= om * (cA * du.x + cB * dd.x + cC * yz.y);
       kz.y -= om * (cA * du.y + cB * dd.y - cC * yz.x);
@@ -930,12 +943,12 @@ __device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, co
     float2 yv[3], av[3];
 #pragma unroll
     for (int f = 0; f < 3; f++) {
-      yv[f] = xf[base + static_cast<size_t>(f) * d.ntri];
-      av[f] = sa.stage > 0 ? acc[base + static_cast<size_t>(f) * d.ntri] : make_float2(0.0f, 0.0f);
+      yv[f] = xf[basep + static_cast<size_t>(f) * d.ntri];
+      av[f] = sa.stage > 0 ? acc[basep + static_cast<size_t>(f) * d.ntri] : make_float2(0.0f, 0.0f);
     }
 #pragma unroll
     for (int f = 0; f < 3; f++) {
-      const size_t i = base + static_cast<size_t>(f) * d.ntri;
+      const size_t i = basep + static_cast<size_t>(f) * d.ntri;
       acc[i] = sa.stage == 0 ? k[f] : make_float2(fmaf(2.0f, k[f].x, av[f].x), fmaf(2.0f, k[f].y, av[f].y));
       nv[f] = make_float2(fmaf(sa.c32, k[f].x, yv[f].x), fmaf(sa.c32, k[f].y, yv[f].y));
       // the next stage input is kept when the linear-exact form reads it (the split synthesis reads the packed
@@ -948,18 +961,17 @@ __device__ __forceinline__ void ana_coef(const SphDev &d, const SplitDev &sd, co
 #pragma unroll
     for (int f = 0; f < 3; f++) {
       xv[f] = x0[base + static_cast<size_t>(f) * d.ntri];
-      av[f] = acc[base + static_cast<size_t>(f) * d.ntri];
+      av[f] = acc[basep + static_cast<size_t>(f) * d.ntri];
     }
 #pragma unroll
     for (int f = 0; f < 3; f++) {
-      const size_t i = base + static_cast<size_t>(f) * d.ntri;
       const double2 sum = make_double2(f2d_int(av[f].x + k[f].x), f2d_int(av[f].y + k[f].y));
       const double2 val = make_double2(fma(sa.c, sum.x, xv[f].x), fma(sa.c, sum.y, xv[f].y));
       const double fac = sa.filt[(f == 2 ? 1 : 0) * d.M + n];
       const double2 x1 = q == 0 ? val : cscale(val, fac);
-      x0[i] = x1;
+      x0[base + static_cast<size_t>(f) * d.ntri] = x1;
       nv[f] = d2f2(x1);
-      xf[i] = nv[f];
+      xf[basep + static_cast<size_t>(f) * d.ntri] = nv[f];
     }
   }
   pack_syn_coef(d, sd, t.kfac[n], b, m, n, nv[0], nv[1], nv[2]);
