@@ -619,20 +619,28 @@ def other_workloads(lw, lib, args, ens):
     return out
 
 
-def surrogate_workload(lw, trajectories=2560, windows=80, epochs=100, members=1024, rollout_windows=80, member_windows=16,
-                       kinetic_weight=0.25):
+def surrogate_workload(lw, trajectories=2560, windows=80, epochs=200, members=1024, rollout_windows=80, member_windows=16,
+                       kinetic_weight=0.25, maps=16, averaging=0.9998, drift_trajectories=768, drift_windows=8, drift_epochs=100):
     """Config 4 inside the benchmark: the T42 residual MLP (5676 -> 4096 x 3 -> 5676, GELU, BF16 on tcgen05) trained
     on the configured 204,800 solver pairs (`trajectories` x `windows`; split-precision RK4 data, FP64 state; 6-hour
     windows of 900 s steps, mean height 8000 m) for `epochs` epochs with symmetry-augmented batches, averaged
-    weights and the kinetic-energy part of the loss weighted by `kinetic_weight`, then hybrid rollouts of `members`
-    held-out members (the 8-map averaged network; split-precision RK4 checking every 4th window against the 1e-3
-    threshold): over the configured 20 days (`rollout_windows`) with FP64 RK4 replacing each failed window (the
-    network keeps the member), and over `member_windows` windows with FP64 RK4 taking failed members over for good."""
+    weights and the kinetic-energy part of the loss weighted by `kinetic_weight`; then `drift_trajectories` more
+    RK4 trajectories that start from states the trained network advanced `drift_windows` windows, and a continued
+    fit of `drift_epochs` epochs on all training trajectories (the held-out ones stay held out). Then hybrid
+    rollouts of `members` held-out members (the `maps`-map averaged network; split-precision RK4 checking every 4th
+    window against the 1e-3 threshold): over the configured 20 days (`rollout_windows`) with FP64 RK4 replacing
+    each failed window (the network keeps the member), and over `member_windows` windows with FP64 RK4 taking
+    failed members over for good."""
     t0 = time.perf_counter()
     sur = lw.Surrogate(42, hidden=4096, seed=1)
     sur.set_kinetic_weight(kinetic_weight)
+    sur.set_averaging(averaging)
+    sur.set_symmetry_average(maps)
     gen_s = sur.generate(trajectories, windows, seed0=1_000_000, hmin=8000.0, hmax=8000.0, precision=lw.SPLIT_BF16)
-    fit = sur.fit(epochs, batch=512, lr=3e-4, lr_min=3e-5, val_fraction=0.1, seed=1, loss="energy")
+    fit0 = sur.fit(epochs, batch=512, lr=3e-4, lr_min=3e-5, val_fraction=0.1, seed=1, loss="energy")
+    gen2_s = sur.generate_drifted(drift_trajectories, drift_windows, seed0=3_000_000, hmin=8000.0, hmax=8000.0, precision=lw.SPLIT_BF16)
+    fit = sur.fit(drift_epochs, batch=512, lr=3e-4, lr_min=3e-5, val_fraction=0.1, seed=2, loss="energy")
+    fit["seconds"] += fit0["seconds"]
     train_ms, fwd_ms = sur.time(512, 10)
     _, fwd1024 = sur.time(1024, 10)
     sur.set_takeover("window")
@@ -643,7 +651,6 @@ def surrogate_workload(lw, trajectories=2560, windows=80, epochs=100, members=10
                      ref_windows=4, hmin=8000.0, hmax=8000.0)
     sur.close()
     fl = 2 * (5676 * 4096 * 2 + 4096 * 4096 * 2)
-    maps = 8  # the inference average over symmetry maps (the library default)
     return {"config": "4: learned surrogate T42, 6-hour windows (configured training, 20-day rollout)",
             "unit": "member-sim-days/s",
             "network_only": members * 0.25 / (maps * fwd1024 * 1e-3), "network_in_rollout": r["network_rate"],
@@ -660,6 +667,9 @@ def surrogate_workload(lw, trajectories=2560, windows=80, epochs=100, members=10
                                 "speedup_hybrid_vs_rk4": rm["hybrid_rate"] / rm["rk4_rate"],
                                 "rollout_checks_over_threshold": rm["frac_over"]},
             "threshold": 1e-3, "members": members, "rollout_windows": rollout_windows, "kinetic_weight": kinetic_weight,
+            "symmetry_maps_averaged": maps, "weight_averaging": averaging,
+            "drift": {"trajectories": drift_trajectories, "network_windows": drift_windows, "epochs": drift_epochs, "generate_s": gen2_s,
+                      "validation_mean_before": fit0["val_err_mean"], "validation_p90_before": fit0["val_err_p90"]},
             "pairs": trajectories * windows, "epochs": epochs, "generate_s": gen_s, "train_s": fit["seconds"],
             "train_step_ms_batch512": train_ms, "forward_ms_batch1024": fwd1024,
             "forward_tflops_batch1024": fl * 1024 / (fwd1024 * 1e-3) / 1e12, "wall_s": time.perf_counter() - t0}
@@ -876,22 +886,22 @@ def main():
     ap.add_argument("--days", type=float, default=2.0)
     ap.add_argument("--trajectories", type=int, default=2560)
     ap.add_argument("--windows", type=int, default=80)
-    ap.add_argument("--epochs", type=int, default=100)
+    ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--rollout-windows", type=int, default=80)
     ap.add_argument("--rollout-members", type=int, default=1024)
     ap.add_argument("--threshold", type=float, default=1e-3)
     ap.add_argument("--check-precision", default="split3", choices=["fp64", "split3"])
     ap.add_argument("--sweep", default="", help="comma-separated extra take-over thresholds")
     ap.add_argument("--augment", type=int, default=1, help="symmetry augmentation of the training pairs (1/0)")
-    ap.add_argument("--averaging", type=float, default=0.9995, help="weight averaging decay (0: last weights)")
-    ap.add_argument("--sym-average", type=int, default=8, help="symmetry maps averaged at inference (1: plain network)")
+    ap.add_argument("--averaging", type=float, default=0.9998, help="weight averaging decay (0: last weights)")
+    ap.add_argument("--sym-average", type=int, default=16, help="symmetry maps averaged at inference (1: plain network)")
     ap.add_argument("--kinetic-weight", type=float, default=0.25, help="weight of the kinetic-energy part of the loss")
     ap.add_argument("--takeover", default="window,member", help="rollout takeover modes to run (window: RK4 replaces a failed window; "
                     "member: RK4 keeps a failed member)")
     ap.add_argument("--lr-min", type=float, default=3e-5)
-    ap.add_argument("--drift-trajectories", type=int, default=0, help="training trajectories added from network-advanced states")
+    ap.add_argument("--drift-trajectories", type=int, default=768, help="training trajectories added from network-advanced states")
     ap.add_argument("--drift-windows", type=int, default=8, help="network windows before those trajectories start")
-    ap.add_argument("--drift-epochs", type=int, default=50, help="epochs of the continued fit after adding them")
+    ap.add_argument("--drift-epochs", type=int, default=100, help="epochs of the continued fit after adding them")
     ap.add_argument("--data-precision", default="split3", choices=["fp64", "split3"])
     args = ap.parse_args()
     rank, world, local = dist_env()

@@ -1467,19 +1467,26 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
   rs_mode.alloc(members);
   rs_mode.zero(stream);
   LMW_CUDA(cudaMemcpyAsync(rs_state.p, init.device_state(), nst * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-  // the network's members are checked by one batched RK4 engine of exactly their count (rebuilt when
-  // takeovers change the count)
+  // the network's members are checked by one batched RK4 engine built once for all members: after takeovers its
+  // first slots hold the network's members and the remaining slots repeat the first of them (the same RK4 step
+  // for the members that count, no rebuild of the engine and its launch plan)
   std::vector<int> netids(members);
   std::iota(netids.begin(), netids.end(), 0);
   DevBuf<int> netids_d;
+  netids_d.alloc(members);
   std::unique_ptr<SphereEngine> check;
+  std::vector<int> slots(members);
+  auto upload_slots = [&]() {
+    for (int i = 0; i < members; i++) slots[i] = netids[i < static_cast<int>(netids.size()) ? i : 0];
+    LMW_CUDA(cudaMemcpyAsync(netids_d.p, slots.data(), members * sizeof(int), cudaMemcpyHostToDevice, check->stream));
+    LMW_CUDA(cudaStreamSynchronize(check->stream));
+  };
   auto make_check = [&](int k) {
     SphereConfig cc = c;
     cc.members = k;
     cc.precision = check_precision;
     check = std::make_unique<SphereEngine>(cc);
-    netids_d.alloc(k);
-    LMW_CUDA(cudaMemcpyAsync(netids_d.p, netids.data(), k * sizeof(int), cudaMemcpyHostToDevice, check->stream));
+    upload_slots();
   };
   struct Group {
     std::unique_ptr<SphereEngine> e;
@@ -1540,9 +1547,8 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
     if (netids.empty()) continue;
     const auto tc0 = std::chrono::steady_clock::now();
     const int k = static_cast<int>(netids.size());
-    if (check->B != k) make_check(k);
     LMW_CUDA(cudaStreamSynchronize(stream));
-    copy_members_launch(rs_start.p, netids_d.p, check->device_state(), nullptr, k, nfeat, check->stream);
+    copy_members_launch(rs_start.p, netids_d.p, check->device_state(), nullptr, members, nfeat, check->stream);
     check->state_written();
     rk4_window(*check);
     state_errors<<<k, 256, 0, check->stream>>>(rs_state.p, netids_d.p, check->device_state(), nfeat, cw.p, merr.p);
@@ -1600,10 +1606,7 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
       groups.push_back(std::move(g));
       LMW_CUDA(cudaMemcpyAsync(rs_mode.p, mode.data(), members * sizeof(int), cudaMemcpyHostToDevice, stream));
       netids = keep;
-      if (!netids.empty()) {
-        LMW_CUDA(cudaStreamSynchronize(check->stream));
-        make_check(static_cast<int>(netids.size()));
-      }
+      if (!netids.empty()) upload_slots();
     }
     t_check += seconds_since(tc0);
   }
