@@ -636,10 +636,11 @@ __global__ void __launch_bounds__(SPLIT_SYN_WS_THREADS, CTAS) split_syn_ws(SphDe
 // latitudes per store), which the analysis gathers (cheaper for a few members, where jb is small)
 // FMAX: the largest FFT stage group the instantiation takes (4: sixteen elements per thread, two CTAs per SM)
 // LOGN: log2 of the transform length when it is fixed at compile time (the FFT groups then address shared memory
-// with immediates), 0 for any length. Register budget: three CTAs per SM for the three-stage groups and for the
-// four-stage groups of transforms up to 128 points (their rows leave room for a third CTA), else two
+// with immediates), 0 for any length. Register budget: three CTAs per SM (77 registers) for the three-stage groups
+// and for the four-stage groups of transforms up to 256 points, where the rows of a CTA's latitude pairs leave room
+// for a third CTA or the fixed addressing frees the registers; two for the any-length and longer forms
 template <bool DIRECT, int FMAX, int LOGN>
-__global__ void __launch_bounds__(GRID_THREADS, FMAX < 4 || (LOGN > 0 && LOGN <= 7) ? 3 : 2) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
+__global__ void __launch_bounds__(GRID_THREADS, FMAX < 4 || (LOGN > 0 && LOGN <= 8) ? 3 : 2) split_grid(SphDev d, SphTab<float> t, SplitDev sd, const double *__restrict__ fgrid,
                                                            const double *__restrict__ hsgrid) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float2 *sm = reinterpret_cast<float2 *>(smraw);  // rows f * jb + p: U, V, zeta, Phi and the fifth product of pair p
