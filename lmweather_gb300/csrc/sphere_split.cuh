@@ -392,9 +392,19 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
   split_teardown(tmem, ncols);
 }
 
+// The k-th work item of a persistent CTA. Work items are numbered in order of decreasing size (m, the wavenumber,
+// is the slowest index: K and the coefficient count shrink as m grows) and dealt to the CTAs in snake order
+// (round 0 to CTAs 0..G-1, round 1 to G-1..0, ...), so every CTA gets an even share of the work (a plain
+// round-robin over m-fastest items left the busiest CTA with half again the mean). Returns a value >= nitems past
+// the CTA's last item.
+__device__ __forceinline__ int snake_item(int k) {
+  const int g = static_cast<int>(gridDim.x), c = static_cast<int>(blockIdx.x);
+  return k * g + ((k & 1) ? g - 1 - c : c);
+}
+
 // ------------------------------------------------------------------------------------------- synthesis, warp-specialised
 // The same work as split_syn, by persistent CTAs whose warps take roles (as split_ana_ws): thread 0 streams the H
-// and P operand and table chunks of the CTA's items (m, member tile, latitude slice; m the fastest index) through
+// and P operand and table chunks of the CTA's items (m, member tile, latitude slice; dealt by snake_item) through
 // a ring of ns fixed-size stages; thread 32 issues the MMAs of item i into tensor-memory buffer i % 2 (four
 // accumulators H E/O, P E/O of nh columns each) and commits it to accf[i % 2]; warps 2..9 copy a finished buffer
 // to shared memory, release it (acce) and write the item's Fourier records while the next item loads and
@@ -442,8 +452,9 @@ __global__ void __launch_bounds__(SPLIT_SYN_WS_THREADS, CTAS) split_syn_ws(SphDe
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tslot;
   auto item_of = [&](int item, int &m, int &tile, int &jh0) {
-    m = item % d.M;
-    const int rest = item / d.M;
+    const int per_m = sd.ntiles * nsl;
+    m = item / per_m;
+    const int rest = item - m * per_m;
     tile = rest % sd.ntiles;
     jh0 = (rest / sd.ntiles) * nh;
   };
@@ -451,7 +462,7 @@ __global__ void __launch_bounds__(SPLIT_SYN_WS_THREADS, CTAS) split_syn_ws(SphDe
     // producer
     int git = 0;
     bool ok = true;
-    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+    for (int k = 0, item = snake_item(0); item < nitems && ok; item = snake_item(++k)) {
       int m, tile, jh0;
       item_of(item, m, tile, jh0);
       const long kp = sd.kps[m];
@@ -491,7 +502,7 @@ __global__ void __launch_bounds__(SPLIT_SYN_WS_THREADS, CTAS) split_syn_ws(SphDe
     const uint32_t idesc = idesc_m128(nh);
     int git = 0, it = 0;
     bool ok = true;
-    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+    for (int k = 0, item = snake_item(0); item < nitems && ok; item = snake_item(++k)) {
       int m, tile, jh0;
       item_of(item, m, tile, jh0);
       const int nchunk = static_cast<int>(sd.kps[m] / bk), kseg = sd.ke16[m];
@@ -542,7 +553,7 @@ __global__ void __launch_bounds__(SPLIT_SYN_WS_THREADS, CTAS) split_syn_ws(SphDe
     const int et = tid - 64;
     int it = 0;
     const float ia = d.inv_a_f;
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    for (int k = 0, item = snake_item(0); item < nitems; item = snake_item(++k)) {
       int m, tile, jh0;
       item_of(item, m, tile, jh0);
       const int bb = it & 1;
@@ -1156,7 +1167,7 @@ __global__ void __launch_bounds__(SPLIT_ANA_THREADS, MINB) split_ana(SphDev d, S
 // items (m, parity or both, member tile) through a ring of ns fixed-size stages; thread 32 issues the MMAs of item i
 // into tensor-memory accumulator buffer i % 2 and commits it to accf[i % 2]; warps 2..9 (256 threads) wait for it,
 // copy it to shared memory, release the buffer (acce[i % 2]) and run the epilogue (ana_coef, the same arithmetic as
-// split_ana). Items are visited with m the fastest index. Every wait is bounded; after a failure each role stops,
+// split_ana). Items are dealt by snake_item. Every wait is bounded; after a failure each role stops,
 // the CTA drains its own copies and MMAs and frees its tensor memory.
 template <bool BOTH, int CTAS>
 __global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d, SplitDev sd, SphTab<float> t, StageArgs sa, int B, int ns,
@@ -1199,10 +1210,10 @@ __global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d,
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tslot;
-  // the item sequence every role walks: (m, parity or both, tile), m fastest
+  // the item sequence every role walks (snake_item): (m, parity or both, tile), m the slowest index
   auto item_of = [&](int item, int &m, int &s_first, int &s_last, int &tile, int &R0, int &R1) {
-    m = item % d.M;
-    const int rest = item / d.M;
+    m = item / per_m;
+    const int rest = item - m * per_m;
     s_first = BOTH ? 0 : rest % 2;
     tile = BOTH ? rest : rest / 2;
     R0 = (d.N - m) / 2 + 1;
@@ -1213,7 +1224,7 @@ __global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d,
     // producer
     int git = 0;
     bool ok = true;
-    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+    for (int k = 0, item = snake_item(0); item < nitems && ok; item = snake_item(++k)) {
       int m, s_first, s_last, tile, R0, R1;
       item_of(item, m, s_first, s_last, tile, R0, R1);
       if ((s_first ? R1 : R0) == 0) continue;
@@ -1253,7 +1264,7 @@ __global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d,
     const uint32_t sbo = static_cast<uint32_t>(bk) * 16u;
     int git = 0, it = 0;
     bool ok = true;
-    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+    for (int k = 0, item = snake_item(0); item < nitems && ok; item = snake_item(++k)) {
       int m, s_first, s_last, tile, R0, R1;
       item_of(item, m, s_first, s_last, tile, R0, R1);
       if ((s_first ? R1 : R0) == 0) continue;
@@ -1309,7 +1320,7 @@ __global__ void __launch_bounds__(SPLIT_WS_THREADS, CTAS) split_ana_ws(SphDev d,
     // epilogue warps
     const int et = tid - 64;
     int it = 0;
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    for (int k = 0, item = snake_item(0); item < nitems; item = snake_item(++k)) {
       int m, s_first, s_last, tile, R0, R1;
       item_of(item, m, s_first, s_last, tile, R0, R1);
       if ((s_first ? R1 : R0) == 0) continue;
