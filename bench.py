@@ -441,7 +441,7 @@ def run_ours(args, rank, world, local):
                 "next synthesis operands out")
     # DRAM bytes per launch measured by ncu (cold caches) for the T85 x 128 group's kernels, from
     # profiles/split_kernels_t85x128_ensemble.md; the live bench does not run under the profiler
-    ncu_traffic = {(85, 1, 1): 66.2e6, (85, 2, 1): 114.2e6} if args.precision == "split3" else {}
+    ncu_traffic = {(85, 1, 1): 66.2e6, (85, 2, 1): 107.1e6} if args.precision == "split3" else {}
     pk = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
     achieved = moved / (kt[gtop][ktop] * 1e-3) / 1e9
