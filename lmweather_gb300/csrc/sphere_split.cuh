@@ -1559,8 +1559,17 @@ inline void build_split_plan(SplitPlan &sp, const HostTables &h, int B, int term
   LMW_CUDA(cudaMemcpy(sp.lin32.p, lin32.data(), lin32.size() * sizeof(float), cudaMemcpyHostToDevice));
 }
 
+// bytes past the end of a warp-specialised kernel's layout (ns stage slots of `slot` bytes, then `tail` bytes of
+// staging) that an M = 128 MMA reads: it reads 128 rows (16 row groups of bk x 16 bytes) from the A base of the last
+// piece of the last slot, whatever the operand's row count
+inline size_t ws_margin(int ns, size_t slot, size_t last_piece_offset, int bk, size_t tail) {
+  const size_t end = static_cast<size_t>(ns - 1) * slot + last_piece_offset + static_cast<size_t>(128) * bk * 2;
+  const size_t have = static_cast<size_t>(ns) * slot + tail;
+  return end > have ? ((end - have + 15) & ~static_cast<size_t>(15)) : 0;
+}
+
 // shared-memory layout of the warp-specialised analysis for one parity (both = 0) or both per item and ns stages:
-// stage slots of a fixed size, then the accumulator copy, then the margin an M = 128 MMA may read past an A base.
+// stage slots of a fixed size, then the accumulator copy, then what an M = 128 MMA may read past the end (ws_margin).
 // Returns false when the form does not fit (tensor memory: two accumulator buffers per CTA, `ctas` CTAs per SM).
 inline bool ws_layout(const SplitPlan &sp, int both, int ns, int ctas, size_t *smem, int *buf_cols, int *slot) {
   const int ldmax = both ? 2 * sp.ra_pair : 2 * sp.ra_max;
@@ -1568,7 +1577,7 @@ inline bool ws_layout(const SplitPlan &sp, int both, int ns, int ctas, size_t *s
   while (bc < ldmax) bc <<= 1;
   const size_t sl = static_cast<size_t>(sp.pieces) * (sp.rAP + sp.ra_max) * sp.bka * 2;
   const size_t dsm = (static_cast<size_t>(sp.rAP) * (ldmax + 1) * sizeof(float) + 15) & ~static_cast<size_t>(15);
-  const size_t total = ns * sl + dsm + SPLIT_MARGIN;
+  const size_t total = ns * sl + dsm + ws_margin(ns, sl, static_cast<size_t>(sp.pieces - 1) * sp.rAP * sp.bka * 2, sp.bka, dsm);
   *smem = total;
   *buf_cols = bc;
   *slot = static_cast<int>(sl);
@@ -1579,8 +1588,8 @@ inline bool ws_layout(const SplitPlan &sp, int both, int ns, int ctas, size_t *s
 }
 
 // shared-memory layout of the warp-specialised synthesis with `sl` latitude slices and ns stages: stage slots,
-// then the staging of one accumulator buffer (H E/O with rSH rows, P E/O with rSP rows, stride nh + 1), then the
-// margin an M = 128 MMA may read past an A base. Returns false when it does not fit (tensor memory: two buffers of
+// then the staging of one accumulator buffer (H E/O with rSH rows, P E/O with rSP rows, stride nh + 1), then what an
+// M = 128 MMA may read past the end (ws_margin). Returns false when it does not fit (tensor memory: two buffers of
 // four nh-column accumulators per CTA, `ctas` CTAs per SM).
 inline bool syn_ws_layout(const SplitPlan &sp, int sl, int ns, int ctas, size_t *smem, int *buf_cols, int *slot) {
   if (sl < 1 || sp.nh16 % sl != 0) return false;
@@ -1590,7 +1599,7 @@ inline bool syn_ws_layout(const SplitPlan &sp, int sl, int ns, int ctas, size_t 
   while (bc < 4 * nh) bc <<= 1;
   const size_t st = static_cast<size_t>(sp.pieces) * (sp.rSP + nh) * sp.bks * 2;
   const size_t stg = (static_cast<size_t>(2 * sp.rSH + 2 * sp.rSP) * (nh + 1) * sizeof(float) + 15) & ~static_cast<size_t>(15);
-  const size_t total = ns * st + stg + SPLIT_MARGIN;
+  const size_t total = ns * st + stg + ws_margin(ns, st, static_cast<size_t>(sp.pieces - 1) * sp.rSP * sp.bks * 2, sp.bks, stg);
   *smem = total;
   *buf_cols = bc;
   *slot = static_cast<int>(st);
