@@ -1438,9 +1438,9 @@ void Surrogate::advance_states(double *states, int count, const int *mode) {
 // Hybrid rollout. Every window the network advances the members it still owns; every check_every-th window plain
 // RK4 recomputes that window from the same start states, the per-window height error of every network member is
 // recorded, and a member whose error exceeds the threshold is taken over: its state becomes the RK4 state and
-// (takeover_mode 0) RK4 advances it from then on (a takeover group: one more batched engine per check that took
-// members over), or (takeover_mode 1) the network keeps advancing it from the RK4 state (out[4] then counts the
-// member-windows RK4 replaced).
+// (takeover_mode 0) RK4 advances it from then on (one batched FP64 engine for every member taken over so far), or
+// (takeover_mode 1) the network keeps advancing it from the RK4 state (out[4] then counts the member-windows RK4
+// replaced).
 // out[0] hybrid seconds, [1] network seconds, [2] check seconds, [3] takeover seconds, [4] members taken over,
 // [5] checks, [6] median window error, [7] max, [8] fraction of checked windows over the threshold,
 // [9] plain RK4 seconds for ref windows (measured on the same members), [10] ref windows, [11] hybrid
@@ -1491,6 +1491,7 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
   struct Group {
     std::unique_ptr<SphereEngine> e;
     DevBuf<int> ids;
+    std::vector<int> hids;
     int n = 0;
   };
   std::vector<std::unique_ptr<Group>> groups;
@@ -1603,7 +1604,32 @@ void Surrogate::rollout(int members, uint64_t seed0, double hmin, double hmax, i
         t_check += seconds_since(tc0);
         continue;
       }
-      groups.push_back(std::move(g));
+      // one FP64 engine advances every member taken over so far: the new members join the existing group (their
+      // states and the group's copied into an engine of the combined count), so each window is one batched run
+      if (groups.empty()) {
+        g->hids = fresh;
+        groups.push_back(std::move(g));
+      } else {
+        Group &old = *groups[0];
+        auto mg = std::make_unique<Group>();
+        mg->n = old.n + g->n;
+        mg->hids = old.hids;
+        mg->hids.insert(mg->hids.end(), fresh.begin(), fresh.end());
+        mg->ids.alloc(mg->n);
+        SphereConfig mc = cfg;
+        mc.members = mg->n;
+        mc.precision = kFP64;
+        mg->e = std::make_unique<SphereEngine>(mc);
+        LMW_CUDA(cudaMemcpyAsync(mg->ids.p, mg->hids.data(), mg->n * sizeof(int), cudaMemcpyHostToDevice, mg->e->stream));
+        LMW_CUDA(cudaStreamSynchronize(old.e->stream));
+        LMW_CUDA(cudaMemcpyAsync(mg->e->device_state(), old.e->device_state(), static_cast<size_t>(old.n) * nfeat * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, mg->e->stream));
+        LMW_CUDA(cudaMemcpyAsync(mg->e->device_state() + static_cast<size_t>(old.n) * nfeat, g->e->device_state(),
+                                 static_cast<size_t>(g->n) * nfeat * sizeof(double), cudaMemcpyDeviceToDevice, mg->e->stream));
+        LMW_CUDA(cudaStreamSynchronize(mg->e->stream));
+        mg->e->state_written();
+        groups[0] = std::move(mg);
+      }
       LMW_CUDA(cudaMemcpyAsync(rs_mode.p, mode.data(), members * sizeof(int), cudaMemcpyHostToDevice, stream));
       netids = keep;
       if (!netids.empty()) upload_slots();

@@ -232,3 +232,21 @@ def test_drifted_trajectories_keep_the_held_out_set(engine):
     with pytest.raises(ValueError):
         engine.Surrogate(21, hidden=256, seed=6).generate_drifted(8, 1)
     sur.close()
+
+
+def test_member_takeovers_at_several_checks(trained, engine):
+    # members taken over at different checks join one FP64 engine; each member is taken over at its first check
+    # above the threshold (the network members' window errors do not depend on who was taken over before)
+    sur, _ = trained
+    sur.set_takeover("member")
+    kw = dict(seed0=1300, windows=4, check_every=1, ref_windows=1, hmin=7000.0, hmax=7000.0, check_precision=engine.SPLIT_BF16)
+    r1 = sur.rollout(8, threshold=1e9, with_errors=True, **kw)
+    err = r1["window_errors"]
+    assert np.all(err > 0)
+    # a threshold between the members' errors, so that members are taken over at different checks
+    th = float(np.median(err))
+    over = err > th
+    when = [int(np.argmax(over[:, b])) if over[:, b].any() else -1 for b in range(8)]
+    r2 = sur.rollout(8, threshold=th, with_states=True, **kw)
+    assert r2["taken_over"] == sum(w >= 0 for w in when)
+    assert np.all(np.isfinite(r2["final_states"]))
