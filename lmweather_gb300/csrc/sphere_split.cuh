@@ -394,9 +394,9 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 1) split_syn(SphDev d, SplitDev
 
 // The k-th work item of a persistent CTA. Work items are numbered in order of decreasing size (m, the wavenumber,
 // is the slowest index: K and the coefficient count shrink as m grows) and dealt to the CTAs in snake order
-// (round 0 to CTAs 0..G-1, round 1 to G-1..0, ...), so every CTA gets an even share of the work (a plain
-// round-robin over m-fastest items left the busiest CTA with half again the mean). Returns a value >= nitems past
-// the CTA's last item.
+// (pass 0 to CTAs 0..G-1, pass 1 to G-1..0, ...), so every CTA gets an even share of the work (dealing m-fastest
+// items in one direction left the busiest CTA with half again the mean). Returns a value >= nitems past the CTA's
+// last item.
 __device__ __forceinline__ int snake_item(int k) {
   const int g = static_cast<int>(gridDim.x), c = static_cast<int>(blockIdx.x);
   return k * g + ((k & 1) ? g - 1 - c : c);

@@ -186,7 +186,7 @@ def test_rollout_takeover_semantics(trained, engine, check, takeover):
     sur, _ = trained
     # threshold 0 and a check every window: every member is taken over at the first check (member mode), or every
     # window of every member is replaced (window mode), so the hybrid is plain FP64 RK4 (a split-precision check is
-    # only the judge: the window of a member it takes over is recomputed in FP64)
+    # only decides: the window of a member it takes over is recomputed in FP64)
     cp = engine.FP64 if check == "fp64" else engine.SPLIT_BF16
     sur.set_takeover(takeover)
     r0 = sur.rollout(8, seed0=900, windows=3, check_every=1, threshold=0.0, ref_windows=1, hmin=7000.0, hmax=7000.0, with_states=True,
