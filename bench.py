@@ -689,8 +689,9 @@ def weighted_l2(a, b, w):
 
 
 def precision_study(T: int, days: float, seed: int = 1, modes=("fp64", "fp32", "split3", "split6", "split3_plain", "split6_plain")) -> dict:
-    """The same seeded state run in FP64, FP32 and split-BF16 (3 and 6 products per term; the default form keeps the
-    linear terms of the tendencies in FP64, the "_plain" form sends every term through the BF16 products) for `days`;
+    """The same seeded state run in FP64, FP32 and split-BF16 (3 and 6 products per term; the default form adds the
+    linear terms of the tendencies in spectral space, outside the BF16 products; the "_plain" form sends every term
+    through the BF16 products) for `days`;
     errors against the FP64 run (relative L2 of the height, area-weighted with the Gauss weights; L-infinity;
     relative drift of energy and potential enstrophy) and speeds."""
     import lmweather_gb300 as lw

@@ -304,8 +304,8 @@ int lmw_sphere_split_plan(lmw_sphere *s, int *out);
  * hook; no reference counterpart. */
 int lmw_sphere_set_split_plan(lmw_sphere *s, const int *plan);
 /* The split path's treatment of the linear terms of the tendencies (cpp/sphere.cpp:338-390 computes every term
- * on the grid). linear_exact = 1 (the default): the terms that are linear in the state are added in FP64 in
- * spectral space by the analysis epilogue -- n(n+1)/a^2 Phi in d delta, -Phi_mean delta in d Phi (the mean
+ * on the grid). linear_exact = 1 (the default): the terms that are linear in the state are added exactly in
+ * spectral space by the analysis epilogue (in FP32, from the stage input rounded to FP32) -- n(n+1)/a^2 Phi in d delta, -Phi_mean delta in d Phi (the mean
  * height's gravity-wave term; D(U, V) = delta holds exactly for n <= T) and, for an untilted axis, the Coriolis
  * terms -D(fU, fV) and D(fV, -fU) with f = 2 Omega mu, which couple n - 1, n and n + 1 -- and only the nonlinear
  * products (U zeta, V zeta, U Phi', V Phi', E) go through the BF16 pieces. linear_exact = 0: every term through the

@@ -402,8 +402,9 @@ class Sphere:
         _check(self._lib.lmw_sphere_set_split_plan(self._h, arr.ctypes.data_as(_IP)))
 
     def set_split_form(self, linear_exact: bool) -> None:
-        """Split path: True (the default) adds the linear terms of the tendencies in FP64 spectral space and sends only
-        the nonlinear products through the BF16 pieces; False sends every term through the BF16 GEMMs."""
+        """Split path: True (the default) adds the linear terms of the tendencies in spectral space (FP32, outside the
+        BF16 pieces) and sends only the nonlinear products through the BF16 pieces; False sends every term through
+        the BF16 GEMMs."""
         _check(self._lib.lmw_sphere_set_split_form(self._h, 1 if linear_exact else 0))
 
     def get_state(self, member: int = 0):

@@ -187,7 +187,7 @@ class SphereEngine {
   // replaces the autotuned plan (same 7 entries as split_plan); checked against the shared-memory and
   // tensor-memory limits the autotuner's candidates obey
   void set_split_plan(const int *in);
-  // 1 (default): the linear terms of the tendencies in FP64 spectral space, the nonlinear products through the BF16
+  // 1 (default): the linear terms of the tendencies in spectral space (FP32), the nonlinear products through the BF16
   // pieces; 0: every term through the BF16 GEMMs
   void set_split_form(int linear_exact);
   // writes `code` into the split path's error word, as a tensor-core wait that ran out does (failure tests)

@@ -74,7 +74,8 @@ struct SplitPlan {
   int nsm = 152;              // multiprocessors of the device (the persistent grid)
   int ra_pair = 32;           // largest ra16[2m] + ra16[2m + 1]
   // 1: the linear terms of the tendencies (gravity-wave terms of the mean height, the Laplacian of Phi, the
-  // untilted Coriolis terms) in FP64 spectral space; only the nonlinear products go through the BF16 pieces.
+  // untilted Coriolis terms) added in spectral space, in FP32 from the FP32 stage input; only the nonlinear
+  // products go through the BF16 pieces.
   // 0: every term through the BF16 GEMMs (the plain split form)
   int lin_exact = 1;
   DevBuf<float> lin32;        // per coefficient q: eps_{n+1} n/(n+1), eps_n (n+1)/n, m/(n(n+1)) (3 x ntri), FP32
@@ -706,7 +707,7 @@ __global__ void __launch_bounds__(GRID_THREADS, FMAX < 4 || (LOGN > 0 && LOGN <=
     // the FP64 Coriolis and orography rows (tilted or mountain members only) are rounded to FP32 on the integer
     // pipe: the same values as the hardware conversion, without the narrow FP64 pipe
     // linear-exact form: the untilted Coriolis parameter and Phi leave eta and Phi + E (their terms are added in
-    // FP64 spectral space by the analysis), and P is Phi' (the synthesis left out Phi_00)
+    // spectral space by the analysis), and P is Phi' (the synthesis left out Phi_00)
     const bool lx = sd.lin_exact != 0;
     {
       const float eta = Z.x + ((gf & 1) ? d2f_int(fr_s[k]) : (lx ? 0.0f : cor[2 * pr]));
