@@ -73,3 +73,21 @@ def test_single_config_cpu_timing(config):
     r = bench.cpu_single_rate(config, budget_s=0.05)
     assert r["cores"] == 1 and r["kind"] == "port" and r["unit"] == "sim-days/s"
     assert r["value"] > 0 and "RK4 steps" in r["sample"]
+
+
+def test_reference_arm_line_keeps_the_contract():
+    """`bench.py --impl reference` times the oracle port on the host's cores and prints one JSON line with the
+    benchmark's keys: the metric and unit of the GPU arm, a timed cpu_baseline and an e2e figure without copies."""
+    import json
+    import subprocess
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
+                          "--ref-seconds", "0.5"], capture_output=True, text=True, timeout=600, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][-1])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling", "dtype", "config"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["sample"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
