@@ -484,8 +484,10 @@ def run_ours(args, rank, world, local):
     # end before the next starts) against the same 1024 members run together, the groups' kernels interleaving
     # on their own streams: what the concurrent form gains over back-to-back launches of each group. Wall time
     # around each synchronised 2-day run, the faster of two, the same way for both forms.
+    # (N = 1 only, like the other configurations below: at N > 1 the other ranks would hold their GPUs idle while
+    # rank 0 runs them, and the N = 1 line reports them)
     ragged = None
-    if rank == 0:
+    if rank == 0 and world == 1:
         def wall_run(e, z):
             best = 1e30
             for _ in range(2):
@@ -513,9 +515,9 @@ def run_ours(args, rank, world, local):
                           "launches interleaved on three streams) against each group alone, one after another (wall time, "
                           "synchronised, L2 not flushed)"}
 
-    # --- the other configurations (rank 0)
+    # --- the other configurations (rank 0, N = 1)
     workloads = []
-    if rank == 0:
+    if rank == 0 and world == 1:
         workloads = other_workloads(lw, lib, args, ens)
 
     # --- CPU baseline (rank 0, N = 1): the oracle on every host core, a timed pass of whole member-steps
